@@ -1,0 +1,244 @@
+/*
+ * hande_gpu.h -- C ABI of the GB300 FCIQMC walker-propagation engine.
+ *
+ * The engine replaces the body of one FCIQMC Monte Carlo cycle of HANDE
+ * (src/fciqmc.f90:307-399: init_mc_cycle, the loop over occupied
+ * determinants with spawning and death, direct_annihilation, end_mc_cycle) and
+ * the estimator/shift part of end_report_loop (src/qmc_common.F90:1082-1166 ->
+ * src/energy_evaluation.F90:126-711) with kernels that run on one GPU, on
+ * walker lists that stay resident in device memory between calls.
+ *
+ * Every entry point is extern "C", takes plain C scalars, pointers and POD
+ * structs and returns an int status (HGPU_OK == 0), so the header can be bound
+ * from Fortran with ISO_C_BINDING (bind(c) interfaces) as well as from C, C++
+ * and Python ctypes.  No entry point aborts, traps or throws across the ABI.
+ *
+ * Conventions shared with HANDE's data model (src/qmc_data.f90:615-682,
+ * lib/local/const.F90:25-56 with DET_SIZE=64, POP_SIZE=64):
+ *   - a determinant is nwords = ceil(nbasis/64) int64 words; spin orbital p
+ *     (0-based; HANDE orbital p+1) is bit p%64 of word p/64; even p are alpha
+ *     (Ms=+1), odd p beta (src/basis_types.f90:134-170);
+ *   - determinants are ordered by unsigned comparison with the LAST word most
+ *     significant, ascending (src/bit_utils.F90:452-478, src/search.f90:47);
+ *   - populations are int64 fixed point with pop_real_factor = 2^31 for real
+ *     amplitudes and 1 otherwise (src/particle_t_utils.f90:53-82);
+ *   - dat(1) of a walker is K_ii = <D_i|H|D_i> - E_HF (src/annihilation.f90:855).
+ * Arrays passed across the ABI use HANDE's column-major layout: states(nwords, n)
+ * i.e. the words of one determinant are contiguous, pops(nspaces, n).
+ */
+#ifndef HANDE_GPU_H
+#define HANDE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HGPU_MAX_WORDS 2   /* up to 128 spin orbitals */
+#define HGPU_MAX_SPACES 2  /* nspaces: 1, or 2 with replica_tricks */
+
+/* Status codes. */
+enum {
+    HGPU_OK = 0,
+    HGPU_ERR_INVALID = 1,         /* invalid argument or configuration */
+    HGPU_ERR_OOM = 2,             /* device allocation failed */
+    HGPU_ERR_SPAWN_OVERFLOW = 3,  /* spawned list full (spawn%error, src/spawning.F90:938) */
+    HGPU_ERR_MAIN_OVERFLOW = 4,   /* main list full (psip_list%error, src/annihilation.f90:750) */
+    HGPU_ERR_TIMEOUT = 5,         /* a bounded device wait gave up */
+    HGPU_ERR_CUDA = 6,            /* CUDA runtime error */
+    HGPU_ERR_NO_DEVICE = 7,       /* no usable CUDA device */
+    HGPU_ERR_UNSUPPORTED = 8      /* option outside what this build implements */
+};
+
+/* Error flags reported per report (bit mask). */
+#define HGPU_FLAG_SPAWN_OVERFLOW 1
+#define HGPU_FLAG_MAIN_OVERFLOW 2
+
+/* System kinds (sys%system in src/system.f90). */
+enum { HGPU_SYS_HUB_K = 1, HGPU_SYS_READ_IN = 2 };
+
+/* Excitation generators: same numbering as the excit_gen enum of
+ * src/qmc_data.f90:31-45. */
+enum {
+    HGPU_EXCIT_GEN_RENORM = 0,
+    HGPU_EXCIT_GEN_RENORM_SPIN = 1,
+    HGPU_EXCIT_GEN_NO_RENORM = 2,
+    HGPU_EXCIT_GEN_NO_RENORM_SPIN = 3,
+    HGPU_EXCIT_GEN_HEAT_BATH = 10,
+    HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM = 11,
+    HGPU_EXCIT_GEN_HEAT_BATH_SINGLE = 12
+};
+
+/* Arithmetic of the spawning step. */
+enum {
+    HGPU_PREC_FP64 = 0,   /* everything in FP64 (the reference's real(p) = real64) */
+    HGPU_PREC_MIXED = 1   /* FP32 off-diagonal H_ij and p_gen; FP64 K_ii, shift, estimators */
+};
+
+/* The system, as HANDE holds it after init_system / read_in_integrals.  All
+ * pointers are read during hgpu_create only (copied to device memory). */
+typedef struct hgpu_system {
+    int32_t kind;              /* HGPU_SYS_* */
+    int32_t nbasis;            /* number of spin orbitals (sys%basis%nbasis) */
+    int32_t nel, nalpha, nbeta;
+    int32_t nwords;            /* ceil(nbasis/64) (sys%basis%tot_string_len) */
+    const int32_t *orb_sym;    /* [nbasis] basis_fns(p+1)%sym: k-point index (hub_k) or irrep */
+    const int32_t *orb_ms;     /* [nbasis] basis_fns(p+1)%ms: +1 or -1 */
+    const double *sp_eigv;     /* [nbasis] single-particle eigenvalues */
+    /* Hubbard model in momentum space (src/momentum_symmetry.f90:17-80). */
+    int32_t nkpoints;          /* sys%nsym = nbasis/2 */
+    const int32_t *sym_table;  /* [nkpoints*nkpoints] k_i+k_j, 0-based, row-major */
+    const int32_t *inv_sym;    /* [nkpoints] -k_i, 0-based */
+    double coulomb_k;          /* U/nsites (src/system.f90:578) */
+    /* Molecular systems read from an FCIDUMP (src/read_in.F90, RHF, no Lz). */
+    int32_t norb;              /* spatial orbitals M */
+    int32_t nsym_pg;           /* number of irreps (power of two); cross product = XOR */
+    const double *h1;          /* [norb*norb] one-body integrals, row-major, symmetric */
+    const double *v2;          /* packed (ia|jb), index tri(tri(i,a),tri(j,b)); npair=M(M+1)/2 */
+    int64_t nv2;               /* npair*(npair+1)/2 */
+    double ecore;
+    const int32_t *nbasis_sym_spin;    /* [2*nsym_pg] index ims*nsym_pg+sym; ims 0=beta 1=alpha */
+    int32_t max_sym_spin;              /* max of nbasis_sym_spin */
+    const int32_t *sym_spin_basis_fns; /* [nsym_pg*2*max_sym_spin] index (sym*2+ims)*max+k */
+} hgpu_system;
+
+/* Calculation options: the scalar fields of qmc_in_t / fciqmc_in_t
+ * (src/qmc_data.f90:121-260) that the FCIQMC cycle uses. */
+typedef struct hgpu_config {
+    double tau;
+    double shift_damping;          /* qs%shift_damping, default 0.05 */
+    double initial_shift;
+    double vary_shift_from;
+    double target_particles;
+    double initiator_pop;          /* initiator_threshold, default 3 */
+    double spawn_cutoff;           /* in walker units (0.01 default) */
+    double pattempt_single;        /* < 0: HANDE's default for the system */
+    double pattempt_double;
+    double D0_population;          /* init_pop */
+    int32_t vary_shift_from_proje;
+    int32_t excit_gen;             /* HGPU_EXCIT_GEN_* */
+    int32_t real_amplitudes;
+    int32_t initiator_approx;
+    int32_t nspaces;               /* 1, or 2 for replica_tricks */
+    int32_t ncycles;               /* mc_cycles per report */
+    int32_t precision;             /* HGPU_PREC_* */
+    int32_t reserved0;
+    int64_t seed;                  /* rng_seed */
+    int64_t walker_length;         /* main-list capacity; < 0 means MB (state_size) */
+    int64_t spawned_walker_length; /* spawned-list capacity; < 0 means MB */
+    uint64_t ref_det[HGPU_MAX_WORDS]; /* reference determinant f0 */
+} hgpu_config;
+
+/* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */
+typedef struct hgpu_report {
+    int64_t iteration;                       /* cycles completed so far */
+    double shift[HGPU_MAX_SPACES];
+    double proj_energy[HGPU_MAX_SPACES];     /* \sum H_0j N_j, averaged over the report */
+    double D0_population[HGPU_MAX_SPACES];   /* N_0, averaged over the report */
+    double nparticles[HGPU_MAX_SPACES];      /* # H psips at the end of the report */
+    int32_t vary_shift[HGPU_MAX_SPACES];
+    int64_t nstates;                         /* # states */
+    int64_t nspawn_events;                   /* # spawn_events (last cycle) */
+    double rspawn;                           /* R_spawn, averaged over cycles */
+    int64_t nattempts;                       /* spawn attempts in the report (decide_nattempts sums) */
+    int64_t nspawned;                        /* spawned entries in the report */
+    int32_t error_flags;                     /* HGPU_FLAG_* */
+    int32_t reserved0;
+    double device_ms;                        /* device time of the report's cycles */
+} hgpu_report;
+
+typedef struct hgpu_handle hgpu_handle;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int32_t hgpu_version(void);
+
+/* Human-readable text for a status code. */
+const char *hgpu_error_string(int32_t status);
+
+/* Number of CUDA devices visible; 0 when no driver/device is present. */
+int32_t hgpu_device_count(void);
+
+/* Create an engine on the current CUDA device: copies the system to device
+ * memory and allocates the main list, spawned list and scratch sized from
+ * walker_length / spawned_walker_length.  Replaces init_qmc's allocation part
+ * (src/qmc.F90:10-215, init_spawn_store :1418). */
+int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle **out);
+
+int32_t hgpu_destroy(hgpu_handle *h);
+
+/* Put D0_population walkers on the reference determinant: initial_distribution
+ * (src/qmc.F90:1507-1560); also sets the shift to initial_shift. */
+int32_t hgpu_initial_distribution(hgpu_handle *h);
+
+/* Replace the walker list.  states is (nwords, n) column-major, pops is
+ * (nspaces, n) in encoded fixed point; dat may be NULL (K_ii is then
+ * evaluated by slater_condon0).  The list must be sorted and unique. */
+int32_t hgpu_upload_walkers(hgpu_handle *h, const int64_t *states, const int64_t *pops,
+                            const double *dat, int64_t n);
+
+/* Copy the walker list to the host.  *n_out receives the number of states;
+ * nothing is written when capacity < *n_out (status HGPU_ERR_INVALID). */
+int32_t hgpu_download_walkers(hgpu_handle *h, int64_t *states, int64_t *pops, double *dat,
+                              int64_t capacity, int64_t *n_out);
+
+/* Run ncycles Monte Carlo cycles (src/fciqmc.f90:293-413) on the device;
+ * estimators accumulate until hgpu_end_report. */
+int32_t hgpu_run_cycles(hgpu_handle *h, int32_t ncycles);
+
+/* Close a report loop: average the estimators over the cycles run since the
+ * last call, update the shift and vary_shift (communicated_energy_estimators,
+ * src/energy_evaluation.F90:425-657; update_shift :659-711). */
+int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out);
+
+/* Run one whole report (ncycles from the config, then hgpu_end_report). */
+int32_t hgpu_run_report(hgpu_handle *h, hgpu_report *out);
+
+/* Scalars of the qmc_state that a checkpoint needs. */
+typedef struct hgpu_state {
+    int64_t iteration;
+    double shift[HGPU_MAX_SPACES];
+    int32_t vary_shift[HGPU_MAX_SPACES];
+    double nparticles_old[HGPU_MAX_SPACES];  /* N_w at the end of the last report */
+    double tau;
+    int64_t seed;
+} hgpu_state;
+
+int32_t hgpu_get_state(hgpu_handle *h, hgpu_state *out);
+int32_t hgpu_set_state(hgpu_handle *h, const hgpu_state *in);
+
+/* Write / read a binary checkpoint of the walker list and hgpu_state (the
+ * logical fields of HANDE's restart file, src/restart_hdf5.F90:40-100, with
+ * the counter-based RNG's (seed, iteration) in place of the dSFMT state). */
+int32_t hgpu_checkpoint(hgpu_handle *h, const char *path);
+int32_t hgpu_restore(hgpu_handle *h, const char *path);
+
+/* ---- Parity entry points (fixed inputs, results returned to the host) ---- */
+
+/* For n parent determinants (nwords each), draw one excitation with the
+ * generator of the configuration, using RNG stream (iteration, parent index
+ * i, attempt, space 0): gen_excit_ptr%full / %init+%finalise
+ * (src/proc_pointers.f90:279-309).  Outputs per parent: from/to spin
+ * orbitals (4 x int32, -1 when unused), p_gen, H_ij (signed), allowed flag,
+ * and the encoded spawned population of the attempt (attempt_to_spawn,
+ * src/spawning.F90:711) given parent_pops[i]. */
+int32_t hgpu_eval_excitations(hgpu_handle *h, const int64_t *parents, const int64_t *parent_pops,
+                              int64_t n, int64_t iteration, int32_t *orbs, double *pgen,
+                              double *hmatel, int32_t *allowed, int64_t *nspawn);
+
+/* Annihilate a fixed spawned list into the resident main list exactly as
+ * direct_annihilation does (src/annihilation.f90:9-214): sort, self-annihilate
+ * (src/spawn_data.F90:859/:937), annihilate_main_list[_initiator] (:294/:372),
+ * remove_unoccupied_dets (:537), round_low_population_spawns (:600) and
+ * insert_new_walkers (:677).  sdata is (nwords + nspaces + 1, n) column-major
+ * (det words, pops, flag).  iteration keys the stochastic rounding. */
+int32_t hgpu_annihilate_fixed(hgpu_handle *h, const int64_t *sdata, int64_t n, int64_t iteration);
+
+/* K_ii = slater_condon0(D_i) - H00 for n determinants (sc0_ptr). */
+int32_t hgpu_eval_diagonal(hgpu_handle *h, const int64_t *dets, int64_t n, double *kii);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HANDE_GPU_H */

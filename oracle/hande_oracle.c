@@ -1,0 +1,1528 @@
+/*
+ * hande_oracle.c -- CPU restatement of HANDE's FCIQMC cycle (TEST INFRASTRUCTURE).
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+ * this file, as the checker.  It restates the reference algorithm function by
+ * function; each function names the reference file:line it follows.  The
+ * arithmetic follows the reference's operation order so that the values it
+ * produces are the ones the reference formulae give in IEEE double precision
+ * (build with -ffp-contract=off).
+ *
+ * Orbitals are 0-based (HANDE orbital k is p = k-1); the parity of every
+ * difference and the outcome of every comparison is unchanged by the shift.
+ */
+#include "hande_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXW HGPU_MAX_WORDS
+#define MAXB (64 * MAXW)
+#define MAXEL 64
+#define DEPSILON 1.0e-12 /* lib/local/const.F90:90 */
+
+/* ------------------------------------------------------------------------- */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the stream layout.   */
+/* ------------------------------------------------------------------------- */
+
+enum { P_NATTEMPT = 1, P_SPAWN = 2, P_DEATH = 3, P_ROUND_MAIN = 4, P_ROUND_SPAWN = 5 };
+
+static void philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+    uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int r = 0; r < 10; r++) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n1 = lo1;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        uint32_t n3 = lo0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* A stream of uniform doubles in [0,1): counter = (idx, sub, iteration,
+ * purpose<<28 | space<<26 | block), key = (seed lo, seed hi); each block gives
+ * two doubles (53 bits each). */
+typedef struct {
+    uint32_t key[2];
+    uint32_t ctr[4];
+    uint32_t block;
+    double buf[2];
+    int have;
+} rstream;
+
+static void rs_init(rstream *s, uint64_t seed, int purpose, int space, uint64_t idx, uint64_t sub,
+                    uint64_t iter) {
+    s->key[0] = (uint32_t)seed;
+    s->key[1] = (uint32_t)(seed >> 32);
+    s->ctr[0] = (uint32_t)idx;
+    s->ctr[1] = (uint32_t)sub;
+    s->ctr[2] = (uint32_t)iter;
+    s->ctr[3] = ((uint32_t)purpose << 28) | ((uint32_t)space << 26);
+    s->block = 0;
+    s->have = 0;
+}
+
+static double u53(uint32_t hi, uint32_t lo) {
+    uint64_t x = ((uint64_t)hi << 32) | lo;
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* get_rand_close_open (lib/dSFMT_F03_interface/dSFMT_interface.F90:387). */
+static double rs_next(rstream *s) {
+    if (s->have == 0) {
+        uint32_t c[4] = {s->ctr[0], s->ctr[1], s->ctr[2], s->ctr[3] | s->block};
+        uint32_t o[4];
+        philox4x32_10(c, s->key, o);
+        s->block++;
+        s->buf[0] = u53(o[0], o[1]);
+        s->buf[1] = u53(o[2], o[3]);
+        s->have = 2;
+    }
+    double r = s->buf[2 - s->have];
+    s->have--;
+    return r;
+}
+
+double oracle_uniform(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, int which) {
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t c[4] = {c0, c1, c2, c3}, o[4];
+    philox4x32_10(c, key, o);
+    return which ? u53(o[2], o[3]) : u53(o[0], o[1]);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Context                                                                    */
+/* ------------------------------------------------------------------------- */
+
+struct oracle_ctx {
+    hgpu_config cfg;
+    int kind, nbasis, nel, nalpha, nbeta, nw, nvirt_alpha, nvirt_beta, nvirt;
+    int32_t *orb_sym, *orb_ms;
+    double *sp_eigv;
+    int nk;
+    int32_t *sym_table, *inv_sym;
+    double coulomb_k;
+    int norb, nsym;
+    double *h1, *v2;
+    int64_t nv2;
+    double ecore;
+    int32_t *nbss, *ssbf;
+    int maxss;
+    uint64_t mask[MAXB][MAXW]; /* excit_mask (src/excitations.F90:25-70) */
+    int64_t real_factor, cutoff;
+    double pattempt_single, pattempt_double;
+    int R;
+    uint64_t f0[MAXW];
+    double H00;
+    /* main list */
+    int64_t n, cap;
+    uint64_t *dets;
+    int64_t *pops;
+    double *kii;
+    /* qmc state */
+    double shift[2];
+    int vary_shift[2];
+    double nparticles_old[2];
+    int64_t iter;
+    /* report accumulators */
+    double acc_proj[2], acc_d0[2], acc_rspawn;
+    int64_t last_nspawn_events, rep_attempts, rep_spawned, total_attempts;
+    int rep_cycles;
+    int error_flags;
+    /* spawned list: W det words, R pops, flag, generation order */
+    int64_t sn, scap;
+    uint64_t *sdets;
+    int64_t *spops, *sflag, *sord, *suid;
+};
+
+/* determinant helpers ------------------------------------------------------ */
+
+static inline int tbit(const uint64_t *f, int p) { return (int)((f[p >> 6] >> (p & 63)) & 1u); }
+static inline void sbit(uint64_t *f, int p) { f[p >> 6] |= (uint64_t)1 << (p & 63); }
+static inline void cbit(uint64_t *f, int p) { f[p >> 6] &= ~((uint64_t)1 << (p & 63)); }
+
+static int popc64(uint64_t x) {
+    int n = 0;
+    while (x) { x &= x - 1; n++; }
+    return n;
+}
+
+/* bit_str_cmp (src/bit_utils.F90:452-478): 1 if a<b, -1 if a>b, 0 if equal;
+ * last word most significant, unsigned. */
+static int det_cmp(const uint64_t *a, const uint64_t *b, int nw) {
+    for (int i = nw - 1; i >= 0; i--) {
+        if (a[i] < b[i]) return 1;
+        if (a[i] > b[i]) return -1;
+    }
+    return 0;
+}
+
+/* decode_det (src/determinants.f90:243): ascending occupied spin orbitals. */
+static int decode(const oracle_ctx *c, const uint64_t *f, int *occ) {
+    int n = 0;
+    for (int p = 0; p < c->nbasis; p++)
+        if (tbit(f, p)) occ[n++] = p;
+    return n;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Excitations (src/excitations.F90)                                          */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    int nexcit;
+    int from[2], to[2];
+    int perm;
+} excit_t;
+
+/* get_excitation (src/excitations.F90:75-200).  The reference skips the
+ * electron count of identical words when iexcit1-iexcit2 is even; that skip
+ * changes perm by an even number, so counting every word gives the same parity. */
+static excit_t get_excitation(const oracle_ctx *c, const uint64_t *f1, const uint64_t *f2) {
+    excit_t e = {0, {-1, -1}, {-1, -1}, 0};
+    int diff = 0;
+    for (int w = 0; w < c->nw; w++) diff += popc64(f1[w] ^ f2[w]);
+    if (diff == 0) return e;
+    e.nexcit = diff / 2;
+    if (e.nexcit > 2) return e;
+    int shift = c->nel - e.nexcit;
+    int iexcit1 = 0, iexcit2 = 0, iel1 = 0, iel2 = 0, perm = 0;
+    for (int p = 0; p < c->nbasis; p++) {
+        int t1 = tbit(f1, p), t2 = tbit(f2, p);
+        if (t2) iel2++;
+        if (t1) {
+            iel1++;
+            if (!t2) {
+                iexcit1++;
+                e.from[iexcit1 - 1] = p;
+                perm += shift - iel1 + iexcit1;
+            }
+        } else if (t2) {
+            iexcit2++;
+            e.to[iexcit2 - 1] = p;
+            perm += shift - iel2 + iexcit2;
+        }
+    }
+    e.perm = (((perm % 2) + 2) % 2) == 1;
+    return e;
+}
+
+/* find_excitation_permutation1 (src/excitations.F90:247-280). */
+static int perm1(const oracle_ctx *c, const uint64_t *f, int i, int a) {
+    int perm = 0;
+    for (int w = 0; w < c->nw; w++) perm += popc64(f[w] & (c->mask[i][w] ^ c->mask[a][w]));
+    if (i > a) perm -= 1;
+    return (((perm % 2) + 2) % 2) == 1;
+}
+
+/* find_excitation_permutation2 (src/excitations.F90:282-330). */
+static int perm2(const oracle_ctx *c, const uint64_t *f, int i, int j, int a, int b) {
+    int perm = 0;
+    for (int w = 0; w < c->nw; w++) {
+        uint64_t ia = c->mask[i][w] ^ c->mask[a][w];
+        uint64_t jb = c->mask[j][w] ^ c->mask[b][w];
+        perm += popc64((f[w] & ia) ^ (f[w] & jb));
+    }
+    if (i > a) perm += 1;
+    if (i > b) perm += 1;
+    if (j > b || j < a) perm += 1;
+    return (perm % 2) == 1;
+}
+
+/* create_excited_det (src/excitations.F90:365-406). */
+static void excited_det(const oracle_ctx *c, const uint64_t *f, const excit_t *e, uint64_t *out) {
+    for (int w = 0; w < c->nw; w++) out[w] = f[w];
+    for (int k = 0; k < e->nexcit; k++) {
+        cbit(out, e->from[k]);
+        sbit(out, e->to[k]);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Hubbard model in momentum space                                            */
+/* ------------------------------------------------------------------------- */
+
+static inline int kidx(int p) { return p >> 1; }
+
+/* momentum_conserved (src/hubbard_k.f90:57-84). */
+static int momentum_conserved(const oracle_ctx *c, int i, int j, int k, int l) {
+    int dk = c->sym_table[kidx(i) * c->nk + kidx(j)];
+    dk = c->sym_table[dk * c->nk + c->inv_sym[kidx(k)]];
+    return dk == kidx(l);
+}
+
+/* get_two_e_int_hub_k (src/hubbard_k.f90:11-55). */
+static double two_e_int_hub_k(const oracle_ctx *c, int p1, int p2, int p3, int p4) {
+    int s12 = c->orb_ms[p1] == c->orb_ms[p2];
+    int s34 = c->orb_ms[p3] == c->orb_ms[p4];
+    if (!s12 && (s12 == s34) && momentum_conserved(c, p1, p2, p3, p4)) {
+        if (c->orb_ms[p1] == c->orb_ms[p3]) return c->coulomb_k;
+        return -c->coulomb_k;
+    }
+    return 0.0;
+}
+
+/* slater_condon0_hub_k (src/hamiltonian_hub_k.f90:91-132). */
+static double sc0_hub_k(const oracle_ctx *c, const uint64_t *f) {
+    int occ[MAXB];
+    int n = decode(c, f, occ);
+    double h = (double)(c->nalpha * c->nbeta) * c->coulomb_k;
+    for (int i = 0; i < n; i++) h = h + c->sp_eigv[occ[i]];
+    return h;
+}
+
+/* slater_condon2_hub_k_excit (src/hamiltonian_hub_k.f90:163-234). */
+static double sc2_hub_k_excit(const oracle_ctx *c, const uint64_t *f, excit_t *e) {
+    int t;
+    if (e->from[0] > e->from[1]) { t = e->from[0]; e->from[0] = e->from[1]; e->from[1] = t; }
+    if (e->to[0] > e->to[1]) { t = e->to[0]; e->to[0] = e->to[1]; e->to[1] = t; }
+    double h = c->coulomb_k;
+    e->perm = perm2(c, f, e->from[0], e->from[1], e->to[0], e->to[1]);
+    if (e->perm) h = -h;
+    if (((e->from[0] - e->to[0]) % 2) != 0) h = -h;
+    return h;
+}
+
+typedef struct {
+    int occ[MAXEL], occ_a[MAXEL], occ_b[MAXEL], unocc_a[MAXB];
+    int nocc, na, nb, nua;
+    int symunocc[2 * 64]; /* [ims*nsym + sym] */
+} det_info;
+
+/* decode_det_spinocc_spinunocc (src/determinant_decoders.f90:261-370). */
+static void decode_hub_k(const oracle_ctx *c, const uint64_t *f, det_info *d) {
+    d->nocc = d->na = d->nb = d->nua = 0;
+    for (int p = 0; p < c->nbasis; p++) {
+        if (tbit(f, p)) {
+            d->occ[d->nocc++] = p;
+            if ((p & 1) == 0) d->occ_a[d->na++] = p; else d->occ_b[d->nb++] = p;
+        } else if ((p & 1) == 0) {
+            d->unocc_a[d->nua++] = p;
+        }
+    }
+}
+
+/* choose_ij_hub_k (src/excit_gen_hub_k.f90:469-532). */
+static void choose_ij_hub_k(const oracle_ctx *c, rstream *rs, const det_info *d, int *i, int *j, int *ij_sym) {
+    double r = rs_next(rs);
+    int ind = (int)(r * (double)c->nalpha * (double)c->nbeta) + 1;
+    int ii = (int)(((double)ind - 1.0) / (double)c->nbeta) + 1;
+    int jj = ind - (ii - 1) * c->nbeta;
+    *i = d->occ_a[ii - 1];
+    *j = d->occ_b[jj - 1];
+    *ij_sym = c->sym_table[kidx(*i) * c->nk + kidx(*j)];
+}
+
+/* beta partner b of alpha orbital a for total momentum ij_sym (find_ab_hub_k). */
+static inline int hub_k_partner(const oracle_ctx *c, int ij_sym, int a) {
+    return 2 * c->sym_table[ij_sym * c->nk + c->inv_sym[kidx(a)]] + 1;
+}
+
+/* calc_pgen_hub_k (src/excit_gen_hub_k.f90:651-770). */
+static double calc_pgen_hub_k(const oracle_ctx *c, int ab_sym, const uint64_t *f, const det_info *d) {
+    int forbidden = 0;
+    for (int k = 0; k < c->nvirt_alpha; k++) {
+        int b = hub_k_partner(c, ab_sym, d->unocc_a[k]);
+        if (tbit(f, b)) forbidden++;
+    }
+    return 1.0 / (double)(c->nalpha * c->nbeta * (c->nvirt_alpha - forbidden));
+}
+
+/* find_ab_hub_k (src/excit_gen_hub_k.f90:579-649). */
+static int find_ab_hub_k(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int ij_sym,
+                         int *a, int *b) {
+    int r = (int)(rs_next(rs) * (double)c->nvirt_alpha) + 1;
+    *a = d->unocc_a[r - 1];
+    *b = hub_k_partner(c, ij_sym, *a);
+    return !tbit(f, *b);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Molecular systems                                                          */
+/* ------------------------------------------------------------------------- */
+
+static inline int64_t tri0(int64_t i, int64_t j) { return i * (i + 1) / 2 + j; }
+
+/* two_body_int_indx (src/molecular_integrals.F90:736-845), RHF. */
+static inline double v2_get(const oracle_ctx *c, int i, int j, int a, int b) {
+    int si = i >> 1, sj = j >> 1, sa = a >> 1, sb = b >> 1;
+    int64_t ia = si >= sa ? tri0(si, sa) : tri0(sa, si);
+    int64_t jb = sj >= sb ? tri0(sj, sb) : tri0(sb, sj);
+    int64_t idx = ia >= jb ? tri0(ia, jb) : tri0(jb, ia);
+    return c->v2[idx];
+}
+
+/* get_one_body_int_mol_nonzero (src/molecular_integrals.F90:685-734). */
+static inline double h1_get(const oracle_ctx *c, int i, int j) { return c->h1[(i >> 1) * c->norb + (j >> 1)]; }
+
+static inline int ims_of(const oracle_ctx *c, int p) { return (c->orb_ms[p] + 1) / 2; } /* 0 beta, 1 alpha */
+
+/* slater_condon0_mol (src/hamiltonian_molecular.f90:73-139). */
+static double sc0_mol(const oracle_ctx *c, const uint64_t *f) {
+    int occ[MAXB];
+    int n = decode(c, f, occ);
+    double h = c->ecore;
+    for (int iel = 0; iel < n; iel++) {
+        int i = occ[iel];
+        h = h + h1_get(c, i, i);
+        for (int jel = iel + 1; jel < n; jel++) {
+            int j = occ[jel];
+            h = h + v2_get(c, i, j, i, j);
+            if (c->orb_ms[i] == c->orb_ms[j]) h = h - v2_get(c, i, j, j, i);
+        }
+    }
+    return h;
+}
+
+/* slater_condon1_mol_excit (src/hamiltonian_molecular.f90:199-259). */
+static double sc1_mol_excit(const oracle_ctx *c, const int *occ, int i, int a, int perm) {
+    double h = h1_get(c, i, a);
+    for (int iel = 0; iel < c->nel; iel++) {
+        int k = occ[iel];
+        if (k != i) {
+            h = h + v2_get(c, i, k, a, k);
+            if (c->orb_ms[k] == c->orb_ms[i]) h = h - v2_get(c, i, k, k, a);
+        }
+    }
+    if (perm) h = -h;
+    return h;
+}
+
+/* slater_condon2_mol_excit (src/hamiltonian_molecular.f90:300-346). */
+static double sc2_mol_excit(const oracle_ctx *c, int i, int j, int a, int b, int perm) {
+    double h = 0.0;
+    if (c->orb_ms[i] == c->orb_ms[a]) h = v2_get(c, i, j, a, b);
+    if (c->orb_ms[i] == c->orb_ms[b]) h = h - v2_get(c, i, j, b, a);
+    if (perm) h = -h;
+    return h;
+}
+
+/* decode_det_occ_symunocc (src/determinant_decoders.f90:166-180). */
+static void decode_mol(const oracle_ctx *c, const uint64_t *f, det_info *d) {
+    d->nocc = decode(c, f, d->occ);
+    for (int k = 0; k < 2 * c->nsym; k++) d->symunocc[k] = c->nbss[k];
+    for (int i = 0; i < d->nocc; i++) {
+        int p = d->occ[i];
+        d->symunocc[ims_of(c, p) * c->nsym + c->orb_sym[p]]--;
+    }
+}
+
+#define SYMUNOCC(d, ims, s) ((d)->symunocc[(ims) * c->nsym + (s)])
+#define NBSS(ims, s) (c->nbss[(ims) * c->nsym + (s)])
+#define SSBF(ind, ims, s) (c->ssbf[((s) * 2 + (ims)) * c->maxss + (ind)])
+
+/* cross_product_pg_sym / pg_sym_conj (src/pg_symmetry.f90) without Lz. */
+static inline int cross(const oracle_ctx *c, int a, int b) { return (a ^ b) & (c->nsym - 1); }
+
+/* choose_ij_mol (src/excit_gen_mol.f90:620-660). */
+static void choose_ij_mol(const oracle_ctx *c, rstream *rs, const det_info *d, int *i, int *j, int *ij_sym,
+                          int *ij_spin, double *pgen_ij) {
+    double x = rs_next(rs) * (double)c->nel * (double)(c->nel - 1) / 2.0;
+    int ind = (int)x + 1;
+    int j_ind = (int)(1.50 + sqrt((double)(2 * ind) - 1.750));
+    int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
+    *i = d->occ[i_ind - 1];
+    *j = d->occ[j_ind - 1];
+    *ij_sym = cross(c, c->orb_sym[*i], c->orb_sym[*j]);
+    *ij_spin = c->orb_ms[*i] + c->orb_ms[*j];
+    *pgen_ij = 2.0 / (double)(c->nel * (c->nel - 1));
+}
+
+/* spin-dependent (fac, shift, na) of choose_ab_mol / find_ab_mol, 0-based:
+ * spin -2 -> beta orbitals 2k+1, spin 2 -> alpha 2k, spin 0 -> any. */
+static inline int pick_a(const oracle_ctx *c, int spin, double r) {
+    if (spin == 0) return (int)(r * (double)c->nbasis);
+    int k = (int)(r * (double)(c->nbasis / 2));
+    return spin == -2 ? 2 * k + 1 : 2 * k;
+}
+
+/* choose_ab_mol (src/excit_gen_mol.f90:802-948). */
+static int choose_ab_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, int sym, int spin,
+                         const det_info *d, int *a_out, int *b_out) {
+    int allowed = 0;
+    int ia = spin == -2 ? 0 : 1; /* ims of the spin-parallel case */
+    for (int isyma = 0; isyma < c->nsym; isyma++) {
+        int isymb = cross(c, isyma, sym);
+        if (spin == 0) {
+            if ((SYMUNOCC(d, 0, isyma) > 0 && SYMUNOCC(d, 1, isymb) > 0) ||
+                (SYMUNOCC(d, 1, isyma) > 0 && SYMUNOCC(d, 0, isymb) > 0)) { allowed = 1; break; }
+        } else {
+            if (SYMUNOCC(d, ia, isyma) > 0 &&
+                (SYMUNOCC(d, ia, isymb) > 1 || (SYMUNOCC(d, ia, isymb) == 1 && isyma != isymb))) {
+                allowed = 1;
+                break;
+            }
+        }
+    }
+    if (!allowed) return 0;
+    int a, b = -1;
+    for (;;) {
+        a = pick_a(c, spin, rs_next(rs));
+        if (!tbit(f, a)) {
+            int imsb = (spin - c->orb_ms[a] + 3) / 2 - 1;
+            int isymb = cross(c, sym, c->orb_sym[a]);
+            int nu = SYMUNOCC(d, imsb, isymb);
+            if (nu > 1 || (nu == 1 && (isymb != c->orb_sym[a] || spin == 0))) {
+                for (;;) {
+                    int ind = (int)((double)NBSS(imsb, isymb) * rs_next(rs));
+                    b = SSBF(ind, imsb, isymb);
+                    if (b != a && !tbit(f, b)) break;
+                }
+                break;
+            }
+        }
+    }
+    if (a > b) { int t = a; a = b; b = t; }
+    *a_out = a;
+    *b_out = b;
+    return 1;
+}
+
+/* find_ab_mol (src/excit_gen_mol.f90:1018-1138). */
+static int find_ab_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, int sym, int spin, int *a_out,
+                       int *b_out) {
+    int a, b;
+    for (;;) {
+        a = pick_a(c, spin, rs_next(rs));
+        if (!tbit(f, a)) break;
+    }
+    int imsb = (spin - c->orb_ms[a] + 3) / 2 - 1;
+    int isymb = cross(c, sym, c->orb_sym[a]);
+    int allowed;
+    if (NBSS(imsb, isymb) == 0) {
+        allowed = 0;
+    } else if (spin != 0 && isymb == c->orb_sym[a] && NBSS(imsb, isymb) == 1) {
+        allowed = 0;
+    } else {
+        for (;;) {
+            int ind = (int)((double)NBSS(imsb, isymb) * rs_next(rs));
+            b = SSBF(ind, imsb, isymb);
+            if (b != a) break;
+        }
+        allowed = !tbit(f, b);
+        if (a > b) { int t = a; a = b; b = t; }
+    }
+    *a_out = a;
+    *b_out = allowed ? b : -1;
+    return allowed;
+}
+
+/* choose_ia_mol (src/excit_gen_mol.f90:521-618), op_sym = gamma. */
+static int choose_ia_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int *i_out,
+                         int *a_out) {
+    int allowed = 0;
+    for (int k = 0; k < c->nel; k++) {
+        int p = d->occ[k];
+        if (SYMUNOCC(d, ims_of(c, p), c->orb_sym[p]) != 0) { allowed = 1; break; }
+    }
+    if (!allowed) return 0;
+    int i, a;
+    for (;;) {
+        i = d->occ[(int)(rs_next(rs) * (double)c->nel)];
+        int imsa = ims_of(c, i), isyma = c->orb_sym[i];
+        if (SYMUNOCC(d, imsa, isyma) != 0) {
+            for (;;) {
+                int ind = (int)((double)NBSS(imsa, isyma) * rs_next(rs));
+                a = SSBF(ind, imsa, isyma);
+                if (!tbit(f, a)) break;
+            }
+            break;
+        }
+    }
+    *i_out = i;
+    *a_out = a;
+    return 1;
+}
+
+/* find_ia_mol (src/excit_gen_mol.f90:950-1016). */
+static int find_ia_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int *i_out,
+                       int *a_out) {
+    int i = d->occ[(int)(rs_next(rs) * (double)c->nel)];
+    int imsa = ims_of(c, i), isyma = c->orb_sym[i];
+    int ind = (int)((double)NBSS(imsa, isyma) * rs_next(rs));
+    *i_out = i;
+    if (NBSS(imsa, isyma) == 0) return 0;
+    int a = SSBF(ind, imsa, isyma);
+    *a_out = a;
+    return !tbit(f, a);
+}
+
+/* calc_pgen_single_mol (src/excit_gen_mol.f90:1140-1200). */
+static double calc_pgen_single_mol(const oracle_ctx *c, const det_info *d, int a) {
+    int ni = c->nel;
+    for (int k = 0; k < c->nel; k++) {
+        int p = d->occ[k];
+        if (SYMUNOCC(d, ims_of(c, p), c->orb_sym[p]) == 0) ni--;
+    }
+    return 1.0 / (double)(ni * SYMUNOCC(d, ims_of(c, a), c->orb_sym[a]));
+}
+
+/* calc_pgen_double_mol (src/excit_gen_mol.f90:1202-1327). */
+static double calc_pgen_double_mol(const oracle_ctx *c, int ij_sym, int a, int b, int spin, const det_info *d) {
+    int imsa = ims_of(c, a), imsb = ims_of(c, b);
+    int n_aij;
+    double p_bija, p_aijb;
+    if (spin == 0) {
+        n_aij = c->nvirt;
+        for (int isyma = 0; isyma < c->nsym; isyma++) {
+            int isymb = cross(c, isyma, ij_sym);
+            if (SYMUNOCC(d, 0, isymb) == 0) n_aij -= SYMUNOCC(d, 1, isyma);
+            if (SYMUNOCC(d, 1, isymb) == 0) n_aij -= SYMUNOCC(d, 0, isyma);
+        }
+        p_aijb = 1.0 / (double)SYMUNOCC(d, imsa, c->orb_sym[a]);
+        p_bija = 1.0 / (double)SYMUNOCC(d, imsb, c->orb_sym[b]);
+    } else {
+        int is = spin == -2 ? 0 : 1;
+        n_aij = spin == -2 ? c->nvirt_beta : c->nvirt_alpha;
+        for (int isyma = 0; isyma < c->nsym; isyma++) {
+            int isymb = cross(c, isyma, ij_sym);
+            if (SYMUNOCC(d, is, isymb) == 0)
+                n_aij -= SYMUNOCC(d, is, isyma);
+            else if (isyma == isymb && SYMUNOCC(d, is, isymb) == 1)
+                n_aij -= SYMUNOCC(d, is, isyma);
+        }
+        if (c->orb_sym[a] == c->orb_sym[b]) {
+            p_aijb = 1.0 / (double)(SYMUNOCC(d, imsa, c->orb_sym[a]) - 1);
+            p_bija = 1.0 / (double)(SYMUNOCC(d, imsb, c->orb_sym[b]) - 1);
+        } else {
+            p_aijb = 1.0 / (double)SYMUNOCC(d, imsa, c->orb_sym[a]);
+            p_bija = 1.0 / (double)SYMUNOCC(d, imsb, c->orb_sym[b]);
+        }
+    }
+    return (1.0 / (double)n_aij) * (p_bija + p_aijb);
+}
+
+/* calc_pgen_single_mol_no_renorm (src/excit_gen_mol.f90:1329-1366). */
+static double calc_pgen_single_mol_no_renorm(const oracle_ctx *c, int a) {
+    return 1.0 / (double)(c->nel * NBSS(ims_of(c, a), c->orb_sym[a]));
+}
+
+/* calc_pgen_double_mol_no_renorm (src/excit_gen_mol.f90:1368-1445). */
+static double calc_pgen_double_mol_no_renorm(const oracle_ctx *c, int a, int b, int spin) {
+    int n_aij = spin == -2 ? c->nvirt_beta : (spin == 0 ? c->nvirt : c->nvirt_alpha);
+    int imsa = ims_of(c, a), isyma = c->orb_sym[a], imsb = ims_of(c, b), isymb = c->orb_sym[b];
+    double p_bija, p_aijb;
+    if (isyma == isymb && imsa == imsb) {
+        p_aijb = 1.0 / (double)(NBSS(imsa, isyma) - 1);
+        p_bija = 1.0 / (double)(NBSS(imsb, isymb) - 1);
+    } else {
+        p_aijb = 1.0 / (double)NBSS(imsa, isyma);
+        p_bija = 1.0 / (double)NBSS(imsb, isymb);
+    }
+    return (1.0 / (double)n_aij) * (p_bija + p_aijb);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Excitation generation: one spawning attempt                                */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    excit_t e;
+    double pgen, hmatel;
+    int allowed;
+    int64_t nspawn;
+} attempt_t;
+
+/* stochastic_round_spawned_particle (src/stoch_utils.f90:87-136). */
+static int64_t round_spawned(int64_t cutoff, double pspawn, rstream *rs) {
+    int64_t nspawn;
+    if (pspawn < (double)cutoff) {
+        if (pspawn > rs_next(rs) * (double)cutoff) nspawn = cutoff;
+        else nspawn = 0;
+    } else {
+        nspawn = (int64_t)pspawn;
+        double padd = pspawn - (double)nspawn;
+        if (padd > rs_next(rs)) nspawn = nspawn + 1;
+    }
+    return nspawn;
+}
+
+/* Fortran sign(a, b) for integers: |a| with the sign of b (b >= 0 -> +). */
+static inline int64_t isign64(int64_t a, int64_t b) {
+    int64_t m = a < 0 ? -a : a;
+    return b >= 0 ? m : -m;
+}
+
+/* set_child_sign (src/spawning.F90:680-709). */
+static inline int64_t child_sign(double hmatel, int64_t parent, int64_t nspawn) {
+    if (hmatel > 0.0) return -isign64(nspawn, parent);
+    return isign64(nspawn, parent);
+}
+
+/* spawn_lattice_split_gen (src/spawning.F90:215-315) with gen_excit_init_hub_k /
+ * gen_excit_finalise_hub_k (src/excit_gen_hub_k.f90:29-156) or the no_renorm
+ * pair (:158-277). */
+static void attempt_hub_k(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int64_t parent,
+                          attempt_t *out, int complete) {
+    int i, j, ij_sym, a = -1, b = -1;
+    double pgen, abs_h;
+    memset(out, 0, sizeof(*out));
+    out->e.nexcit = 2;
+    choose_ij_hub_k(c, rs, d, &i, &j, &ij_sym);
+    int renorm = c->cfg.excit_gen != HGPU_EXCIT_GEN_NO_RENORM;
+    if (renorm) {
+        pgen = calc_pgen_hub_k(c, ij_sym, f, d);
+        out->allowed = 1.0 / pgen > DEPSILON;
+        abs_h = fabs(c->coulomb_k);
+    } else {
+        out->allowed = find_ab_hub_k(c, rs, f, d, ij_sym, &a, &b);
+        if (out->allowed) {
+            pgen = 1.0 / (double)(c->nalpha * c->nbeta * c->nvirt_alpha);
+            abs_h = fabs(c->coulomb_k);
+        } else {
+            pgen = 1.0;
+            abs_h = 0.0;
+        }
+    }
+    out->pgen = pgen;
+    double pspawn = (double)c->real_factor * c->cfg.tau * abs_h / pgen;
+    int64_t nspawn = round_spawned(c->cutoff, pspawn, rs);
+    out->e.from[0] = i;
+    out->e.from[1] = j;
+    if (nspawn != 0 || (complete && out->allowed)) {
+        /* gen_excit_finalise_hub_k: choose_ab_hub_k redraws until b is free */
+        if (renorm) {
+            int ok = 0;
+            while (!ok) ok = find_ab_hub_k(c, rs, f, d, ij_sym, &a, &b);
+        }
+        out->e.to[0] = a;
+        out->e.to[1] = b;
+        out->hmatel = sc2_hub_k_excit(c, f, &out->e);
+        if (nspawn != 0) nspawn = child_sign(out->hmatel, parent, nspawn);
+    } else {
+        out->e.to[0] = a;
+        out->e.to[1] = b;
+        out->hmatel = abs_h;
+    }
+    out->nspawn = nspawn;
+}
+
+/* gen_excit_mol / gen_excit_mol_no_renorm (src/excit_gen_mol.f90:16-284) with
+ * spawn_standard + attempt_to_spawn (src/spawning.F90:34-123, :711-768). */
+static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int64_t parent,
+                        attempt_t *out) {
+    memset(out, 0, sizeof(*out));
+    out->e.from[0] = out->e.from[1] = out->e.to[0] = out->e.to[1] = -1;
+    int renorm = c->cfg.excit_gen == HGPU_EXCIT_GEN_RENORM;
+    double pgen, hmatel;
+    if (rs_next(rs) < c->pattempt_single) {
+        int i = -1, a = -1, ok;
+        out->e.nexcit = 1;
+        if (renorm) ok = choose_ia_mol(c, rs, f, d, &i, &a);
+        else ok = find_ia_mol(c, rs, f, d, &i, &a);
+        out->allowed = ok;
+        out->e.from[0] = i;
+        out->e.to[0] = ok ? a : -1;
+        if (ok) {
+            pgen = c->pattempt_single *
+                   (renorm ? calc_pgen_single_mol(c, d, a) : calc_pgen_single_mol_no_renorm(c, a));
+            out->e.perm = perm1(c, f, i, a);
+            hmatel = sc1_mol_excit(c, d->occ, i, a, out->e.perm);
+        } else {
+            hmatel = 0.0;
+            pgen = 1.0;
+        }
+    } else {
+        int i, j, ij_sym, ij_spin, a = -1, b = -1, ok;
+        double pgen_ij;
+        out->e.nexcit = 2;
+        choose_ij_mol(c, rs, d, &i, &j, &ij_sym, &ij_spin, &pgen_ij);
+        if (renorm) ok = choose_ab_mol(c, rs, f, ij_sym, ij_spin, d, &a, &b);
+        else ok = find_ab_mol(c, rs, f, ij_sym, ij_spin, &a, &b);
+        out->allowed = ok;
+        out->e.from[0] = i;
+        out->e.from[1] = j;
+        if (ok) {
+            out->e.to[0] = a;
+            out->e.to[1] = b;
+            if (renorm)
+                pgen = c->pattempt_double * pgen_ij * calc_pgen_double_mol(c, ij_sym, a, b, ij_spin, d);
+            else
+                pgen = c->pattempt_double * pgen_ij * calc_pgen_double_mol_no_renorm(c, a, b, ij_spin);
+            out->e.perm = perm2(c, f, i, j, a, b);
+            hmatel = sc2_mol_excit(c, i, j, a, b, out->e.perm);
+        } else {
+            hmatel = 0.0;
+            pgen = 1.0;
+        }
+    }
+    out->pgen = pgen;
+    out->hmatel = hmatel;
+    /* attempt_to_spawn */
+    double pspawn = c->cfg.tau * fabs(hmatel) / pgen;
+    pspawn = pspawn * (double)c->real_factor;
+    int64_t nspawn = round_spawned(c->cutoff, pspawn, rs);
+    if (nspawn > 0) nspawn = child_sign(hmatel, parent, nspawn);
+    out->nspawn = nspawn;
+}
+
+static void decode_any(const oracle_ctx *c, const uint64_t *f, det_info *d) {
+    if (c->kind == HGPU_SYS_HUB_K) decode_hub_k(c, f, d);
+    else decode_mol(c, f, d);
+}
+
+static void attempt(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int64_t parent,
+                    attempt_t *out, int complete) {
+    if (c->kind == HGPU_SYS_HUB_K) attempt_hub_k(c, rs, f, d, parent, out, complete);
+    else attempt_mol(c, rs, f, d, parent, out);
+}
+
+static double sc0(const oracle_ctx *c, const uint64_t *f) {
+    return c->kind == HGPU_SYS_HUB_K ? sc0_hub_k(c, f) : sc0_mol(c, f);
+}
+
+/* get_hmatel_hub_k (src/hamiltonian_hub_k.f90:12-89) / get_hmatel_mol
+ * (src/hamiltonian_molecular.f90:12-65). */
+static double hmatel_any(const oracle_ctx *c, const uint64_t *f1, const uint64_t *f2) {
+    excit_t e = get_excitation(c, f1, f2);
+    if (e.nexcit == 0) return sc0(c, f1);
+    if (c->kind == HGPU_SYS_HUB_K) {
+        if (e.nexcit != 2) return 0.0;
+        double h = two_e_int_hub_k(c, e.from[0], e.from[1], e.to[0], e.to[1]);
+        return e.perm ? -h : h;
+    }
+    if (e.nexcit == 1) {
+        if (c->orb_sym[e.from[0]] != c->orb_sym[e.to[0]] || c->orb_ms[e.from[0]] != c->orb_ms[e.to[0]]) return 0.0;
+        int occ[MAXB];
+        decode(c, f1, occ);
+        return sc1_mol_excit(c, occ, e.from[0], e.to[0], e.perm);
+    }
+    if (e.nexcit == 2) {
+        int i = e.from[0], j = e.from[1], a = e.to[0], b = e.to[1];
+        if (cross(c, c->orb_sym[i], c->orb_sym[j]) != cross(c, c->orb_sym[a], c->orb_sym[b])) return 0.0;
+        /* slater_condon2_mol: get_two_body_int_mol_real checks the spins */
+        double h = 0.0, x = 0.0;
+        if (c->orb_ms[i] == c->orb_ms[a] && c->orb_ms[j] == c->orb_ms[b]) h = v2_get(c, i, j, a, b);
+        if (c->orb_ms[i] == c->orb_ms[b] && c->orb_ms[j] == c->orb_ms[a]) x = v2_get(c, i, j, b, a);
+        h = h - x;
+        return e.perm ? -h : h;
+    }
+    return 0.0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Per-determinant steps                                                      */
+/* ------------------------------------------------------------------------- */
+
+/* decide_nattempts (src/qmc_common.F90:379-406). */
+static int64_t decide_nattempts(rstream *rs, double population) {
+    double ap = fabs(population);
+    int64_t n = (int64_t)ap;
+    double pextra = ap - (double)n;
+    if (fabs(pextra) > DEPSILON) {
+        if (pextra > rs_next(rs)) n = n + 1;
+    }
+    return n;
+}
+
+/* stochastic_death (src/death.f90:11-130) with quasi-Newton and Chebyshev
+ * off: weight = quasi_newton_pop_control = dmqmc_factor = 1 and p_d reduces
+ * to tau*(K_ii - S). */
+static int64_t stochastic_death(const oracle_ctx *c, rstream *rs, double Kii, double shift, int64_t *population) {
+    double pd = c->cfg.tau * (Kii - shift);
+    pd = pd * fabs((double)*population);
+    int64_t kill = (int64_t)pd;
+    pd = pd - (double)kill;
+    double r = rs_next(rs);
+    if (fabs(pd) > r) {
+        if (pd > 0.0) kill = kill + 1;
+        else kill = kill - 1;
+    }
+    if (*population < 0) *population = *population + kill;
+    else *population = *population - kill;
+    return kill < 0 ? -kill : kill;
+}
+
+/* set_parent_flag (src/ifciqmc.f90:14-57): bit s set if NOT an initiator in space s. */
+static int64_t parent_flag(const oracle_ctx *c, const double *real_pop) {
+    int64_t flag = 0;
+    for (int s = 0; s < c->R; s++)
+        if (!(fabs(real_pop[s]) > c->cfg.initiator_pop)) flag |= (int64_t)1 << s;
+    return flag;
+}
+
+/* update_proj_energy_hub_k / update_proj_energy_mol
+ * (src/energy_evaluation.F90:795-849, :906-985). */
+static void update_proj_energy(oracle_ctx *c, const uint64_t *f, const det_info *d, const excit_t *ex, double pop,
+                               int s) {
+    excit_t e = *ex;
+    if (e.nexcit == 0) {
+        c->acc_d0[s] += pop;
+        return;
+    }
+    if (c->kind == HGPU_SYS_HUB_K) {
+        if (e.nexcit == 2) {
+            double h = two_e_int_hub_k(c, e.from[0], e.from[1], e.to[0], e.to[1]);
+            if (e.perm) h = -h;
+            c->acc_proj[s] += h * pop;
+        }
+        return;
+    }
+    if (e.nexcit == 1) {
+        if (c->orb_ms[e.from[0]] == c->orb_ms[e.to[0]] && c->orb_sym[e.from[0]] == c->orb_sym[e.to[0]]) {
+            double h = sc1_mol_excit(c, d->occ, e.from[0], e.to[0], e.perm);
+            c->acc_proj[s] += h * pop;
+        }
+    } else if (e.nexcit == 2) {
+        int i = e.from[0], j = e.from[1], a = e.to[0], b = e.to[1];
+        if (c->orb_ms[i] + c->orb_ms[j] == c->orb_ms[a] + c->orb_ms[b]) {
+            if (cross(c, c->orb_sym[i], c->orb_sym[j]) == cross(c, c->orb_sym[a], c->orb_sym[b])) {
+                double h = sc2_mol_excit(c, i, j, a, b, e.perm);
+                c->acc_proj[s] += h * pop;
+            }
+        }
+    }
+    (void)f;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Annihilation                                                               */
+/* ------------------------------------------------------------------------- */
+
+static const oracle_ctx *g_sort_ctx;
+
+static int cmp_spawn(const void *x, const void *y) {
+    const oracle_ctx *c = g_sort_ctx;
+    int64_t i = *(const int64_t *)x, j = *(const int64_t *)y;
+    int r = det_cmp(&c->sdets[i * c->nw], &c->sdets[j * c->nw], c->nw);
+    if (r != 0) return r == 1 ? -1 : 1;
+    if (c->sord[i] < c->sord[j]) return -1;
+    if (c->sord[i] > c->sord[j]) return 1;
+    return 0;
+}
+
+/* Sort the spawned list by determinant; entries on the same determinant keep
+ * their generation order (the reference's qsort, src/sort.f90:213-394, leaves
+ * that order unspecified; a stable order makes the oracle deterministic). */
+static void sort_spawns(oracle_ctx *c) {
+    int64_t n = c->sn;
+    int64_t *perm = (int64_t *)malloc(sizeof(int64_t) * (n > 0 ? n : 1));
+    for (int64_t i = 0; i < n; i++) perm[i] = i;
+    g_sort_ctx = c;
+    qsort(perm, (size_t)n, sizeof(int64_t), cmp_spawn);
+    uint64_t *d2 = (uint64_t *)malloc(sizeof(uint64_t) * c->nw * (n > 0 ? n : 1));
+    int64_t *p2 = (int64_t *)malloc(sizeof(int64_t) * c->R * (n > 0 ? n : 1));
+    int64_t *f2 = (int64_t *)malloc(sizeof(int64_t) * (n > 0 ? n : 1));
+    int64_t *o2 = (int64_t *)malloc(sizeof(int64_t) * (n > 0 ? n : 1));
+    for (int64_t k = 0; k < n; k++) {
+        int64_t i = perm[k];
+        memcpy(&d2[k * c->nw], &c->sdets[i * c->nw], sizeof(uint64_t) * c->nw);
+        memcpy(&p2[k * c->R], &c->spops[i * c->R], sizeof(int64_t) * c->R);
+        f2[k] = c->sflag[i];
+        o2[k] = c->sord[i];
+    }
+    memcpy(c->sdets, d2, sizeof(uint64_t) * c->nw * n);
+    memcpy(c->spops, p2, sizeof(int64_t) * c->R * n);
+    memcpy(c->sflag, f2, sizeof(int64_t) * n);
+    memcpy(c->sord, o2, sizeof(int64_t) * n);
+    free(perm); free(d2); free(p2); free(f2); free(o2);
+}
+
+static void scopy(oracle_ctx *c, int64_t dst, int64_t src) {
+    if (dst == src) return;
+    memcpy(&c->sdets[dst * c->nw], &c->sdets[src * c->nw], sizeof(uint64_t) * c->nw);
+    memcpy(&c->spops[dst * c->R], &c->spops[src * c->R], sizeof(int64_t) * c->R);
+    c->sflag[dst] = c->sflag[src];
+    c->sord[dst] = c->sord[src];
+    c->suid[dst] = c->suid[src];
+}
+
+static int all_zero(const int64_t *p, int R) {
+    for (int s = 0; s < R; s++)
+        if (p[s] != 0) return 0;
+    return 1;
+}
+
+/* annihilate_spawn_t (src/spawn_data.F90:859-935). */
+static void annihilate_spawn_t(oracle_ctx *c) {
+    int64_t ub = c->sn; /* number of entries (1-based upper bound) */
+    if (ub == 0) return;
+    int64_t islot = 0, k = 0; /* 0-based */
+    for (;;) {
+        scopy(c, islot, k);
+        int done = 0;
+        for (;;) {
+            k++;
+            if (k > ub - 1) { done = 1; break; }
+            if (det_cmp(&c->sdets[k * c->nw], &c->sdets[islot * c->nw], c->nw) == 0) {
+                for (int s = 0; s < c->R; s++) c->spops[islot * c->R + s] += c->spops[k * c->R + s];
+            } else {
+                break;
+            }
+        }
+        if (done) break;
+        if (islot == ub - 1) break;
+        if (!all_zero(&c->spops[islot * c->R], c->R)) islot++;
+    }
+    if (all_zero(&c->spops[islot * c->R], c->R)) islot--;
+    c->sn = islot + 1;
+}
+
+/* Fortran sign(1, int(x)) for an int_s population: int() converts to default
+ * (32-bit) integer, which keeps the low 32 bits. */
+static inline int sign1_int32(int64_t x) {
+    int32_t v = (int32_t)(uint32_t)(uint64_t)x;
+    return v >= 0 ? 1 : -1;
+}
+
+/* annihilate_spawn_t_initiator (src/spawn_data.F90:937-1101). */
+static void annihilate_spawn_t_initiator(oracle_ctx *c) {
+    int64_t ub = c->sn;
+    if (ub == 0) return;
+    int64_t islot = 0, k = 0;
+    int64_t events[2], ipop[2];
+    for (;;) {
+        scopy(c, islot, k);
+        for (int s = 0; s < c->R; s++) {
+            if (!((c->sflag[k] >> s) & 1)) {
+                ipop[s] = c->spops[k * c->R + s];
+                events[s] = 0;
+            } else {
+                ipop[s] = 0;
+                events[s] = sign1_int32(c->spops[k * c->R + s]);
+            }
+        }
+        for (;;) {
+            k++;
+            int same = k <= ub - 1;
+            if (same) same = det_cmp(&c->sdets[k * c->nw], &c->sdets[islot * c->nw], c->nw) == 0;
+            if (same) {
+                for (int s = 0; s < c->R; s++) {
+                    int64_t v = c->spops[k * c->R + s];
+                    if (!((c->sflag[k] >> s) & 1)) ipop[s] += v;
+                    else if (v < 0) events[s] -= 1;
+                    else if (v > 0) events[s] += 1;
+                }
+                for (int s = 0; s < c->R; s++) c->spops[islot * c->R + s] += c->spops[k * c->R + s];
+            } else {
+                int64_t flag = 0;
+                for (int s = 0; s < c->R; s++) {
+                    int64_t tot = c->spops[islot * c->R + s];
+                    if (ipop[s] != 0 && (tot >= 0 ? 1 : -1) == (ipop[s] >= 0 ? 1 : -1)) {
+                        /* keep: sign-coherent with the initiator-sourced particles */
+                    } else if (llabs(events[s]) > 1) {
+                        /* keep: multiple coherent events */
+                    } else {
+                        flag += (int64_t)1 << s;
+                    }
+                }
+                c->sflag[islot] = flag;
+                break;
+            }
+        }
+        if (islot == ub - 1 || k > ub - 1) break;
+        if (!all_zero(&c->spops[islot * c->R], c->R)) islot++;
+    }
+    if (all_zero(&c->spops[islot * c->R], c->R)) islot--;
+    c->sn = islot + 1;
+}
+
+/* binary_search_i0_list (src/search.f90:47-170), 0-based, [istart, iend]. */
+static int64_t bsearch_main(const oracle_ctx *c, const uint64_t *item, int64_t istart, int64_t iend, int *hit) {
+    int64_t pos;
+    *hit = 0;
+    if (istart > iend) return istart;
+    int64_t lo = istart, hi = iend;
+    pos = lo;
+    while (hi != lo) {
+        pos = (hi + lo) / 2;
+        int cmp = det_cmp(&c->dets[pos * c->nw], item, c->nw);
+        if (cmp == 0) { *hit = 1; return pos; }
+        if (cmp == 1) lo = pos + 1;
+        else hi = pos;
+    }
+    int cmp = det_cmp(&c->dets[hi * c->nw], item, c->nw);
+    if (cmp == 0) { *hit = 1; return hi; }
+    if (cmp == 1) return hi + 1;
+    return hi;
+}
+
+/* annihilate_main_list (src/annihilation.f90:294-370) and
+ * annihilate_main_list_initiator (:372-486). */
+static void annihilate_main_list(oracle_ctx *c, int initiator) {
+    int64_t nann = 0, istart = 0, iend = c->n - 1;
+    for (int64_t i = 0; i < c->sn; i++) {
+        int hit;
+        int64_t pos = bsearch_main(c, &c->sdets[i * c->nw], istart, iend, &hit);
+        if (hit) {
+            for (int s = 0; s < c->R; s++) {
+                int64_t sp = c->spops[i * c->R + s];
+                if (!initiator) {
+                    c->pops[pos * c->R + s] += sp;
+                } else if (c->pops[pos * c->R + s] != 0) {
+                    c->pops[pos * c->R + s] += sp;
+                } else if (!((c->sflag[i] >> s) & 1)) {
+                    c->pops[pos * c->R + s] = sp;
+                }
+            }
+            nann++;
+            istart = pos + 1;
+        } else if (!initiator) {
+            scopy(c, i - nann, i);
+        } else {
+            int discard = 1;
+            int64_t keep[2];
+            for (int s = 0; s < c->R; s++) {
+                if ((c->sflag[i] >> s) & 1) keep[s] = 0;
+                else { keep[s] = c->spops[i * c->R + s]; discard = 0; }
+            }
+            if (discard) {
+                nann++;
+            } else {
+                scopy(c, i - nann, i);
+                for (int s = 0; s < c->R; s++) c->spops[(i - nann) * c->R + s] = keep[s];
+            }
+        }
+    }
+    c->sn -= nann;
+}
+
+/* stochastic_round_int_64 (src/stoch_utils.f90:51-85) for one entry. */
+static void stochastic_round_pops(const oracle_ctx *c, int64_t *pop, int purpose, int64_t idx) {
+    for (int s = 0; s < c->R; s++) {
+        int64_t p = pop[s];
+        if (llabs(p) < c->real_factor && p != 0) {
+            rstream rs;
+            rs_init(&rs, (uint64_t)c->cfg.seed, purpose, s, (uint64_t)idx, 0, (uint64_t)c->iter);
+            double r = rs_next(&rs) * (double)c->real_factor;
+            if ((double)llabs(p) > r) pop[s] = isign64(c->real_factor, p);
+            else pop[s] = 0;
+        }
+    }
+}
+
+/* remove_unoccupied_dets (src/annihilation.f90:537-598). */
+static void remove_unoccupied_dets(oracle_ctx *c) {
+    int64_t nzero = 0;
+    for (int64_t i = 0; i < c->n; i++) {
+        if (c->cfg.real_amplitudes) stochastic_round_pops(c, &c->pops[i * c->R], P_ROUND_MAIN, i);
+        if (all_zero(&c->pops[i * c->R], c->R)) {
+            nzero++;
+        } else if (nzero > 0) {
+            int64_t k = i - nzero;
+            memcpy(&c->dets[k * c->nw], &c->dets[i * c->nw], sizeof(uint64_t) * c->nw);
+            memcpy(&c->pops[k * c->R], &c->pops[i * c->R], sizeof(int64_t) * c->R);
+            c->kii[k] = c->kii[i];
+        }
+    }
+    c->n -= nzero;
+}
+
+/* round_low_population_spawns (src/annihilation.f90:600-675); the rounding
+ * stream of an entry is keyed by its index in the self-annihilated list. */
+static void round_low_population_spawns(oracle_ctx *c) {
+    int64_t nrem = 0;
+    for (int64_t i = 0; i < c->sn; i++) {
+        stochastic_round_pops(c, &c->spops[i * c->R], P_ROUND_SPAWN, c->suid[i]);
+        if (all_zero(&c->spops[i * c->R], c->R)) nrem++;
+        else scopy(c, i - nrem, i);
+    }
+    c->sn -= nrem;
+}
+
+/* insert_new_walkers / insert_new_walker (src/annihilation.f90:677-901): a
+ * merge of two sorted lists, with dat(1) = sc0 - H00 for new determinants. */
+static void insert_new_walkers(oracle_ctx *c) {
+    if (c->n + c->sn > c->cap) {
+        c->error_flags |= HGPU_FLAG_MAIN_OVERFLOW;
+        return;
+    }
+    int64_t n = c->n, m = c->sn, tot = n + m;
+    uint64_t *nd = (uint64_t *)malloc(sizeof(uint64_t) * c->nw * (tot > 0 ? tot : 1));
+    int64_t *np = (int64_t *)malloc(sizeof(int64_t) * c->R * (tot > 0 ? tot : 1));
+    double *nk = (double *)malloc(sizeof(double) * (tot > 0 ? tot : 1));
+    int64_t i = 0, j = 0, k = 0;
+    while (i < n || j < m) {
+        int take_spawn;
+        if (i >= n) take_spawn = 1;
+        else if (j >= m) take_spawn = 0;
+        else take_spawn = det_cmp(&c->sdets[j * c->nw], &c->dets[i * c->nw], c->nw) == 1;
+        if (take_spawn) {
+            memcpy(&nd[k * c->nw], &c->sdets[j * c->nw], sizeof(uint64_t) * c->nw);
+            memcpy(&np[k * c->R], &c->spops[j * c->R], sizeof(int64_t) * c->R);
+            nk[k] = sc0(c, &c->sdets[j * c->nw]) - c->H00;
+            j++;
+        } else {
+            memcpy(&nd[k * c->nw], &c->dets[i * c->nw], sizeof(uint64_t) * c->nw);
+            memcpy(&np[k * c->R], &c->pops[i * c->R], sizeof(int64_t) * c->R);
+            nk[k] = c->kii[i];
+            i++;
+        }
+        k++;
+    }
+    memcpy(c->dets, nd, sizeof(uint64_t) * c->nw * tot);
+    memcpy(c->pops, np, sizeof(int64_t) * c->R * tot);
+    memcpy(c->kii, nk, sizeof(double) * tot);
+    c->n = tot;
+    free(nd); free(np); free(nk);
+}
+
+/* direct_annihilation (src/annihilation.f90:9-80) with
+ * annihilate_main_list_wrapper (:214-292). */
+static void direct_annihilation(oracle_ctx *c) {
+    int initiator = c->cfg.initiator_approx;
+    if (c->sn > 0) {
+        sort_spawns(c);
+        if (initiator) annihilate_spawn_t_initiator(c);
+        else annihilate_spawn_t(c);
+    }
+    for (int64_t i = 0; i < c->sn; i++) c->suid[i] = i;
+    if (c->sn >= 1) {
+        annihilate_main_list(c, initiator);
+        remove_unoccupied_dets(c);
+        if (c->cfg.real_amplitudes) round_low_population_spawns(c);
+        insert_new_walkers(c);
+    } else {
+        remove_unoccupied_dets(c);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* The Monte Carlo cycle (src/fciqmc.f90:293-413)                             */
+/* ------------------------------------------------------------------------- */
+
+static void add_spawn(oracle_ctx *c, const uint64_t *f, int s, int64_t nspawn, int64_t flag, int64_t ord) {
+    if (c->sn >= c->scap) {
+        c->error_flags |= HGPU_FLAG_SPAWN_OVERFLOW;
+        return;
+    }
+    int64_t k = c->sn++;
+    memcpy(&c->sdets[k * c->nw], f, sizeof(uint64_t) * c->nw);
+    for (int t = 0; t < c->R; t++) c->spops[k * c->R + t] = 0;
+    c->spops[k * c->R + s] = nspawn;
+    c->sflag[k] = flag;
+    c->sord[k] = ord;
+}
+
+static int64_t abs_pop_sum(const oracle_ctx *c, int s) {
+    int64_t t = 0;
+    for (int64_t i = 0; i < c->n; i++) t += llabs(c->pops[i * c->R + s]);
+    return t;
+}
+
+static double nparticles(const oracle_ctx *c, int s) {
+    return (double)abs_pop_sum(c, s) / (double)c->real_factor;
+}
+
+static void mc_cycle(oracle_ctx *c) {
+    c->iter++;
+    /* init_mc_cycle (src/qmc_common.F90:950-1017) */
+    int64_t nattempts_acc = llround(2.0 * nparticles(c, 0));
+    int64_t ndeath = 0;
+    c->sn = 0;
+    uint64_t child[MAXW];
+    for (int64_t idet = 0; idet < c->n; idet++) {
+        const uint64_t *f = &c->dets[idet * c->nw];
+        det_info d;
+        decode_any(c, f, &d);
+        double real_pop[2];
+        for (int s = 0; s < c->R; s++) real_pop[s] = (double)c->pops[idet * c->R + s] / (double)c->real_factor;
+        int64_t flag = parent_flag(c, real_pop);
+        excit_t ex = get_excitation(c, f, c->f0);
+        for (int s = 0; s < c->R; s++) {
+            update_proj_energy(c, f, &d, &ex, real_pop[s], s);
+            rstream rs;
+            rs_init(&rs, (uint64_t)c->cfg.seed, P_NATTEMPT, s, (uint64_t)idet, 0, (uint64_t)c->iter);
+            int64_t nat = decide_nattempts(&rs, real_pop[s]);
+            c->rep_attempts += nat;
+            c->total_attempts += nat;
+            int64_t parent = c->pops[idet * c->R + s];
+            for (int64_t a = 0; a < nat; a++) {
+                attempt_t at;
+                rs_init(&rs, (uint64_t)c->cfg.seed, P_SPAWN, s, (uint64_t)idet, (uint64_t)a, (uint64_t)c->iter);
+                attempt(c, &rs, f, &d, parent, &at, 0);
+                if (at.nspawn != 0) {
+                    excited_det(c, f, &at.e, child);
+                    add_spawn(c, child, s, at.nspawn, c->cfg.initiator_approx ? flag : 0, c->sn);
+                }
+            }
+            rs_init(&rs, (uint64_t)c->cfg.seed, P_DEATH, s, (uint64_t)idet, 0, (uint64_t)c->iter);
+            ndeath += stochastic_death(c, &rs, c->kii[idet], c->shift[s], &c->pops[idet * c->R + s]);
+        }
+    }
+    int64_t nspawn_events = c->sn; /* calc_events_spawn_t */
+    c->rep_spawned += c->sn;
+    direct_annihilation(c);
+    c->last_nspawn_events = nspawn_events;
+    /* end_mc_cycle / spawning_rate (src/qmc_common.F90:1240-1304) */
+    if (nattempts_acc > 0)
+        c->acc_rspawn += ((double)nspawn_events + (double)ndeath / (double)c->real_factor) / (double)nattempts_acc;
+    c->rep_cycles++;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Public API                                                                 */
+/* ------------------------------------------------------------------------- */
+
+oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
+    if (sys->nwords > MAXW || sys->nbasis > MAXB || sys->nel > MAXEL) return NULL;
+    oracle_ctx *c = (oracle_ctx *)calloc(1, sizeof(oracle_ctx));
+    c->cfg = *cfg;
+    c->kind = sys->kind;
+    c->nbasis = sys->nbasis;
+    c->nel = sys->nel;
+    c->nalpha = sys->nalpha;
+    c->nbeta = sys->nbeta;
+    c->nw = sys->nwords;
+    c->nvirt_alpha = sys->nbasis / 2 - sys->nalpha;
+    c->nvirt_beta = sys->nbasis / 2 - sys->nbeta;
+    c->nvirt = sys->nbasis - sys->nel;
+    c->orb_sym = (int32_t *)malloc(sizeof(int32_t) * c->nbasis);
+    c->orb_ms = (int32_t *)malloc(sizeof(int32_t) * c->nbasis);
+    c->sp_eigv = (double *)malloc(sizeof(double) * c->nbasis);
+    memcpy(c->orb_sym, sys->orb_sym, sizeof(int32_t) * c->nbasis);
+    memcpy(c->orb_ms, sys->orb_ms, sizeof(int32_t) * c->nbasis);
+    memcpy(c->sp_eigv, sys->sp_eigv, sizeof(double) * c->nbasis);
+    if (c->kind == HGPU_SYS_HUB_K) {
+        c->nk = sys->nkpoints;
+        c->sym_table = (int32_t *)malloc(sizeof(int32_t) * c->nk * c->nk);
+        c->inv_sym = (int32_t *)malloc(sizeof(int32_t) * c->nk);
+        memcpy(c->sym_table, sys->sym_table, sizeof(int32_t) * c->nk * c->nk);
+        memcpy(c->inv_sym, sys->inv_sym, sizeof(int32_t) * c->nk);
+        c->coulomb_k = sys->coulomb_k;
+        c->nsym = 1;
+    } else {
+        c->norb = sys->norb;
+        c->nsym = sys->nsym_pg;
+        c->h1 = (double *)malloc(sizeof(double) * c->norb * c->norb);
+        memcpy(c->h1, sys->h1, sizeof(double) * c->norb * c->norb);
+        c->nv2 = sys->nv2;
+        c->v2 = (double *)malloc(sizeof(double) * c->nv2);
+        memcpy(c->v2, sys->v2, sizeof(double) * c->nv2);
+        c->ecore = sys->ecore;
+        c->maxss = sys->max_sym_spin;
+        c->nbss = (int32_t *)malloc(sizeof(int32_t) * 2 * c->nsym);
+        memcpy(c->nbss, sys->nbasis_sym_spin, sizeof(int32_t) * 2 * c->nsym);
+        c->ssbf = (int32_t *)malloc(sizeof(int32_t) * c->nsym * 2 * c->maxss);
+        memcpy(c->ssbf, sys->sym_spin_basis_fns, sizeof(int32_t) * c->nsym * 2 * c->maxss);
+    }
+    for (int p = 0; p < c->nbasis; p++) {
+        for (int w = 0; w < MAXW; w++) c->mask[p][w] = 0;
+        for (int q = p + 1; q < c->nbasis; q++) c->mask[p][q >> 6] |= (uint64_t)1 << (q & 63);
+    }
+    c->R = cfg->nspaces > 0 ? cfg->nspaces : 1;
+    c->real_factor = cfg->real_amplitudes ? ((int64_t)1 << 31) : 1;
+    /* alloc_spawn_t: cutoff = ceiling(cutoff*real_factor); 0 for integer walkers
+     * (src/spawn_data.F90:215, src/qmc.F90:1484-1485) */
+    c->cutoff = cfg->real_amplitudes ? (int64_t)ceil(cfg->spawn_cutoff * (double)c->real_factor) : 0;
+    /* init_excit_gen (src/qmc.F90:951-972) */
+    if (cfg->pattempt_single < 0 || cfg->pattempt_double < 0) {
+        if (c->kind == HGPU_SYS_HUB_K) { c->pattempt_single = 0.0; c->pattempt_double = 1.0; }
+        else { c->pattempt_single = 0.1; c->pattempt_double = 0.9; }
+    } else {
+        c->pattempt_single = cfg->pattempt_single / (cfg->pattempt_single + cfg->pattempt_double);
+        c->pattempt_double = 1.0 - cfg->pattempt_single;
+    }
+    for (int w = 0; w < MAXW; w++) c->f0[w] = w < c->nw ? cfg->ref_det[w] : 0;
+    c->H00 = sc0(c, c->f0);
+    c->cap = cfg->walker_length > 0 ? cfg->walker_length : 1000000;
+    c->scap = cfg->spawned_walker_length > 0 ? cfg->spawned_walker_length : 1000000;
+    c->dets = (uint64_t *)calloc((size_t)(c->cap * c->nw), sizeof(uint64_t));
+    c->pops = (int64_t *)calloc((size_t)(c->cap * c->R), sizeof(int64_t));
+    c->kii = (double *)calloc((size_t)c->cap, sizeof(double));
+    c->sdets = (uint64_t *)calloc((size_t)(c->scap * c->nw), sizeof(uint64_t));
+    c->spops = (int64_t *)calloc((size_t)(c->scap * c->R), sizeof(int64_t));
+    c->sflag = (int64_t *)calloc((size_t)c->scap, sizeof(int64_t));
+    c->sord = (int64_t *)calloc((size_t)c->scap, sizeof(int64_t));
+    c->suid = (int64_t *)calloc((size_t)c->scap, sizeof(int64_t));
+    for (int s = 0; s < 2; s++) c->shift[s] = cfg->initial_shift;
+    return c;
+}
+
+void oracle_destroy(oracle_ctx *c) {
+    if (!c) return;
+    free(c->orb_sym); free(c->orb_ms); free(c->sp_eigv);
+    free(c->sym_table); free(c->inv_sym); free(c->h1); free(c->v2); free(c->nbss); free(c->ssbf);
+    free(c->dets); free(c->pops); free(c->kii);
+    free(c->sdets); free(c->spops); free(c->sflag); free(c->sord); free(c->suid);
+    free(c);
+}
+
+/* initial_distribution (src/qmc.F90:1507-1560). */
+int oracle_initial_distribution(oracle_ctx *c) {
+    c->n = 1;
+    memcpy(c->dets, c->f0, sizeof(uint64_t) * c->nw);
+    for (int s = 0; s < c->R; s++) c->pops[s] = (int64_t)llround(c->cfg.D0_population) * c->real_factor;
+    c->kii[0] = 0.0;
+    for (int s = 0; s < c->R; s++) {
+        c->nparticles_old[s] = nparticles(c, s);
+        c->shift[s] = c->cfg.initial_shift;
+        c->vary_shift[s] = 0;
+    }
+    return 0;
+}
+
+int oracle_set_walkers(oracle_ctx *c, const int64_t *states, const int64_t *pops, const double *dat, int64_t n) {
+    if (n > c->cap) return HGPU_ERR_INVALID;
+    c->n = n;
+    memcpy(c->dets, states, sizeof(uint64_t) * c->nw * n);
+    memcpy(c->pops, pops, sizeof(int64_t) * c->R * n);
+    for (int64_t i = 0; i < n; i++) c->kii[i] = dat ? dat[i] : sc0(c, &c->dets[i * c->nw]) - c->H00;
+    for (int s = 0; s < c->R; s++) c->nparticles_old[s] = nparticles(c, s);
+    return 0;
+}
+
+int64_t oracle_get_walkers(oracle_ctx *c, int64_t *states, int64_t *pops, double *dat, int64_t cap) {
+    if (cap >= c->n) {
+        if (states) memcpy(states, c->dets, sizeof(uint64_t) * c->nw * c->n);
+        if (pops) memcpy(pops, c->pops, sizeof(int64_t) * c->R * c->n);
+        if (dat) memcpy(dat, c->kii, sizeof(double) * c->n);
+    }
+    return c->n;
+}
+
+int oracle_run_cycles(oracle_ctx *c, int32_t ncycles) {
+    for (int k = 0; k < ncycles; k++) mc_cycle(c);
+    return c->error_flags ? (c->error_flags & HGPU_FLAG_SPAWN_OVERFLOW ? HGPU_ERR_SPAWN_OVERFLOW
+                                                                       : HGPU_ERR_MAIN_OVERFLOW)
+                          : 0;
+}
+
+/* communicated_energy_estimators (src/energy_evaluation.F90:425-657) and
+ * update_shift (:659-711), for one process and shift_harmonic_forcing = 0. */
+int oracle_end_report(oracle_ctx *c, hgpu_report *out) {
+    int nc = c->rep_cycles > 0 ? c->rep_cycles : 1;
+    memset(out, 0, sizeof(*out));
+    double ntot[2];
+    for (int s = 0; s < c->R; s++) {
+        out->proj_energy[s] = c->acc_proj[s] / (double)nc;
+        out->D0_population[s] = c->acc_d0[s] / (double)nc;
+        ntot[s] = nparticles(c, s);
+    }
+    for (int s = 0; s < c->R; s++) {
+        if (c->vary_shift[s]) {
+            c->shift[s] = c->shift[s] - log(ntot[s] / c->nparticles_old[s]) * c->cfg.shift_damping /
+                                            (1.0 * c->cfg.tau * (double)nc);
+        }
+    }
+    for (int s = 0; s < c->R; s++) c->nparticles_old[s] = ntot[s];
+    for (int s = 0; s < c->R; s++) {
+        if (!c->vary_shift[s] && ntot[s] > c->cfg.target_particles) {
+            c->vary_shift[s] = 1;
+            if (c->cfg.vary_shift_from_proje) c->shift[s] = out->proj_energy[s] / out->D0_population[s];
+            else c->shift[s] = c->cfg.vary_shift_from;
+        }
+    }
+    for (int s = 0; s < c->R; s++) {
+        out->shift[s] = c->shift[s];
+        out->nparticles[s] = ntot[s];
+        out->vary_shift[s] = c->vary_shift[s];
+    }
+    out->iteration = c->iter;
+    out->nstates = c->n;
+    out->nspawn_events = c->last_nspawn_events;
+    out->rspawn = c->acc_rspawn / (double)nc;
+    out->nattempts = c->rep_attempts;
+    out->nspawned = c->rep_spawned;
+    out->error_flags = c->error_flags;
+    for (int s = 0; s < 2; s++) { c->acc_proj[s] = 0.0; c->acc_d0[s] = 0.0; }
+    c->acc_rspawn = 0.0;
+    c->rep_attempts = 0;
+    c->rep_spawned = 0;
+    c->rep_cycles = 0;
+    return c->error_flags ? HGPU_ERR_SPAWN_OVERFLOW : 0;
+}
+
+int oracle_get_state(oracle_ctx *c, hgpu_state *out) {
+    memset(out, 0, sizeof(*out));
+    out->iteration = c->iter;
+    for (int s = 0; s < 2; s++) {
+        out->shift[s] = c->shift[s];
+        out->vary_shift[s] = c->vary_shift[s];
+        out->nparticles_old[s] = c->nparticles_old[s];
+    }
+    out->tau = c->cfg.tau;
+    out->seed = c->cfg.seed;
+    return 0;
+}
+
+int oracle_set_state(oracle_ctx *c, const hgpu_state *in) {
+    c->iter = in->iteration;
+    for (int s = 0; s < 2; s++) {
+        c->shift[s] = in->shift[s];
+        c->vary_shift[s] = in->vary_shift[s];
+        c->nparticles_old[s] = in->nparticles_old[s];
+    }
+    return 0;
+}
+
+int oracle_eval_excitations(oracle_ctx *c, const int64_t *parents, const int64_t *parent_pops, int64_t n,
+                            int64_t iteration, int32_t *orbs, double *pgen, double *hmatel, int32_t *allowed,
+                            int64_t *nspawn) {
+    for (int64_t i = 0; i < n; i++) {
+        const uint64_t *f = (const uint64_t *)&parents[i * c->nw];
+        det_info d;
+        decode_any(c, f, &d);
+        rstream rs;
+        rs_init(&rs, (uint64_t)c->cfg.seed, P_SPAWN, 0, (uint64_t)i, 0, (uint64_t)iteration);
+        attempt_t at;
+        attempt(c, &rs, f, &d, parent_pops[i], &at, 1);
+        orbs[4 * i + 0] = at.e.from[0];
+        orbs[4 * i + 1] = at.e.nexcit == 2 ? at.e.from[1] : -1;
+        orbs[4 * i + 2] = at.e.to[0];
+        orbs[4 * i + 3] = at.e.nexcit == 2 ? at.e.to[1] : -1;
+        pgen[i] = at.pgen;
+        hmatel[i] = at.hmatel;
+        allowed[i] = at.allowed;
+        nspawn[i] = at.nspawn;
+    }
+    return 0;
+}
+
+int oracle_annihilate_fixed(oracle_ctx *c, const int64_t *sdata, int64_t n, int64_t iteration) {
+    int el = c->nw + c->R + 1;
+    if (n > c->scap) return HGPU_ERR_SPAWN_OVERFLOW;
+    c->sn = 0;
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t *e = &sdata[k * el];
+        memcpy(&c->sdets[k * c->nw], e, sizeof(uint64_t) * c->nw);
+        for (int s = 0; s < c->R; s++) c->spops[k * c->R + s] = e[c->nw + s];
+        c->sflag[k] = c->cfg.initiator_approx ? e[c->nw + c->R] : 0;
+        c->sord[k] = k;
+    }
+    c->sn = n;
+    int64_t save = c->iter;
+    c->iter = iteration;
+    direct_annihilation(c);
+    c->iter = save;
+    return c->error_flags & HGPU_FLAG_MAIN_OVERFLOW ? HGPU_ERR_MAIN_OVERFLOW : 0;
+}
+
+double oracle_hmatel(oracle_ctx *c, const int64_t *f1, const int64_t *f2) {
+    return hmatel_any(c, (const uint64_t *)f1, (const uint64_t *)f2);
+}
+
+double oracle_sc0(oracle_ctx *c, const int64_t *f) { return sc0(c, (const uint64_t *)f); }
+
+double oracle_pgen(oracle_ctx *c, const int64_t *fi, const int32_t *orbs) {
+    const uint64_t *f = (const uint64_t *)fi;
+    det_info d;
+    decode_any(c, f, &d);
+    if (c->kind == HGPU_SYS_HUB_K) {
+        int ij_sym = c->sym_table[kidx(orbs[0]) * c->nk + kidx(orbs[1])];
+        if (c->cfg.excit_gen == HGPU_EXCIT_GEN_NO_RENORM)
+            return 1.0 / (double)(c->nalpha * c->nbeta * c->nvirt_alpha);
+        return calc_pgen_hub_k(c, ij_sym, f, &d);
+    }
+    int renorm = c->cfg.excit_gen == HGPU_EXCIT_GEN_RENORM;
+    if (orbs[1] < 0) {
+        return c->pattempt_single *
+               (renorm ? calc_pgen_single_mol(c, &d, orbs[2]) : calc_pgen_single_mol_no_renorm(c, orbs[2]));
+    }
+    int ij_sym = cross(c, c->orb_sym[orbs[0]], c->orb_sym[orbs[1]]);
+    int spin = c->orb_ms[orbs[0]] + c->orb_ms[orbs[1]];
+    double pij = 2.0 / (double)(c->nel * (c->nel - 1));
+    if (renorm) return c->pattempt_double * pij * calc_pgen_double_mol(c, ij_sym, orbs[2], orbs[3], spin, &d);
+    return c->pattempt_double * pij * calc_pgen_double_mol_no_renorm(c, orbs[2], orbs[3], spin);
+}
+
+int64_t oracle_total_attempts(oracle_ctx *c) { return c->total_attempts; }

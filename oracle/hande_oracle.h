@@ -1,0 +1,59 @@
+/*
+ * hande_oracle.h -- CPU restatement of HANDE's FCIQMC cycle.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the GPU engine is checked
+ * against: only tests/, __graft_entry__.smoke() and bench.py's CPU baseline
+ * load it.  The product library (libhande_gpu.so) never links or calls it.
+ *
+ * The reference (HANDE, Fortran) cannot be compiled in this environment, so
+ * the oracle restates its algorithm function by function, each citing the
+ * reference file:line it follows.  It is pinned against the FCI energies of
+ * the reference's own test suite (tests/golden/), which fix the Hamiltonian
+ * (Slater-Condon rules, integral indexing, k-space symmetry tables).
+ *
+ * The random numbers come from the same counter-based Philox4x32-10 streams
+ * as the GPU engine (keyed by iteration, determinant index, attempt, purpose),
+ * not from HANDE's dSFMT; stream-level parity with HANDE itself is therefore
+ * unpinned, and whole runs are compared with the reference statistically.
+ */
+#ifndef HANDE_ORACLE_H
+#define HANDE_ORACLE_H
+
+#include <stdint.h>
+#include "../include/hande_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_ctx oracle_ctx;
+
+oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys);
+void oracle_destroy(oracle_ctx *c);
+int oracle_initial_distribution(oracle_ctx *c);
+int oracle_set_walkers(oracle_ctx *c, const int64_t *states, const int64_t *pops, const double *dat,
+                       int64_t n);
+int64_t oracle_get_walkers(oracle_ctx *c, int64_t *states, int64_t *pops, double *dat, int64_t cap);
+int oracle_run_cycles(oracle_ctx *c, int32_t ncycles);
+int oracle_end_report(oracle_ctx *c, hgpu_report *out);
+int oracle_get_state(oracle_ctx *c, hgpu_state *out);
+int oracle_set_state(oracle_ctx *c, const hgpu_state *in);
+int oracle_eval_excitations(oracle_ctx *c, const int64_t *parents, const int64_t *parent_pops, int64_t n,
+                            int64_t iteration, int32_t *orbs, double *pgen, double *hmatel,
+                            int32_t *allowed, int64_t *nspawn);
+int oracle_annihilate_fixed(oracle_ctx *c, const int64_t *sdata, int64_t n, int64_t iteration);
+/* <D1|H|D2> (get_hmatel_hub_k / get_hmatel_mol) and <D|H|D> (sc0_ptr). */
+double oracle_hmatel(oracle_ctx *c, const int64_t *f1, const int64_t *f2);
+double oracle_sc0(oracle_ctx *c, const int64_t *f);
+/* pgen of an explicit excitation (calc_pgen_* of the configured generator) */
+double oracle_pgen(oracle_ctx *c, const int64_t *f, const int32_t *orbs);
+/* Counters of the last cycles (spawn attempts etc.). */
+int64_t oracle_total_attempts(oracle_ctx *c);
+/* Philox4x32-10 uniform, for cross-checking the device generator. */
+double oracle_uniform(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, int which);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

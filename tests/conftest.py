@@ -1,0 +1,16 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the engine through the C ABI)")
+    config.addinivalue_line("markers", "slow: longer CPU-side statistical runs")
+
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")

@@ -1,0 +1,78 @@
+"""Pin the oracle against the reference's own FCI energies (test_suite/fci/*),
+which fixes the Hamiltonian both the oracle and the GPU engine use."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from hande_gb300 import systems
+from oracle import fci
+from oracle.pyoracle import Oracle
+from tests.conftest import GOLDEN
+
+CASES = json.load(open(os.path.join(GOLDEN, "fci_energies.json")))
+
+
+def _system(case):
+    p = case["params"]
+    if case["system"] == "hubbard_k":
+        return systems.hubbard_k(p["lattice"], p["electrons"], U=p.get("U", 1.0), t=p.get("t", 1.0),
+                                 ms=p.get("ms", 0), twist=p.get("twist"))
+    return systems.read_in(os.path.join(GOLDEN, case["int_file"]), nel=p.get("nel"), ms=p.get("ms"))
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_fci_energies(case):
+    s = _system(case)
+    o = Oracle(s, tau=0.01)
+    p = case["params"]
+    if case["system"] == "hubbard_k":
+        sym = p["sym"] - 1  # HANDE k-point labels are 1-based
+    else:
+        sym = p.get("sym", fci.det_symmetry(s, s.aufbau_occ()))
+    ref = np.array(case["energies"])
+    if p.get("diagonal_only"):
+        dets = fci.enumerate_dets(s, sym)
+        w = np.array(sorted(o.sc0(d) for d in dets)[: len(ref)])
+    else:
+        w, _ = fci.lowest(o, s, sym, nroots=len(ref))
+    # benchmark outputs print 12 decimals
+    assert np.max(np.abs(w - ref)) < 2e-11
+
+
+def test_hubbard_4x4_basis():
+    """Config-1 lattice: 16 k-points, closed-shell aufbau reference (10 e)."""
+    s = systems.hubbard_k([[4, 0], [0, 4]], 10, U=4.0, t=1.0)
+    assert s.nbasis == 32 and s.nwords == 1
+    assert abs(s.coulomb_k - 0.25) < 1e-15
+    e = s.sp_eigv[::2]
+    assert abs(e[0] + 4.0) < 1e-12 and np.allclose(e[1:5], -2.0)
+    assert e[5] > e[4] + 1e-6  # closed shell: 5th and 6th levels not degenerate
+    # sym table: k + (-k) = gamma
+    gamma = int(np.where(np.all(s.kpoints == 0, axis=1))[0][0])
+    for k in range(s.nkpoints):
+        assert s.sym_table[k, s.inv_sym[k]] == gamma
+
+
+def test_fcidump_roundtrip(tmp_path):
+    h, v2 = systems.synthetic_integrals(6, seed=3)
+    path = str(tmp_path / "FCIDUMP")
+    systems.write_fcidump(path, h, v2, nel=4, sp_eigv=np.diag(h))
+    s = systems.read_in(path)
+    assert s.extra["fcidump_rank"] == list(range(6))
+    np.testing.assert_array_equal(s.h1, h)
+    np.testing.assert_array_equal(s.v2, v2)
+
+
+def test_synthetic_symmetric_psd():
+    h, v2 = systems.synthetic_integrals(5, seed=11)
+    M = 5
+    npair = M * (M + 1) // 2
+    V = np.zeros((npair, npair))
+    li, lj = np.tril_indices(npair)
+    V[li, lj] = v2
+    V[lj, li] = v2
+    assert np.min(np.linalg.eigvalsh(V)) > -1e-10
+    assert np.allclose(h, h.T)

@@ -1,0 +1,122 @@
+"""The fciqmc calculation driver: the report loop of do_fciqmc
+(src/fciqmc.f90:276-470) around the GPU engine, with the option names of
+HANDE's Lua interface (``qmc``/``fciqmc`` tables, src/lua_hande_calc.f90:304,
+:1318-1331, :1549).
+
+Per report the engine runs mc_cycles cycles on the device, then the host closes
+the report (estimators, shift update) and prints a line with the columns of
+write_qmc_report (src/qmc_io.f90:23-136)."""
+
+from __future__ import annotations
+
+import os
+import sys
+import time
+from typing import Optional
+
+from ._abi import PREC_FP64, PREC_MIXED, make_config
+from .engine import Engine
+from .systems import System
+
+QMC_KEYS = {
+    "tau", "init_pop", "mc_cycles", "nreports", "state_size", "spawned_state_size", "rng_seed",
+    "target_population", "real_amplitudes", "spawn_cutoff", "excit_gen", "pattempt_single",
+    "pattempt_double", "initiator", "initiator_threshold", "shift_damping", "vary_shift_from",
+    "initial_shift", "precision",
+}
+FCIQMC_KEYS = {"replica_tricks"}
+
+
+def _opts(qmc: dict, fciqmc_opts: Optional[dict]):
+    unknown = set(qmc) - QMC_KEYS
+    if unknown:
+        raise ValueError("unknown qmc option(s): %s" % ", ".join(sorted(unknown)))
+    fo = fciqmc_opts or {}
+    unknown = set(fo) - FCIQMC_KEYS
+    if unknown:
+        raise ValueError("unknown fciqmc option(s): %s" % ", ".join(sorted(unknown)))
+    for key in ("tau", "init_pop", "mc_cycles", "nreports"):
+        if key not in qmc:
+            raise ValueError("qmc.%s is required" % key)
+    return fo
+
+
+def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] = None, reference=None):
+    fo = _opts(qmc, fciqmc_opts)
+    vsf = qmc.get("vary_shift_from", 0.0)
+    prec = qmc.get("precision", "fp64")
+    return make_config(
+        system, tau=qmc["tau"], ncycles=int(qmc["mc_cycles"]), seed=int(qmc.get("rng_seed", 7)),
+        init_pop=float(qmc["init_pop"]), target_population=float(qmc.get("target_population", 1e300)),
+        shift_damping=float(qmc.get("shift_damping", 0.05)), initial_shift=float(qmc.get("initial_shift", 0.0)),
+        vary_shift_from=0.0 if vsf == "proje" else float(vsf), vary_shift_from_proje=(vsf == "proje"),
+        real_amplitudes=bool(qmc.get("real_amplitudes", False)), spawn_cutoff=float(qmc.get("spawn_cutoff", 0.01)),
+        excit_gen=qmc.get("excit_gen", "renorm"), pattempt_single=float(qmc.get("pattempt_single", -1.0)),
+        pattempt_double=float(qmc.get("pattempt_double", -1.0)), initiator=bool(qmc.get("initiator", False)),
+        initiator_threshold=float(qmc.get("initiator_threshold", 3.0)),
+        nspaces=2 if fo.get("replica_tricks") else 1,
+        precision=PREC_MIXED if prec in ("mixed", "fp32", PREC_MIXED) else PREC_FP64,
+        state_size=int(qmc.get("state_size", -1000)), spawned_state_size=int(qmc.get("spawned_state_size", -500)),
+        reference=reference)
+
+
+HEADER = (" iterations      Shift        \\sum H_0j N_j       N_0          # H psips    # states  "
+          "# spawn_events  R_spawn   time")
+
+
+def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None, out=None,
+           comm_file: str = "HANDE.COMM", verbose: bool = True) -> dict:
+    """Run FCIQMC on the GPU.  Returns {'reports': [...], 'engine': Engine}.
+
+    A file named ``comm_file`` containing ``softexit = true`` in the working
+    directory ends the calculation after the current report (calc_interact,
+    src/interact.F90:11-188)."""
+    cfg = config_from_options(sys, qmc, fciqmc, reference)
+    eng = Engine(sys, cfg)
+    eng.initial_distribution()
+    stream = out if out is not None else sys_stdout()
+    if verbose:
+        stream.write(HEADER + "\n")
+    reports = []
+    t0 = time.time()
+    for ireport in range(int(qmc["nreports"])):
+        rep = eng.run_report()
+        t1 = time.time()
+        row = rep.as_dict(eng.R)
+        row["time"] = t1 - t0
+        t0 = t1
+        reports.append(row)
+        if verbose:
+            stream.write(" %10d  %14.8f  %16.8f  %12.4f  %14.4f  %10d  %10d  %8.4f  %7.4f\n" % (
+                row["iterations"], row["Shift"][0], row["\\sum H_0j N_j"][0], row["N_0"][0], row["# H psips"][0],
+                row["# states"], row["# spawn_events"], row["R_spawn"], row["time"]))
+        if row["error_flags"]:
+            if verbose:
+                stream.write("# Error: walker list full (flags %d); exiting at the end of this report.\n"
+                             % row["error_flags"])
+            break
+        if _softexit(comm_file):
+            if verbose:
+                stream.write("# Soft exit requested through %s.\n" % comm_file)
+            break
+    return {"reports": reports, "engine": eng}
+
+
+def _softexit(path: str) -> bool:
+    if not os.path.exists(path):
+        return False
+    try:
+        txt = open(path).read().lower().replace(" ", "")
+    except OSError:
+        return False
+    if "softexit=true" in txt:
+        try:
+            os.remove(path)
+        except OSError:
+            pass
+        return True
+    return False
+
+
+def sys_stdout():
+    return sys.stdout

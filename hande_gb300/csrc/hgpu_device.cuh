@@ -1,0 +1,896 @@
+// hgpu_device.cuh -- device-side system description, RNG streams, determinant
+// bit operations, excitation generators and Slater-Condon rules of the GB300
+// FCIQMC engine.
+//
+// Orbitals are 0-based spin orbitals: p is bit p%64 of word p/64, even p alpha.
+// All FP64 arithmetic is written in the operation order of the HANDE
+// expressions it implements; the library is built with -fmad=false so no
+// multiply-add is contracted and the results round exactly as written.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/hande_gpu.h"
+
+namespace hgpu {
+
+constexpr int kMaxWords = HGPU_MAX_WORDS;
+// Upper bound on the redraws of a rejection loop.  Acceptance is at least
+// 1/nbasis per draw, so the bound is never reached in a correct run; it only
+// guarantees that a kernel always terminates (the attempt is then dropped).
+constexpr int kMaxRedraw = 1 << 16;
+constexpr int kMaxSym = 8;  // D2h subgroups: at most 8 irreps
+
+// RNG stream purposes (counter word 3, bits 28..31).
+enum Purpose : uint32_t { P_NATTEMPT = 1, P_SPAWN = 2, P_DEATH = 3, P_ROUND_MAIN = 4, P_ROUND_SPAWN = 5 };
+
+// Everything the kernels need to know about the system and the calculation.
+// Lives in device global memory; small tables are staged to shared memory by
+// the kernels that gather from them.
+struct DevSys {
+    int kind, nbasis, nel, nalpha, nbeta, nw;
+    int nvirt_alpha, nvirt_beta, nvirt;
+    int nspaces;
+    int excit_gen;
+    int initiator;
+    int real_amplitudes;
+    int precision;
+    int64_t real_factor;
+    int64_t cutoff;  // encoded spawn cutoff
+    double tau;
+    double pattempt_single, pattempt_double;
+    double initiator_pop;
+    double H00;
+    uint64_t seed;
+    uint64_t f0[kMaxWords];
+    // hub_k
+    int nk;
+    double coulomb_k;
+    const uint8_t *sym_table;  // nk*nk
+    const uint8_t *inv_sym;    // nk
+    const double *sp_eigv;     // nbasis
+    // molecular
+    int norb, nsym;
+    double ecore;
+    const double *h1;   // norb*norb
+    const double *v2;   // packed (ia|jb)
+    const float *h1f;   // FP32 copies for the mixed-precision spawning path
+    const float *v2f;
+    // per-irrep, per-spin orbital masks: symmask[(sym*2+ims)*nw + w]
+    uint64_t symmask[kMaxSym * 2 * kMaxWords];
+    int nbss[kMaxSym * 2];  // orbitals per (sym, ims): index sym*2+ims
+    uint8_t orbsym[64 * kMaxWords];  // irrep of each spin orbital
+};
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11): 10 rounds of the published round function and Weyl key
+// schedule.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t lo0 = 0xD2511F53u * c[0];
+        uint32_t hi0 = __umulhi(0xD2511F53u, c[0]);
+        uint32_t lo1 = 0xCD9E8D57u * c[2];
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]);
+        uint32_t n0 = hi1 ^ c[1] ^ k0;
+        uint32_t n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
+    uint64_t x = ((uint64_t)hi << 32) | lo;
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// Stream of uniforms in [0,1) for one (purpose, space, index, sub, iteration):
+// counter = (index, sub, iteration, purpose<<28 | space<<26 | block).
+struct RStream {
+    uint32_t c0, c1, c2, c3;
+    uint32_t k0, k1;
+    uint32_t block;
+    double buf;
+    bool have;
+
+    __device__ __forceinline__ void init(uint64_t seed, uint32_t purpose, uint32_t space, uint64_t idx,
+                                         uint64_t sub, uint64_t iter) {
+        k0 = (uint32_t)seed;
+        k1 = (uint32_t)(seed >> 32);
+        c0 = (uint32_t)idx;
+        c1 = (uint32_t)sub;
+        c2 = (uint32_t)iter;
+        c3 = (purpose << 28) | (space << 26);
+        block = 0;
+        have = false;
+    }
+    // get_rand_close_open
+    __device__ __forceinline__ double next() {
+        if (have) {
+            have = false;
+            return buf;
+        }
+        uint32_t c[4] = {c0, c1, c2, c3 | block};
+        philox(c, k0, k1);
+        block++;
+        buf = u53(c[2], c[3]);
+        have = true;
+        return u53(c[0], c[1]);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Determinant bit operations
+// ---------------------------------------------------------------------------
+template <int W>
+struct Det {
+    uint64_t w[W];
+};
+
+template <int W>
+__device__ __forceinline__ bool tbit(const Det<W> &f, int p) {
+    return (f.w[p >> 6] >> (p & 63)) & 1ull;
+}
+
+template <int W>
+__device__ __forceinline__ int popc(const Det<W> &f) {
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < W; i++) n += __popcll(f.w[i]);
+    return n;
+}
+
+// Unsigned comparison with the last word most significant (bit_str_cmp).
+template <int W>
+__device__ __forceinline__ bool det_less(const Det<W> &a, const Det<W> &b) {
+#pragma unroll
+    for (int i = W - 1; i >= 0; i--) {
+        if (a.w[i] != b.w[i]) return a.w[i] < b.w[i];
+    }
+    return false;
+}
+
+template <int W>
+__device__ __forceinline__ bool det_eq(const Det<W> &a, const Det<W> &b) {
+    bool e = true;
+#pragma unroll
+    for (int i = 0; i < W; i++) e = e && (a.w[i] == b.w[i]);
+    return e;
+}
+
+// Position of the r-th (0-based) set bit of x; x has more than r set bits.
+__device__ __forceinline__ int select64(uint64_t x, int r) {
+    int base = 0;
+    uint32_t lo = (uint32_t)x;
+    int c = __popc(lo);
+    uint32_t v;
+    if (r >= c) {
+        r -= c;
+        v = (uint32_t)(x >> 32);
+        base = 32;
+    } else {
+        v = lo;
+    }
+    uint32_t l16 = v & 0xFFFFu;
+    c = __popc(l16);
+    if (r >= c) {
+        r -= c;
+        v >>= 16;
+        base += 16;
+    }
+    uint32_t l8 = v & 0xFFu;
+    c = __popc(l8);
+    if (r >= c) {
+        r -= c;
+        v >>= 8;
+        base += 8;
+    }
+    // at most 8 candidate bits left
+    v &= 0xFFu;
+    for (;;) {
+        int t = __ffs(v) - 1;
+        if (r == 0) return base + t;
+        v &= v - 1;
+        r--;
+    }
+}
+
+// r-th set bit of a W-word mask m (occupied-orbital list occ(r), etc.).
+template <int W>
+__device__ __forceinline__ int select_det(const uint64_t *m, int r) {
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        int c = __popcll(m[i]);
+        if (r < c) return 64 * i + select64(m[i], r);
+        r -= c;
+    }
+    return -1;
+}
+
+constexpr uint64_t kAlpha = 0x5555555555555555ull;  // even bits
+constexpr uint64_t kBeta = 0xAAAAAAAAAAAAAAAAull;
+
+// Orbitals strictly above p (excit_mask(:, p), src/excitations.F90:25-70), word i.
+__device__ __forceinline__ uint64_t above_mask(int p, int i) {
+    int wp = p >> 6;
+    if (i < wp) return 0ull;
+    if (i > wp) return ~0ull;
+    int b = p & 63;
+    return b == 63 ? 0ull : (~0ull << (b + 1));
+}
+
+// find_excitation_permutation1 (src/excitations.F90:247-280).
+template <int W>
+__device__ __forceinline__ bool perm1(const Det<W> &f, int i, int a) {
+    int perm = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) perm += __popcll(f.w[k] & (above_mask(i, k) ^ above_mask(a, k)));
+    if (i > a) perm -= 1;
+    return (perm & 1) != 0;
+}
+
+// find_excitation_permutation2 (src/excitations.F90:282-330).
+template <int W>
+__device__ __forceinline__ bool perm2(const Det<W> &f, int i, int j, int a, int b) {
+    int perm = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        uint64_t ia = above_mask(i, k) ^ above_mask(a, k);
+        uint64_t jb = above_mask(j, k) ^ above_mask(b, k);
+        perm += __popcll((f.w[k] & ia) ^ (f.w[k] & jb));
+    }
+    if (i > a) perm += 1;
+    if (i > b) perm += 1;
+    if (j > b || j < a) perm += 1;
+    return (perm & 1) != 0;
+}
+
+// get_excitation (src/excitations.F90:75-200) for D (f1) against the reference
+// (f2): from = in f1 not in f2, to = in f2 not in f1, both ascending; perm is
+// the parity of sum(shift - iel + iexcit) over the excited orbitals, which
+// equals the parity computed below from the number of electrons of each
+// determinant below each excited orbital.
+struct Excit {
+    int nexcit;
+    int from[2], to[2];
+    bool perm;
+};
+
+template <int W>
+__device__ __forceinline__ Excit get_excitation(const Det<W> &f1, const Det<W> &f2, int nel) {
+    Excit e;
+    e.nexcit = 0;
+    e.from[0] = e.from[1] = e.to[0] = e.to[1] = -1;
+    e.perm = false;
+    int diff = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) diff += __popcll(f1.w[k] ^ f2.w[k]);
+    if (diff == 0) return e;
+    e.nexcit = diff >> 1;
+    if (e.nexcit > 2) return e;
+    int shift = nel - e.nexcit;
+    int n1 = 0, n2 = 0;
+    int perm = 0;
+    // Each excited orbital p in f1 only: iel1 = (# f1 electrons <= p), iexcit1 = its rank.
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        uint64_t d1 = f1.w[k] & ~f2.w[k];
+        uint64_t d2 = f2.w[k] & ~f1.w[k];
+        while (d1) {
+            int b = __ffsll((long long)d1) - 1;
+            d1 &= d1 - 1;
+            uint64_t below = b == 63 ? ~0ull : ((1ull << (b + 1)) - 1);
+            int iel1 = 0;
+#pragma unroll
+            for (int q = 0; q < W; q++) iel1 += q < k ? __popcll(f1.w[q]) : (q == k ? __popcll(f1.w[q] & below) : 0);
+            e.from[n1] = 64 * k + b;
+            n1++;
+            perm += shift - iel1 + n1;
+        }
+        while (d2) {
+            int b = __ffsll((long long)d2) - 1;
+            d2 &= d2 - 1;
+            uint64_t below = b == 63 ? ~0ull : ((1ull << (b + 1)) - 1);
+            int iel2 = 0;
+#pragma unroll
+            for (int q = 0; q < W; q++) iel2 += q < k ? __popcll(f2.w[q]) : (q == k ? __popcll(f2.w[q] & below) : 0);
+            e.to[n2] = 64 * k + b;
+            n2++;
+            perm += shift - iel2 + n2;
+        }
+    }
+    e.perm = (perm & 1) != 0;
+    return e;
+}
+
+// ---------------------------------------------------------------------------
+// Integrals
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t tri0(int64_t i, int64_t j) { return i * (i + 1) / 2 + j; }
+
+// two_body_int_indx (src/molecular_integrals.F90:736-845), RHF, spin orbitals.
+__device__ __forceinline__ int64_t v2_index(int i, int j, int a, int b) {
+    int si = i >> 1, sj = j >> 1, sa = a >> 1, sb = b >> 1;
+    int64_t ia = si >= sa ? tri0(si, sa) : tri0(sa, si);
+    int64_t jb = sj >= sb ? tri0(sj, sb) : tri0(sb, sj);
+    return ia >= jb ? tri0(ia, jb) : tri0(jb, ia);
+}
+
+template <typename Real>
+struct Ints;
+
+template <>
+struct Ints<double> {
+    __device__ __forceinline__ static double v2(const DevSys &s, int i, int j, int a, int b) {
+        return __ldg(&s.v2[v2_index(i, j, a, b)]);
+    }
+    __device__ __forceinline__ static double h1(const DevSys &s, int i, int a) {
+        return __ldg(&s.h1[(i >> 1) * s.norb + (a >> 1)]);
+    }
+};
+
+template <>
+struct Ints<float> {
+    __device__ __forceinline__ static float v2(const DevSys &s, int i, int j, int a, int b) {
+        return __ldg(&s.v2f[v2_index(i, j, a, b)]);
+    }
+    __device__ __forceinline__ static float h1(const DevSys &s, int i, int a) {
+        return __ldg(&s.h1f[(i >> 1) * s.norb + (a >> 1)]);
+    }
+};
+
+__device__ __forceinline__ int ms_of(int p) { return (p & 1) ? -1 : 1; }
+__device__ __forceinline__ int ims_of(int p) { return (p & 1) ? 0 : 1; }  // 0 beta, 1 alpha
+
+// slater_condon0_mol (src/hamiltonian_molecular.f90:73-139), FP64.
+template <int W>
+__device__ double sc0_mol(const DevSys &s, const Det<W> &f) {
+    double h = s.ecore;
+    int occ[64 * W];
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        uint64_t x = f.w[k];
+        while (x) {
+            occ[n++] = 64 * k + __ffsll((long long)x) - 1;
+            x &= x - 1;
+        }
+    }
+    for (int iel = 0; iel < n; iel++) {
+        int i = occ[iel];
+        h = h + Ints<double>::h1(s, i, i);
+        for (int jel = iel + 1; jel < n; jel++) {
+            int j = occ[jel];
+            h = h + Ints<double>::v2(s, i, j, i, j);
+            if (((i ^ j) & 1) == 0) h = h - Ints<double>::v2(s, i, j, j, i);
+        }
+    }
+    return h;
+}
+
+// slater_condon0_hub_k (src/hamiltonian_hub_k.f90:91-132).
+template <int W>
+__device__ double sc0_hub_k(const DevSys &s, const Det<W> &f) {
+    double h = (double)(s.nalpha * s.nbeta) * s.coulomb_k;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        uint64_t x = f.w[k];
+        while (x) {
+            int p = 64 * k + __ffsll((long long)x) - 1;
+            x &= x - 1;
+            h = h + __ldg(&s.sp_eigv[p]);
+        }
+    }
+    return h;
+}
+
+template <int W>
+__device__ __forceinline__ double sc0(const DevSys &s, const Det<W> &f) {
+    return s.kind == HGPU_SYS_HUB_K ? sc0_hub_k<W>(s, f) : sc0_mol<W>(s, f);
+}
+
+// slater_condon1_mol_excit (src/hamiltonian_molecular.f90:199-259).
+template <int W, typename Real>
+__device__ Real sc1_mol(const DevSys &s, const Det<W> &f, int i, int a, bool perm) {
+    Real h = Ints<Real>::h1(s, i, a);
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        uint64_t x = f.w[k];
+        while (x) {
+            int q = 64 * k + __ffsll((long long)x) - 1;
+            x &= x - 1;
+            if (q != i) {
+                h = h + Ints<Real>::v2(s, i, q, a, q);
+                if (((q ^ i) & 1) == 0) h = h - Ints<Real>::v2(s, i, q, q, a);
+            }
+        }
+    }
+    if (perm) h = -h;
+    return h;
+}
+
+// slater_condon2_mol_excit (src/hamiltonian_molecular.f90:300-346).
+template <typename Real>
+__device__ __forceinline__ Real sc2_mol(const DevSys &s, int i, int j, int a, int b, bool perm) {
+    Real h = (Real)0;
+    if (((i ^ a) & 1) == 0) h = Ints<Real>::v2(s, i, j, a, b);
+    if (((i ^ b) & 1) == 0) h = h - Ints<Real>::v2(s, i, j, b, a);
+    if (perm) h = -h;
+    return h;
+}
+
+// ---------------------------------------------------------------------------
+// Hubbard model in momentum space
+// ---------------------------------------------------------------------------
+struct HubTables {
+    const uint8_t *sym;  // nk*nk (shared memory)
+    const uint8_t *inv;  // nk
+    int nk;
+};
+
+// get_two_e_int_hub_k (src/hubbard_k.f90:11-55) with momentum_conserved (:57-84).
+__device__ __forceinline__ double two_e_int_hub_k(const DevSys &s, const HubTables &t, int p1, int p2, int p3,
+                                                  int p4) {
+    bool s12 = ((p1 ^ p2) & 1) == 0;
+    bool s34 = ((p3 ^ p4) & 1) == 0;
+    if (!s12 && (s12 == s34)) {
+        int dk = t.sym[(p1 >> 1) * t.nk + (p2 >> 1)];
+        dk = t.sym[dk * t.nk + t.inv[p3 >> 1]];
+        if (dk == (p4 >> 1)) return ((p1 ^ p3) & 1) == 0 ? s.coulomb_k : -s.coulomb_k;
+    }
+    return 0.0;
+}
+
+// beta partner of alpha orbital a for total momentum ij_sym (find_ab_hub_k).
+__device__ __forceinline__ int hub_partner(const HubTables &t, int ij_sym, int a) {
+    return 2 * t.sym[ij_sym * t.nk + t.inv[a >> 1]] + 1;
+}
+
+// Result of one spawning attempt.
+struct Attempt {
+    int nexcit;
+    int from[2], to[2];
+    double pgen, hmatel;
+    bool allowed;
+    int64_t nspawn;
+};
+
+// stochastic_round_spawned_particle (src/stoch_utils.f90:87-136).
+__device__ __forceinline__ int64_t round_spawned(int64_t cutoff, double pspawn, RStream &rs) {
+    int64_t nspawn;
+    if (pspawn < (double)cutoff) {
+        nspawn = (pspawn > rs.next() * (double)cutoff) ? cutoff : 0;
+    } else {
+        nspawn = (int64_t)pspawn;
+        double padd = pspawn - (double)nspawn;
+        if (padd > rs.next()) nspawn = nspawn + 1;
+    }
+    return nspawn;
+}
+
+__device__ __forceinline__ int64_t isign64(int64_t a, int64_t b) {
+    int64_t m = a < 0 ? -a : a;
+    return b >= 0 ? m : -m;
+}
+
+// set_child_sign (src/spawning.F90:680-709).
+__device__ __forceinline__ int64_t child_sign(double hmatel, int64_t parent, int64_t nspawn) {
+    return hmatel > 0.0 ? -isign64(nspawn, parent) : isign64(nspawn, parent);
+}
+
+// spawn_lattice_split_gen (src/spawning.F90:215-315) with gen_excit_init_hub_k /
+// gen_excit_finalise_hub_k (src/excit_gen_hub_k.f90:29-156) or the no_renorm
+// pair (:158-277).  complete: finish the excitation even when nothing spawns
+// (parity evaluation only).
+template <int W>
+__device__ void attempt_hub_k(const DevSys &s, const HubTables &t, RStream &rs, const Det<W> &f, int64_t parent,
+                              bool complete, Attempt &out) {
+    out.nexcit = 2;
+    out.to[0] = out.to[1] = -1;
+    // occupied alpha / beta and unoccupied alpha masks
+    uint64_t oa[W], ob[W], ua[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        uint64_t valid = (64 * (k + 1) <= s.nbasis) ? ~0ull : ((1ull << (s.nbasis - 64 * k)) - 1);
+        oa[k] = f.w[k] & kAlpha;
+        ob[k] = f.w[k] & kBeta;
+        ua[k] = ~f.w[k] & kAlpha & valid;
+    }
+    // choose_ij_hub_k (src/excit_gen_hub_k.f90:469-532)
+    double r = rs.next();
+    int ind = (int)(r * (double)s.nalpha * (double)s.nbeta) + 1;
+    int ii = (int)(((double)ind - 1.0) / (double)s.nbeta) + 1;
+    int jj = ind - (ii - 1) * s.nbeta;
+    int i = select_det<W>(oa, ii - 1);
+    int j = select_det<W>(ob, jj - 1);
+    int ij_sym = t.sym[(i >> 1) * t.nk + (j >> 1)];
+    out.from[0] = i;
+    out.from[1] = j;
+    bool renorm = s.excit_gen != HGPU_EXCIT_GEN_NO_RENORM;
+    double pgen, abs_h;
+    int a = -1, b = -1;
+    if (renorm) {
+        // calc_pgen_hub_k (src/excit_gen_hub_k.f90:651-770)
+        int forbidden = 0;
+#pragma unroll
+        for (int k = 0; k < W; k++) {
+            uint64_t x = ua[k];
+            while (x) {
+                int aa = 64 * k + __ffsll((long long)x) - 1;
+                x &= x - 1;
+                if (tbit<W>(f, hub_partner(t, ij_sym, aa))) forbidden++;
+            }
+        }
+        pgen = 1.0 / (double)(s.nalpha * s.nbeta * (s.nvirt_alpha - forbidden));
+        out.allowed = 1.0 / pgen > 1.0e-12;
+        abs_h = fabs(s.coulomb_k);
+    } else {
+        // find_ab_hub_k (src/excit_gen_hub_k.f90:579-649)
+        int rr = (int)(rs.next() * (double)s.nvirt_alpha);
+        a = select_det<W>(ua, rr);
+        b = hub_partner(t, ij_sym, a);
+        out.allowed = !tbit<W>(f, b);
+        if (out.allowed) {
+            pgen = 1.0 / (double)(s.nalpha * s.nbeta * s.nvirt_alpha);
+            abs_h = fabs(s.coulomb_k);
+        } else {
+            pgen = 1.0;
+            abs_h = 0.0;
+        }
+    }
+    out.pgen = pgen;
+    double pspawn = (double)s.real_factor * s.tau * abs_h / pgen;
+    int64_t nspawn = round_spawned(s.cutoff, pspawn, rs);
+    if (nspawn != 0 || (complete && out.allowed)) {
+        if (renorm) {
+            // choose_ab_hub_k: redraw until b is unoccupied
+            for (int it = 0;; it++) {
+                int rr = (int)(rs.next() * (double)s.nvirt_alpha);
+                a = select_det<W>(ua, rr);
+                b = hub_partner(t, ij_sym, a);
+                if (!tbit<W>(f, b)) break;
+                if (it >= kMaxRedraw) {
+                    out.nspawn = 0;
+                    out.allowed = false;
+                    return;
+                }
+            }
+        }
+        // slater_condon2_hub_k_excit (src/hamiltonian_hub_k.f90:163-234)
+        int f0 = i < j ? i : j, f1 = i < j ? j : i;
+        int t0 = a < b ? a : b, t1 = a < b ? b : a;
+        out.from[0] = f0;
+        out.from[1] = f1;
+        out.to[0] = t0;
+        out.to[1] = t1;
+        double h = s.coulomb_k;
+        if (perm2<W>(f, f0, f1, t0, t1)) h = -h;
+        if (((f0 - t0) % 2) != 0) h = -h;
+        out.hmatel = h;
+        if (nspawn != 0) nspawn = child_sign(h, parent, nspawn);
+    } else {
+        out.to[0] = a;
+        out.to[1] = b;
+        out.hmatel = abs_h;
+    }
+    out.nspawn = nspawn;
+}
+
+// ---------------------------------------------------------------------------
+// Molecular uniform generators (src/excit_gen_mol.f90)
+// ---------------------------------------------------------------------------
+// Per-determinant view: occupied mask and unoccupied counts per (sym, ims).
+template <int W>
+struct MolDet {
+    Det<W> f;
+    uint64_t valid[W];
+    int symunocc[kMaxSym * 2];  // index sym*2+ims
+};
+
+template <int W>
+__device__ __forceinline__ void mol_decode(const DevSys &s, const Det<W> &f, MolDet<W> &d) {
+    d.f = f;
+#pragma unroll
+    for (int k = 0; k < W; k++)
+        d.valid[k] = (64 * (k + 1) <= s.nbasis) ? ~0ull : ((1ull << (s.nbasis - 64 * k)) - 1);
+    for (int q = 0; q < 2 * s.nsym; q++) {
+        int n = 0;
+#pragma unroll
+        for (int k = 0; k < W; k++) n += __popcll(~f.w[k] & s.symmask[q * W + k] & d.valid[k]);
+        d.symunocc[q] = n;
+    }
+}
+
+#define SU(d, ims, sym) ((d).symunocc[(sym)*2 + (ims)])
+
+// ind-th orbital (0-based) of irrep sym with spin ims (sym_spin_basis_fns).
+template <int W>
+__device__ __forceinline__ int ssbf(const DevSys &s, int ims, int sym, int ind) {
+    return select_det<W>(&s.symmask[(sym * 2 + ims) * W], ind);
+}
+
+__device__ __forceinline__ int xsym(const DevSys &s, int a, int b) { return (a ^ b) & (s.nsym - 1); }
+
+template <int W>
+__device__ __forceinline__ int sym_of(const DevSys &s, int p) {
+    return s.orbsym[p];
+}
+
+template <int W>
+__device__ __forceinline__ int pick_a(const DevSys &s, int spin, double r) {
+    if (spin == 0) return (int)(r * (double)s.nbasis);
+    int k = (int)(r * (double)(s.nbasis / 2));
+    return spin == -2 ? 2 * k + 1 : 2 * k;
+}
+
+template <int W, typename Real>
+__device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, int64_t parent, Attempt &out) {
+    const Det<W> &f = d.f;
+    out.from[0] = out.from[1] = out.to[0] = out.to[1] = -1;
+    bool renorm = s.excit_gen == HGPU_EXCIT_GEN_RENORM;
+    double pgen;
+    Real hm;
+    if (rs.next() < s.pattempt_single) {
+        out.nexcit = 1;
+        int i = -1, a = -1;
+        bool ok;
+        if (renorm) {
+            // choose_ia_mol (src/excit_gen_mol.f90:521-618)
+            ok = false;
+            for (int k = 0; k < s.nel; k++) {
+                int p = select_det<W>(f.w, k);
+                if (SU(d, ims_of(p), sym_of<W>(s, p)) != 0) {
+                    ok = true;
+                    break;
+                }
+            }
+            if (ok) {
+                int guard = 0;
+                for (;;) {
+                    i = select_det<W>(f.w, (int)(rs.next() * (double)s.nel));
+                    int imsa = ims_of(i), isyma = sym_of<W>(s, i);
+                    if (SU(d, imsa, isyma) != 0) {
+                        for (;;) {
+                            int ind = (int)((double)s.nbss[isyma * 2 + imsa] * rs.next());
+                            a = ssbf<W>(s, imsa, isyma, ind);
+                            if (!tbit<W>(f, a) || ++guard > kMaxRedraw) break;
+                        }
+                        break;
+                    }
+                    if (++guard > kMaxRedraw) break;
+                }
+                if (guard > kMaxRedraw) ok = false;
+            }
+        } else {
+            // find_ia_mol (src/excit_gen_mol.f90:950-1016)
+            i = select_det<W>(f.w, (int)(rs.next() * (double)s.nel));
+            int imsa = ims_of(i), isyma = sym_of<W>(s, i);
+            int nb = s.nbss[isyma * 2 + imsa];
+            int ind = (int)((double)nb * rs.next());
+            if (nb == 0) {
+                ok = false;
+            } else {
+                a = ssbf<W>(s, imsa, isyma, ind);
+                ok = !tbit<W>(f, a);
+            }
+        }
+        out.allowed = ok;
+        out.from[0] = i;
+        out.to[0] = ok ? a : -1;
+        if (ok) {
+            double pg;
+            if (renorm) {
+                // calc_pgen_single_mol (src/excit_gen_mol.f90:1140-1200)
+                int ni = s.nel;
+                for (int k = 0; k < s.nel; k++) {
+                    int p = select_det<W>(f.w, k);
+                    if (SU(d, ims_of(p), sym_of<W>(s, p)) == 0) ni--;
+                }
+                pg = 1.0 / (double)(ni * SU(d, ims_of(a), sym_of<W>(s, a)));
+            } else {
+                pg = 1.0 / (double)(s.nel * s.nbss[sym_of<W>(s, a) * 2 + ims_of(a)]);
+            }
+            pgen = s.pattempt_single * pg;
+            hm = sc1_mol<W, Real>(s, f, i, a, perm1<W>(f, i, a));
+        } else {
+            hm = (Real)0;
+            pgen = 1.0;
+        }
+    } else {
+        out.nexcit = 2;
+        // choose_ij_mol (src/excit_gen_mol.f90:620-660)
+        double x = rs.next() * (double)s.nel * (double)(s.nel - 1) / 2.0;
+        int ind = (int)x + 1;
+        int j_ind = (int)(1.50 + sqrt((double)(2 * ind) - 1.750));
+        int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
+        int i = select_det<W>(f.w, i_ind - 1);
+        int j = select_det<W>(f.w, j_ind - 1);
+        int ij_sym = xsym(s, sym_of<W>(s, i), sym_of<W>(s, j));
+        int ij_spin = ms_of(i) + ms_of(j);
+        double pgen_ij = 2.0 / (double)(s.nel * (s.nel - 1));
+        out.from[0] = i;
+        out.from[1] = j;
+        int a = -1, b = -1;
+        bool ok = false;
+        if (renorm) {
+            // choose_ab_mol (src/excit_gen_mol.f90:802-948)
+            int is = ij_spin == -2 ? 0 : 1;
+            for (int isyma = 0; isyma < s.nsym; isyma++) {
+                int isymb = xsym(s, isyma, ij_sym);
+                if (ij_spin == 0) {
+                    if ((SU(d, 0, isyma) > 0 && SU(d, 1, isymb) > 0) || (SU(d, 1, isyma) > 0 && SU(d, 0, isymb) > 0)) {
+                        ok = true;
+                        break;
+                    }
+                } else if (SU(d, is, isyma) > 0 &&
+                           (SU(d, is, isymb) > 1 || (SU(d, is, isymb) == 1 && isyma != isymb))) {
+                    ok = true;
+                    break;
+                }
+            }
+            if (ok) {
+                int guard = 0;
+                for (;;) {
+                    a = pick_a<W>(s, ij_spin, rs.next());
+                    if (!tbit<W>(f, a)) {
+                        int imsb = (ij_spin - ms_of(a) + 3) / 2 - 1;
+                        int syma = sym_of<W>(s, a);
+                        int isymb = xsym(s, ij_sym, syma);
+                        int nu = SU(d, imsb, isymb);
+                        if (nu > 1 || (nu == 1 && (isymb != syma || ij_spin == 0))) {
+                            for (;;) {
+                                int k = (int)((double)s.nbss[isymb * 2 + imsb] * rs.next());
+                                b = ssbf<W>(s, imsb, isymb, k);
+                                if ((b != a && !tbit<W>(f, b)) || ++guard > kMaxRedraw) break;
+                            }
+                            break;
+                        }
+                    }
+                    if (++guard > kMaxRedraw) break;
+                }
+                if (guard > kMaxRedraw) ok = false;
+                if (a > b) {
+                    int tt = a;
+                    a = b;
+                    b = tt;
+                }
+            }
+        } else {
+            // find_ab_mol (src/excit_gen_mol.f90:1018-1138)
+            for (int it = 0;; it++) {
+                a = pick_a<W>(s, ij_spin, rs.next());
+                if (!tbit<W>(f, a) || it >= kMaxRedraw) break;
+            }
+            int imsb = (ij_spin - ms_of(a) + 3) / 2 - 1;
+            int syma = sym_of<W>(s, a);
+            int isymb = xsym(s, ij_sym, syma);
+            int nb = s.nbss[isymb * 2 + imsb];
+            if (nb == 0) {
+                ok = false;
+            } else if (ij_spin != 0 && isymb == syma && nb == 1) {
+                ok = false;
+            } else {
+                for (int it = 0;; it++) {
+                    int k = (int)((double)nb * rs.next());
+                    b = ssbf<W>(s, imsb, isymb, k);
+                    if (b != a || it >= kMaxRedraw) break;
+                }
+                ok = b != a && !tbit<W>(f, b);
+                if (a > b) {
+                    int tt = a;
+                    a = b;
+                    b = tt;
+                }
+            }
+        }
+        out.allowed = ok;
+        if (ok) {
+            out.to[0] = a;
+            out.to[1] = b;
+            double pg;
+            int imsa = ims_of(a), imsb = ims_of(b), syma = sym_of<W>(s, a), symb = sym_of<W>(s, b);
+            if (renorm) {
+                // calc_pgen_double_mol (src/excit_gen_mol.f90:1202-1327)
+                int n_aij;
+                double p_bija, p_aijb;
+                if (ij_spin == 0) {
+                    n_aij = s.nvirt;
+                    for (int isyma = 0; isyma < s.nsym; isyma++) {
+                        int isymb = xsym(s, isyma, ij_sym);
+                        if (SU(d, 0, isymb) == 0) n_aij -= SU(d, 1, isyma);
+                        if (SU(d, 1, isymb) == 0) n_aij -= SU(d, 0, isyma);
+                    }
+                    p_aijb = 1.0 / (double)SU(d, imsa, syma);
+                    p_bija = 1.0 / (double)SU(d, imsb, symb);
+                } else {
+                    int is = ij_spin == -2 ? 0 : 1;
+                    n_aij = ij_spin == -2 ? s.nvirt_beta : s.nvirt_alpha;
+                    for (int isyma = 0; isyma < s.nsym; isyma++) {
+                        int isymb = xsym(s, isyma, ij_sym);
+                        if (SU(d, is, isymb) == 0)
+                            n_aij -= SU(d, is, isyma);
+                        else if (isyma == isymb && SU(d, is, isymb) == 1)
+                            n_aij -= SU(d, is, isyma);
+                    }
+                    if (syma == symb) {
+                        p_aijb = 1.0 / (double)(SU(d, imsa, syma) - 1);
+                        p_bija = 1.0 / (double)(SU(d, imsb, symb) - 1);
+                    } else {
+                        p_aijb = 1.0 / (double)SU(d, imsa, syma);
+                        p_bija = 1.0 / (double)SU(d, imsb, symb);
+                    }
+                }
+                pg = (1.0 / (double)n_aij) * (p_bija + p_aijb);
+            } else {
+                // calc_pgen_double_mol_no_renorm (src/excit_gen_mol.f90:1368-1445)
+                int n_aij = ij_spin == -2 ? s.nvirt_beta : (ij_spin == 0 ? s.nvirt : s.nvirt_alpha);
+                double p_bija, p_aijb;
+                if (syma == symb && imsa == imsb) {
+                    p_aijb = 1.0 / (double)(s.nbss[syma * 2 + imsa] - 1);
+                    p_bija = 1.0 / (double)(s.nbss[symb * 2 + imsb] - 1);
+                } else {
+                    p_aijb = 1.0 / (double)s.nbss[syma * 2 + imsa];
+                    p_bija = 1.0 / (double)s.nbss[symb * 2 + imsb];
+                }
+                pg = (1.0 / (double)n_aij) * (p_bija + p_aijb);
+            }
+            pgen = s.pattempt_double * pgen_ij * pg;
+            hm = sc2_mol<Real>(s, i, j, a, b, perm2<W>(f, i, j, a, b));
+        } else {
+            hm = (Real)0;
+            pgen = 1.0;
+        }
+    }
+    // attempt_to_spawn (src/spawning.F90:711-768)
+    double h = (double)hm;
+    out.pgen = pgen;
+    out.hmatel = h;
+    double pspawn = s.tau * fabs(h) / pgen;
+    pspawn = pspawn * (double)s.real_factor;
+    int64_t nspawn = round_spawned(s.cutoff, pspawn, rs);
+    if (nspawn > 0) nspawn = child_sign(h, parent, nspawn);
+    out.nspawn = nspawn;
+}
+
+// Child determinant of an attempt (create_excited_det, src/excitations.F90:365-406).
+template <int W>
+__device__ __forceinline__ Det<W> excited(const Det<W> &f, const Attempt &a) {
+    Det<W> c = f;
+    for (int k = 0; k < a.nexcit; k++) {
+        c.w[a.from[k] >> 6] &= ~(1ull << (a.from[k] & 63));
+        c.w[a.to[k] >> 6] |= (1ull << (a.to[k] & 63));
+    }
+    return c;
+}
+
+// update_proj_energy_hub_k / update_proj_energy_mol
+// (src/energy_evaluation.F90:795-849, :906-985): H_0i for D_i against D_0
+// (0 when D_i is D_0 or not connected).
+template <int W>
+__device__ double proj_hmatel(const DevSys &s, const HubTables &t, const Det<W> &f, const Excit &e) {
+    if (e.nexcit == 0 || e.nexcit > 2) return 0.0;
+    if (s.kind == HGPU_SYS_HUB_K) {
+        if (e.nexcit != 2) return 0.0;
+        double h = two_e_int_hub_k(s, t, e.from[0], e.from[1], e.to[0], e.to[1]);
+        return e.perm ? -h : h;
+    }
+    if (e.nexcit == 1) {
+        if (ms_of(e.from[0]) == ms_of(e.to[0]) && sym_of<W>(s, e.from[0]) == sym_of<W>(s, e.to[0]))
+            return sc1_mol<W, double>(s, f, e.from[0], e.to[0], e.perm);
+        return 0.0;
+    }
+    int i = e.from[0], j = e.from[1], a = e.to[0], b = e.to[1];
+    if (ms_of(i) + ms_of(j) == ms_of(a) + ms_of(b)) {
+        if (xsym(s, sym_of<W>(s, i), sym_of<W>(s, j)) == xsym(s, sym_of<W>(s, a), sym_of<W>(s, b)))
+            return sc2_mol<double>(s, i, j, a, b, e.perm);
+    }
+    return 0.0;
+}
+
+}  // namespace hgpu

@@ -1,0 +1,756 @@
+// hgpu_engine.cu -- host engine and C ABI (include/hande_gpu.h).
+//
+// One handle = one FCIQMC calculation resident on the current CUDA device: the
+// system, the double-buffered main walker list, the spawned list and all
+// scratch are allocated once at hgpu_create.  A Monte Carlo cycle is a fixed
+// launch sequence on the handle's stream (hgpu_kernels.cu); it is captured as
+// a CUDA graph per main-list buffer parity and replayed, so a report of
+// ncycles cycles costs ncycles graph launches and one small readback.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/hande_gpu.h"
+#include "hgpu_kernels.cuh"
+
+using namespace hgpu;
+
+struct hgpu_handle {
+    hgpu_config cfg;
+    int W, R, kind;
+    int device;
+    cudaStream_t stream;
+    DevBuffers b;
+    DevSys hsys;  // host copy of the device system struct
+    int cur;      // buffer holding the current main list
+    cudaGraphExec_t graph[2];
+    bool graph_ok[2];
+    bool use_graphs;
+    // report bookkeeping (host side, as qmc_state_t)
+    double shift[HGPU_MAX_SPACES];
+    int vary_shift[HGPU_MAX_SPACES];
+    double nparticles_old[HGPU_MAX_SPACES];
+    int64_t iter;
+    cudaEvent_t ev0, ev1;
+    double report_ms;
+    std::vector<void *> allocs;
+    // device staging for parity entry points
+    void *scratch;
+    size_t scratch_bytes;
+};
+
+#define CK(x)                                                \
+    do {                                                     \
+        cudaError_t e_ = (x);                                \
+        if (e_ != cudaSuccess) {                             \
+            last_error_text(cudaGetErrorString(e_), #x);     \
+            return HGPU_ERR_CUDA;                            \
+        }                                                    \
+    } while (0)
+
+static char g_last_error[512];
+static void last_error_text(const char *what, const char *where) {
+    snprintf(g_last_error, sizeof(g_last_error), "%s (%s)", what, where);
+}
+
+template <typename T>
+static int dalloc(hgpu_handle *h, T **p, size_t n) {
+    if (n == 0) n = 1;
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+    if (e != cudaSuccess) {
+        last_error_text(cudaGetErrorString(e), "cudaMalloc");
+        *p = nullptr;
+        return HGPU_ERR_OOM;
+    }
+    h->allocs.push_back(q);
+    *p = static_cast<T *>(q);
+    return HGPU_OK;
+}
+
+extern "C" {
+
+int32_t hgpu_version(void) { return 100; }
+
+const char *hgpu_error_string(int32_t status) {
+    switch (status) {
+        case HGPU_OK: return "ok";
+        case HGPU_ERR_INVALID: return "invalid argument";
+        case HGPU_ERR_OOM: return "out of device memory";
+        case HGPU_ERR_SPAWN_OVERFLOW: return "spawned walker list full";
+        case HGPU_ERR_MAIN_OVERFLOW: return "main walker list full";
+        case HGPU_ERR_TIMEOUT: return "device wait timed out";
+        case HGPU_ERR_CUDA: return g_last_error[0] ? g_last_error : "CUDA error";
+        case HGPU_ERR_NO_DEVICE: return "no CUDA device";
+        case HGPU_ERR_UNSUPPORTED: return "unsupported option";
+        default: return "unknown status";
+    }
+}
+
+int32_t hgpu_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+}  // extern "C"
+
+static int64_t capacity_entries(int64_t v, size_t bytes_per_entry, int64_t fallback) {
+    // qmc_in%walker_length: > 0 entries, < 0 megabytes (src/qmc.F90:1462-1465)
+    if (v > 0) return v;
+    if (v < 0) return (int64_t)((double)(-v) * 1048576.0 / (double)bytes_per_entry);
+    return fallback;
+}
+
+static double host_sc0(const hgpu_system *sys, const uint64_t *f) {
+    // slater_condon0 on the host, same operation order as the device (for H00)
+    std::vector<int> occ;
+    for (int p = 0; p < sys->nbasis; p++)
+        if ((f[p >> 6] >> (p & 63)) & 1ull) occ.push_back(p);
+    if (sys->kind == HGPU_SYS_HUB_K) {
+        double h = (double)(sys->nalpha * sys->nbeta) * sys->coulomb_k;
+        for (int p : occ) h = h + sys->sp_eigv[p];
+        return h;
+    }
+    auto tri0 = [](int64_t i, int64_t j) { return i * (i + 1) / 2 + j; };
+    auto v2 = [&](int i, int j, int a, int b) {
+        int si = i >> 1, sj = j >> 1, sa = a >> 1, sb = b >> 1;
+        int64_t ia = si >= sa ? tri0(si, sa) : tri0(sa, si);
+        int64_t jb = sj >= sb ? tri0(sj, sb) : tri0(sb, sj);
+        return sys->v2[ia >= jb ? tri0(ia, jb) : tri0(jb, ia)];
+    };
+    double h = sys->ecore;
+    for (size_t a = 0; a < occ.size(); a++) {
+        int i = occ[a];
+        h = h + sys->h1[(i >> 1) * sys->norb + (i >> 1)];
+        for (size_t c = a + 1; c < occ.size(); c++) {
+            int j = occ[c];
+            h = h + v2(i, j, i, j);
+            if (((i ^ j) & 1) == 0) h = h - v2(i, j, j, i);
+        }
+    }
+    return h;
+}
+
+static int build_system(hgpu_handle *h, const hgpu_system *sys) {
+    DevSys &s = h->hsys;
+    memset(&s, 0, sizeof(s));
+    const hgpu_config &c = h->cfg;
+    s.kind = sys->kind;
+    s.nbasis = sys->nbasis;
+    s.nel = sys->nel;
+    s.nalpha = sys->nalpha;
+    s.nbeta = sys->nbeta;
+    s.nw = sys->nwords;
+    s.nvirt_alpha = sys->nbasis / 2 - sys->nalpha;
+    s.nvirt_beta = sys->nbasis / 2 - sys->nbeta;
+    s.nvirt = sys->nbasis - sys->nel;
+    s.nspaces = h->R;
+    s.excit_gen = c.excit_gen;
+    s.initiator = c.initiator_approx ? 1 : 0;
+    s.real_amplitudes = c.real_amplitudes ? 1 : 0;
+    s.precision = c.precision;
+    s.real_factor = c.real_amplitudes ? ((int64_t)1 << 31) : 1;
+    s.cutoff = c.real_amplitudes ? (int64_t)std::ceil(c.spawn_cutoff * (double)s.real_factor) : 0;
+    s.tau = c.tau;
+    // init_excit_gen (src/qmc.F90:951-972)
+    if (c.pattempt_single < 0 || c.pattempt_double < 0) {
+        s.pattempt_single = sys->kind == HGPU_SYS_HUB_K ? 0.0 : 0.1;
+        s.pattempt_double = sys->kind == HGPU_SYS_HUB_K ? 1.0 : 0.9;
+    } else {
+        s.pattempt_single = c.pattempt_single / (c.pattempt_single + c.pattempt_double);
+        s.pattempt_double = 1.0 - c.pattempt_single;
+    }
+    s.initiator_pop = c.initiator_pop;
+    s.seed = (uint64_t)c.seed;
+    for (int w = 0; w < kMaxWords; w++) s.f0[w] = w < s.nw ? c.ref_det[w] : 0;
+    s.H00 = host_sc0(sys, s.f0);
+    int rc;
+    double *sp;
+    if ((rc = dalloc(h, &sp, sys->nbasis))) return rc;
+    CK(cudaMemcpy(sp, sys->sp_eigv, sizeof(double) * sys->nbasis, cudaMemcpyHostToDevice));
+    s.sp_eigv = sp;
+    if (sys->kind == HGPU_SYS_HUB_K) {
+        int nk = sys->nkpoints;
+        if (nk > 255) return HGPU_ERR_UNSUPPORTED;
+        s.nk = nk;
+        s.coulomb_k = sys->coulomb_k;
+        std::vector<uint8_t> st(nk * nk), inv(nk);
+        for (int i = 0; i < nk * nk; i++) st[i] = (uint8_t)sys->sym_table[i];
+        for (int i = 0; i < nk; i++) inv[i] = (uint8_t)sys->inv_sym[i];
+        uint8_t *dst, *dinv;
+        if ((rc = dalloc(h, &dst, nk * nk))) return rc;
+        if ((rc = dalloc(h, &dinv, nk))) return rc;
+        CK(cudaMemcpy(dst, st.data(), nk * nk, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dinv, inv.data(), nk, cudaMemcpyHostToDevice));
+        s.sym_table = dst;
+        s.inv_sym = dinv;
+        s.nsym = 1;
+        h->b.nk = nk;
+    } else if (sys->kind == HGPU_SYS_READ_IN) {
+        if (sys->nsym_pg > kMaxSym || sys->nsym_pg < 1) return HGPU_ERR_UNSUPPORTED;
+        s.norb = sys->norb;
+        s.nsym = sys->nsym_pg;
+        s.ecore = sys->ecore;
+        int M = sys->norb;
+        double *dh1, *dv2;
+        float *fh1, *fv2;
+        if ((rc = dalloc(h, &dh1, (size_t)M * M))) return rc;
+        if ((rc = dalloc(h, &dv2, (size_t)sys->nv2))) return rc;
+        CK(cudaMemcpy(dh1, sys->h1, sizeof(double) * M * M, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dv2, sys->v2, sizeof(double) * sys->nv2, cudaMemcpyHostToDevice));
+        s.h1 = dh1;
+        s.v2 = dv2;
+        if (c.precision == HGPU_PREC_MIXED) {
+            std::vector<float> t1(M * M), t2(sys->nv2);
+            for (int i = 0; i < M * M; i++) t1[i] = (float)sys->h1[i];
+            for (int64_t i = 0; i < sys->nv2; i++) t2[i] = (float)sys->v2[i];
+            if ((rc = dalloc(h, &fh1, (size_t)M * M))) return rc;
+            if ((rc = dalloc(h, &fv2, (size_t)sys->nv2))) return rc;
+            CK(cudaMemcpy(fh1, t1.data(), sizeof(float) * M * M, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(fv2, t2.data(), sizeof(float) * sys->nv2, cudaMemcpyHostToDevice));
+            s.h1f = fh1;
+            s.v2f = fv2;
+        }
+        for (int p = 0; p < sys->nbasis; p++) {
+            int sym = sys->orb_sym[p];
+            int ims = (p & 1) ? 0 : 1;
+            if (sym < 0 || sym >= s.nsym) return HGPU_ERR_INVALID;
+            s.symmask[(sym * 2 + ims) * s.nw + (p >> 6)] |= 1ull << (p & 63);
+            s.nbss[sym * 2 + ims]++;
+            s.orbsym[p] = (uint8_t)sym;
+        }
+        h->b.nk = 0;
+    } else {
+        return HGPU_ERR_INVALID;
+    }
+    DevSys *d;
+    if ((rc = dalloc(h, &d, 1))) return rc;
+    CK(cudaMemcpy(d, &s, sizeof(DevSys), cudaMemcpyHostToDevice));
+    h->b.sys = d;
+    return HGPU_OK;
+}
+
+static int alloc_lists(hgpu_handle *h) {
+    int W = h->W, R = h->R, rc;
+    DevBuffers &b = h->b;
+    size_t main_entry = 8 * W + 8 * R + 8;
+    b.cap = capacity_entries(h->cfg.walker_length, main_entry, 1 << 20);
+    b.scap = capacity_entries(h->cfg.spawned_walker_length, 8 * (W + R + 1), 1 << 20);
+    if (b.cap >= ((int64_t)1 << 32) || b.scap >= ((int64_t)1 << 31)) return HGPU_ERR_UNSUPPORTED;
+    for (int k = 0; k < 2; k++) {
+        if ((rc = dalloc(h, &b.dets[k], (size_t)b.cap * W))) return rc;
+        if ((rc = dalloc(h, &b.pops[k], (size_t)b.cap * R))) return rc;
+        if ((rc = dalloc(h, &b.kii[k], (size_t)b.cap))) return rc;
+    }
+    if ((rc = dalloc(h, &b.natt, (size_t)b.cap * R))) return rc;
+    if ((rc = dalloc(h, &b.aoff, (size_t)b.cap * R))) return rc;
+    if ((rc = dalloc(h, &b.pinfo, (size_t)b.cap))) return rc;
+    if ((rc = dalloc(h, &b.sdets, (size_t)b.scap * W))) return rc;
+    if ((rc = dalloc(h, &b.spops, (size_t)b.scap * R))) return rc;
+    b.sflag = nullptr;
+    if (h->cfg.initiator_approx)
+        if ((rc = dalloc(h, &b.sflag, (size_t)b.scap))) return rc;
+    for (int k = 0; k < 2; k++) {
+        if ((rc = dalloc(h, &b.keys[k], (size_t)b.scap * W))) return rc;
+        if ((rc = dalloc(h, &b.idx[k], (size_t)b.scap))) return rc;
+    }
+    if ((rc = dalloc(h, &b.hist, (size_t)kRadix * b.grid))) return rc;
+    if ((rc = dalloc(h, &b.segpops, (size_t)b.scap * R))) return rc;
+    if ((rc = dalloc(h, &b.segflag, (size_t)b.scap))) return rc;
+    if ((rc = dalloc(h, &b.segkeep, (size_t)b.scap))) return rc;
+    if ((rc = dalloc(h, &b.segpos, (size_t)b.scap))) return rc;
+    if ((rc = dalloc(h, &b.udets, (size_t)b.scap * W))) return rc;
+    if ((rc = dalloc(h, &b.upops, (size_t)b.scap * R))) return rc;
+    if ((rc = dalloc(h, &b.uflag, (size_t)b.scap))) return rc;
+    size_t merged = (size_t)b.cap + (size_t)b.scap;
+    if ((rc = dalloc(h, &b.mref, merged))) return rc;
+    if ((rc = dalloc(h, &b.mkeep, merged))) return rc;
+    if ((rc = dalloc(h, &b.mpos, merged))) return rc;
+    if ((rc = dalloc(h, &b.scan_part, (size_t)kMaxBlocks * 2))) return rc;
+    if ((rc = dalloc(h, &b.part_d, (size_t)kMaxBlocks * 4))) return rc;
+    if ((rc = dalloc(h, &b.part_i, (size_t)kMaxBlocks * 4))) return rc;
+    if ((rc = dalloc(h, &b.state, 1))) return rc;
+    CK(cudaMemset(b.state, 0, sizeof(DevState)));
+    CK(cudaMemset(b.part_i, 0, sizeof(int64_t) * kMaxBlocks * 4));
+    CK(cudaMemset(b.part_d, 0, sizeof(double) * kMaxBlocks * 4));
+    return HGPU_OK;
+}
+
+static void invalidate_graphs(hgpu_handle *h) {
+    for (int k = 0; k < 2; k++) {
+        if (h->graph_ok[k]) cudaGraphExecDestroy(h->graph[k]);
+        h->graph_ok[k] = false;
+    }
+}
+
+static int read_state(hgpu_handle *h, DevState *st) {
+    CK(cudaMemcpyAsync(st, h->b.state, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return HGPU_OK;
+}
+
+static int write_state(hgpu_handle *h, const DevState *st) {
+    CK(cudaMemcpyAsync(h->b.state, st, sizeof(DevState), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return HGPU_OK;
+}
+
+extern "C" {
+
+int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle **out) {
+    if (!cfg || !sys || !out) return HGPU_ERR_INVALID;
+    *out = nullptr;
+    if (sys->nwords < 1 || sys->nwords > HGPU_MAX_WORDS || sys->nbasis > 64 * sys->nwords ||
+        sys->nbasis <= 64 * (sys->nwords - 1))
+        return HGPU_ERR_INVALID;
+    if (sys->nel < 2 || sys->nalpha + sys->nbeta != sys->nel) return HGPU_ERR_INVALID;
+    if (cfg->nspaces < 1 || cfg->nspaces > HGPU_MAX_SPACES) return HGPU_ERR_INVALID;
+    if (!(cfg->tau > 0.0)) return HGPU_ERR_INVALID;
+    if (sys->kind == HGPU_SYS_HUB_K) {
+        if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM)
+            return HGPU_ERR_UNSUPPORTED;
+    } else if (sys->kind == HGPU_SYS_READ_IN) {
+        if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM)
+            return HGPU_ERR_UNSUPPORTED;
+    } else {
+        return HGPU_ERR_INVALID;
+    }
+    int ndev = hgpu_device_count();
+    if (ndev <= 0) return HGPU_ERR_NO_DEVICE;
+    hgpu_handle *h = new (std::nothrow) hgpu_handle();
+    if (!h) return HGPU_ERR_OOM;
+    h->cfg = *cfg;
+    h->W = sys->nwords;
+    h->R = cfg->nspaces;
+    h->kind = sys->kind;
+    h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;
+    cudaGetDevice(&h->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (sms <= 0) sms = 148;
+    h->b.grid = sms * 4 > kMaxBlocks ? kMaxBlocks : sms * 4;
+    h->b.spawn_grid = sms * 8;
+    h->b.sort_passes = (sys->nbasis + kRadixBits - 1) / kRadixBits;
+    int rc = HGPU_OK;
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) rc = HGPU_ERR_CUDA;
+    if (!rc) rc = build_system(h, sys);
+    if (!rc) rc = alloc_lists(h);
+    if (!rc) {
+        cudaEventCreate(&h->ev0);
+        cudaEventCreate(&h->ev1);
+        for (int s = 0; s < HGPU_MAX_SPACES; s++) h->shift[s] = cfg->initial_shift;
+    }
+    if (rc) {
+        hgpu_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return HGPU_OK;
+}
+
+int32_t hgpu_destroy(hgpu_handle *h) {
+    if (!h) return HGPU_ERR_INVALID;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    invalidate_graphs(h);
+    for (void *p : h->allocs) cudaFree(p);
+    if (h->scratch) cudaFree(h->scratch);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return HGPU_OK;
+}
+
+static int set_list(hgpu_handle *h, const int64_t *states, const int64_t *pops, const double *dat, int64_t n,
+                    bool compute_kii) {
+    if (n < 0 || n > h->b.cap) return HGPU_ERR_INVALID;
+    int W = h->W, R = h->R;
+    h->cur = 0;
+    if (n > 0) {
+        CK(cudaMemcpyAsync(h->b.dets[0], states, sizeof(uint64_t) * W * n, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->b.pops[0], pops, sizeof(int64_t) * R * n, cudaMemcpyHostToDevice, h->stream));
+        if (dat && !compute_kii)
+            CK(cudaMemcpyAsync(h->b.kii[0], dat, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+        else
+            launch_eval_diagonal(h->b, W, h->b.dets[0], n, h->b.kii[0], h->stream);
+    }
+    DevState st;
+    int rc = read_state(h, &st);
+    if (rc) return rc;
+    st.n_main = n;
+    st.abs_pop[0] = st.abs_pop[1] = 0;
+    if ((rc = write_state(h, &st))) return rc;
+    launch_abs_pop(h->b, R, 0, h->stream);
+    if ((rc = read_state(h, &st))) return rc;
+    for (int s = 0; s < R; s++) h->nparticles_old[s] = (double)st.abs_pop[s] / (double)h->hsys.real_factor;
+    return HGPU_OK;
+}
+
+int32_t hgpu_initial_distribution(hgpu_handle *h) {
+    if (!h) return HGPU_ERR_INVALID;
+    int64_t st[HGPU_MAX_WORDS], po[HGPU_MAX_SPACES];
+    for (int w = 0; w < h->W; w++) st[w] = (int64_t)h->hsys.f0[w];
+    for (int s = 0; s < h->R; s++) po[s] = (int64_t)llround(h->cfg.D0_population) * h->hsys.real_factor;
+    double kii = 0.0;
+    DevState ds;
+    int rc = read_state(h, &ds);
+    if (rc) return rc;
+    memset(&ds, 0, sizeof(ds));
+    for (int s = 0; s < HGPU_MAX_SPACES; s++) {
+        h->shift[s] = h->cfg.initial_shift;
+        h->vary_shift[s] = 0;
+        ds.shift[s] = h->cfg.initial_shift;
+    }
+    h->iter = 0;
+    if ((rc = write_state(h, &ds))) return rc;
+    return set_list(h, st, po, &kii, 1, false);
+}
+
+int32_t hgpu_upload_walkers(hgpu_handle *h, const int64_t *states, const int64_t *pops, const double *dat,
+                            int64_t n) {
+    if (!h || (n > 0 && (!states || !pops))) return HGPU_ERR_INVALID;
+    return set_list(h, states, pops, dat, n, dat == nullptr);
+}
+
+int32_t hgpu_download_walkers(hgpu_handle *h, int64_t *states, int64_t *pops, double *dat, int64_t capacity,
+                              int64_t *n_out) {
+    if (!h || !n_out) return HGPU_ERR_INVALID;
+    DevState st;
+    int rc = read_state(h, &st);
+    if (rc) return rc;
+    *n_out = st.n_main;
+    if (capacity < st.n_main) return HGPU_ERR_INVALID;
+    int64_t n = st.n_main;
+    if (n > 0) {
+        if (states)
+            CK(cudaMemcpyAsync(states, h->b.dets[h->cur], sizeof(uint64_t) * h->W * n, cudaMemcpyDeviceToHost,
+                               h->stream));
+        if (pops)
+            CK(cudaMemcpyAsync(pops, h->b.pops[h->cur], sizeof(int64_t) * h->R * n, cudaMemcpyDeviceToHost, h->stream));
+        if (dat) CK(cudaMemcpyAsync(dat, h->b.kii[h->cur], sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    return HGPU_OK;
+}
+
+static int launch_one_cycle(hgpu_handle *h) {
+    int cur = h->cur;
+    if (h->use_graphs) {
+        if (!h->graph_ok[cur]) {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            launch_cycle(h->b, h->W, h->R, h->kind, h->cfg.precision, cur, h->stream);
+            CK(cudaStreamEndCapture(h->stream, &g));
+            cudaError_t e = cudaGraphInstantiate(&h->graph[cur], g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                last_error_text(cudaGetErrorString(e), "cudaGraphInstantiate");
+                return HGPU_ERR_CUDA;
+            }
+            h->graph_ok[cur] = true;
+        }
+        CK(cudaGraphLaunch(h->graph[cur], h->stream));
+    } else {
+        launch_cycle(h->b, h->W, h->R, h->kind, h->cfg.precision, cur, h->stream);
+        CK(cudaGetLastError());
+    }
+    h->cur = 1 - cur;
+    return HGPU_OK;
+}
+
+int32_t hgpu_run_cycles(hgpu_handle *h, int32_t ncycles) {
+    if (!h || ncycles < 0) return HGPU_ERR_INVALID;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    for (int k = 0; k < ncycles; k++) {
+        int rc = launch_one_cycle(h);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaEventSynchronize(h->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->report_ms += ms;
+    h->iter += ncycles;
+    DevState st;
+    int rc = read_state(h, &st);
+    if (rc) return rc;
+    if (st.error_flags & HGPU_FLAG_SPAWN_OVERFLOW) return HGPU_ERR_SPAWN_OVERFLOW;
+    if (st.error_flags & HGPU_FLAG_MAIN_OVERFLOW) return HGPU_ERR_MAIN_OVERFLOW;
+    return HGPU_OK;
+}
+
+int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
+    if (!h || !out) return HGPU_ERR_INVALID;
+    DevState st;
+    int rc = read_state(h, &st);
+    if (rc) return rc;
+    memset(out, 0, sizeof(*out));
+    int R = h->R;
+    int nc = st.rep_cycles > 0 ? st.rep_cycles : 1;
+    double ntot[HGPU_MAX_SPACES] = {0, 0};
+    for (int s = 0; s < R; s++) {
+        out->proj_energy[s] = (st.acc_proj[s] + st.acc_proj_c[s]) / (double)nc;
+        out->D0_population[s] = (st.acc_d0[s] + st.acc_d0_c[s]) / (double)nc;
+        ntot[s] = (double)st.abs_pop[s] / (double)h->hsys.real_factor;
+    }
+    // update_shift (src/energy_evaluation.F90:659-711), shift_harmonic_forcing = 0
+    for (int s = 0; s < R; s++)
+        if (h->vary_shift[s])
+            h->shift[s] = h->shift[s] - std::log(ntot[s] / h->nparticles_old[s]) * h->cfg.shift_damping /
+                                            (1.0 * h->cfg.tau * (double)nc);
+    for (int s = 0; s < R; s++) h->nparticles_old[s] = ntot[s];
+    for (int s = 0; s < R; s++) {
+        if (!h->vary_shift[s] && ntot[s] > h->cfg.target_particles) {
+            h->vary_shift[s] = 1;
+            h->shift[s] = h->cfg.vary_shift_from_proje ? out->proj_energy[s] / out->D0_population[s]
+                                                       : h->cfg.vary_shift_from;
+        }
+    }
+    for (int s = 0; s < R; s++) {
+        out->shift[s] = h->shift[s];
+        out->nparticles[s] = ntot[s];
+        out->vary_shift[s] = h->vary_shift[s];
+    }
+    out->iteration = st.iter;
+    out->nstates = st.n_main;
+    out->nspawn_events = st.last_nspawn_events;
+    out->rspawn = st.acc_rspawn / (double)nc;
+    out->nattempts = st.acc_attempts;
+    out->nspawned = st.acc_spawned;
+    out->error_flags = st.error_flags;
+    out->device_ms = h->report_ms;
+    h->report_ms = 0.0;
+    // reset the report accumulators, publish the new shift
+    for (int s = 0; s < HGPU_MAX_SPACES; s++) {
+        st.shift[s] = h->shift[s];
+        st.acc_proj[s] = st.acc_proj_c[s] = st.acc_d0[s] = st.acc_d0_c[s] = 0.0;
+    }
+    st.acc_rspawn = 0.0;
+    st.acc_attempts = st.acc_spawned = 0;
+    st.rep_cycles = 0;
+    if ((rc = write_state(h, &st))) return rc;
+    if (out->error_flags & HGPU_FLAG_SPAWN_OVERFLOW) return HGPU_ERR_SPAWN_OVERFLOW;
+    if (out->error_flags & HGPU_FLAG_MAIN_OVERFLOW) return HGPU_ERR_MAIN_OVERFLOW;
+    return HGPU_OK;
+}
+
+int32_t hgpu_run_report(hgpu_handle *h, hgpu_report *out) {
+    if (!h) return HGPU_ERR_INVALID;
+    int rc = hgpu_run_cycles(h, h->cfg.ncycles);
+    if (rc && rc != HGPU_ERR_SPAWN_OVERFLOW && rc != HGPU_ERR_MAIN_OVERFLOW) return rc;
+    return hgpu_end_report(h, out);
+}
+
+int32_t hgpu_get_state(hgpu_handle *h, hgpu_state *out) {
+    if (!h || !out) return HGPU_ERR_INVALID;
+    DevState st;
+    int rc = read_state(h, &st);
+    if (rc) return rc;
+    memset(out, 0, sizeof(*out));
+    out->iteration = st.iter;
+    for (int s = 0; s < HGPU_MAX_SPACES; s++) {
+        out->shift[s] = h->shift[s];
+        out->vary_shift[s] = h->vary_shift[s];
+        out->nparticles_old[s] = h->nparticles_old[s];
+    }
+    out->tau = h->cfg.tau;
+    out->seed = h->cfg.seed;
+    return HGPU_OK;
+}
+
+int32_t hgpu_set_state(hgpu_handle *h, const hgpu_state *in) {
+    if (!h || !in) return HGPU_ERR_INVALID;
+    DevState st;
+    int rc = read_state(h, &st);
+    if (rc) return rc;
+    st.iter = in->iteration;
+    for (int s = 0; s < HGPU_MAX_SPACES; s++) {
+        h->shift[s] = in->shift[s];
+        h->vary_shift[s] = in->vary_shift[s];
+        h->nparticles_old[s] = in->nparticles_old[s];
+        st.shift[s] = in->shift[s];
+    }
+    h->iter = in->iteration;
+    return write_state(h, &st);
+}
+
+// Checkpoint layout: magic, version, nwords, nspaces, n, hgpu_state, then
+// states (nwords*n int64), pops (nspaces*n int64), dat (n double).
+static const char kMagic[8] = {'H', 'G', 'P', 'U', 'C', 'K', 'P', 'T'};
+
+int32_t hgpu_checkpoint(hgpu_handle *h, const char *path) {
+    if (!h || !path) return HGPU_ERR_INVALID;
+    int64_t n = 0;
+    int rc = hgpu_download_walkers(h, nullptr, nullptr, nullptr, 0, &n);
+    if (rc && rc != HGPU_ERR_INVALID) return rc;
+    std::vector<int64_t> st((size_t)(n * h->W + 1)), po((size_t)(n * h->R + 1));
+    std::vector<double> da((size_t)(n + 1));
+    if ((rc = hgpu_download_walkers(h, st.data(), po.data(), da.data(), n, &n))) return rc;
+    hgpu_state s;
+    if ((rc = hgpu_get_state(h, &s))) return rc;
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return HGPU_ERR_INVALID;
+    int32_t hdr[4] = {1, h->W, h->R, 0};
+    bool ok = fwrite(kMagic, 1, 8, fp) == 8 && fwrite(hdr, sizeof(hdr), 1, fp) == 1 &&
+              fwrite(&n, sizeof(n), 1, fp) == 1 && fwrite(&s, sizeof(s), 1, fp) == 1 &&
+              fwrite(st.data(), sizeof(int64_t), (size_t)(n * h->W), fp) == (size_t)(n * h->W) &&
+              fwrite(po.data(), sizeof(int64_t), (size_t)(n * h->R), fp) == (size_t)(n * h->R) &&
+              fwrite(da.data(), sizeof(double), (size_t)n, fp) == (size_t)n;
+    ok = (fclose(fp) == 0) && ok;
+    return ok ? HGPU_OK : HGPU_ERR_INVALID;
+}
+
+int32_t hgpu_restore(hgpu_handle *h, const char *path) {
+    if (!h || !path) return HGPU_ERR_INVALID;
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return HGPU_ERR_INVALID;
+    char magic[8];
+    int32_t hdr[4];
+    int64_t n = -1;
+    hgpu_state s;
+    bool ok = fread(magic, 1, 8, fp) == 8 && memcmp(magic, kMagic, 8) == 0 && fread(hdr, sizeof(hdr), 1, fp) == 1 &&
+              hdr[0] == 1 && hdr[1] == h->W && hdr[2] == h->R && fread(&n, sizeof(n), 1, fp) == 1 && n >= 0 &&
+              n <= h->b.cap && fread(&s, sizeof(s), 1, fp) == 1;
+    std::vector<int64_t> st, po;
+    std::vector<double> da;
+    if (ok) {
+        st.resize((size_t)(n * h->W + 1));
+        po.resize((size_t)(n * h->R + 1));
+        da.resize((size_t)(n + 1));
+        ok = fread(st.data(), sizeof(int64_t), (size_t)(n * h->W), fp) == (size_t)(n * h->W) &&
+             fread(po.data(), sizeof(int64_t), (size_t)(n * h->R), fp) == (size_t)(n * h->R) &&
+             fread(da.data(), sizeof(double), (size_t)n, fp) == (size_t)n;
+        // nothing may follow
+        char extra;
+        ok = ok && fread(&extra, 1, 1, fp) == 0;
+    }
+    fclose(fp);
+    if (!ok) return HGPU_ERR_INVALID;
+    int rc = set_list(h, st.data(), po.data(), da.data(), n, false);
+    if (rc) return rc;
+    return hgpu_set_state(h, &s);
+}
+
+static int ensure_scratch(hgpu_handle *h, size_t bytes) {
+    if (h->scratch_bytes >= bytes) return HGPU_OK;
+    if (h->scratch) cudaFree(h->scratch);
+    h->scratch = nullptr;
+    h->scratch_bytes = 0;
+    CK(cudaMalloc(&h->scratch, bytes));
+    h->scratch_bytes = bytes;
+    return HGPU_OK;
+}
+
+int32_t hgpu_eval_excitations(hgpu_handle *h, const int64_t *parents, const int64_t *parent_pops, int64_t n,
+                              int64_t iteration, int32_t *orbs, double *pgen, double *hmatel, int32_t *allowed,
+                              int64_t *nspawn) {
+    if (!h || n < 0 || (n > 0 && (!parents || !parent_pops || !orbs || !pgen || !hmatel || !allowed || !nspawn)))
+        return HGPU_ERR_INVALID;
+    if (n == 0) return HGPU_OK;
+    size_t off_par = 0, off_pp = off_par + sizeof(int64_t) * h->W * n, off_or = off_pp + sizeof(int64_t) * n;
+    size_t off_pg = off_or + sizeof(int32_t) * 4 * n, off_hm = off_pg + sizeof(double) * n;
+    size_t off_al = off_hm + sizeof(double) * n, off_ns = off_al + sizeof(int32_t) * n + 8;
+    off_ns = (off_ns + 7) & ~(size_t)7;
+    size_t total = off_ns + sizeof(int64_t) * n;
+    int rc = ensure_scratch(h, total);
+    if (rc) return rc;
+    char *base = static_cast<char *>(h->scratch);
+    CK(cudaMemcpyAsync(base + off_par, parents, sizeof(int64_t) * h->W * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(base + off_pp, parent_pops, sizeof(int64_t) * n, cudaMemcpyHostToDevice, h->stream));
+    launch_eval_excitations(h->b, h->W, h->kind, h->cfg.precision, (const uint64_t *)(base + off_par),
+                            (const int64_t *)(base + off_pp), n, iteration, (int32_t *)(base + off_or),
+                            (double *)(base + off_pg), (double *)(base + off_hm), (int32_t *)(base + off_al),
+                            (int64_t *)(base + off_ns), h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(orbs, base + off_or, sizeof(int32_t) * 4 * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(pgen, base + off_pg, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(hmatel, base + off_hm, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(allowed, base + off_al, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(nspawn, base + off_ns, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return HGPU_OK;
+}
+
+int32_t hgpu_annihilate_fixed(hgpu_handle *h, const int64_t *sdata, int64_t n, int64_t iteration) {
+    if (!h || n < 0 || (n > 0 && !sdata)) return HGPU_ERR_INVALID;
+    if (n > h->b.scap) return HGPU_ERR_SPAWN_OVERFLOW;
+    int el = h->W + h->R + 1;
+    int rc = ensure_scratch(h, sizeof(int64_t) * el * (n > 0 ? n : 1));
+    if (rc) return rc;
+    if (n > 0) CK(cudaMemcpyAsync(h->scratch, sdata, sizeof(int64_t) * el * n, cudaMemcpyHostToDevice, h->stream));
+    DevState st;
+    if ((rc = read_state(h, &st))) return rc;
+    int64_t save = st.iter;
+    st.iter = iteration;
+    st.error_flags = 0;
+    if ((rc = write_state(h, &st))) return rc;
+    launch_load_fixed_spawns(h->b, h->W, h->R, (const int64_t *)h->scratch, n, h->stream);
+    launch_annihilation(h->b, h->W, h->R, h->kind, h->cur, h->stream);
+    CK(cudaGetLastError());
+    h->cur = 1 - h->cur;
+    if ((rc = read_state(h, &st))) return rc;
+    st.iter = save;
+    int flags = st.error_flags;
+    if ((rc = write_state(h, &st))) return rc;
+    return (flags & HGPU_FLAG_MAIN_OVERFLOW) ? HGPU_ERR_MAIN_OVERFLOW : HGPU_OK;
+}
+
+int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int64_t *counts) {
+    if (!h || !phase_ms || nphase < 1) return HGPU_ERR_INVALID;
+    PhaseMarks pm;
+    for (int k = 0; k < kNumMarks; k++) CK(cudaEventCreate(&pm.ev[k]));
+    DevState before;
+    int rc = read_state(h, &before);
+    if (rc) return rc;
+    launch_cycle(h->b, h->W, h->R, h->kind, h->cfg.precision, h->cur, h->stream, &pm);
+    CK(cudaGetLastError());
+    h->cur = 1 - h->cur;
+    h->iter += 1;
+    CK(cudaEventSynchronize(pm.ev[kNumMarks - 1]));
+    for (int k = 0; k < nphase && k < kNumMarks - 1; k++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pm.ev[k], pm.ev[k + 1]);
+        phase_ms[k] = ms;
+    }
+    for (int k = 0; k < kNumMarks; k++) cudaEventDestroy(pm.ev[k]);
+    DevState st;
+    if ((rc = read_state(h, &st))) return rc;
+    if (counts) {
+        // N before, A, S, U, N after, launches in the cycle
+        counts[0] = before.n_main;
+        counts[1] = st.n_attempts;
+        counts[2] = st.n_spawn;
+        counts[3] = st.n_uniq;
+        counts[4] = st.n_main;
+        counts[5] = launches_per_cycle(h->b);
+        counts[6] = h->b.sort_passes;
+    }
+    return HGPU_OK;
+}
+
+int32_t hgpu_eval_diagonal(hgpu_handle *h, const int64_t *dets, int64_t n, double *kii) {
+    if (!h || n < 0 || (n > 0 && (!dets || !kii))) return HGPU_ERR_INVALID;
+    if (n == 0) return HGPU_OK;
+    size_t bytes = sizeof(int64_t) * h->W * n + sizeof(double) * n;
+    int rc = ensure_scratch(h, bytes);
+    if (rc) return rc;
+    char *base = static_cast<char *>(h->scratch);
+    CK(cudaMemcpyAsync(base, dets, sizeof(int64_t) * h->W * n, cudaMemcpyHostToDevice, h->stream));
+    double *dk = (double *)(base + sizeof(int64_t) * h->W * n);
+    launch_eval_diagonal(h->b, h->W, (const uint64_t *)base, n, dk, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(kii, dk, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return HGPU_OK;
+}
+
+}  // extern "C"

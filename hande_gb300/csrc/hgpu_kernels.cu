@@ -1,0 +1,1003 @@
+// hgpu_kernels.cu -- the kernels of one FCIQMC Monte Carlo cycle on one GPU.
+//
+// One cycle (src/fciqmc.f90:293-413) is a fixed sequence of launches whose
+// grids do not depend on the list sizes: every kernel reads N, S, U, A from
+// DevState and loops over its share.  The sequence can therefore be captured
+// once as a CUDA graph and replayed every cycle.
+//
+//   cycle_begin     iteration counter, nattempts = nint(2 N_w)      (qmc_common.F90:950)
+//   prep_parents    E_proj / N_0 partials, decide_nattempts, initiator
+//                   flags, stochastic_death in place                 (fciqmc.f90:315-373)
+//   scan            attempt offsets (one flattened attempt per thread)
+//   spawn           excitation generation + spawning, appended with
+//                   warp-aggregated atomics                          (spawning.F90:34/215)
+//   radix sort      stable LSD sort of the spawned determinants       (spawn_data.F90:406)
+//   seg_reduce      self-annihilation incl. the initiator flag rule   (spawn_data.F90:859/:937)
+//   merge_spawn     annihilate_main_list[_initiator] + rounding of new
+//   merge_main      remove_unoccupied_dets rounding                    (annihilation.f90:294-675)
+//   scan + scatter  insert_new_walkers as a stable merge of two sorted
+//                   lists, K_ii = sc0 - H00 for new determinants      (annihilation.f90:677-901)
+//   cycle_end       per-cycle statistics, report accumulators         (qmc_common.F90:1240)
+#include "hgpu_kernels.cuh"
+
+#include <cstdio>
+
+namespace hgpu {
+
+#define FULL_MASK 0xffffffffu
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ uint2 operator+(uint2 a, uint2 b) { return make_uint2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ uint2 operator-(uint2 a, uint2 b) { return make_uint2(a.x - b.x, a.y - b.y); }
+
+template <typename T>
+__device__ __forceinline__ T zero_of();
+template <>
+__device__ __forceinline__ int64_t zero_of<int64_t>() { return 0; }
+template <>
+__device__ __forceinline__ uint2 zero_of<uint2>() { return make_uint2(0, 0); }
+
+template <typename T>
+__device__ __forceinline__ T shfl_up(T v, int d);
+template <>
+__device__ __forceinline__ int64_t shfl_up<int64_t>(int64_t v, int d) {
+    return __shfl_up_sync(FULL_MASK, (long long)v, d);
+}
+template <>
+__device__ __forceinline__ uint2 shfl_up<uint2>(uint2 v, int d) {
+    return make_uint2(__shfl_up_sync(FULL_MASK, v.x, d), __shfl_up_sync(FULL_MASK, v.y, d));
+}
+
+// Inclusive warp scan, then block scan through shared memory.  Returns the
+// exclusive prefix of v within the block and the block total in *tot.
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T *tot) {
+    __shared__ T wsum[32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T y = shfl_up<T>(x, d);
+        if (lane >= d) x = x + y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    int nw = blockDim.x >> 5;
+    if (warp == 0) {
+        T w = lane < nw ? wsum[lane] : zero_of<T>();
+        T s = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            T y = shfl_up<T>(s, d);
+            if (lane >= d) s = s + y;
+        }
+        if (lane < nw) wsum[lane] = s;  // inclusive over warps
+    }
+    __syncthreads();
+    T before = warp > 0 ? wsum[warp - 1] : zero_of<T>();
+    *tot = wsum[nw - 1];
+    __syncthreads();
+    // exclusive = inclusive - v
+    return before + x - v;
+}
+
+__device__ __forceinline__ double shfl_down_any(double v, int d) { return __shfl_down_sync(FULL_MASK, v, d); }
+__device__ __forceinline__ int64_t shfl_down_any(int64_t v, int d) {
+    return (int64_t)__shfl_down_sync(FULL_MASK, (long long)v, d);
+}
+
+template <typename T>
+__device__ __forceinline__ T block_reduce_sum(T v) {
+    __shared__ T red[32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += shfl_down_any(v, d);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    int nw = blockDim.x >> 5;
+    T r = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < nw; k++) r += red[k];
+    __syncthreads();
+    return r;  // valid in thread 0
+}
+
+__device__ __forceinline__ void chunk_range(int64_t n, int64_t &begin, int64_t &end) {
+    int64_t G = gridDim.x;
+    int64_t chunk = (n + G - 1) / G;
+    chunk = (chunk + 255) & ~(int64_t)255;
+    begin = (int64_t)blockIdx.x * chunk;
+    end = begin + chunk < n ? begin + chunk : n;
+    if (begin > n) begin = n;
+}
+
+// ---------------------------------------------------------------------------
+// Device-wide exclusive scan, three phases over a fixed grid.
+// ---------------------------------------------------------------------------
+template <typename T, typename Load>
+__global__ void __launch_bounds__(kBlock) k_scan_reduce(Load load, const int64_t *n_ptr, T *part) {
+    int64_t n = *n_ptr, begin, end;
+    chunk_range(n, begin, end);
+    T acc = zero_of<T>();
+    for (int64_t i = begin + threadIdx.x; i < end; i += blockDim.x) acc = acc + load(i);
+    T tot;
+    block_exclusive_scan<T>(acc, &tot);
+    if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_scan_parts(T *part, int G, T *total) {
+    // exclusive scan of G <= 1024 block sums in place
+    T v = threadIdx.x < G ? part[threadIdx.x] : zero_of<T>();
+    T tot;
+    T ex = block_exclusive_scan<T>(v, &tot);
+    if (threadIdx.x < G) part[threadIdx.x] = ex;
+    if (threadIdx.x == 0 && total) *total = tot;
+}
+
+template <typename T, typename Load, typename Store>
+__global__ void __launch_bounds__(kBlock) k_scan_down(Load load, Store store, const int64_t *n_ptr, const T *part) {
+    int64_t n = *n_ptr, begin, end;
+    chunk_range(n, begin, end);
+    T running = part[blockIdx.x];
+    for (int64_t base = begin; base < end; base += blockDim.x) {
+        int64_t i = base + threadIdx.x;
+        T v = i < end ? load(i) : zero_of<T>();
+        T tot;
+        T ex = block_exclusive_scan<T>(v, &tot);
+        if (i < end) store(i, running + ex, v);
+        running = running + tot;
+    }
+}
+
+// functors
+struct LoadNatt {
+    const uint32_t *a;
+    __device__ int64_t operator()(int64_t i) const { return (int64_t)a[i]; }
+};
+struct StoreInclusive {
+    int64_t *out;
+    __device__ void operator()(int64_t i, int64_t ex, int64_t v) const { out[i] = ex + v; }
+};
+struct LoadKeep {
+    const uint32_t *a;
+    __device__ int64_t operator()(int64_t i) const { return (int64_t)a[i]; }
+};
+struct StoreExclusive {
+    int64_t *out;
+    __device__ void operator()(int64_t i, int64_t ex, int64_t) const { out[i] = ex; }
+};
+struct LoadMKeep {
+    const uint2 *a;
+    __device__ uint2 operator()(int64_t i) const { return a[i]; }
+};
+struct StoreMPos {
+    uint2 *out;
+    __device__ void operator()(int64_t i, uint2 ex, uint2) const { out[i] = ex; }
+};
+
+// n_ptr points at an int64 count; for N*R lists a small kernel writes the product.
+__global__ void k_set_count(int64_t *dst, const int64_t *a, int64_t mul, const int64_t *b) {
+    *dst = *a * mul + (b ? *b : 0);
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory staging of the system
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void stage_sys(DevSys &dst, const DevSys *src) {
+    const uint32_t *s = reinterpret_cast<const uint32_t *>(src);
+    uint32_t *d = reinterpret_cast<uint32_t *>(&dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(DevSys) / 4); k += blockDim.x) d[k] = s[k];
+}
+
+__device__ __forceinline__ HubTables stage_hub(const DevSys *src, uint8_t *smem) {
+    HubTables t;
+    int nk = src->nk;
+    t.nk = nk;
+    if (src->kind == HGPU_SYS_HUB_K) {
+        for (int k = threadIdx.x; k < nk * nk; k += blockDim.x) smem[k] = src->sym_table[k];
+        for (int k = threadIdx.x; k < nk; k += blockDim.x) smem[nk * nk + k] = src->inv_sym[k];
+    }
+    t.sym = smem;
+    t.inv = smem + nk * nk;
+    return t;
+}
+
+template <int W>
+__device__ __forceinline__ Det<W> load_det(const uint64_t *p, int64_t i) {
+    Det<W> d;
+#pragma unroll
+    for (int k = 0; k < W; k++) d.w[k] = p[i * W + k];
+    return d;
+}
+
+template <int W>
+__device__ __forceinline__ void store_det(uint64_t *p, int64_t i, const Det<W> &d) {
+#pragma unroll
+    for (int k = 0; k < W; k++) p[i * W + k] = d.w[k];
+}
+
+// first index in [0, n) whose determinant is not less than x
+template <int W>
+__device__ __forceinline__ int64_t lower_bound_det(const uint64_t *list, int64_t n, const Det<W> &x) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        Det<W> m = load_det<W>(list, mid);
+        if (det_less<W>(m, x)) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Cycle kernels
+// ---------------------------------------------------------------------------
+__global__ void k_cycle_begin(DevState *st, const DevSys *sys) {
+    st->iter += 1;
+    st->n_spawn = 0;
+    double np = (double)st->abs_pop[0] / (double)sys->real_factor;
+    st->nattempts_cycle = llround(2.0 * np);
+}
+
+// decide_nattempts (src/qmc_common.F90:379-406).
+__device__ __forceinline__ uint32_t decide_nattempts(RStream &rs, double population) {
+    double ap = fabs(population);
+    int64_t n = (int64_t)ap;
+    double pextra = ap - (double)n;
+    if (fabs(pextra) > 1.0e-12) {
+        if (pextra > rs.next()) n = n + 1;
+    }
+    return (uint32_t)n;
+}
+
+// stochastic_death (src/death.f90:11-130) with weight = pop_control = 1.
+__device__ __forceinline__ int64_t stochastic_death(double tau, RStream &rs, double Kii, double shift,
+                                                    int64_t &population) {
+    double pd = tau * (Kii - shift);
+    pd = pd * fabs((double)population);
+    int64_t kill = (int64_t)pd;
+    pd = pd - (double)kill;
+    double r = rs.next();
+    if (fabs(pd) > r) {
+        if (pd > 0.0) kill = kill + 1;
+        else kill = kill - 1;
+    }
+    if (population < 0) population = population + kill;
+    else population = population - kill;
+    return kill < 0 ? -kill : kill;
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_prep_parents(DevBuffers b, int R, int cur) {
+    __shared__ DevSys s;
+    extern __shared__ uint8_t smem[];
+    stage_sys(s, b.sys);
+    HubTables t = stage_hub(b.sys, smem);
+    __syncthreads();
+    const DevState *st = b.state;
+    int64_t n = st->n_main;
+    uint64_t iter = (uint64_t)st->iter;
+    double shift[2] = {st->shift[0], st->shift[1]};
+    Det<W> f0;
+#pragma unroll
+    for (int k = 0; k < W; k++) f0.w[k] = s.f0[k];
+    const uint64_t *dets = b.dets[cur];
+    int64_t *pops = b.pops[cur];
+    const double *kii = b.kii[cur];
+    double proj[2] = {0.0, 0.0}, d0[2] = {0.0, 0.0};
+    int64_t ndeath = 0;
+    double rf = (double)s.real_factor;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        Det<W> f = load_det<W>(dets, i);
+        Excit e = get_excitation<W>(f, f0, s.nel);
+        double h = (e.nexcit == 1 || e.nexcit == 2) ? proj_hmatel<W>(s, t, f, e) : 0.0;
+        double k = kii[i];
+        uint32_t info = 0;
+        for (int sp = 0; sp < R; sp++) {
+            int64_t p = pops[i * R + sp];
+            double rp = (double)p / rf;
+            // update_proj_energy
+            if (e.nexcit == 0) d0[sp] += rp;
+            else proj[sp] += h * rp;
+            // set_parent_flag: bit set if not an initiator
+            if (!(fabs(rp) > s.initiator_pop)) info |= 4u << sp;
+            if (p < 0) info |= 1u << sp;
+            RStream rs;
+            rs.init(s.seed, P_NATTEMPT, sp, i, 0, iter);
+            b.natt[i * R + sp] = decide_nattempts(rs, rp);
+            rs.init(s.seed, P_DEATH, sp, i, 0, iter);
+            ndeath += stochastic_death(s.tau, rs, k, shift[sp], p);
+            pops[i * R + sp] = p;
+        }
+        b.pinfo[i] = (uint8_t)info;
+    }
+    double r0 = block_reduce_sum<double>(proj[0]);
+    double r1 = block_reduce_sum<double>(proj[1]);
+    double r2 = block_reduce_sum<double>(d0[0]);
+    double r3 = block_reduce_sum<double>(d0[1]);
+    int64_t r4 = block_reduce_sum<int64_t>(ndeath);
+    if (threadIdx.x == 0) {
+        b.part_d[blockIdx.x * 4 + 0] = r0;
+        b.part_d[blockIdx.x * 4 + 1] = r1;
+        b.part_d[blockIdx.x * 4 + 2] = r2;
+        b.part_d[blockIdx.x * 4 + 3] = r3;
+        b.part_i[blockIdx.x * 4 + 2] = r4;
+    }
+}
+
+// first k in [0, n) with off[k] > a (off is the inclusive scan of attempts)
+__device__ __forceinline__ int64_t upper_bound_off(const int64_t *off, int64_t n, int64_t a) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (off[mid] > a) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+template <int W, int KIND, typename Real>
+__global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) {
+    __shared__ DevSys s;
+    extern __shared__ uint8_t smem[];
+    stage_sys(s, b.sys);
+    HubTables t = stage_hub(b.sys, smem);
+    __syncthreads();
+    const DevState *st = b.state;
+    int64_t A = st->n_attempts;
+    int64_t NR = st->n_main * R;
+    uint64_t iter = (uint64_t)st->iter;
+    const uint64_t *dets = b.dets[cur];
+    int lane = threadIdx.x & 31;
+    int64_t warp_base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = warp_base; base < A; base += stride) {
+        int64_t a = base + lane;
+        bool want = false;
+        Det<W> child;
+        int64_t nspawn = 0;
+        int sp = 0;
+        uint64_t flagword = 0;
+        if (a < A) {
+            int64_t k = upper_bound_off(b.aoff, NR, a);
+            int64_t i = k / R;
+            sp = (int)(k - i * R);
+            int64_t att = a - (k > 0 ? b.aoff[k - 1] : 0);
+            Det<W> f = load_det<W>(dets, i);
+            uint32_t info = b.pinfo[i];
+            int64_t parent = (info >> sp) & 1u ? -1 : 1;
+            RStream rs;
+            rs.init(s.seed, P_SPAWN, sp, i, att, iter);
+            Attempt at;
+            if (KIND == HGPU_SYS_HUB_K) {
+                attempt_hub_k<W>(s, t, rs, f, parent, false, at);
+            } else {
+                MolDet<W> d;
+                mol_decode<W>(s, f, d);
+                attempt_mol<W, Real>(s, rs, d, parent, at);
+            }
+            if (at.nspawn != 0) {
+                want = true;
+                nspawn = at.nspawn;
+                child = excited<W>(f, at);
+                flagword = (uint64_t)((info >> 2) & 3u) | ((uint64_t)a << 2);
+            }
+        }
+        uint32_t ball = __ballot_sync(FULL_MASK, want);
+        if (ball) {
+            int leader = __ffs(ball) - 1;
+            unsigned long long basepos = 0;
+            if (lane == leader) basepos = atomicAdd((unsigned long long *)&b.state->n_spawn, (unsigned long long)__popc(ball));
+            basepos = __shfl_sync(FULL_MASK, basepos, leader);
+            if (want) {
+                int64_t pos = (int64_t)basepos + __popc(ball & lanemask_lt());
+                if (pos < b.scap) {
+                    store_det<W>(b.sdets, pos, child);
+                    for (int q = 0; q < R; q++) b.spops[pos * R + q] = q == sp ? nspawn : 0;
+                    if (b.sflag) b.sflag[pos] = flagword;
+                } else {
+                    atomicOr(&b.state->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_clamp_spawns(DevState *st, int64_t scap) {
+    if (st->n_spawn > scap) {
+        st->n_spawn = scap;
+        st->error_flags |= HGPU_FLAG_SPAWN_OVERFLOW;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort of the spawned determinants (8-bit digits)
+// ---------------------------------------------------------------------------
+template <int W>
+__device__ __forceinline__ uint32_t digit_of(const uint64_t *keys, int64_t i, int shift) {
+    return (uint32_t)((keys[i * W + (shift >> 6)] >> (shift & 63)) & (kRadix - 1));
+}
+
+template <int W>
+__global__ void __launch_bounds__(kRadix) k_radix_up(const uint64_t *keys, const int64_t *n_ptr, int shift,
+                                                     uint32_t *hist) {
+    __shared__ uint32_t h[kRadix];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t n = *n_ptr, begin, end;
+    chunk_range(n, begin, end);
+    for (int64_t i = begin + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&h[digit_of<W>(keys, i, shift)], 1u);
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t *hist, int total) {
+    // exclusive scan of total (= kRadix * grid) counts, digit-major
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < total; base += 1024) {
+        int i = base + threadIdx.x;
+        int64_t v = i < total ? (int64_t)hist[i] : 0;
+        int64_t tot;
+        int64_t ex = block_exclusive_scan<int64_t>(v, &tot);
+        uint32_t c = carry;
+        if (i < total) hist[i] = (uint32_t)(ex + c);
+        __syncthreads();
+        if (threadIdx.x == 0) carry = c + (uint32_t)tot;
+        __syncthreads();
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kRadix) k_radix_down(const uint64_t *keys_in, const uint32_t *idx_in,
+                                                       uint64_t *keys_out, uint32_t *idx_out, const int64_t *n_ptr,
+                                                       int shift, const uint32_t *hist) {
+    constexpr int NW = kRadix / 32;  // warps
+    __shared__ uint32_t wcnt[NW][kRadix];
+    __shared__ uint32_t boff[kRadix];
+    __shared__ uint32_t ttot[kRadix];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t n = *n_ptr, begin, end;
+    chunk_range(n, begin, end);
+    boff[threadIdx.x] = hist[(int64_t)threadIdx.x * gridDim.x + blockIdx.x];
+    const int64_t tile = (int64_t)NW * kSortItems * 32;
+    for (int64_t tb = begin; tb < end; tb += tile) {
+#pragma unroll
+        for (int w = 0; w < NW; w++) wcnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        uint64_t kv[kSortItems][W];
+        uint32_t iv[kSortItems], off[kSortItems], dg[kSortItems];
+#pragma unroll
+        for (int r = 0; r < kSortItems; r++) {
+            int64_t e = tb + ((int64_t)(warp * kSortItems + r)) * 32 + lane;
+            bool valid = e < end;
+            uint32_t mask = __ballot_sync(FULL_MASK, valid);
+            dg[r] = 0xFFFFFFFFu;
+            if (valid) {
+#pragma unroll
+                for (int k = 0; k < W; k++) kv[r][k] = keys_in[e * W + k];
+                iv[r] = idx_in ? idx_in[e] : (uint32_t)e;
+                uint32_t d = (uint32_t)((kv[r][shift >> 6] >> (shift & 63)) & (kRadix - 1));
+                dg[r] = d;
+                uint32_t peers = __match_any_sync(mask, d);
+                int leader = __ffs(peers) - 1;
+                uint32_t rank = __popc(peers & lanemask_lt());
+                uint32_t old = 0;
+                if (lane == leader) {
+                    old = wcnt[warp][d];
+                    wcnt[warp][d] = old + __popc(peers);
+                }
+                old = __shfl_sync(mask, old, leader);
+                off[r] = old + rank;
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        {
+            uint32_t run = 0;
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
+                uint32_t c = wcnt[w][threadIdx.x];
+                wcnt[w][threadIdx.x] = run;
+                run += c;
+            }
+            ttot[threadIdx.x] = run;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kSortItems; r++) {
+            if (dg[r] != 0xFFFFFFFFu) {
+                uint32_t d = dg[r];
+                int64_t pos = (int64_t)boff[d] + wcnt[warp][d] + off[r];
+#pragma unroll
+                for (int k = 0; k < W; k++) keys_out[pos * W + k] = kv[r][k];
+                idx_out[pos] = iv[r];
+            }
+        }
+        __syncthreads();
+        boff[threadIdx.x] += ttot[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Self-annihilation of the sorted spawned list
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int sgn3(int64_t x) { return x > 0 ? 1 : (x < 0 ? -1 : 0); }
+__device__ __forceinline__ int sgn1(int64_t x) { return x >= 0 ? 1 : -1; }
+// Fortran sign(1, int(x)): int() keeps the low 32 bits of an int64.
+__device__ __forceinline__ int sign1_int32(int64_t x) { return (int32_t)(uint32_t)(uint64_t)x >= 0 ? 1 : -1; }
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_seg_reduce(DevBuffers b, int R, const uint64_t *keys, const uint32_t *idx,
+                                                       int initiator) {
+    int64_t S = b.state->n_spawn;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
+        Det<W> ki = load_det<W>(keys, i);
+        bool head = i == 0 || !det_eq<W>(load_det<W>(keys, i - 1), ki);
+        if (!head) {
+            b.segkeep[i] = 0;
+            continue;
+        }
+        int64_t sum[2] = {0, 0}, ip[2] = {0, 0}, ev[2] = {0, 0}, firstpop[2] = {0, 0};
+        uint64_t minord = ~0ull, firstflag = 0;
+        for (int64_t j = i; j < S; j++) {
+            if (j > i && !det_eq<W>(load_det<W>(keys, j), ki)) break;
+            uint32_t e = idx[j];
+            uint64_t fl = initiator ? b.sflag[e] : 0;
+            for (int q = 0; q < R; q++) {
+                int64_t p = b.spops[(int64_t)e * R + q];
+                sum[q] += p;
+                if (initiator) {
+                    if (!((fl >> q) & 1)) ip[q] += p;
+                    else ev[q] += sgn3(p);
+                }
+            }
+            if (initiator && (fl >> 2) < minord) {
+                minord = fl >> 2;
+                firstflag = fl;
+                for (int q = 0; q < R; q++) firstpop[q] = b.spops[(int64_t)e * R + q];
+            }
+        }
+        uint64_t flag = 0;
+        if (initiator) {
+            // annihilate_spawn_t_initiator (src/spawn_data.F90:937-1101): the
+            // first entry of a determinant counts sign(1, int(pop)) events.
+            for (int q = 0; q < R; q++) {
+                if ((firstflag >> q) & 1) ev[q] += sign1_int32(firstpop[q]) - sgn3(firstpop[q]);
+                bool keep = (ip[q] != 0 && sgn1(sum[q]) == sgn1(ip[q])) || (ev[q] > 1 || ev[q] < -1);
+                if (!keep) flag |= 1ull << q;
+            }
+        }
+        bool nz = false;
+        for (int q = 0; q < R; q++) {
+            b.segpops[i * R + q] = sum[q];
+            nz = nz || sum[q] != 0;
+        }
+        b.segflag[i] = flag;
+        b.segkeep[i] = nz ? 1u : 0u;
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_seg_compact(DevBuffers b, int R, const uint64_t *keys) {
+    int64_t S = b.state->n_spawn;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!b.segkeep[i]) continue;
+        int64_t u = b.segpos[i];
+        store_det<W>(b.udets, u, load_det<W>(keys, i));
+        for (int q = 0; q < R; q++) b.upops[u * R + q] = b.segpops[i * R + q];
+        b.uflag[u] = b.segflag[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Merge of the unique spawned list into the main list
+// ---------------------------------------------------------------------------
+// stochastic_round_int_64 (src/stoch_utils.f90:51-85) of one entry's pops.
+__device__ __forceinline__ void round_pops(const DevSys &s, int64_t *p, int R, uint32_t purpose, int64_t idx,
+                                           uint64_t iter) {
+    for (int q = 0; q < R; q++) {
+        int64_t v = p[q];
+        int64_t av = v < 0 ? -v : v;
+        if (av < s.real_factor && v != 0) {
+            RStream rs;
+            rs.init(s.seed, purpose, q, idx, 0, iter);
+            double r = rs.next() * (double)s.real_factor;
+            p[q] = ((double)av > r) ? isign64(s.real_factor, v) : 0;
+        }
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_merge_spawn(DevBuffers b, int R, int cur) {
+    __shared__ DevSys s;
+    stage_sys(s, b.sys);
+    __syncthreads();
+    int64_t U = b.state->n_uniq, N = b.state->n_main;
+    uint64_t iter = (uint64_t)b.state->iter;
+    const uint64_t *mdets = b.dets[cur];
+    int64_t *mpops = b.pops[cur];
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < U; j += (int64_t)gridDim.x * blockDim.x) {
+        Det<W> d = load_det<W>(b.udets, j);
+        int64_t sp[2] = {0, 0};
+        for (int q = 0; q < R; q++) sp[q] = b.upops[j * R + q];
+        uint64_t fl = b.uflag[j];
+        int64_t pos = lower_bound_det<W>(mdets, N, d);
+        bool hit = pos < N && det_eq<W>(load_det<W>(mdets, pos), d);
+        int64_t rank;
+        uint32_t keep;
+        if (hit) {
+            // annihilate_main_list[_initiator] (src/annihilation.f90:294-486)
+            for (int q = 0; q < R; q++) {
+                int64_t m = mpops[pos * R + q];
+                if (!s.initiator || m != 0) m += sp[q];
+                else if (!((fl >> q) & 1)) m = sp[q];
+                mpops[pos * R + q] = m;
+            }
+            rank = j + pos + 1;
+            keep = 0;
+        } else {
+            bool discard = false;
+            if (s.initiator) {
+                discard = true;
+                for (int q = 0; q < R; q++) {
+                    if ((fl >> q) & 1) sp[q] = 0;
+                    else discard = false;
+                }
+            }
+            if (!discard && s.real_amplitudes) round_pops(s, sp, R, P_ROUND_SPAWN, j, iter);
+            bool nz = false;
+            for (int q = 0; q < R; q++) {
+                b.upops[j * R + q] = sp[q];
+                nz = nz || sp[q] != 0;
+            }
+            keep = discard ? 0u : (s.real_amplitudes ? (nz ? 1u : 0u) : 1u);
+            rank = j + pos;
+        }
+        b.mref[rank] = -(j + 1);
+        b.mkeep[rank] = make_uint2(0u, keep);
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_merge_main(DevBuffers b, int R, int cur) {
+    __shared__ DevSys s;
+    stage_sys(s, b.sys);
+    __syncthreads();
+    int64_t U = b.state->n_uniq, N = b.state->n_main;
+    uint64_t iter = (uint64_t)b.state->iter;
+    const uint64_t *mdets = b.dets[cur];
+    int64_t *mpops = b.pops[cur];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        Det<W> d = load_det<W>(mdets, i);
+        int64_t lb = U > 0 ? lower_bound_det<W>(b.udets, U, d) : 0;
+        int64_t p[2] = {0, 0};
+        for (int q = 0; q < R; q++) p[q] = mpops[i * R + q];
+        // remove_unoccupied_dets (src/annihilation.f90:537-598)
+        if (s.real_amplitudes) {
+            round_pops(s, p, R, P_ROUND_MAIN, i, iter);
+            for (int q = 0; q < R; q++) mpops[i * R + q] = p[q];
+        }
+        bool nz = false;
+        for (int q = 0; q < R; q++) nz = nz || p[q] != 0;
+        int64_t rank = i + lb;
+        b.mref[rank] = i;
+        b.mkeep[rank] = make_uint2(nz ? 1u : 0u, nz ? 1u : 0u);
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_merge_scatter(DevBuffers b, int R, int cur) {
+    __shared__ DevSys s;
+    stage_sys(s, b.sys);
+    __syncthreads();
+    int64_t U = b.state->n_uniq, N = b.state->n_main, M = U + N;
+    uint2 tot = *reinterpret_cast<const uint2 *>(&b.state->n_merged_keep);
+    bool overflow = (int64_t)tot.y > b.cap;
+    const uint64_t *mdets = b.dets[cur];
+    const int64_t *mpops = b.pops[cur];
+    const double *mkii = b.kii[cur];
+    uint64_t *odets = b.dets[1 - cur];
+    int64_t *opops = b.pops[1 - cur];
+    double *okii = b.kii[1 - cur];
+    int64_t ap0 = 0, ap1 = 0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < M; r += (int64_t)gridDim.x * blockDim.x) {
+        uint2 k = b.mkeep[r];
+        if (!k.y) continue;
+        if (overflow && !k.x) continue;
+        uint2 pos2 = b.mpos[r];
+        int64_t dst = overflow ? (int64_t)pos2.x : (int64_t)pos2.y;
+        if (dst >= b.cap) continue;
+        int64_t ref = b.mref[r];
+        int64_t p[2] = {0, 0};
+        if (ref >= 0) {
+            store_det<W>(odets, dst, load_det<W>(mdets, ref));
+            for (int q = 0; q < R; q++) p[q] = mpops[ref * R + q];
+            okii[dst] = mkii[ref];
+        } else {
+            int64_t j = -ref - 1;
+            Det<W> d = load_det<W>(b.udets, j);
+            store_det<W>(odets, dst, d);
+            for (int q = 0; q < R; q++) p[q] = b.upops[j * R + q];
+            // insert_new_walker: dat(1) = sc0(det) - H00 (src/annihilation.f90:855)
+            okii[dst] = sc0<W>(s, d) - s.H00;
+        }
+        for (int q = 0; q < R; q++) opops[dst * R + q] = p[q];
+        ap0 += p[0] < 0 ? -p[0] : p[0];
+        ap1 += p[1] < 0 ? -p[1] : p[1];
+    }
+    int64_t r0 = block_reduce_sum<int64_t>(ap0);
+    int64_t r1 = block_reduce_sum<int64_t>(ap1);
+    if (threadIdx.x == 0) {
+        b.part_i[blockIdx.x * 4 + 0] = r0;
+        b.part_i[blockIdx.x * 4 + 1] = r1;
+    }
+}
+
+// Neumaier-compensated accumulation.
+__device__ __forceinline__ void comp_add(double &sum, double &c, double x) {
+    double t = sum + x;
+    if (fabs(sum) >= fabs(x)) c += (sum - t) + x;
+    else c += (x - t) + sum;
+    sum = t;
+}
+
+__global__ void k_cycle_end(DevBuffers b, int R, int G, int had_prep) {
+    // single thread: fixed summation order over the per-block partials
+    if (threadIdx.x != 0) return;
+    DevState *st = b.state;
+    const DevSys *s = b.sys;
+    uint2 tot = *reinterpret_cast<const uint2 *>(&st->n_merged_keep);
+    bool overflow = (int64_t)tot.y > b.cap;
+    if (overflow) st->error_flags |= HGPU_FLAG_MAIN_OVERFLOW;
+    int64_t nn = overflow ? (int64_t)tot.x : (int64_t)tot.y;
+    st->n_main = nn < b.cap ? nn : b.cap;
+    int64_t ap[2] = {0, 0}, ndeath = 0;
+    double proj[2] = {0, 0}, pc[2] = {0, 0}, d0[2] = {0, 0}, dc[2] = {0, 0};
+    for (int k = 0; k < G; k++) {
+        ap[0] += b.part_i[k * 4 + 0];
+        ap[1] += b.part_i[k * 4 + 1];
+        if (had_prep) {
+            ndeath += b.part_i[k * 4 + 2];
+            comp_add(proj[0], pc[0], b.part_d[k * 4 + 0]);
+            comp_add(proj[1], pc[1], b.part_d[k * 4 + 1]);
+            comp_add(d0[0], dc[0], b.part_d[k * 4 + 2]);
+            comp_add(d0[1], dc[1], b.part_d[k * 4 + 3]);
+        }
+    }
+    st->abs_pop[0] = ap[0];
+    st->abs_pop[1] = R > 1 ? ap[1] : 0;
+    if (!had_prep) return;
+    for (int q = 0; q < R; q++) {
+        comp_add(st->acc_proj[q], st->acc_proj_c[q], proj[q] + pc[q]);
+        comp_add(st->acc_d0[q], st->acc_d0_c[q], d0[q] + dc[q]);
+    }
+    int64_t S = st->n_spawn;
+    // spawning_rate (src/qmc_common.F90:1264-1304)
+    if (st->nattempts_cycle > 0)
+        st->acc_rspawn += ((double)S + (double)ndeath / (double)s->real_factor) / (double)st->nattempts_cycle;
+    st->acc_attempts += st->n_attempts;
+    st->acc_spawned += S;
+    st->last_nspawn_events = S;
+    st->rep_cycles += 1;
+}
+
+__global__ void k_zero_parts(int64_t *part_i, int G) {
+    for (int k = threadIdx.x; k < G * 4; k += blockDim.x) part_i[k] = 0;
+}
+
+// Kernels of the parity / utility entry points.
+template <int W, int KIND, typename Real>
+__global__ void __launch_bounds__(kBlock) k_eval_excitations(const DevSys *gsys, const uint64_t *parents,
+                                                             const int64_t *ppops, int64_t n, uint64_t iteration,
+                                                             int32_t *orbs, double *pgen, double *hmatel,
+                                                             int32_t *allowed, int64_t *nspawn) {
+    __shared__ DevSys s;
+    extern __shared__ uint8_t smem[];
+    stage_sys(s, gsys);
+    HubTables t = stage_hub(gsys, smem);
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        Det<W> f = load_det<W>(parents, i);
+        RStream rs;
+        rs.init(s.seed, P_SPAWN, 0, i, 0, iteration);
+        Attempt at;
+        if (KIND == HGPU_SYS_HUB_K) {
+            attempt_hub_k<W>(s, t, rs, f, ppops[i], true, at);
+        } else {
+            MolDet<W> d;
+            mol_decode<W>(s, f, d);
+            attempt_mol<W, Real>(s, rs, d, ppops[i], at);
+        }
+        orbs[4 * i + 0] = at.from[0];
+        orbs[4 * i + 1] = at.nexcit == 2 ? at.from[1] : -1;
+        orbs[4 * i + 2] = at.to[0];
+        orbs[4 * i + 3] = at.nexcit == 2 ? at.to[1] : -1;
+        pgen[i] = at.pgen;
+        hmatel[i] = at.hmatel;
+        allowed[i] = at.allowed ? 1 : 0;
+        nspawn[i] = at.nspawn;
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_eval_diagonal(const DevSys *gsys, const uint64_t *dets, int64_t n,
+                                                          double *kii) {
+    __shared__ DevSys s;
+    stage_sys(s, gsys);
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        kii[i] = sc0<W>(s, load_det<W>(dets, i)) - s.H00;
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_load_fixed(DevBuffers b, int R, const int64_t *sdata, int64_t n) {
+    int el = W + R + 1;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t *e = sdata + i * el;
+        for (int k = 0; k < W; k++) b.sdets[i * W + k] = (uint64_t)e[k];
+        for (int q = 0; q < R; q++) b.spops[i * R + q] = e[W + q];
+        if (b.sflag) b.sflag[i] = ((uint64_t)e[W + R] & 3ull) | ((uint64_t)i << 2);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) b.state->n_spawn = n;
+}
+
+__global__ void __launch_bounds__(kBlock) k_abs_pop(DevBuffers b, int R, int cur) {
+    int64_t n = b.state->n_main;
+    int64_t a0 = 0, a1 = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p0 = b.pops[cur][i * R];
+        a0 += p0 < 0 ? -p0 : p0;
+        if (R > 1) {
+            int64_t p1 = b.pops[cur][i * R + 1];
+            a1 += p1 < 0 ? -p1 : p1;
+        }
+    }
+    int64_t r0 = block_reduce_sum<int64_t>(a0);
+    int64_t r1 = block_reduce_sum<int64_t>(a1);
+    if (threadIdx.x == 0) {
+        atomicAdd((unsigned long long *)&b.state->abs_pop[0], (unsigned long long)r0);
+        atomicAdd((unsigned long long *)&b.state->abs_pop[1], (unsigned long long)r1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launch sequences
+// ---------------------------------------------------------------------------
+static size_t hub_smem(int kind, int nk) {
+    return kind == HGPU_SYS_HUB_K ? (size_t)(nk * nk + nk + 16) : 16;
+}
+
+template <typename T, typename Load, typename Store>
+static void device_scan(const DevBuffers &b, Load load, Store store, const int64_t *n_ptr, T *part, T *total,
+                        cudaStream_t st) {
+    k_scan_reduce<T, Load><<<b.grid, kBlock, 0, st>>>(load, n_ptr, part);
+    k_scan_parts<T><<<1, 1024, 0, st>>>(part, b.grid, total);
+    k_scan_down<T, Load, Store><<<b.grid, kBlock, 0, st>>>(load, store, n_ptr, part);
+}
+
+template <int W>
+static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st, const PhaseMarks *pm = nullptr) {
+    DevState *S = b.state;
+    int initiator_flagged = b.sflag != nullptr;
+    k_clamp_spawns<<<1, 1, 0, st>>>(S, b.scap);
+    // radix sort: pass 0 reads the spawned list directly
+    const uint64_t *kin = b.sdets;
+    const uint32_t *iin = nullptr;
+    int o = 0;
+    for (int p = 0; p < b.sort_passes; p++) {
+        int shift = p * kRadixBits;
+        k_radix_up<W><<<b.grid, kRadix, 0, st>>>(kin, &S->n_spawn, shift, b.hist);
+        k_radix_scan<<<1, 1024, 0, st>>>(b.hist, kRadix * b.grid);
+        k_radix_down<W><<<b.grid, kRadix, 0, st>>>(kin, iin, b.keys[o], b.idx[o], &S->n_spawn, shift, b.hist);
+        kin = b.keys[o];
+        iin = b.idx[o];
+        o ^= 1;
+    }
+    if (pm) cudaEventRecord(pm->ev[4], st);
+    k_seg_reduce<W><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
+    device_scan<int64_t>(b, LoadKeep{b.segkeep}, StoreExclusive{b.segpos}, &S->n_spawn, b.scan_part, &S->n_uniq, st);
+    k_seg_compact<W><<<b.grid, kBlock, 0, st>>>(b, R, kin);
+    if (pm) cudaEventRecord(pm->ev[5], st);
+    k_merge_spawn<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
+    k_merge_main<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
+    k_set_count<<<1, 1, 0, st>>>(&S->n_merged, &S->n_main, 1, &S->n_uniq);
+    device_scan<uint2>(b, LoadMKeep{b.mkeep}, StoreMPos{b.mpos}, &S->n_merged, reinterpret_cast<uint2 *>(b.scan_part),
+                       reinterpret_cast<uint2 *>(&S->n_merged_keep), st);
+    k_merge_scatter<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
+    if (pm) cudaEventRecord(pm->ev[6], st);
+}
+
+template <int W>
+static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur, cudaStream_t st,
+                    const PhaseMarks *pm) {
+    DevState *S = b.state;
+    size_t sm = hub_smem(kind, b.nk);
+    if (pm) cudaEventRecord(pm->ev[0], st);
+    k_cycle_begin<<<1, 1, 0, st>>>(S, b.sys);
+    k_prep_parents<W><<<b.grid, kBlock, sm, st>>>(b, R, cur);
+    if (pm) cudaEventRecord(pm->ev[1], st);
+    // attempt offsets over the N*R (parent, space) slots; total -> n_attempts
+    k_set_count<<<1, 1, 0, st>>>(&S->n_slots, &S->n_main, R, nullptr);
+    device_scan<int64_t>(b, LoadNatt{b.natt}, StoreInclusive{b.aoff}, &S->n_slots, b.scan_part, &S->n_attempts, st);
+    if (pm) cudaEventRecord(pm->ev[2], st);
+    if (kind == HGPU_SYS_HUB_K)
+        k_spawn<W, HGPU_SYS_HUB_K, double><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+    else if (precision == HGPU_PREC_MIXED)
+        k_spawn<W, HGPU_SYS_READ_IN, float><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+    else
+        k_spawn<W, HGPU_SYS_READ_IN, double><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+    if (pm) cudaEventRecord(pm->ev[3], st);
+    annihilation_w<W>(b, R, cur, st, pm);
+    k_cycle_end<<<1, 32, 0, st>>>(b, R, b.grid, 1);
+    if (pm) cudaEventRecord(pm->ev[7], st);
+}
+
+void launch_cycle(const DevBuffers &b, int W, int R, int kind, int precision, int cur, cudaStream_t st,
+                  const PhaseMarks *pm) {
+    if (W == 1) cycle_w<1>(b, R, kind, precision, cur, st, pm);
+    else cycle_w<2>(b, R, kind, precision, cur, st, pm);
+}
+
+int launches_per_cycle(const DevBuffers &b) {
+    // begin, prep, count, scan(3), spawn, clamp, sort(3/pass), seg_reduce,
+    // scan(3), compact, merge_spawn, merge_main, count, scan(3), scatter, end
+    return 2 + 1 + 3 + 1 + 1 + 3 * b.sort_passes + 1 + 3 + 1 + 2 + 1 + 3 + 1 + 1;
+}
+
+void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st) {
+    (void)kind;
+    k_zero_parts<<<1, kBlock, 0, st>>>(b.part_i, b.grid);
+    if (W == 1) annihilation_w<1>(b, R, cur, st);
+    else annihilation_w<2>(b, R, cur, st);
+    k_cycle_end<<<1, 32, 0, st>>>(b, R, b.grid, 0);
+}
+
+void launch_eval_excitations(const DevBuffers &b, int W, int kind, int precision, const uint64_t *parents,
+                             const int64_t *parent_pops, int64_t n, int64_t iteration, int32_t *orbs, double *pgen,
+                             double *hmatel, int32_t *allowed, int64_t *nspawn, cudaStream_t st) {
+    size_t sm = hub_smem(kind, b.nk);
+    int grid = (int)((n + kBlock - 1) / kBlock);
+    if (grid < 1) grid = 1;
+    if (grid > b.grid) grid = b.grid;
+#define HGPU_EVAL(WW, KK, RR)                                                                                   \
+    k_eval_excitations<WW, KK, RR><<<grid, kBlock, sm, st>>>(b.sys, parents, parent_pops, n, (uint64_t)iteration, \
+                                                             orbs, pgen, hmatel, allowed, nspawn)
+    if (W == 1) {
+        if (kind == HGPU_SYS_HUB_K) HGPU_EVAL(1, HGPU_SYS_HUB_K, double);
+        else if (precision == HGPU_PREC_MIXED) HGPU_EVAL(1, HGPU_SYS_READ_IN, float);
+        else HGPU_EVAL(1, HGPU_SYS_READ_IN, double);
+    } else {
+        if (kind == HGPU_SYS_HUB_K) HGPU_EVAL(2, HGPU_SYS_HUB_K, double);
+        else if (precision == HGPU_PREC_MIXED) HGPU_EVAL(2, HGPU_SYS_READ_IN, float);
+        else HGPU_EVAL(2, HGPU_SYS_READ_IN, double);
+    }
+#undef HGPU_EVAL
+}
+
+void launch_eval_diagonal(const DevBuffers &b, int W, const uint64_t *dets, int64_t n, double *kii, cudaStream_t st) {
+    int grid = (int)((n + kBlock - 1) / kBlock);
+    if (grid < 1) grid = 1;
+    if (grid > b.grid) grid = b.grid;
+    if (W == 1) k_eval_diagonal<1><<<grid, kBlock, 0, st>>>(b.sys, dets, n, kii);
+    else k_eval_diagonal<2><<<grid, kBlock, 0, st>>>(b.sys, dets, n, kii);
+}
+
+void launch_load_fixed_spawns(const DevBuffers &b, int W, int R, const int64_t *sdata, int64_t n, cudaStream_t st) {
+    if (W == 1) k_load_fixed<1><<<b.grid, kBlock, 0, st>>>(b, R, sdata, n);
+    else k_load_fixed<2><<<b.grid, kBlock, 0, st>>>(b, R, sdata, n);
+}
+
+void launch_abs_pop(const DevBuffers &b, int R, int cur, cudaStream_t st) {
+    k_abs_pop<<<b.grid, kBlock, 0, st>>>(b, R, cur);
+}
+
+}  // namespace hgpu

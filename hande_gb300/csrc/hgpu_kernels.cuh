@@ -1,0 +1,109 @@
+// hgpu_kernels.cuh -- device state and kernel launchers of one FCIQMC cycle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "hgpu_device.cuh"
+
+namespace hgpu {
+
+constexpr int kBlock = 256;      // threads per block of the streaming kernels
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kSortItems = 8;    // keys per thread per radix tile
+constexpr int kMaxBlocks = 1024; // upper bound of the fixed grid (partials arrays)
+
+// Per-cycle counters and per-report accumulators, resident in device memory so
+// that a whole cycle runs without host synchronisation (and can be replayed
+// as a CUDA graph).  Sizes of the variable-length lists live here.
+struct DevState {
+    int64_t n_main;        // N: occupied determinants
+    int64_t n_spawn;       // S: spawned entries this cycle
+    int64_t n_uniq;        // U: entries after self-annihilation
+    int64_t n_attempts;    // A: spawning attempts this cycle
+    int64_t n_merged_keep; // uint2 (kept main, kept total) after the merge
+    int64_t n_slots;       // N * nspaces
+    int64_t n_merged;      // N + U
+    int64_t iter;          // current iteration (cycle number, 1-based)
+    double shift[HGPU_MAX_SPACES];
+    int64_t abs_pop[HGPU_MAX_SPACES];  // exact sum |pop| of the main list (encoded units)
+    int64_t nattempts_cycle;           // nint(2 N_w) at the start of the cycle (rspawn)
+    int32_t error_flags;
+    int32_t pad;
+    // report accumulators
+    double acc_proj[HGPU_MAX_SPACES], acc_proj_c[HGPU_MAX_SPACES];
+    double acc_d0[HGPU_MAX_SPACES], acc_d0_c[HGPU_MAX_SPACES];
+    double acc_rspawn;
+    int64_t acc_attempts, acc_spawned, last_nspawn_events;
+    int32_t rep_cycles;
+    int32_t pad2;
+};
+
+// Device buffers of one engine (all allocated once, at create).
+struct DevBuffers {
+    // main list, double-buffered: states (nw per entry), pops (R per entry), K_ii
+    uint64_t *dets[2];
+    int64_t *pops[2];
+    double *kii[2];
+    int64_t cap;
+    // per-parent work arrays (size cap)
+    uint32_t *natt;     // attempts per (parent, space)
+    int64_t *aoff;      // inclusive offsets of natt
+    uint8_t *pinfo;     // per parent: bit s = sign(pop_s) < 0, bit 2+s = non-initiator in space s
+    // spawned list (size scap)
+    uint64_t *sdets;
+    int64_t *spops;
+    uint64_t *sflag;    // initiator bits | generation order << 2
+    int64_t scap;
+    // sort buffers
+    uint64_t *keys[2];
+    uint32_t *idx[2];
+    uint32_t *hist;     // kRadix * grid
+    // self-annihilated list (size scap)
+    int64_t *segpops;   // per sorted position (R)
+    uint64_t *segflag;
+    uint32_t *segkeep;
+    int64_t *segpos;
+    uint64_t *udets;
+    int64_t *upops;
+    uint64_t *uflag;
+    // merge
+    int64_t *mref;      // per merged rank: >= 0 main index, < 0 -(j+1) unique spawn
+    uint2 *mkeep;       // per merged rank: (kept main, kept any)
+    uint2 *mpos;        // exclusive scan of mkeep
+    // scan scratch and per-block partials
+    int64_t *scan_part;     // kMaxBlocks * 2
+    double *part_d;         // kMaxBlocks * 4 (proj, d0 per space)
+    int64_t *part_i;        // kMaxBlocks * 4 (abs pop per space, ndeath)
+    DevState *state;
+    DevSys *sys;
+    int grid;               // blocks of the streaming kernels
+    int spawn_grid;         // blocks of the spawning kernel
+    int sort_passes;
+    int nk;                 // hub_k: number of k-points (shared-memory tables)
+};
+
+// Events recorded between the phases of a cycle in profiling mode:
+// 0 start, 1 after prep, 2 after attempt scan, 3 after spawn, 4 after sort,
+// 5 after self-annihilation, 6 after merge, 7 end.
+constexpr int kNumMarks = 8;
+struct PhaseMarks {
+    cudaEvent_t ev[kNumMarks];
+};
+
+// One cycle, split in launchable phases.  cur = buffer index of the main list
+// at the start of the cycle; the merged list is written to 1-cur.
+void launch_cycle(const DevBuffers &b, int W, int R, int kind, int precision, int cur, cudaStream_t st,
+                  const PhaseMarks *pm = nullptr);
+int launches_per_cycle(const DevBuffers &b);
+void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st);
+void launch_eval_excitations(const DevBuffers &b, int W, int kind, int precision, const uint64_t *parents,
+                             const int64_t *parent_pops, int64_t n, int64_t iteration, int32_t *orbs, double *pgen,
+                             double *hmatel, int32_t *allowed, int64_t *nspawn, cudaStream_t st);
+void launch_eval_diagonal(const DevBuffers &b, int W, const uint64_t *dets, int64_t n, double *kii, cudaStream_t st);
+void launch_load_fixed_spawns(const DevBuffers &b, int W, int R, const int64_t *sdata, int64_t n, cudaStream_t st);
+void launch_abs_pop(const DevBuffers &b, int R, int cur, cudaStream_t st);
+
+}  // namespace hgpu

@@ -237,6 +237,14 @@ int32_t hgpu_annihilate_fixed(hgpu_handle *h, const int64_t *sdata, int64_t n, i
 /* K_ii = slater_condon0(D_i) - H00 for n determinants (sc0_ptr). */
 int32_t hgpu_eval_diagonal(hgpu_handle *h, const int64_t *dets, int64_t n, double *kii);
 
+/* Run one cycle with device timestamps between its phases (the role of
+ * HANDE's per-section timing report, parallel_timing_t in
+ * lib/local/parallel.F90:80-88).  phase_ms[0..6]: prep (E_proj, nattempts,
+ * death), attempt scan, spawning, sort, self-annihilation, merge, end of
+ * cycle.  counts[0..6] (may be NULL): N before, attempts, spawned, unique
+ * spawned, N after, kernel launches per cycle, radix passes. */
+int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int64_t *counts);
+
 #ifdef __cplusplus
 }
 #endif

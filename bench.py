@@ -1,0 +1,347 @@
+"""Benchmark: FCIQMC spawn attempts/s and iteration time on one GB300.
+
+Workload (one "step" = one FCIQMC Monte Carlo cycle): the synthetic molecular
+Hamiltonian with 26 spatial orbitals and 10 electrons (C1, ms=0), real
+amplitudes (2^-31 fixed point), spawn cutoff 0.01, uniform excitation
+generator with p_double = 0.9, tau = 1e-3, FP64, target population 1e7.  The
+population is grown from the reference determinant until the shift varies
+(untimed), then W warm-up and K timed cycles run on the device.
+
+  value      spawn attempts/s over the K timed cycles, device-timed with CUDA
+             events on the engine's stream (the main and spawned lists,
+             >= 200 MB each, exceed the 129 MB L2 between cycles)
+  e2e        the same metric through the C ABI with host-resident walker
+             lists: upload (pinned host -> device), one cycle, download
+  roofline   HBM roofline of the dominant kernel (spawning) and of the
+             annihilation phases (sort + self-annihilation + merge)
+  cpu_baseline  the CPU oracle (C restatement of HANDE's cycle) on a bounded
+             sample of the same workload
+
+--impl reference times the CPU restatement of the reference algorithm on all
+host cores (the reference itself, Fortran + MPI + Lua, cannot be built here).
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "spawn attempts/s & iter time @1 GB300: FP32-batched vs FP64 plain at equal E_proj σ"
+WORKLOAD = "config2: synthetic molecule M=26 nel=10 C1, real amplitudes, cutoff 0.01, uniform renorm p_double=0.9, tau=1e-3, target 1e7, FP64"
+
+
+def system_and_config(target=1e7, seed_ham=2024, seed_rng=7, cap_main=None, cap_spawn=None):
+    from hande_gb300 import systems
+    from hande_gb300._abi import make_config
+    s = systems.synthetic_molecule(26, 10, seed=seed_ham)
+    cm = cap_main or int(7 * target) + 200000
+    cs = cap_spawn or int(6 * target) + 200000
+    cfg = make_config(s, tau=1e-3, init_pop=10, target_population=target, ncycles=10, seed=seed_rng,
+                      real_amplitudes=True, spawn_cutoff=0.01, excit_gen="renorm", pattempt_single=0.1,
+                      pattempt_double=0.9, state_size=cm, spawned_state_size=cs)
+    return s, cfg
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cudart():
+    for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            continue
+    return None
+
+
+def pinned_array(rt, shape, dtype):
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    p = C.c_void_p()
+    if rt is None or rt.cudaHostAlloc(C.byref(p), C.c_size_t(max(n, 8)), 0) != 0:
+        return np.zeros(shape, dtype=dtype), None
+    buf = (C.c_byte * max(n, 8)).from_address(p.value)
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape), p
+
+
+def grow(eng, max_reports=60):
+    rep = None
+    settled = 0
+    for _ in range(max_reports):
+        rep = eng.run_report()
+        if rep.error_flags:
+            raise RuntimeError("walker list overflow while growing (flags %d)" % rep.error_flags)
+        if rep.vary_shift[0]:
+            settled += 1
+            if settled >= 3:
+                break
+    return rep
+
+
+def cpu_sample(seconds=15.0, target=2e5, seed=7):
+    """The oracle on a bounded sample of the same workload: grow to `target`
+    walkers, then time whole cycles for about `seconds` s."""
+    from oracle.pyoracle import Oracle
+    s, cfg = system_and_config(target=target, seed_rng=seed, cap_main=int(20 * target), cap_spawn=int(40 * target))
+    o = Oracle(s, cfg)
+    o.initial_distribution()
+    for _ in range(300):  # grow cycle by cycle up to the sample size
+        o.run_cycles(1)
+        if o.end_report().nparticles[0] >= target:
+            break
+    a0 = o.total_attempts()
+    t0 = time.perf_counter()
+    ncyc = 0
+    while time.perf_counter() - t0 < seconds:
+        o.run_cycles(1)
+        ncyc += 1
+    dt = time.perf_counter() - t0
+    att = o.total_attempts() - a0
+    rep = o.end_report()
+    return {"attempts": att, "seconds": dt, "cycles": ncyc, "walkers": rep.nparticles[0],
+            "states": rep.nstates}
+
+
+def cpu_sample_on_state(states, pops, dat, seconds=10.0, seed=7):
+    """The oracle timed on whole cycles of the engine's own walker list."""
+    from oracle.pyoracle import Oracle
+    n = states.shape[0]
+    s, cfg = system_and_config(target=1e7, seed_rng=seed, cap_main=int(3 * n) + 1000, cap_spawn=int(4 * n) + 1000)
+    o = Oracle(s, cfg)
+    o.set_walkers(states, pops, dat)
+    a0 = o.total_attempts()
+    t0 = time.perf_counter()
+    ncyc = 0
+    while ncyc == 0 or time.perf_counter() - t0 < seconds:
+        o.run_cycles(1)
+        ncyc += 1
+    dt = time.perf_counter() - t0
+    return {"attempts": o.total_attempts() - a0, "seconds": dt, "cycles": ncyc, "walkers": float(np.abs(pops).sum()) / 2 ** 31,
+            "states": n}
+
+
+def _cpu_worker(args):
+    seconds, target, seed = args
+    return cpu_sample(seconds, target, seed)
+
+
+def reference_arm(args):
+    """CPU restatement of HANDE's FCIQMC cycle on every host core: one
+    independent calculation per core (HANDE runs one MPI rank per core)."""
+    import multiprocessing as mp
+    ncores = os.cpu_count() or 1
+    seconds = float(os.environ.get("HGPU_REF_SECONDS", "20"))
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(ncores) as pool:
+        res = pool.map(_cpu_worker, [(seconds, 2e5, 7 + k) for k in range(ncores)])
+    wall = time.perf_counter() - t0
+    att = sum(r["attempts"] for r in res)
+    rate = att / max(r["seconds"] for r in res)
+    ms_per_cycle = 1e3 * np.mean([r["seconds"] / max(r["cycles"], 1) for r in res])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "attempts/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_cycle, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": "per core: grow to 2e5 walkers, time whole cycles %.0f s" % seconds,
+                   "parallelism": "one independent calculation per host core"},
+        "cpu_baseline": {"value": rate, "unit": "attempts/s", "cores": ncores, "kind": "port",
+                         "sample": "%d cores x %.0f s of cycles at ~2e5 walkers (CPU restatement of HANDE's cycle)"
+                                   % (ncores, seconds)},
+        "e2e": {"value": rate, "unit": "attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--target", type=float, default=1e7)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        return
+    args.warmup = max(args.warmup, 3)
+
+    cpu = None
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        td.init_process_group("nccl")
+        dist = td
+
+    from hande_gb300.engine import Engine
+    s, cfg = system_and_config(target=args.target, seed_rng=7 + rank)
+    eng = Engine(s, cfg)
+    eng.initial_distribution()
+    grow(eng)
+    eng.run_cycles(args.warmup)
+    eng.end_report()
+
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    if dist:
+        dist.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    rc = eng.run_cycles(args.steps)  # synchronises the engine stream at the end
+    rep = eng.end_report()
+    clk = clocks.stop()
+    dev_ms = rep.device_ms
+    attempts = rep.nattempts
+    if rep.error_flags:
+        raise RuntimeError("walker list overflow during the timed cycles (flags %d, rc %d)" % (rep.error_flags, rc))
+    if dist:
+        import torch
+        t = torch.tensor([dev_ms, float(attempts)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        dev_ms, attempts = float(mx[0]), float(t[1])
+    value = attempts / (dev_ms * 1e-3)
+    ms_per_step = dev_ms / args.steps
+
+    # per-phase times of one cycle and the HBM roofline figures
+    phases, counts = eng.profile_cycle()
+    from hande_gb300.measure import roofline_figures
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    roof, annih = roofline_figures(phases, counts, W=s.nwords, R=1, initiator=False, peaks=peaks)
+
+    # end to end through the C ABI with host-resident walker lists
+    rt = cudart()
+    st, po, da = eng.walkers()
+    n0 = st.shape[0]
+    cap = int(n0 * 1.6) + 1000
+    hst, _ = pinned_array(rt, (cap, s.nwords), np.int64)
+    hpo, _ = pinned_array(rt, (cap, 1), np.int64)
+    hda, _ = pinned_array(rt, (cap,), np.float64)
+    hst[:n0] = st
+    hpo[:n0] = po
+    hda[:n0] = da
+    n = n0
+    from hande_gb300.engine import _p
+    L = eng.L
+    h2d = d2h = 0
+    e_att = 0
+    eng.end_report()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        eng._check(L.hgpu_upload_walkers(eng.h, _p(hst, C.c_int64), _p(hpo, C.c_int64), _p(hda, C.c_double), n),
+                   "upload")
+        h2d += n * (8 * s.nwords + 8 + 8)
+        eng.run_cycles(1)
+        m = C.c_int64()
+        eng._check(L.hgpu_download_walkers(eng.h, _p(hst, C.c_int64), _p(hpo, C.c_int64), _p(hda, C.c_double),
+                                           cap, C.byref(m)), "download")
+        n = m.value
+        d2h += n * (8 * s.nwords + 8 + 8)
+    e2e_s = time.perf_counter() - t0
+    e_rep = eng.end_report()
+    e_att = e_rep.nattempts
+    e2e = {"value": e_att / e2e_s, "unit": "attempts/s", "h2d_bytes_per_step": h2d // args.e2e_steps,
+           "d2h_bytes_per_step": d2h // args.e2e_steps,
+           "note": "per step: hgpu_upload_walkers from pinned host memory, one cycle, hgpu_download_walkers"}
+
+    if rank == 0 and not args.no_cpu:
+        # the oracle on whole cycles of the same (device-grown) walker list, 1 core
+        r = cpu_sample_on_state(st, po, da, args.cpu_seconds)
+        cpu = {"value": r["attempts"] / r["seconds"], "unit": "attempts/s", "cores": 1, "kind": "port",
+               "sample": "CPU oracle, 1 core, %d whole cycle(s) in %.1f s on the benchmark's own %.3g-walker list"
+                         % (r["cycles"], r["seconds"], r["walkers"])}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "attempts/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "walkers": rep.nparticles[0], "states": int(rep.nstates),
+                       "attempts_per_step": attempts / args.steps / world, "l2": "inputs larger than L2",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": e2e,
+            "gpu_launches": int(counts["launches_per_cycle"]) * args.steps,
+            "roofline": roof,
+            "annihilation_roofline": annih,
+            "phase_ms": phases,
+            "cycle_counts": counts,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

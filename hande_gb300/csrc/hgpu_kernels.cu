@@ -364,8 +364,22 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
         int64_t nspawn = 0;
         int sp = 0;
         uint64_t flagword = 0;
+        // (parent, space) slot of each attempt: one global search per warp,
+        // then a search among the next 32 slots (each slot holds >= 1 attempt
+        // unless a replica space is empty there), global search as fallback.
+        int64_t k0 = 0;
+        if (lane == 0) k0 = upper_bound_off(b.aoff, NR, base);
+        k0 = __shfl_sync(FULL_MASK, k0, 0);
+        int64_t wv = k0 + lane < NR ? b.aoff[k0 + lane] : INT64_MAX;
+        uint32_t le_mask = 0;
+#pragma unroll 1
+        for (int m = 0; m < 32; m++) {
+            int64_t v = __shfl_sync(FULL_MASK, wv, m);
+            if (v <= a) le_mask |= 1u << m;
+        }
         if (a < A) {
-            int64_t k = upper_bound_off(b.aoff, NR, a);
+            int cnt = __popc(le_mask);
+            int64_t k = (cnt < 32 && k0 + cnt < NR) ? k0 + cnt : upper_bound_off(b.aoff, NR, a);
             int64_t i = k / R;
             sp = (int)(k - i * R);
             int64_t att = a - (k > 0 ? b.aoff[k - 1] : 0);
@@ -750,35 +764,50 @@ __device__ __forceinline__ void comp_add(double &sum, double &c, double x) {
     sum = t;
 }
 
-__global__ void k_cycle_end(DevBuffers b, int R, int G, int had_prep) {
-    // single thread: fixed summation order over the per-block partials
-    if (threadIdx.x != 0) return;
+// Fixed-order (hence deterministic) tree reduction over the per-block partials.
+template <typename T>
+__device__ __forceinline__ T tree_sum(T v, T *buf) {
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = blockDim.x >> 1; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) buf[threadIdx.x] = buf[threadIdx.x] + buf[threadIdx.x + w];
+        __syncthreads();
+    }
+    T r = buf[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(1024) k_cycle_end(DevBuffers b, int R, int G, int had_prep) {
+    __shared__ double dbuf[1024];
+    __shared__ int64_t ibuf[1024];
     DevState *st = b.state;
+    int t = threadIdx.x;
+    bool in = t < G;
+    int64_t ap0 = tree_sum<int64_t>(in ? b.part_i[t * 4 + 0] : 0, ibuf);
+    int64_t ap1 = tree_sum<int64_t>(in ? b.part_i[t * 4 + 1] : 0, ibuf);
+    int64_t ndeath = 0;
+    double proj[2] = {0, 0}, d0[2] = {0, 0};
+    if (had_prep) {
+        ndeath = tree_sum<int64_t>(in ? b.part_i[t * 4 + 2] : 0, ibuf);
+        proj[0] = tree_sum<double>(in ? b.part_d[t * 4 + 0] : 0.0, dbuf);
+        proj[1] = tree_sum<double>(in ? b.part_d[t * 4 + 1] : 0.0, dbuf);
+        d0[0] = tree_sum<double>(in ? b.part_d[t * 4 + 2] : 0.0, dbuf);
+        d0[1] = tree_sum<double>(in ? b.part_d[t * 4 + 3] : 0.0, dbuf);
+    }
+    if (t != 0) return;
     const DevSys *s = b.sys;
     uint2 tot = *reinterpret_cast<const uint2 *>(&st->n_merged_keep);
     bool overflow = (int64_t)tot.y > b.cap;
     if (overflow) st->error_flags |= HGPU_FLAG_MAIN_OVERFLOW;
     int64_t nn = overflow ? (int64_t)tot.x : (int64_t)tot.y;
     st->n_main = nn < b.cap ? nn : b.cap;
-    int64_t ap[2] = {0, 0}, ndeath = 0;
-    double proj[2] = {0, 0}, pc[2] = {0, 0}, d0[2] = {0, 0}, dc[2] = {0, 0};
-    for (int k = 0; k < G; k++) {
-        ap[0] += b.part_i[k * 4 + 0];
-        ap[1] += b.part_i[k * 4 + 1];
-        if (had_prep) {
-            ndeath += b.part_i[k * 4 + 2];
-            comp_add(proj[0], pc[0], b.part_d[k * 4 + 0]);
-            comp_add(proj[1], pc[1], b.part_d[k * 4 + 1]);
-            comp_add(d0[0], dc[0], b.part_d[k * 4 + 2]);
-            comp_add(d0[1], dc[1], b.part_d[k * 4 + 3]);
-        }
-    }
-    st->abs_pop[0] = ap[0];
-    st->abs_pop[1] = R > 1 ? ap[1] : 0;
+    st->abs_pop[0] = ap0;
+    st->abs_pop[1] = R > 1 ? ap1 : 0;
     if (!had_prep) return;
     for (int q = 0; q < R; q++) {
-        comp_add(st->acc_proj[q], st->acc_proj_c[q], proj[q] + pc[q]);
-        comp_add(st->acc_d0[q], st->acc_d0_c[q], d0[q] + dc[q]);
+        comp_add(st->acc_proj[q], st->acc_proj_c[q], proj[q]);
+        comp_add(st->acc_d0[q], st->acc_d0_c[q], d0[q]);
     }
     int64_t S = st->n_spawn;
     // spawning_rate (src/qmc_common.F90:1264-1304)
@@ -937,7 +966,7 @@ static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur
         k_spawn<W, HGPU_SYS_READ_IN, double><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
     if (pm) cudaEventRecord(pm->ev[3], st);
     annihilation_w<W>(b, R, cur, st, pm);
-    k_cycle_end<<<1, 32, 0, st>>>(b, R, b.grid, 1);
+    k_cycle_end<<<1, 1024, 0, st>>>(b, R, b.grid, 1);
     if (pm) cudaEventRecord(pm->ev[7], st);
 }
 
@@ -958,7 +987,7 @@ void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, c
     k_zero_parts<<<1, kBlock, 0, st>>>(b.part_i, b.grid);
     if (W == 1) annihilation_w<1>(b, R, cur, st);
     else annihilation_w<2>(b, R, cur, st);
-    k_cycle_end<<<1, 32, 0, st>>>(b, R, b.grid, 0);
+    k_cycle_end<<<1, 1024, 0, st>>>(b, R, b.grid, 0);
 }
 
 void launch_eval_excitations(const DevBuffers &b, int W, int kind, int precision, const uint64_t *parents,

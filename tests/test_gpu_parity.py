@@ -134,11 +134,10 @@ RUNS = [
     ("hub_k_4x4", dict(tau=0.005, init_pop=10, target_population=1000, excit_gen="no_renorm"), 5),
     ("hub_k_3x3_ms1", dict(tau=0.02, init_pop=100, target_population=500, initiator=True), 8),
     ("h2o_sto2g", dict(tau=0.01, init_pop=100, target_population=200, real_amplitudes=True, initial_shift=3.0), 10),
-    ("mol26", dict(tau=1e-3, init_pop=10, target_population=500, real_amplitudes=True, initial_shift=0.0,
+    ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
                    pattempt_single=0.1, pattempt_double=0.9), 5),
-    ("mol26", dict(tau=1e-3, init_pop=10, target_population=500, real_amplitudes=True, initiator=True,
-                   initial_shift=0.0), 5),
-    ("mol40_w2", dict(tau=1e-3, init_pop=10, target_population=300, real_amplitudes=True, initial_shift=0.0,
+    ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True, initiator=True), 5),
+    ("mol40_w2", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
                       excit_gen="no_renorm"), 4),
 ]
 
@@ -148,7 +147,7 @@ def test_whole_run_bit_exact(name, opts, nrep):
     """Whole FCIQMC runs: same counter-based streams, so the walker lists must
     agree exactly after every report; estimators agree to rounding."""
     s = SYS[name]
-    cfg = make_config(s, ncycles=10, seed=7, state_size=200000, spawned_state_size=200000, **opts)
+    cfg = make_config(s, ncycles=10, seed=7, state_size=1500000, spawned_state_size=1500000, **opts)
     o = Oracle(s, cfg)
     g = engine(s, cfg)
     o.initial_distribution()
@@ -156,6 +155,7 @@ def test_whole_run_bit_exact(name, opts, nrep):
     for r in range(nrep):
         ro = o.run_report()
         rg = g.run_report()
+        assert ro.error_flags == 0 and rg.error_flags == 0, "list capacity too small for a parity run"
         so, po, ko = o.walkers()
         sg, pg, kg = g.walkers()
         np.testing.assert_array_equal(sg, so, err_msg="report %d states" % r)

@@ -38,15 +38,16 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "spawn attempts/s & iter time @1 GB300: FP32-batched vs FP64 plain at equal E_proj σ"
-WORKLOAD = "config2: synthetic molecule M=26 nel=10 C1, real amplitudes, cutoff 0.01, uniform renorm p_double=0.9, tau=1e-3, target 1e7, FP64"
+WORKLOAD = ("config2: synthetic molecule M=26 nel=10 C1, real amplitudes, cutoff 0.01, uniform renorm p_double=0.9, "
+            "tau=1e-3, ~1e7 walkers, FP64; each step = one full cycle on the same device-grown walker list")
 
 
 def system_and_config(target=1e7, seed_ham=2024, seed_rng=7, cap_main=None, cap_spawn=None):
     from hande_gb300 import systems
     from hande_gb300._abi import make_config
     s = systems.synthetic_molecule(26, 10, seed=seed_ham)
-    cm = cap_main or int(7 * target) + 200000
-    cs = cap_spawn or int(6 * target) + 200000
+    cm = cap_main or int(4 * target) + 200000
+    cs = cap_spawn or int(4 * target) + 200000
     cfg = make_config(s, tau=1e-3, init_pop=10, target_population=target, ncycles=10, seed=seed_rng,
                       real_amplitudes=True, spawn_cutoff=0.01, excit_gen="renorm", pattempt_single=0.1,
                       pattempt_double=0.9, state_size=cm, spawned_state_size=cs)
@@ -124,17 +125,21 @@ def pinned_array(rt, shape, dtype):
     return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape), p
 
 
-def grow(eng, max_reports=60):
+def grow(eng, target, max_cycles=400, verbose=False):
+    """Grow from the reference, one cycle at a time, until the population
+    reaches half the target (the benchmark Hamiltonian grows about 3x per cycle
+    at tau = 1e-3, so the list ends between 0.5x and 1.5x the target)."""
     rep = None
-    settled = 0
-    for _ in range(max_reports):
-        rep = eng.run_report()
+    for c in range(max_cycles):
+        eng.run_cycles(1)
+        rep = eng.end_report()
+        if verbose:
+            sys.stderr.write("grow %d Nw=%.4g states=%d shift=%.3f\n" % (c, rep.nparticles[0], rep.nstates,
+                                                                         rep.shift[0]))
         if rep.error_flags:
             raise RuntimeError("walker list overflow while growing (flags %d)" % rep.error_flags)
-        if rep.vary_shift[0]:
-            settled += 1
-            if settled >= 3:
-                break
+        if rep.nparticles[0] >= 0.5 * target:
+            break
     return rep
 
 
@@ -246,8 +251,13 @@ def main():
     s, cfg = system_and_config(target=args.target, seed_rng=7 + rank)
     eng = Engine(s, cfg)
     eng.initial_distribution()
-    grow(eng)
-    eng.run_cycles(args.warmup)
+    grown = grow(eng, args.target, verbose=bool(os.environ.get("HGPU_BENCH_VERBOSE")))
+    # the step input: this walker list, restored (device to device, untimed)
+    # before every cycle
+    eng.snapshot()
+    for _ in range(args.warmup):
+        eng.snapshot(restore=True)
+        eng.run_cycles(1)
     eng.end_report()
 
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
@@ -255,13 +265,20 @@ def main():
         dist.barrier()
     clocks.start()
     time.sleep(0.3)
-    rc = eng.run_cycles(args.steps)  # synchronises the engine stream at the end
-    rep = eng.end_report()
+    dev_ms = 0.0
+    attempts = 0
+    flags = 0
+    for _ in range(args.steps):
+        eng.snapshot(restore=True)
+        eng.run_cycles(1)  # device-timed with events on the engine stream; synchronises
+        r1 = eng.end_report()
+        dev_ms += r1.device_ms
+        attempts += r1.nattempts
+        flags |= r1.error_flags
     clk = clocks.stop()
-    dev_ms = rep.device_ms
-    attempts = rep.nattempts
-    if rep.error_flags:
-        raise RuntimeError("walker list overflow during the timed cycles (flags %d, rc %d)" % (rep.error_flags, rc))
+    rep = grown
+    if flags:
+        raise RuntimeError("walker list overflow during the timed cycles (flags %d)" % flags)
     if dist:
         import torch
         t = torch.tensor([dev_ms, float(attempts)], dtype=torch.float64, device="cuda")
@@ -273,6 +290,7 @@ def main():
     ms_per_step = dev_ms / args.steps
 
     # per-phase times of one cycle and the HBM roofline figures
+    eng.snapshot(restore=True)
     phases, counts = eng.profile_cycle()
     from hande_gb300.measure import roofline_figures
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
@@ -281,12 +299,16 @@ def main():
 
     # end to end through the C ABI with host-resident walker lists
     rt = cudart()
+    eng.snapshot(restore=True)
     st, po, da = eng.walkers()
     n0 = st.shape[0]
     cap = int(n0 * 1.6) + 1000
     hst, _ = pinned_array(rt, (cap, s.nwords), np.int64)
     hpo, _ = pinned_array(rt, (cap, 1), np.int64)
     hda, _ = pinned_array(rt, (cap,), np.float64)
+    ost, _ = pinned_array(rt, (cap, s.nwords), np.int64)
+    opo, _ = pinned_array(rt, (cap, 1), np.int64)
+    oda, _ = pinned_array(rt, (cap,), np.float64)
     hst[:n0] = st
     hpo[:n0] = po
     hda[:n0] = da
@@ -298,15 +320,15 @@ def main():
     eng.end_report()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
+        n = n0  # every step starts from the same host walker list
         eng._check(L.hgpu_upload_walkers(eng.h, _p(hst, C.c_int64), _p(hpo, C.c_int64), _p(hda, C.c_double), n),
                    "upload")
         h2d += n * (8 * s.nwords + 8 + 8)
         eng.run_cycles(1)
         m = C.c_int64()
-        eng._check(L.hgpu_download_walkers(eng.h, _p(hst, C.c_int64), _p(hpo, C.c_int64), _p(hda, C.c_double),
+        eng._check(L.hgpu_download_walkers(eng.h, _p(ost, C.c_int64), _p(opo, C.c_int64), _p(oda, C.c_double),
                                            cap, C.byref(m)), "download")
-        n = m.value
-        d2h += n * (8 * s.nwords + 8 + 8)
+        d2h += m.value * (8 * s.nwords + 8 + 8)
     e2e_s = time.perf_counter() - t0
     e_rep = eng.end_report()
     e_att = e_rep.nattempts

@@ -42,6 +42,12 @@ struct hgpu_handle {
     // device staging for parity entry points
     void *scratch;
     size_t scratch_bytes;
+    // walker-list snapshot (hgpu_snapshot)
+    uint64_t *snap_dets;
+    int64_t *snap_pops;
+    double *snap_kii;
+    int64_t snap_n;
+    int64_t snap_abs[HGPU_MAX_SPACES];
 };
 
 #define CK(x)                                                \
@@ -702,6 +708,40 @@ int32_t hgpu_annihilate_fixed(hgpu_handle *h, const int64_t *sdata, int64_t n, i
     int flags = st.error_flags;
     if ((rc = write_state(h, &st))) return rc;
     return (flags & HGPU_FLAG_MAIN_OVERFLOW) ? HGPU_ERR_MAIN_OVERFLOW : HGPU_OK;
+}
+
+int32_t hgpu_snapshot(hgpu_handle *h, int32_t restore) {
+    if (!h) return HGPU_ERR_INVALID;
+    int W = h->W, R = h->R, rc;
+    DevState st;
+    if ((rc = read_state(h, &st))) return rc;
+    if (!restore) {
+        if (!h->snap_dets) {
+            if ((rc = dalloc(h, &h->snap_dets, (size_t)h->b.cap * W))) return rc;
+            if ((rc = dalloc(h, &h->snap_pops, (size_t)h->b.cap * R))) return rc;
+            if ((rc = dalloc(h, &h->snap_kii, (size_t)h->b.cap))) return rc;
+        }
+        int64_t n = st.n_main;
+        CK(cudaMemcpyAsync(h->snap_dets, h->b.dets[h->cur], sizeof(uint64_t) * W * n, cudaMemcpyDeviceToDevice,
+                           h->stream));
+        CK(cudaMemcpyAsync(h->snap_pops, h->b.pops[h->cur], sizeof(int64_t) * R * n, cudaMemcpyDeviceToDevice,
+                           h->stream));
+        CK(cudaMemcpyAsync(h->snap_kii, h->b.kii[h->cur], sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        h->snap_n = n;
+        for (int s = 0; s < HGPU_MAX_SPACES; s++) h->snap_abs[s] = st.abs_pop[s];
+        return HGPU_OK;
+    }
+    if (!h->snap_dets) return HGPU_ERR_INVALID;
+    int64_t n = h->snap_n;
+    CK(cudaMemcpyAsync(h->b.dets[h->cur], h->snap_dets, sizeof(uint64_t) * W * n, cudaMemcpyDeviceToDevice,
+                       h->stream));
+    CK(cudaMemcpyAsync(h->b.pops[h->cur], h->snap_pops, sizeof(int64_t) * R * n, cudaMemcpyDeviceToDevice,
+                       h->stream));
+    CK(cudaMemcpyAsync(h->b.kii[h->cur], h->snap_kii, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    st.n_main = n;
+    for (int s = 0; s < HGPU_MAX_SPACES; s++) st.abs_pop[s] = h->snap_abs[s];
+    return write_state(h, &st);
 }
 
 int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int64_t *counts) {

@@ -22,7 +22,7 @@ EXPORTS = [
     "hgpu_initial_distribution", "hgpu_upload_walkers", "hgpu_download_walkers", "hgpu_run_cycles",
     "hgpu_end_report", "hgpu_run_report", "hgpu_get_state", "hgpu_set_state", "hgpu_checkpoint",
     "hgpu_restore", "hgpu_eval_excitations", "hgpu_annihilate_fixed", "hgpu_eval_diagonal",
-    "hgpu_profile_cycle",
+    "hgpu_profile_cycle", "hgpu_snapshot",
 ]
 
 
@@ -66,6 +66,7 @@ def load_library(path: str = LIB_PATH):
     L.hgpu_annihilate_fixed.argtypes = [vp, P(C.c_int64), C.c_int64, C.c_int64]
     L.hgpu_eval_diagonal.argtypes = [vp, P(C.c_int64), C.c_int64, P(C.c_double)]
     L.hgpu_profile_cycle.argtypes = [vp, P(C.c_double), C.c_int32, P(C.c_int64)]
+    L.hgpu_snapshot.argtypes = [vp, C.c_int32]
     for name in EXPORTS:
         if name != "hgpu_error_string":
             getattr(L, name).restype = C.c_int32
@@ -175,6 +176,9 @@ class Engine:
         sd = np.ascontiguousarray(sdata, dtype=np.int64)
         return self._check(self.L.hgpu_annihilate_fixed(self.h, _p(sd, C.c_int64), sd.shape[0], iteration),
                            "hgpu_annihilate_fixed", allow=(4,))
+
+    def snapshot(self, restore: bool = False):
+        self._check(self.L.hgpu_snapshot(self.h, 1 if restore else 0), "hgpu_snapshot")
 
     PHASES = ["prep", "attempt_scan", "spawn", "sort", "self_annihilate", "merge", "end"]
 

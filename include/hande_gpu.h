@@ -237,6 +237,14 @@ int32_t hgpu_annihilate_fixed(hgpu_handle *h, const int64_t *sdata, int64_t n, i
 /* K_ii = slater_condon0(D_i) - H00 for n determinants (sc0_ptr). */
 int32_t hgpu_eval_diagonal(hgpu_handle *h, const int64_t *dets, int64_t n, double *kii);
 
+/* Save (restore = 0) or restore (restore = 1) the walker list and the
+ * population counters in device memory.  A benchmark or a caller that
+ * replays cycles from one walker distribution restores it before each cycle
+ * without a host round trip; the iteration counter keeps advancing, so every
+ * replay draws fresh random numbers.  (No counterpart in the reference; its
+ * nearest relative is reading a restart file, src/restart_hdf5.F90:539.) */
+int32_t hgpu_snapshot(hgpu_handle *h, int32_t restore);
+
 /* Run one cycle with device timestamps between its phases (the role of
  * HANDE's per-section timing report, parallel_timing_t in
  * lib/local/parallel.F90:80-88).  phase_ms[0..6]: prep (E_proj, nattempts,

@@ -135,10 +135,10 @@ RUNS = [
     ("hub_k_3x3_ms1", dict(tau=0.02, init_pop=100, target_population=500, initiator=True), 8),
     ("h2o_sto2g", dict(tau=0.01, init_pop=100, target_population=200, real_amplitudes=True, initial_shift=3.0), 10),
     ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
-                   pattempt_single=0.1, pattempt_double=0.9), 5),
+                   pattempt_single=0.1, pattempt_double=0.9), 3),
     ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True, initiator=True), 5),
     ("mol40_w2", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
-                      excit_gen="no_renorm"), 4),
+                      excit_gen="no_renorm"), 2),
 ]
 
 

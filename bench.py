@@ -302,7 +302,7 @@ def main():
     eng.snapshot(restore=True)
     st, po, da = eng.walkers()
     n0 = st.shape[0]
-    cap = int(n0 * 1.6) + 1000
+    cap = int(n0 * 4) + 1000
     hst, _ = pinned_array(rt, (cap, s.nwords), np.int64)
     hpo, _ = pinned_array(rt, (cap, 1), np.int64)
     hda, _ = pinned_array(rt, (cap,), np.float64)

@@ -19,7 +19,8 @@ OUT = os.path.join(HERE, "libhande_gpu.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["hgpu_kernels.cu", "hgpu_engine.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:

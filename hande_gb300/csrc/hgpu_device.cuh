@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "../../include/hande_gpu.h"
+#include "hgpu_fixed.h"
 
 namespace hgpu {
 
@@ -27,7 +28,24 @@ enum Purpose : uint32_t { P_NATTEMPT = 1, P_SPAWN = 2, P_DEATH = 3, P_ROUND_MAIN
 // Everything the kernels need to know about the system and the calculation.
 // Lives in device global memory; small tables are staged to shared memory by
 // the kernels that gather from them.
-struct DevSys {
+struct alignas(16) DevSys {
+    // exact diagonal energies (hgpu_fixed.h): E(D) = fx_const + sum_i h_i + sum_{i<j} pair_ij
+    fx128 fx_const;          // Ecore (read_in) or nalpha*nbeta*U/N (hub_k)
+    fx128 fx_E0;             // E(D_0)
+    const fx128 *fx_h1;      // [norb] h_pp
+    const fx128 *fx_pair;    // [2][norb][norb]: [0] opposite spins (pp|qq), [1] same spin (pp|qq)-(pq|qp)
+    const fx128 *fx_eps;     // [nbasis] hub_k single-particle energies
+    // exact reciprocal tables (values of 1.0/(double)x, so results are unchanged)
+    const double *inv;       // [inv_max+1]
+    int inv_max;
+    int pad_inv;
+    double pgen_ij;          // 2/(nel(nel-1))
+    const double *hub_pgen;  // [nvirt_alpha+1] 1/(nalpha nbeta (nvirt_alpha - forbidden)), renorm
+    const double *hub_pspawn;  // [nvirt_alpha+1] real_factor tau |U/N| / hub_pgen
+    const uint8_t *hub_allowed;  // [nvirt_alpha+1] 1/pgen > depsilon
+    double hub_pgen_nr, hub_pspawn_nr;  // no_renorm: constant p_gen and p_spawn
+    double d_nel, d_nelm1, d_nbasis, d_half_nbasis, d_nalpha, d_nbeta, d_nvirt_alpha, d_real_factor, d_cutoff;
+    double d_nbss[16];
     int kind, nbasis, nel, nalpha, nbeta, nw;
     int nvirt_alpha, nvirt_beta, nvirt;
     int nspaces;
@@ -85,9 +103,15 @@ __device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1) 
     }
 }
 
+// (double)(x >> 11) * 2^-53, built from its bit pattern on the integer pipes
+// (the value is exact, so this is the same number the conversion gives).
 __device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
-    uint64_t x = ((uint64_t)hi << 32) | lo;
-    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+    uint64_t k = (((uint64_t)hi << 32) | lo) >> 11;
+    if (k == 0) return 0.0;
+    int msb = 63 - __clzll((long long)k);
+    uint64_t man = (k << (52 - msb)) & ((1ull << 52) - 1);
+    uint64_t bits = ((uint64_t)(msb - 53 + 1023) << 52) | man;
+    return __longlong_as_double((long long)bits);
 }
 
 // Stream of uniforms in [0,1) for one (purpose, space, index, sub, iteration):
@@ -348,51 +372,63 @@ struct Ints<float> {
 __device__ __forceinline__ int ms_of(int p) { return (p & 1) ? -1 : 1; }
 __device__ __forceinline__ int ims_of(int p) { return (p & 1) ? 0 : 1; }  // 0 beta, 1 alpha
 
-// slater_condon0_mol (src/hamiltonian_molecular.f90:73-139), FP64.
+// Exact diagonal energy E(D) in units of 2^-96 (hgpu_fixed.h): the terms of
+// slater_condon0_mol (src/hamiltonian_molecular.f90:73-139) -- Ecore, h_ii,
+// (ii|jj) and, for parallel spins, -(ij|ji) -- or of slater_condon0_hub_k
+// (src/hamiltonian_hub_k.f90:91-132) -- nalpha*nbeta*U/N and the
+// single-particle energies -- accumulated in 128-bit integers.
 template <int W>
-__device__ double sc0_mol(const DevSys &s, const Det<W> &f) {
-    double h = s.ecore;
-    int occ[64 * W];
-    int n = 0;
+__device__ fx128 fx_energy(const DevSys &s, const Det<W> &f) {
+    fx128 e = s.fx_const;
+    if (s.kind == HGPU_SYS_HUB_K) {
+#pragma unroll
+        for (int k = 0; k < W; k++) {
+            uint64_t x = f.w[k];
+            while (x) {
+                int p = 64 * k + __ffsll((long long)x) - 1;
+                x &= x - 1;
+                e += s.fx_eps[p];
+            }
+        }
+        return e;
+    }
+    const int M = s.norb;
 #pragma unroll
     for (int k = 0; k < W; k++) {
         uint64_t x = f.w[k];
         while (x) {
-            occ[n++] = 64 * k + __ffsll((long long)x) - 1;
+            int i = 64 * k + __ffsll((long long)x) - 1;
             x &= x - 1;
-        }
-    }
-    for (int iel = 0; iel < n; iel++) {
-        int i = occ[iel];
-        h = h + Ints<double>::h1(s, i, i);
-        for (int jel = iel + 1; jel < n; jel++) {
-            int j = occ[jel];
-            h = h + Ints<double>::v2(s, i, j, i, j);
-            if (((i ^ j) & 1) == 0) h = h - Ints<double>::v2(s, i, j, j, i);
-        }
-    }
-    return h;
-}
-
-// slater_condon0_hub_k (src/hamiltonian_hub_k.f90:91-132).
-template <int W>
-__device__ double sc0_hub_k(const DevSys &s, const Det<W> &f) {
-    double h = (double)(s.nalpha * s.nbeta) * s.coulomb_k;
+            int si = i >> 1;
+            e += s.fx_h1[si];
+            const fx128 *opp = s.fx_pair + (size_t)si * M;
+            const fx128 *same = opp + (size_t)M * M;
+            // partners j > i
 #pragma unroll
-    for (int k = 0; k < W; k++) {
-        uint64_t x = f.w[k];
-        while (x) {
-            int p = 64 * k + __ffsll((long long)x) - 1;
-            x &= x - 1;
-            h = h + __ldg(&s.sp_eigv[p]);
+            for (int q = k; q < W; q++) {
+                uint64_t y = q == k ? x : f.w[q];
+                while (y) {
+                    int j = 64 * q + __ffsll((long long)y) - 1;
+                    y &= y - 1;
+                    e += (((i ^ j) & 1) == 0) ? same[j >> 1] : opp[j >> 1];
+                }
+            }
         }
     }
-    return h;
+    return e;
 }
 
+// slater_condon0 (sc0_ptr): nearest double to the exact sum.
 template <int W>
 __device__ __forceinline__ double sc0(const DevSys &s, const Det<W> &f) {
-    return s.kind == HGPU_SYS_HUB_K ? sc0_hub_k<W>(s, f) : sc0_mol<W>(s, f);
+    return fx_to_double(fx_energy<W>(s, f));
+}
+
+// dat(1) of a new walker: K_ii = <D_i|H|D_i> - E_HF (src/annihilation.f90:855),
+// the nearest double to the exact difference.
+template <int W>
+__device__ __forceinline__ double kii_of(const DevSys &s, const Det<W> &f) {
+    return fx_to_double(fx_energy<W>(s, f) - s.fx_E0);
 }
 
 // slater_condon1_mol_excit (src/hamiltonian_molecular.f90:199-259).
@@ -462,10 +498,10 @@ struct Attempt {
 };
 
 // stochastic_round_spawned_particle (src/stoch_utils.f90:87-136).
-__device__ __forceinline__ int64_t round_spawned(int64_t cutoff, double pspawn, RStream &rs) {
+__device__ __forceinline__ int64_t round_spawned(int64_t cutoff, double dcutoff, double pspawn, RStream &rs) {
     int64_t nspawn;
-    if (pspawn < (double)cutoff) {
-        nspawn = (pspawn > rs.next() * (double)cutoff) ? cutoff : 0;
+    if (pspawn < dcutoff) {
+        nspawn = (pspawn > rs.next() * dcutoff) ? cutoff : 0;
     } else {
         nspawn = (int64_t)pspawn;
         double padd = pspawn - (double)nspawn;
@@ -504,8 +540,9 @@ __device__ void attempt_hub_k(const DevSys &s, const HubTables &t, RStream &rs, 
     }
     // choose_ij_hub_k (src/excit_gen_hub_k.f90:469-532)
     double r = rs.next();
-    int ind = (int)(r * (double)s.nalpha * (double)s.nbeta) + 1;
-    int ii = (int)(((double)ind - 1.0) / (double)s.nbeta) + 1;
+    int ind = (int)(r * s.d_nalpha * s.d_nbeta) + 1;
+    // int((ind-1.0)/nbeta): exact for integers, so integer division gives it
+    int ii = (ind - 1) / s.nbeta + 1;
     int jj = ind - (ii - 1) * s.nbeta;
     int i = select_det<W>(oa, ii - 1);
     int j = select_det<W>(ob, jj - 1);
@@ -515,9 +552,9 @@ __device__ void attempt_hub_k(const DevSys &s, const HubTables &t, RStream &rs, 
     bool renorm = s.excit_gen != HGPU_EXCIT_GEN_NO_RENORM;
     double pgen, abs_h;
     int a = -1, b = -1;
+    int forbidden = 0;
     if (renorm) {
         // calc_pgen_hub_k (src/excit_gen_hub_k.f90:651-770)
-        int forbidden = 0;
 #pragma unroll
         for (int k = 0; k < W; k++) {
             uint64_t x = ua[k];
@@ -527,17 +564,18 @@ __device__ void attempt_hub_k(const DevSys &s, const HubTables &t, RStream &rs, 
                 if (tbit<W>(f, hub_partner(t, ij_sym, aa))) forbidden++;
             }
         }
-        pgen = 1.0 / (double)(s.nalpha * s.nbeta * (s.nvirt_alpha - forbidden));
-        out.allowed = 1.0 / pgen > 1.0e-12;
+        // p_gen, the allowed test and p_spawn from tables of the same expressions
+        pgen = s.hub_pgen[forbidden];
+        out.allowed = s.hub_allowed[forbidden] != 0;
         abs_h = fabs(s.coulomb_k);
     } else {
         // find_ab_hub_k (src/excit_gen_hub_k.f90:579-649)
-        int rr = (int)(rs.next() * (double)s.nvirt_alpha);
+        int rr = (int)(rs.next() * s.d_nvirt_alpha);
         a = select_det<W>(ua, rr);
         b = hub_partner(t, ij_sym, a);
         out.allowed = !tbit<W>(f, b);
         if (out.allowed) {
-            pgen = 1.0 / (double)(s.nalpha * s.nbeta * s.nvirt_alpha);
+            pgen = s.hub_pgen_nr;
             abs_h = fabs(s.coulomb_k);
         } else {
             pgen = 1.0;
@@ -545,13 +583,15 @@ __device__ void attempt_hub_k(const DevSys &s, const HubTables &t, RStream &rs, 
         }
     }
     out.pgen = pgen;
-    double pspawn = (double)s.real_factor * s.tau * abs_h / pgen;
-    int64_t nspawn = round_spawned(s.cutoff, pspawn, rs);
+    double pspawn;
+    if (renorm) pspawn = s.hub_pspawn[forbidden];
+    else pspawn = out.allowed ? s.hub_pspawn_nr : 0.0;
+    int64_t nspawn = round_spawned(s.cutoff, s.d_cutoff, pspawn, rs);
     if (nspawn != 0 || (complete && out.allowed)) {
         if (renorm) {
             // choose_ab_hub_k: redraw until b is unoccupied
             for (int it = 0;; it++) {
-                int rr = (int)(rs.next() * (double)s.nvirt_alpha);
+                int rr = (int)(rs.next() * s.d_nvirt_alpha);
                 a = select_det<W>(ua, rr);
                 b = hub_partner(t, ij_sym, a);
                 if (!tbit<W>(f, b)) break;
@@ -624,8 +664,8 @@ __device__ __forceinline__ int sym_of(const DevSys &s, int p) {
 
 template <int W>
 __device__ __forceinline__ int pick_a(const DevSys &s, int spin, double r) {
-    if (spin == 0) return (int)(r * (double)s.nbasis);
-    int k = (int)(r * (double)(s.nbasis / 2));
+    if (spin == 0) return (int)(r * s.d_nbasis);
+    int k = (int)(r * s.d_half_nbasis);
     return spin == -2 ? 2 * k + 1 : 2 * k;
 }
 
@@ -653,11 +693,11 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
             if (ok) {
                 int guard = 0;
                 for (;;) {
-                    i = select_det<W>(f.w, (int)(rs.next() * (double)s.nel));
+                    i = select_det<W>(f.w, (int)(rs.next() * s.d_nel));
                     int imsa = ims_of(i), isyma = sym_of<W>(s, i);
                     if (SU(d, imsa, isyma) != 0) {
                         for (;;) {
-                            int ind = (int)((double)s.nbss[isyma * 2 + imsa] * rs.next());
+                            int ind = (int)(s.d_nbss[isyma * 2 + imsa] * rs.next());
                             a = ssbf<W>(s, imsa, isyma, ind);
                             if (!tbit<W>(f, a) || ++guard > kMaxRedraw) break;
                         }
@@ -669,10 +709,10 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
             }
         } else {
             // find_ia_mol (src/excit_gen_mol.f90:950-1016)
-            i = select_det<W>(f.w, (int)(rs.next() * (double)s.nel));
+            i = select_det<W>(f.w, (int)(rs.next() * s.d_nel));
             int imsa = ims_of(i), isyma = sym_of<W>(s, i);
             int nb = s.nbss[isyma * 2 + imsa];
-            int ind = (int)((double)nb * rs.next());
+            int ind = (int)(s.d_nbss[isyma * 2 + imsa] * rs.next());
             if (nb == 0) {
                 ok = false;
             } else {
@@ -692,9 +732,9 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
                     int p = select_det<W>(f.w, k);
                     if (SU(d, ims_of(p), sym_of<W>(s, p)) == 0) ni--;
                 }
-                pg = 1.0 / (double)(ni * SU(d, ims_of(a), sym_of<W>(s, a)));
+                pg = s.inv[ni * SU(d, ims_of(a), sym_of<W>(s, a))];
             } else {
-                pg = 1.0 / (double)(s.nel * s.nbss[sym_of<W>(s, a) * 2 + ims_of(a)]);
+                pg = s.inv[s.nel * s.nbss[sym_of<W>(s, a) * 2 + ims_of(a)]];
             }
             pgen = s.pattempt_single * pg;
             hm = sc1_mol<W, Real>(s, f, i, a, perm1<W>(f, i, a));
@@ -705,15 +745,19 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
     } else {
         out.nexcit = 2;
         // choose_ij_mol (src/excit_gen_mol.f90:620-660)
-        double x = rs.next() * (double)s.nel * (double)(s.nel - 1) / 2.0;
+        double x = rs.next() * s.d_nel * s.d_nelm1 / 2.0;
         int ind = (int)x + 1;
-        int j_ind = (int)(1.50 + sqrt((double)(2 * ind) - 1.750));
+        // int(1.5 + sqrt(2 ind - 1.75)) is exactly the j with
+        // (j-1)(j-2)/2 < ind <= j(j-1)/2; found here in integer arithmetic
+        int j_ind = (int)(1.5f + sqrtf((float)(2 * ind) - 1.75f));
+        while (j_ind * (j_ind - 1) / 2 < ind) j_ind++;
+        while ((j_ind - 1) * (j_ind - 2) / 2 >= ind) j_ind--;
         int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
         int i = select_det<W>(f.w, i_ind - 1);
         int j = select_det<W>(f.w, j_ind - 1);
         int ij_sym = xsym(s, sym_of<W>(s, i), sym_of<W>(s, j));
         int ij_spin = ms_of(i) + ms_of(j);
-        double pgen_ij = 2.0 / (double)(s.nel * (s.nel - 1));
+        double pgen_ij = s.pgen_ij;
         out.from[0] = i;
         out.from[1] = j;
         int a = -1, b = -1;
@@ -745,7 +789,7 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
                         int nu = SU(d, imsb, isymb);
                         if (nu > 1 || (nu == 1 && (isymb != syma || ij_spin == 0))) {
                             for (;;) {
-                                int k = (int)((double)s.nbss[isymb * 2 + imsb] * rs.next());
+                                int k = (int)(s.d_nbss[isymb * 2 + imsb] * rs.next());
                                 b = ssbf<W>(s, imsb, isymb, k);
                                 if ((b != a && !tbit<W>(f, b)) || ++guard > kMaxRedraw) break;
                             }
@@ -777,7 +821,7 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
                 ok = false;
             } else {
                 for (int it = 0;; it++) {
-                    int k = (int)((double)nb * rs.next());
+                    int k = (int)(s.d_nbss[isymb * 2 + imsb] * rs.next());
                     b = ssbf<W>(s, imsb, isymb, k);
                     if (b != a || it >= kMaxRedraw) break;
                 }
@@ -806,8 +850,8 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
                         if (SU(d, 0, isymb) == 0) n_aij -= SU(d, 1, isyma);
                         if (SU(d, 1, isymb) == 0) n_aij -= SU(d, 0, isyma);
                     }
-                    p_aijb = 1.0 / (double)SU(d, imsa, syma);
-                    p_bija = 1.0 / (double)SU(d, imsb, symb);
+                    p_aijb = s.inv[SU(d, imsa, syma)];
+                    p_bija = s.inv[SU(d, imsb, symb)];
                 } else {
                     int is = ij_spin == -2 ? 0 : 1;
                     n_aij = ij_spin == -2 ? s.nvirt_beta : s.nvirt_alpha;
@@ -819,26 +863,26 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
                             n_aij -= SU(d, is, isyma);
                     }
                     if (syma == symb) {
-                        p_aijb = 1.0 / (double)(SU(d, imsa, syma) - 1);
-                        p_bija = 1.0 / (double)(SU(d, imsb, symb) - 1);
+                        p_aijb = s.inv[SU(d, imsa, syma) - 1];
+                        p_bija = s.inv[SU(d, imsb, symb) - 1];
                     } else {
-                        p_aijb = 1.0 / (double)SU(d, imsa, syma);
-                        p_bija = 1.0 / (double)SU(d, imsb, symb);
+                        p_aijb = s.inv[SU(d, imsa, syma)];
+                        p_bija = s.inv[SU(d, imsb, symb)];
                     }
                 }
-                pg = (1.0 / (double)n_aij) * (p_bija + p_aijb);
+                pg = s.inv[n_aij] * (p_bija + p_aijb);
             } else {
                 // calc_pgen_double_mol_no_renorm (src/excit_gen_mol.f90:1368-1445)
                 int n_aij = ij_spin == -2 ? s.nvirt_beta : (ij_spin == 0 ? s.nvirt : s.nvirt_alpha);
                 double p_bija, p_aijb;
                 if (syma == symb && imsa == imsb) {
-                    p_aijb = 1.0 / (double)(s.nbss[syma * 2 + imsa] - 1);
-                    p_bija = 1.0 / (double)(s.nbss[symb * 2 + imsb] - 1);
+                    p_aijb = s.inv[s.nbss[syma * 2 + imsa] - 1];
+                    p_bija = s.inv[s.nbss[symb * 2 + imsb] - 1];
                 } else {
-                    p_aijb = 1.0 / (double)s.nbss[syma * 2 + imsa];
-                    p_bija = 1.0 / (double)s.nbss[symb * 2 + imsb];
+                    p_aijb = s.inv[s.nbss[syma * 2 + imsa]];
+                    p_bija = s.inv[s.nbss[symb * 2 + imsb]];
                 }
-                pg = (1.0 / (double)n_aij) * (p_bija + p_aijb);
+                pg = s.inv[n_aij] * (p_bija + p_aijb);
             }
             pgen = s.pattempt_double * pgen_ij * pg;
             hm = sc2_mol<Real>(s, i, j, a, b, perm2<W>(f, i, j, a, b));
@@ -852,8 +896,8 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
     out.pgen = pgen;
     out.hmatel = h;
     double pspawn = s.tau * fabs(h) / pgen;
-    pspawn = pspawn * (double)s.real_factor;
-    int64_t nspawn = round_spawned(s.cutoff, pspawn, rs);
+    pspawn = pspawn * s.d_real_factor;
+    int64_t nspawn = round_spawned(s.cutoff, s.d_cutoff, pspawn, rs);
     if (nspawn > 0) nspawn = child_sign(h, parent, nspawn);
     out.nspawn = nspawn;
 }

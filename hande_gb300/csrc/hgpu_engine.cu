@@ -116,34 +116,70 @@ static int64_t capacity_entries(int64_t v, size_t bytes_per_entry, int64_t fallb
     return fallback;
 }
 
-static double host_sc0(const hgpu_system *sys, const uint64_t *f) {
-    // slater_condon0 on the host, same operation order as the device (for H00)
+// Exact-diagonal tables (hgpu_fixed.h) and E(D) on the host, same definition
+// as the device's fx_energy.
+struct FxTables {
+    fx128 cst;
+    std::vector<fx128> h1, pair, eps;
+};
+
+static void build_fx(const hgpu_system *sys, FxTables &t) {
+    if (sys->kind == HGPU_SYS_HUB_K) {
+        t.cst = fx_from_double((double)(sys->nalpha * sys->nbeta) * sys->coulomb_k);
+        t.eps.resize(sys->nbasis);
+        for (int p = 0; p < sys->nbasis; p++) t.eps[p] = fx_from_double(sys->sp_eigv[p]);
+        return;
+    }
+    int M = sys->norb;
+    auto tri0 = [](int64_t i, int64_t j) { return i * (i + 1) / 2 + j; };
+    auto v2 = [&](int p, int q, int r, int s) {  // (pq|rs), spatial
+        int64_t pq = p >= q ? tri0(p, q) : tri0(q, p);
+        int64_t rs = r >= s ? tri0(r, s) : tri0(s, r);
+        return sys->v2[pq >= rs ? tri0(pq, rs) : tri0(rs, pq)];
+    };
+    t.cst = fx_from_double(sys->ecore);
+    t.h1.resize(M);
+    t.pair.resize((size_t)2 * M * M);
+    for (int p = 0; p < M; p++) {
+        t.h1[p] = fx_from_double(sys->h1[p * M + p]);
+        for (int q = 0; q < M; q++) {
+            fx128 J = fx_from_double(v2(p, p, q, q));  // <ij|ij> = (ii|jj)
+            fx128 K = fx_from_double(v2(p, q, q, p));  // <ij|ji> = (ij|ji)
+            t.pair[(size_t)p * M + q] = J;
+            t.pair[(size_t)M * M + (size_t)p * M + q] = J - K;
+        }
+    }
+}
+
+static fx128 host_energy(const hgpu_system *sys, const FxTables &t, const uint64_t *f) {
+    fx128 e = t.cst;
     std::vector<int> occ;
     for (int p = 0; p < sys->nbasis; p++)
         if ((f[p >> 6] >> (p & 63)) & 1ull) occ.push_back(p);
     if (sys->kind == HGPU_SYS_HUB_K) {
-        double h = (double)(sys->nalpha * sys->nbeta) * sys->coulomb_k;
-        for (int p : occ) h = h + sys->sp_eigv[p];
-        return h;
+        for (int p : occ) e += t.eps[p];
+        return e;
     }
-    auto tri0 = [](int64_t i, int64_t j) { return i * (i + 1) / 2 + j; };
-    auto v2 = [&](int i, int j, int a, int b) {
-        int si = i >> 1, sj = j >> 1, sa = a >> 1, sb = b >> 1;
-        int64_t ia = si >= sa ? tri0(si, sa) : tri0(sa, si);
-        int64_t jb = sj >= sb ? tri0(sj, sb) : tri0(sb, sj);
-        return sys->v2[ia >= jb ? tri0(ia, jb) : tri0(jb, ia)];
-    };
-    double h = sys->ecore;
+    int M = sys->norb;
     for (size_t a = 0; a < occ.size(); a++) {
         int i = occ[a];
-        h = h + sys->h1[(i >> 1) * sys->norb + (i >> 1)];
+        e += t.h1[i >> 1];
         for (size_t c = a + 1; c < occ.size(); c++) {
             int j = occ[c];
-            h = h + v2(i, j, i, j);
-            if (((i ^ j) & 1) == 0) h = h - v2(i, j, j, i);
+            e += t.pair[(((i ^ j) & 1) == 0 ? (size_t)M * M : 0) + (size_t)(i >> 1) * M + (j >> 1)];
         }
     }
-    return h;
+    return e;
+}
+
+template <typename T>
+static int upload(hgpu_handle *h, const T *src, size_t n, const T **out) {
+    T *d;
+    int rc = dalloc(h, &d, n);
+    if (rc) return rc;
+    CK(cudaMemcpy(d, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+    *out = d;
+    return HGPU_OK;
 }
 
 static int build_system(hgpu_handle *h, const hgpu_system *sys) {
@@ -178,8 +214,52 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
     s.initiator_pop = c.initiator_pop;
     s.seed = (uint64_t)c.seed;
     for (int w = 0; w < kMaxWords; w++) s.f0[w] = w < s.nw ? c.ref_det[w] : 0;
-    s.H00 = host_sc0(sys, s.f0);
+    FxTables fx;
+    build_fx(sys, fx);
+    s.fx_const = fx.cst;
+    s.fx_E0 = host_energy(sys, fx, s.f0);
+    s.H00 = fx_to_double(s.fx_E0);
     int rc;
+    if (sys->kind == HGPU_SYS_HUB_K) {
+        if ((rc = upload(h, fx.eps.data(), fx.eps.size(), &s.fx_eps))) return rc;
+    } else {
+        if ((rc = upload(h, fx.h1.data(), fx.h1.size(), &s.fx_h1))) return rc;
+        if ((rc = upload(h, fx.pair.data(), fx.pair.size(), &s.fx_pair))) return rc;
+    }
+    // reciprocal table 1/x (x = 0..inv_max) and the FP64 constants of the generators
+    s.inv_max = 2 * sys->nbasis * (sys->nel + 1) + 16;
+    {
+        std::vector<double> inv((size_t)s.inv_max + 1);
+        for (int x = 0; x <= s.inv_max; x++) inv[x] = 1.0 / (double)x;
+        if ((rc = upload(h, inv.data(), inv.size(), &s.inv))) return rc;
+    }
+    s.pgen_ij = 2.0 / (double)(s.nel * (s.nel - 1));
+    s.d_nel = (double)s.nel;
+    s.d_nelm1 = (double)(s.nel - 1);
+    s.d_nbasis = (double)s.nbasis;
+    s.d_half_nbasis = (double)(s.nbasis / 2);
+    s.d_nalpha = (double)s.nalpha;
+    s.d_nbeta = (double)s.nbeta;
+    s.d_nvirt_alpha = (double)s.nvirt_alpha;
+    s.d_real_factor = (double)s.real_factor;
+    s.d_cutoff = (double)s.cutoff;
+    if (sys->kind == HGPU_SYS_HUB_K) {
+        int nv = s.nvirt_alpha;
+        std::vector<double> pg(nv + 1), ps(nv + 1);
+        std::vector<uint8_t> al(nv + 1);
+        double abs_h = std::fabs(sys->coulomb_k);
+        for (int f = 0; f <= nv; f++) {
+            // calc_pgen_hub_k and spawn_lattice_split_gen's p_spawn, per forbidden count
+            pg[f] = 1.0 / (double)(s.nalpha * s.nbeta * (nv - f));
+            al[f] = 1.0 / pg[f] > 1.0e-12 ? 1 : 0;
+            ps[f] = (double)s.real_factor * c.tau * abs_h / pg[f];
+        }
+        if ((rc = upload(h, pg.data(), pg.size(), &s.hub_pgen))) return rc;
+        if ((rc = upload(h, ps.data(), ps.size(), &s.hub_pspawn))) return rc;
+        if ((rc = upload(h, al.data(), al.size(), &s.hub_allowed))) return rc;
+        s.hub_pgen_nr = 1.0 / (double)(s.nalpha * s.nbeta * nv);
+        s.hub_pspawn_nr = (double)s.real_factor * c.tau * abs_h / s.hub_pgen_nr;
+    }
     double *sp;
     if ((rc = dalloc(h, &sp, sys->nbasis))) return rc;
     CK(cudaMemcpy(sp, sys->sp_eigv, sizeof(double) * sys->nbasis, cudaMemcpyHostToDevice));
@@ -234,6 +314,7 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
             s.nbss[sym * 2 + ims]++;
             s.orbsym[p] = (uint8_t)sym;
         }
+        for (int k = 0; k < 2 * kMaxSym; k++) s.d_nbss[k] = (double)s.nbss[k];
         h->b.nk = 0;
     } else {
         return HGPU_ERR_INVALID;
@@ -286,6 +367,10 @@ static int alloc_lists(hgpu_handle *h) {
     if ((rc = dalloc(h, &b.part_i, (size_t)kMaxBlocks * 4))) return rc;
     if ((rc = dalloc(h, &b.state, 1))) return rc;
     CK(cudaMemset(b.state, 0, sizeof(DevState)));
+    {
+        int64_t nh = (int64_t)kRadix * b.grid;
+        CK(cudaMemcpy(&b.state->n_hist, &nh, sizeof(nh), cudaMemcpyHostToDevice));
+    }
     CK(cudaMemset(b.part_i, 0, sizeof(int64_t) * kMaxBlocks * 4));
     CK(cudaMemset(b.part_d, 0, sizeof(double) * kMaxBlocks * 4));
     return HGPU_OK;
@@ -410,7 +495,9 @@ int32_t hgpu_initial_distribution(hgpu_handle *h) {
     DevState ds;
     int rc = read_state(h, &ds);
     if (rc) return rc;
+    int64_t nh = ds.n_hist;
     memset(&ds, 0, sizeof(ds));
+    ds.n_hist = nh;
     for (int s = 0; s < HGPU_MAX_SPACES; s++) {
         h->shift[s] = h->cfg.initial_shift;
         h->vary_shift[s] = 0;

@@ -176,6 +176,14 @@ struct LoadMKeep {
     const uint2 *a;
     __device__ uint2 operator()(int64_t i) const { return a[i]; }
 };
+struct LoadHist {
+    const uint32_t *a;
+    __device__ int64_t operator()(int64_t i) const { return (int64_t)a[i]; }
+};
+struct StoreHist {
+    uint32_t *out;
+    __device__ void operator()(int64_t i, int64_t ex, int64_t) const { out[i] = (uint32_t)ex; }
+};
 struct StoreMPos {
     uint2 *out;
     __device__ void operator()(int64_t i, uint2 ex, uint2) const { out[i] = ex; }
@@ -742,7 +750,7 @@ __global__ void __launch_bounds__(kBlock) k_merge_scatter(DevBuffers b, int R, i
             store_det<W>(odets, dst, d);
             for (int q = 0; q < R; q++) p[q] = b.upops[j * R + q];
             // insert_new_walker: dat(1) = sc0(det) - H00 (src/annihilation.f90:855)
-            okii[dst] = sc0<W>(s, d) - s.H00;
+            okii[dst] = kii_of<W>(s, d);
         }
         for (int q = 0; q < R; q++) opops[dst * R + q] = p[q];
         ap0 += p[0] < 0 ? -p[0] : p[0];
@@ -864,7 +872,7 @@ __global__ void __launch_bounds__(kBlock) k_eval_diagonal(const DevSys *gsys, co
     stage_sys(s, gsys);
     __syncthreads();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        kii[i] = sc0<W>(s, load_det<W>(dets, i)) - s.H00;
+        kii[i] = kii_of<W>(s, load_det<W>(dets, i));
 }
 
 template <int W>
@@ -925,7 +933,8 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
     for (int p = 0; p < b.sort_passes; p++) {
         int shift = p * kRadixBits;
         k_radix_up<W><<<b.grid, kRadix, 0, st>>>(kin, &S->n_spawn, shift, b.hist);
-        k_radix_scan<<<1, 1024, 0, st>>>(b.hist, kRadix * b.grid);
+        device_scan<int64_t>(b, LoadHist{b.hist}, StoreHist{b.hist}, &S->n_hist, b.scan_part, (int64_t *)nullptr,
+                             st);
         k_radix_down<W><<<b.grid, kRadix, 0, st>>>(kin, iin, b.keys[o], b.idx[o], &S->n_spawn, shift, b.hist);
         kin = b.keys[o];
         iin = b.idx[o];
@@ -977,9 +986,9 @@ void launch_cycle(const DevBuffers &b, int W, int R, int kind, int precision, in
 }
 
 int launches_per_cycle(const DevBuffers &b) {
-    // begin, prep, count, scan(3), spawn, clamp, sort(3/pass), seg_reduce,
+    // begin, prep, count, scan(3), spawn, clamp, sort(5/pass), seg_reduce,
     // scan(3), compact, merge_spawn, merge_main, count, scan(3), scatter, end
-    return 2 + 1 + 3 + 1 + 1 + 3 * b.sort_passes + 1 + 3 + 1 + 2 + 1 + 3 + 1 + 1;
+    return 2 + 1 + 3 + 1 + 1 + 5 * b.sort_passes + 1 + 3 + 1 + 2 + 1 + 3 + 1 + 1;
 }
 
 void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st) {

@@ -26,6 +26,7 @@ struct DevState {
     int64_t n_merged_keep; // uint2 (kept main, kept total) after the merge
     int64_t n_slots;       // N * nspaces
     int64_t n_merged;      // N + U
+    int64_t n_hist;        // kRadix * grid (length of the radix histogram)
     int64_t iter;          // current iteration (cycle number, 1-based)
     double shift[HGPU_MAX_SPACES];
     int64_t abs_pop[HGPU_MAX_SPACES];  // exact sum |pop| of the main list (encoded units)

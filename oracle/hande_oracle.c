@@ -123,6 +123,9 @@ struct oracle_ctx {
     int R;
     uint64_t f0[MAXW];
     double H00;
+    /* exact diagonal: terms on the 2^-96 grid (see fx_energy) */
+    __int128 fx_cst, fx_E0;
+    __int128 *fx_h1, *fx_J, *fx_JK, *fx_eps;
     /* main list */
     int64_t n, cap;
     uint64_t *dets;
@@ -271,13 +274,37 @@ static double two_e_int_hub_k(const oracle_ctx *c, int p1, int p2, int p3, int p
     return 0.0;
 }
 
-/* slater_condon0_hub_k (src/hamiltonian_hub_k.f90:91-132). */
-static double sc0_hub_k(const oracle_ctx *c, const uint64_t *f) {
+/* Exact diagonal energies.  <D|H|D> (slater_condon0_hub_k,
+ * src/hamiltonian_hub_k.f90:91-132; slater_condon0_mol,
+ * src/hamiltonian_molecular.f90:73-139) is evaluated as the exact sum of the
+ * same terms, each rounded once to a multiple of 2^-96 (ties to even) and
+ * accumulated in 128-bit integers, then rounded once to double.  HANDE sums
+ * the terms left to right in FP64; the two differ by a few ulps. */
+static __int128 fx_of(double x) {
+    double y = ldexp(x, 96);  /* exact */
+    return (__int128)rint(y); /* nearest integer, ties to even (default rounding mode) */
+}
+
+static double fx_val(__int128 v) { return ldexp((double)v, -96); /* one rounding */ }
+
+static __int128 fx_energy(const oracle_ctx *c, const uint64_t *f) {
     int occ[MAXB];
     int n = decode(c, f, occ);
-    double h = (double)(c->nalpha * c->nbeta) * c->coulomb_k;
-    for (int i = 0; i < n; i++) h = h + c->sp_eigv[occ[i]];
-    return h;
+    __int128 e = c->fx_cst;
+    if (c->kind == HGPU_SYS_HUB_K) {
+        for (int i = 0; i < n; i++) e += c->fx_eps[occ[i]];
+        return e;
+    }
+    for (int a = 0; a < n; a++) {
+        int i = occ[a];
+        e += c->fx_h1[i >> 1];
+        for (int b = a + 1; b < n; b++) {
+            int j = occ[b];
+            int k = (i >> 1) * c->norb + (j >> 1);
+            e += (c->orb_ms[i] == c->orb_ms[j]) ? c->fx_JK[k] : c->fx_J[k];
+        }
+    }
+    return e;
 }
 
 /* slater_condon2_hub_k_excit (src/hamiltonian_hub_k.f90:163-234). */
@@ -365,23 +392,6 @@ static inline double v2_get(const oracle_ctx *c, int i, int j, int a, int b) {
 static inline double h1_get(const oracle_ctx *c, int i, int j) { return c->h1[(i >> 1) * c->norb + (j >> 1)]; }
 
 static inline int ims_of(const oracle_ctx *c, int p) { return (c->orb_ms[p] + 1) / 2; } /* 0 beta, 1 alpha */
-
-/* slater_condon0_mol (src/hamiltonian_molecular.f90:73-139). */
-static double sc0_mol(const oracle_ctx *c, const uint64_t *f) {
-    int occ[MAXB];
-    int n = decode(c, f, occ);
-    double h = c->ecore;
-    for (int iel = 0; iel < n; iel++) {
-        int i = occ[iel];
-        h = h + h1_get(c, i, i);
-        for (int jel = iel + 1; jel < n; jel++) {
-            int j = occ[jel];
-            h = h + v2_get(c, i, j, i, j);
-            if (c->orb_ms[i] == c->orb_ms[j]) h = h - v2_get(c, i, j, j, i);
-        }
-    }
-    return h;
-}
 
 /* slater_condon1_mol_excit (src/hamiltonian_molecular.f90:199-259). */
 static double sc1_mol_excit(const oracle_ctx *c, const int *occ, int i, int a, int perm) {
@@ -776,9 +786,10 @@ static void attempt(const oracle_ctx *c, rstream *rs, const uint64_t *f, const d
     else attempt_mol(c, rs, f, d, parent, out);
 }
 
-static double sc0(const oracle_ctx *c, const uint64_t *f) {
-    return c->kind == HGPU_SYS_HUB_K ? sc0_hub_k(c, f) : sc0_mol(c, f);
-}
+static double sc0(const oracle_ctx *c, const uint64_t *f) { return fx_val(fx_energy(c, f)); }
+
+/* dat(1) = K_ii = <D_i|H|D_i> - E_HF (src/annihilation.f90:855), from the exact difference. */
+static double kii_of(const oracle_ctx *c, const uint64_t *f) { return fx_val(fx_energy(c, f) - c->fx_E0); }
 
 /* get_hmatel_hub_k (src/hamiltonian_hub_k.f90:12-89) / get_hmatel_mol
  * (src/hamiltonian_molecular.f90:12-65). */
@@ -1149,7 +1160,7 @@ static void insert_new_walkers(oracle_ctx *c) {
         if (take_spawn) {
             memcpy(&nd[k * c->nw], &c->sdets[j * c->nw], sizeof(uint64_t) * c->nw);
             memcpy(&np[k * c->R], &c->spops[j * c->R], sizeof(int64_t) * c->R);
-            nk[k] = sc0(c, &c->sdets[j * c->nw]) - c->H00;
+            nk[k] = kii_of(c, &c->sdets[j * c->nw]);
             j++;
         } else {
             memcpy(&nd[k * c->nw], &c->dets[i * c->nw], sizeof(uint64_t) * c->nw);
@@ -1323,7 +1334,28 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
         c->pattempt_double = 1.0 - cfg->pattempt_single;
     }
     for (int w = 0; w < MAXW; w++) c->f0[w] = w < c->nw ? cfg->ref_det[w] : 0;
-    c->H00 = sc0(c, c->f0);
+    if (c->kind == HGPU_SYS_HUB_K) {
+        c->fx_cst = fx_of((double)(c->nalpha * c->nbeta) * c->coulomb_k);
+        c->fx_eps = (__int128 *)malloc(sizeof(__int128) * c->nbasis);
+        for (int p = 0; p < c->nbasis; p++) c->fx_eps[p] = fx_of(c->sp_eigv[p]);
+    } else {
+        int M = c->norb;
+        c->fx_cst = fx_of(c->ecore);
+        c->fx_h1 = (__int128 *)malloc(sizeof(__int128) * M);
+        c->fx_J = (__int128 *)malloc(sizeof(__int128) * M * M);
+        c->fx_JK = (__int128 *)malloc(sizeof(__int128) * M * M);
+        for (int p = 0; p < M; p++) {
+            c->fx_h1[p] = fx_of(c->h1[p * M + p]);
+            for (int q = 0; q < M; q++) {
+                __int128 J = fx_of(v2_get(c, 2 * p, 2 * q, 2 * p, 2 * q)); /* <ij|ij> = (ii|jj) */
+                __int128 K = fx_of(v2_get(c, 2 * p, 2 * q, 2 * q, 2 * p)); /* <ij|ji> = (ij|ji) */
+                c->fx_J[p * M + q] = J;
+                c->fx_JK[p * M + q] = J - K;
+            }
+        }
+    }
+    c->fx_E0 = fx_energy(c, c->f0);
+    c->H00 = fx_val(c->fx_E0);
     c->cap = cfg->walker_length > 0 ? cfg->walker_length : 1000000;
     c->scap = cfg->spawned_walker_length > 0 ? cfg->spawned_walker_length : 1000000;
     c->dets = (uint64_t *)calloc((size_t)(c->cap * c->nw), sizeof(uint64_t));
@@ -1342,6 +1374,7 @@ void oracle_destroy(oracle_ctx *c) {
     if (!c) return;
     free(c->orb_sym); free(c->orb_ms); free(c->sp_eigv);
     free(c->sym_table); free(c->inv_sym); free(c->h1); free(c->v2); free(c->nbss); free(c->ssbf);
+    free(c->fx_h1); free(c->fx_J); free(c->fx_JK); free(c->fx_eps);
     free(c->dets); free(c->pops); free(c->kii);
     free(c->sdets); free(c->spops); free(c->sflag); free(c->sord); free(c->suid);
     free(c);
@@ -1366,7 +1399,7 @@ int oracle_set_walkers(oracle_ctx *c, const int64_t *states, const int64_t *pops
     c->n = n;
     memcpy(c->dets, states, sizeof(uint64_t) * c->nw * n);
     memcpy(c->pops, pops, sizeof(int64_t) * c->R * n);
-    for (int64_t i = 0; i < n; i++) c->kii[i] = dat ? dat[i] : sc0(c, &c->dets[i * c->nw]) - c->H00;
+    for (int64_t i = 0; i < n; i++) c->kii[i] = dat ? dat[i] : kii_of(c, &c->dets[i * c->nw]);
     for (int s = 0; s < c->R; s++) c->nparticles_old[s] = nparticles(c, s);
     return 0;
 }

@@ -1,0 +1,122 @@
+! hande_gpu_m.f90 -- ISO_C_BINDING interface to the GB300 FCIQMC engine
+! (include/hande_gpu.h).  A HANDE build links libhande_gpu.so and replaces the
+! body of the Monte Carlo cycle loop of do_fciqmc (src/fciqmc.f90:307-413) and
+! the estimator part of end_report_loop with calls to these procedures.
+!
+! The derived types mirror the C structs field for field (bind(c)); keep the
+! two in step.  This module is compiled only where a Fortran compiler exists.
+module hande_gpu_m
+
+    use, intrinsic :: iso_c_binding, only: c_int32_t, c_int64_t, c_double, c_ptr, c_char, &
+                                           c_null_ptr, c_uint64_t => c_int64_t
+    implicit none
+
+    integer(c_int32_t), parameter :: HGPU_OK = 0
+    integer(c_int32_t), parameter :: HGPU_SYS_HUB_K = 1, HGPU_SYS_READ_IN = 2
+    integer(c_int32_t), parameter :: HGPU_PREC_FP64 = 0, HGPU_PREC_MIXED = 1
+    integer, parameter :: HGPU_MAX_WORDS = 2, HGPU_MAX_SPACES = 2
+
+    type, bind(c) :: hgpu_system
+        integer(c_int32_t) :: kind, nbasis, nel, nalpha, nbeta, nwords
+        type(c_ptr) :: orb_sym, orb_ms, sp_eigv
+        integer(c_int32_t) :: nkpoints
+        type(c_ptr) :: sym_table, inv_sym
+        real(c_double) :: coulomb_k
+        integer(c_int32_t) :: norb, nsym_pg
+        type(c_ptr) :: h1, v2
+        integer(c_int64_t) :: nv2
+        real(c_double) :: ecore
+        type(c_ptr) :: nbasis_sym_spin
+        integer(c_int32_t) :: max_sym_spin
+        type(c_ptr) :: sym_spin_basis_fns
+    end type hgpu_system
+
+    type, bind(c) :: hgpu_config
+        real(c_double) :: tau, shift_damping, initial_shift, vary_shift_from, target_particles
+        real(c_double) :: initiator_pop, spawn_cutoff, pattempt_single, pattempt_double, D0_population
+        integer(c_int32_t) :: vary_shift_from_proje, excit_gen, real_amplitudes, initiator_approx
+        integer(c_int32_t) :: nspaces, ncycles, precision, reserved0
+        integer(c_int64_t) :: seed, walker_length, spawned_walker_length
+        integer(c_uint64_t) :: ref_det(HGPU_MAX_WORDS)
+    end type hgpu_config
+
+    type, bind(c) :: hgpu_report
+        integer(c_int64_t) :: iteration
+        real(c_double) :: shift(HGPU_MAX_SPACES), proj_energy(HGPU_MAX_SPACES)
+        real(c_double) :: D0_population(HGPU_MAX_SPACES), nparticles(HGPU_MAX_SPACES)
+        integer(c_int32_t) :: vary_shift(HGPU_MAX_SPACES)
+        integer(c_int64_t) :: nstates, nspawn_events
+        real(c_double) :: rspawn
+        integer(c_int64_t) :: nattempts, nspawned
+        integer(c_int32_t) :: error_flags, reserved0
+        real(c_double) :: device_ms
+    end type hgpu_report
+
+    interface
+        integer(c_int32_t) function hgpu_create(cfg, sys, h) bind(c, name='hgpu_create')
+            import :: hgpu_config, hgpu_system, c_ptr, c_int32_t
+            type(hgpu_config), intent(in) :: cfg
+            type(hgpu_system), intent(in) :: sys
+            type(c_ptr), intent(out) :: h
+        end function hgpu_create
+
+        integer(c_int32_t) function hgpu_destroy(h) bind(c, name='hgpu_destroy')
+            import :: c_ptr, c_int32_t
+            type(c_ptr), value :: h
+        end function hgpu_destroy
+
+        integer(c_int32_t) function hgpu_initial_distribution(h) bind(c, name='hgpu_initial_distribution')
+            import :: c_ptr, c_int32_t
+            type(c_ptr), value :: h
+        end function hgpu_initial_distribution
+
+        integer(c_int32_t) function hgpu_upload_walkers(h, states, pops, dat, n) bind(c, name='hgpu_upload_walkers')
+            import :: c_ptr, c_int32_t, c_int64_t, c_double
+            type(c_ptr), value :: h
+            integer(c_int64_t), intent(in) :: states(*), pops(*)
+            real(c_double), intent(in) :: dat(*)
+            integer(c_int64_t), value :: n
+        end function hgpu_upload_walkers
+
+        integer(c_int32_t) function hgpu_download_walkers(h, states, pops, dat, capacity, n_out) &
+                bind(c, name='hgpu_download_walkers')
+            import :: c_ptr, c_int32_t, c_int64_t, c_double
+            type(c_ptr), value :: h
+            integer(c_int64_t), intent(out) :: states(*), pops(*)
+            real(c_double), intent(out) :: dat(*)
+            integer(c_int64_t), value :: capacity
+            integer(c_int64_t), intent(out) :: n_out
+        end function hgpu_download_walkers
+
+        integer(c_int32_t) function hgpu_run_cycles(h, ncycles) bind(c, name='hgpu_run_cycles')
+            import :: c_ptr, c_int32_t
+            type(c_ptr), value :: h
+            integer(c_int32_t), value :: ncycles
+        end function hgpu_run_cycles
+
+        integer(c_int32_t) function hgpu_end_report(h, rep) bind(c, name='hgpu_end_report')
+            import :: c_ptr, c_int32_t, hgpu_report
+            type(c_ptr), value :: h
+            type(hgpu_report), intent(out) :: rep
+        end function hgpu_end_report
+
+        integer(c_int32_t) function hgpu_run_report(h, rep) bind(c, name='hgpu_run_report')
+            import :: c_ptr, c_int32_t, hgpu_report
+            type(c_ptr), value :: h
+            type(hgpu_report), intent(out) :: rep
+        end function hgpu_run_report
+
+        integer(c_int32_t) function hgpu_checkpoint(h, path) bind(c, name='hgpu_checkpoint')
+            import :: c_ptr, c_int32_t, c_char
+            type(c_ptr), value :: h
+            character(kind=c_char), intent(in) :: path(*)
+        end function hgpu_checkpoint
+
+        integer(c_int32_t) function hgpu_restore(h, path) bind(c, name='hgpu_restore')
+            import :: c_ptr, c_int32_t, c_char
+            type(c_ptr), value :: h
+            character(kind=c_char), intent(in) :: path(*)
+        end function hgpu_restore
+    end interface
+
+end module hande_gpu_m

@@ -22,7 +22,7 @@ EXPORTS = [
     "hgpu_initial_distribution", "hgpu_upload_walkers", "hgpu_download_walkers", "hgpu_run_cycles",
     "hgpu_end_report", "hgpu_run_report", "hgpu_get_state", "hgpu_set_state", "hgpu_checkpoint",
     "hgpu_restore", "hgpu_eval_excitations", "hgpu_annihilate_fixed", "hgpu_eval_diagonal",
-    "hgpu_profile_cycle", "hgpu_snapshot",
+    "hgpu_profile_cycle", "hgpu_snapshot", "hgpu_self_annihilate_noalloc",
 ]
 
 
@@ -67,6 +67,7 @@ def load_library(path: str = LIB_PATH):
     L.hgpu_eval_diagonal.argtypes = [vp, P(C.c_int64), C.c_int64, P(C.c_double)]
     L.hgpu_profile_cycle.argtypes = [vp, P(C.c_double), C.c_int32, P(C.c_int64)]
     L.hgpu_snapshot.argtypes = [vp, C.c_int32]
+    L.hgpu_self_annihilate_noalloc.argtypes = [vp, C.c_int64, C.c_int32, C.c_int32, vp, P(C.c_int64), vp]
     for name in EXPORTS:
         if name != "hgpu_error_string":
             getattr(L, name).restype = C.c_int32

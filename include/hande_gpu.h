@@ -245,6 +245,32 @@ int32_t hgpu_eval_diagonal(hgpu_handle *h, const int64_t *dets, int64_t n, doubl
  * nearest relative is reading a restart file, src/restart_hdf5.F90:539.) */
 int32_t hgpu_snapshot(hgpu_handle *h, int32_t restore);
 
+/* Self-annihilation of a spawned list with no device allocation by the
+ * library.  For callers that cannot let a library allocate device memory: a
+ * host program whose pool allocator owns all device memory, or a caller that
+ * must not allocate on its critical path (cudaMalloc/cudaFree can synchronise
+ * the device).  No counterpart in the reference: it is an allocation-free form
+ * of annihilate_spawn_t after its qsort (src/spawn_data.F90:406, :859-935).
+ *
+ * d_sdata: device array (nwords + nspaces + 1, n) column-major, as for
+ * hgpu_annihilate_fixed (the flag word is ignored); d_out: device array with
+ * room for (nwords + nspaces, n) int64 -- receives the distinct determinants
+ * in ascending order with their summed populations, entries whose populations
+ * all cancel removed; *n_out (host): number of entries written.  stream: a
+ * cudaStream_t, or NULL for the default stream; the call returns when the
+ * work is done.
+ *
+ * Limits: n <= HGPU_NOALLOC_MAX_ENTRIES; larger lists are rejected with
+ * HGPU_ERR_INVALID and *n_out = -HGPU_NOALLOC_MAX_ENTRIES.  The working space
+ * is one fixed array (about 5 MB) inside the library, held on every GPU that
+ * loads the library until the process exits.  The first call on a device looks
+ * up that array's device address, so make it with that device current.  Every
+ * call uses the same array: calls that overlap on the GPU (e.g. on two streams
+ * or from two host threads) race; order them. */
+#define HGPU_NOALLOC_MAX_ENTRIES 65536
+int32_t hgpu_self_annihilate_noalloc(const int64_t *d_sdata, int64_t n, int32_t nwords, int32_t nspaces,
+                                     int64_t *d_out, int64_t *n_out, void *stream);
+
 /* Run one cycle with device timestamps between its phases (the role of
  * HANDE's per-section timing report, parallel_timing_t in
  * lib/local/parallel.F90:80-88).  phase_ms[0..6]: prep (E_proj, nattempts,

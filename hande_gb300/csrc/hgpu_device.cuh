@@ -29,12 +29,16 @@ enum Purpose : uint32_t { P_NATTEMPT = 1, P_SPAWN = 2, P_DEATH = 3, P_ROUND_MAIN
 // Lives in device global memory; small tables are staged to shared memory by
 // the kernels that gather from them.
 struct alignas(16) DevSys {
-    // exact diagonal energies (hgpu_fixed.h): E(D) = fx_const + sum_i h_i + sum_{i<j} pair_ij
-    fx128 fx_const;          // Ecore (read_in) or nalpha*nbeta*U/N (hub_k)
-    fx128 fx_E0;             // E(D_0)
-    const fx128 *fx_h1;      // [norb] h_pp
-    const fx128 *fx_pair;    // [2][norb][norb]: [0] opposite spins (pp|qq), [1] same spin (pp|qq)-(pq|qp)
-    const fx128 *fx_eps;     // [nbasis] hub_k single-particle energies
+    // exact diagonal energies (hgpu_fixed.h): E(D) = fx_const + sum_i h_i + sum_{i<j} pair_ij,
+    // in units of 2^-fx_shift
+    int64_t fx_const;          // Ecore (read_in) or nalpha*nbeta*U/N (hub_k)
+    int64_t fx_E0;             // E(D_0)
+    double fx_inv_scale;       // 2^-fx_shift
+    const int64_t *fx_h1;      // [norb] h_pp
+    const int64_t *fx_pair;    // [2][norb][norb]: [0] opposite spins (pp|qq), [1] same spin (pp|qq)-(pq|qp)
+    const int64_t *fx_eps;     // [nbasis] hub_k single-particle energies
+    int fx_shift;
+    int pad_fx;
     // exact reciprocal tables (values of 1.0/(double)x, so results are unchanged)
     const double *inv;       // [inv_max+1]
     int inv_max;
@@ -372,14 +376,14 @@ struct Ints<float> {
 __device__ __forceinline__ int ms_of(int p) { return (p & 1) ? -1 : 1; }
 __device__ __forceinline__ int ims_of(int p) { return (p & 1) ? 0 : 1; }  // 0 beta, 1 alpha
 
-// Exact diagonal energy E(D) in units of 2^-96 (hgpu_fixed.h): the terms of
+// Exact diagonal energy E(D) in units of 2^-fx_shift (hgpu_fixed.h): the terms of
 // slater_condon0_mol (src/hamiltonian_molecular.f90:73-139) -- Ecore, h_ii,
 // (ii|jj) and, for parallel spins, -(ij|ji) -- or of slater_condon0_hub_k
 // (src/hamiltonian_hub_k.f90:91-132) -- nalpha*nbeta*U/N and the
-// single-particle energies -- accumulated in 128-bit integers.
+// single-particle energies -- accumulated in 64-bit integers.
 template <int W>
-__device__ fx128 fx_energy(const DevSys &s, const Det<W> &f) {
-    fx128 e = s.fx_const;
+__device__ int64_t fx_energy(const DevSys &s, const Det<W> &f) {
+    int64_t e = s.fx_const;
     if (s.kind == HGPU_SYS_HUB_K) {
 #pragma unroll
         for (int k = 0; k < W; k++) {
@@ -401,8 +405,8 @@ __device__ fx128 fx_energy(const DevSys &s, const Det<W> &f) {
             x &= x - 1;
             int si = i >> 1;
             e += s.fx_h1[si];
-            const fx128 *opp = s.fx_pair + (size_t)si * M;
-            const fx128 *same = opp + (size_t)M * M;
+            const int64_t *opp = s.fx_pair + (size_t)si * M;
+            const int64_t *same = opp + (size_t)M * M;
             // partners j > i
 #pragma unroll
             for (int q = k; q < W; q++) {
@@ -421,14 +425,14 @@ __device__ fx128 fx_energy(const DevSys &s, const Det<W> &f) {
 // slater_condon0 (sc0_ptr): nearest double to the exact sum.
 template <int W>
 __device__ __forceinline__ double sc0(const DevSys &s, const Det<W> &f) {
-    return fx_to_double(fx_energy<W>(s, f));
+    return fx_to_double(fx_energy<W>(s, f), s.fx_inv_scale);
 }
 
 // dat(1) of a new walker: K_ii = <D_i|H|D_i> - E_HF (src/annihilation.f90:855),
 // the nearest double to the exact difference.
 template <int W>
 __device__ __forceinline__ double kii_of(const DevSys &s, const Det<W> &f) {
-    return fx_to_double(fx_energy<W>(s, f) - s.fx_E0);
+    return fx_to_double(fx_energy<W>(s, f) - s.fx_E0, s.fx_inv_scale);
 }
 
 // slater_condon1_mol_excit (src/hamiltonian_molecular.f90:199-259).

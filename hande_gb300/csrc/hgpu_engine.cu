@@ -119,15 +119,20 @@ static int64_t capacity_entries(int64_t v, size_t bytes_per_entry, int64_t fallb
 // Exact-diagonal tables (hgpu_fixed.h) and E(D) on the host, same definition
 // as the device's fx_energy.
 struct FxTables {
-    fx128 cst;
-    std::vector<fx128> h1, pair, eps;
+    int shift;
+    int64_t cst;
+    std::vector<int64_t> h1, pair, eps;
 };
 
 static void build_fx(const hgpu_system *sys, FxTables &t) {
     if (sys->kind == HGPU_SYS_HUB_K) {
-        t.cst = fx_from_double((double)(sys->nalpha * sys->nbeta) * sys->coulomb_k);
+        double c0 = (double)(sys->nalpha * sys->nbeta) * sys->coulomb_k;
+        int64_t B = fx_ceil_abs(c0);
+        for (int p = 0; p < sys->nbasis; p++) B += fx_ceil_abs(sys->sp_eigv[p]);
+        t.shift = fx_scale_for_bound(B);
+        t.cst = fx_from_double(c0, t.shift);
         t.eps.resize(sys->nbasis);
-        for (int p = 0; p < sys->nbasis; p++) t.eps[p] = fx_from_double(sys->sp_eigv[p]);
+        for (int p = 0; p < sys->nbasis; p++) t.eps[p] = fx_from_double(sys->sp_eigv[p], t.shift);
         return;
     }
     int M = sys->norb;
@@ -137,22 +142,33 @@ static void build_fx(const hgpu_system *sys, FxTables &t) {
         int64_t rs = r >= s ? tri0(r, s) : tri0(s, r);
         return sys->v2[pq >= rs ? tri0(pq, rs) : tri0(rs, pq)];
     };
-    t.cst = fx_from_double(sys->ecore);
+    // bound over every term of every determinant: spin orbitals i < j
+    int nb = sys->nbasis;
+    int64_t B = fx_ceil_abs(sys->ecore);
+    for (int i = 0; i < nb; i++) {
+        B += fx_ceil_abs(sys->h1[(i >> 1) * M + (i >> 1)]);
+        for (int j = i + 1; j < nb; j++) {
+            B += fx_ceil_abs(v2(i >> 1, i >> 1, j >> 1, j >> 1));
+            if (((i ^ j) & 1) == 0) B += fx_ceil_abs(v2(i >> 1, j >> 1, j >> 1, i >> 1));
+        }
+    }
+    t.shift = fx_scale_for_bound(B);
+    t.cst = fx_from_double(sys->ecore, t.shift);
     t.h1.resize(M);
     t.pair.resize((size_t)2 * M * M);
     for (int p = 0; p < M; p++) {
-        t.h1[p] = fx_from_double(sys->h1[p * M + p]);
+        t.h1[p] = fx_from_double(sys->h1[p * M + p], t.shift);
         for (int q = 0; q < M; q++) {
-            fx128 J = fx_from_double(v2(p, p, q, q));  // <ij|ij> = (ii|jj)
-            fx128 K = fx_from_double(v2(p, q, q, p));  // <ij|ji> = (ij|ji)
+            int64_t J = fx_from_double(v2(p, p, q, q), t.shift);  // <ij|ij> = (ii|jj)
+            int64_t K = fx_from_double(v2(p, q, q, p), t.shift);  // <ij|ji> = (ij|ji)
             t.pair[(size_t)p * M + q] = J;
             t.pair[(size_t)M * M + (size_t)p * M + q] = J - K;
         }
     }
 }
 
-static fx128 host_energy(const hgpu_system *sys, const FxTables &t, const uint64_t *f) {
-    fx128 e = t.cst;
+static int64_t host_energy(const hgpu_system *sys, const FxTables &t, const uint64_t *f) {
+    int64_t e = t.cst;
     std::vector<int> occ;
     for (int p = 0; p < sys->nbasis; p++)
         if ((f[p >> 6] >> (p & 63)) & 1ull) occ.push_back(p);
@@ -216,9 +232,11 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
     for (int w = 0; w < kMaxWords; w++) s.f0[w] = w < s.nw ? c.ref_det[w] : 0;
     FxTables fx;
     build_fx(sys, fx);
+    s.fx_shift = fx.shift;
+    s.fx_inv_scale = std::ldexp(1.0, -fx.shift);
     s.fx_const = fx.cst;
     s.fx_E0 = host_energy(sys, fx, s.f0);
-    s.H00 = fx_to_double(s.fx_E0);
+    s.H00 = fx_to_double(s.fx_E0, s.fx_inv_scale);
     int rc;
     if (sys->kind == HGPU_SYS_HUB_K) {
         if ((rc = upload(h, fx.eps.data(), fx.eps.size(), &s.fx_eps))) return rc;
@@ -358,6 +376,8 @@ static int alloc_lists(hgpu_handle *h) {
     if ((rc = dalloc(h, &b.udets, (size_t)b.scap * W))) return rc;
     if ((rc = dalloc(h, &b.upops, (size_t)b.scap * R))) return rc;
     if ((rc = dalloc(h, &b.uflag, (size_t)b.scap))) return rc;
+    if ((rc = dalloc(h, &b.ukii, (size_t)b.scap))) return rc;
+    if ((rc = dalloc(h, &b.msplit, ((size_t)b.cap + (size_t)b.scap) / kMergeTile + 2))) return rc;
     size_t merged = (size_t)b.cap + (size_t)b.scap;
     if ((rc = dalloc(h, &b.mref, merged))) return rc;
     if ((rc = dalloc(h, &b.mkeep, merged))) return rc;

@@ -638,81 +638,161 @@ __device__ __forceinline__ void round_pops(const DevSys &s, int64_t *p, int R, u
     }
 }
 
+// Merge path (Odeh, Green, Mwassi, Shmueli, Birk, "Merge Path", 2012) of the
+// sorted main list and the sorted unique spawned list, equal determinants with
+// the main entry first: the number of main entries among the first d merged
+// elements, for every tile boundary d = t * kMergeTile.
 template <int W>
-__global__ void __launch_bounds__(kBlock) k_merge_spawn(DevBuffers b, int R, int cur) {
-    __shared__ DevSys s;
-    stage_sys(s, b.sys);
-    __syncthreads();
-    int64_t U = b.state->n_uniq, N = b.state->n_main;
-    uint64_t iter = (uint64_t)b.state->iter;
+__global__ void __launch_bounds__(kBlock) k_merge_splits(DevBuffers b, int cur) {
+    int64_t U = b.state->n_uniq, N = b.state->n_main, L = N + U;
+    int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
     const uint64_t *mdets = b.dets[cur];
-    int64_t *mpops = b.pops[cur];
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < U; j += (int64_t)gridDim.x * blockDim.x) {
-        Det<W> d = load_det<W>(b.udets, j);
-        int64_t sp[2] = {0, 0};
-        for (int q = 0; q < R; q++) sp[q] = b.upops[j * R + q];
-        uint64_t fl = b.uflag[j];
-        int64_t pos = lower_bound_det<W>(mdets, N, d);
-        bool hit = pos < N && det_eq<W>(load_det<W>(mdets, pos), d);
-        int64_t rank;
-        uint32_t keep;
-        if (hit) {
-            // annihilate_main_list[_initiator] (src/annihilation.f90:294-486)
-            for (int q = 0; q < R; q++) {
-                int64_t m = mpops[pos * R + q];
-                if (!s.initiator || m != 0) m += sp[q];
-                else if (!((fl >> q) & 1)) m = sp[q];
-                mpops[pos * R + q] = m;
-            }
-            rank = j + pos + 1;
-            keep = 0;
-        } else {
-            bool discard = false;
-            if (s.initiator) {
-                discard = true;
-                for (int q = 0; q < R; q++) {
-                    if ((fl >> q) & 1) sp[q] = 0;
-                    else discard = false;
-                }
-            }
-            if (!discard && s.real_amplitudes) round_pops(s, sp, R, P_ROUND_SPAWN, j, iter);
-            bool nz = false;
-            for (int q = 0; q < R; q++) {
-                b.upops[j * R + q] = sp[q];
-                nz = nz || sp[q] != 0;
-            }
-            keep = discard ? 0u : (s.real_amplitudes ? (nz ? 1u : 0u) : 1u);
-            rank = j + pos;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t d = t * kMergeTile < L ? t * kMergeTile : L;
+        int64_t lo = d - U > 0 ? d - U : 0, hi = d < N ? d : N;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) >> 1;
+            // main[mid] precedes spawn[d-1-mid] when main[mid] <= spawn[d-1-mid]
+            if (!det_less<W>(load_det<W>(b.udets, d - 1 - mid), load_det<W>(mdets, mid))) lo = mid + 1;
+            else hi = mid;
         }
-        b.mref[rank] = -(j + 1);
-        b.mkeep[rank] = make_uint2(0u, keep);
+        b.msplit[t] = lo;
     }
 }
 
+// One tile of the merged sequence per iteration: annihilate_main_list[_initiator]
+// (src/annihilation.f90:294-486), remove_unoccupied_dets' rounding (:537-598),
+// round_low_population_spawns (:600-675), the merged rank of every element and,
+// densely over the tile's new determinants, their K_ii (insert_new_walker :855).
 template <int W>
-__global__ void __launch_bounds__(kBlock) k_merge_main(DevBuffers b, int R, int cur) {
+__global__ void __launch_bounds__(kBlock) k_merge_tiles(DevBuffers b, int R, int cur) {
     __shared__ DevSys s;
+    __shared__ uint64_t tdet[kMergeTile * W];
+    __shared__ int32_t newlist[kMergeTile];
+    __shared__ int nnew;
     stage_sys(s, b.sys);
     __syncthreads();
-    int64_t U = b.state->n_uniq, N = b.state->n_main;
+    int64_t U = b.state->n_uniq, N = b.state->n_main, L = N + U;
     uint64_t iter = (uint64_t)b.state->iter;
+    int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
     const uint64_t *mdets = b.dets[cur];
     int64_t *mpops = b.pops[cur];
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        Det<W> d = load_det<W>(mdets, i);
-        int64_t lb = U > 0 ? lower_bound_det<W>(b.udets, U, d) : 0;
-        int64_t p[2] = {0, 0};
-        for (int q = 0; q < R; q++) p[q] = mpops[i * R + q];
-        // remove_unoccupied_dets (src/annihilation.f90:537-598)
-        if (s.real_amplitudes) {
-            round_pops(s, p, R, P_ROUND_MAIN, i, iter);
-            for (int q = 0; q < R; q++) mpops[i * R + q] = p[q];
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int64_t d0 = t * kMergeTile, d1 = d0 + kMergeTile < L ? d0 + kMergeTile : L;
+        int64_t i0 = b.msplit[t], i1 = b.msplit[t + 1];
+        int64_t j0 = d0 - i0, j1 = d1 - i1;
+        int nm = (int)(i1 - i0), ns = (int)(j1 - j0);
+        for (int k = threadIdx.x; k < nm + ns; k += blockDim.x) {
+            Det<W> d = k < nm ? load_det<W>(mdets, i0 + k) : load_det<W>(b.udets, j0 + (k - nm));
+#pragma unroll
+            for (int w = 0; w < W; w++) tdet[k * W + w] = d.w[w];
         }
-        bool nz = false;
-        for (int q = 0; q < R; q++) nz = nz || p[q] != 0;
-        int64_t rank = i + lb;
-        b.mref[rank] = i;
-        b.mkeep[rank] = make_uint2(nz ? 1u : 0u, nz ? 1u : 0u);
+        if (threadIdx.x == 0) nnew = 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < nm + ns; k += blockDim.x) {
+            Det<W> d;
+#pragma unroll
+            for (int w = 0; w < W; w++) d.w[w] = tdet[k * W + w];
+            if (k < nm) {
+                // main entry: how many tile spawns are strictly below it
+                int lo = 0, hi = ns;
+                while (lo < hi) {
+                    int mid = (lo + hi) >> 1;
+                    Det<W> x;
+#pragma unroll
+                    for (int w = 0; w < W; w++) x.w[w] = tdet[(nm + mid) * W + w];
+                    if (det_less<W>(x, d)) lo = mid + 1;
+                    else hi = mid;
+                }
+                int64_t i = i0 + k, j = j0 + lo;
+                bool hit = false;
+                if (lo < ns) {
+                    Det<W> x;
+#pragma unroll
+                    for (int w = 0; w < W; w++) x.w[w] = tdet[(nm + lo) * W + w];
+                    hit = det_eq<W>(x, d);
+                } else if (j < U) {
+                    hit = det_eq<W>(load_det<W>(b.udets, j), d);
+                }
+                int64_t p[2] = {0, 0};
+                for (int q = 0; q < R; q++) p[q] = mpops[i * R + q];
+                if (hit) {
+                    uint64_t fl = b.uflag[j];
+                    for (int q = 0; q < R; q++) {
+                        int64_t sp = b.upops[j * R + q];
+                        if (!s.initiator || p[q] != 0) p[q] += sp;
+                        else if (!((fl >> q) & 1)) p[q] = sp;
+                    }
+                }
+                if (s.real_amplitudes) round_pops(s, p, R, P_ROUND_MAIN, i, iter);
+                bool nz = false;
+                for (int q = 0; q < R; q++) {
+                    mpops[i * R + q] = p[q];
+                    nz = nz || p[q] != 0;
+                }
+                int64_t rank = i + j;
+                b.mref[rank] = i;
+                b.mkeep[rank] = make_uint2(nz ? 1u : 0u, nz ? 1u : 0u);
+            } else {
+                int bb = k - nm;
+                // spawned entry: how many tile main entries are at or below it
+                int lo = 0, hi = nm;
+                while (lo < hi) {
+                    int mid = (lo + hi) >> 1;
+                    Det<W> x;
+#pragma unroll
+                    for (int w = 0; w < W; w++) x.w[w] = tdet[mid * W + w];
+                    if (!det_less<W>(d, x)) lo = mid + 1;
+                    else hi = mid;
+                }
+                int64_t j = j0 + bb;
+                bool hit;
+                if (lo > 0) {
+                    Det<W> x;
+#pragma unroll
+                    for (int w = 0; w < W; w++) x.w[w] = tdet[(lo - 1) * W + w];
+                    hit = det_eq<W>(x, d);
+                } else {
+                    hit = i0 > 0 && det_eq<W>(load_det<W>(mdets, i0 - 1), d);
+                }
+                uint32_t keep = 0;
+                if (!hit) {
+                    int64_t sp[2] = {0, 0};
+                    for (int q = 0; q < R; q++) sp[q] = b.upops[j * R + q];
+                    bool discard = false;
+                    if (s.initiator) {
+                        uint64_t fl = b.uflag[j];
+                        discard = true;
+                        for (int q = 0; q < R; q++) {
+                            if ((fl >> q) & 1) sp[q] = 0;
+                            else discard = false;
+                        }
+                    }
+                    if (!discard && s.real_amplitudes) round_pops(s, sp, R, P_ROUND_SPAWN, j, iter);
+                    bool nz = false;
+                    for (int q = 0; q < R; q++) {
+                        b.upops[j * R + q] = sp[q];
+                        nz = nz || sp[q] != 0;
+                    }
+                    keep = discard ? 0u : (s.real_amplitudes ? (nz ? 1u : 0u) : 1u);
+                    if (keep) newlist[atomicAdd(&nnew, 1)] = k;
+                }
+                int64_t rank = j + i0 + lo;
+                b.mref[rank] = -(j + 1);
+                b.mkeep[rank] = make_uint2(0u, keep);
+            }
+        }
+        __syncthreads();
+        // K_ii of the tile's new determinants, one dense pass
+        int n_new = nnew;
+        for (int k = threadIdx.x; k < n_new; k += blockDim.x) {
+            int e = newlist[k];
+            Det<W> d;
+#pragma unroll
+            for (int w = 0; w < W; w++) d.w[w] = tdet[e * W + w];
+            b.ukii[j0 + (e - nm)] = kii_of<W>(s, d);
+        }
+        __syncthreads();
     }
 }
 
@@ -749,8 +829,7 @@ __global__ void __launch_bounds__(kBlock) k_merge_scatter(DevBuffers b, int R, i
             Det<W> d = load_det<W>(b.udets, j);
             store_det<W>(odets, dst, d);
             for (int q = 0; q < R; q++) p[q] = b.upops[j * R + q];
-            // insert_new_walker: dat(1) = sc0(det) - H00 (src/annihilation.f90:855)
-            okii[dst] = kii_of<W>(s, d);
+            okii[dst] = b.ukii[j];  // K_ii from the merge tiles (insert_new_walker)
         }
         for (int q = 0; q < R; q++) opops[dst * R + q] = p[q];
         ap0 += p[0] < 0 ? -p[0] : p[0];
@@ -945,8 +1024,8 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
     device_scan<int64_t>(b, LoadKeep{b.segkeep}, StoreExclusive{b.segpos}, &S->n_spawn, b.scan_part, &S->n_uniq, st);
     k_seg_compact<W><<<b.grid, kBlock, 0, st>>>(b, R, kin);
     if (pm) cudaEventRecord(pm->ev[5], st);
-    k_merge_spawn<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
-    k_merge_main<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
+    k_merge_splits<W><<<b.grid, kBlock, 0, st>>>(b, cur);
+    k_merge_tiles<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
     k_set_count<<<1, 1, 0, st>>>(&S->n_merged, &S->n_main, 1, &S->n_uniq);
     device_scan<uint2>(b, LoadMKeep{b.mkeep}, StoreMPos{b.mpos}, &S->n_merged, reinterpret_cast<uint2 *>(b.scan_part),
                        reinterpret_cast<uint2 *>(&S->n_merged_keep), st);
@@ -987,7 +1066,7 @@ void launch_cycle(const DevBuffers &b, int W, int R, int kind, int precision, in
 
 int launches_per_cycle(const DevBuffers &b) {
     // begin, prep, count, scan(3), spawn, clamp, sort(5/pass), seg_reduce,
-    // scan(3), compact, merge_spawn, merge_main, count, scan(3), scatter, end
+    // scan(3), compact, merge_splits, merge_tiles, count, scan(3), scatter, end
     return 2 + 1 + 3 + 1 + 1 + 5 * b.sort_passes + 1 + 3 + 1 + 2 + 1 + 3 + 1 + 1;
 }
 

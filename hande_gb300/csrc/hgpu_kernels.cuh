@@ -14,6 +14,7 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortItems = 8;    // keys per thread per radix tile
 constexpr int kMaxBlocks = 1024; // upper bound of the fixed grid (partials arrays)
+constexpr int kMergeTile = 2048; // merged elements per tile of the merge-path kernel
 
 // Per-cycle counters and per-report accumulators, resident in device memory so
 // that a whole cycle runs without host synchronisation (and can be replayed
@@ -70,7 +71,9 @@ struct DevBuffers {
     uint64_t *udets;
     int64_t *upops;
     uint64_t *uflag;
+    double *ukii;       // K_ii of unique spawned determinants that become new walkers
     // merge
+    int64_t *msplit;    // merge-path split (main index) at every tile boundary
     int64_t *mref;      // per merged rank: >= 0 main index, < 0 -(j+1) unique spawn
     uint2 *mkeep;       // per merged rank: (kept main, kept any)
     uint2 *mpos;        // exclusive scan of mkeep

@@ -123,9 +123,10 @@ struct oracle_ctx {
     int R;
     uint64_t f0[MAXW];
     double H00;
-    /* exact diagonal: terms on the 2^-96 grid (see fx_energy) */
-    __int128 fx_cst, fx_E0;
-    __int128 *fx_h1, *fx_J, *fx_JK, *fx_eps;
+    /* exact diagonal: terms on the 2^-fx_s grid (see fx_energy) */
+    int fx_s;
+    int64_t fx_cst, fx_E0;
+    int64_t *fx_h1, *fx_J, *fx_JK, *fx_eps;
     /* main list */
     int64_t n, cap;
     uint64_t *dets;
@@ -277,20 +278,31 @@ static double two_e_int_hub_k(const oracle_ctx *c, int p1, int p2, int p3, int p
 /* Exact diagonal energies.  <D|H|D> (slater_condon0_hub_k,
  * src/hamiltonian_hub_k.f90:91-132; slater_condon0_mol,
  * src/hamiltonian_molecular.f90:73-139) is evaluated as the exact sum of the
- * same terms, each rounded once to a multiple of 2^-96 (ties to even) and
- * accumulated in 128-bit integers, then rounded once to double.  HANDE sums
- * the terms left to right in FP64; the two differ by a few ulps. */
-static __int128 fx_of(double x) {
-    double y = ldexp(x, 96);  /* exact */
-    return (__int128)rint(y); /* nearest integer, ties to even (default rounding mode) */
+ * same terms, each rounded once to a multiple of 2^-s (ties to even) and
+ * accumulated in 64-bit integers, then rounded once to double.  s is the largest
+ * scale (<= 60) with 2 B 2^s < 2^62, B = sum over every possible term of
+ * ceil(|term|).  HANDE sums the terms left to right in FP64; the two differ by a
+ * few ulps. */
+static int64_t fx_of(const oracle_ctx *c, double x) {
+    double y = ldexp(x, c->fx_s); /* exact */
+    return (int64_t)rint(y);      /* nearest integer, ties to even (default rounding mode) */
 }
 
-static double fx_val(__int128 v) { return ldexp((double)v, -96); /* one rounding */ }
+static double fx_val(const oracle_ctx *c, int64_t v) { return ldexp((double)v, -c->fx_s); /* one rounding */ }
 
-static __int128 fx_energy(const oracle_ctx *c, const uint64_t *f) {
+static int64_t ceil_abs(double x) { return (int64_t)ceil(fabs(x)); }
+
+static int scale_for_bound(int64_t B) {
+    int bits = 0;
+    while (bits < 63 && (B >> bits) != 0) bits++;
+    int s = 61 - bits;
+    return s > 60 ? 60 : (s < 0 ? 0 : s);
+}
+
+static int64_t fx_energy(const oracle_ctx *c, const uint64_t *f) {
     int occ[MAXB];
     int n = decode(c, f, occ);
-    __int128 e = c->fx_cst;
+    int64_t e = c->fx_cst;
     if (c->kind == HGPU_SYS_HUB_K) {
         for (int i = 0; i < n; i++) e += c->fx_eps[occ[i]];
         return e;
@@ -786,10 +798,10 @@ static void attempt(const oracle_ctx *c, rstream *rs, const uint64_t *f, const d
     else attempt_mol(c, rs, f, d, parent, out);
 }
 
-static double sc0(const oracle_ctx *c, const uint64_t *f) { return fx_val(fx_energy(c, f)); }
+static double sc0(const oracle_ctx *c, const uint64_t *f) { return fx_val(c, fx_energy(c, f)); }
 
 /* dat(1) = K_ii = <D_i|H|D_i> - E_HF (src/annihilation.f90:855), from the exact difference. */
-static double kii_of(const oracle_ctx *c, const uint64_t *f) { return fx_val(fx_energy(c, f) - c->fx_E0); }
+static double kii_of(const oracle_ctx *c, const uint64_t *f) { return fx_val(c, fx_energy(c, f) - c->fx_E0); }
 
 /* get_hmatel_hub_k (src/hamiltonian_hub_k.f90:12-89) / get_hmatel_mol
  * (src/hamiltonian_molecular.f90:12-65). */
@@ -1335,27 +1347,40 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
     }
     for (int w = 0; w < MAXW; w++) c->f0[w] = w < c->nw ? cfg->ref_det[w] : 0;
     if (c->kind == HGPU_SYS_HUB_K) {
-        c->fx_cst = fx_of((double)(c->nalpha * c->nbeta) * c->coulomb_k);
-        c->fx_eps = (__int128 *)malloc(sizeof(__int128) * c->nbasis);
-        for (int p = 0; p < c->nbasis; p++) c->fx_eps[p] = fx_of(c->sp_eigv[p]);
+        double c0 = (double)(c->nalpha * c->nbeta) * c->coulomb_k;
+        int64_t B = ceil_abs(c0);
+        for (int p = 0; p < c->nbasis; p++) B += ceil_abs(c->sp_eigv[p]);
+        c->fx_s = scale_for_bound(B);
+        c->fx_cst = fx_of(c, c0);
+        c->fx_eps = (int64_t *)malloc(sizeof(int64_t) * c->nbasis);
+        for (int p = 0; p < c->nbasis; p++) c->fx_eps[p] = fx_of(c, c->sp_eigv[p]);
     } else {
         int M = c->norb;
-        c->fx_cst = fx_of(c->ecore);
-        c->fx_h1 = (__int128 *)malloc(sizeof(__int128) * M);
-        c->fx_J = (__int128 *)malloc(sizeof(__int128) * M * M);
-        c->fx_JK = (__int128 *)malloc(sizeof(__int128) * M * M);
+        int64_t B = ceil_abs(c->ecore);
+        for (int i = 0; i < c->nbasis; i++) {
+            B += ceil_abs(c->h1[(i >> 1) * M + (i >> 1)]);
+            for (int j = i + 1; j < c->nbasis; j++) {
+                B += ceil_abs(v2_get(c, i, j, i, j));
+                if (c->orb_ms[i] == c->orb_ms[j]) B += ceil_abs(v2_get(c, i, j, j, i));
+            }
+        }
+        c->fx_s = scale_for_bound(B);
+        c->fx_cst = fx_of(c, c->ecore);
+        c->fx_h1 = (int64_t *)malloc(sizeof(int64_t) * M);
+        c->fx_J = (int64_t *)malloc(sizeof(int64_t) * M * M);
+        c->fx_JK = (int64_t *)malloc(sizeof(int64_t) * M * M);
         for (int p = 0; p < M; p++) {
-            c->fx_h1[p] = fx_of(c->h1[p * M + p]);
+            c->fx_h1[p] = fx_of(c, c->h1[p * M + p]);
             for (int q = 0; q < M; q++) {
-                __int128 J = fx_of(v2_get(c, 2 * p, 2 * q, 2 * p, 2 * q)); /* <ij|ij> = (ii|jj) */
-                __int128 K = fx_of(v2_get(c, 2 * p, 2 * q, 2 * q, 2 * p)); /* <ij|ji> = (ij|ji) */
+                int64_t J = fx_of(c, v2_get(c, 2 * p, 2 * q, 2 * p, 2 * q)); /* <ij|ij> = (ii|jj) */
+                int64_t K = fx_of(c, v2_get(c, 2 * p, 2 * q, 2 * q, 2 * p)); /* <ij|ji> = (ij|ji) */
                 c->fx_J[p * M + q] = J;
                 c->fx_JK[p * M + q] = J - K;
             }
         }
     }
     c->fx_E0 = fx_energy(c, c->f0);
-    c->H00 = fx_val(c->fx_E0);
+    c->H00 = fx_val(c, c->fx_E0);
     c->cap = cfg->walker_length > 0 ? cfg->walker_length : 1000000;
     c->scap = cfg->spawned_walker_length > 0 ? cfg->spawned_walker_length : 1000000;
     c->dets = (uint64_t *)calloc((size_t)(c->cap * c->nw), sizeof(uint64_t));

@@ -219,6 +219,76 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+BATCH_WORKLOAD = ("config4: 128 independent Hubbard k-space calculations (2D periodic LxL, L in 3..6, "
+                  "U in {2,4,8}, electrons = sites - 2, ms = 0 or 1 for odd counts, integer walkers, targets "
+                  "log-uniform in [1e4, 1e6], seeded draw) advanced together, one graph launch per cycle")
+
+
+def batched_instances(n=128, seed=4):
+    """The batched configuration: systems and configurations of n instances."""
+    from hande_gb300 import systems
+    from hande_gb300._abi import make_config
+    rng = np.random.default_rng(seed)
+    out = []
+    cache = {}
+    for k in range(n):
+        L = int(rng.choice([3, 4, 5, 6]))
+        U = float(rng.choice([2.0, 4.0, 8.0]))
+        target = float(10 ** rng.uniform(4, 6))
+        nel = L * L - 2
+        ms = nel % 2
+        key = (L, U)
+        if key not in cache:
+            cache[key] = systems.hubbard_k([[L, 0], [0, L]], nel, U=U, ms=ms)
+        s = cache[key]
+        na, nb = (nel + ms) // 2, (nel - ms) // 2
+        nvirt = L * L - na
+        # tau: about 0.7 expected spawned walkers per attempt at most
+        tau = min(0.005, 0.7 / ((U / (L * L)) * na * nb * nvirt))
+        cap = int(6 * target) + 20000
+        cfg = make_config(s, tau=tau, init_pop=10, target_population=target, ncycles=10, seed=1000 + k,
+                          state_size=cap, spawned_state_size=cap)
+        out.append((s, cfg, dict(L=L, U=U, target=target, tau=tau)))
+    return out
+
+
+def batched_measure(steps, max_reports=40):
+    """config 4: grow every instance until its shift varies (untimed), then time
+    `steps` batch cycles (one graph launch each for all instances)."""
+    from hande_gb300.engine import Batch, Engine
+    inst = batched_instances()
+    engines = [Engine(s, cfg) for s, cfg, _ in inst]
+    for e in engines:
+        e.initial_distribution()
+    batch = Batch(engines)
+    reps = None
+    for r in range(max_reports):
+        reps = batch.run_report()
+        if all(rp.vary_shift[0] for rp in reps):
+            break
+    grown = sum(1 for rp in reps if rp.vary_shift[0])
+    walkers = sum(rp.nparticles[0] for rp in reps)
+    states = sum(rp.nstates for rp in reps)
+    batch.run_cycles(3)  # warm-up
+    for e in engines:
+        e.end_report()
+    t0 = time.perf_counter()
+    batch.run_cycles(steps)  # synchronises at the end
+    dt = time.perf_counter() - t0
+    reps = [e.end_report() for e in engines]
+    att = sum(rp.nattempts for rp in reps)
+    flags = 0
+    for rp in reps:
+        flags |= rp.error_flags
+    batch.close()
+    for e in engines:
+        e.close()
+    return {"workload": BATCH_WORKLOAD, "instances": len(inst), "value": att / dt, "unit": "attempts/s",
+            "ms_per_step": 1e3 * dt / steps, "steps": steps, "walkers": walkers, "states": int(states),
+            "instances_at_target": grown, "error_flags": flags, "dtype": "int64 walkers, f64",
+            "timing": "host wall clock around hgpu_batch_run_cycles (graph launches and the final synchronisation)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -229,6 +299,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched (config 4) measurement")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -336,6 +407,14 @@ def main():
            "d2h_bytes_per_step": d2h // args.e2e_steps,
            "note": "per step: hgpu_upload_walkers from pinned host memory, one cycle, hgpu_download_walkers"}
 
+    batched = None
+    if rank == 0 and not args.no_batched:
+        eng.close()
+        try:
+            batched = batched_measure(args.steps)
+        except Exception as exc:  # reported in the line; the config-2 numbers stand
+            batched = {"workload": BATCH_WORKLOAD, "error": "%s: %s" % (type(exc).__name__, exc)}
+
     if rank == 0 and not args.no_cpu:
         # the oracle on whole cycles of the same (device-grown) walker list, 1 core
         r = cpu_sample_on_state(st, po, da, args.cpu_seconds)
@@ -359,6 +438,7 @@ def main():
             "cycle_counts": counts,
             "clocks": clk,
             "cpu_baseline": cpu,
+            "batched": batched,
         }
         print(json.dumps(line))
     if dist:

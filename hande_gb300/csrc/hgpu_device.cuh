@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "../../include/hande_gpu.h"
+#include "hgpu_exact.h"
 #include "hgpu_fixed.h"
 
 namespace hgpu {
@@ -61,6 +62,9 @@ struct alignas(16) DevSys {
     int64_t cutoff;  // encoded spawn cutoff
     double tau;
     double pattempt_single, pattempt_double;
+    uint64_t t_single;  // u < pattempt_single  <=>  k < t_single for u = k 2^-53: ceil(pattempt_single 2^53)
+    const double *pg2;  // [n_aij][xa][xb] double-excitation p_gen (pgen_double), pg2_x = max orbitals per (irrep, spin) + 1
+    int pg2_x, pg2_n;
     double initiator_pop;
     double H00;
     uint64_t seed;
@@ -82,6 +86,10 @@ struct alignas(16) DevSys {
     uint64_t symmask[kMaxSym * 2 * kMaxWords];
     int nbss[kMaxSym * 2];  // orbitals per (sym, ims): index sym*2+ims
     uint8_t orbsym[64 * kMaxWords];  // irrep of each spin orbital
+    // heat-bath generator tables (hgpu_heat_bath.h); element type double, or
+    // float in the mixed-precision mode
+    const void *hb_i_w, *hb_ij_w, *hb_ija_w, *hb_ija_tot, *hb_ija_U, *hb_ijab_tot, *hb_ijab_U;
+    const uint8_t *hb_ija_K, *hb_ijab_K;
 };
 
 // ---------------------------------------------------------------------------
@@ -107,10 +115,9 @@ __device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1) 
     }
 }
 
-// (double)(x >> 11) * 2^-53, built from its bit pattern on the integer pipes
+// k * 2^-53 for k < 2^53, built from its bit pattern on the integer pipes
 // (the value is exact, so this is the same number the conversion gives).
-__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
-    uint64_t k = (((uint64_t)hi << 32) | lo) >> 11;
+__device__ __forceinline__ double kdouble(uint64_t k) {
     if (k == 0) return 0.0;
     int msb = 63 - __clzll((long long)k);
     uint64_t man = (k << (52 - msb)) & ((1ull << 52) - 1);
@@ -118,13 +125,19 @@ __device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {
     return __longlong_as_double((long long)bits);
 }
 
+// The 53-bit integer k of the uniform u = k * 2^-53 drawn from two Philox words.
+__device__ __forceinline__ uint64_t k53(uint32_t hi, uint32_t lo) { return (((uint64_t)hi << 32) | lo) >> 11; }
+
+// (double)(x >> 11) * 2^-53 of the 64-bit word x = hi:lo.
+__device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) { return kdouble(k53(hi, lo)); }
+
 // Stream of uniforms in [0,1) for one (purpose, space, index, sub, iteration):
 // counter = (index, sub, iteration, purpose<<28 | space<<26 | block).
 struct RStream {
     uint32_t c0, c1, c2, c3;
     uint32_t k0, k1;
     uint32_t block;
-    double buf;
+    uint64_t bufk;
     bool have;
 
     __device__ __forceinline__ void init(uint64_t seed, uint32_t purpose, uint32_t space, uint64_t idx,
@@ -138,19 +151,22 @@ struct RStream {
         block = 0;
         have = false;
     }
-    // get_rand_close_open
-    __device__ __forceinline__ double next() {
+    // The next uniform as its integer k (u = k * 2^-53), for comparisons and
+    // products that are exact in integer arithmetic.
+    __device__ __forceinline__ uint64_t next_k() {
         if (have) {
             have = false;
-            return buf;
+            return bufk;
         }
         uint32_t c[4] = {c0, c1, c2, c3 | block};
         philox(c, k0, k1);
         block++;
-        buf = u53(c[2], c[3]);
+        bufk = k53(c[2], c[3]);
         have = true;
-        return u53(c[0], c[1]);
+        return k53(c[0], c[1]);
     }
+    // get_rand_close_open
+    __device__ __forceinline__ double next() { return kdouble(next_k()); }
 };
 
 // ---------------------------------------------------------------------------
@@ -381,8 +397,34 @@ __device__ __forceinline__ int ims_of(int p) { return (p & 1) ? 0 : 1; }  // 0 b
 // (ii|jj) and, for parallel spins, -(ij|ji) -- or of slater_condon0_hub_k
 // (src/hamiltonian_hub_k.f90:91-132) -- nalpha*nbeta*U/N and the
 // single-particle energies -- accumulated in 64-bit integers.
+// The tables (fx_h1, fx_pair, fx_eps) are passed explicitly so that a kernel can
+// read them from a shared-memory copy (FxTabs).
+struct FxTabs {
+    const int64_t *h1, *pair, *eps;
+};
+
+__device__ __forceinline__ FxTabs fx_tabs(const DevSys &s) { return FxTabs{s.fx_h1, s.fx_pair, s.fx_eps}; }
+
+// Words of the exact-diagonal tables: eps[nbasis] (hub_k) or h1[norb] + pair[2 norb^2].
+__host__ __device__ __forceinline__ int fx_table_words(int kind, int nbasis, int norb) {
+    return kind == HGPU_SYS_HUB_K ? nbasis : norb + 2 * norb * norb;
+}
+
+// Copies the exact-diagonal tables into dst (fx_table_words entries) with the
+// whole block; the caller synchronises before use.
+__device__ __forceinline__ FxTabs stage_fx(const DevSys &s, int64_t *dst) {
+    if (s.kind == HGPU_SYS_HUB_K) {
+        for (int k = threadIdx.x; k < s.nbasis; k += blockDim.x) dst[k] = s.fx_eps[k];
+        return FxTabs{nullptr, nullptr, dst};
+    }
+    const int M = s.norb;
+    for (int k = threadIdx.x; k < M; k += blockDim.x) dst[k] = s.fx_h1[k];
+    for (int k = threadIdx.x; k < 2 * M * M; k += blockDim.x) dst[M + k] = s.fx_pair[k];
+    return FxTabs{dst, dst + M, nullptr};
+}
+
 template <int W>
-__device__ int64_t fx_energy(const DevSys &s, const Det<W> &f) {
+__device__ int64_t fx_energy(const DevSys &s, const Det<W> &f, const FxTabs &tb) {
     int64_t e = s.fx_const;
     if (s.kind == HGPU_SYS_HUB_K) {
 #pragma unroll
@@ -391,7 +433,7 @@ __device__ int64_t fx_energy(const DevSys &s, const Det<W> &f) {
             while (x) {
                 int p = 64 * k + __ffsll((long long)x) - 1;
                 x &= x - 1;
-                e += s.fx_eps[p];
+                e += tb.eps[p];
             }
         }
         return e;
@@ -404,8 +446,8 @@ __device__ int64_t fx_energy(const DevSys &s, const Det<W> &f) {
             int i = 64 * k + __ffsll((long long)x) - 1;
             x &= x - 1;
             int si = i >> 1;
-            e += s.fx_h1[si];
-            const int64_t *opp = s.fx_pair + (size_t)si * M;
+            e += tb.h1[si];
+            const int64_t *opp = tb.pair + (size_t)si * M;
             const int64_t *same = opp + (size_t)M * M;
             // partners j > i
 #pragma unroll
@@ -422,6 +464,11 @@ __device__ int64_t fx_energy(const DevSys &s, const Det<W> &f) {
     return e;
 }
 
+template <int W>
+__device__ __forceinline__ int64_t fx_energy(const DevSys &s, const Det<W> &f) {
+    return fx_energy<W>(s, f, fx_tabs(s));
+}
+
 // slater_condon0 (sc0_ptr): nearest double to the exact sum.
 template <int W>
 __device__ __forceinline__ double sc0(const DevSys &s, const Det<W> &f) {
@@ -431,23 +478,49 @@ __device__ __forceinline__ double sc0(const DevSys &s, const Det<W> &f) {
 // dat(1) of a new walker: K_ii = <D_i|H|D_i> - E_HF (src/annihilation.f90:855),
 // the nearest double to the exact difference.
 template <int W>
+__device__ __forceinline__ double kii_of(const DevSys &s, const Det<W> &f, const FxTabs &tb) {
+    return fx_to_double(fx_energy<W>(s, f, tb) - s.fx_E0, s.fx_inv_scale);
+}
+
+template <int W>
 __device__ __forceinline__ double kii_of(const DevSys &s, const Det<W> &f) {
-    return fx_to_double(fx_energy<W>(s, f) - s.fx_E0, s.fx_inv_scale);
+    return kii_of<W>(s, f, fx_tabs(s));
 }
 
 // slater_condon1_mol_excit (src/hamiltonian_molecular.f90:199-259).
+// The integrals of four occupied orbitals at a time are loaded before any of
+// them is added, so a determinant costs nel/4 memory round trips instead of
+// nel; the additions stay in ascending orbital order, as the reference sums.
 template <int W, typename Real>
 __device__ Real sc1_mol(const DevSys &s, const Det<W> &f, int i, int a, bool perm) {
+    constexpr int G = 4;
     Real h = Ints<Real>::h1(s, i, a);
 #pragma unroll
     for (int k = 0; k < W; k++) {
-        uint64_t x = f.w[k];
+        uint64_t x = f.w[k] & ~((k == (i >> 6)) ? (1ull << (i & 63)) : 0ull);  // q != i
         while (x) {
-            int q = 64 * k + __ffsll((long long)x) - 1;
-            x &= x - 1;
-            if (q != i) {
-                h = h + Ints<Real>::v2(s, i, q, a, q);
-                if (((q ^ i) & 1) == 0) h = h - Ints<Real>::v2(s, i, q, q, a);
+            int q[G];
+            Real v[G], e[G];
+#pragma unroll
+            for (int u = 0; u < G; u++) {
+                q[u] = x ? 64 * k + __ffsll((long long)x) - 1 : -1;
+                x &= x - 1;
+            }
+#pragma unroll
+            for (int u = 0; u < G; u++) {
+                v[u] = (Real)0;
+                e[u] = (Real)0;
+                if (q[u] >= 0) {
+                    v[u] = Ints<Real>::v2(s, i, q[u], a, q[u]);
+                    if (((q[u] ^ i) & 1) == 0) e[u] = Ints<Real>::v2(s, i, q[u], q[u], a);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < G; u++) {
+                if (q[u] >= 0) {
+                    h = h + v[u];
+                    if (((q[u] ^ i) & 1) == 0) h = h - e[u];
+                }
             }
         }
     }
@@ -502,16 +575,12 @@ struct Attempt {
 };
 
 // stochastic_round_spawned_particle (src/stoch_utils.f90:87-136).
+// pspawn >= 0; the comparisons and the large-amplitude branch are evaluated in
+// integer arithmetic with identical results (hgpu_exact.h).
 __device__ __forceinline__ int64_t round_spawned(int64_t cutoff, double dcutoff, double pspawn, RStream &rs) {
-    int64_t nspawn;
-    if (pspawn < dcutoff) {
-        nspawn = (pspawn > rs.next() * dcutoff) ? cutoff : 0;
-    } else {
-        nspawn = (int64_t)pspawn;
-        double padd = pspawn - (double)nspawn;
-        if (padd > rs.next()) nspawn = nspawn + 1;
-    }
-    return nspawn;
+    if (less_nonneg(dbits(pspawn), dbits(dcutoff))) return (pspawn > rs.next() * dcutoff) ? cutoff : 0;
+    // nspawn = int(pspawn); if (pspawn - nspawn > rand) nspawn = nspawn + 1
+    return round_up_frac(dbits(pspawn), rs.next_k());
 }
 
 __device__ __forceinline__ int64_t isign64(int64_t a, int64_t b) {
@@ -521,7 +590,7 @@ __device__ __forceinline__ int64_t isign64(int64_t a, int64_t b) {
 
 // set_child_sign (src/spawning.F90:680-709).
 __device__ __forceinline__ int64_t child_sign(double hmatel, int64_t parent, int64_t nspawn) {
-    return hmatel > 0.0 ? -isign64(nspawn, parent) : isign64(nspawn, parent);
+    return positive(dbits(hmatel)) ? -isign64(nspawn, parent) : isign64(nspawn, parent);  // hmatel > 0
 }
 
 // spawn_lattice_split_gen (src/spawning.F90:215-315) with gen_excit_init_hub_k /
@@ -543,8 +612,7 @@ __device__ void attempt_hub_k(const DevSys &s, const HubTables &t, RStream &rs, 
         ua[k] = ~f.w[k] & kAlpha & valid;
     }
     // choose_ij_hub_k (src/excit_gen_hub_k.f90:469-532)
-    double r = rs.next();
-    int ind = (int)(r * s.d_nalpha * s.d_nbeta) + 1;
+    int ind = floor_uab(rs.next_k(), s.nalpha, s.nbeta) + 1;  // int(rand * nalpha * nbeta) + 1
     // int((ind-1.0)/nbeta): exact for integers, so integer division gives it
     int ii = (ind - 1) / s.nbeta + 1;
     int jj = ind - (ii - 1) * s.nbeta;
@@ -574,7 +642,7 @@ __device__ void attempt_hub_k(const DevSys &s, const HubTables &t, RStream &rs, 
         abs_h = fabs(s.coulomb_k);
     } else {
         // find_ab_hub_k (src/excit_gen_hub_k.f90:579-649)
-        int rr = (int)(rs.next() * s.d_nvirt_alpha);
+        int rr = floor_un(rs.next_k(), s.nvirt_alpha);  // int(rand * nvirt_alpha)
         a = select_det<W>(ua, rr);
         b = hub_partner(t, ij_sym, a);
         out.allowed = !tbit<W>(f, b);
@@ -595,7 +663,7 @@ __device__ void attempt_hub_k(const DevSys &s, const HubTables &t, RStream &rs, 
         if (renorm) {
             // choose_ab_hub_k: redraw until b is unoccupied
             for (int it = 0;; it++) {
-                int rr = (int)(rs.next() * s.d_nvirt_alpha);
+                int rr = floor_un(rs.next_k(), s.nvirt_alpha);
                 a = select_det<W>(ua, rr);
                 b = hub_partner(t, ij_sym, a);
                 if (!tbit<W>(f, b)) break;
@@ -666,237 +734,24 @@ __device__ __forceinline__ int sym_of(const DevSys &s, int p) {
     return s.orbsym[p];
 }
 
+// int(rand * nbasis) or the spin-restricted int(rand * nbasis/2), u = k 2^-53.
 template <int W>
-__device__ __forceinline__ int pick_a(const DevSys &s, int spin, double r) {
-    if (spin == 0) return (int)(r * s.d_nbasis);
-    int k = (int)(r * s.d_half_nbasis);
+__device__ __forceinline__ int pick_a(const DevSys &s, int spin, uint64_t ku) {
+    if (spin == 0) return floor_un(ku, s.nbasis);
+    int k = floor_un(ku, s.nbasis / 2);
     return spin == -2 ? 2 * k + 1 : 2 * k;
 }
 
-template <int W, typename Real>
-__device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, int64_t parent, Attempt &out) {
-    const Det<W> &f = d.f;
-    out.from[0] = out.from[1] = out.to[0] = out.to[1] = -1;
-    bool renorm = s.excit_gen == HGPU_EXCIT_GEN_RENORM;
-    double pgen;
-    Real hm;
-    if (rs.next() < s.pattempt_single) {
-        out.nexcit = 1;
-        int i = -1, a = -1;
-        bool ok;
-        if (renorm) {
-            // choose_ia_mol (src/excit_gen_mol.f90:521-618)
-            ok = false;
-            for (int k = 0; k < s.nel; k++) {
-                int p = select_det<W>(f.w, k);
-                if (SU(d, ims_of(p), sym_of<W>(s, p)) != 0) {
-                    ok = true;
-                    break;
-                }
-            }
-            if (ok) {
-                int guard = 0;
-                for (;;) {
-                    i = select_det<W>(f.w, (int)(rs.next() * s.d_nel));
-                    int imsa = ims_of(i), isyma = sym_of<W>(s, i);
-                    if (SU(d, imsa, isyma) != 0) {
-                        for (;;) {
-                            int ind = (int)(s.d_nbss[isyma * 2 + imsa] * rs.next());
-                            a = ssbf<W>(s, imsa, isyma, ind);
-                            if (!tbit<W>(f, a) || ++guard > kMaxRedraw) break;
-                        }
-                        break;
-                    }
-                    if (++guard > kMaxRedraw) break;
-                }
-                if (guard > kMaxRedraw) ok = false;
-            }
-        } else {
-            // find_ia_mol (src/excit_gen_mol.f90:950-1016)
-            i = select_det<W>(f.w, (int)(rs.next() * s.d_nel));
-            int imsa = ims_of(i), isyma = sym_of<W>(s, i);
-            int nb = s.nbss[isyma * 2 + imsa];
-            int ind = (int)(s.d_nbss[isyma * 2 + imsa] * rs.next());
-            if (nb == 0) {
-                ok = false;
-            } else {
-                a = ssbf<W>(s, imsa, isyma, ind);
-                ok = !tbit<W>(f, a);
-            }
-        }
-        out.allowed = ok;
-        out.from[0] = i;
-        out.to[0] = ok ? a : -1;
-        if (ok) {
-            double pg;
-            if (renorm) {
-                // calc_pgen_single_mol (src/excit_gen_mol.f90:1140-1200)
-                int ni = s.nel;
-                for (int k = 0; k < s.nel; k++) {
-                    int p = select_det<W>(f.w, k);
-                    if (SU(d, ims_of(p), sym_of<W>(s, p)) == 0) ni--;
-                }
-                pg = s.inv[ni * SU(d, ims_of(a), sym_of<W>(s, a))];
-            } else {
-                pg = s.inv[s.nel * s.nbss[sym_of<W>(s, a) * 2 + ims_of(a)]];
-            }
-            pgen = s.pattempt_single * pg;
-            hm = sc1_mol<W, Real>(s, f, i, a, perm1<W>(f, i, a));
-        } else {
-            hm = (Real)0;
-            pgen = 1.0;
-        }
-    } else {
-        out.nexcit = 2;
-        // choose_ij_mol (src/excit_gen_mol.f90:620-660)
-        double x = rs.next() * s.d_nel * s.d_nelm1 / 2.0;
-        int ind = (int)x + 1;
-        // int(1.5 + sqrt(2 ind - 1.75)) is exactly the j with
-        // (j-1)(j-2)/2 < ind <= j(j-1)/2; found here in integer arithmetic
-        int j_ind = (int)(1.5f + sqrtf((float)(2 * ind) - 1.75f));
-        while (j_ind * (j_ind - 1) / 2 < ind) j_ind++;
-        while ((j_ind - 1) * (j_ind - 2) / 2 >= ind) j_ind--;
-        int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
-        int i = select_det<W>(f.w, i_ind - 1);
-        int j = select_det<W>(f.w, j_ind - 1);
-        int ij_sym = xsym(s, sym_of<W>(s, i), sym_of<W>(s, j));
-        int ij_spin = ms_of(i) + ms_of(j);
-        double pgen_ij = s.pgen_ij;
-        out.from[0] = i;
-        out.from[1] = j;
-        int a = -1, b = -1;
-        bool ok = false;
-        if (renorm) {
-            // choose_ab_mol (src/excit_gen_mol.f90:802-948)
-            int is = ij_spin == -2 ? 0 : 1;
-            for (int isyma = 0; isyma < s.nsym; isyma++) {
-                int isymb = xsym(s, isyma, ij_sym);
-                if (ij_spin == 0) {
-                    if ((SU(d, 0, isyma) > 0 && SU(d, 1, isymb) > 0) || (SU(d, 1, isyma) > 0 && SU(d, 0, isymb) > 0)) {
-                        ok = true;
-                        break;
-                    }
-                } else if (SU(d, is, isyma) > 0 &&
-                           (SU(d, is, isymb) > 1 || (SU(d, is, isymb) == 1 && isyma != isymb))) {
-                    ok = true;
-                    break;
-                }
-            }
-            if (ok) {
-                int guard = 0;
-                for (;;) {
-                    a = pick_a<W>(s, ij_spin, rs.next());
-                    if (!tbit<W>(f, a)) {
-                        int imsb = (ij_spin - ms_of(a) + 3) / 2 - 1;
-                        int syma = sym_of<W>(s, a);
-                        int isymb = xsym(s, ij_sym, syma);
-                        int nu = SU(d, imsb, isymb);
-                        if (nu > 1 || (nu == 1 && (isymb != syma || ij_spin == 0))) {
-                            for (;;) {
-                                int k = (int)(s.d_nbss[isymb * 2 + imsb] * rs.next());
-                                b = ssbf<W>(s, imsb, isymb, k);
-                                if ((b != a && !tbit<W>(f, b)) || ++guard > kMaxRedraw) break;
-                            }
-                            break;
-                        }
-                    }
-                    if (++guard > kMaxRedraw) break;
-                }
-                if (guard > kMaxRedraw) ok = false;
-                if (a > b) {
-                    int tt = a;
-                    a = b;
-                    b = tt;
-                }
-            }
-        } else {
-            // find_ab_mol (src/excit_gen_mol.f90:1018-1138)
-            for (int it = 0;; it++) {
-                a = pick_a<W>(s, ij_spin, rs.next());
-                if (!tbit<W>(f, a) || it >= kMaxRedraw) break;
-            }
-            int imsb = (ij_spin - ms_of(a) + 3) / 2 - 1;
-            int syma = sym_of<W>(s, a);
-            int isymb = xsym(s, ij_sym, syma);
-            int nb = s.nbss[isymb * 2 + imsb];
-            if (nb == 0) {
-                ok = false;
-            } else if (ij_spin != 0 && isymb == syma && nb == 1) {
-                ok = false;
-            } else {
-                for (int it = 0;; it++) {
-                    int k = (int)(s.d_nbss[isymb * 2 + imsb] * rs.next());
-                    b = ssbf<W>(s, imsb, isymb, k);
-                    if (b != a || it >= kMaxRedraw) break;
-                }
-                ok = b != a && !tbit<W>(f, b);
-                if (a > b) {
-                    int tt = a;
-                    a = b;
-                    b = tt;
-                }
-            }
-        }
-        out.allowed = ok;
-        if (ok) {
-            out.to[0] = a;
-            out.to[1] = b;
-            double pg;
-            int imsa = ims_of(a), imsb = ims_of(b), syma = sym_of<W>(s, a), symb = sym_of<W>(s, b);
-            if (renorm) {
-                // calc_pgen_double_mol (src/excit_gen_mol.f90:1202-1327)
-                int n_aij;
-                double p_bija, p_aijb;
-                if (ij_spin == 0) {
-                    n_aij = s.nvirt;
-                    for (int isyma = 0; isyma < s.nsym; isyma++) {
-                        int isymb = xsym(s, isyma, ij_sym);
-                        if (SU(d, 0, isymb) == 0) n_aij -= SU(d, 1, isyma);
-                        if (SU(d, 1, isymb) == 0) n_aij -= SU(d, 0, isyma);
-                    }
-                    p_aijb = s.inv[SU(d, imsa, syma)];
-                    p_bija = s.inv[SU(d, imsb, symb)];
-                } else {
-                    int is = ij_spin == -2 ? 0 : 1;
-                    n_aij = ij_spin == -2 ? s.nvirt_beta : s.nvirt_alpha;
-                    for (int isyma = 0; isyma < s.nsym; isyma++) {
-                        int isymb = xsym(s, isyma, ij_sym);
-                        if (SU(d, is, isymb) == 0)
-                            n_aij -= SU(d, is, isyma);
-                        else if (isyma == isymb && SU(d, is, isymb) == 1)
-                            n_aij -= SU(d, is, isyma);
-                    }
-                    if (syma == symb) {
-                        p_aijb = s.inv[SU(d, imsa, syma) - 1];
-                        p_bija = s.inv[SU(d, imsb, symb) - 1];
-                    } else {
-                        p_aijb = s.inv[SU(d, imsa, syma)];
-                        p_bija = s.inv[SU(d, imsb, symb)];
-                    }
-                }
-                pg = s.inv[n_aij] * (p_bija + p_aijb);
-            } else {
-                // calc_pgen_double_mol_no_renorm (src/excit_gen_mol.f90:1368-1445)
-                int n_aij = ij_spin == -2 ? s.nvirt_beta : (ij_spin == 0 ? s.nvirt : s.nvirt_alpha);
-                double p_bija, p_aijb;
-                if (syma == symb && imsa == imsb) {
-                    p_aijb = s.inv[s.nbss[syma * 2 + imsa] - 1];
-                    p_bija = s.inv[s.nbss[symb * 2 + imsb] - 1];
-                } else {
-                    p_aijb = s.inv[s.nbss[syma * 2 + imsa]];
-                    p_bija = s.inv[s.nbss[symb * 2 + imsb]];
-                }
-                pg = s.inv[n_aij] * (p_bija + p_aijb);
-            }
-            pgen = s.pattempt_double * pgen_ij * pg;
-            hm = sc2_mol<Real>(s, i, j, a, b, perm2<W>(f, i, j, a, b));
-        } else {
-            hm = (Real)0;
-            pgen = 1.0;
-        }
-    }
-    // attempt_to_spawn (src/spawning.F90:711-768)
-    double h = (double)hm;
+// p_gen of a double excitation, pattempt_double * 2/(nel(nel-1)) * (1/n_aij) *
+// (1/xb + 1/xa) in the reference's rounding order, read from a table the host
+// fills with exactly that expression (DevSys::pg2; symmetric in xa, xb).
+__device__ __forceinline__ double pgen_double(const DevSys &s, int n_aij, int xa, int xb) {
+    return __ldg(&s.pg2[((size_t)n_aij * s.pg2_x + xa) * s.pg2_x + xb]);
+}
+
+// attempt_to_spawn (src/spawning.F90:711-768).
+__device__ __forceinline__ void attempt_to_spawn(const DevSys &s, RStream &rs, int64_t parent, double pgen, double h,
+                                                 Attempt &out) {
     out.pgen = pgen;
     out.hmatel = h;
     double pspawn = s.tau * fabs(h) / pgen;
@@ -904,6 +759,523 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
     int64_t nspawn = round_spawned(s.cutoff, s.d_cutoff, pspawn, rs);
     if (nspawn > 0) nspawn = child_sign(h, parent, nspawn);
     out.nspawn = nspawn;
+}
+
+// gen_single_excit_mol / gen_single_excit_mol_no_renorm (src/excit_gen_mol.f90:384-519):
+// one single excitation with its p_gen and matrix element.
+template <int W, typename Real>
+__device__ __forceinline__ void gen_single_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, bool renorm,
+                                               Attempt &out, double &pgen, Real &hm) {
+    const Det<W> &f = d.f;
+    out.nexcit = 1;
+    int i = -1, a = -1;
+    bool ok;
+    if (renorm) {
+        // choose_ia_mol (src/excit_gen_mol.f90:521-618)
+        ok = false;
+        for (int k = 0; k < s.nel; k++) {
+            int p = select_det<W>(f.w, k);
+            if (SU(d, ims_of(p), sym_of<W>(s, p)) != 0) {
+                ok = true;
+                break;
+            }
+        }
+        if (ok) {
+            int guard = 0;
+            for (;;) {
+                i = select_det<W>(f.w, floor_un(rs.next_k(), s.nel));  // int(rand * nel)
+                int imsa = ims_of(i), isyma = sym_of<W>(s, i);
+                if (SU(d, imsa, isyma) != 0) {
+                    for (;;) {
+                        int ind = floor_un(rs.next_k(), s.nbss[isyma * 2 + imsa]);  // int(nbss * rand)
+                        a = ssbf<W>(s, imsa, isyma, ind);
+                        if (!tbit<W>(f, a) || ++guard > kMaxRedraw) break;
+                    }
+                    break;
+                }
+                if (++guard > kMaxRedraw) break;
+            }
+            if (guard > kMaxRedraw) ok = false;
+        }
+    } else {
+        // find_ia_mol (src/excit_gen_mol.f90:950-1016)
+        i = select_det<W>(f.w, floor_un(rs.next_k(), s.nel));
+        int imsa = ims_of(i), isyma = sym_of<W>(s, i);
+        int nb = s.nbss[isyma * 2 + imsa];
+        int ind = floor_un(rs.next_k(), nb);
+        if (nb == 0) {
+            ok = false;
+        } else {
+            a = ssbf<W>(s, imsa, isyma, ind);
+            ok = !tbit<W>(f, a);
+        }
+    }
+    out.allowed = ok;
+    out.from[0] = i;
+    out.to[0] = ok ? a : -1;
+    if (ok) {
+        double pg;
+        if (renorm) {
+            // calc_pgen_single_mol (src/excit_gen_mol.f90:1140-1200)
+            int ni = s.nel;
+            for (int k = 0; k < s.nel; k++) {
+                int p = select_det<W>(f.w, k);
+                if (SU(d, ims_of(p), sym_of<W>(s, p)) == 0) ni--;
+            }
+            pg = s.inv[ni * SU(d, ims_of(a), sym_of<W>(s, a))];
+        } else {
+            pg = s.inv[s.nel * s.nbss[sym_of<W>(s, a) * 2 + ims_of(a)]];
+        }
+        pgen = s.pattempt_single * pg;
+        hm = sc1_mol<W, Real>(s, f, i, a, perm1<W>(f, i, a));
+    } else {
+        hm = (Real)0;
+        pgen = 1.0;
+    }
+}
+
+// gen_excit_mol / gen_excit_mol_no_renorm, double branch (src/excit_gen_mol.f90:16-101,
+// :195-284): one double excitation with its p_gen and matrix element.
+template <int W, typename Real>
+__device__ __forceinline__ void gen_double_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, bool renorm,
+                                               Attempt &out, double &pgen, Real &hm) {
+    const Det<W> &f = d.f;
+    out.nexcit = 2;
+    // choose_ij_mol (src/excit_gen_mol.f90:620-660)
+    int ind = floor_uab_half(rs.next_k(), s.nel, s.nel - 1) + 1;  // int(rand * nel * (nel-1) / 2) + 1
+    // int(1.5 + sqrt(2 ind - 1.75)) is exactly the j with
+    // (j-1)(j-2)/2 < ind <= j(j-1)/2; found here in integer arithmetic
+    int j_ind = (int)(1.5f + sqrtf((float)(2 * ind) - 1.75f));
+    while (j_ind * (j_ind - 1) / 2 < ind) j_ind++;
+    while ((j_ind - 1) * (j_ind - 2) / 2 >= ind) j_ind--;
+    int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
+    int i = select_det<W>(f.w, i_ind - 1);
+    int j = select_det<W>(f.w, j_ind - 1);
+    int ij_sym = xsym(s, sym_of<W>(s, i), sym_of<W>(s, j));
+    int ij_spin = ms_of(i) + ms_of(j);
+    double pgen_ij = s.pgen_ij;
+    out.from[0] = i;
+    out.from[1] = j;
+    int a = -1, b = -1;
+    bool ok = false;
+    if (renorm) {
+        // choose_ab_mol (src/excit_gen_mol.f90:802-948)
+        int is = ij_spin == -2 ? 0 : 1;
+        for (int isyma = 0; isyma < s.nsym; isyma++) {
+            int isymb = xsym(s, isyma, ij_sym);
+            if (ij_spin == 0) {
+                if ((SU(d, 0, isyma) > 0 && SU(d, 1, isymb) > 0) || (SU(d, 1, isyma) > 0 && SU(d, 0, isymb) > 0)) {
+                    ok = true;
+                    break;
+                }
+            } else if (SU(d, is, isyma) > 0 &&
+                       (SU(d, is, isymb) > 1 || (SU(d, is, isymb) == 1 && isyma != isymb))) {
+                ok = true;
+                break;
+            }
+        }
+        if (ok) {
+            int guard = 0;
+            for (;;) {
+                a = pick_a<W>(s, ij_spin, rs.next_k());
+                if (!tbit<W>(f, a)) {
+                    int imsb = (ij_spin - ms_of(a) + 3) / 2 - 1;
+                    int syma = sym_of<W>(s, a);
+                    int isymb = xsym(s, ij_sym, syma);
+                    int nu = SU(d, imsb, isymb);
+                    if (nu > 1 || (nu == 1 && (isymb != syma || ij_spin == 0))) {
+                        for (;;) {
+                            int k = floor_un(rs.next_k(), s.nbss[isymb * 2 + imsb]);
+                            b = ssbf<W>(s, imsb, isymb, k);
+                            if ((b != a && !tbit<W>(f, b)) || ++guard > kMaxRedraw) break;
+                        }
+                        break;
+                    }
+                }
+                if (++guard > kMaxRedraw) break;
+            }
+            if (guard > kMaxRedraw) ok = false;
+            if (a > b) {
+                int tt = a;
+                a = b;
+                b = tt;
+            }
+        }
+    } else {
+        // find_ab_mol (src/excit_gen_mol.f90:1018-1138)
+        for (int it = 0;; it++) {
+            a = pick_a<W>(s, ij_spin, rs.next_k());
+            if (!tbit<W>(f, a) || it >= kMaxRedraw) break;
+        }
+        int imsb = (ij_spin - ms_of(a) + 3) / 2 - 1;
+        int syma = sym_of<W>(s, a);
+        int isymb = xsym(s, ij_sym, syma);
+        int nb = s.nbss[isymb * 2 + imsb];
+        if (nb == 0) {
+            ok = false;
+        } else if (ij_spin != 0 && isymb == syma && nb == 1) {
+            ok = false;
+        } else {
+            for (int it = 0;; it++) {
+                int k = floor_un(rs.next_k(), s.nbss[isymb * 2 + imsb]);
+                b = ssbf<W>(s, imsb, isymb, k);
+                if (b != a || it >= kMaxRedraw) break;
+            }
+            ok = b != a && !tbit<W>(f, b);
+            if (a > b) {
+                int tt = a;
+                a = b;
+                b = tt;
+            }
+        }
+    }
+    out.allowed = ok;
+    if (ok) {
+        out.to[0] = a;
+        out.to[1] = b;
+        int imsa = ims_of(a), imsb = ims_of(b), syma = sym_of<W>(s, a), symb = sym_of<W>(s, b);
+        if (renorm) {
+            // calc_pgen_double_mol (src/excit_gen_mol.f90:1202-1327)
+            int n_aij, xa, xb;
+            if (ij_spin == 0) {
+                n_aij = s.nvirt;
+                for (int isyma = 0; isyma < s.nsym; isyma++) {
+                    int isymb = xsym(s, isyma, ij_sym);
+                    if (SU(d, 0, isymb) == 0) n_aij -= SU(d, 1, isyma);
+                    if (SU(d, 1, isymb) == 0) n_aij -= SU(d, 0, isyma);
+                }
+                xa = SU(d, imsa, syma);
+                xb = SU(d, imsb, symb);
+            } else {
+                int is = ij_spin == -2 ? 0 : 1;
+                n_aij = ij_spin == -2 ? s.nvirt_beta : s.nvirt_alpha;
+                for (int isyma = 0; isyma < s.nsym; isyma++) {
+                    int isymb = xsym(s, isyma, ij_sym);
+                    if (SU(d, is, isymb) == 0)
+                        n_aij -= SU(d, is, isyma);
+                    else if (isyma == isymb && SU(d, is, isymb) == 1)
+                        n_aij -= SU(d, is, isyma);
+                }
+                int same = syma == symb ? 1 : 0;
+                xa = SU(d, imsa, syma) - same;
+                xb = SU(d, imsb, symb) - same;
+            }
+            // p_aijb = 1/xa, p_bija = 1/xb
+            pgen = pgen_double(s, n_aij, xa, xb);
+        } else {
+            // calc_pgen_double_mol_no_renorm (src/excit_gen_mol.f90:1368-1445)
+            int n_aij = ij_spin == -2 ? s.nvirt_beta : (ij_spin == 0 ? s.nvirt : s.nvirt_alpha);
+            int same = (syma == symb && imsa == imsb) ? 1 : 0;
+            pgen = pgen_double(s, n_aij, s.nbss[syma * 2 + imsa] - same, s.nbss[symb * 2 + imsb] - same);
+        }
+        hm = sc2_mol<Real>(s, i, j, a, b, perm2<W>(f, i, j, a, b));
+    } else {
+        hm = (Real)0;
+        pgen = 1.0;
+    }
+}
+
+template <int W, typename Real>
+__device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, int64_t parent, Attempt &out) {
+    out.from[0] = out.from[1] = out.to[0] = out.to[1] = -1;
+    bool renorm = s.excit_gen == HGPU_EXCIT_GEN_RENORM;
+    double pgen;
+    Real hm;
+    if (rs.next_k() < s.t_single) gen_single_mol<W, Real>(s, rs, d, renorm, out, pgen, hm);  // rand < pattempt_single
+    else gen_double_mol<W, Real>(s, rs, d, renorm, out, pgen, hm);
+    attempt_to_spawn(s, rs, parent, pgen, (double)hm, out);
+}
+
+// ---------------------------------------------------------------------------
+// Heat-bath generators (src/excit_gen_heat_bath_mol.F90), Real = double or float
+// ---------------------------------------------------------------------------
+constexpr int kHBMaxEl = 32;  // on-the-fly alias tables over the occupied orbitals
+
+__device__ __forceinline__ double rabs(double x) { return fabs(x); }
+__device__ __forceinline__ float rabs(float x) { return fabsf(x); }
+
+// Typed view of the heat-bath tables (layout in hgpu_heat_bath.h).
+template <typename Real>
+struct HBView {
+    const Real *i_w, *ij_w, *ija_w, *ija_tot, *ija_U, *ijab_tot, *ijab_U;
+    const uint8_t *ija_K, *ijab_K;
+    size_t nb;
+    __device__ __forceinline__ explicit HBView(const DevSys &s)
+        : i_w(static_cast<const Real *>(s.hb_i_w)), ij_w(static_cast<const Real *>(s.hb_ij_w)),
+          ija_w(static_cast<const Real *>(s.hb_ija_w)), ija_tot(static_cast<const Real *>(s.hb_ija_tot)),
+          ija_U(static_cast<const Real *>(s.hb_ija_U)), ijab_tot(static_cast<const Real *>(s.hb_ijab_tot)),
+          ijab_U(static_cast<const Real *>(s.hb_ijab_U)), ija_K(s.hb_ija_K), ijab_K(s.hb_ijab_K),
+          nb((size_t)s.nbasis) {}
+    // ij_weights(j,i), hb_ija%weights(a,j,i), hb_ija%weights_tot(j,i), hb_ijab%weights_tot(a,j,i)
+    __device__ __forceinline__ Real ij(int i, int j) const { return __ldg(&ij_w[i * nb + j]); }
+    __device__ __forceinline__ Real ija(int i, int j, int a) const { return __ldg(&ija_w[(i * nb + j) * nb + a]); }
+    __device__ __forceinline__ Real ija_t(int i, int j) const { return __ldg(&ija_tot[i * nb + j]); }
+    __device__ __forceinline__ Real ijab_t(int i, int j, int a) const {
+        return __ldg(&ijab_tot[(i * nb + j) * nb + a]);
+    }
+};
+
+// h_ijab of init_excit_mol_heat_bath (src/excit_gen_heat_bath_mol.F90:131-152):
+// |<ij|ab> - <ij|ba>| with i<j, a<b ordered, 0 for a disallowed excitation.  The
+// same expression as the host table builder, so in FP64 it is the stored weight.
+template <typename Real>
+__device__ __forceinline__ Real hb_weight(const DevSys &s, int i, int j, int a, int b) {
+    if (i == j || a == i || a == j || b == a || b == i || b == j) return (Real)0;
+    int it = i < j ? i : j, jt = i < j ? j : i;
+    int isymb = xsym(s, xsym(s, s.orbsym[it], s.orbsym[jt]), s.orbsym[a]);
+    bool spin = (ms_of(it) == ms_of(a) && ms_of(jt) == ms_of(b)) || (ms_of(it) == ms_of(b) && ms_of(jt) == ms_of(a));
+    if (!spin || s.orbsym[b] != isymb) return (Real)0;
+    int at = a < b ? a : b, bt = a < b ? b : a;
+    return rabs(sc2_mol<Real>(s, it, jt, at, bt, false));
+}
+
+// select_weighted_value (lib/local/alias.f90:62-98): generate_alias_tables
+// (:100-184) over n <= kHBMaxEl weights, then one draw.
+template <typename Real>
+__device__ __forceinline__ int hb_alias_select(RStream &rs, int n, const Real *w, Real tot) {
+    Real U[kHBMaxEl];
+    uint8_t K[kHBMaxEl], under[kHBMaxEl], over[kHBMaxEl];
+    int nu = 0, no = 0;
+    Real f = (Real)n / tot;
+    for (int i = 0; i < n; i++) {
+        Real u = w[i] * f;
+        U[i] = u;
+        if (u <= (Real)1) under[nu++] = (uint8_t)i;
+        else over[no++] = (uint8_t)i;
+        K[i] = (uint8_t)i;
+    }
+    while (no > 0 && nu > 0) {
+        int ov = over[no - 1], un = under[nu - 1];
+        K[un] = (uint8_t)ov;
+        nu--;
+        U[ov] = U[ov] - ((Real)1 - U[un]);
+        if (U[ov] < (Real)1) {
+            under[nu++] = over[no - 1];
+            no--;
+        }
+    }
+    double x = rs.next() * (double)n;
+    int k = (int)x;
+    x = x - (double)k;
+    return x < (double)U[k] ? k : (int)K[k];
+}
+
+// select_weighted_value_precalc (lib/local/alias.f90:13-60) on a stored table.
+template <typename Real>
+__device__ __forceinline__ int hb_alias_draw(RStream &rs, int n, const Real *U, const uint8_t *K) {
+    double x = rs.next() * (double)n;
+    int k = (int)x;
+    x = x - (double)k;
+    return x < (double)__ldg(&U[k]) ? k : (int)__ldg(&K[k]);
+}
+
+// psingle of a single i -> a inside the heat-bath double branch
+// (src/excit_gen_heat_bath_mol.F90:396-454): 0 if the single breaks spin or
+// symmetry, |h_ia|/(W + |h_ia|) below W = hb_ijab%weights_tot, else 0.5.
+template <int W, typename Real>
+__device__ __forceinline__ Real hb_psingle(const DevSys &s, const Det<W> &f, int i, int a, Real wtot) {
+    if (s.orbsym[a] != s.orbsym[i] || ms_of(a) != ms_of(i)) return (Real)0;
+    Real h = rabs(sc1_mol<W, Real>(s, f, i, a, false));
+    return h < wtot ? h / (wtot + h) : (Real)0.5;
+}
+
+// find_i_d_weights + select_ij_heat_bath (src/excit_gen_utils.f90:9-66, :142-167).
+template <typename Real>
+struct HBSel {
+    uint8_t occ[kHBMaxEl];
+    Real wi[kHBMaxEl], ijw[kHBMaxEl], jiw[kHBMaxEl];
+    Real wi_tot, ij_tot, ji_tot;
+    int i_ind, j_ind, i, j;
+};
+
+template <int W, typename Real>
+__device__ __forceinline__ bool hb_select_ij(const DevSys &s, const HBView<Real> &hb, RStream &rs, const Det<W> &f,
+                                             HBSel<Real> &q) {
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        uint64_t x = f.w[k];
+        while (x && n < kHBMaxEl) {
+            q.occ[n++] = (uint8_t)(64 * k + __ffsll((long long)x) - 1);
+            x &= x - 1;
+        }
+    }
+    const int nel = s.nel;
+    q.wi_tot = (Real)0;
+    for (int p = 0; p < nel; p++) {
+        q.wi[p] = __ldg(&hb.i_w[q.occ[p]]);
+        q.wi_tot = q.wi_tot + q.wi[p];
+    }
+    q.i_ind = hb_alias_select<Real>(rs, nel, q.wi, q.wi_tot);
+    q.i = q.occ[q.i_ind];
+    q.ij_tot = (Real)0;
+    for (int p = 0; p < nel; p++) {
+        q.ijw[p] = hb.ij(q.i, q.occ[p]);
+        q.ij_tot = q.ij_tot + q.ijw[p];
+    }
+    q.j_ind = -1;
+    q.j = -1;
+    if (!(q.ij_tot > (Real)0)) return false;
+    q.j_ind = hb_alias_select<Real>(rs, nel, q.ijw, q.ij_tot);
+    q.j = q.occ[q.j_ind];
+    q.ji_tot = (Real)0;
+    for (int p = 0; p < nel; p++) {
+        q.jiw[p] = hb.ij(q.j, q.occ[p]);
+        q.ji_tot = q.ji_tot + q.jiw[p];
+    }
+    return true;
+}
+
+// gen_excit_mol_heat_bath (src/excit_gen_heat_bath_mol.F90:258-547).
+template <int W, typename Real>
+__device__ void gen_heat_bath(const DevSys &s, RStream &rs, const Det<W> &f, Attempt &out, double &pgen, Real &hm) {
+    HBView<Real> hb(s);
+    HBSel<Real> q;
+    const int nb = s.nbasis;
+    out.nexcit = 2;
+    bool allowed = hb_select_ij<W, Real>(s, hb, rs, f, q);
+    int i = q.i, j = q.j;
+    out.from[0] = i;
+    out.from[1] = j;
+    if (!(allowed && rabs(hb.ija_t(i, j)) > (Real)0)) allowed = false;
+    int a = -1, b = -1;
+    bool dbl = true;
+    Real psingle = (Real)0, hmod_ia = (Real)0;
+    if (allowed) {
+        size_t o3 = ((size_t)i * nb + j) * nb;
+        a = hb_alias_draw<Real>(rs, nb, hb.ija_U + o3, hb.ija_K + o3);
+        if (!tbit<W>(f, a)) {
+            if (s.orbsym[a] == s.orbsym[i] && ms_of(a) == ms_of(i)) {
+                hmod_ia = rabs(sc1_mol<W, Real>(s, f, i, a, perm1<W>(f, i, a)));
+                double x = rs.next();
+                Real wt = hb.ijab_t(i, j, a);
+                psingle = hmod_ia < wt ? hmod_ia / (wt + hmod_ia) : (Real)0.5;
+                dbl = !(x < (double)psingle);
+            } else {
+                dbl = true;
+                psingle = (Real)0;
+            }
+        } else {
+            allowed = false;
+        }
+    }
+    Real pg = (Real)1, h = (Real)0;
+    if (allowed) {
+        if (dbl) {
+            size_t o4 = (((size_t)i * nb + j) * nb + a) * nb;
+            b = hb_alias_draw<Real>(rs, nb, hb.ijab_U + o4, hb.ijab_K + o4);
+            if (!tbit<W>(f, b)) {
+                const Real one = (Real)1;
+                Real p_ij = (q.wi[q.i_ind] / q.wi_tot) * (q.ijw[q.j_ind] / q.ij_tot);
+                Real p_ji = (q.wi[q.j_ind] / q.wi_tot) * (q.jiw[q.i_ind] / q.ji_tot);
+                Real pgen_ija = p_ij * (hb.ija(i, j, a) / hb.ija_t(i, j)) * (one - psingle) *
+                                (hb_weight<Real>(s, i, j, a, b) / hb.ijab_t(i, j, a));
+                psingle = hb_psingle<W, Real>(s, f, i, b, hb.ijab_t(i, j, b));
+                Real pgen_ijb = p_ij * (hb.ija(i, j, b) / hb.ija_t(i, j)) * (one - psingle) *
+                                (hb_weight<Real>(s, i, j, b, a) / hb.ijab_t(i, j, b));
+                psingle = hb_psingle<W, Real>(s, f, j, a, hb.ijab_t(j, i, a));
+                Real pgen_jia = p_ji * (hb.ija(j, i, a) / hb.ija_t(j, i)) * (one - psingle) *
+                                (hb_weight<Real>(s, j, i, a, b) / hb.ijab_t(j, i, a));
+                psingle = hb_psingle<W, Real>(s, f, j, b, hb.ijab_t(j, i, b));
+                Real pgen_jib = p_ji * (hb.ija(j, i, b) / hb.ija_t(j, i)) * (one - psingle) *
+                                (hb_weight<Real>(s, j, i, b, a) / hb.ijab_t(j, i, b));
+                pg = pgen_ija + pgen_ijb + pgen_jia + pgen_jib;
+                int f0 = i < j ? i : j, f1 = i < j ? j : i, t0 = a < b ? a : b, t1 = a < b ? b : a;
+                out.from[0] = f0;
+                out.from[1] = f1;
+                out.to[0] = t0;
+                out.to[1] = t1;
+                h = sc2_mol<Real>(s, f0, f1, t0, t1, perm2<W>(f, f0, f1, t0, t1));
+            } else {
+                allowed = false;
+            }
+        } else {
+            out.nexcit = 1;
+            out.from[1] = -1;
+            out.to[0] = a;
+            h = sc1_mol<W, Real>(s, f, i, a, perm1<W>(f, i, a));
+            pg = (Real)0;
+            for (int p = 0; p < s.nel; p++) {
+                int oq = q.occ[p];
+                // a q with no double excitation from (i,q) (weights_tot(q,i) = 0)
+                // contributes 0 * (0/0) in the reference, a NaN p_gen; it adds 0 here
+                if (i != oq && a != oq && hb.ija_t(i, oq) > (Real)0) {
+                    Real wt = hb.ijab_t(i, oq, a);
+                    Real psq = hmod_ia < wt ? hmod_ia / (wt + hmod_ia) : (Real)0.5;
+                    pg = pg + psq * (q.ijw[p] / q.ij_tot) * (hb.ija(i, oq, a) / hb.ija_t(i, oq));
+                }
+            }
+            pg = pg * (q.wi[q.i_ind] / q.wi_tot);
+        }
+    }
+    out.allowed = allowed;
+    pgen = allowed ? (double)pg : 1.0;
+    hm = allowed ? h : (Real)0;
+}
+
+// gen_excit_mol_heat_bath_uniform, double branch (src/excit_gen_heat_bath_mol.F90:619-705).
+template <int W, typename Real>
+__device__ void gen_heat_bath_uniform_double(const DevSys &s, RStream &rs, const Det<W> &f, Attempt &out,
+                                             double &pgen, Real &hm) {
+    HBView<Real> hb(s);
+    HBSel<Real> q;
+    const int nb = s.nbasis;
+    out.nexcit = 2;
+    bool allowed = hb_select_ij<W, Real>(s, hb, rs, f, q);
+    int i = q.i, j = q.j;
+    if (!(allowed && rabs(hb.ija_t(i, j)) > (Real)0)) allowed = false;
+    Real pij = (Real)0;
+    if (q.j_ind >= 0)
+        pij = ((q.wi[q.i_ind] / q.wi_tot) * (q.ijw[q.j_ind] / q.ij_tot)) +
+              ((q.wi[q.j_ind] / q.wi_tot) * (q.jiw[q.i_ind] / q.ji_tot));
+    if (j >= 0 && j < i) {
+        int t = j;
+        j = i;
+        i = t;
+    }
+    out.from[0] = i;
+    out.from[1] = j;
+    int a = -1, b = -1;
+    if (allowed) {
+        size_t o3 = ((size_t)i * nb + j) * nb;
+        a = hb_alias_draw<Real>(rs, nb, hb.ija_U + o3, hb.ija_K + o3);
+        if (rabs(hb.ijab_t(i, j, a)) > (Real)0 && !tbit<W>(f, a)) {
+            size_t o4 = (o3 + a) * nb;
+            b = hb_alias_draw<Real>(rs, nb, hb.ijab_U + o4, hb.ijab_K + o4);
+            allowed = !tbit<W>(f, b);
+        } else {
+            allowed = false;
+        }
+    }
+    Real pg = (Real)1, h = (Real)0;
+    if (allowed) {
+        int t0 = a < b ? a : b, t1 = a < b ? b : a;
+        out.to[0] = t0;
+        out.to[1] = t1;
+        h = sc2_mol<Real>(s, i, j, t0, t1, perm2<W>(f, i, j, t0, t1));
+        pg = ((Real)1 - (Real)s.pattempt_single) * pij *
+             (((hb.ija(i, j, a) / hb.ija_t(i, j)) * (hb_weight<Real>(s, i, j, a, b) / hb.ijab_t(i, j, a))) +
+              ((hb.ija(i, j, b) / hb.ija_t(i, j)) * (hb_weight<Real>(s, i, j, b, a) / hb.ijab_t(i, j, b))));
+    }
+    out.allowed = allowed;
+    pgen = (double)pg;
+    hm = h;
+}
+
+// spawn_standard + attempt_to_spawn with a heat-bath generator (heat_bath, or
+// heat_bath_uniform whose singles are gen_single_excit_mol's).
+template <int W, typename Real>
+__device__ void attempt_heat_bath(const DevSys &s, RStream &rs, const MolDet<W> &d, int64_t parent, Attempt &out) {
+    out.from[0] = out.from[1] = out.to[0] = out.to[1] = -1;
+    double pgen;
+    Real hm;
+    if (s.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH)
+        gen_heat_bath<W, Real>(s, rs, d.f, out, pgen, hm);
+    else if (rs.next_k() < s.t_single)  // rand < pattempt_single
+        gen_single_mol<W, Real>(s, rs, d, true, out, pgen, hm);
+    else
+        gen_heat_bath_uniform_double<W, Real>(s, rs, d.f, out, pgen, hm);
+    attempt_to_spawn(s, rs, parent, pgen, (double)hm, out);
 }
 
 // Child determinant of an attempt (create_excited_det, src/excitations.F90:365-406).

@@ -8,6 +8,7 @@
 // ncycles cycles costs ncycles graph launches and one small readback.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -16,6 +17,7 @@
 #include <vector>
 
 #include "../../include/hande_gpu.h"
+#include "hgpu_heat_bath.h"
 #include "hgpu_kernels.cuh"
 
 using namespace hgpu;
@@ -23,6 +25,8 @@ using namespace hgpu;
 struct hgpu_handle {
     hgpu_config cfg;
     int W, R, kind;
+    int sms;    // multiprocessors of the device
+    int gkind;  // generator kind of the spawning kernels (hgpu_kernels.cuh: kKind*, or the system kind)
     int device;
     cudaStream_t stream;
     DevBuffers b;
@@ -198,6 +202,43 @@ static int upload(hgpu_handle *h, const T *src, size_t n, const T **out) {
     return HGPU_OK;
 }
 
+// Heat-bath tables (hgpu_heat_bath.h) in the precision of the spawning path.
+template <typename Real>
+static int upload_heat_bath(hgpu_handle *h, const HeatBathTables &t, DevSys &s) {
+    auto put = [&](const std::vector<double> &v, const void **out) -> int {
+        std::vector<Real> r(v.size());
+        for (size_t k = 0; k < v.size(); k++) r[k] = (Real)v[k];
+        const Real *d;
+        int rc = upload(h, r.data(), r.size(), &d);
+        *out = d;
+        return rc;
+    };
+    int rc;
+    if ((rc = put(t.i_w, &s.hb_i_w))) return rc;
+    if ((rc = put(t.ij_w, &s.hb_ij_w))) return rc;
+    if ((rc = put(t.ija_w, &s.hb_ija_w))) return rc;
+    if ((rc = put(t.ija_tot, &s.hb_ija_tot))) return rc;
+    if ((rc = put(t.ija_U, &s.hb_ija_U))) return rc;
+    if ((rc = put(t.ijab_tot, &s.hb_ijab_tot))) return rc;
+    if ((rc = put(t.ijab_U, &s.hb_ijab_U))) return rc;
+    if ((rc = upload(h, t.ija_K.data(), t.ija_K.size(), &s.hb_ija_K))) return rc;
+    if ((rc = upload(h, t.ijab_K.data(), t.ijab_K.size(), &s.hb_ijab_K))) return rc;
+    return HGPU_OK;
+}
+
+static int build_heat_bath(hgpu_handle *h, const hgpu_system *sys, DevSys &s) {
+    HeatBathTables t;
+    if (!HeatBathBuilder(sys).build(t, h->cfg.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH)) return HGPU_ERR_OOM;
+    if (t.bias && h->cfg.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH) {
+        // init_excit_mol_heat_bath stops the calculation here (src/excit_gen_heat_bath_mol.F90:185-197)
+        last_error_text("Not all possible single excitations can be accounted for. Use another excitation generator.",
+                        "heat bath");
+        return HGPU_ERR_INVALID;
+    }
+    if (h->cfg.precision == HGPU_PREC_MIXED) return upload_heat_bath<float>(h, t, s);
+    return upload_heat_bath<double>(h, t, s);
+}
+
 static int build_system(hgpu_handle *h, const hgpu_system *sys) {
     DevSys &s = h->hsys;
     memset(&s, 0, sizeof(s));
@@ -227,6 +268,7 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
         s.pattempt_single = c.pattempt_single / (c.pattempt_single + c.pattempt_double);
         s.pattempt_double = 1.0 - c.pattempt_single;
     }
+    s.t_single = (uint64_t)std::ceil(std::ldexp(s.pattempt_single, 53));
     s.initiator_pop = c.initiator_pop;
     s.seed = (uint64_t)c.seed;
     for (int w = 0; w < kMaxWords; w++) s.f0[w] = w < s.nw ? c.ref_det[w] : 0;
@@ -334,6 +376,28 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
         }
         for (int k = 0; k < 2 * kMaxSym; k++) s.d_nbss[k] = (double)s.nbss[k];
         h->b.nk = 0;
+        {
+            // double-excitation p_gen table: pattempt_double * pgen_ij * (inv[n] * (inv[xb] + inv[xa])),
+            // each product and sum rounded as the generator writes it
+            int X = 1;
+            for (int k = 0; k < 2 * kMaxSym; k++) X = std::max(X, s.nbss[k] + 1);
+            int Nn = s.nvirt + 1;
+            std::vector<double> tab((size_t)Nn * X * X);
+            double c0 = s.pattempt_double * s.pgen_ij;
+            for (int n = 0; n < Nn; n++)
+                for (int xa = 0; xa < X; xa++)
+                    for (int xb = 0; xb < X; xb++) {
+                        double pb = 1.0 / (double)xb, pa = 1.0 / (double)xa;
+                        double pg = (1.0 / (double)n) * (pb + pa);
+                        tab[((size_t)n * X + xa) * X + xb] = c0 * pg;
+                    }
+            if ((rc = upload(h, tab.data(), tab.size(), &s.pg2))) return rc;
+            s.pg2_x = X;
+            s.pg2_n = Nn;
+        }
+        if (c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM) {
+            if ((rc = build_heat_bath(h, sys, s))) return rc;
+        }
     } else {
         return HGPU_ERR_INVALID;
     }
@@ -342,6 +406,32 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
     CK(cudaMemcpy(d, &s, sizeof(DevSys), cudaMemcpyHostToDevice));
     h->b.sys = d;
     return HGPU_OK;
+}
+
+// Binomial table C(p, k) (k = 0..nel, p = 0..nbasis-1, saturated at 2^64-1) of
+// the colexicographic rank; returns the bits of the largest rank, or 0 when
+// C(nbasis, nel) does not fit 64 bits (then the sort keys are the words).
+static int rank_bits(int nbasis, int nel, std::vector<uint64_t> &binom) {
+    const unsigned __int128 cap = ~(uint64_t)0;
+    std::vector<unsigned __int128> c((size_t)(nbasis + 1) * (nel + 1), 0);
+    auto C = [&](int p, int k) -> unsigned __int128 & { return c[(size_t)p * (nel + 1) + k]; };
+    for (int p = 0; p <= nbasis; p++) {
+        C(p, 0) = 1;
+        for (int k = 1; k <= nel && k <= p; k++) {
+            unsigned __int128 v = C(p - 1, k - 1) + (k <= p - 1 ? C(p - 1, k) : 0);
+            C(p, k) = v > cap ? cap : v;
+        }
+    }
+    unsigned __int128 total = C(nbasis, nel);
+    if (total >= cap) return 0;
+    if ((size_t)(nel + 1) * nbasis * sizeof(uint64_t) > 32768) return 0;  // shared-memory table of k_sort_hist
+    binom.assign((size_t)(nel + 1) * nbasis, 0);
+    for (int k = 0; k <= nel; k++)
+        for (int p = 0; p < nbasis; p++) binom[(size_t)k * nbasis + p] = (uint64_t)C(p, k);
+    uint64_t maxrank = (uint64_t)total - 1;
+    int bits = 1;
+    while (bits < 64 && (maxrank >> bits) != 0) bits++;
+    return bits;
 }
 
 static int alloc_lists(hgpu_handle *h) {
@@ -365,10 +455,44 @@ static int alloc_lists(hgpu_handle *h) {
     if (h->cfg.initiator_approx)
         if ((rc = dalloc(h, &b.sflag, (size_t)b.scap))) return rc;
     for (int k = 0; k < 2; k++) {
-        if ((rc = dalloc(h, &b.keys[k], (size_t)b.scap * W))) return rc;
+        if ((rc = dalloc(h, &b.keys[k], (size_t)b.scap * W))) return rc;  // key_words <= W
         if ((rc = dalloc(h, &b.idx[k], (size_t)b.scap))) return rc;
     }
-    if ((rc = dalloc(h, &b.hist, (size_t)kRadix * b.grid))) return rc;
+    // sort: ranks (when the colexicographic rank fits 64 bits) or determinant words
+    {
+        std::vector<uint64_t> binom;
+        int bits = rank_bits(h->hsys.nbasis, h->hsys.nel, binom);
+        b.use_rank = bits > 0 ? 1 : 0;
+        b.sort_nel = h->hsys.nel;
+        b.sort_nbasis = h->hsys.nbasis;
+        b.key_words = b.use_rank ? 1 : W;
+        int key_bits = b.use_rank ? bits : h->hsys.nbasis;
+        b.sort_passes = (key_bits + kRadixBits - 1) / kRadixBits;
+        if (b.sort_passes < 1) b.sort_passes = 1;
+        if (b.sort_passes > kMaxPasses) return HGPU_ERR_UNSUPPORTED;
+        // passes whose digit has at most 5 significant bits (the top of the key)
+        b.sort_few_from = b.sort_passes;
+        for (int p = 0; p < kMaxPasses; p++) {
+            int bits = key_bits - p * kRadixBits;
+            b.sort_few_values[p] = bits >= kRadixBits ? kRadix : (bits > 0 ? 1 << bits : 1);
+            if (p < b.sort_passes && bits <= 5 && b.sort_few_from == b.sort_passes) b.sort_few_from = p;
+        }
+        b.binom = nullptr;
+        if (b.use_rank) {
+            if ((rc = upload(h, binom.data(), binom.size(), &b.binom))) return rc;
+            if ((rc = dalloc(h, &b.skeys, (size_t)b.scap))) return rc;
+        }
+    }
+    if ((rc = dalloc(h, &b.ghist, (size_t)kMaxPasses * kRadix))) return rc;
+    if ((rc = dalloc(h, &b.gofs, (size_t)kMaxPasses * kRadix))) return rc;
+    CK(cudaMemset(b.ghist, 0, sizeof(uint32_t) * kMaxPasses * kRadix));
+    {
+        size_t tiles = (size_t)b.scap / OSConf<2>::tile + 2;
+        if ((rc = dalloc(h, &b.lookback, tiles * kRadix))) return rc;
+        CK(cudaMemset(b.lookback, 0, sizeof(uint64_t) * tiles * kRadix));
+        if ((rc = dalloc(h, &b.os_epoch, 1))) return rc;
+        CK(cudaMemset(b.os_epoch, 0, sizeof(uint32_t)));
+    }
     if ((rc = dalloc(h, &b.segpops, (size_t)b.scap * R))) return rc;
     if ((rc = dalloc(h, &b.segflag, (size_t)b.scap))) return rc;
     if ((rc = dalloc(h, &b.segkeep, (size_t)b.scap))) return rc;
@@ -381,16 +505,23 @@ static int alloc_lists(hgpu_handle *h) {
     size_t merged = (size_t)b.cap + (size_t)b.scap;
     if ((rc = dalloc(h, &b.mref, merged))) return rc;
     if ((rc = dalloc(h, &b.mkeep, merged))) return rc;
-    if ((rc = dalloc(h, &b.mpos, merged))) return rc;
+    if ((rc = dalloc(h, &b.tile_cnt, merged / kMergeTile + 2))) return rc;
+    if ((rc = dalloc(h, &b.tile_base, merged / kMergeTile + 2))) return rc;
     if ((rc = dalloc(h, &b.scan_part, (size_t)kMaxBlocks * 2))) return rc;
     if ((rc = dalloc(h, &b.part_d, (size_t)kMaxBlocks * 4))) return rc;
     if ((rc = dalloc(h, &b.part_i, (size_t)kMaxBlocks * 4))) return rc;
+    // Grids: sized to the lists, up to a few resident blocks per SM (every kernel
+    // loops over its work, so a grid only bounds the parallelism): a small
+    // calculation, one of many in a batch, does not launch thousands of idle blocks
+    {
+        auto clampi = [](int64_t v, int lo, int hi) { return (int)std::max<int64_t>(lo, std::min<int64_t>(hi, v)); };
+        const int sms = h->sms;
+        b.grid = clampi(b.cap / 4096, 8, std::min(4 * sms, kMaxBlocks));
+        b.spawn_grid = clampi(b.scap / 1024, 8, 8 * sms);
+        b.sort_grid = clampi(b.scap / OSConf<1>::tile + 1, 4, 3 * sms);  // 256 threads, ~58 KB shared memory
+    }
     if ((rc = dalloc(h, &b.state, 1))) return rc;
     CK(cudaMemset(b.state, 0, sizeof(DevState)));
-    {
-        int64_t nh = (int64_t)kRadix * b.grid;
-        CK(cudaMemcpy(&b.state->n_hist, &nh, sizeof(nh), cudaMemcpyHostToDevice));
-    }
     CK(cudaMemset(b.part_i, 0, sizeof(int64_t) * kMaxBlocks * 4));
     CK(cudaMemset(b.part_d, 0, sizeof(double) * kMaxBlocks * 4));
     return HGPU_OK;
@@ -430,8 +561,10 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
         if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM)
             return HGPU_ERR_UNSUPPORTED;
     } else if (sys->kind == HGPU_SYS_READ_IN) {
-        if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM)
+        bool hb = cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM;
+        if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM && !hb)
             return HGPU_ERR_UNSUPPORTED;
+        if (hb && sys->nel > kHBMaxEl) return HGPU_ERR_UNSUPPORTED;
     } else {
         return HGPU_ERR_INVALID;
     }
@@ -443,17 +576,28 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     h->W = sys->nwords;
     h->R = cfg->nspaces;
     h->kind = sys->kind;
+    h->gkind = sys->kind;
+    if (sys->kind == HGPU_SYS_READ_IN) {
+        if (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH) h->gkind = kKindHeatBath;
+        else if (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM) h->gkind = kKindHeatBathUniform;
+        else if (cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM) h->gkind = kKindReadInNoRenorm;
+    }
     h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;
     cudaGetDevice(&h->device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
     if (sms <= 0) sms = 148;
-    h->b.grid = sms * 4 > kMaxBlocks ? kMaxBlocks : sms * 4;
-    h->b.spawn_grid = sms * 8;
-    h->b.sort_passes = (sys->nbasis + kRadixBits - 1) / kRadixBits;
+    h->sms = sms;
     int rc = HGPU_OK;
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) rc = HGPU_ERR_CUDA;
     if (!rc) rc = build_system(h, sys);
+    if (!rc) {
+        h->b.fx_smem_bytes = sizeof(int64_t) * (size_t)fx_table_words(sys->kind, sys->nbasis, sys->norb);
+        if (set_kernel_attributes(h->b)) {
+            last_error_text(cudaGetErrorString(cudaGetLastError()), "cudaFuncSetAttribute");
+            rc = HGPU_ERR_CUDA;
+        }
+    }
     if (!rc) rc = alloc_lists(h);
     if (!rc) {
         cudaEventCreate(&h->ev0);
@@ -515,9 +659,7 @@ int32_t hgpu_initial_distribution(hgpu_handle *h) {
     DevState ds;
     int rc = read_state(h, &ds);
     if (rc) return rc;
-    int64_t nh = ds.n_hist;
     memset(&ds, 0, sizeof(ds));
-    ds.n_hist = nh;
     for (int s = 0; s < HGPU_MAX_SPACES; s++) {
         h->shift[s] = h->cfg.initial_shift;
         h->vary_shift[s] = 0;
@@ -561,7 +703,7 @@ static int launch_one_cycle(hgpu_handle *h) {
         if (!h->graph_ok[cur]) {
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-            launch_cycle(h->b, h->W, h->R, h->kind, h->cfg.precision, cur, h->stream);
+            launch_cycle(h->b, h->W, h->R, h->gkind, h->cfg.precision, cur, h->stream);
             CK(cudaStreamEndCapture(h->stream, &g));
             cudaError_t e = cudaGraphInstantiate(&h->graph[cur], g, 0);
             cudaGraphDestroy(g);
@@ -573,7 +715,7 @@ static int launch_one_cycle(hgpu_handle *h) {
         }
         CK(cudaGraphLaunch(h->graph[cur], h->stream));
     } else {
-        launch_cycle(h->b, h->W, h->R, h->kind, h->cfg.precision, cur, h->stream);
+        launch_cycle(h->b, h->W, h->R, h->gkind, h->cfg.precision, cur, h->stream);
         CK(cudaGetLastError());
     }
     h->cur = 1 - cur;
@@ -598,6 +740,142 @@ int32_t hgpu_run_cycles(hgpu_handle *h, int32_t ncycles) {
     if (rc) return rc;
     if (st.error_flags & HGPU_FLAG_SPAWN_OVERFLOW) return HGPU_ERR_SPAWN_OVERFLOW;
     if (st.error_flags & HGPU_FLAG_MAIN_OVERFLOW) return HGPU_ERR_MAIN_OVERFLOW;
+    if (st.error_flags & HGPU_FLAG_TIMEOUT) return HGPU_ERR_TIMEOUT;
+    return HGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches of handles: one graph launch per cycle for all of them
+// ---------------------------------------------------------------------------
+struct hgpu_batch {
+    std::vector<hgpu_handle *> hs;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    std::vector<int> parity[2];  // buffer parity of every handle each graph was built for
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+static void batch_free_graphs(hgpu_batch *b) {
+    for (int k = 0; k < 2; k++) {
+        if (b->exec[k]) cudaGraphExecDestroy(b->exec[k]);
+        b->exec[k] = nullptr;
+        b->parity[k].clear();
+    }
+}
+
+// One graph whose independent branches are the handles' cycles at the given
+// buffer parities (each captured on its handle's stream, then added as a child
+// graph, which the graph copies).
+static int batch_build(hgpu_batch *b, int slot, const std::vector<int> &par) {
+    cudaGraph_t g;
+    CK(cudaGraphCreate(&g, 0));
+    for (size_t i = 0; i < b->hs.size(); i++) {
+        hgpu_handle *h = b->hs[i];
+        cudaGraph_t hg;
+        cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            launch_cycle(h->b, h->W, h->R, h->gkind, h->cfg.precision, par[i], h->stream);
+            e = cudaStreamEndCapture(h->stream, &hg);
+        }
+        cudaGraphNode_t node;
+        if (e == cudaSuccess) {
+            e = cudaGraphAddChildGraphNode(&node, g, nullptr, 0, hg);
+            cudaGraphDestroy(hg);
+        }
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            last_error_text(cudaGetErrorString(e), "batch graph");
+            return HGPU_ERR_CUDA;
+        }
+    }
+    cudaError_t e = cudaGraphInstantiate(&b->exec[slot], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        b->exec[slot] = nullptr;
+        last_error_text(cudaGetErrorString(e), "cudaGraphInstantiate");
+        return HGPU_ERR_CUDA;
+    }
+    b->parity[slot] = par;
+    return HGPU_OK;
+}
+
+int32_t hgpu_batch_create(hgpu_handle *const *handles, int32_t n, hgpu_batch **out) {
+    if (!handles || n < 1 || !out) return HGPU_ERR_INVALID;
+    *out = nullptr;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    std::vector<hgpu_handle *> hs(handles, handles + n);
+    for (int i = 0; i < n; i++) {
+        if (!hs[i] || hs[i]->device != dev) return HGPU_ERR_INVALID;
+        for (int j = 0; j < i; j++)
+            if (hs[j] == hs[i]) return HGPU_ERR_INVALID;
+    }
+    hgpu_batch *b = new (std::nothrow) hgpu_batch();
+    if (!b) return HGPU_ERR_OOM;
+    b->hs = hs;
+    b->device = dev;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+        hgpu_batch_destroy(b);
+        return HGPU_ERR_CUDA;
+    }
+    *out = b;
+    return HGPU_OK;
+}
+
+int32_t hgpu_batch_run_cycles(hgpu_batch *b, int32_t ncycles) {
+    if (!b || ncycles < 0) return HGPU_ERR_INVALID;
+    std::vector<int> par(b->hs.size()), flip(b->hs.size());
+    for (size_t i = 0; i < b->hs.size(); i++) {
+        par[i] = b->hs[i]->cur;
+        flip[i] = 1 - par[i];
+        CK(cudaStreamSynchronize(b->hs[i]->stream));  // earlier per-handle work
+    }
+    int slot;
+    if (b->exec[0] && b->parity[0] == par) {
+        slot = 0;
+    } else if (b->exec[1] && b->parity[1] == par) {
+        slot = 1;
+    } else {
+        batch_free_graphs(b);
+        int rc = batch_build(b, 0, par);
+        if (!rc) rc = batch_build(b, 1, flip);
+        if (rc) return rc;
+        slot = 0;
+    }
+    CK(cudaEventRecord(b->ev0, b->stream));
+    for (int k = 0; k < ncycles; k++) {
+        CK(cudaGraphLaunch(b->exec[slot], b->stream));
+        slot ^= 1;
+    }
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    int first = HGPU_OK;
+    for (hgpu_handle *h : b->hs) {
+        h->cur ^= ncycles & 1;
+        h->iter += ncycles;
+        h->report_ms += ms;
+        DevState st;
+        int rc = read_state(h, &st);
+        if (!rc && (st.error_flags & HGPU_FLAG_SPAWN_OVERFLOW)) rc = HGPU_ERR_SPAWN_OVERFLOW;
+        if (!rc && (st.error_flags & HGPU_FLAG_MAIN_OVERFLOW)) rc = HGPU_ERR_MAIN_OVERFLOW;
+        if (!rc && (st.error_flags & HGPU_FLAG_TIMEOUT)) rc = HGPU_ERR_TIMEOUT;
+        if (rc && !first) first = rc;
+    }
+    return first;
+}
+
+int32_t hgpu_batch_destroy(hgpu_batch *b) {
+    if (!b) return HGPU_ERR_INVALID;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_free_graphs(b);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
     return HGPU_OK;
 }
 
@@ -653,6 +931,7 @@ int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
     if ((rc = write_state(h, &st))) return rc;
     if (out->error_flags & HGPU_FLAG_SPAWN_OVERFLOW) return HGPU_ERR_SPAWN_OVERFLOW;
     if (out->error_flags & HGPU_FLAG_MAIN_OVERFLOW) return HGPU_ERR_MAIN_OVERFLOW;
+    if (out->error_flags & HGPU_FLAG_TIMEOUT) return HGPU_ERR_TIMEOUT;
     return HGPU_OK;
 }
 
@@ -779,7 +1058,7 @@ int32_t hgpu_eval_excitations(hgpu_handle *h, const int64_t *parents, const int6
     char *base = static_cast<char *>(h->scratch);
     CK(cudaMemcpyAsync(base + off_par, parents, sizeof(int64_t) * h->W * n, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(base + off_pp, parent_pops, sizeof(int64_t) * n, cudaMemcpyHostToDevice, h->stream));
-    launch_eval_excitations(h->b, h->W, h->kind, h->cfg.precision, (const uint64_t *)(base + off_par),
+    launch_eval_excitations(h->b, h->W, h->gkind, h->cfg.precision, (const uint64_t *)(base + off_par),
                             (const int64_t *)(base + off_pp), n, iteration, (int32_t *)(base + off_or),
                             (double *)(base + off_pg), (double *)(base + off_hm), (int32_t *)(base + off_al),
                             (int64_t *)(base + off_ns), h->stream);
@@ -858,7 +1137,7 @@ int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int
     DevState before;
     int rc = read_state(h, &before);
     if (rc) return rc;
-    launch_cycle(h->b, h->W, h->R, h->kind, h->cfg.precision, h->cur, h->stream, &pm);
+    launch_cycle(h->b, h->W, h->R, h->gkind, h->cfg.precision, h->cur, h->stream, &pm);
     CK(cudaGetLastError());
     h->cur = 1 - h->cur;
     h->iter += 1;

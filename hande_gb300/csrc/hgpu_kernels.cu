@@ -41,12 +41,18 @@ template <>
 __device__ __forceinline__ int64_t zero_of<int64_t>() { return 0; }
 template <>
 __device__ __forceinline__ uint2 zero_of<uint2>() { return make_uint2(0, 0); }
+template <>
+__device__ __forceinline__ uint32_t zero_of<uint32_t>() { return 0u; }
 
 template <typename T>
 __device__ __forceinline__ T shfl_up(T v, int d);
 template <>
 __device__ __forceinline__ int64_t shfl_up<int64_t>(int64_t v, int d) {
     return __shfl_up_sync(FULL_MASK, (long long)v, d);
+}
+template <>
+__device__ __forceinline__ uint32_t shfl_up<uint32_t>(uint32_t v, int d) {
+    return __shfl_up_sync(FULL_MASK, v, d);
 }
 template <>
 __device__ __forceinline__ uint2 shfl_up<uint2>(uint2 v, int d) {
@@ -87,6 +93,7 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *tot) {
 }
 
 __device__ __forceinline__ double shfl_down_any(double v, int d) { return __shfl_down_sync(FULL_MASK, v, d); }
+__device__ __forceinline__ uint32_t shfl_down_any(uint32_t v, int d) { return __shfl_down_sync(FULL_MASK, v, d); }
 __device__ __forceinline__ int64_t shfl_down_any(int64_t v, int d) {
     return (int64_t)__shfl_down_sync(FULL_MASK, (long long)v, d);
 }
@@ -172,22 +179,6 @@ struct StoreExclusive {
     int64_t *out;
     __device__ void operator()(int64_t i, int64_t ex, int64_t) const { out[i] = ex; }
 };
-struct LoadMKeep {
-    const uint2 *a;
-    __device__ uint2 operator()(int64_t i) const { return a[i]; }
-};
-struct LoadHist {
-    const uint32_t *a;
-    __device__ int64_t operator()(int64_t i) const { return (int64_t)a[i]; }
-};
-struct StoreHist {
-    uint32_t *out;
-    __device__ void operator()(int64_t i, int64_t ex, int64_t) const { out[i] = (uint32_t)ex; }
-};
-struct StoreMPos {
-    uint2 *out;
-    __device__ void operator()(int64_t i, uint2 ex, uint2) const { out[i] = ex; }
-};
 
 // n_ptr points at an int64 count; for N*R lists a small kernel writes the product.
 __global__ void k_set_count(int64_t *dst, const int64_t *a, int64_t mul, const int64_t *b) {
@@ -249,6 +240,7 @@ __device__ __forceinline__ int64_t lower_bound_det(const uint64_t *list, int64_t
 __global__ void k_cycle_begin(DevState *st, const DevSys *sys) {
     st->iter += 1;
     st->n_spawn = 0;
+    st->spawn_next = 0;
     double np = (double)st->abs_pop[0] / (double)sys->real_factor;
     st->nattempts_cycle = llround(2.0 * np);
 }
@@ -350,84 +342,172 @@ __device__ __forceinline__ int64_t upper_bound_off(const int64_t *off, int64_t n
     return lo;
 }
 
+// Attempts per chunk a warp claims from the spawning kernel's work counter.
+constexpr int kSpawnChunk = 8 * 32;
+
+// A warp's chunk of attempts: (parent, space) slot, attempt number in the slot
+// and, for generators whose first draw chooses a single or a double excitation,
+// the stream position after that draw; dlist/slist hold the chunk offsets of
+// the doubles (or of every attempt) and of the singles.
+struct SpawnQueue {
+    uint32_t slot[kSpawnChunk];
+    uint32_t att[kSpawnChunk];
+    uint64_t bufk[kSpawnChunk];
+    uint8_t dlist[kSpawnChunk];
+    uint8_t slist[kSpawnChunk];
+};
+
+// One spawning attempt of a queued chunk entry; returns the spawned amount.
+template <int W, int KIND, typename Real>
+__device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
+                                               const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
+                                               bool drew, uint64_t bufk, bool single, Det<W> &child, int &sp,
+                                               uint32_t &info) {
+    int64_t i = slot / R;
+    sp = (int)(slot - i * R);
+    Det<W> f = load_det<W>(dets, i);
+    info = b.pinfo[i];
+    int64_t parent = (info >> sp) & 1u ? -1 : 1;
+    RStream rs;
+    rs.init(s.seed, P_SPAWN, sp, i, att, iter);
+    if (drew) {  // resume after the single/double draw
+        rs.block = 1;
+        rs.have = true;
+        rs.bufk = bufk;
+    }
+    Attempt at;
+    at.from[0] = at.from[1] = at.to[0] = at.to[1] = -1;
+    if (KIND == HGPU_SYS_HUB_K) {
+        attempt_hub_k<W>(s, t, rs, f, parent, false, at);
+    } else {
+        MolDet<W> d;
+        mol_decode<W>(s, f, d);
+        double pgen;
+        Real hm;
+        if (KIND == kKindHeatBath) gen_heat_bath<W, Real>(s, rs, f, at, pgen, hm);
+        else if (single) gen_single_mol<W, Real>(s, rs, d, KIND != kKindReadInNoRenorm, at, pgen, hm);
+        else if (KIND == kKindHeatBathUniform) gen_heat_bath_uniform_double<W, Real>(s, rs, f, at, pgen, hm);
+        else gen_double_mol<W, Real>(s, rs, d, KIND == HGPU_SYS_READ_IN, at, pgen, hm);
+        attempt_to_spawn(s, rs, parent, pgen, (double)hm, at);
+    }
+    if (at.nspawn != 0) child = excited<W>(f, at);
+    return at.nspawn;
+}
+
 template <int W, int KIND, typename Real>
 __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) {
     __shared__ DevSys s;
+    __shared__ SpawnQueue queue[kBlock / 32];
     extern __shared__ uint8_t smem[];
     stage_sys(s, b.sys);
     HubTables t = stage_hub(b.sys, smem);
     __syncthreads();
-    const DevState *st = b.state;
-    int64_t A = st->n_attempts;
-    int64_t NR = st->n_main * R;
-    uint64_t iter = (uint64_t)st->iter;
+    DevState *st = b.state;
+    const int64_t A = st->n_attempts;
+    const int64_t NR = st->n_main * R;
+    const uint64_t iter = (uint64_t)st->iter;
     const uint64_t *dets = b.dets[cur];
-    int lane = threadIdx.x & 31;
-    int64_t warp_base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
-    int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = warp_base; base < A; base += stride) {
-        int64_t a = base + lane;
-        bool want = false;
-        Det<W> child;
-        int64_t nspawn = 0;
-        int sp = 0;
-        uint64_t flagword = 0;
-        // (parent, space) slot of each attempt: one global search per warp,
-        // then a search among the next 32 slots (each slot holds >= 1 attempt
-        // unless a replica space is empty there), global search as fallback.
+    const int lane = threadIdx.x & 31;
+    SpawnQueue &q = queue[threadIdx.x >> 5];
+    // generators whose first draw is the single/double choice: the chunk is
+    // split by that draw so that each excitation type runs with the warp
+    // converged (a tenth of the attempts are singles, with their own code)
+    constexpr bool drew = KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm || KIND == kKindHeatBathUniform;
+    // Each warp claims chunks of kSpawnChunk consecutive attempts.  The (parent,
+    // space) slot of attempt a is the first k with aoff[k] > a; one binary search
+    // per chunk finds the slot of its first attempt, and every later step of 32
+    // attempts searches a window of 32 slots starting at the slot of the previous
+    // step's last attempt (a lower bound), with the binary search as fallback when
+    // a window holds no slot for an attempt (runs of zero-attempt slots).
+    for (;;) {
+        unsigned long long cbase = 0;
+        if (lane == 0) cbase = atomicAdd((unsigned long long *)&st->spawn_next, (unsigned long long)kSpawnChunk);
+        cbase = __shfl_sync(FULL_MASK, cbase, 0);
+        if ((int64_t)cbase >= A) break;
+        const int64_t cend = min((int64_t)cbase + kSpawnChunk, A);
         int64_t k0 = 0;
-        if (lane == 0) k0 = upper_bound_off(b.aoff, NR, base);
+        if (lane == 0) k0 = upper_bound_off(b.aoff, NR, (int64_t)cbase);
         k0 = __shfl_sync(FULL_MASK, k0, 0);
-        int64_t wv = k0 + lane < NR ? b.aoff[k0 + lane] : INT64_MAX;
-        uint32_t le_mask = 0;
+        int nd = 0, ns = 0;
+        for (int64_t base = (int64_t)cbase; base < cend; base += 32) {
+            int64_t a = base + lane;
+            int64_t wv = k0 + lane < NR ? b.aoff[k0 + lane] : INT64_MAX;
+            uint32_t le_mask = 0;
 #pragma unroll 1
-        for (int m = 0; m < 32; m++) {
-            int64_t v = __shfl_sync(FULL_MASK, wv, m);
-            if (v <= a) le_mask |= 1u << m;
-        }
-        if (a < A) {
-            int cnt = __popc(le_mask);
-            int64_t k = (cnt < 32 && k0 + cnt < NR) ? k0 + cnt : upper_bound_off(b.aoff, NR, a);
-            int64_t i = k / R;
-            sp = (int)(k - i * R);
-            int64_t att = a - (k > 0 ? b.aoff[k - 1] : 0);
-            Det<W> f = load_det<W>(dets, i);
-            uint32_t info = b.pinfo[i];
-            int64_t parent = (info >> sp) & 1u ? -1 : 1;
-            RStream rs;
-            rs.init(s.seed, P_SPAWN, sp, i, att, iter);
-            Attempt at;
-            if (KIND == HGPU_SYS_HUB_K) {
-                attempt_hub_k<W>(s, t, rs, f, parent, false, at);
-            } else {
-                MolDet<W> d;
-                mol_decode<W>(s, f, d);
-                attempt_mol<W, Real>(s, rs, d, parent, at);
+            for (int m = 0; m < 32; m++) {
+                int64_t v = __shfl_sync(FULL_MASK, wv, m);
+                if (v <= a) le_mask |= 1u << m;
             }
-            if (at.nspawn != 0) {
-                want = true;
-                nspawn = at.nspawn;
-                child = excited<W>(f, at);
-                flagword = (uint64_t)((info >> 2) & 3u) | ((uint64_t)a << 2);
+            int64_t k = NR;
+            bool valid = a < cend, single = false;
+            if (valid) {
+                int cnt = __popc(le_mask);
+                k = (cnt < 32 && k0 + cnt < NR) ? k0 + cnt : upper_bound_off(b.aoff, NR, a);
+                int64_t att = a - (k > 0 ? b.aoff[k - 1] : 0);
+                int off = (int)(a - (int64_t)cbase);
+                q.slot[off] = (uint32_t)k;
+                q.att[off] = (uint32_t)att;
+                if (drew) {
+                    int64_t i = k / R;
+                    RStream rs;
+                    rs.init(s.seed, P_SPAWN, (uint32_t)(k - i * R), i, att, iter);
+                    single = rs.next_k() < s.t_single;  // rs.next() < pattempt_single
+                    q.bufk[off] = rs.bufk;
+                }
             }
+            uint32_t dball = __ballot_sync(FULL_MASK, valid && !single);
+            uint32_t sball = __ballot_sync(FULL_MASK, valid && single);
+            int off = (int)(a - (int64_t)cbase);
+            if (valid && !single) q.dlist[nd + __popc(dball & lanemask_lt())] = (uint8_t)off;
+            if (valid && single) q.slist[ns + __popc(sball & lanemask_lt())] = (uint8_t)off;
+            nd += __popc(dball);
+            ns += __popc(sball);
+            // slot of the last valid attempt of this step: lower bound for the next step
+            int last = (int)min((int64_t)31, cend - 1 - base);
+            k0 = __shfl_sync(FULL_MASK, k, last);
         }
-        uint32_t ball = __ballot_sync(FULL_MASK, want);
-        if (ball) {
-            int leader = __ffs(ball) - 1;
-            unsigned long long basepos = 0;
-            if (lane == leader) basepos = atomicAdd((unsigned long long *)&b.state->n_spawn, (unsigned long long)__popc(ball));
-            basepos = __shfl_sync(FULL_MASK, basepos, leader);
-            if (want) {
-                int64_t pos = (int64_t)basepos + __popc(ball & lanemask_lt());
-                if (pos < b.scap) {
-                    store_det<W>(b.sdets, pos, child);
-                    for (int q = 0; q < R; q++) b.spops[pos * R + q] = q == sp ? nspawn : 0;
-                    if (b.sflag) b.sflag[pos] = flagword;
-                } else {
-                    atomicOr(&b.state->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+        __syncwarp();
+        // doubles (or every attempt), then singles, 32 at a time
+        for (int pass = 0; pass < 2; pass++) {
+            const int n = pass == 0 ? nd : ns;
+            const uint8_t *list = pass == 0 ? q.dlist : q.slist;
+            for (int j0 = 0; j0 < n; j0 += 32) {
+                bool want = false;
+                Det<W> child;
+                int64_t nspawn = 0;
+                int sp = 0;
+                uint64_t flagword = 0;
+                if (j0 + lane < n) {
+                    int off = list[j0 + lane];
+                    uint32_t info;
+                    nspawn = spawn_entry<W, KIND, Real>(s, t, b, R, dets, iter, q.slot[off], q.att[off], drew,
+                                                        q.bufk[off], pass == 1, child, sp, info);
+                    if (nspawn != 0) {
+                        want = true;
+                        flagword = (uint64_t)((info >> 2) & 3u) | ((uint64_t)(cbase + off) << 2);
+                    }
+                }
+                uint32_t ball = __ballot_sync(FULL_MASK, want);
+                if (ball) {
+                    int leader = __ffs(ball) - 1;
+                    unsigned long long basepos = 0;
+                    if (lane == leader)
+                        basepos = atomicAdd((unsigned long long *)&st->n_spawn, (unsigned long long)__popc(ball));
+                    basepos = __shfl_sync(FULL_MASK, basepos, leader);
+                    if (want) {
+                        int64_t pos = (int64_t)basepos + __popc(ball & lanemask_lt());
+                        if (pos < b.scap) {
+                            store_det<W>(b.sdets, pos, child);
+                            for (int qq = 0; qq < R; qq++) b.spops[pos * R + qq] = qq == sp ? nspawn : 0;
+                            if (b.sflag) b.sflag[pos] = flagword;
+                        } else {
+                            atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+                        }
+                    }
                 }
             }
         }
+        __syncwarp();
     }
 }
 
@@ -438,116 +518,11 @@ __global__ void k_clamp_spawns(DevState *st, int64_t scap) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// Stable LSD radix sort of the spawned determinants (8-bit digits)
-// ---------------------------------------------------------------------------
-template <int W>
-__device__ __forceinline__ uint32_t digit_of(const uint64_t *keys, int64_t i, int shift) {
-    return (uint32_t)((keys[i * W + (shift >> 6)] >> (shift & 63)) & (kRadix - 1));
-}
+}  // namespace hgpu
 
-template <int W>
-__global__ void __launch_bounds__(kRadix) k_radix_up(const uint64_t *keys, const int64_t *n_ptr, int shift,
-                                                     uint32_t *hist) {
-    __shared__ uint32_t h[kRadix];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    int64_t n = *n_ptr, begin, end;
-    chunk_range(n, begin, end);
-    for (int64_t i = begin + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&h[digit_of<W>(keys, i, shift)], 1u);
-    __syncthreads();
-    hist[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
-}
+#include "hgpu_sort.cuh"
 
-__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t *hist, int total) {
-    // exclusive scan of total (= kRadix * grid) counts, digit-major
-    __shared__ uint32_t carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int base = 0; base < total; base += 1024) {
-        int i = base + threadIdx.x;
-        int64_t v = i < total ? (int64_t)hist[i] : 0;
-        int64_t tot;
-        int64_t ex = block_exclusive_scan<int64_t>(v, &tot);
-        uint32_t c = carry;
-        if (i < total) hist[i] = (uint32_t)(ex + c);
-        __syncthreads();
-        if (threadIdx.x == 0) carry = c + (uint32_t)tot;
-        __syncthreads();
-    }
-}
-
-template <int W>
-__global__ void __launch_bounds__(kRadix) k_radix_down(const uint64_t *keys_in, const uint32_t *idx_in,
-                                                       uint64_t *keys_out, uint32_t *idx_out, const int64_t *n_ptr,
-                                                       int shift, const uint32_t *hist) {
-    constexpr int NW = kRadix / 32;  // warps
-    __shared__ uint32_t wcnt[NW][kRadix];
-    __shared__ uint32_t boff[kRadix];
-    __shared__ uint32_t ttot[kRadix];
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int64_t n = *n_ptr, begin, end;
-    chunk_range(n, begin, end);
-    boff[threadIdx.x] = hist[(int64_t)threadIdx.x * gridDim.x + blockIdx.x];
-    const int64_t tile = (int64_t)NW * kSortItems * 32;
-    for (int64_t tb = begin; tb < end; tb += tile) {
-#pragma unroll
-        for (int w = 0; w < NW; w++) wcnt[w][threadIdx.x] = 0;
-        __syncthreads();
-        uint64_t kv[kSortItems][W];
-        uint32_t iv[kSortItems], off[kSortItems], dg[kSortItems];
-#pragma unroll
-        for (int r = 0; r < kSortItems; r++) {
-            int64_t e = tb + ((int64_t)(warp * kSortItems + r)) * 32 + lane;
-            bool valid = e < end;
-            uint32_t mask = __ballot_sync(FULL_MASK, valid);
-            dg[r] = 0xFFFFFFFFu;
-            if (valid) {
-#pragma unroll
-                for (int k = 0; k < W; k++) kv[r][k] = keys_in[e * W + k];
-                iv[r] = idx_in ? idx_in[e] : (uint32_t)e;
-                uint32_t d = (uint32_t)((kv[r][shift >> 6] >> (shift & 63)) & (kRadix - 1));
-                dg[r] = d;
-                uint32_t peers = __match_any_sync(mask, d);
-                int leader = __ffs(peers) - 1;
-                uint32_t rank = __popc(peers & lanemask_lt());
-                uint32_t old = 0;
-                if (lane == leader) {
-                    old = wcnt[warp][d];
-                    wcnt[warp][d] = old + __popc(peers);
-                }
-                old = __shfl_sync(mask, old, leader);
-                off[r] = old + rank;
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-        {
-            uint32_t run = 0;
-#pragma unroll
-            for (int w = 0; w < NW; w++) {
-                uint32_t c = wcnt[w][threadIdx.x];
-                wcnt[w][threadIdx.x] = run;
-                run += c;
-            }
-            ttot[threadIdx.x] = run;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < kSortItems; r++) {
-            if (dg[r] != 0xFFFFFFFFu) {
-                uint32_t d = dg[r];
-                int64_t pos = (int64_t)boff[d] + wcnt[warp][d] + off[r];
-#pragma unroll
-                for (int k = 0; k < W; k++) keys_out[pos * W + k] = kv[r][k];
-                idx_out[pos] = iv[r];
-            }
-        }
-        __syncthreads();
-        boff[threadIdx.x] += ttot[threadIdx.x];
-        __syncthreads();
-    }
-}
+namespace hgpu {
 
 // ---------------------------------------------------------------------------
 // Self-annihilation of the sorted spawned list
@@ -557,13 +532,15 @@ __device__ __forceinline__ int sgn1(int64_t x) { return x >= 0 ? 1 : -1; }
 // Fortran sign(1, int(x)): int() keeps the low 32 bits of an int64.
 __device__ __forceinline__ int sign1_int32(int64_t x) { return (int32_t)(uint32_t)(uint64_t)x >= 0 ? 1 : -1; }
 
-template <int W>
+// Sorted keys (KW words: the rank, or the determinant) are equal exactly when
+// the determinants are.
+template <int KW>
 __global__ void __launch_bounds__(kBlock) k_seg_reduce(DevBuffers b, int R, const uint64_t *keys, const uint32_t *idx,
                                                        int initiator) {
     int64_t S = b.state->n_spawn;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
-        Det<W> ki = load_det<W>(keys, i);
-        bool head = i == 0 || !det_eq<W>(load_det<W>(keys, i - 1), ki);
+        Det<KW> ki = load_det<KW>(keys, i);
+        bool head = i == 0 || !det_eq<KW>(load_det<KW>(keys, i - 1), ki);
         if (!head) {
             b.segkeep[i] = 0;
             continue;
@@ -571,7 +548,7 @@ __global__ void __launch_bounds__(kBlock) k_seg_reduce(DevBuffers b, int R, cons
         int64_t sum[2] = {0, 0}, ip[2] = {0, 0}, ev[2] = {0, 0}, firstpop[2] = {0, 0};
         uint64_t minord = ~0ull, firstflag = 0;
         for (int64_t j = i; j < S; j++) {
-            if (j > i && !det_eq<W>(load_det<W>(keys, j), ki)) break;
+            if (j > i && !det_eq<KW>(load_det<KW>(keys, j), ki)) break;
             uint32_t e = idx[j];
             uint64_t fl = initiator ? b.sflag[e] : 0;
             for (int q = 0; q < R; q++) {
@@ -608,13 +585,16 @@ __global__ void __launch_bounds__(kBlock) k_seg_reduce(DevBuffers b, int R, cons
     }
 }
 
-template <int W>
-__global__ void __launch_bounds__(kBlock) k_seg_compact(DevBuffers b, int R, const uint64_t *keys) {
+// Unique entries in sorted order; the determinant comes from the sorted keys, or
+// through the permutation from the spawned list when the keys are ranks.
+template <int W, bool RANK>
+__global__ void __launch_bounds__(kBlock) k_seg_compact(DevBuffers b, int R, const uint64_t *keys,
+                                                        const uint32_t *idx) {
     int64_t S = b.state->n_spawn;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
         if (!b.segkeep[i]) continue;
         int64_t u = b.segpos[i];
-        store_det<W>(b.udets, u, load_det<W>(keys, i));
+        store_det<W>(b.udets, u, RANK ? load_det<W>(b.sdets, idx[i]) : load_det<W>(keys, i));
         for (int q = 0; q < R; q++) b.upops[u * R + q] = b.segpops[i * R + q];
         b.uflag[u] = b.segflag[i];
     }
@@ -632,8 +612,10 @@ __device__ __forceinline__ void round_pops(const DevSys &s, int64_t *p, int R, u
         if (av < s.real_factor && v != 0) {
             RStream rs;
             rs.init(s.seed, purpose, q, idx, 0, iter);
-            double r = rs.next() * (double)s.real_factor;
-            p[q] = ((double)av > r) ? isign64(s.real_factor, v) : 0;
+            // (double)av > u * real_factor with real_factor = 2^31 and u = k 2^-53,
+            // both sides exact: av * 2^22 > k in integers
+            uint64_t k = rs.next_k();
+            p[q] = (((uint64_t)av << 22) > k) ? isign64(s.real_factor, v) : 0;
         }
     }
 }
@@ -664,19 +646,32 @@ __global__ void __launch_bounds__(kBlock) k_merge_splits(DevBuffers b, int cur) 
 // (src/annihilation.f90:294-486), remove_unoccupied_dets' rounding (:537-598),
 // round_low_population_spawns (:600-675), the merged rank of every element and,
 // densely over the tile's new determinants, their K_ii (insert_new_walker :855).
+// Each thread takes kMergeTile/kBlock consecutive merged positions of the tile:
+// one merge-path search finds where they start, then a sequential merge of the
+// two sorted slices (main entry first among equals) walks them.
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_merge_tiles(DevBuffers b, int R, int cur) {
+    constexpr int PER = kMergeTile / kBlock;
     __shared__ DevSys s;
     __shared__ uint64_t tdet[kMergeTile * W];
     __shared__ int32_t newlist[kMergeTile];
     __shared__ int nnew;
+    extern __shared__ int64_t fx_smem[];  // exact-diagonal tables (fx_table_words)
     stage_sys(s, b.sys);
+    __syncthreads();
+    const FxTabs tb = stage_fx(s, fx_smem);
     __syncthreads();
     int64_t U = b.state->n_uniq, N = b.state->n_main, L = N + U;
     uint64_t iter = (uint64_t)b.state->iter;
     int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
     const uint64_t *mdets = b.dets[cur];
     int64_t *mpops = b.pops[cur];
+    auto tile_det = [&](int k) {
+        Det<W> x;
+#pragma unroll
+        for (int w = 0; w < W; w++) x.w[w] = tdet[k * W + w];
+        return x;
+    };
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int64_t d0 = t * kMergeTile, d1 = d0 + kMergeTile < L ? d0 + kMergeTile : L;
         int64_t i0 = b.msplit[t], i1 = b.msplit[t + 1];
@@ -689,119 +684,128 @@ __global__ void __launch_bounds__(kBlock) k_merge_tiles(DevBuffers b, int R, int
         }
         if (threadIdx.x == 0) nnew = 0;
         __syncthreads();
-        for (int k = threadIdx.x; k < nm + ns; k += blockDim.x) {
-            Det<W> d;
-#pragma unroll
-            for (int w = 0; w < W; w++) d.w[w] = tdet[k * W + w];
-            if (k < nm) {
-                // main entry: how many tile spawns are strictly below it
-                int lo = 0, hi = ns;
-                while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    Det<W> x;
-#pragma unroll
-                    for (int w = 0; w < W; w++) x.w[w] = tdet[(nm + mid) * W + w];
-                    if (det_less<W>(x, d)) lo = mid + 1;
-                    else hi = mid;
-                }
-                int64_t i = i0 + k, j = j0 + lo;
-                bool hit = false;
-                if (lo < ns) {
-                    Det<W> x;
-#pragma unroll
-                    for (int w = 0; w < W; w++) x.w[w] = tdet[(nm + lo) * W + w];
-                    hit = det_eq<W>(x, d);
-                } else if (j < U) {
-                    hit = det_eq<W>(load_det<W>(b.udets, j), d);
-                }
-                int64_t p[2] = {0, 0};
-                for (int q = 0; q < R; q++) p[q] = mpops[i * R + q];
-                if (hit) {
-                    uint64_t fl = b.uflag[j];
-                    for (int q = 0; q < R; q++) {
-                        int64_t sp = b.upops[j * R + q];
-                        if (!s.initiator || p[q] != 0) p[q] += sp;
-                        else if (!((fl >> q) & 1)) p[q] = sp;
-                    }
-                }
-                if (s.real_amplitudes) round_pops(s, p, R, P_ROUND_MAIN, i, iter);
-                bool nz = false;
-                for (int q = 0; q < R; q++) {
-                    mpops[i * R + q] = p[q];
-                    nz = nz || p[q] != 0;
-                }
-                int64_t rank = i + j;
-                b.mref[rank] = i;
-                b.mkeep[rank] = make_uint2(nz ? 1u : 0u, nz ? 1u : 0u);
-            } else {
-                int bb = k - nm;
-                // spawned entry: how many tile main entries are at or below it
-                int lo = 0, hi = nm;
-                while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    Det<W> x;
-#pragma unroll
-                    for (int w = 0; w < W; w++) x.w[w] = tdet[mid * W + w];
-                    if (!det_less<W>(d, x)) lo = mid + 1;
-                    else hi = mid;
-                }
-                int64_t j = j0 + bb;
-                bool hit;
-                if (lo > 0) {
-                    Det<W> x;
-#pragma unroll
-                    for (int w = 0; w < W; w++) x.w[w] = tdet[(lo - 1) * W + w];
-                    hit = det_eq<W>(x, d);
-                } else {
-                    hit = i0 > 0 && det_eq<W>(load_det<W>(mdets, i0 - 1), d);
-                }
-                uint32_t keep = 0;
-                if (!hit) {
-                    int64_t sp[2] = {0, 0};
-                    for (int q = 0; q < R; q++) sp[q] = b.upops[j * R + q];
-                    bool discard = false;
-                    if (s.initiator) {
+        uint32_t kept_main = 0, kept_any = 0;  // this thread's elements of the tile
+        const int p0 = threadIdx.x * PER;
+        const int plen = min(PER, nm + ns - p0);
+        if (plen > 0) {
+            // main entries among the first p0 merged elements of the tile
+            int lo = max(0, p0 - ns), hi = min(p0, nm);
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (!det_less<W>(tile_det(nm + p0 - 1 - mid), tile_det(mid))) lo = mid + 1;
+                else hi = mid;
+            }
+            int a = lo, bb = p0 - lo;
+            for (int q = 0; q < plen; q++) {
+                const int64_t rank = d0 + p0 + q;
+                bool take_main = a < nm && (bb >= ns || !det_less<W>(tile_det(nm + bb), tile_det(a)));
+                if (take_main) {
+                    Det<W> d = tile_det(a);
+                    int64_t i = i0 + a, j = j0 + bb;
+                    bool hit;
+                    if (bb < ns) hit = det_eq<W>(tile_det(nm + bb), d);
+                    else hit = j < U && det_eq<W>(load_det<W>(b.udets, j), d);
+                    int64_t p[2] = {0, 0};
+                    for (int qq = 0; qq < R; qq++) p[qq] = mpops[i * R + qq];
+                    if (hit) {
                         uint64_t fl = b.uflag[j];
-                        discard = true;
-                        for (int q = 0; q < R; q++) {
-                            if ((fl >> q) & 1) sp[q] = 0;
-                            else discard = false;
+                        for (int qq = 0; qq < R; qq++) {
+                            int64_t sp = b.upops[j * R + qq];
+                            if (!s.initiator || p[qq] != 0) p[qq] += sp;
+                            else if (!((fl >> qq) & 1)) p[qq] = sp;
                         }
                     }
-                    if (!discard && s.real_amplitudes) round_pops(s, sp, R, P_ROUND_SPAWN, j, iter);
+                    if (s.real_amplitudes) round_pops(s, p, R, P_ROUND_MAIN, i, iter);
                     bool nz = false;
-                    for (int q = 0; q < R; q++) {
-                        b.upops[j * R + q] = sp[q];
-                        nz = nz || sp[q] != 0;
+                    for (int qq = 0; qq < R; qq++) {
+                        mpops[i * R + qq] = p[qq];
+                        nz = nz || p[qq] != 0;
                     }
-                    keep = discard ? 0u : (s.real_amplitudes ? (nz ? 1u : 0u) : 1u);
-                    if (keep) newlist[atomicAdd(&nnew, 1)] = k;
+                    b.mref[rank] = i;
+                    b.mkeep[rank] = make_uint2(nz ? 1u : 0u, nz ? 1u : 0u);
+                    kept_main += nz ? 1u : 0u;
+                    kept_any += nz ? 1u : 0u;
+                    a++;
+                } else {
+                    Det<W> d = tile_det(nm + bb);
+                    int64_t j = j0 + bb;
+                    bool hit;
+                    if (a > 0) hit = det_eq<W>(tile_det(a - 1), d);
+                    else hit = i0 > 0 && det_eq<W>(load_det<W>(mdets, i0 - 1), d);
+                    uint32_t keep = 0;
+                    if (!hit) {
+                        int64_t sp[2] = {0, 0};
+                        for (int qq = 0; qq < R; qq++) sp[qq] = b.upops[j * R + qq];
+                        bool discard = false;
+                        if (s.initiator) {
+                            uint64_t fl = b.uflag[j];
+                            discard = true;
+                            for (int qq = 0; qq < R; qq++) {
+                                if ((fl >> qq) & 1) sp[qq] = 0;
+                                else discard = false;
+                            }
+                        }
+                        if (!discard && s.real_amplitudes) round_pops(s, sp, R, P_ROUND_SPAWN, j, iter);
+                        bool nz = false;
+                        for (int qq = 0; qq < R; qq++) {
+                            b.upops[j * R + qq] = sp[qq];
+                            nz = nz || sp[qq] != 0;
+                        }
+                        keep = discard ? 0u : (s.real_amplitudes ? (nz ? 1u : 0u) : 1u);
+                        if (keep) newlist[atomicAdd(&nnew, 1)] = nm + bb;
+                    }
+                    b.mref[rank] = -(j + 1);
+                    b.mkeep[rank] = make_uint2(0u, keep);
+                    kept_any += keep;
+                    bb++;
                 }
-                int64_t rank = j + i0 + lo;
-                b.mref[rank] = -(j + 1);
-                b.mkeep[rank] = make_uint2(0u, keep);
             }
         }
+        // kept counts of the tile, for the tile-level scan of output positions
+        uint32_t tm = block_reduce_sum<uint32_t>(kept_main);
+        uint32_t ta = block_reduce_sum<uint32_t>(kept_any);
+        if (threadIdx.x == 0) b.tile_cnt[t] = make_uint2(tm, ta);
         __syncthreads();
         // K_ii of the tile's new determinants, one dense pass
         int n_new = nnew;
         for (int k = threadIdx.x; k < n_new; k += blockDim.x) {
             int e = newlist[k];
-            Det<W> d;
-#pragma unroll
-            for (int w = 0; w < W; w++) d.w[w] = tdet[e * W + w];
-            b.ukii[j0 + (e - nm)] = kii_of<W>(s, d);
+            b.ukii[j0 + (e - nm)] = kii_of<W>(s, tile_det(e), tb);
         }
         __syncthreads();
     }
 }
 
+// Exclusive scan of the per-tile kept counts (kept main, kept any) into the
+// tiles' output offsets; the totals go to n_merged_keep.
+__global__ void __launch_bounds__(1024) k_merge_tile_scan(DevBuffers b) {
+    const int64_t L = b.state->n_main + b.state->n_uniq;
+    const int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
+    __shared__ uint2 carry;
+    if (threadIdx.x == 0) carry = make_uint2(0u, 0u);
+    __syncthreads();
+    for (int64_t t0 = 0; t0 < ntiles; t0 += blockDim.x) {
+        int64_t t = t0 + threadIdx.x;
+        uint2 v = t < ntiles ? b.tile_cnt[t] : make_uint2(0u, 0u);
+        uint2 tot;
+        uint2 ex = block_exclusive_scan<uint2>(v, &tot);
+        uint2 c = carry;
+        if (t < ntiles) b.tile_base[t] = ex + c;
+        __syncthreads();
+        if (threadIdx.x == 0) carry = c + tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *reinterpret_cast<uint2 *>(&b.state->n_merged_keep) = carry;
+}
+
+// The survivors of each merge tile, in merged order, written contiguously from
+// the tile's output offset (insert_new_walkers' compaction,
+// src/annihilation.f90:677-818).  With more survivors than the list holds,
+// only the main-list survivors are kept (the overflow is flagged).
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_merge_scatter(DevBuffers b, int R, int cur) {
-    __shared__ DevSys s;
-    stage_sys(s, b.sys);
-    __syncthreads();
-    int64_t U = b.state->n_uniq, N = b.state->n_main, M = U + N;
+    int64_t U = b.state->n_uniq, N = b.state->n_main, L = U + N;
+    const int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
     uint2 tot = *reinterpret_cast<const uint2 *>(&b.state->n_merged_keep);
     bool overflow = (int64_t)tot.y > b.cap;
     const uint64_t *mdets = b.dets[cur];
@@ -811,29 +815,46 @@ __global__ void __launch_bounds__(kBlock) k_merge_scatter(DevBuffers b, int R, i
     int64_t *opops = b.pops[1 - cur];
     double *okii = b.kii[1 - cur];
     int64_t ap0 = 0, ap1 = 0;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < M; r += (int64_t)gridDim.x * blockDim.x) {
-        uint2 k = b.mkeep[r];
-        if (!k.y) continue;
-        if (overflow && !k.x) continue;
-        uint2 pos2 = b.mpos[r];
-        int64_t dst = overflow ? (int64_t)pos2.x : (int64_t)pos2.y;
-        if (dst >= b.cap) continue;
-        int64_t ref = b.mref[r];
-        int64_t p[2] = {0, 0};
-        if (ref >= 0) {
-            store_det<W>(odets, dst, load_det<W>(mdets, ref));
-            for (int q = 0; q < R; q++) p[q] = mpops[ref * R + q];
-            okii[dst] = mkii[ref];
-        } else {
-            int64_t j = -ref - 1;
-            Det<W> d = load_det<W>(b.udets, j);
-            store_det<W>(odets, dst, d);
-            for (int q = 0; q < R; q++) p[q] = b.upops[j * R + q];
-            okii[dst] = b.ukii[j];  // K_ii from the merge tiles (insert_new_walker)
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t d0 = t * kMergeTile, d1 = min(d0 + kMergeTile, L);
+        const uint2 base = b.tile_base[t];
+        int64_t run = overflow ? (int64_t)base.x : (int64_t)base.y;
+        for (int64_t r0 = d0; r0 < d1; r0 += blockDim.x) {
+            int64_t r = r0 + threadIdx.x;
+            uint2 k = r < d1 ? b.mkeep[r] : make_uint2(0u, 0u);
+            uint32_t keep = overflow ? k.x : k.y;
+            // the survivor's data is loaded before the scan of positions, which
+            // hides the loads' latency
+            Det<W> det;
+            int64_t p[2] = {0, 0};
+            double kii = 0.0;
+            if (keep) {
+                int64_t ref = b.mref[r];
+                if (ref >= 0) {
+                    det = load_det<W>(mdets, ref);
+                    for (int q = 0; q < R; q++) p[q] = mpops[ref * R + q];
+                    kii = mkii[ref];
+                } else {
+                    int64_t j = -ref - 1;
+                    det = load_det<W>(b.udets, j);
+                    for (int q = 0; q < R; q++) p[q] = b.upops[j * R + q];
+                    kii = b.ukii[j];  // K_ii from the merge tiles (insert_new_walker)
+                }
+            }
+            int64_t ktot;
+            int64_t ex = block_exclusive_scan<int64_t>((int64_t)keep, &ktot);
+            if (keep) {
+                int64_t dst = run + ex;
+                if (dst < b.cap) {
+                    store_det<W>(odets, dst, det);
+                    for (int q = 0; q < R; q++) opops[dst * R + q] = p[q];
+                    okii[dst] = kii;
+                    ap0 += p[0] < 0 ? -p[0] : p[0];
+                    ap1 += p[1] < 0 ? -p[1] : p[1];
+                }
+            }
+            run += ktot;
         }
-        for (int q = 0; q < R; q++) opops[dst * R + q] = p[q];
-        ap0 += p[0] < 0 ? -p[0] : p[0];
-        ap1 += p[1] < 0 ? -p[1] : p[1];
     }
     int64_t r0 = block_reduce_sum<int64_t>(ap0);
     int64_t r1 = block_reduce_sum<int64_t>(ap1);
@@ -931,7 +952,8 @@ __global__ void __launch_bounds__(kBlock) k_eval_excitations(const DevSys *gsys,
         } else {
             MolDet<W> d;
             mol_decode<W>(s, f, d);
-            attempt_mol<W, Real>(s, rs, d, ppops[i], at);
+            if (KIND == kKindHeatBath || KIND == kKindHeatBathUniform) attempt_heat_bath<W, Real>(s, rs, d, ppops[i], at);
+            else attempt_mol<W, Real>(s, rs, d, ppops[i], at);
         }
         orbs[4 * i + 0] = at.from[0];
         orbs[4 * i + 1] = at.nexcit == 2 ? at.from[1] : -1;
@@ -1005,30 +1027,35 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
     DevState *S = b.state;
     int initiator_flagged = b.sflag != nullptr;
     k_clamp_spawns<<<1, 1, 0, st>>>(S, b.scap);
-    // radix sort: pass 0 reads the spawned list directly
-    const uint64_t *kin = b.sdets;
+    // radix sort (hgpu_sort.cuh): pass 0 reads the ranks, or the spawned list itself
+    const int nel = b.sort_nel, nbasis = b.sort_nbasis;
+    const size_t hist_smem = sizeof(uint32_t) * kMaxPasses * kRadix +
+                             (b.use_rank ? sizeof(uint64_t) * (size_t)(nel + 1) * nbasis : 0);
+    if (b.use_rank) k_sort_hist<W, 1, true><<<b.grid, kBlock, hist_smem, st>>>(b, nel, nbasis);
+    else k_sort_hist<W, W, false><<<b.grid, kBlock, hist_smem, st>>>(b, nel, nbasis);
+    k_sort_offsets<<<1, kRadix, 0, st>>>(b);
+    const uint64_t *kin = b.use_rank ? b.skeys : b.sdets;
     const uint32_t *iin = nullptr;
     int o = 0;
     for (int p = 0; p < b.sort_passes; p++) {
-        int shift = p * kRadixBits;
-        k_radix_up<W><<<b.grid, kRadix, 0, st>>>(kin, &S->n_spawn, shift, b.hist);
-        device_scan<int64_t>(b, LoadHist{b.hist}, StoreHist{b.hist}, &S->n_hist, b.scan_part, (int64_t *)nullptr,
-                             st);
-        k_radix_down<W><<<b.grid, kRadix, 0, st>>>(kin, iin, b.keys[o], b.idx[o], &S->n_spawn, shift, b.hist);
+        if (b.key_words == 1)
+            k_onesweep<1><<<b.sort_grid, kOSThreads, OSConf<1>::smem, st>>>(b, p, kin, iin, b.keys[o], b.idx[o]);
+        else
+            k_onesweep<2><<<b.sort_grid, kOSThreads, OSConf<2>::smem, st>>>(b, p, kin, iin, b.keys[o], b.idx[o]);
         kin = b.keys[o];
         iin = b.idx[o];
         o ^= 1;
     }
     if (pm) cudaEventRecord(pm->ev[4], st);
-    k_seg_reduce<W><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
+    if (b.key_words == 1) k_seg_reduce<1><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
+    else k_seg_reduce<2><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
     device_scan<int64_t>(b, LoadKeep{b.segkeep}, StoreExclusive{b.segpos}, &S->n_spawn, b.scan_part, &S->n_uniq, st);
-    k_seg_compact<W><<<b.grid, kBlock, 0, st>>>(b, R, kin);
+    if (b.use_rank) k_seg_compact<W, true><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin);
+    else k_seg_compact<W, false><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin);
     if (pm) cudaEventRecord(pm->ev[5], st);
     k_merge_splits<W><<<b.grid, kBlock, 0, st>>>(b, cur);
-    k_merge_tiles<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
-    k_set_count<<<1, 1, 0, st>>>(&S->n_merged, &S->n_main, 1, &S->n_uniq);
-    device_scan<uint2>(b, LoadMKeep{b.mkeep}, StoreMPos{b.mpos}, &S->n_merged, reinterpret_cast<uint2 *>(b.scan_part),
-                       reinterpret_cast<uint2 *>(&S->n_merged_keep), st);
+    k_merge_tiles<W><<<b.grid, kBlock, b.fx_smem_bytes, st>>>(b, R, cur);
+    k_merge_tile_scan<<<1, 1024, 0, st>>>(b);
     k_merge_scatter<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
     if (pm) cudaEventRecord(pm->ev[6], st);
 }
@@ -1046,12 +1073,19 @@ static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur
     k_set_count<<<1, 1, 0, st>>>(&S->n_slots, &S->n_main, R, nullptr);
     device_scan<int64_t>(b, LoadNatt{b.natt}, StoreInclusive{b.aoff}, &S->n_slots, b.scan_part, &S->n_attempts, st);
     if (pm) cudaEventRecord(pm->ev[2], st);
-    if (kind == HGPU_SYS_HUB_K)
-        k_spawn<W, HGPU_SYS_HUB_K, double><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
-    else if (precision == HGPU_PREC_MIXED)
-        k_spawn<W, HGPU_SYS_READ_IN, float><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
-    else
-        k_spawn<W, HGPU_SYS_READ_IN, double><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+#define HGPU_SPAWN(KK)                                                                      \
+    do {                                                                                    \
+        if (precision == HGPU_PREC_MIXED)                                                   \
+            k_spawn<W, KK, float><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);             \
+        else                                                                                \
+            k_spawn<W, KK, double><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);            \
+    } while (0)
+    if (kind == HGPU_SYS_HUB_K) k_spawn<W, HGPU_SYS_HUB_K, double><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+    else if (kind == kKindHeatBath) HGPU_SPAWN(kKindHeatBath);
+    else if (kind == kKindHeatBathUniform) HGPU_SPAWN(kKindHeatBathUniform);
+    else if (kind == kKindReadInNoRenorm) HGPU_SPAWN(kKindReadInNoRenorm);
+    else HGPU_SPAWN(HGPU_SYS_READ_IN);
+#undef HGPU_SPAWN
     if (pm) cudaEventRecord(pm->ev[3], st);
     annihilation_w<W>(b, R, cur, st, pm);
     k_cycle_end<<<1, 1024, 0, st>>>(b, R, b.grid, 1);
@@ -1064,10 +1098,34 @@ void launch_cycle(const DevBuffers &b, int W, int R, int kind, int precision, in
     else cycle_w<2>(b, R, kind, precision, cur, st, pm);
 }
 
+int set_kernel_attributes(const DevBuffers &b) {
+    // hub_k momentum tables (hub_smem) next to the spawning queues, for up to 255 k-points
+    const int hub_max = (int)hub_smem(HGPU_SYS_HUB_K, 255);
+    if (cudaFuncSetAttribute(k_spawn<1, HGPU_SYS_HUB_K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             hub_max) != cudaSuccess ||
+        cudaFuncSetAttribute(k_spawn<2, HGPU_SYS_HUB_K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             hub_max) != cudaSuccess)
+        return 1;
+    if (cudaFuncSetAttribute(k_onesweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OSConf<1>::smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_onesweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OSConf<2>::smem) !=
+            cudaSuccess)
+        return 1;
+    // The largest table any supported system needs (64 spatial orbitals), so
+    // that handles of different systems in one process never lower the limit
+    // another handle's captured graph relies on.
+    const int max_bytes = (int)sizeof(int64_t) * fx_table_words(HGPU_SYS_READ_IN, 128, 64);
+    if (b.fx_smem_bytes > (size_t)max_bytes) return 1;
+    cudaError_t e1 = cudaFuncSetAttribute(k_merge_tiles<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_bytes);
+    cudaError_t e2 = cudaFuncSetAttribute(k_merge_tiles<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_bytes);
+    return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : 1;
+}
+
 int launches_per_cycle(const DevBuffers &b) {
-    // begin, prep, count, scan(3), spawn, clamp, sort(5/pass), seg_reduce,
-    // scan(3), compact, merge_splits, merge_tiles, count, scan(3), scatter, end
-    return 2 + 1 + 3 + 1 + 1 + 5 * b.sort_passes + 1 + 3 + 1 + 2 + 1 + 3 + 1 + 1;
+    // begin, prep, count, scan(3), spawn, clamp, sort_hist, sort_offsets,
+    // one per pass, seg_reduce, scan(3), compact, merge_splits, merge_tiles,
+    // tile_scan, scatter, end
+    return 2 + 1 + 3 + 1 + 1 + 2 + b.sort_passes + 1 + 3 + 1 + 2 + 1 + 1 + 1;
 }
 
 void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st) {
@@ -1090,10 +1148,16 @@ void launch_eval_excitations(const DevBuffers &b, int W, int kind, int precision
                                                              orbs, pgen, hmatel, allowed, nspawn)
     if (W == 1) {
         if (kind == HGPU_SYS_HUB_K) HGPU_EVAL(1, HGPU_SYS_HUB_K, double);
+        else if ((kind == kKindHeatBath || kind == kKindHeatBathUniform) && precision == HGPU_PREC_MIXED)
+            HGPU_EVAL(1, kKindHeatBath, float);
+        else if (kind == kKindHeatBath || kind == kKindHeatBathUniform) HGPU_EVAL(1, kKindHeatBath, double);
         else if (precision == HGPU_PREC_MIXED) HGPU_EVAL(1, HGPU_SYS_READ_IN, float);
         else HGPU_EVAL(1, HGPU_SYS_READ_IN, double);
     } else {
         if (kind == HGPU_SYS_HUB_K) HGPU_EVAL(2, HGPU_SYS_HUB_K, double);
+        else if ((kind == kKindHeatBath || kind == kKindHeatBathUniform) && precision == HGPU_PREC_MIXED)
+            HGPU_EVAL(2, kKindHeatBath, float);
+        else if (kind == kKindHeatBath || kind == kKindHeatBathUniform) HGPU_EVAL(2, kKindHeatBath, double);
         else if (precision == HGPU_PREC_MIXED) HGPU_EVAL(2, HGPU_SYS_READ_IN, float);
         else HGPU_EVAL(2, HGPU_SYS_READ_IN, double);
     }

@@ -10,6 +10,22 @@
 namespace hgpu {
 
 constexpr int kBlock = 256;      // threads per block of the streaming kernels
+// Generator kind of the spawning kernels (a template parameter, so that each
+// kernel holds the code of one generator): HGPU_SYS_HUB_K, HGPU_SYS_READ_IN
+// (molecular, uniform renorm generator) or one of the kinds below.
+constexpr int kKindHeatBath = 3;         // molecular, heat_bath
+constexpr int kKindReadInNoRenorm = 4;   // molecular, uniform no_renorm generator
+constexpr int kKindHeatBathUniform = 5;  // molecular, heat_bath_uniform
+// Radix sort of the spawned list (hgpu_sort.cuh): 8-bit digits, at most
+// kMaxPasses passes, tiles of kOSThreads x items keys of KW words each.
+constexpr int kOSThreads = 256;  // one thread per digit value in the look-back
+constexpr int kMaxPasses = 16;
+template <int KW>
+struct OSConf {
+    static constexpr int items = KW == 1 ? 16 : 8;  // keys per thread
+    static constexpr int tile = kOSThreads * items;
+    static constexpr size_t smem = (size_t)tile * (8 * KW + 4);  // staged keys + indices
+};
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortItems = 8;    // keys per thread per radix tile
@@ -26,8 +42,6 @@ struct DevState {
     int64_t n_attempts;    // A: spawning attempts this cycle
     int64_t n_merged_keep; // uint2 (kept main, kept total) after the merge
     int64_t n_slots;       // N * nspaces
-    int64_t n_merged;      // N + U
-    int64_t n_hist;        // kRadix * grid (length of the radix histogram)
     int64_t iter;          // current iteration (cycle number, 1-based)
     double shift[HGPU_MAX_SPACES];
     int64_t abs_pop[HGPU_MAX_SPACES];  // exact sum |pop| of the main list (encoded units)
@@ -41,6 +55,8 @@ struct DevState {
     int64_t acc_attempts, acc_spawned, last_nspawn_events;
     int32_t rep_cycles;
     int32_t pad2;
+    uint64_t spawn_next;  // next unclaimed attempt chunk of the spawning kernel
+    uint32_t os_ticket[16];  // next tile of each radix pass (hgpu_sort.cuh)
 };
 
 // Device buffers of one engine (all allocated once, at create).
@@ -59,10 +75,22 @@ struct DevBuffers {
     int64_t *spops;
     uint64_t *sflag;    // initiator bits | generation order << 2
     int64_t scap;
-    // sort buffers
-    uint64_t *keys[2];
+    // sort (hgpu_sort.cuh)
+    uint64_t *skeys;    // colexicographic ranks of the spawned determinants (when use_rank)
+    uint64_t *keys[2];  // key_words per entry
     uint32_t *idx[2];
-    uint32_t *hist;     // kRadix * grid
+    uint32_t *ghist;    // [kMaxPasses][kRadix] digit counts
+    uint32_t *gofs;     // [kMaxPasses][kRadix] global digit offsets
+    uint64_t *lookback; // [tiles][kRadix] look-back status words
+    uint32_t *os_epoch;  // look-back epoch of the current sort (kept out of DevState,
+                         // which the host rewrites, so that an epoch is never reused)
+    const uint64_t *binom;  // [nel+1][nbasis]: C(p, k) at k*nbasis + p
+    int use_rank;       // keys are ranks (one word); else the determinant words
+    int key_words;
+    int sort_nel, sort_nbasis;  // shape of the binomial table
+    int sort_few_from;          // first pass whose digits take at most 32 values
+    int sort_few_values[16];    // number of digit values of each such pass
+    int sort_grid;      // blocks of the radix passes
     // self-annihilated list (size scap)
     int64_t *segpops;   // per sorted position (R)
     uint64_t *segflag;
@@ -76,7 +104,8 @@ struct DevBuffers {
     int64_t *msplit;    // merge-path split (main index) at every tile boundary
     int64_t *mref;      // per merged rank: >= 0 main index, < 0 -(j+1) unique spawn
     uint2 *mkeep;       // per merged rank: (kept main, kept any)
-    uint2 *mpos;        // exclusive scan of mkeep
+    uint2 *tile_cnt;    // per merge tile: (kept main, kept any)
+    uint2 *tile_base;   // exclusive scan of tile_cnt: output offset of each tile
     // scan scratch and per-block partials
     int64_t *scan_part;     // kMaxBlocks * 2
     double *part_d;         // kMaxBlocks * 4 (proj, d0 per space)
@@ -86,6 +115,7 @@ struct DevBuffers {
     int grid;               // blocks of the streaming kernels
     int spawn_grid;         // blocks of the spawning kernel
     int sort_passes;
+    size_t fx_smem_bytes;  // dynamic shared memory of the merge tiles (exact-diagonal tables)
     int nk;                 // hub_k: number of k-points (shared-memory tables)
 };
 
@@ -102,6 +132,8 @@ struct PhaseMarks {
 void launch_cycle(const DevBuffers &b, int W, int R, int kind, int precision, int cur, cudaStream_t st,
                   const PhaseMarks *pm = nullptr);
 int launches_per_cycle(const DevBuffers &b);
+// Kernel attributes that depend on the system (dynamic shared memory); 0 on success.
+int set_kernel_attributes(const DevBuffers &b);
 void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st);
 void launch_eval_excitations(const DevBuffers &b, int W, int kind, int precision, const uint64_t *parents,
                              const int64_t *parent_pops, int64_t n, int64_t iteration, int32_t *orbs, double *pgen,

@@ -1,0 +1,274 @@
+// hgpu_sort.cuh -- stable LSD radix sort of the spawned list.
+//
+// HANDE sorts the spawned list by determinant (qsort, src/sort.f90:213-395,
+// called from annihilate_wrapper_spawn_t_single, src/spawn_data.F90:359-421)
+// before summing repeated determinants.  Here the sort key of a determinant is
+// its colexicographic rank, sum_k C(p_k, k) over its occupied orbitals p_1 <
+// ... < p_nel (the combinatorial number system): a bijection onto
+// [0, C(nbasis, nel)) that orders determinants exactly as HANDE's comparison
+// does (unsigned, last word most significant), in ceil(log2 C(nbasis, nel))
+// bits instead of nbasis -- 34 instead of 52 bits for 52 spin orbitals and 10
+// electrons.  Systems whose rank does not fit 64 bits sort the raw words.
+//
+// One pass per 8-bit digit.  Digit histograms of all passes are counted in one
+// read of the list (k_sort_hist); each pass (k_onesweep) then ranks a tile of
+// keys in shared memory and finds the tile's global offsets by decoupled
+// look-back over the preceding tiles (Merrill and Garland, "Single-pass
+// parallel prefix scan with decoupled look-back", 2016; Adinets and Merrill,
+// "Onesweep", 2022), so a pass reads and writes each key once.  Tiles are taken
+// in ticket order, so a tile only ever waits on tiles that running blocks
+// hold; every wait is bounded and a timeout raises HGPU_FLAG_TIMEOUT.
+#pragma once
+
+namespace hgpu {
+
+constexpr int kSpinLimit = 1 << 22;  // polls of one look-back wait before it gives up
+constexpr int kOSLook = 8;           // predecessor tiles read per look-back round trip
+
+// look-back status word: [63:62] flag, [61:32] epoch of the pass, [31:0] count
+constexpr uint64_t kOSAggregate = 1, kOSPrefix = 2;
+__device__ __forceinline__ uint64_t os_word(uint64_t flag, uint32_t epoch, uint32_t count) {
+    return (flag << 62) | ((uint64_t)(epoch & 0x3FFFFFFFu) << 32) | count;
+}
+
+// Epoch of pass p of the current sort: never 0, so zeroed memory is never valid.
+__device__ __forceinline__ uint32_t os_epoch(uint32_t base, int pass) {
+    return (uint32_t)((base + (uint32_t)pass) % 0x3FFFFFFFu) + 1u;
+}
+
+template <int KW>
+__device__ __forceinline__ uint32_t os_digit(const uint64_t *k, int shift) {
+    return (uint32_t)((k[shift >> 6] >> (shift & 63)) & (kRadix - 1));
+}
+
+// Lanes of `mask` whose 8-bit digit equals this lane's: one ballot per digit
+// bit (cheaper on this GPU than match.any).
+__device__ __forceinline__ uint32_t warp_peers8(uint32_t mask, uint32_t d) {
+    uint32_t peers = mask;
+#pragma unroll
+    for (int bit = 0; bit < kRadixBits; bit++) {
+        uint32_t bb = __ballot_sync(mask, (d >> bit) & 1u);
+        peers &= ((d >> bit) & 1u) ? bb : ~bb;
+    }
+    return peers;
+}
+
+// Colexicographic rank of a determinant; binom[k * nbasis + p] = C(p, k).
+template <int W>
+__device__ __forceinline__ uint64_t det_rank(const Det<W> &f, const uint64_t *binom, int nbasis) {
+    uint64_t r = 0;
+    int k = 0;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        uint64_t x = f.w[w];
+        while (x) {
+            int p = 64 * w + __ffsll((long long)x) - 1;
+            x &= x - 1;
+            k++;
+            r += binom[k * nbasis + p];
+        }
+    }
+    return r;
+}
+
+// Sort keys of the spawned list (ranks into b.skeys, when ranks are used) and
+// the digit histograms of every pass, added into b.ghist[pass][digit].
+template <int W, int KW, bool RANK>
+__global__ void __launch_bounds__(kBlock) k_sort_hist(DevBuffers b, int nel, int nbasis) {
+    extern __shared__ uint64_t hist_smem[];
+    uint32_t *h = reinterpret_cast<uint32_t *>(hist_smem);  // [passes][kRadix]
+    uint64_t *binom = hist_smem + (kMaxPasses * kRadix) / 2;
+    const int passes = b.sort_passes;
+    for (int k = threadIdx.x; k < passes * kRadix; k += blockDim.x) h[k] = 0;
+    if (RANK)
+        for (int k = threadIdx.x; k < (nel + 1) * nbasis; k += blockDim.x) binom[k] = b.binom[k];
+    __syncthreads();
+    const int64_t n = b.state->n_spawn;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        Det<W> f = load_det<W>(b.sdets, i);
+        uint64_t key[KW];
+        if (RANK) {
+            key[0] = det_rank<W>(f, binom, nbasis);
+            b.skeys[i] = key[0];
+        } else {
+#pragma unroll
+            for (int w = 0; w < KW; w++) key[w] = f.w[w];
+        }
+        // Digits of the top passes take few values (ranks are far below 2^64):
+        // those are counted with one ballot per value, the others with plain
+        // shared-memory atomics (spread over 256 counters)
+        const uint32_t active = __activemask();
+        const int lane = threadIdx.x & 31;
+        for (int p = 0; p < passes; p++) {
+            uint32_t dd = os_digit<KW>(key, p * kRadixBits);
+            const int nv = p < b.sort_few_from ? kRadix : b.sort_few_values[p];
+            if (nv > 32) {
+                atomicAdd(&h[p * kRadix + dd], 1u);
+            } else {
+                for (int v = 0; v < nv; v++) {
+                    uint32_t c = __popc(__ballot_sync(active, dd == (uint32_t)v));
+                    if (lane == __ffs(active) - 1 && c) atomicAdd(&h[p * kRadix + v], c);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < passes * kRadix; k += blockDim.x)
+        if (h[k]) atomicAdd(&b.ghist[k], h[k]);
+}
+
+// Global digit offsets of every pass; clears the histograms for the next sort,
+// the tile tickets and advances the look-back epoch.
+__global__ void __launch_bounds__(kRadix) k_sort_offsets(DevBuffers b) {
+    const int passes = b.sort_passes;
+    for (int p = 0; p < passes; p++) {
+        uint32_t c = b.ghist[p * kRadix + threadIdx.x];
+        uint32_t tot;
+        uint32_t ex = block_exclusive_scan<uint32_t>(c, &tot);
+        b.gofs[p * kRadix + threadIdx.x] = ex;
+        b.ghist[p * kRadix + threadIdx.x] = 0;
+    }
+    if (threadIdx.x < kMaxPasses) b.state->os_ticket[threadIdx.x] = 0;
+    if (threadIdx.x == 0) *b.os_epoch += (uint32_t)kMaxPasses;
+}
+
+// One stable pass on digit `pass`: keys (KW words) and 32-bit indices (the
+// identity when idx_in is null).
+template <int KW>
+__global__ void __launch_bounds__(kOSThreads, 3) k_onesweep(DevBuffers b, int pass, const uint64_t *keys_in,
+                                                         const uint32_t *idx_in, uint64_t *keys_out,
+                                                         uint32_t *idx_out) {
+    constexpr int ITEMS = OSConf<KW>::items;
+    constexpr int TILE = OSConf<KW>::tile;
+    constexpr int NW = kOSThreads / 32;
+    extern __shared__ uint64_t os_smem[];
+    uint64_t *skey = os_smem;                                          // [TILE][KW]
+    uint32_t *sidx = reinterpret_cast<uint32_t *>(os_smem + TILE * KW);  // [TILE]
+    __shared__ uint32_t wcnt[NW][kRadix];
+    __shared__ uint32_t lstart[kRadix], gbase[kRadix];
+    __shared__ uint32_t s_tile;
+    DevState *st = b.state;
+    const int64_t n = st->n_spawn;
+    const int64_t ntiles = (n + TILE - 1) / TILE;
+    const uint32_t epoch = os_epoch(*b.os_epoch, pass);
+    const int shift = pass * kRadixBits;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int d = threadIdx.x;  // digit owned in the look-back
+    uint64_t *status = b.lookback;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&st->os_ticket[pass], 1u);
+#pragma unroll
+        for (int w = 0; w < NW; w++) wcnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        const int64_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const int64_t t0 = tile * TILE;
+        uint64_t kv[ITEMS][KW];
+        uint32_t iv[ITEMS], off[ITEMS], dg[ITEMS];
+        // stable ranking: element t0 + (warp*ITEMS + r)*32 + lane
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            int64_t e = t0 + (int64_t)(warp * ITEMS + r) * 32 + lane;
+            bool valid = e < n;
+            uint32_t mask = __ballot_sync(FULL_MASK, valid);
+            dg[r] = 0xFFFFFFFFu;
+            if (valid) {
+#pragma unroll
+                for (int w = 0; w < KW; w++) kv[r][w] = keys_in[e * KW + w];
+                iv[r] = idx_in ? idx_in[e] : (uint32_t)e;
+                uint32_t dd = os_digit<KW>(kv[r], shift);
+                dg[r] = dd;
+                uint32_t peers = warp_peers8(mask, dd);
+                int leader = __ffs(peers) - 1;
+                uint32_t old = 0;
+                if (lane == leader) {
+                    old = wcnt[warp][dd];
+                    wcnt[warp][dd] = old + __popc(peers);
+                }
+                old = __shfl_sync(mask, old, leader);
+                off[r] = old + __popc(peers & lanemask_lt());
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            uint32_t c = wcnt[w][d];
+            wcnt[w][d] = cnt;
+            cnt += c;
+        }
+        // publish this tile's count of digit d, then look back for its prefix
+        volatile uint64_t *my = status + tile * kRadix + d;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            *my = os_word(kOSPrefix, epoch, cnt);
+        } else {
+            *my = os_word(kOSAggregate, epoch, cnt);
+            // walk back kOSLook tiles per round trip: the loads of a round are
+            // independent, so a long run of tiles that have only published their
+            // aggregates costs one memory latency per kOSLook tiles
+            int64_t k = tile - 1;
+            int spins = 0;
+            bool done = false;
+            while (!done) {
+                uint64_t v[kOSLook];
+#pragma unroll
+                for (int u = 0; u < kOSLook; u++)
+                    v[u] = k - u >= 0 ? *(volatile uint64_t *)(status + (k - u) * kRadix + d) : 0;
+                int u = 0;
+                for (; u < kOSLook && k - u >= 0; u++) {
+                    uint32_t ve = (uint32_t)(v[u] >> 32) & 0x3FFFFFFFu;
+                    uint64_t fl = v[u] >> 62;
+                    if (ve != (epoch & 0x3FFFFFFFu) || fl == 0) break;  // not published yet
+                    excl += (uint32_t)v[u];
+                    if (fl == kOSPrefix) {
+                        done = true;
+                        break;
+                    }
+                }
+                if (done) break;
+                k -= u;  // resume at the first tile that was not ready
+                if (u == 0) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(&st->error_flags, HGPU_FLAG_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            *my = os_word(kOSPrefix, epoch, excl + cnt);
+        }
+        gbase[d] = b.gofs[pass * kRadix + d] + excl;
+        uint32_t ltot;
+        lstart[d] = block_exclusive_scan<uint32_t>(cnt, &ltot);
+        __syncthreads();
+        // stage in digit order, then write each digit's run contiguously
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (dg[r] != 0xFFFFFFFFu) {
+                uint32_t lp = lstart[dg[r]] + wcnt[warp][dg[r]] + off[r];
+#pragma unroll
+                for (int w = 0; w < KW; w++) skey[lp * KW + w] = kv[r][w];
+                sidx[lp] = iv[r];
+            }
+        }
+        __syncthreads();
+        const int tn = (int)min((int64_t)TILE, n - t0);
+        for (int j = threadIdx.x; j < tn; j += kOSThreads) {
+            uint64_t k[KW];
+#pragma unroll
+            for (int w = 0; w < KW; w++) k[w] = skey[j * KW + w];
+            uint32_t dd = os_digit<KW>(k, shift);
+            int64_t pos = (int64_t)gbase[dd] + (j - (int64_t)lstart[dd]);
+            if (pos < n) {
+#pragma unroll
+                for (int w = 0; w < KW; w++) keys_out[pos * KW + w] = k[w];
+                idx_out[pos] = sidx[j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace hgpu

@@ -23,6 +23,7 @@ EXPORTS = [
     "hgpu_end_report", "hgpu_run_report", "hgpu_get_state", "hgpu_set_state", "hgpu_checkpoint",
     "hgpu_restore", "hgpu_eval_excitations", "hgpu_annihilate_fixed", "hgpu_eval_diagonal",
     "hgpu_profile_cycle", "hgpu_snapshot", "hgpu_self_annihilate_noalloc",
+    "hgpu_batch_create", "hgpu_batch_run_cycles", "hgpu_batch_destroy",
 ]
 
 
@@ -199,3 +200,45 @@ class Engine:
         self._check(self.L.hgpu_eval_diagonal(self.h, _p(d, C.c_int64), n, _p(out, C.c_double)),
                     "hgpu_eval_diagonal")
         return out
+
+
+class Batch:
+    """Independent calculations (Engines) advanced together: one CUDA graph launch
+    per cycle for all of them (hgpu_batch_*).  The engines stay usable on their
+    own between batch calls (reports, downloads, snapshots)."""
+
+    def __init__(self, engines):
+        self.L = load_library()
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(self.engines))(*[e.h.value for e in self.engines])
+        b = C.c_void_p()
+        rc = self.L.hgpu_batch_create(arr, len(self.engines), C.byref(b))
+        if rc != 0:
+            raise HgpuError(rc, "hgpu_batch_create", self.L.hgpu_error_string(rc).decode())
+        self.b = b
+
+    def run_cycles(self, n):
+        rc = self.L.hgpu_batch_run_cycles(self.b, n)
+        if rc not in (0, 3, 4):
+            raise HgpuError(rc, "hgpu_batch_run_cycles", self.L.hgpu_error_string(rc).decode())
+        return rc
+
+    def run_report(self):
+        """ncycles of every engine (each engine's own ncycles must agree), then
+        each engine's report."""
+        nc = {e.cfg.ncycles for e in self.engines}
+        if len(nc) != 1:
+            raise ValueError("engines of a batch report must share ncycles")
+        self.run_cycles(nc.pop())
+        return [e.end_report() for e in self.engines]
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.L.hgpu_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

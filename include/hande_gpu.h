@@ -54,6 +54,7 @@ enum {
 /* Error flags reported per report (bit mask). */
 #define HGPU_FLAG_SPAWN_OVERFLOW 1
 #define HGPU_FLAG_MAIN_OVERFLOW 2
+#define HGPU_FLAG_TIMEOUT 4   /* a bounded device wait gave up (results of that cycle invalid) */
 
 /* System kinds (sys%system in src/system.f90). */
 enum { HGPU_SYS_HUB_K = 1, HGPU_SYS_READ_IN = 2 };
@@ -278,6 +279,25 @@ int32_t hgpu_self_annihilate_noalloc(const int64_t *d_sdata, int64_t n, int32_t 
  * cycle.  counts[0..6] (may be NULL): N before, attempts, spawned, unique
  * spawned, N after, kernel launches per cycle, radix passes. */
 int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int64_t *counts);
+
+/* Batches: many independent calculations advanced together.  HANDE runs one
+ * calculation per process; a batch groups already-created handles (different
+ * systems, sizes, seeds, replicas) on one device and advances all of them by
+ * a cycle with a single CUDA graph launch, each handle's cycle a branch of the
+ * graph, so small calculations fill the GPU together.  The handles stay owned
+ * by the caller and must outlive the batch; hgpu_end_report and every other
+ * per-handle call remain valid between batch calls.
+ *
+ * hgpu_batch_create: n >= 1 distinct handles on the current device.
+ * hgpu_batch_run_cycles: ncycles cycles of every handle (as hgpu_run_cycles
+ *   on each); handles must all be at the same buffer parity, which they are
+ *   when they have run the same number of cycles since their list was set.
+ *   Returns the first non-OK status of any handle (overflow flags), else OK.
+ * hgpu_batch_destroy: frees the batch's graphs, not the handles. */
+typedef struct hgpu_batch hgpu_batch;
+int32_t hgpu_batch_create(hgpu_handle *const *handles, int32_t n, hgpu_batch **out);
+int32_t hgpu_batch_run_cycles(hgpu_batch *b, int32_t ncycles);
+int32_t hgpu_batch_destroy(hgpu_batch *b);
 
 #ifdef __cplusplus
 }

@@ -146,6 +146,14 @@ struct oracle_ctx {
     int64_t sn, scap;
     uint64_t *sdets;
     int64_t *spops, *sflag, *sord, *suid;
+    /* heat-bath tables (excit_gen_heat_bath_t, src/excit_gens.f90:143-153), 0-based
+     * and first Fortran index fastest: ij_w[i*nb + j] = ij_weights(j,i),
+     * ija_w[(i*nb + j)*nb + a] = hb_ija%weights(a,j,i), ija_tot[i*nb + j] =
+     * hb_ija%weights_tot(j,i), ijab_*[((i*nb + j)*nb + a)*nb + b] and
+     * ijab_tot[(i*nb + j)*nb + a] likewise. */
+    int hb_on;
+    double *hb_i_w, *hb_ij_w, *hb_ija_w, *hb_ija_tot, *hb_ija_U, *hb_ijab_w, *hb_ijab_tot, *hb_ijab_U;
+    int32_t *hb_ija_K, *hb_ijab_K;
 };
 
 /* determinant helpers ------------------------------------------------------ */
@@ -728,15 +736,336 @@ static void attempt_hub_k(const oracle_ctx *c, rstream *rs, const uint64_t *f, c
     out->nspawn = nspawn;
 }
 
+/* ------------------------------------------------------------------------- */
+/* Heat-bath generators (src/excit_gen_heat_bath_mol.F90)                     */
+/* ------------------------------------------------------------------------- */
+
+#define HB_IJ(c, i, j) ((c)->hb_ij_w[(size_t)(i) * (c)->nbasis + (j)])
+#define HB_IJA(c, i, j, a) ((c)->hb_ija_w[((size_t)(i) * (c)->nbasis + (j)) * (c)->nbasis + (a)])
+#define HB_IJA_TOT(c, i, j) ((c)->hb_ija_tot[(size_t)(i) * (c)->nbasis + (j)])
+#define HB_IJAB(c, i, j, a, b) \
+    ((c)->hb_ijab_w[(((size_t)(i) * (c)->nbasis + (j)) * (c)->nbasis + (a)) * (c)->nbasis + (b)])
+#define HB_IJAB_TOT(c, i, j, a) ((c)->hb_ijab_tot[((size_t)(i) * (c)->nbasis + (j)) * (c)->nbasis + (a)])
+
+/* generate_alias_tables (lib/local/alias.f90:100-184), 0-based: the last
+ * overfull entry is paired with the last underfull one until either list is
+ * empty. */
+static void alias_build(int n, const double *w, double tot, double *U, int32_t *K) {
+    int under[MAXB], over[MAXB], nu = 0, no = 0;
+    double f = (double)n / tot;
+    for (int i = 0; i < n; i++) {
+        U[i] = w[i] * f;
+        if (U[i] <= 1.0) under[nu++] = i;
+        else over[no++] = i;
+        K[i] = i;
+    }
+    while (no > 0 && nu > 0) {
+        int ov = over[no - 1], un = under[nu - 1];
+        K[un] = ov;
+        nu--;
+        U[ov] = U[ov] - (1.0 - U[un]);
+        if (U[ov] < 1.0) {
+            under[nu++] = over[no - 1];
+            no--;
+        }
+    }
+}
+
+/* select_weighted_value_precalc (lib/local/alias.f90:13-60). */
+static int alias_draw(rstream *rs, int n, const double *U, const int32_t *K) {
+    double x = rs_next(rs) * (double)n;
+    int k = (int)floor(x);
+    x = x - (double)k;
+    return x < U[k] ? k : K[k];
+}
+
+/* select_weighted_value (lib/local/alias.f90:62-98): alias table built on the fly. */
+static int alias_select(rstream *rs, int n, const double *w, double tot) {
+    double U[MAXEL];
+    int32_t K[MAXEL];
+    alias_build(n, w, tot, U, K);
+    return alias_draw(rs, n, U, K);
+}
+
+/* init_excit_mol_heat_bath (src/excit_gen_heat_bath_mol.F90:14-243), serial
+ * loop order.  Alias tables that the reference leaves unset (zero total weight)
+ * are U = 0, K = self here.  Returns -1 where the reference stops with "Not all
+ * possible single excitations can be accounted for" (original = 1 only). */
+static int init_heat_bath(oracle_ctx *c, int original) {
+    int nb = c->nbasis;
+    size_t n2 = (size_t)nb * nb, n3 = n2 * nb, n4 = n3 * nb;
+    c->hb_i_w = (double *)calloc(nb, sizeof(double));
+    c->hb_ij_w = (double *)calloc(n2, sizeof(double));
+    c->hb_ija_w = (double *)calloc(n3, sizeof(double));
+    c->hb_ija_tot = (double *)calloc(n2, sizeof(double));
+    c->hb_ija_U = (double *)calloc(n3, sizeof(double));
+    c->hb_ija_K = (int32_t *)calloc(n3, sizeof(int32_t));
+    c->hb_ijab_w = (double *)calloc(n4, sizeof(double));
+    c->hb_ijab_tot = (double *)calloc(n3, sizeof(double));
+    c->hb_ijab_U = (double *)calloc(n4, sizeof(double));
+    c->hb_ijab_K = (int32_t *)calloc(n4, sizeof(int32_t));
+    int *j_nonzero = (int *)calloc(n2, sizeof(int)); /* [i*nb + a] */
+    if (!c->hb_ijab_U || !c->hb_ijab_K || !c->hb_ijab_w || !j_nonzero) return -2;
+    c->hb_on = 1;
+    int bias = 0;
+    for (int i = 0; i < nb; i++) {
+        double i_weight = 0.0;
+        for (int j = 0; j < nb; j++) {
+            double ij_weight = 0.0;
+            HB_IJA_TOT(c, i, j) = 0.0;
+            if (i != j) {
+                int it = j < i ? j : i, jt = j < i ? i : j;
+                int ij_sym = cross(c, c->orb_sym[it], c->orb_sym[jt]);
+                double ija_weights_tot = 0.0, i_weight_extra = 0.0;
+                for (int a = 0; a < nb; a++) {
+                    double ija_weight = 0.0;
+                    HB_IJAB_TOT(c, i, j, a) = 0.0;
+                    if (a != i && a != j) {
+                        int isymb = cross(c, ij_sym, c->orb_sym[a]);
+                        for (int b = 0; b < nb; b++) {
+                            double ijab_weight = 0.0;
+                            if (((c->orb_ms[it] == c->orb_ms[a] && c->orb_ms[jt] == c->orb_ms[b]) ||
+                                 (c->orb_ms[it] == c->orb_ms[b] && c->orb_ms[jt] == c->orb_ms[a])) &&
+                                c->orb_sym[b] == isymb && b != a && b != i && b != j) {
+                                int at = b < a ? b : a, bt = b < a ? a : b;
+                                double h = fabs(sc2_mol_excit(c, it, jt, at, bt, 0));
+                                i_weight_extra = i_weight_extra + h;
+                                ij_weight = ij_weight + h;
+                                ija_weight = ija_weight + h;
+                                ijab_weight = ijab_weight + h;
+                            }
+                            HB_IJAB(c, i, j, a, b) = ijab_weight;
+                            HB_IJAB_TOT(c, i, j, a) = HB_IJAB_TOT(c, i, j, a) + ijab_weight;
+                        }
+                    }
+                    HB_IJA(c, i, j, a) = ija_weight;
+                    ija_weights_tot = ija_weights_tot + ija_weight;
+                    if (ija_weight > DEPSILON) j_nonzero[(size_t)i * nb + a]++;
+                }
+                i_weight = i_weight + i_weight_extra;
+                HB_IJA_TOT(c, i, j) = HB_IJA_TOT(c, i, j) + ija_weights_tot;
+            }
+            HB_IJ(c, i, j) = ij_weight;
+        }
+        c->hb_i_w[i] = i_weight;
+        for (int a = 0; a < nb; a++) {
+            if (j_nonzero[(size_t)i * nb + a] < nb - c->nel && original && i != a) {
+                if (c->orb_sym[a] == c->orb_sym[i] && c->orb_ms[a] == c->orb_ms[i]) bias = 1;
+            }
+        }
+    }
+    free(j_nonzero);
+    for (size_t t = 0; t < n3; t++) c->hb_ija_K[t] = (int32_t)(t % nb);
+    for (size_t t = 0; t < n4; t++) c->hb_ijab_K[t] = (int32_t)(t % nb);
+    for (int i = 0; i < nb; i++) {
+        for (int j = 0; j < nb; j++) {
+            if (fabs(HB_IJA_TOT(c, i, j)) > 0.0) {
+                size_t o3 = ((size_t)i * nb + j) * nb;
+                alias_build(nb, c->hb_ija_w + o3, HB_IJA_TOT(c, i, j), c->hb_ija_U + o3, c->hb_ija_K + o3);
+                for (int a = 0; a < nb; a++) {
+                    if (fabs(HB_IJAB_TOT(c, i, j, a)) > 0.0) {
+                        size_t o4 = (o3 + a) * nb;
+                        alias_build(nb, c->hb_ijab_w + o4, HB_IJAB_TOT(c, i, j, a), c->hb_ijab_U + o4,
+                                    c->hb_ijab_K + o4);
+                    }
+                }
+            }
+        }
+    }
+    return bias ? -1 : 0;
+}
+
+/* The psingle of a single i -> a inside the heat-bath double branch
+ * (src/excit_gen_heat_bath_mol.F90:350-366, :396-409, ...): 0 when i -> a breaks
+ * spin or symmetry, else |h_ia| / (W + |h_ia|) below W = weights_tot(a,j,i), 0.5 above. */
+static double hb_psingle(const oracle_ctx *c, const det_info *d, int i, int a, double wtot, double *abs_h) {
+    if (c->orb_sym[a] != c->orb_sym[i] || c->orb_ms[a] != c->orb_ms[i]) return 0.0;
+    double h = fabs(sc1_mol_excit(c, d->occ, i, a, 0));
+    if (abs_h) *abs_h = h;
+    return h < wtot ? h / (wtot + h) : 0.5;
+}
+
+/* select_ij_heat_bath (src/excit_gen_utils.f90:9-66) after find_i_d_weights
+ * (:142-167). */
+typedef struct {
+    double wi[MAXEL], ijw[MAXEL], jiw[MAXEL];
+    double wi_tot, ij_tot, ji_tot;
+    int i_ind, j_ind, i, j;
+} hb_ij_t;
+
+static int select_ij_heat_bath(const oracle_ctx *c, rstream *rs, const det_info *d, hb_ij_t *s) {
+    int nel = c->nel;
+    s->wi_tot = 0.0;
+    for (int p = 0; p < nel; p++) {
+        s->wi[p] = c->hb_i_w[d->occ[p]];
+        s->wi_tot = s->wi_tot + s->wi[p];
+    }
+    s->i_ind = alias_select(rs, nel, s->wi, s->wi_tot);
+    s->i = d->occ[s->i_ind];
+    s->ij_tot = 0.0;
+    for (int p = 0; p < nel; p++) {
+        s->ijw[p] = HB_IJ(c, s->i, d->occ[p]);
+        s->ij_tot = s->ij_tot + s->ijw[p];
+    }
+    s->j_ind = -1;
+    s->j = -1;
+    if (!(s->ij_tot > 0.0)) return 0;
+    s->j_ind = alias_select(rs, nel, s->ijw, s->ij_tot);
+    s->j = d->occ[s->j_ind];
+    s->ji_tot = 0.0;
+    for (int p = 0; p < nel; p++) {
+        s->jiw[p] = HB_IJ(c, s->j, d->occ[p]);
+        s->ji_tot = s->ji_tot + s->jiw[p];
+    }
+    return 1;
+}
+
+/* gen_excit_mol_heat_bath (src/excit_gen_heat_bath_mol.F90:258-547). */
+static void gen_heat_bath(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, attempt_t *out,
+                          double *pgen_out, double *hmatel_out) {
+    hb_ij_t s;
+    out->e.nexcit = 2;
+    int allowed = select_ij_heat_bath(c, rs, d, &s);
+    int i = s.i, j = s.j;
+    out->e.from[0] = i;
+    out->e.from[1] = j;
+    if (!(allowed && fabs(HB_IJA_TOT(c, i, j)) > 0.0)) allowed = 0;
+    int a = -1, b = -1, dbl = 1;
+    double psingle = 0.0, hmod_ia = 0.0;
+    if (allowed) {
+        size_t o3 = ((size_t)i * c->nbasis + j) * c->nbasis;
+        a = alias_draw(rs, c->nbasis, c->hb_ija_U + o3, c->hb_ija_K + o3);
+        if (!tbit(f, a)) {
+            if (c->orb_sym[a] == c->orb_sym[i] && c->orb_ms[a] == c->orb_ms[i]) {
+                hmod_ia = fabs(sc1_mol_excit(c, d->occ, i, a, perm1(c, f, i, a)));
+                double x = rs_next(rs);
+                double wt = HB_IJAB_TOT(c, i, j, a);
+                psingle = hmod_ia < wt ? hmod_ia / (wt + hmod_ia) : 0.5;
+                dbl = !(x < psingle);
+            } else {
+                dbl = 1;
+                psingle = 0.0;
+            }
+        } else {
+            allowed = 0;
+        }
+    }
+    double pgen = 1.0, hmatel = 0.0;
+    if (allowed) {
+        if (dbl) {
+            size_t o4 = (((size_t)i * c->nbasis + j) * c->nbasis + a) * c->nbasis;
+            b = alias_draw(rs, c->nbasis, c->hb_ijab_U + o4, c->hb_ijab_K + o4);
+            if (!tbit(f, b)) {
+                double p_ij = (s.wi[s.i_ind] / s.wi_tot) * (s.ijw[s.j_ind] / s.ij_tot);
+                double p_ji = (s.wi[s.j_ind] / s.wi_tot) * (s.jiw[s.i_ind] / s.ji_tot);
+                double pgen_ija = p_ij * (HB_IJA(c, i, j, a) / HB_IJA_TOT(c, i, j)) * (1.0 - psingle) *
+                                  (HB_IJAB(c, i, j, a, b) / HB_IJAB_TOT(c, i, j, a));
+                psingle = hb_psingle(c, d, i, b, HB_IJAB_TOT(c, i, j, b), NULL);
+                double pgen_ijb = p_ij * (HB_IJA(c, i, j, b) / HB_IJA_TOT(c, i, j)) * (1.0 - psingle) *
+                                  (HB_IJAB(c, i, j, b, a) / HB_IJAB_TOT(c, i, j, b));
+                psingle = hb_psingle(c, d, j, a, HB_IJAB_TOT(c, j, i, a), NULL);
+                double pgen_jia = p_ji * (HB_IJA(c, j, i, a) / HB_IJA_TOT(c, j, i)) * (1.0 - psingle) *
+                                  (HB_IJAB(c, j, i, a, b) / HB_IJAB_TOT(c, j, i, a));
+                psingle = hb_psingle(c, d, j, b, HB_IJAB_TOT(c, j, i, b), NULL);
+                double pgen_jib = p_ji * (HB_IJA(c, j, i, b) / HB_IJA_TOT(c, j, i)) * (1.0 - psingle) *
+                                  (HB_IJAB(c, j, i, b, a) / HB_IJAB_TOT(c, j, i, b));
+                pgen = pgen_ija + pgen_ijb + pgen_jia + pgen_jib;
+                int f0 = i < j ? i : j, f1 = i < j ? j : i, t0 = a < b ? a : b, t1 = a < b ? b : a;
+                out->e.from[0] = f0;
+                out->e.from[1] = f1;
+                out->e.to[0] = t0;
+                out->e.to[1] = t1;
+                out->e.perm = perm2(c, f, f0, f1, t0, t1);
+                hmatel = sc2_mol_excit(c, f0, f1, t0, t1, out->e.perm);
+            } else {
+                allowed = 0;
+            }
+        } else {
+            out->e.nexcit = 1;
+            out->e.from[1] = -1;
+            out->e.to[0] = a;
+            out->e.perm = perm1(c, f, i, a);
+            hmatel = sc1_mol_excit(c, d->occ, i, a, out->e.perm);
+            pgen = 0.0;
+            for (int q = 0; q < c->nel; q++) {
+                int oq = d->occ[q];
+                /* a q that has no double excitation with i (weights_tot(q,i) = 0) adds
+                 * 0 * (0/0) in the reference, a NaN p_gen; its true contribution is 0 */
+                if (i != oq && a != oq && HB_IJA_TOT(c, i, oq) > 0.0) {
+                    double wt = HB_IJAB_TOT(c, i, oq, a);
+                    double psq = hmod_ia < wt ? hmod_ia / (wt + hmod_ia) : 0.5;
+                    pgen = pgen + psq * (s.ijw[q] / s.ij_tot) * (HB_IJA(c, i, oq, a) / HB_IJA_TOT(c, i, oq));
+                }
+            }
+            pgen = pgen * (s.wi[s.i_ind] / s.wi_tot);
+        }
+    }
+    out->allowed = allowed;
+    *pgen_out = allowed ? pgen : 1.0;
+    *hmatel_out = allowed ? hmatel : 0.0;
+}
+
+/* gen_excit_mol_heat_bath_uniform, double branch
+ * (src/excit_gen_heat_bath_mol.F90:619-705). */
+static void gen_heat_bath_uniform_double(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d,
+                                         attempt_t *out, double *pgen_out, double *hmatel_out) {
+    hb_ij_t s;
+    out->e.nexcit = 2;
+    int allowed = select_ij_heat_bath(c, rs, d, &s);
+    int i = s.i, j = s.j;
+    if (!(allowed && fabs(HB_IJA_TOT(c, i, j)) > 0.0)) allowed = 0;
+    double pgen = 1.0, hmatel = 0.0;
+    double pij = 0.0;
+    if (s.j_ind >= 0)
+        pij = ((s.wi[s.i_ind] / s.wi_tot) * (s.ijw[s.j_ind] / s.ij_tot)) +
+              ((s.wi[s.j_ind] / s.wi_tot) * (s.jiw[s.i_ind] / s.ji_tot));
+    if (j >= 0 && j < i) {
+        int t = j;
+        j = i;
+        i = t;
+    }
+    out->e.from[0] = i;
+    out->e.from[1] = j;
+    int a = -1, b = -1;
+    if (allowed) {
+        size_t o3 = ((size_t)i * c->nbasis + j) * c->nbasis;
+        a = alias_draw(rs, c->nbasis, c->hb_ija_U + o3, c->hb_ija_K + o3);
+        if (fabs(HB_IJAB_TOT(c, i, j, a)) > 0.0 && !tbit(f, a)) {
+            size_t o4 = (o3 + a) * c->nbasis;
+            b = alias_draw(rs, c->nbasis, c->hb_ijab_U + o4, c->hb_ijab_K + o4);
+            allowed = !tbit(f, b);
+        } else {
+            allowed = 0;
+        }
+    }
+    if (allowed) {
+        int t0 = a < b ? a : b, t1 = a < b ? b : a;
+        out->e.to[0] = t0;
+        out->e.to[1] = t1;
+        out->e.perm = perm2(c, f, i, j, t0, t1);
+        hmatel = sc2_mol_excit(c, i, j, t0, t1, out->e.perm);
+        pgen = (1.0 - c->pattempt_single) * pij *
+               (((HB_IJA(c, i, j, a) / HB_IJA_TOT(c, i, j)) * (HB_IJAB(c, i, j, a, b) / HB_IJAB_TOT(c, i, j, a))) +
+                ((HB_IJA(c, i, j, b) / HB_IJA_TOT(c, i, j)) * (HB_IJAB(c, i, j, b, a) / HB_IJAB_TOT(c, i, j, b))));
+    }
+    out->allowed = allowed;
+    *pgen_out = pgen;
+    *hmatel_out = hmatel;
+}
+
 /* gen_excit_mol / gen_excit_mol_no_renorm (src/excit_gen_mol.f90:16-284) with
  * spawn_standard + attempt_to_spawn (src/spawning.F90:34-123, :711-768). */
 static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int64_t parent,
                         attempt_t *out) {
     memset(out, 0, sizeof(*out));
     out->e.from[0] = out->e.from[1] = out->e.to[0] = out->e.to[1] = -1;
-    int renorm = c->cfg.excit_gen == HGPU_EXCIT_GEN_RENORM;
+    int gen = c->cfg.excit_gen;
+    /* gen_excit_mol_heat_bath_uniform takes its singles from gen_single_excit_mol */
+    int renorm = gen == HGPU_EXCIT_GEN_RENORM || gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM;
     double pgen, hmatel;
-    if (rs_next(rs) < c->pattempt_single) {
+    if (gen == HGPU_EXCIT_GEN_HEAT_BATH) {
+        gen_heat_bath(c, rs, f, d, out, &pgen, &hmatel);
+    } else if (rs_next(rs) < c->pattempt_single) {
         int i = -1, a = -1, ok;
         out->e.nexcit = 1;
         if (renorm) ok = choose_ia_mol(c, rs, f, d, &i, &a);
@@ -753,6 +1082,8 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
             hmatel = 0.0;
             pgen = 1.0;
         }
+    } else if (gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM) {
+        gen_heat_bath_uniform_double(c, rs, f, d, out, &pgen, &hmatel);
     } else {
         int i, j, ij_sym, ij_spin, a = -1, b = -1, ok;
         double pgen_ij;
@@ -1379,6 +1710,13 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
             }
         }
     }
+    if (c->kind == HGPU_SYS_READ_IN &&
+        (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM)) {
+        if (init_heat_bath(c, cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH) != 0) {
+            oracle_destroy(c);
+            return NULL;
+        }
+    }
     c->fx_E0 = fx_energy(c, c->f0);
     c->H00 = fx_val(c, c->fx_E0);
     c->cap = cfg->walker_length > 0 ? cfg->walker_length : 1000000;
@@ -1402,6 +1740,8 @@ void oracle_destroy(oracle_ctx *c) {
     free(c->fx_h1); free(c->fx_J); free(c->fx_JK); free(c->fx_eps);
     free(c->dets); free(c->pops); free(c->kii);
     free(c->sdets); free(c->spops); free(c->sflag); free(c->sord); free(c->suid);
+    free(c->hb_i_w); free(c->hb_ij_w); free(c->hb_ija_w); free(c->hb_ija_tot); free(c->hb_ija_U);
+    free(c->hb_ija_K); free(c->hb_ijab_w); free(c->hb_ijab_tot); free(c->hb_ijab_U); free(c->hb_ijab_K);
     free(c);
 }
 

@@ -243,18 +243,24 @@ def batched_instances(n=128, seed=4):
         s = cache[key]
         na, nb = (nel + ms) // 2, (nel - ms) // 2
         nvirt = L * L - na
-        # tau: about 0.7 expected spawned walkers per attempt at most
-        tau = min(0.005, 0.7 / ((U / (L * L)) * na * nb * nvirt))
-        cap = int(6 * target) + 20000
-        cfg = make_config(s, tau=tau, init_pop=10, target_population=target, ncycles=10, seed=1000 + k,
+        # tau: at most 0.2 expected spawned walkers per attempt, so that the
+        # population grows by at most ~20 % per cycle
+        tau = min(0.005, 0.2 / ((U / (L * L)) * na * nb * nvirt))
+        cap = int(16 * target) + 20000
+        # the calculation starts with the target population on the reference
+        # determinant and reports (updates the shift) every cycle, so the shift
+        # acts from the first cycle on
+        cfg = make_config(s, tau=tau, init_pop=target, target_population=target, ncycles=1, seed=1000 + k,
                           state_size=cap, spawned_state_size=cap)
         out.append((s, cfg, dict(L=L, U=U, target=target, tau=tau)))
     return out
 
 
-def batched_measure(steps, max_reports=40):
-    """config 4: grow every instance until its shift varies (untimed), then time
-    `steps` batch cycles (one graph launch each for all instances)."""
+def batched_measure(steps, equil_cycles=150):
+    """config 4: every instance starts with its target population on the
+    reference determinant; `equil_cycles` untimed cycles (a report after each,
+    so that the shift acts every cycle) spread it out, then `steps` batch
+    cycles are timed (one graph launch each for all instances)."""
     from hande_gb300.engine import Batch, Engine
     inst = batched_instances()
     engines = [Engine(s, cfg) for s, cfg, _ in inst]
@@ -262,11 +268,11 @@ def batched_measure(steps, max_reports=40):
         e.initial_distribution()
     batch = Batch(engines)
     reps = None
-    for r in range(max_reports):
-        reps = batch.run_report()
-        if all(rp.vary_shift[0] for rp in reps):
-            break
-    grown = sum(1 for rp in reps if rp.vary_shift[0])
+    for c in range(equil_cycles):
+        batch.run_cycles(1)
+        reps = [e.end_report() for e in engines]
+    varying = sum(1 for rp in reps if rp.vary_shift[0])
+    targets = sum(m["target"] for _, _, m in inst)
     walkers = sum(rp.nparticles[0] for rp in reps)
     states = sum(rp.nstates for rp in reps)
     batch.run_cycles(3)  # warm-up
@@ -285,7 +291,8 @@ def batched_measure(steps, max_reports=40):
         e.close()
     return {"workload": BATCH_WORKLOAD, "instances": len(inst), "value": att / dt, "unit": "attempts/s",
             "ms_per_step": 1e3 * dt / steps, "steps": steps, "walkers": walkers, "states": int(states),
-            "instances_at_target": grown, "error_flags": flags, "dtype": "int64 walkers, f64",
+            "target_walkers": targets, "instances_shift_varying": varying, "equilibration_cycles": equil_cycles,
+            "error_flags": flags, "dtype": "int64 walkers, f64",
             "timing": "host wall clock around hgpu_batch_run_cycles (graph launches and the final synchronisation)"}
 
 

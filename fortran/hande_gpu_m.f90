@@ -117,6 +117,25 @@ module hande_gpu_m
             type(c_ptr), value :: h
             character(kind=c_char), intent(in) :: path(*)
         end function hgpu_restore
+
+        ! Batches: many handles advanced together, one graph launch per cycle.
+        integer(c_int32_t) function hgpu_batch_create(handles, n, batch) bind(c, name='hgpu_batch_create')
+            import :: c_ptr, c_int32_t
+            type(c_ptr), intent(in) :: handles(*)
+            integer(c_int32_t), value :: n
+            type(c_ptr), intent(out) :: batch
+        end function hgpu_batch_create
+
+        integer(c_int32_t) function hgpu_batch_run_cycles(batch, ncycles) bind(c, name='hgpu_batch_run_cycles')
+            import :: c_ptr, c_int32_t
+            type(c_ptr), value :: batch
+            integer(c_int32_t), value :: ncycles
+        end function hgpu_batch_run_cycles
+
+        integer(c_int32_t) function hgpu_batch_destroy(batch) bind(c, name='hgpu_batch_destroy')
+            import :: c_ptr, c_int32_t
+            type(c_ptr), value :: batch
+        end function hgpu_batch_destroy
     end interface
 
 end module hande_gpu_m

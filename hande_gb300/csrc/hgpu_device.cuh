@@ -397,6 +397,18 @@ __device__ __forceinline__ int ims_of(int p) { return (p & 1) ? 0 : 1; }  // 0 b
 // (ii|jj) and, for parallel spins, -(ij|ji) -- or of slater_condon0_hub_k
 // (src/hamiltonian_hub_k.f90:91-132) -- nalpha*nbeta*U/N and the
 // single-particle energies -- accumulated in 64-bit integers.
+// The even bits of x (bits 0, 2, 4, ...) packed into the low 32 bits: the
+// spatial orbitals of one spin of a determinant word.
+__device__ __forceinline__ uint64_t unzip_even(uint64_t x) {
+    x &= 0x5555555555555555ull;
+    x = (x | (x >> 1)) & 0x3333333333333333ull;
+    x = (x | (x >> 2)) & 0x0F0F0F0F0F0F0F0Full;
+    x = (x | (x >> 4)) & 0x00FF00FF00FF00FFull;
+    x = (x | (x >> 8)) & 0x0000FFFF0000FFFFull;
+    x = (x | (x >> 16)) & 0x00000000FFFFFFFFull;
+    return x;
+}
+
 // The tables (fx_h1, fx_pair, fx_eps) are passed explicitly so that a kernel can
 // read them from a shared-memory copy (FxTabs).
 struct FxTabs {
@@ -438,28 +450,33 @@ __device__ int64_t fx_energy(const DevSys &s, const Det<W> &f, const FxTabs &tb)
         }
         return e;
     }
+    // Spin-resolved spatial occupations: every term is an integer, so the
+    // pairs may be summed in any order -- alpha-alpha and beta-beta pairs from
+    // the same-spin table, every alpha-beta pair (a doubly occupied orbital
+    // included) from the opposite-spin table.
     const int M = s.norb;
+    uint64_t am = 0, bm = 0;
 #pragma unroll
     for (int k = 0; k < W; k++) {
-        uint64_t x = f.w[k];
-        while (x) {
-            int i = 64 * k + __ffsll((long long)x) - 1;
-            x &= x - 1;
-            int si = i >> 1;
-            e += tb.h1[si];
-            const int64_t *opp = tb.pair + (size_t)si * M;
-            const int64_t *same = opp + (size_t)M * M;
-            // partners j > i
-#pragma unroll
-            for (int q = k; q < W; q++) {
-                uint64_t y = q == k ? x : f.w[q];
-                while (y) {
-                    int j = 64 * q + __ffsll((long long)y) - 1;
-                    y &= y - 1;
-                    e += (((i ^ j) & 1) == 0) ? same[j >> 1] : opp[j >> 1];
-                }
-            }
-        }
+        am |= unzip_even(f.w[k]) << (32 * k);
+        bm |= unzip_even(f.w[k] >> 1) << (32 * k);
+    }
+    const int64_t *same_tab = tb.pair + (size_t)M * M;
+    for (uint64_t x = am; x;) {
+        int p = __ffsll((long long)x) - 1;
+        x &= x - 1;
+        e += tb.h1[p];
+        const int64_t *opp = tb.pair + (size_t)p * M;
+        const int64_t *same = same_tab + (size_t)p * M;
+        for (uint64_t y = x; y; y &= y - 1) e += same[__ffsll((long long)y) - 1];  // alpha partners above p
+        for (uint64_t y = bm; y; y &= y - 1) e += opp[__ffsll((long long)y) - 1];  // every beta partner
+    }
+    for (uint64_t x = bm; x;) {
+        int p = __ffsll((long long)x) - 1;
+        x &= x - 1;
+        e += tb.h1[p];
+        const int64_t *same = same_tab + (size_t)p * M;
+        for (uint64_t y = x; y; y &= y - 1) e += same[__ffsll((long long)y) - 1];  // beta partners above p
     }
     return e;
 }

@@ -518,7 +518,7 @@ static int alloc_lists(hgpu_handle *h) {
         const int sms = h->sms;
         b.grid = clampi(b.cap / 4096, 8, std::min(4 * sms, kMaxBlocks));
         b.spawn_grid = clampi(b.scap / 1024, 8, 8 * sms);
-        b.sort_grid = clampi(b.scap / OSConf<1>::tile + 1, 4, 3 * sms);  // 256 threads, ~58 KB shared memory
+        b.sort_grid = clampi(b.scap / OSConf<1>::tile + 1, 4, 4 * sms);  // 256 threads, ~46 KB shared memory
     }
     if ((rc = dalloc(h, &b.state, 1))) return rc;
     CK(cudaMemset(b.state, 0, sizeof(DevState)));

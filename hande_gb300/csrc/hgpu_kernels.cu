@@ -646,15 +646,20 @@ __global__ void __launch_bounds__(kBlock) k_merge_splits(DevBuffers b, int cur) 
 // (src/annihilation.f90:294-486), remove_unoccupied_dets' rounding (:537-598),
 // round_low_population_spawns (:600-675), the merged rank of every element and,
 // densely over the tile's new determinants, their K_ii (insert_new_walker :855).
-// Each thread takes kMergeTile/kBlock consecutive merged positions of the tile:
-// one merge-path search finds where they start, then a sequential merge of the
-// two sorted slices (main entry first among equals) walks them.
+// The merge itself: each thread takes kMergeTile/kBlock consecutive merged
+// positions, finds where they start by one merge-path search and walks them
+// with a sequential merge of the two sorted slices (main entry first among
+// equals), recording for each position which entry it holds and whether that
+// entry meets its equal in the other list; the entries are then processed with
+// consecutive threads on consecutive positions, so the global accesses coalesce.
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_merge_tiles(DevBuffers b, int R, int cur) {
     constexpr int PER = kMergeTile / kBlock;
+    constexpr uint32_t kSpawnBit = 1u << 31, kHitBit = 1u << 30, kIdxMask = kHitBit - 1;
     __shared__ DevSys s;
     __shared__ uint64_t tdet[kMergeTile * W];
-    __shared__ int32_t newlist[kMergeTile];
+    __shared__ uint32_t desc[kMergeTile];     // per merged position: spawn bit, hit bit, slice index
+    __shared__ uint16_t newlist[kMergeTile];  // tile indices of new determinants
     __shared__ int nnew;
     extern __shared__ int64_t fx_smem[];  // exact-diagonal tables (fx_table_words)
     stage_sys(s, b.sys);
@@ -684,81 +689,95 @@ __global__ void __launch_bounds__(kBlock) k_merge_tiles(DevBuffers b, int R, int
         }
         if (threadIdx.x == 0) nnew = 0;
         __syncthreads();
-        uint32_t kept_main = 0, kept_any = 0;  // this thread's elements of the tile
-        const int p0 = threadIdx.x * PER;
-        const int plen = min(PER, nm + ns - p0);
-        if (plen > 0) {
-            // main entries among the first p0 merged elements of the tile
-            int lo = max(0, p0 - ns), hi = min(p0, nm);
-            while (lo < hi) {
-                int mid = (lo + hi) >> 1;
-                if (!det_less<W>(tile_det(nm + p0 - 1 - mid), tile_det(mid))) lo = mid + 1;
-                else hi = mid;
-            }
-            int a = lo, bb = p0 - lo;
-            for (int q = 0; q < plen; q++) {
-                const int64_t rank = d0 + p0 + q;
-                bool take_main = a < nm && (bb >= ns || !det_less<W>(tile_det(nm + bb), tile_det(a)));
-                if (take_main) {
-                    Det<W> d = tile_det(a);
-                    int64_t i = i0 + a, j = j0 + bb;
-                    bool hit;
-                    if (bb < ns) hit = det_eq<W>(tile_det(nm + bb), d);
-                    else hit = j < U && det_eq<W>(load_det<W>(b.udets, j), d);
-                    int64_t p[2] = {0, 0};
-                    for (int qq = 0; qq < R; qq++) p[qq] = mpops[i * R + qq];
-                    if (hit) {
-                        uint64_t fl = b.uflag[j];
-                        for (int qq = 0; qq < R; qq++) {
-                            int64_t sp = b.upops[j * R + qq];
-                            if (!s.initiator || p[qq] != 0) p[qq] += sp;
-                            else if (!((fl >> qq) & 1)) p[qq] = sp;
-                        }
-                    }
-                    if (s.real_amplitudes) round_pops(s, p, R, P_ROUND_MAIN, i, iter);
-                    bool nz = false;
-                    for (int qq = 0; qq < R; qq++) {
-                        mpops[i * R + qq] = p[qq];
-                        nz = nz || p[qq] != 0;
-                    }
-                    b.mref[rank] = i;
-                    b.mkeep[rank] = make_uint2(nz ? 1u : 0u, nz ? 1u : 0u);
-                    kept_main += nz ? 1u : 0u;
-                    kept_any += nz ? 1u : 0u;
-                    a++;
-                } else {
-                    Det<W> d = tile_det(nm + bb);
-                    int64_t j = j0 + bb;
-                    bool hit;
-                    if (a > 0) hit = det_eq<W>(tile_det(a - 1), d);
-                    else hit = i0 > 0 && det_eq<W>(load_det<W>(mdets, i0 - 1), d);
-                    uint32_t keep = 0;
-                    if (!hit) {
-                        int64_t sp[2] = {0, 0};
-                        for (int qq = 0; qq < R; qq++) sp[qq] = b.upops[j * R + qq];
-                        bool discard = false;
-                        if (s.initiator) {
-                            uint64_t fl = b.uflag[j];
-                            discard = true;
-                            for (int qq = 0; qq < R; qq++) {
-                                if ((fl >> qq) & 1) sp[qq] = 0;
-                                else discard = false;
-                            }
-                        }
-                        if (!discard && s.real_amplitudes) round_pops(s, sp, R, P_ROUND_SPAWN, j, iter);
-                        bool nz = false;
-                        for (int qq = 0; qq < R; qq++) {
-                            b.upops[j * R + qq] = sp[qq];
-                            nz = nz || sp[qq] != 0;
-                        }
-                        keep = discard ? 0u : (s.real_amplitudes ? (nz ? 1u : 0u) : 1u);
-                        if (keep) newlist[atomicAdd(&nnew, 1)] = nm + bb;
-                    }
-                    b.mref[rank] = -(j + 1);
-                    b.mkeep[rank] = make_uint2(0u, keep);
-                    kept_any += keep;
-                    bb++;
+        {
+            const int p0 = threadIdx.x * PER;
+            const int plen = min(PER, nm + ns - p0);
+            if (plen > 0) {
+                // main entries among the first p0 merged elements of the tile
+                int lo = max(0, p0 - ns), hi = min(p0, nm);
+                while (lo < hi) {
+                    int mid = (lo + hi) >> 1;
+                    if (!det_less<W>(tile_det(nm + p0 - 1 - mid), tile_det(mid))) lo = mid + 1;
+                    else hi = mid;
                 }
+                int a = lo, bb = p0 - lo;
+                for (int q = 0; q < plen; q++) {
+                    if (a < nm && (bb >= ns || !det_less<W>(tile_det(nm + bb), tile_det(a)))) {
+                        // main entry a meets the smallest spawned entry not below it
+                        bool hit;
+                        if (bb < ns) hit = det_eq<W>(tile_det(nm + bb), tile_det(a));
+                        else hit = j1 < U && det_eq<W>(load_det<W>(b.udets, j1), tile_det(a));
+                        desc[p0 + q] = (uint32_t)a | (hit ? kHitBit : 0u);
+                        a++;
+                    } else {
+                        // spawned entry bb meets the largest main entry not above it
+                        bool hit;
+                        if (a > 0) hit = det_eq<W>(tile_det(a - 1), tile_det(nm + bb));
+                        else hit = i0 > 0 && det_eq<W>(load_det<W>(mdets, i0 - 1), tile_det(nm + bb));
+                        desc[p0 + q] = kSpawnBit | (uint32_t)bb | (hit ? kHitBit : 0u);
+                        bb++;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        uint32_t kept_main = 0, kept_any = 0;  // this thread's elements of the tile
+        for (int k = threadIdx.x; k < nm + ns; k += blockDim.x) {
+            const uint32_t dsc = desc[k];
+            const bool hit = (dsc & kHitBit) != 0;
+            const int64_t rank = d0 + k;
+            if (!(dsc & kSpawnBit)) {
+                int64_t i = i0 + (dsc & kIdxMask);
+                int64_t p[2] = {0, 0};
+                for (int q = 0; q < R; q++) p[q] = mpops[i * R + q];
+                if (hit) {
+                    // the equal spawned entry is the first not below i in the spawned list
+                    int64_t j = j0 + (k - (int64_t)(dsc & kIdxMask));
+                    uint64_t fl = b.uflag[j];
+                    for (int q = 0; q < R; q++) {
+                        int64_t sp = b.upops[j * R + q];
+                        if (!s.initiator || p[q] != 0) p[q] += sp;
+                        else if (!((fl >> q) & 1)) p[q] = sp;
+                    }
+                }
+                if (s.real_amplitudes) round_pops(s, p, R, P_ROUND_MAIN, i, iter);
+                bool nz = false;
+                for (int q = 0; q < R; q++) {
+                    mpops[i * R + q] = p[q];
+                    nz = nz || p[q] != 0;
+                }
+                b.mref[rank] = i;
+                b.mkeep[rank] = make_uint2(nz ? 1u : 0u, nz ? 1u : 0u);
+                kept_main += nz ? 1u : 0u;
+                kept_any += nz ? 1u : 0u;
+            } else {
+                int bb = (int)(dsc & kIdxMask);
+                int64_t j = j0 + bb;
+                uint32_t keep = 0;
+                if (!hit) {
+                    int64_t sp[2] = {0, 0};
+                    for (int q = 0; q < R; q++) sp[q] = b.upops[j * R + q];
+                    bool discard = false;
+                    if (s.initiator) {
+                        uint64_t fl = b.uflag[j];
+                        discard = true;
+                        for (int q = 0; q < R; q++) {
+                            if ((fl >> q) & 1) sp[q] = 0;
+                            else discard = false;
+                        }
+                    }
+                    if (!discard && s.real_amplitudes) round_pops(s, sp, R, P_ROUND_SPAWN, j, iter);
+                    bool nz = false;
+                    for (int q = 0; q < R; q++) {
+                        b.upops[j * R + q] = sp[q];
+                        nz = nz || sp[q] != 0;
+                    }
+                    keep = discard ? 0u : (s.real_amplitudes ? (nz ? 1u : 0u) : 1u);
+                    if (keep) newlist[atomicAdd(&nnew, 1)] = (uint16_t)(nm + bb);
+                }
+                b.mref[rank] = -(j + 1);
+                b.mkeep[rank] = make_uint2(0u, keep);
+                kept_any += keep;
             }
         }
         // kept counts of the tile, for the tile-level scan of output positions

@@ -22,7 +22,7 @@ constexpr int kOSThreads = 256;  // one thread per digit value in the look-back
 constexpr int kMaxPasses = 16;
 template <int KW>
 struct OSConf {
-    static constexpr int items = KW == 1 ? 16 : 8;  // keys per thread
+    static constexpr int items = KW == 1 ? 12 : 6;  // keys per thread (4 blocks of 256 fit an SM)
     static constexpr int tile = kOSThreads * items;
     static constexpr size_t smem = (size_t)tile * (8 * KW + 4);  // staged keys + indices
 };

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kRadix) k_sort_offsets(DevBuffers b) {
 // One stable pass on digit `pass`: keys (KW words) and 32-bit indices (the
 // identity when idx_in is null).
 template <int KW>
-__global__ void __launch_bounds__(kOSThreads, 3) k_onesweep(DevBuffers b, int pass, const uint64_t *keys_in,
+__global__ void __launch_bounds__(kOSThreads, 4) k_onesweep(DevBuffers b, int pass, const uint64_t *keys_in,
                                                          const uint32_t *idx_in, uint64_t *keys_out,
                                                          uint32_t *idx_out) {
     constexpr int ITEMS = OSConf<KW>::items;

@@ -14,9 +14,12 @@ from __future__ import annotations
 
 import os
 
-# DRAM bytes per spawning attempt of k_spawn measured by Nsight Compute on the
-# 26-orbital synthetic molecule (profiles/k_spawn_mol26.md); None until captured.
-SPAWN_DRAM_BYTES_PER_ATTEMPT = None
+# DRAM bytes (read + write) per spawning attempt of one k_spawn launch, measured
+# by Nsight Compute on the 26-orbital synthetic molecule at 3.05e6 attempts
+# (profiles/k_spawn_mol26.md: 18.87 MB read + 7.31 MB written); the traffic of a
+# launch grows in proportion to its attempts (parents read once, spawned entries
+# written once), so the bench scales it by the attempts of its own cycle.
+SPAWN_DRAM_BYTES_PER_ATTEMPT = (18.87e6 + 7.31e6) / 3.0548e6
 
 
 def entry_bytes(W: int, R: int, initiator: bool):

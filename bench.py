@@ -296,6 +296,77 @@ def batched_measure(steps, equil_cycles=150):
             "timing": "host wall clock around hgpu_batch_run_cycles (graph launches and the final synchronisation)"}
 
 
+PRECISION_WORKLOAD = ("config3: synthetic molecule M=48 nel=16 C1 (96 spin orbitals, 2-word determinants), heat-bath "
+                      "excitation generator, initiator (threshold 3), real amplitudes, cutoff 0.01; FP32 spawning "
+                      "(integrals, heat-bath weights, p_gen) against FP64 with the same seed")
+
+
+def precision_study(target=2e5, tau=5e-5, equil=60, reports=300, nsample=1 << 20, seed=2024):
+    """config 3: the mixed-precision engine against the FP64 engine on the same
+    seed -- the largest relative error of FP32 H_ij and p_gen over nsample
+    generated excitations, the reblocked E_proj of both runs and their
+    difference in units of the combined standard error, and the attempts/s of
+    each."""
+    from hande_gb300 import analysis, systems
+    from hande_gb300._abi import PREC_FP64, PREC_MIXED, make_config
+    from hande_gb300.engine import Engine
+    s = systems.synthetic_molecule(48, 16, seed=seed)
+    out = {"workload": PRECISION_WORKLOAD, "target": target, "tau": tau}
+    res = {}
+    for name, prec in (("fp64", PREC_FP64), ("fp32", PREC_MIXED)):
+        cfg = make_config(s, tau=tau, init_pop=10, target_population=target, ncycles=10, seed=77,
+                          real_amplitudes=True, spawn_cutoff=0.01, excit_gen="heat_bath", initiator=True,
+                          initiator_threshold=3.0, precision=prec, state_size=int(20 * target) + 100000,
+                          spawned_state_size=int(20 * target) + 100000)
+        t0 = time.perf_counter()
+        e = Engine(s, cfg)
+        build_s = time.perf_counter() - t0
+        e.initial_distribution()
+        num, d0 = [], []
+        att = 0
+        dev_ms = 0.0
+        flags = 0
+        for r in range(equil + reports):
+            rep = e.run_report()
+            flags |= rep.error_flags
+            if r % 20 == 0:
+                sys.stderr.write("%s report %d Nw=%.4g states=%d shift=%.4f flags=%d\n" % (
+                    name, r, rep.nparticles[0], rep.nstates, rep.shift[0], rep.error_flags))
+            if r >= equil:
+                num.append(rep.proj_energy[0])
+                d0.append(rep.D0_population[0])
+                att += rep.nattempts
+                dev_ms += rep.device_ms
+        E, err, opt = analysis.projected_energy(num, d0)
+        res[name] = {"E_proj": E, "sigma": err, "opt_block": opt, "attempts_per_s": att / (dev_ms * 1e-3),
+                     "walkers": rep.nparticles[0], "states": int(rep.nstates), "error_flags": flags,
+                     "table_build_s": build_s}
+        res[name + "_engine"] = e
+    # generated excitations of the same parents, FP32 against FP64
+    e64, e32 = res.pop("fp64_engine"), res.pop("fp32_engine")
+    st, po, _ = e64.walkers()
+    rng = np.random.default_rng(5)
+    pick = rng.integers(0, st.shape[0], nsample)
+    parents, pp = st[pick], np.ones(nsample, np.int64)
+    r64 = e64.eval_excitations(parents, pp, 3)
+    r32 = e32.eval_excitations(parents, pp, 3)
+    same = np.all(r32[0] == r64[0], axis=1) & (r32[3] == r64[3]) & (r64[3] == 1)
+    rel_h = np.abs(r32[2][same] - r64[2][same]) / np.abs(r64[2][same])
+    rel_p = np.abs(r32[1][same] - r64[1][same]) / np.abs(r64[1][same])
+    big = np.abs(r64[2][same]) > 1e-3 * np.max(np.abs(r64[2][same]))
+    out.update(res)
+    out["excitations"] = {"sampled": nsample, "same_excitation": float(same.sum()) / max(int((r64[3] == 1).sum()), 1),
+                          "max_rel_err_hij": float(rel_h.max()), "max_rel_err_hij_above_1e-3_of_max":
+                          float(rel_h[big].max()), "max_rel_err_pgen": float(rel_p.max())}
+    d = res["fp32"]["E_proj"] - res["fp64"]["E_proj"]
+    sig = float(np.hypot(res["fp32"]["sigma"], res["fp64"]["sigma"]))
+    out["dE_proj"] = d
+    out["dE_proj_over_sigma"] = d / sig if sig > 0 else None
+    e64.close()
+    e32.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -307,6 +378,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (config 4) measurement")
+    ap.add_argument("--config", type=int, default=2,
+                    help="2: the headline line (default); 3: the mixed-precision study of config 3, one JSON line")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -315,6 +388,10 @@ def main():
             reference_arm(args)
         return
     args.warmup = max(args.warmup, 3)
+    if args.config == 3:
+        if rank == 0:
+            print(json.dumps(precision_study()))
+        return
 
     cpu = None
     dist = None

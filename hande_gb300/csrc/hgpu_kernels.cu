@@ -358,11 +358,11 @@ struct SpawnQueue {
 };
 
 // One spawning attempt of a queued chunk entry; returns the spawned amount.
-template <int W, int KIND, typename Real>
+template <int W, int KIND, typename Real, bool SINGLE>
 __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
                                                const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
-                                               bool drew, uint64_t bufk, bool single, Det<W> &child, int &sp,
-                                               uint32_t &info) {
+                                               bool drew, uint64_t bufk, Det<W> &child, int &sp, uint32_t &info) {
+    constexpr bool single = SINGLE;
     int64_t i = slot / R;
     sp = (int)(slot - i * R);
     Det<W> f = load_det<W>(dets, i);
@@ -392,6 +392,15 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
     }
     if (at.nspawn != 0) child = excited<W>(f, at);
     return at.nspawn;
+}
+
+// The singles (a tenth of the attempts) in a function of their own, so that the
+// doubles' loop in k_spawn stays small in the instruction cache.
+template <int W, int KIND, typename Real>
+__device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
+                                                   const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
+                                                   uint64_t bufk, Det<W> &child, int &sp, uint32_t &info) {
+    return spawn_entry<W, KIND, Real, true>(s, t, b, R, dets, iter, slot, att, true, bufk, child, sp, info);
 }
 
 template <int W, int KIND, typename Real>
@@ -480,8 +489,12 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
                 if (j0 + lane < n) {
                     int off = list[j0 + lane];
                     uint32_t info;
-                    nspawn = spawn_entry<W, KIND, Real>(s, t, b, R, dets, iter, q.slot[off], q.att[off], drew,
-                                                        q.bufk[off], pass == 1, child, sp, info);
+                    if (pass == 0)
+                        nspawn = spawn_entry<W, KIND, Real, false>(s, t, b, R, dets, iter, q.slot[off], q.att[off],
+                                                                   drew, q.bufk[off], child, sp, info);
+                    else
+                        nspawn = spawn_entry_single<W, KIND, Real>(s, t, b, R, dets, iter, q.slot[off], q.att[off],
+                                                                   q.bufk[off], child, sp, info);
                     if (nspawn != 0) {
                         want = true;
                         flagword = (uint64_t)((info >> 2) & 3u) | ((uint64_t)(cbase + off) << 2);

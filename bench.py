@@ -301,7 +301,7 @@ PRECISION_WORKLOAD = ("config3: synthetic molecule M=48 nel=16 C1 (96 spin orbit
                       "(integrals, heat-bath weights, p_gen) against FP64 with the same seed")
 
 
-def precision_study(target=2e5, tau=5e-5, equil=60, reports=300, nsample=1 << 20, seed=2024):
+def precision_study(target=2e5, tau=5e-5, equil=100, reports=600, nsample=1 << 20, seed=2024, max_grow=600):
     """config 3: the mixed-precision engine against the FP64 engine on the same
     seed -- the largest relative error of FP32 H_ij and p_gen over nsample
     generated excitations, the reblocked E_proj of both runs and their
@@ -314,7 +314,7 @@ def precision_study(target=2e5, tau=5e-5, equil=60, reports=300, nsample=1 << 20
     out = {"workload": PRECISION_WORKLOAD, "target": target, "tau": tau}
     res = {}
     for name, prec in (("fp64", PREC_FP64), ("fp32", PREC_MIXED)):
-        cfg = make_config(s, tau=tau, init_pop=10, target_population=target, ncycles=10, seed=77,
+        cfg = make_config(s, tau=tau, init_pop=2000, target_population=target, ncycles=10, seed=77,
                           real_amplitudes=True, spawn_cutoff=0.01, excit_gen="heat_bath", initiator=True,
                           initiator_threshold=3.0, precision=prec, state_size=int(20 * target) + 100000,
                           spawned_state_size=int(20 * target) + 100000)
@@ -326,10 +326,17 @@ def precision_study(target=2e5, tau=5e-5, equil=60, reports=300, nsample=1 << 20
         att = 0
         dev_ms = 0.0
         flags = 0
+        grown = 0
+        for r in range(max_grow):  # until the shift varies
+            rep = e.run_report()
+            flags |= rep.error_flags
+            grown = r + 1
+            if rep.vary_shift[0]:
+                break
         for r in range(equil + reports):
             rep = e.run_report()
             flags |= rep.error_flags
-            if r % 20 == 0:
+            if r % 50 == 0:
                 sys.stderr.write("%s report %d Nw=%.4g states=%d shift=%.4f flags=%d\n" % (
                     name, r, rep.nparticles[0], rep.nstates, rep.shift[0], rep.error_flags))
             if r >= equil:
@@ -339,6 +346,7 @@ def precision_study(target=2e5, tau=5e-5, equil=60, reports=300, nsample=1 << 20
                 dev_ms += rep.device_ms
         E, err, opt = analysis.projected_energy(num, d0)
         res[name] = {"E_proj": E, "sigma": err, "opt_block": opt, "attempts_per_s": att / (dev_ms * 1e-3),
+                     "growth_reports": grown, "reports": reports,
                      "walkers": rep.nparticles[0], "states": int(rep.nstates), "error_flags": flags,
                      "table_build_s": build_s}
         res[name + "_engine"] = e

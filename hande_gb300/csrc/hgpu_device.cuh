@@ -1047,11 +1047,11 @@ __device__ __forceinline__ Real hb_weight(const DevSys &s, int i, int j, int a, 
 }
 
 // select_weighted_value (lib/local/alias.f90:62-98): generate_alias_tables
-// (:100-184) over n <= kHBMaxEl weights, then one draw.
-template <typename Real>
+// (:100-184) over n <= CAP weights, then one draw.
+template <typename Real, int CAP = kHBMaxEl>
 __device__ __forceinline__ int hb_alias_select(RStream &rs, int n, const Real *w, Real tot) {
-    Real U[kHBMaxEl];
-    uint8_t K[kHBMaxEl], under[kHBMaxEl], over[kHBMaxEl];
+    Real U[CAP];
+    uint8_t K[CAP], under[CAP], over[CAP];
     int nu = 0, no = 0;
     Real f = (Real)n / tot;
     for (int i = 0; i < n; i++) {
@@ -1279,8 +1279,71 @@ __device__ void gen_heat_bath_uniform_double(const DevSys &s, RStream &rs, const
     hm = h;
 }
 
-// spawn_standard + attempt_to_spawn with a heat-bath generator (heat_bath, or
-// heat_bath_uniform whose singles are gen_single_excit_mol's).
+// slater_condon1_mol (src/hamiltonian_molecular.f90:140-196) with perm = false:
+// 0 unless i and a share spin and symmetry.
+template <int W, typename Real>
+__device__ __forceinline__ Real sc1_checked(const DevSys &s, const Det<W> &f, int i, int a) {
+    if (s.orbsym[i] != s.orbsym[a] || ms_of(i) != ms_of(a)) return (Real)0;
+    return sc1_mol<W, Real>(s, f, i, a, false);
+}
+
+// find_ia_single_weights (src/excit_gen_utils.f90:169-212) and
+// gen_single_excit_heat_bath_exact (src/excit_gen_heat_bath_mol.F90:732-807):
+// i chosen with weight sum_a |H_ia| over the unoccupied a, then a with weight
+// |H_ia|.  The row of the chosen i is evaluated again rather than stored (the
+// same values), so a thread holds O(nvirt) weights, not O(nel nvirt).
+template <int W, typename Real>
+__device__ void gen_single_hb_exact(const DevSys &s, RStream &rs, const MolDet<W> &d, Attempt &out, double &pgen,
+                                    Real &hm) {
+    const Det<W> &f = d.f;
+    out.nexcit = 1;
+    uint8_t occ[kHBMaxEl];
+    Real wi[kHBMaxEl];
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++)
+        for (uint64_t x = f.w[k]; x && n < kHBMaxEl; x &= x - 1) occ[n++] = (uint8_t)(64 * k + __ffsll((long long)x) - 1);
+    Real tot = (Real)0;
+    for (int ii = 0; ii < s.nel; ii++) {
+        Real w = (Real)0;
+#pragma unroll
+        for (int k = 0; k < W; k++)
+            for (uint64_t x = ~f.w[k] & d.valid[k]; x; x &= x - 1)
+                w = w + rabs(sc1_checked<W, Real>(s, f, occ[ii], 64 * k + __ffsll((long long)x) - 1));
+        wi[ii] = w;
+        tot = tot + w;
+    }
+    if (tot < (Real)1.0e-12) {
+        out.allowed = false;
+        pgen = 1.0;
+        hm = (Real)0;
+        return;
+    }
+    const int i_ind = hb_alias_select<Real>(rs, s.nel, wi, tot);
+    const int i = occ[i_ind];
+    constexpr int CAP = 64 * W;
+    Real row[CAP];
+    uint8_t unocc[CAP];
+    int nv = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++)
+        for (uint64_t x = ~f.w[k] & d.valid[k]; x; x &= x - 1) {
+            int a = 64 * k + __ffsll((long long)x) - 1;
+            unocc[nv] = (uint8_t)a;
+            row[nv++] = rabs(sc1_checked<W, Real>(s, f, i, a));
+        }
+    const int a_ind = hb_alias_select<Real, CAP>(rs, nv, row, wi[i_ind]);
+    const int a = unocc[a_ind];
+    out.allowed = true;
+    out.from[0] = i;
+    out.to[0] = a;
+    pgen = (double)((Real)s.pattempt_single * (wi[i_ind] / tot) * (row[a_ind] / wi[i_ind]));
+    hm = sc1_mol<W, Real>(s, f, i, a, perm1<W>(f, i, a));
+}
+
+// spawn_standard + attempt_to_spawn with a heat-bath generator (heat_bath;
+// heat_bath_uniform, whose singles are gen_single_excit_mol's; heat_bath_single,
+// whose singles are gen_single_excit_heat_bath_exact's).
 template <int W, typename Real>
 __device__ void attempt_heat_bath(const DevSys &s, RStream &rs, const MolDet<W> &d, int64_t parent, Attempt &out) {
     out.from[0] = out.from[1] = out.to[0] = out.to[1] = -1;
@@ -1288,10 +1351,12 @@ __device__ void attempt_heat_bath(const DevSys &s, RStream &rs, const MolDet<W> 
     Real hm;
     if (s.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH)
         gen_heat_bath<W, Real>(s, rs, d.f, out, pgen, hm);
-    else if (rs.next_k() < s.t_single)  // rand < pattempt_single
-        gen_single_mol<W, Real>(s, rs, d, true, out, pgen, hm);
-    else
+    else if (rs.next_k() >= s.t_single)  // rand >= pattempt_single: a double
         gen_heat_bath_uniform_double<W, Real>(s, rs, d.f, out, pgen, hm);
+    else if (s.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE)
+        gen_single_hb_exact<W, Real>(s, rs, d, out, pgen, hm);
+    else
+        gen_single_mol<W, Real>(s, rs, d, true, out, pgen, hm);
     attempt_to_spawn(s, rs, parent, pgen, (double)hm, out);
 }
 

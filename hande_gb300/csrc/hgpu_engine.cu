@@ -395,7 +395,8 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
             s.pg2_x = X;
             s.pg2_n = Nn;
         }
-        if (c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM) {
+        if (c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM ||
+            c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE) {
             if ((rc = build_heat_bath(h, sys, s))) return rc;
         }
     } else {
@@ -493,10 +494,13 @@ static int alloc_lists(hgpu_handle *h) {
         if ((rc = dalloc(h, &b.os_epoch, 1))) return rc;
         CK(cudaMemset(b.os_epoch, 0, sizeof(uint32_t)));
     }
-    if ((rc = dalloc(h, &b.segpops, (size_t)b.scap * R))) return rc;
-    if ((rc = dalloc(h, &b.segflag, (size_t)b.scap))) return rc;
-    if ((rc = dalloc(h, &b.segkeep, (size_t)b.scap))) return rc;
-    if ((rc = dalloc(h, &b.segpos, (size_t)b.scap))) return rc;
+    {
+        size_t tiles = (size_t)b.scap / kSegTile + 2;  // tiles of the self-annihilation
+        if ((rc = dalloc(h, &b.seg_status, tiles))) return rc;
+        CK(cudaMemset(b.seg_status, 0, sizeof(uint64_t) * tiles));
+        if ((rc = dalloc(h, &b.seg_epoch, 1))) return rc;
+        CK(cudaMemset(b.seg_epoch, 0, sizeof(uint32_t)));
+    }
     if ((rc = dalloc(h, &b.udets, (size_t)b.scap * W))) return rc;
     if ((rc = dalloc(h, &b.upops, (size_t)b.scap * R))) return rc;
     if ((rc = dalloc(h, &b.uflag, (size_t)b.scap))) return rc;
@@ -561,7 +565,8 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
         if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM)
             return HGPU_ERR_UNSUPPORTED;
     } else if (sys->kind == HGPU_SYS_READ_IN) {
-        bool hb = cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM;
+        bool hb = cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM ||
+                  cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE;
         if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM && !hb)
             return HGPU_ERR_UNSUPPORTED;
         if (hb && sys->nel > kHBMaxEl) return HGPU_ERR_UNSUPPORTED;
@@ -579,7 +584,9 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     h->gkind = sys->kind;
     if (sys->kind == HGPU_SYS_READ_IN) {
         if (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH) h->gkind = kKindHeatBath;
-        else if (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM) h->gkind = kKindHeatBathUniform;
+        else if (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM ||
+                 cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE)
+            h->gkind = kKindHeatBathUniform;  // the singles differ at run time
         else if (cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM) h->gkind = kKindReadInNoRenorm;
     }
     h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;

@@ -171,14 +171,6 @@ struct StoreInclusive {
     int64_t *out;
     __device__ void operator()(int64_t i, int64_t ex, int64_t v) const { out[i] = ex + v; }
 };
-struct LoadKeep {
-    const uint32_t *a;
-    __device__ int64_t operator()(int64_t i) const { return (int64_t)a[i]; }
-};
-struct StoreExclusive {
-    int64_t *out;
-    __device__ void operator()(int64_t i, int64_t ex, int64_t) const { out[i] = ex; }
-};
 
 // n_ptr points at an int64 count; for N*R lists a small kernel writes the product.
 __global__ void k_set_count(int64_t *dst, const int64_t *a, int64_t mul, const int64_t *b) {
@@ -256,18 +248,29 @@ __device__ __forceinline__ uint32_t decide_nattempts(RStream &rs, double populat
     return (uint32_t)n;
 }
 
+// decide_nattempts for population = p / 2^F (the encoded population and the
+// encoding's exponent), in integer arithmetic with the same result while
+// |p| < 2^53: the fraction frac 2^-F is non-zero exactly when it exceeds
+// 1e-12 (F <= 31), and frac 2^-F > u = k 2^-53 is frac 2^(53-F) > k.
+__device__ __forceinline__ uint32_t decide_nattempts_fx(RStream &rs, int64_t p, int F, double population) {
+    uint64_t ap = p < 0 ? (uint64_t)(-p) : (uint64_t)p;
+    if (ap >= (1ull << 53)) return decide_nattempts(rs, population);
+    uint64_t n = ap >> F, frac = ap & ((1ull << F) - 1);
+    if (frac != 0 && (frac << (53 - F)) > rs.next_k()) n = n + 1;
+    return (uint32_t)n;
+}
+
 // stochastic_death (src/death.f90:11-130) with weight = pop_control = 1.
 __device__ __forceinline__ int64_t stochastic_death(double tau, RStream &rs, double Kii, double shift,
                                                     int64_t &population) {
     double pd = tau * (Kii - shift);
     pd = pd * fabs((double)population);
-    int64_t kill = (int64_t)pd;
-    pd = pd - (double)kill;
-    double r = rs.next();
-    if (fabs(pd) > r) {
-        if (pd > 0.0) kill = kill + 1;
-        else kill = kill - 1;
-    }
+    // kill = int(pd); if (|pd - kill| > rand) kill = kill + sign(pd): the
+    // truncation and the fraction's comparison in integer arithmetic
+    // (hgpu_exact.h), valid while |pd| < 2^63
+    uint64_t pb = dbits(pd);
+    int64_t kill = round_up_frac(pb & 0x7FFFFFFFFFFFFFFFull, rs.next_k());
+    if (pb >> 63) kill = -kill;
     if (population < 0) population = population + kill;
     else population = population - kill;
     return kill < 0 ? -kill : kill;
@@ -310,7 +313,7 @@ __global__ void __launch_bounds__(kBlock) k_prep_parents(DevBuffers b, int R, in
             if (p < 0) info |= 1u << sp;
             RStream rs;
             rs.init(s.seed, P_NATTEMPT, sp, i, 0, iter);
-            b.natt[i * R + sp] = decide_nattempts(rs, rp);
+            b.natt[i * R + sp] = decide_nattempts_fx(rs, p, s.real_amplitudes ? 31 : 0, rp);
             rs.init(s.seed, P_DEATH, sp, i, 0, iter);
             ndeath += stochastic_death(s.tau, rs, k, shift[sp], p);
             pops[i * R + sp] = p;
@@ -385,6 +388,8 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
         double pgen;
         Real hm;
         if (KIND == kKindHeatBath) gen_heat_bath<W, Real>(s, rs, f, at, pgen, hm);
+        else if (single && KIND == kKindHeatBathUniform && s.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE)
+            gen_single_hb_exact<W, Real>(s, rs, d, at, pgen, hm);
         else if (single) gen_single_mol<W, Real>(s, rs, d, KIND != kKindReadInNoRenorm, at, pgen, hm);
         else if (KIND == kKindHeatBathUniform) gen_heat_bath_uniform_double<W, Real>(s, rs, f, at, pgen, hm);
         else gen_double_mol<W, Real>(s, rs, d, KIND == HGPU_SYS_READ_IN, at, pgen, hm);
@@ -545,71 +550,172 @@ __device__ __forceinline__ int sgn1(int64_t x) { return x >= 0 ? 1 : -1; }
 // Fortran sign(1, int(x)): int() keeps the low 32 bits of an int64.
 __device__ __forceinline__ int sign1_int32(int64_t x) { return (int32_t)(uint32_t)(uint64_t)x >= 0 ? 1 : -1; }
 
-// Sorted keys (KW words: the rank, or the determinant) are equal exactly when
-// the determinants are.
+// annihilate_spawn_t[_initiator] (src/spawn_data.F90:859-1101) of the segment
+// of equal keys that starts at sorted position i: the summed populations and,
+// for the initiator approximation, the flag of spaces whose sum may not create a
+// new walker.  Sorted keys (KW words: the rank, or the determinant) are equal
+// exactly when the determinants are.
 template <int KW>
-__global__ void __launch_bounds__(kBlock) k_seg_reduce(DevBuffers b, int R, const uint64_t *keys, const uint32_t *idx,
-                                                       int initiator) {
-    int64_t S = b.state->n_spawn;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
-        Det<KW> ki = load_det<KW>(keys, i);
-        bool head = i == 0 || !det_eq<KW>(load_det<KW>(keys, i - 1), ki);
-        if (!head) {
-            b.segkeep[i] = 0;
-            continue;
-        }
-        int64_t sum[2] = {0, 0}, ip[2] = {0, 0}, ev[2] = {0, 0}, firstpop[2] = {0, 0};
-        uint64_t minord = ~0ull, firstflag = 0;
-        for (int64_t j = i; j < S; j++) {
-            if (j > i && !det_eq<KW>(load_det<KW>(keys, j), ki)) break;
-            uint32_t e = idx[j];
-            uint64_t fl = initiator ? b.sflag[e] : 0;
-            for (int q = 0; q < R; q++) {
-                int64_t p = b.spops[(int64_t)e * R + q];
-                sum[q] += p;
-                if (initiator) {
-                    if (!((fl >> q) & 1)) ip[q] += p;
-                    else ev[q] += sgn3(p);
-                }
-            }
-            if (initiator && (fl >> 2) < minord) {
-                minord = fl >> 2;
-                firstflag = fl;
-                for (int q = 0; q < R; q++) firstpop[q] = b.spops[(int64_t)e * R + q];
-            }
-        }
-        uint64_t flag = 0;
-        if (initiator) {
-            // annihilate_spawn_t_initiator (src/spawn_data.F90:937-1101): the
-            // first entry of a determinant counts sign(1, int(pop)) events.
-            for (int q = 0; q < R; q++) {
-                if ((firstflag >> q) & 1) ev[q] += sign1_int32(firstpop[q]) - sgn3(firstpop[q]);
-                bool keep = (ip[q] != 0 && sgn1(sum[q]) == sgn1(ip[q])) || (ev[q] > 1 || ev[q] < -1);
-                if (!keep) flag |= 1ull << q;
-            }
-        }
-        bool nz = false;
+__device__ __forceinline__ void reduce_segment(const DevBuffers &b, int R, const uint64_t *keys, const uint32_t *idx,
+                                               int64_t i, int64_t S, int initiator, int64_t sum[2], uint64_t &flag) {
+    Det<KW> ki = load_det<KW>(keys, i);
+    int64_t ip[2] = {0, 0}, ev[2] = {0, 0}, firstpop[2] = {0, 0};
+    sum[0] = sum[1] = 0;
+    uint64_t minord = ~0ull, firstflag = 0;
+    for (int64_t j = i; j < S; j++) {
+        if (j > i && !det_eq<KW>(load_det<KW>(keys, j), ki)) break;
+        uint32_t e = idx[j];
+        uint64_t fl = initiator ? b.sflag[e] : 0;
         for (int q = 0; q < R; q++) {
-            b.segpops[i * R + q] = sum[q];
-            nz = nz || sum[q] != 0;
+            int64_t p = b.spops[(int64_t)e * R + q];
+            sum[q] += p;
+            if (initiator) {
+                if (!((fl >> q) & 1)) ip[q] += p;
+                else ev[q] += sgn3(p);
+            }
         }
-        b.segflag[i] = flag;
-        b.segkeep[i] = nz ? 1u : 0u;
+        if (initiator && (fl >> 2) < minord) {
+            minord = fl >> 2;
+            firstflag = fl;
+            for (int q = 0; q < R; q++) firstpop[q] = b.spops[(int64_t)e * R + q];
+        }
+    }
+    flag = 0;
+    if (initiator) {
+        // the first entry of a determinant counts sign(1, int(pop)) events
+        for (int q = 0; q < R; q++) {
+            if ((firstflag >> q) & 1) ev[q] += sign1_int32(firstpop[q]) - sgn3(firstpop[q]);
+            bool keep = (ip[q] != 0 && sgn1(sum[q]) == sgn1(ip[q])) || (ev[q] > 1 || ev[q] < -1);
+            if (!keep) flag |= 1ull << q;
+        }
     }
 }
 
-// Unique entries in sorted order; the determinant comes from the sorted keys, or
-// through the permutation from the spawned list when the keys are ranks.
-template <int W, bool RANK>
-__global__ void __launch_bounds__(kBlock) k_seg_compact(DevBuffers b, int R, const uint64_t *keys,
-                                                        const uint32_t *idx) {
-    int64_t S = b.state->n_spawn;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
-        if (!b.segkeep[i]) continue;
-        int64_t u = b.segpos[i];
-        store_det<W>(b.udets, u, RANK ? load_det<W>(b.sdets, idx[i]) : load_det<W>(keys, i));
-        for (int q = 0; q < R; q++) b.upops[u * R + q] = b.segpops[i * R + q];
-        b.uflag[u] = b.segflag[i];
+// Resets of the self-annihilation: tile tickets, the unique count, the look-back epoch.
+__global__ void k_seg_begin(DevBuffers b) {
+    b.state->seg_ticket = 0;
+    b.state->n_uniq = 0;
+    *b.seg_epoch += 1;
+}
+
+// Self-annihilation of the sorted spawned list in one pass: tiles of kSegTile
+// sorted positions, taken in ticket order, each thread holding kSegRounds
+// consecutive positions; the heads of segments of equal keys sum their
+// segment, one block scan orders the surviving (non-zero) sums, the tile's
+// output offset comes from a decoupled look-back over the preceding tiles, and
+// every thread writes its survivors to the unique spawned list (udets, upops,
+// uflag) in sorted order.
+template <int W, int KW, bool RANK>
+__global__ void __launch_bounds__(kBlock) k_seg_fused(DevBuffers b, int R, const uint64_t *keys, const uint32_t *idx,
+                                                      int initiator) {
+    __shared__ uint32_t s_tile, s_base;
+    DevState *st = b.state;
+    const int64_t S = st->n_spawn;
+    const int64_t ntiles = (S + kSegTile - 1) / kSegTile;
+    const uint32_t epoch = os_epoch(*b.seg_epoch, 0);
+    uint64_t *status = b.seg_status;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&st->seg_ticket, 1u);
+        __syncthreads();
+        const int64_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const int64_t p0 = tile * kSegTile + (int64_t)threadIdx.x * kSegRounds;
+        // keys of positions p0-1 .. p0+kSegRounds: heads and singleton segments
+        Det<KW> k[kSegRounds + 2];
+#pragma unroll
+        for (int r = 0; r < kSegRounds + 2; r++) {
+            int64_t i = p0 - 1 + r;
+            if (i >= 0 && i < S) k[r] = load_det<KW>(keys, i);
+        }
+        int64_t sum[kSegRounds][2];
+        uint64_t flag[kSegRounds];
+        uint32_t kept = 0, keepmask = 0;
+#pragma unroll
+        for (int r = 0; r < kSegRounds; r++) {
+            const int64_t i = p0 + r;
+            sum[r][0] = sum[r][1] = 0;
+            flag[r] = 0;
+            if (i >= S) continue;
+            bool head = i == 0 || !det_eq<KW>(k[r], k[r + 1]);
+            if (!head) continue;
+            bool single = i + 1 >= S || !det_eq<KW>(k[r + 1], k[r + 2]);
+            if (single && !initiator) {
+                // a segment of one entry: its populations
+                uint32_t e = idx[i];
+                for (int q = 0; q < R; q++) sum[r][q] = b.spops[(int64_t)e * R + q];
+            } else {
+                reduce_segment<KW>(b, R, keys, idx, i, S, initiator, sum[r], flag[r]);
+            }
+            if (sum[r][0] != 0 || (R > 1 && sum[r][1] != 0)) {
+                keepmask |= 1u << r;
+                kept++;
+            }
+        }
+        uint32_t run;
+        uint32_t ex = block_exclusive_scan<uint32_t>(kept, &run);
+        if (threadIdx.x == 0) {
+            // publish this tile's count, look back for its offset
+            volatile uint64_t *my = status + tile;
+            uint32_t excl = 0;
+            if (tile == 0) {
+                *my = os_word(kOSPrefix, epoch, run);
+            } else {
+                *my = os_word(kOSAggregate, epoch, run);
+                int64_t kk = tile - 1;
+                int spins = 0;
+                bool done = false;
+                while (!done) {
+                    uint64_t v[kOSLook];
+#pragma unroll
+                    for (int u = 0; u < kOSLook; u++)
+                        v[u] = kk - u >= 0 ? *(volatile uint64_t *)(status + (kk - u)) : 0;
+                    int u = 0;
+                    for (; u < kOSLook && kk - u >= 0; u++) {
+                        uint32_t ve = (uint32_t)(v[u] >> 32) & 0x3FFFFFFFu;
+                        uint64_t fl = v[u] >> 62;
+                        if (ve != (epoch & 0x3FFFFFFFu) || fl == 0) break;
+                        excl += (uint32_t)v[u];
+                        if (fl == kOSPrefix) {
+                            done = true;
+                            break;
+                        }
+                    }
+                    if (done) break;
+                    kk -= u;
+                    if (u == 0) {
+                        if (++spins > kSpinLimit) {
+                            atomicOr(&st->error_flags, HGPU_FLAG_TIMEOUT);
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
+                }
+                *my = os_word(kOSPrefix, epoch, excl + run);
+            }
+            s_base = excl;
+            atomicAdd((unsigned long long *)&st->n_uniq, (unsigned long long)run);
+        }
+        __syncthreads();
+        int64_t u = (int64_t)s_base + ex;
+#pragma unroll
+        for (int r = 0; r < kSegRounds; r++) {
+            if (!((keepmask >> r) & 1u)) continue;
+            const int64_t i = p0 + r;
+            if (u < b.scap) {
+                Det<W> d;
+                if (RANK) {
+                    d = load_det<W>(b.sdets, idx[i]);
+                } else {
+#pragma unroll
+                    for (int w = 0; w < W; w++) d.w[w] = k[r + 1].w[w % KW];
+                }
+                store_det<W>(b.udets, u, d);
+                for (int q = 0; q < R; q++) b.upops[u * R + q] = sum[r][q];
+                b.uflag[u] = flag[r];
+            }
+            u++;
+        }
+        __syncthreads();
     }
 }
 
@@ -1079,11 +1185,9 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
         o ^= 1;
     }
     if (pm) cudaEventRecord(pm->ev[4], st);
-    if (b.key_words == 1) k_seg_reduce<1><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
-    else k_seg_reduce<2><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
-    device_scan<int64_t>(b, LoadKeep{b.segkeep}, StoreExclusive{b.segpos}, &S->n_spawn, b.scan_part, &S->n_uniq, st);
-    if (b.use_rank) k_seg_compact<W, true><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin);
-    else k_seg_compact<W, false><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin);
+    k_seg_begin<<<1, 1, 0, st>>>(b);
+    if (b.use_rank) k_seg_fused<W, 1, true><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
+    else k_seg_fused<W, W, false><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
     if (pm) cudaEventRecord(pm->ev[5], st);
     k_merge_splits<W><<<b.grid, kBlock, 0, st>>>(b, cur);
     k_merge_tiles<W><<<b.grid, kBlock, b.fx_smem_bytes, st>>>(b, R, cur);
@@ -1155,9 +1259,9 @@ int set_kernel_attributes(const DevBuffers &b) {
 
 int launches_per_cycle(const DevBuffers &b) {
     // begin, prep, count, scan(3), spawn, clamp, sort_hist, sort_offsets,
-    // one per pass, seg_reduce, scan(3), compact, merge_splits, merge_tiles,
-    // tile_scan, scatter, end
-    return 2 + 1 + 3 + 1 + 1 + 2 + b.sort_passes + 1 + 3 + 1 + 2 + 1 + 1 + 1;
+    // one per pass, seg_begin, seg_fused, merge_splits, merge_tiles, tile_scan,
+    // scatter, end
+    return 2 + 1 + 3 + 1 + 1 + 2 + b.sort_passes + 2 + 2 + 1 + 1 + 1;
 }
 
 void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st) {

@@ -31,6 +31,8 @@ constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortItems = 8;    // keys per thread per radix tile
 constexpr int kMaxBlocks = 1024; // upper bound of the fixed grid (partials arrays)
 constexpr int kMergeTile = 2048; // merged elements per tile of the merge-path kernel
+constexpr int kSegRounds = 4;    // sorted positions per thread of a self-annihilation tile
+constexpr int kSegTile = kBlock * kSegRounds;
 
 // Per-cycle counters and per-report accumulators, resident in device memory so
 // that a whole cycle runs without host synchronisation (and can be replayed
@@ -57,6 +59,8 @@ struct DevState {
     int32_t pad2;
     uint64_t spawn_next;  // next unclaimed attempt chunk of the spawning kernel
     uint32_t os_ticket[16];  // next tile of each radix pass (hgpu_sort.cuh)
+    uint32_t seg_ticket;     // next tile of the self-annihilation
+    uint32_t pad3;
 };
 
 // Device buffers of one engine (all allocated once, at create).
@@ -92,10 +96,8 @@ struct DevBuffers {
     int sort_few_values[16];    // number of digit values of each such pass
     int sort_grid;      // blocks of the radix passes
     // self-annihilated list (size scap)
-    int64_t *segpops;   // per sorted position (R)
-    uint64_t *segflag;
-    uint32_t *segkeep;
-    int64_t *segpos;
+    uint64_t *seg_status;  // per self-annihilation tile: look-back status word
+    uint32_t *seg_epoch;   // look-back epoch of the self-annihilation (kept out of DevState)
     uint64_t *udets;
     int64_t *upops;
     uint64_t *uflag;

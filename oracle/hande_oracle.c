@@ -781,8 +781,8 @@ static int alias_draw(rstream *rs, int n, const double *U, const int32_t *K) {
 
 /* select_weighted_value (lib/local/alias.f90:62-98): alias table built on the fly. */
 static int alias_select(rstream *rs, int n, const double *w, double tot) {
-    double U[MAXEL];
-    int32_t K[MAXEL];
+    double U[MAXB];
+    int32_t K[MAXB];
     alias_build(n, w, tot, U, K);
     return alias_draw(rs, n, U, K);
 }
@@ -1005,6 +1005,48 @@ static void gen_heat_bath(const oracle_ctx *c, rstream *rs, const uint64_t *f, c
     *hmatel_out = allowed ? hmatel : 0.0;
 }
 
+/* slater_condon1_mol (src/hamiltonian_molecular.f90:140-196) with perm = false:
+ * 0 unless i and a share spin and symmetry. */
+static double sc1_mol_checked(const oracle_ctx *c, const int *occ, int i, int a) {
+    if (c->orb_sym[i] != c->orb_sym[a] || c->orb_ms[i] != c->orb_ms[a]) return 0.0;
+    return sc1_mol_excit(c, occ, i, a, 0);
+}
+
+/* find_ia_single_weights (src/excit_gen_utils.f90:169-212) and
+ * gen_single_excit_heat_bath_exact (src/excit_gen_heat_bath_mol.F90:732-807):
+ * i chosen with weight sum_a |H_ia|, then a with weight |H_ia|. */
+static void gen_single_heat_bath_exact(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d,
+                                       attempt_t *out, double *pgen_out, double *hmatel_out) {
+    int nel = c->nel, nvirt = c->nvirt;
+    int unocc[MAXB], nu = 0;
+    for (int p = 0; p < c->nbasis; p++)
+        if (!tbit(f, p)) unocc[nu++] = p;
+    double wi[MAXEL], row[MAXB], tot = 0.0;
+    for (int ii = 0; ii < nel; ii++) {
+        wi[ii] = 0.0;
+        for (int aa = 0; aa < nvirt; aa++) wi[ii] = wi[ii] + fabs(sc1_mol_checked(c, d->occ, d->occ[ii], unocc[aa]));
+        tot = tot + wi[ii];
+    }
+    out->e.nexcit = 1;
+    if (tot < DEPSILON) {
+        out->allowed = 0;
+        *pgen_out = 1.0;
+        *hmatel_out = 0.0;
+        return;
+    }
+    int i_ind = alias_select(rs, nel, wi, tot);
+    int i = d->occ[i_ind];
+    for (int aa = 0; aa < nvirt; aa++) row[aa] = fabs(sc1_mol_checked(c, d->occ, i, unocc[aa]));
+    int a_ind = alias_select(rs, nvirt, row, wi[i_ind]);
+    int a = unocc[a_ind];
+    out->allowed = 1;
+    out->e.from[0] = i;
+    out->e.to[0] = a;
+    *pgen_out = c->pattempt_single * (wi[i_ind] / tot) * (row[a_ind] / wi[i_ind]);
+    out->e.perm = perm1(c, f, i, a);
+    *hmatel_out = sc1_mol_excit(c, d->occ, i, a, out->e.perm);
+}
+
 /* gen_excit_mol_heat_bath_uniform, double branch
  * (src/excit_gen_heat_bath_mol.F90:619-705). */
 static void gen_heat_bath_uniform_double(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d,
@@ -1060,11 +1102,16 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
     memset(out, 0, sizeof(*out));
     out->e.from[0] = out->e.from[1] = out->e.to[0] = out->e.to[1] = -1;
     int gen = c->cfg.excit_gen;
-    /* gen_excit_mol_heat_bath_uniform takes its singles from gen_single_excit_mol */
+    /* gen_excit_mol_heat_bath_uniform takes its singles from gen_single_excit_mol
+     * (heat_bath_uniform) or gen_single_excit_heat_bath_exact (heat_bath_single) */
     int renorm = gen == HGPU_EXCIT_GEN_RENORM || gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM;
     double pgen, hmatel;
     if (gen == HGPU_EXCIT_GEN_HEAT_BATH) {
         gen_heat_bath(c, rs, f, d, out, &pgen, &hmatel);
+    } else if (gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE && rs_next(rs) < c->pattempt_single) {
+        gen_single_heat_bath_exact(c, rs, f, d, out, &pgen, &hmatel);
+    } else if (gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE) {
+        gen_heat_bath_uniform_double(c, rs, f, d, out, &pgen, &hmatel);
     } else if (rs_next(rs) < c->pattempt_single) {
         int i = -1, a = -1, ok;
         out->e.nexcit = 1;
@@ -1711,7 +1758,8 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
         }
     }
     if (c->kind == HGPU_SYS_READ_IN &&
-        (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM)) {
+        (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM ||
+         cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE)) {
         if (init_heat_bath(c, cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH) != 0) {
             oracle_destroy(c);
             return NULL;

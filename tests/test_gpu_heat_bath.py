@@ -35,7 +35,7 @@ def hb_sys(name):
 
 
 @pytest.mark.parametrize("name", list(HB_SYS))
-@pytest.mark.parametrize("gen", ["heat_bath", "heat_bath_uniform"])
+@pytest.mark.parametrize("gen", ["heat_bath", "heat_bath_uniform", "heat_bath_single"])
 def test_eval_heat_bath(name, gen):
     s = hb_sys(name)
     rng = np.random.default_rng(21)
@@ -57,11 +57,13 @@ def test_eval_heat_bath(name, gen):
 
 
 HB_RUNS = [
-    ("mol12", dict(tau=2e-3, init_pop=500, target_population=5000, real_amplitudes=True, excit_gen="heat_bath"), 6),
+    ("mol12", dict(tau=2e-3, init_pop=500, target_population=5000, real_amplitudes=True, excit_gen="heat_bath"), 5),
     ("mol12", dict(tau=2e-3, init_pop=500, target_population=5000, real_amplitudes=True,
                    excit_gen="heat_bath_uniform", pattempt_single=0.2, pattempt_double=0.8), 6),
     ("mol12", dict(tau=2e-3, init_pop=500, target_population=5000, real_amplitudes=True, excit_gen="heat_bath",
                    initiator=True), 6),
+    ("mol12", dict(tau=2e-3, init_pop=500, target_population=5000, real_amplitudes=True,
+                   excit_gen="heat_bath_single", pattempt_single=0.2, pattempt_double=0.8), 5),
     ("h2o_sto2g", dict(tau=0.01, init_pop=100, target_population=300, excit_gen="heat_bath", initial_shift=3.0), 8),
     ("mol34_w2", dict(tau=5e-4, init_pop=1000, target_population=20000, real_amplitudes=True,
                       excit_gen="heat_bath", initiator=True), 3),
@@ -99,7 +101,7 @@ MIXED_RTOL_PGEN = 2e-5
 MIXED_RTOL_H, MIXED_ATOL_H = 1e-4, 1e-6
 
 
-@pytest.mark.parametrize("gen", ["heat_bath", "heat_bath_uniform"])
+@pytest.mark.parametrize("gen", ["heat_bath", "heat_bath_uniform", "heat_bath_single"])
 def test_mixed_precision_heat_bath(gen):
     """FP32 heat-bath path against the FP64 oracle: where the same excitation is
     drawn (a draw can fall on the other side of an alias threshold that moved by

@@ -25,7 +25,7 @@ def _sample(s, gen, parent, n, seed=11):
     return orbs, pg, al
 
 
-@pytest.mark.parametrize("gen", ["heat_bath", "heat_bath_uniform"])
+@pytest.mark.parametrize("gen", ["heat_bath", "heat_bath_uniform", "heat_bath_single"])
 def test_heat_bath_pgen_matches_sampling(gen):
     s = systems.synthetic_molecule(6, 4, seed=3)
     rng = np.random.default_rng(5)

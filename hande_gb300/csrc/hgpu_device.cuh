@@ -435,6 +435,32 @@ __device__ __forceinline__ FxTabs stage_fx(const DevSys &s, int64_t *dst) {
     return FxTabs{dst, dst + M, nullptr};
 }
 
+__device__ __forceinline__ int low_bit(uint32_t x) { return __ffs((int)x) - 1; }
+__device__ __forceinline__ int low_bit(uint64_t x) { return __ffsll((long long)x) - 1; }
+
+// One-electron and pair terms of the exact diagonal for alpha and beta
+// spatial occupation masks.
+template <typename Mask>
+__device__ __forceinline__ int64_t fx_pair_sum(const FxTabs &tb, int M, Mask am, Mask bm) {
+    int64_t e = 0;
+    const int64_t *same_tab = tb.pair + (size_t)M * M;
+    for (Mask x = am; x; x &= x - 1) {
+        const int p = low_bit(x);
+        e += tb.h1[p];
+        const int64_t *opp = tb.pair + (size_t)p * M;
+        const int64_t *same = same_tab + (size_t)p * M;
+        for (Mask y = x & (x - 1); y; y &= y - 1) e += same[low_bit(y)];  // alpha partners above p
+        for (Mask y = bm; y; y &= y - 1) e += opp[low_bit(y)];             // every beta partner
+    }
+    for (Mask x = bm; x; x &= x - 1) {
+        const int p = low_bit(x);
+        e += tb.h1[p];
+        const int64_t *same = same_tab + (size_t)p * M;
+        for (Mask y = x & (x - 1); y; y &= y - 1) e += same[low_bit(y)];  // beta partners above p
+    }
+    return e;
+}
+
 template <int W>
 __device__ int64_t fx_energy(const DevSys &s, const Det<W> &f, const FxTabs &tb) {
     int64_t e = s.fx_const;
@@ -453,7 +479,8 @@ __device__ int64_t fx_energy(const DevSys &s, const Det<W> &f, const FxTabs &tb)
     // Spin-resolved spatial occupations: every term is an integer, so the
     // pairs may be summed in any order -- alpha-alpha and beta-beta pairs from
     // the same-spin table, every alpha-beta pair (a doubly occupied orbital
-    // included) from the opposite-spin table.
+    // included) from the opposite-spin table.  One determinant word holds at
+    // most 32 spatial orbitals, whose masks are then 32-bit words.
     const int M = s.norb;
     uint64_t am = 0, bm = 0;
 #pragma unroll
@@ -461,24 +488,8 @@ __device__ int64_t fx_energy(const DevSys &s, const Det<W> &f, const FxTabs &tb)
         am |= unzip_even(f.w[k]) << (32 * k);
         bm |= unzip_even(f.w[k] >> 1) << (32 * k);
     }
-    const int64_t *same_tab = tb.pair + (size_t)M * M;
-    for (uint64_t x = am; x;) {
-        int p = __ffsll((long long)x) - 1;
-        x &= x - 1;
-        e += tb.h1[p];
-        const int64_t *opp = tb.pair + (size_t)p * M;
-        const int64_t *same = same_tab + (size_t)p * M;
-        for (uint64_t y = x; y; y &= y - 1) e += same[__ffsll((long long)y) - 1];  // alpha partners above p
-        for (uint64_t y = bm; y; y &= y - 1) e += opp[__ffsll((long long)y) - 1];  // every beta partner
-    }
-    for (uint64_t x = bm; x;) {
-        int p = __ffsll((long long)x) - 1;
-        x &= x - 1;
-        e += tb.h1[p];
-        const int64_t *same = same_tab + (size_t)p * M;
-        for (uint64_t y = x; y; y &= y - 1) e += same[__ffsll((long long)y) - 1];  // beta partners above p
-    }
-    return e;
+    if (W == 1) return e + fx_pair_sum<uint32_t>(tb, M, (uint32_t)am, (uint32_t)bm);
+    return e + fx_pair_sum<uint64_t>(tb, M, am, bm);
 }
 
 template <int W>

@@ -495,22 +495,14 @@ static int alloc_lists(hgpu_handle *h) {
         CK(cudaMemset(b.os_epoch, 0, sizeof(uint32_t)));
     }
     {
-        size_t tiles = (size_t)b.scap / kSegTile + 2;  // tiles of the self-annihilation
+        // tiles of the annihilation over the merged main and spawned lists
+        size_t tiles = ((size_t)b.cap + (size_t)b.scap) / kAnnTile + 2;
+        if ((rc = dalloc(h, &b.msplit, 3 * (tiles + 1)))) return rc;
         if ((rc = dalloc(h, &b.seg_status, tiles))) return rc;
         CK(cudaMemset(b.seg_status, 0, sizeof(uint64_t) * tiles));
         if ((rc = dalloc(h, &b.seg_epoch, 1))) return rc;
         CK(cudaMemset(b.seg_epoch, 0, sizeof(uint32_t)));
     }
-    if ((rc = dalloc(h, &b.udets, (size_t)b.scap * W))) return rc;
-    if ((rc = dalloc(h, &b.upops, (size_t)b.scap * R))) return rc;
-    if ((rc = dalloc(h, &b.uflag, (size_t)b.scap))) return rc;
-    if ((rc = dalloc(h, &b.ukii, (size_t)b.scap))) return rc;
-    if ((rc = dalloc(h, &b.msplit, ((size_t)b.cap + (size_t)b.scap) / kMergeTile + 2))) return rc;
-    size_t merged = (size_t)b.cap + (size_t)b.scap;
-    if ((rc = dalloc(h, &b.mref, merged))) return rc;
-    if ((rc = dalloc(h, &b.mkeep, merged))) return rc;
-    if ((rc = dalloc(h, &b.tile_cnt, merged / kMergeTile + 2))) return rc;
-    if ((rc = dalloc(h, &b.tile_base, merged / kMergeTile + 2))) return rc;
     if ((rc = dalloc(h, &b.scan_part, (size_t)kMaxBlocks * 2))) return rc;
     if ((rc = dalloc(h, &b.part_d, (size_t)kMaxBlocks * 4))) return rc;
     if ((rc = dalloc(h, &b.part_i, (size_t)kMaxBlocks * 4))) return rc;
@@ -523,6 +515,7 @@ static int alloc_lists(hgpu_handle *h) {
         b.grid = clampi(b.cap / 4096, 8, std::min(4 * sms, kMaxBlocks));
         b.spawn_grid = clampi(b.scap / 1024, 8, 8 * sms);
         b.sort_grid = clampi(b.scap / OSConf<1>::tile + 1, 4, 4 * sms);  // 256 threads, ~46 KB shared memory
+        b.splits_grid = clampi(((b.cap + b.scap) / kAnnTile + 3 + kBlock - 1) / kBlock, 1, b.grid);
     }
     if ((rc = dalloc(h, &b.state, 1))) return rc;
     CK(cudaMemset(b.state, 0, sizeof(DevState)));

@@ -12,116 +12,20 @@
 //   spawn           excitation generation + spawning, appended with
 //                   warp-aggregated atomics                          (spawning.F90:34/215)
 //   radix sort      stable LSD sort of the spawned determinants       (spawn_data.F90:406)
-//   seg_reduce      self-annihilation incl. the initiator flag rule   (spawn_data.F90:859/:937)
-//   merge_spawn     annihilate_main_list[_initiator] + rounding of new
-//   merge_main      remove_unoccupied_dets rounding                    (annihilation.f90:294-675)
-//   scan + scatter  insert_new_walkers as a stable merge of two sorted
-//                   lists, K_ii = sc0 - H00 for new determinants      (annihilation.f90:677-901)
+//   annihilation    one pass over the merge of the main list and the
+//                   sorted spawned list: self-annihilation incl. the
+//                   initiator flag rule, annihilate_main_list, both
+//                   roundings and insert_new_walkers with K_ii
+//                   (spawn_data.F90:859-1101, annihilation.f90:9-901;
+//                   hgpu_annihilate.cu)
 //   cycle_end       per-cycle statistics, report accumulators         (qmc_common.F90:1240)
 #include "hgpu_kernels.cuh"
 
 #include <cstdio>
 
+#include "hgpu_common.cuh"
+
 namespace hgpu {
-
-#define FULL_MASK 0xffffffffu
-
-__device__ __forceinline__ uint32_t lanemask_lt() {
-    uint32_t m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
-__device__ __forceinline__ uint2 operator+(uint2 a, uint2 b) { return make_uint2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ uint2 operator-(uint2 a, uint2 b) { return make_uint2(a.x - b.x, a.y - b.y); }
-
-template <typename T>
-__device__ __forceinline__ T zero_of();
-template <>
-__device__ __forceinline__ int64_t zero_of<int64_t>() { return 0; }
-template <>
-__device__ __forceinline__ uint2 zero_of<uint2>() { return make_uint2(0, 0); }
-template <>
-__device__ __forceinline__ uint32_t zero_of<uint32_t>() { return 0u; }
-
-template <typename T>
-__device__ __forceinline__ T shfl_up(T v, int d);
-template <>
-__device__ __forceinline__ int64_t shfl_up<int64_t>(int64_t v, int d) {
-    return __shfl_up_sync(FULL_MASK, (long long)v, d);
-}
-template <>
-__device__ __forceinline__ uint32_t shfl_up<uint32_t>(uint32_t v, int d) {
-    return __shfl_up_sync(FULL_MASK, v, d);
-}
-template <>
-__device__ __forceinline__ uint2 shfl_up<uint2>(uint2 v, int d) {
-    return make_uint2(__shfl_up_sync(FULL_MASK, v.x, d), __shfl_up_sync(FULL_MASK, v.y, d));
-}
-
-// Inclusive warp scan, then block scan through shared memory.  Returns the
-// exclusive prefix of v within the block and the block total in *tot.
-template <typename T>
-__device__ __forceinline__ T block_exclusive_scan(T v, T *tot) {
-    __shared__ T wsum[32];
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T x = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        T y = shfl_up<T>(x, d);
-        if (lane >= d) x = x + y;
-    }
-    if (lane == 31) wsum[warp] = x;
-    __syncthreads();
-    int nw = blockDim.x >> 5;
-    if (warp == 0) {
-        T w = lane < nw ? wsum[lane] : zero_of<T>();
-        T s = w;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            T y = shfl_up<T>(s, d);
-            if (lane >= d) s = s + y;
-        }
-        if (lane < nw) wsum[lane] = s;  // inclusive over warps
-    }
-    __syncthreads();
-    T before = warp > 0 ? wsum[warp - 1] : zero_of<T>();
-    *tot = wsum[nw - 1];
-    __syncthreads();
-    // exclusive = inclusive - v
-    return before + x - v;
-}
-
-__device__ __forceinline__ double shfl_down_any(double v, int d) { return __shfl_down_sync(FULL_MASK, v, d); }
-__device__ __forceinline__ uint32_t shfl_down_any(uint32_t v, int d) { return __shfl_down_sync(FULL_MASK, v, d); }
-__device__ __forceinline__ int64_t shfl_down_any(int64_t v, int d) {
-    return (int64_t)__shfl_down_sync(FULL_MASK, (long long)v, d);
-}
-
-template <typename T>
-__device__ __forceinline__ T block_reduce_sum(T v) {
-    __shared__ T red[32];
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v += shfl_down_any(v, d);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    int nw = blockDim.x >> 5;
-    T r = 0;
-    if (threadIdx.x == 0)
-        for (int k = 0; k < nw; k++) r += red[k];
-    __syncthreads();
-    return r;  // valid in thread 0
-}
-
-__device__ __forceinline__ void chunk_range(int64_t n, int64_t &begin, int64_t &end) {
-    int64_t G = gridDim.x;
-    int64_t chunk = (n + G - 1) / G;
-    chunk = (chunk + 255) & ~(int64_t)255;
-    begin = (int64_t)blockIdx.x * chunk;
-    end = begin + chunk < n ? begin + chunk : n;
-    if (begin > n) begin = n;
-}
 
 // ---------------------------------------------------------------------------
 // Device-wide exclusive scan, three phases over a fixed grid.
@@ -175,55 +79,6 @@ struct StoreInclusive {
 // n_ptr points at an int64 count; for N*R lists a small kernel writes the product.
 __global__ void k_set_count(int64_t *dst, const int64_t *a, int64_t mul, const int64_t *b) {
     *dst = *a * mul + (b ? *b : 0);
-}
-
-// ---------------------------------------------------------------------------
-// Shared-memory staging of the system
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void stage_sys(DevSys &dst, const DevSys *src) {
-    const uint32_t *s = reinterpret_cast<const uint32_t *>(src);
-    uint32_t *d = reinterpret_cast<uint32_t *>(&dst);
-    for (int k = threadIdx.x; k < (int)(sizeof(DevSys) / 4); k += blockDim.x) d[k] = s[k];
-}
-
-__device__ __forceinline__ HubTables stage_hub(const DevSys *src, uint8_t *smem) {
-    HubTables t;
-    int nk = src->nk;
-    t.nk = nk;
-    if (src->kind == HGPU_SYS_HUB_K) {
-        for (int k = threadIdx.x; k < nk * nk; k += blockDim.x) smem[k] = src->sym_table[k];
-        for (int k = threadIdx.x; k < nk; k += blockDim.x) smem[nk * nk + k] = src->inv_sym[k];
-    }
-    t.sym = smem;
-    t.inv = smem + nk * nk;
-    return t;
-}
-
-template <int W>
-__device__ __forceinline__ Det<W> load_det(const uint64_t *p, int64_t i) {
-    Det<W> d;
-#pragma unroll
-    for (int k = 0; k < W; k++) d.w[k] = p[i * W + k];
-    return d;
-}
-
-template <int W>
-__device__ __forceinline__ void store_det(uint64_t *p, int64_t i, const Det<W> &d) {
-#pragma unroll
-    for (int k = 0; k < W; k++) p[i * W + k] = d.w[k];
-}
-
-// first index in [0, n) whose determinant is not less than x
-template <int W>
-__device__ __forceinline__ int64_t lower_bound_det(const uint64_t *list, int64_t n, const Det<W> &x) {
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-        int64_t mid = (lo + hi) >> 1;
-        Det<W> m = load_det<W>(list, mid);
-        if (det_less<W>(m, x)) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
 }
 
 // ---------------------------------------------------------------------------
@@ -529,478 +384,6 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
     }
 }
 
-__global__ void k_clamp_spawns(DevState *st, int64_t scap) {
-    if (st->n_spawn > scap) {
-        st->n_spawn = scap;
-        st->error_flags |= HGPU_FLAG_SPAWN_OVERFLOW;
-    }
-}
-
-}  // namespace hgpu
-
-#include "hgpu_sort.cuh"
-
-namespace hgpu {
-
-// ---------------------------------------------------------------------------
-// Self-annihilation of the sorted spawned list
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int sgn3(int64_t x) { return x > 0 ? 1 : (x < 0 ? -1 : 0); }
-__device__ __forceinline__ int sgn1(int64_t x) { return x >= 0 ? 1 : -1; }
-// Fortran sign(1, int(x)): int() keeps the low 32 bits of an int64.
-__device__ __forceinline__ int sign1_int32(int64_t x) { return (int32_t)(uint32_t)(uint64_t)x >= 0 ? 1 : -1; }
-
-// annihilate_spawn_t[_initiator] (src/spawn_data.F90:859-1101) of the segment
-// of equal keys that starts at sorted position i: the summed populations and,
-// for the initiator approximation, the flag of spaces whose sum may not create a
-// new walker.  Sorted keys (KW words: the rank, or the determinant) are equal
-// exactly when the determinants are.
-template <int KW>
-__device__ __forceinline__ void reduce_segment(const DevBuffers &b, int R, const uint64_t *keys, const uint32_t *idx,
-                                               int64_t i, int64_t S, int initiator, int64_t sum[2], uint64_t &flag) {
-    Det<KW> ki = load_det<KW>(keys, i);
-    int64_t ip[2] = {0, 0}, ev[2] = {0, 0}, firstpop[2] = {0, 0};
-    sum[0] = sum[1] = 0;
-    uint64_t minord = ~0ull, firstflag = 0;
-    for (int64_t j = i; j < S; j++) {
-        if (j > i && !det_eq<KW>(load_det<KW>(keys, j), ki)) break;
-        uint32_t e = idx[j];
-        uint64_t fl = initiator ? b.sflag[e] : 0;
-        for (int q = 0; q < R; q++) {
-            int64_t p = b.spops[(int64_t)e * R + q];
-            sum[q] += p;
-            if (initiator) {
-                if (!((fl >> q) & 1)) ip[q] += p;
-                else ev[q] += sgn3(p);
-            }
-        }
-        if (initiator && (fl >> 2) < minord) {
-            minord = fl >> 2;
-            firstflag = fl;
-            for (int q = 0; q < R; q++) firstpop[q] = b.spops[(int64_t)e * R + q];
-        }
-    }
-    flag = 0;
-    if (initiator) {
-        // the first entry of a determinant counts sign(1, int(pop)) events
-        for (int q = 0; q < R; q++) {
-            if ((firstflag >> q) & 1) ev[q] += sign1_int32(firstpop[q]) - sgn3(firstpop[q]);
-            bool keep = (ip[q] != 0 && sgn1(sum[q]) == sgn1(ip[q])) || (ev[q] > 1 || ev[q] < -1);
-            if (!keep) flag |= 1ull << q;
-        }
-    }
-}
-
-// Resets of the self-annihilation: tile tickets, the unique count, the look-back epoch.
-__global__ void k_seg_begin(DevBuffers b) {
-    b.state->seg_ticket = 0;
-    b.state->n_uniq = 0;
-    *b.seg_epoch += 1;
-}
-
-// Self-annihilation of the sorted spawned list in one pass: tiles of kSegTile
-// sorted positions, taken in ticket order, each thread holding kSegRounds
-// consecutive positions; the heads of segments of equal keys sum their
-// segment, one block scan orders the surviving (non-zero) sums, the tile's
-// output offset comes from a decoupled look-back over the preceding tiles, and
-// every thread writes its survivors to the unique spawned list (udets, upops,
-// uflag) in sorted order.
-template <int W, int KW, bool RANK>
-__global__ void __launch_bounds__(kBlock) k_seg_fused(DevBuffers b, int R, const uint64_t *keys, const uint32_t *idx,
-                                                      int initiator) {
-    __shared__ uint32_t s_tile, s_base;
-    DevState *st = b.state;
-    const int64_t S = st->n_spawn;
-    const int64_t ntiles = (S + kSegTile - 1) / kSegTile;
-    const uint32_t epoch = os_epoch(*b.seg_epoch, 0);
-    uint64_t *status = b.seg_status;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&st->seg_ticket, 1u);
-        __syncthreads();
-        const int64_t tile = s_tile;
-        if (tile >= ntiles) break;
-        const int64_t p0 = tile * kSegTile + (int64_t)threadIdx.x * kSegRounds;
-        // keys of positions p0-1 .. p0+kSegRounds: heads and singleton segments
-        Det<KW> k[kSegRounds + 2];
-#pragma unroll
-        for (int r = 0; r < kSegRounds + 2; r++) {
-            int64_t i = p0 - 1 + r;
-            if (i >= 0 && i < S) k[r] = load_det<KW>(keys, i);
-        }
-        int64_t sum[kSegRounds][2];
-        uint64_t flag[kSegRounds];
-        uint32_t kept = 0, keepmask = 0;
-#pragma unroll
-        for (int r = 0; r < kSegRounds; r++) {
-            const int64_t i = p0 + r;
-            sum[r][0] = sum[r][1] = 0;
-            flag[r] = 0;
-            if (i >= S) continue;
-            bool head = i == 0 || !det_eq<KW>(k[r], k[r + 1]);
-            if (!head) continue;
-            bool single = i + 1 >= S || !det_eq<KW>(k[r + 1], k[r + 2]);
-            if (single && !initiator) {
-                // a segment of one entry: its populations
-                uint32_t e = idx[i];
-                for (int q = 0; q < R; q++) sum[r][q] = b.spops[(int64_t)e * R + q];
-            } else {
-                reduce_segment<KW>(b, R, keys, idx, i, S, initiator, sum[r], flag[r]);
-            }
-            if (sum[r][0] != 0 || (R > 1 && sum[r][1] != 0)) {
-                keepmask |= 1u << r;
-                kept++;
-            }
-        }
-        uint32_t run;
-        uint32_t ex = block_exclusive_scan<uint32_t>(kept, &run);
-        if (threadIdx.x == 0) {
-            // publish this tile's count, look back for its offset
-            volatile uint64_t *my = status + tile;
-            uint32_t excl = 0;
-            if (tile == 0) {
-                *my = os_word(kOSPrefix, epoch, run);
-            } else {
-                *my = os_word(kOSAggregate, epoch, run);
-                int64_t kk = tile - 1;
-                int spins = 0;
-                bool done = false;
-                while (!done) {
-                    uint64_t v[kOSLook];
-#pragma unroll
-                    for (int u = 0; u < kOSLook; u++)
-                        v[u] = kk - u >= 0 ? *(volatile uint64_t *)(status + (kk - u)) : 0;
-                    int u = 0;
-                    for (; u < kOSLook && kk - u >= 0; u++) {
-                        uint32_t ve = (uint32_t)(v[u] >> 32) & 0x3FFFFFFFu;
-                        uint64_t fl = v[u] >> 62;
-                        if (ve != (epoch & 0x3FFFFFFFu) || fl == 0) break;
-                        excl += (uint32_t)v[u];
-                        if (fl == kOSPrefix) {
-                            done = true;
-                            break;
-                        }
-                    }
-                    if (done) break;
-                    kk -= u;
-                    if (u == 0) {
-                        if (++spins > kSpinLimit) {
-                            atomicOr(&st->error_flags, HGPU_FLAG_TIMEOUT);
-                            break;
-                        }
-                        __nanosleep(32);
-                    }
-                }
-                *my = os_word(kOSPrefix, epoch, excl + run);
-            }
-            s_base = excl;
-            atomicAdd((unsigned long long *)&st->n_uniq, (unsigned long long)run);
-        }
-        __syncthreads();
-        int64_t u = (int64_t)s_base + ex;
-#pragma unroll
-        for (int r = 0; r < kSegRounds; r++) {
-            if (!((keepmask >> r) & 1u)) continue;
-            const int64_t i = p0 + r;
-            if (u < b.scap) {
-                Det<W> d;
-                if (RANK) {
-                    d = load_det<W>(b.sdets, idx[i]);
-                } else {
-#pragma unroll
-                    for (int w = 0; w < W; w++) d.w[w] = k[r + 1].w[w % KW];
-                }
-                store_det<W>(b.udets, u, d);
-                for (int q = 0; q < R; q++) b.upops[u * R + q] = sum[r][q];
-                b.uflag[u] = flag[r];
-            }
-            u++;
-        }
-        __syncthreads();
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Merge of the unique spawned list into the main list
-// ---------------------------------------------------------------------------
-// stochastic_round_int_64 (src/stoch_utils.f90:51-85) of one entry's pops.
-__device__ __forceinline__ void round_pops(const DevSys &s, int64_t *p, int R, uint32_t purpose, int64_t idx,
-                                           uint64_t iter) {
-    for (int q = 0; q < R; q++) {
-        int64_t v = p[q];
-        int64_t av = v < 0 ? -v : v;
-        if (av < s.real_factor && v != 0) {
-            RStream rs;
-            rs.init(s.seed, purpose, q, idx, 0, iter);
-            // (double)av > u * real_factor with real_factor = 2^31 and u = k 2^-53,
-            // both sides exact: av * 2^22 > k in integers
-            uint64_t k = rs.next_k();
-            p[q] = (((uint64_t)av << 22) > k) ? isign64(s.real_factor, v) : 0;
-        }
-    }
-}
-
-// Merge path (Odeh, Green, Mwassi, Shmueli, Birk, "Merge Path", 2012) of the
-// sorted main list and the sorted unique spawned list, equal determinants with
-// the main entry first: the number of main entries among the first d merged
-// elements, for every tile boundary d = t * kMergeTile.
-template <int W>
-__global__ void __launch_bounds__(kBlock) k_merge_splits(DevBuffers b, int cur) {
-    int64_t U = b.state->n_uniq, N = b.state->n_main, L = N + U;
-    int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
-    const uint64_t *mdets = b.dets[cur];
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t d = t * kMergeTile < L ? t * kMergeTile : L;
-        int64_t lo = d - U > 0 ? d - U : 0, hi = d < N ? d : N;
-        while (lo < hi) {
-            int64_t mid = (lo + hi) >> 1;
-            // main[mid] precedes spawn[d-1-mid] when main[mid] <= spawn[d-1-mid]
-            if (!det_less<W>(load_det<W>(b.udets, d - 1 - mid), load_det<W>(mdets, mid))) lo = mid + 1;
-            else hi = mid;
-        }
-        b.msplit[t] = lo;
-    }
-}
-
-// One tile of the merged sequence per iteration: annihilate_main_list[_initiator]
-// (src/annihilation.f90:294-486), remove_unoccupied_dets' rounding (:537-598),
-// round_low_population_spawns (:600-675), the merged rank of every element and,
-// densely over the tile's new determinants, their K_ii (insert_new_walker :855).
-// The merge itself: each thread takes kMergeTile/kBlock consecutive merged
-// positions, finds where they start by one merge-path search and walks them
-// with a sequential merge of the two sorted slices (main entry first among
-// equals), recording for each position which entry it holds and whether that
-// entry meets its equal in the other list; the entries are then processed with
-// consecutive threads on consecutive positions, so the global accesses coalesce.
-template <int W>
-__global__ void __launch_bounds__(kBlock) k_merge_tiles(DevBuffers b, int R, int cur) {
-    constexpr int PER = kMergeTile / kBlock;
-    constexpr uint32_t kSpawnBit = 1u << 31, kHitBit = 1u << 30, kIdxMask = kHitBit - 1;
-    __shared__ DevSys s;
-    __shared__ uint64_t tdet[kMergeTile * W];
-    __shared__ uint32_t desc[kMergeTile];     // per merged position: spawn bit, hit bit, slice index
-    __shared__ uint16_t newlist[kMergeTile];  // tile indices of new determinants
-    __shared__ int nnew;
-    extern __shared__ int64_t fx_smem[];  // exact-diagonal tables (fx_table_words)
-    stage_sys(s, b.sys);
-    __syncthreads();
-    const FxTabs tb = stage_fx(s, fx_smem);
-    __syncthreads();
-    int64_t U = b.state->n_uniq, N = b.state->n_main, L = N + U;
-    uint64_t iter = (uint64_t)b.state->iter;
-    int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
-    const uint64_t *mdets = b.dets[cur];
-    int64_t *mpops = b.pops[cur];
-    auto tile_det = [&](int k) {
-        Det<W> x;
-#pragma unroll
-        for (int w = 0; w < W; w++) x.w[w] = tdet[k * W + w];
-        return x;
-    };
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        int64_t d0 = t * kMergeTile, d1 = d0 + kMergeTile < L ? d0 + kMergeTile : L;
-        int64_t i0 = b.msplit[t], i1 = b.msplit[t + 1];
-        int64_t j0 = d0 - i0, j1 = d1 - i1;
-        int nm = (int)(i1 - i0), ns = (int)(j1 - j0);
-        for (int k = threadIdx.x; k < nm + ns; k += blockDim.x) {
-            Det<W> d = k < nm ? load_det<W>(mdets, i0 + k) : load_det<W>(b.udets, j0 + (k - nm));
-#pragma unroll
-            for (int w = 0; w < W; w++) tdet[k * W + w] = d.w[w];
-        }
-        if (threadIdx.x == 0) nnew = 0;
-        __syncthreads();
-        {
-            const int p0 = threadIdx.x * PER;
-            const int plen = min(PER, nm + ns - p0);
-            if (plen > 0) {
-                // main entries among the first p0 merged elements of the tile
-                int lo = max(0, p0 - ns), hi = min(p0, nm);
-                while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    if (!det_less<W>(tile_det(nm + p0 - 1 - mid), tile_det(mid))) lo = mid + 1;
-                    else hi = mid;
-                }
-                int a = lo, bb = p0 - lo;
-                for (int q = 0; q < plen; q++) {
-                    if (a < nm && (bb >= ns || !det_less<W>(tile_det(nm + bb), tile_det(a)))) {
-                        // main entry a meets the smallest spawned entry not below it
-                        bool hit;
-                        if (bb < ns) hit = det_eq<W>(tile_det(nm + bb), tile_det(a));
-                        else hit = j1 < U && det_eq<W>(load_det<W>(b.udets, j1), tile_det(a));
-                        desc[p0 + q] = (uint32_t)a | (hit ? kHitBit : 0u);
-                        a++;
-                    } else {
-                        // spawned entry bb meets the largest main entry not above it
-                        bool hit;
-                        if (a > 0) hit = det_eq<W>(tile_det(a - 1), tile_det(nm + bb));
-                        else hit = i0 > 0 && det_eq<W>(load_det<W>(mdets, i0 - 1), tile_det(nm + bb));
-                        desc[p0 + q] = kSpawnBit | (uint32_t)bb | (hit ? kHitBit : 0u);
-                        bb++;
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        uint32_t kept_main = 0, kept_any = 0;  // this thread's elements of the tile
-        for (int k = threadIdx.x; k < nm + ns; k += blockDim.x) {
-            const uint32_t dsc = desc[k];
-            const bool hit = (dsc & kHitBit) != 0;
-            const int64_t rank = d0 + k;
-            if (!(dsc & kSpawnBit)) {
-                int64_t i = i0 + (dsc & kIdxMask);
-                int64_t p[2] = {0, 0};
-                for (int q = 0; q < R; q++) p[q] = mpops[i * R + q];
-                if (hit) {
-                    // the equal spawned entry is the first not below i in the spawned list
-                    int64_t j = j0 + (k - (int64_t)(dsc & kIdxMask));
-                    uint64_t fl = b.uflag[j];
-                    for (int q = 0; q < R; q++) {
-                        int64_t sp = b.upops[j * R + q];
-                        if (!s.initiator || p[q] != 0) p[q] += sp;
-                        else if (!((fl >> q) & 1)) p[q] = sp;
-                    }
-                }
-                if (s.real_amplitudes) round_pops(s, p, R, P_ROUND_MAIN, i, iter);
-                bool nz = false;
-                for (int q = 0; q < R; q++) {
-                    mpops[i * R + q] = p[q];
-                    nz = nz || p[q] != 0;
-                }
-                b.mref[rank] = i;
-                b.mkeep[rank] = make_uint2(nz ? 1u : 0u, nz ? 1u : 0u);
-                kept_main += nz ? 1u : 0u;
-                kept_any += nz ? 1u : 0u;
-            } else {
-                int bb = (int)(dsc & kIdxMask);
-                int64_t j = j0 + bb;
-                uint32_t keep = 0;
-                if (!hit) {
-                    int64_t sp[2] = {0, 0};
-                    for (int q = 0; q < R; q++) sp[q] = b.upops[j * R + q];
-                    bool discard = false;
-                    if (s.initiator) {
-                        uint64_t fl = b.uflag[j];
-                        discard = true;
-                        for (int q = 0; q < R; q++) {
-                            if ((fl >> q) & 1) sp[q] = 0;
-                            else discard = false;
-                        }
-                    }
-                    if (!discard && s.real_amplitudes) round_pops(s, sp, R, P_ROUND_SPAWN, j, iter);
-                    bool nz = false;
-                    for (int q = 0; q < R; q++) {
-                        b.upops[j * R + q] = sp[q];
-                        nz = nz || sp[q] != 0;
-                    }
-                    keep = discard ? 0u : (s.real_amplitudes ? (nz ? 1u : 0u) : 1u);
-                    if (keep) newlist[atomicAdd(&nnew, 1)] = (uint16_t)(nm + bb);
-                }
-                b.mref[rank] = -(j + 1);
-                b.mkeep[rank] = make_uint2(0u, keep);
-                kept_any += keep;
-            }
-        }
-        // kept counts of the tile, for the tile-level scan of output positions
-        uint32_t tm = block_reduce_sum<uint32_t>(kept_main);
-        uint32_t ta = block_reduce_sum<uint32_t>(kept_any);
-        if (threadIdx.x == 0) b.tile_cnt[t] = make_uint2(tm, ta);
-        __syncthreads();
-        // K_ii of the tile's new determinants, one dense pass
-        int n_new = nnew;
-        for (int k = threadIdx.x; k < n_new; k += blockDim.x) {
-            int e = newlist[k];
-            b.ukii[j0 + (e - nm)] = kii_of<W>(s, tile_det(e), tb);
-        }
-        __syncthreads();
-    }
-}
-
-// Exclusive scan of the per-tile kept counts (kept main, kept any) into the
-// tiles' output offsets; the totals go to n_merged_keep.
-__global__ void __launch_bounds__(1024) k_merge_tile_scan(DevBuffers b) {
-    const int64_t L = b.state->n_main + b.state->n_uniq;
-    const int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
-    __shared__ uint2 carry;
-    if (threadIdx.x == 0) carry = make_uint2(0u, 0u);
-    __syncthreads();
-    for (int64_t t0 = 0; t0 < ntiles; t0 += blockDim.x) {
-        int64_t t = t0 + threadIdx.x;
-        uint2 v = t < ntiles ? b.tile_cnt[t] : make_uint2(0u, 0u);
-        uint2 tot;
-        uint2 ex = block_exclusive_scan<uint2>(v, &tot);
-        uint2 c = carry;
-        if (t < ntiles) b.tile_base[t] = ex + c;
-        __syncthreads();
-        if (threadIdx.x == 0) carry = c + tot;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *reinterpret_cast<uint2 *>(&b.state->n_merged_keep) = carry;
-}
-
-// The survivors of each merge tile, in merged order, written contiguously from
-// the tile's output offset (insert_new_walkers' compaction,
-// src/annihilation.f90:677-818).  With more survivors than the list holds,
-// only the main-list survivors are kept (the overflow is flagged).
-template <int W>
-__global__ void __launch_bounds__(kBlock) k_merge_scatter(DevBuffers b, int R, int cur) {
-    int64_t U = b.state->n_uniq, N = b.state->n_main, L = U + N;
-    const int64_t ntiles = (L + kMergeTile - 1) / kMergeTile;
-    uint2 tot = *reinterpret_cast<const uint2 *>(&b.state->n_merged_keep);
-    bool overflow = (int64_t)tot.y > b.cap;
-    const uint64_t *mdets = b.dets[cur];
-    const int64_t *mpops = b.pops[cur];
-    const double *mkii = b.kii[cur];
-    uint64_t *odets = b.dets[1 - cur];
-    int64_t *opops = b.pops[1 - cur];
-    double *okii = b.kii[1 - cur];
-    int64_t ap0 = 0, ap1 = 0;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int64_t d0 = t * kMergeTile, d1 = min(d0 + kMergeTile, L);
-        const uint2 base = b.tile_base[t];
-        int64_t run = overflow ? (int64_t)base.x : (int64_t)base.y;
-        for (int64_t r0 = d0; r0 < d1; r0 += blockDim.x) {
-            int64_t r = r0 + threadIdx.x;
-            uint2 k = r < d1 ? b.mkeep[r] : make_uint2(0u, 0u);
-            uint32_t keep = overflow ? k.x : k.y;
-            // the survivor's data is loaded before the scan of positions, which
-            // hides the loads' latency
-            Det<W> det;
-            int64_t p[2] = {0, 0};
-            double kii = 0.0;
-            if (keep) {
-                int64_t ref = b.mref[r];
-                if (ref >= 0) {
-                    det = load_det<W>(mdets, ref);
-                    for (int q = 0; q < R; q++) p[q] = mpops[ref * R + q];
-                    kii = mkii[ref];
-                } else {
-                    int64_t j = -ref - 1;
-                    det = load_det<W>(b.udets, j);
-                    for (int q = 0; q < R; q++) p[q] = b.upops[j * R + q];
-                    kii = b.ukii[j];  // K_ii from the merge tiles (insert_new_walker)
-                }
-            }
-            int64_t ktot;
-            int64_t ex = block_exclusive_scan<int64_t>((int64_t)keep, &ktot);
-            if (keep) {
-                int64_t dst = run + ex;
-                if (dst < b.cap) {
-                    store_det<W>(odets, dst, det);
-                    for (int q = 0; q < R; q++) opops[dst * R + q] = p[q];
-                    okii[dst] = kii;
-                    ap0 += p[0] < 0 ? -p[0] : p[0];
-                    ap1 += p[1] < 0 ? -p[1] : p[1];
-                }
-            }
-            run += ktot;
-        }
-    }
-    int64_t r0 = block_reduce_sum<int64_t>(ap0);
-    int64_t r1 = block_reduce_sum<int64_t>(ap1);
-    if (threadIdx.x == 0) {
-        b.part_i[blockIdx.x * 4 + 0] = r0;
-        b.part_i[blockIdx.x * 4 + 1] = r1;
-    }
-}
 
 // Neumaier-compensated accumulation.
 __device__ __forceinline__ void comp_add(double &sum, double &c, double x) {
@@ -1160,41 +543,6 @@ static void device_scan(const DevBuffers &b, Load load, Store store, const int64
     k_scan_down<T, Load, Store><<<b.grid, kBlock, 0, st>>>(load, store, n_ptr, part);
 }
 
-template <int W>
-static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st, const PhaseMarks *pm = nullptr) {
-    DevState *S = b.state;
-    int initiator_flagged = b.sflag != nullptr;
-    k_clamp_spawns<<<1, 1, 0, st>>>(S, b.scap);
-    // radix sort (hgpu_sort.cuh): pass 0 reads the ranks, or the spawned list itself
-    const int nel = b.sort_nel, nbasis = b.sort_nbasis;
-    const size_t hist_smem = sizeof(uint32_t) * kMaxPasses * kRadix +
-                             (b.use_rank ? sizeof(uint64_t) * (size_t)(nel + 1) * nbasis : 0);
-    if (b.use_rank) k_sort_hist<W, 1, true><<<b.grid, kBlock, hist_smem, st>>>(b, nel, nbasis);
-    else k_sort_hist<W, W, false><<<b.grid, kBlock, hist_smem, st>>>(b, nel, nbasis);
-    k_sort_offsets<<<1, kRadix, 0, st>>>(b);
-    const uint64_t *kin = b.use_rank ? b.skeys : b.sdets;
-    const uint32_t *iin = nullptr;
-    int o = 0;
-    for (int p = 0; p < b.sort_passes; p++) {
-        if (b.key_words == 1)
-            k_onesweep<1><<<b.sort_grid, kOSThreads, OSConf<1>::smem, st>>>(b, p, kin, iin, b.keys[o], b.idx[o]);
-        else
-            k_onesweep<2><<<b.sort_grid, kOSThreads, OSConf<2>::smem, st>>>(b, p, kin, iin, b.keys[o], b.idx[o]);
-        kin = b.keys[o];
-        iin = b.idx[o];
-        o ^= 1;
-    }
-    if (pm) cudaEventRecord(pm->ev[4], st);
-    k_seg_begin<<<1, 1, 0, st>>>(b);
-    if (b.use_rank) k_seg_fused<W, 1, true><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
-    else k_seg_fused<W, W, false><<<b.grid, kBlock, 0, st>>>(b, R, kin, iin, initiator_flagged);
-    if (pm) cudaEventRecord(pm->ev[5], st);
-    k_merge_splits<W><<<b.grid, kBlock, 0, st>>>(b, cur);
-    k_merge_tiles<W><<<b.grid, kBlock, b.fx_smem_bytes, st>>>(b, R, cur);
-    k_merge_tile_scan<<<1, 1024, 0, st>>>(b);
-    k_merge_scatter<W><<<b.grid, kBlock, 0, st>>>(b, R, cur);
-    if (pm) cudaEventRecord(pm->ev[6], st);
-}
 
 template <int W>
 static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur, cudaStream_t st,
@@ -1223,7 +571,7 @@ static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur
     else HGPU_SPAWN(HGPU_SYS_READ_IN);
 #undef HGPU_SPAWN
     if (pm) cudaEventRecord(pm->ev[3], st);
-    annihilation_w<W>(b, R, cur, st, pm);
+    launch_sort_annihilate(b, W, R, cur, st, pm);
     k_cycle_end<<<1, 1024, 0, st>>>(b, R, b.grid, 1);
     if (pm) cudaEventRecord(pm->ev[7], st);
 }
@@ -1242,33 +590,19 @@ int set_kernel_attributes(const DevBuffers &b) {
         cudaFuncSetAttribute(k_spawn<2, HGPU_SYS_HUB_K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              hub_max) != cudaSuccess)
         return 1;
-    if (cudaFuncSetAttribute(k_onesweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OSConf<1>::smem) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(k_onesweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OSConf<2>::smem) !=
-            cudaSuccess)
-        return 1;
-    // The largest table any supported system needs (64 spatial orbitals), so
-    // that handles of different systems in one process never lower the limit
-    // another handle's captured graph relies on.
-    const int max_bytes = (int)sizeof(int64_t) * fx_table_words(HGPU_SYS_READ_IN, 128, 64);
-    if (b.fx_smem_bytes > (size_t)max_bytes) return 1;
-    cudaError_t e1 = cudaFuncSetAttribute(k_merge_tiles<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_bytes);
-    cudaError_t e2 = cudaFuncSetAttribute(k_merge_tiles<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_bytes);
-    return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : 1;
+    return set_annihilate_attributes(b);
 }
 
 int launches_per_cycle(const DevBuffers &b) {
     // begin, prep, count, scan(3), spawn, clamp, sort_hist, sort_offsets,
-    // one per pass, seg_begin, seg_fused, merge_splits, merge_tiles, tile_scan,
-    // scatter, end
-    return 2 + 1 + 3 + 1 + 1 + 2 + b.sort_passes + 2 + 2 + 1 + 1 + 1;
+    // one per pass, ann_splits, annihilate (twice), end
+    return 2 + 1 + 3 + 1 + 1 + 2 + b.sort_passes + 3 + 1;
 }
 
 void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st) {
     (void)kind;
     k_zero_parts<<<1, kBlock, 0, st>>>(b.part_i, b.grid);
-    if (W == 1) annihilation_w<1>(b, R, cur, st);
-    else annihilation_w<2>(b, R, cur, st);
+    launch_sort_annihilate(b, W, R, cur, st, nullptr);
     k_cycle_end<<<1, 1024, 0, st>>>(b, R, b.grid, 0);
 }
 

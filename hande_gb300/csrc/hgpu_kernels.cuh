@@ -30,9 +30,7 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortItems = 8;    // keys per thread per radix tile
 constexpr int kMaxBlocks = 1024; // upper bound of the fixed grid (partials arrays)
-constexpr int kMergeTile = 2048; // merged elements per tile of the merge-path kernel
-constexpr int kSegRounds = 4;    // sorted positions per thread of a self-annihilation tile
-constexpr int kSegTile = kBlock * kSegRounds;
+constexpr int kAnnTile = 2048;   // merged elements per annihilation tile (hgpu_annihilate.cuh)
 
 // Per-cycle counters and per-report accumulators, resident in device memory so
 // that a whole cycle runs without host synchronisation (and can be replayed
@@ -40,9 +38,9 @@ constexpr int kSegTile = kBlock * kSegRounds;
 struct DevState {
     int64_t n_main;        // N: occupied determinants
     int64_t n_spawn;       // S: spawned entries this cycle
-    int64_t n_uniq;        // U: entries after self-annihilation
+    int64_t n_uniq;        // U: spawned determinants with a non-zero summed population
     int64_t n_attempts;    // A: spawning attempts this cycle
-    int64_t n_merged_keep; // uint2 (kept main, kept total) after the merge
+    int64_t n_merged_keep; // uint2 (kept main, kept total) after the annihilation
     int64_t n_slots;       // N * nspaces
     int64_t iter;          // current iteration (cycle number, 1-based)
     double shift[HGPU_MAX_SPACES];
@@ -59,8 +57,7 @@ struct DevState {
     int32_t pad2;
     uint64_t spawn_next;  // next unclaimed attempt chunk of the spawning kernel
     uint32_t os_ticket[16];  // next tile of each radix pass (hgpu_sort.cuh)
-    uint32_t seg_ticket;     // next tile of the self-annihilation
-    uint32_t pad3;
+    uint32_t ann_ticket[2];  // next tile of each annihilation pass (hgpu_annihilate.cuh)
 };
 
 // Device buffers of one engine (all allocated once, at create).
@@ -95,19 +92,11 @@ struct DevBuffers {
     int sort_few_from;          // first pass whose digits take at most 32 values
     int sort_few_values[16];    // number of digit values of each such pass
     int sort_grid;      // blocks of the radix passes
-    // self-annihilated list (size scap)
-    uint64_t *seg_status;  // per self-annihilation tile: look-back status word
-    uint32_t *seg_epoch;   // look-back epoch of the self-annihilation (kept out of DevState)
-    uint64_t *udets;
-    int64_t *upops;
-    uint64_t *uflag;
-    double *ukii;       // K_ii of unique spawned determinants that become new walkers
-    // merge
-    int64_t *msplit;    // merge-path split (main index) at every tile boundary
-    int64_t *mref;      // per merged rank: >= 0 main index, < 0 -(j+1) unique spawn
-    uint2 *mkeep;       // per merged rank: (kept main, kept any)
-    uint2 *tile_cnt;    // per merge tile: (kept main, kept any)
-    uint2 *tile_base;   // exclusive scan of tile_cnt: output offset of each tile
+    // annihilation (hgpu_annihilate.cuh)
+    int64_t *msplit;       // per tile boundary: main index, spawned index, spawned index at the group boundary
+    uint64_t *seg_status;  // per annihilation tile: look-back status word
+    uint32_t *seg_epoch;   // look-back epoch of the annihilation (kept out of DevState)
+    int splits_grid;       // blocks of k_ann_splits
     // scan scratch and per-block partials
     int64_t *scan_part;     // kMaxBlocks * 2
     double *part_d;         // kMaxBlocks * 4 (proj, d0 per space)
@@ -117,13 +106,13 @@ struct DevBuffers {
     int grid;               // blocks of the streaming kernels
     int spawn_grid;         // blocks of the spawning kernel
     int sort_passes;
-    size_t fx_smem_bytes;  // dynamic shared memory of the merge tiles (exact-diagonal tables)
+    size_t fx_smem_bytes;  // exact-diagonal tables staged by the annihilation tiles
     int nk;                 // hub_k: number of k-points (shared-memory tables)
 };
 
 // Events recorded between the phases of a cycle in profiling mode:
 // 0 start, 1 after prep, 2 after attempt scan, 3 after spawn, 4 after sort,
-// 5 after self-annihilation, 6 after merge, 7 end.
+// 5 after the merge-path cuts, 6 after the annihilation, 7 end.
 constexpr int kNumMarks = 8;
 struct PhaseMarks {
     cudaEvent_t ev[kNumMarks];
@@ -137,6 +126,10 @@ int launches_per_cycle(const DevBuffers &b);
 // Kernel attributes that depend on the system (dynamic shared memory); 0 on success.
 int set_kernel_attributes(const DevBuffers &b);
 void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st);
+// Sort and annihilation of one cycle (hgpu_annihilate.cu), and the kernel
+// attributes they need; 0 on success.
+void launch_sort_annihilate(const DevBuffers &b, int W, int R, int cur, cudaStream_t st, const PhaseMarks *pm);
+int set_annihilate_attributes(const DevBuffers &b);
 void launch_eval_excitations(const DevBuffers &b, int W, int kind, int precision, const uint64_t *parents,
                              const int64_t *parent_pops, int64_t n, int64_t iteration, int32_t *orbs, double *pgen,
                              double *hmatel, int32_t *allowed, int64_t *nspawn, cudaStream_t st);

@@ -182,7 +182,7 @@ class Engine:
     def snapshot(self, restore: bool = False):
         self._check(self.L.hgpu_snapshot(self.h, 1 if restore else 0), "hgpu_snapshot")
 
-    PHASES = ["prep", "attempt_scan", "spawn", "sort", "self_annihilate", "merge", "end"]
+    PHASES = ["prep", "attempt_scan", "spawn", "sort", "splits", "annihilate", "end"]
 
     def profile_cycle(self):
         """One cycle with per-phase device times (ms) and list sizes."""

@@ -1519,7 +1519,8 @@ static void remove_unoccupied_dets(oracle_ctx *c) {
 }
 
 /* round_low_population_spawns (src/annihilation.f90:600-675); the rounding
- * stream of an entry is keyed by its index in the self-annihilated list. */
+ * stream of an entry is keyed by the position of its determinant's first entry
+ * in the sorted spawned list (the number of spawned entries below it). */
 static void round_low_population_spawns(oracle_ctx *c) {
     int64_t nrem = 0;
     for (int64_t i = 0; i < c->sn; i++) {
@@ -1573,10 +1574,13 @@ static void direct_annihilation(oracle_ctx *c) {
     int initiator = c->cfg.initiator_approx;
     if (c->sn > 0) {
         sort_spawns(c);
+        /* the rounding stream of a new determinant is keyed by the sorted
+         * position of its first spawned entry, which the self-annihilation
+         * carries along with the entry */
+        for (int64_t i = 0; i < c->sn; i++) c->suid[i] = i;
         if (initiator) annihilate_spawn_t_initiator(c);
         else annihilate_spawn_t(c);
     }
-    for (int64_t i = 0; i < c->sn; i++) c->suid[i] = i;
     if (c->sn >= 1) {
         annihilate_main_list(c, initiator);
         remove_unoccupied_dets(c);

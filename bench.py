@@ -481,23 +481,32 @@ def main():
     h2d = d2h = 0
     e_att = 0
     eng.end_report()
+    t_up = t_cyc = t_down = 0.0
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         n = n0  # every step starts from the same host walker list
+        ta = time.perf_counter()
         eng._check(L.hgpu_upload_walkers(eng.h, _p(hst, C.c_int64), _p(hpo, C.c_int64), _p(hda, C.c_double), n),
                    "upload")
         h2d += n * (8 * s.nwords + 8 + 8)
+        tb = time.perf_counter()
         eng.run_cycles(1)
+        tc = time.perf_counter()
         m = C.c_int64()
         eng._check(L.hgpu_download_walkers(eng.h, _p(ost, C.c_int64), _p(opo, C.c_int64), _p(oda, C.c_double),
                                            cap, C.byref(m)), "download")
         d2h += m.value * (8 * s.nwords + 8 + 8)
+        t_up += tb - ta
+        t_cyc += tc - tb
+        t_down += time.perf_counter() - tc
     e2e_s = time.perf_counter() - t0
     e_rep = eng.end_report()
     e_att = e_rep.nattempts
     e2e = {"value": e_att / e2e_s, "unit": "attempts/s", "h2d_bytes_per_step": h2d // args.e2e_steps,
            "d2h_bytes_per_step": d2h // args.e2e_steps,
-           "note": "per step: hgpu_upload_walkers from pinned host memory, one cycle, hgpu_download_walkers"}
+           "note": "per step: hgpu_upload_walkers from pinned host memory, one cycle, hgpu_download_walkers",
+           "host_ms_per_step": {"upload": 1e3 * t_up / args.e2e_steps, "cycle": 1e3 * t_cyc / args.e2e_steps,
+                                "download": 1e3 * t_down / args.e2e_steps}}
 
     batched = None
     if rank == 0 and not args.no_batched:

@@ -565,20 +565,26 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
     DevState *S = b.state;
     k_clamp_spawns<<<1, 1, 0, st>>>(S, b.scap);
     // radix sort (hgpu_sort.cuh): pass 0 reads the ranks, or the spawned list itself
-    const int nel = b.sort_nel, nbasis = b.sort_nbasis;
+    const int rows = b.binom_rows, cols = b.binom_cols;
     const size_t hist_smem = sizeof(uint32_t) * kMaxPasses * kRadix +
-                             (b.use_rank ? sizeof(uint64_t) * (size_t)(nel + 1) * nbasis : 0);
-    if (b.use_rank) k_sort_hist<W, 1, true><<<b.grid, kBlock, hist_smem, st>>>(b, nel, nbasis);
-    else k_sort_hist<W, W, false><<<b.grid, kBlock, hist_smem, st>>>(b, nel, nbasis);
+                             (b.use_rank ? sizeof(uint64_t) * (size_t)rows * cols : 0);
+    if (b.use_rank) k_sort_hist<W, 1, true><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    else k_sort_hist<W, W, false><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
     k_sort_offsets<<<1, kRadix, 0, st>>>(b);
     const uint64_t *kin = b.use_rank ? b.skeys : b.sdets;
     const uint32_t *iin = nullptr;
     int o = 0;
     for (int p = 0; p < b.sort_passes; p++) {
-        if (b.key_words == 1)
-            k_onesweep<1><<<b.sort_grid, kOSThreads, OSConf<1>::smem, st>>>(b, p, kin, iin, b.keys[o], b.idx[o]);
+        if (b.key32)
+            k_onesweep<uint32_t, 1><<<b.sort_grid, kOSThreads, OSConf<uint32_t, 1>::smem, st>>>(
+                b, p, reinterpret_cast<const uint32_t *>(kin), iin, reinterpret_cast<uint32_t *>(b.keys[o]),
+                b.idx[o]);
+        else if (b.key_words == 1)
+            k_onesweep<uint64_t, 1><<<b.sort_grid, kOSThreads, OSConf<uint64_t, 1>::smem, st>>>(
+                b, p, kin, iin, b.keys[o], b.idx[o]);
         else
-            k_onesweep<2><<<b.sort_grid, kOSThreads, OSConf<2>::smem, st>>>(b, p, kin, iin, b.keys[o], b.idx[o]);
+            k_onesweep<uint64_t, 2><<<b.sort_grid, kOSThreads, OSConf<uint64_t, 2>::smem, st>>>(
+                b, p, kin, iin, b.keys[o], b.idx[o]);
         kin = b.keys[o];
         iin = b.idx[o];
         o ^= 1;
@@ -607,10 +613,12 @@ void launch_sort_annihilate(const DevBuffers &b, int W, int R, int cur, cudaStre
 }
 
 int set_annihilate_attributes(const DevBuffers &b) {
-    if (cudaFuncSetAttribute(k_onesweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OSConf<1>::smem) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(k_onesweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OSConf<2>::smem) !=
-            cudaSuccess)
+    if (cudaFuncSetAttribute(k_onesweep<uint32_t, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)OSConf<uint32_t, 1>::smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_onesweep<uint64_t, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)OSConf<uint64_t, 1>::smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_onesweep<uint64_t, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)OSConf<uint64_t, 2>::smem) != cudaSuccess)
         return 1;
     // The largest table any supported system needs (64 spatial orbitals) with
     // two spaces and initiator flags, so that handles of different systems in

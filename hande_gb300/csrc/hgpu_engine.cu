@@ -409,26 +409,52 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
     return HGPU_OK;
 }
 
-// Binomial table C(p, k) (k = 0..nel, p = 0..nbasis-1, saturated at 2^64-1) of
-// the colexicographic rank; returns the bits of the largest rank, or 0 when
-// C(nbasis, nel) does not fit 64 bits (then the sort keys are the words).
-static int rank_bits(int nbasis, int nel, std::vector<uint64_t> &binom) {
-    const unsigned __int128 cap = ~(uint64_t)0;
-    std::vector<unsigned __int128> c((size_t)(nbasis + 1) * (nel + 1), 0);
-    auto C = [&](int p, int k) -> unsigned __int128 & { return c[(size_t)p * (nel + 1) + k]; };
-    for (int p = 0; p <= nbasis; p++) {
-        C(p, 0) = 1;
-        for (int k = 1; k <= nel && k <= p; k++) {
-            unsigned __int128 v = C(p - 1, k - 1) + (k <= p - 1 ? C(p - 1, k) : 0);
-            C(p, k) = v > cap ? cap : v;
+// Table of the spin-resolved rank of a determinant with na alpha and nb beta
+// electrons among M spatial orbitals (hgpu_sort.cuh, det_rank):
+// T[(ka (nb + 1) + kb) * 2M + p] = C((p + 1) / 2, ka) C(p / 2, kb) when that
+// table fits the shared memory of k_sort_hist (one load per electron), else
+// C(n, k) for k <= max(na, nb), n <= M (two loads and a product per electron).
+// Returns the bits of the largest rank, or 0 when C(M, na) C(M, nb) does not
+// fit 64 bits (then the sort keys are the determinant words).
+static int rank_bits(int M, int na, int nb, std::vector<uint64_t> &table, int &rows, int &cols, int &mode) {
+    typedef unsigned __int128 u128;
+    const u128 cap = ~(uint64_t)0;
+    const int kmax = std::max(na, nb);
+    if (na > M || nb > M || na < 0 || nb < 0) return 0;
+    std::vector<u128> c((size_t)(kmax + 1) * (M + 1), 0);
+    auto C = [&](int n, int k) -> u128 & { return c[(size_t)k * (M + 1) + n]; };
+    for (int n = 0; n <= M; n++) {
+        C(n, 0) = 1;
+        for (int k = 1; k <= kmax && k <= n; k++) {
+            u128 v = C(n - 1, k - 1) + (k <= n - 1 ? C(n - 1, k) : 0);
+            C(n, k) = v > cap ? cap : v;
         }
     }
-    unsigned __int128 total = C(nbasis, nel);
-    if (total >= cap) return 0;
-    if ((size_t)(nel + 1) * nbasis * sizeof(uint64_t) > 32768) return 0;  // shared-memory table of k_sort_hist
-    binom.assign((size_t)(nel + 1) * nbasis, 0);
-    for (int k = 0; k <= nel; k++)
-        for (int p = 0; p < nbasis; p++) binom[(size_t)k * nbasis + p] = (uint64_t)C(p, k);
+    const u128 ca = C(M, na), cb = C(M, nb);
+    if (ca >= cap || cb >= cap || (cb > 0 && ca > cap / cb)) return 0;
+    const u128 total = ca * cb;
+    if (total >= cap || total == 0) return 0;
+    const size_t limit = 32768 / sizeof(uint64_t);  // shared-memory table of k_sort_hist
+    const int nbasis = 2 * M;
+    if ((size_t)(na + 1) * (nb + 1) * nbasis <= limit) {
+        mode = 1;
+        rows = (na + 1) * (nb + 1);
+        cols = nbasis;
+        table.assign((size_t)rows * cols, 0);
+        for (int ka = 0; ka <= na; ka++)
+            for (int kb = 0; kb <= nb; kb++)
+                for (int p = 0; p < nbasis; p++)
+                    table[(size_t)(ka * (nb + 1) + kb) * cols + p] =
+                        (uint64_t)(C((p + 1) / 2, ka) * C(p / 2, kb));  // <= total: no overflow
+    } else if ((size_t)(kmax + 1) * (M + 1) <= limit) {
+        mode = 2;
+        rows = kmax + 1;
+        cols = M + 1;
+        table.assign((size_t)rows * cols, 0);
+        for (size_t k = 0; k < table.size(); k++) table[k] = (uint64_t)c[k];
+    } else {
+        return 0;
+    }
     uint64_t maxrank = (uint64_t)total - 1;
     int bits = 1;
     while (bits < 64 && (maxrank >> bits) != 0) bits++;
@@ -459,13 +485,17 @@ static int alloc_lists(hgpu_handle *h) {
         if ((rc = dalloc(h, &b.keys[k], (size_t)b.scap * W))) return rc;  // key_words <= W
         if ((rc = dalloc(h, &b.idx[k], (size_t)b.scap))) return rc;
     }
-    // sort: ranks (when the colexicographic rank fits 64 bits) or determinant words
+    // sort: ranks (when the spin-resolved rank fits 64 bits) or determinant words
     {
         std::vector<uint64_t> binom;
-        int bits = rank_bits(h->hsys.nbasis, h->hsys.nel, binom);
-        b.use_rank = bits > 0 ? 1 : 0;
-        b.sort_nel = h->hsys.nel;
-        b.sort_nbasis = h->hsys.nbasis;
+        int rows = 0, cols = 0, mode = 0;
+        int bits = rank_bits(h->hsys.nbasis / 2, h->hsys.nalpha, h->hsys.nbeta, binom, rows, cols, mode);
+        b.use_rank = bits > 0 ? mode : 0;
+        b.key32 = b.use_rank && bits <= 32 ? 1 : 0;
+        b.binom_rows = rows;
+        b.binom_cols = cols;
+        b.sort_na = h->hsys.nalpha;
+        b.sort_nb = h->hsys.nbeta;
         b.key_words = b.use_rank ? 1 : W;
         int key_bits = b.use_rank ? bits : h->hsys.nbasis;
         b.sort_passes = (key_bits + kRadixBits - 1) / kRadixBits;
@@ -488,7 +518,7 @@ static int alloc_lists(hgpu_handle *h) {
     if ((rc = dalloc(h, &b.gofs, (size_t)kMaxPasses * kRadix))) return rc;
     CK(cudaMemset(b.ghist, 0, sizeof(uint32_t) * kMaxPasses * kRadix));
     {
-        size_t tiles = (size_t)b.scap / OSConf<2>::tile + 2;
+        size_t tiles = (size_t)b.scap / OSConf<uint64_t, 2>::tile + 2;
         if ((rc = dalloc(h, &b.lookback, tiles * kRadix))) return rc;
         CK(cudaMemset(b.lookback, 0, sizeof(uint64_t) * tiles * kRadix));
         if ((rc = dalloc(h, &b.os_epoch, 1))) return rc;
@@ -514,8 +544,8 @@ static int alloc_lists(hgpu_handle *h) {
         const int sms = h->sms;
         b.grid = clampi(b.cap / 4096, 8, std::min(4 * sms, kMaxBlocks));
         b.spawn_grid = clampi(b.scap / 1024, 8, 8 * sms);
-        b.sort_grid = clampi(b.scap / OSConf<1>::tile + 1, 4, 4 * sms);  // 256 threads, ~46 KB shared memory
-        b.splits_grid = clampi(((b.cap + b.scap) / kAnnTile + 3 + kBlock - 1) / kBlock, 1, b.grid);
+        b.sort_grid = clampi(b.scap / OSConf<uint64_t, 1>::tile + 1, 4, 4 * sms);  // 256 threads, <= 48 KB shared memory
+        b.splits_grid = clampi(((b.cap + b.scap) / kAnnTile + 3 + 7) / 8, 1, 4 * sms);  // a warp per cut
     }
     if ((rc = dalloc(h, &b.state, 1))) return rc;
     CK(cudaMemset(b.state, 0, sizeof(DevState)));

@@ -150,7 +150,9 @@ __global__ void __launch_bounds__(kBlock) k_prep_parents(DevBuffers b, int R, in
     const double *kii = b.kii[cur];
     double proj[2] = {0.0, 0.0}, d0[2] = {0.0, 0.0};
     int64_t ndeath = 0;
-    double rf = (double)s.real_factor;
+    // 1 / real_factor is exact (real_factor is a power of two), so p * inv_rf
+    // is the quotient p / real_factor without an FP64 division
+    const double inv_rf = 1.0 / (double)s.real_factor;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         Det<W> f = load_det<W>(dets, i);
         Excit e = get_excitation<W>(f, f0, s.nel);
@@ -159,7 +161,7 @@ __global__ void __launch_bounds__(kBlock) k_prep_parents(DevBuffers b, int R, in
         uint32_t info = 0;
         for (int sp = 0; sp < R; sp++) {
             int64_t p = pops[i * R + sp];
-            double rp = (double)p / rf;
+            double rp = (double)p * inv_rf;
             // update_proj_energy
             if (e.nexcit == 0) d0[sp] += rp;
             else proj[sp] += h * rp;

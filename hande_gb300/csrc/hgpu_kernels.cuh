@@ -20,11 +20,12 @@ constexpr int kKindHeatBathUniform = 5;  // molecular, heat_bath_uniform
 // kMaxPasses passes, tiles of kOSThreads x items keys of KW words each.
 constexpr int kOSThreads = 256;  // one thread per digit value in the look-back
 constexpr int kMaxPasses = 16;
-template <int KW>
+template <typename K, int KW>
 struct OSConf {
-    static constexpr int items = KW == 1 ? 12 : 6;  // keys per thread (4 blocks of 256 fit an SM)
+    // keys per thread (4 blocks of 256 fit an SM)
+    static constexpr int items = sizeof(K) * KW <= 8 ? 12 : 6;
     static constexpr int tile = kOSThreads * items;
-    static constexpr size_t smem = (size_t)tile * (8 * KW + 4);  // staged keys + indices
+    static constexpr size_t smem = (size_t)tile * (sizeof(K) * KW + 4);  // staged keys + indices
 };
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
@@ -77,18 +78,21 @@ struct DevBuffers {
     uint64_t *sflag;    // initiator bits | generation order << 2
     int64_t scap;
     // sort (hgpu_sort.cuh)
-    uint64_t *skeys;    // colexicographic ranks of the spawned determinants (when use_rank)
-    uint64_t *keys[2];  // key_words per entry
+    uint64_t *skeys;    // ranks of the spawned determinants (when use_rank; 32-bit words when key32)
+    uint64_t *keys[2];  // key_words per entry (32-bit words when key32)
     uint32_t *idx[2];
     uint32_t *ghist;    // [kMaxPasses][kRadix] digit counts
     uint32_t *gofs;     // [kMaxPasses][kRadix] global digit offsets
     uint64_t *lookback; // [tiles][kRadix] look-back status words
     uint32_t *os_epoch;  // look-back epoch of the current sort (kept out of DevState,
                          // which the host rewrites, so that an epoch is never reused)
-    const uint64_t *binom;  // [nel+1][nbasis]: C(p, k) at k*nbasis + p
-    int use_rank;       // keys are ranks (one word); else the determinant words
+    const uint64_t *binom;  // rank table [binom_rows][binom_cols] (hgpu_sort.cuh, det_rank)
+    int use_rank;       // keys are ranks (one word; 1: one table load per electron, 2: two loads
+                        // and a product); 0: the keys are the determinant words
+    int key32;          // the ranks fit 32 bits: 32-bit keys
     int key_words;
-    int sort_nel, sort_nbasis;  // shape of the binomial table
+    int binom_rows, binom_cols;  // shape of the rank table
+    int sort_na, sort_nb;        // electrons of each spin of every determinant
     int sort_few_from;          // first pass whose digits take at most 32 values
     int sort_few_values[16];    // number of digit values of each such pass
     int sort_grid;      // blocks of the radix passes

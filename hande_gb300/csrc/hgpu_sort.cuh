@@ -40,6 +40,10 @@ template <int KW>
 __device__ __forceinline__ uint32_t os_digit(const uint64_t *k, int shift) {
     return (uint32_t)((k[shift >> 6] >> (shift & 63)) & (kRadix - 1));
 }
+template <int KW>
+__device__ __forceinline__ uint32_t os_digit(const uint32_t *k, int shift) {
+    return (k[shift >> 5] >> (shift & 31)) & (kRadix - 1);
+}
 
 // Lanes of `mask` whose 8-bit digit equals this lane's: one ballot per digit
 // bit (cheaper on this GPU than match.any).
@@ -53,19 +57,55 @@ __device__ __forceinline__ uint32_t warp_peers8(uint32_t mask, uint32_t d) {
     return peers;
 }
 
-// Colexicographic rank of a determinant; binom[k * nbasis + p] = C(p, k).
+// Spin-resolved rank of a determinant among those with na alpha (even) and nb
+// beta (odd) spin orbitals: the number of such determinants below it in the
+// list order (unsigned, last word most significant).  A smaller determinant
+// agrees above some occupied spin orbital p, leaves p empty and places below p
+// the ka alpha and kb beta electrons that the determinant holds at or below p:
+// C(alpha orbitals below p, ka) C(beta orbitals below p, kb) ways, summed over
+// p.  mode 1: tab[(ka (nb + 1) + kb) * cols + p] holds that product; mode 2:
+// tab[k * cols + n] = C(n, k).  A determinant with other electron counts sets
+// bad (its key is then 0).
 template <int W>
-__device__ __forceinline__ uint64_t det_rank(const Det<W> &f, const uint64_t *binom, int nbasis) {
+__device__ __forceinline__ uint64_t det_rank(const Det<W> &f, const uint64_t *tab, int cols, int mode, int na,
+                                             int nb, bool &bad) {
+    int ca = 0, cb = 0;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        ca += __popcll(f.w[w] & 0x5555555555555555ull);
+        cb += __popcll(f.w[w] & 0xAAAAAAAAAAAAAAAAull);
+    }
+    if (ca != na || cb != nb) {
+        bad = true;
+        return 0;
+    }
     uint64_t r = 0;
-    int k = 0;
+    if (mode == 1) {
+        // row (ka, kb) of the product table, advanced by one alpha or one beta row per electron
+        const uint64_t *row = tab;
+        const int sa = (nb + 1) * cols, sb = cols;
+#pragma unroll
+        for (int h = 0; h < 2 * W; h++) {
+            uint32_t x = (uint32_t)(f.w[h >> 1] >> (32 * (h & 1)));
+            while (x) {
+                const int p = 32 * h + __ffs((int)x) - 1;
+                x &= x - 1;
+                row += (p & 1) ? sb : sa;
+                r += row[p];
+            }
+        }
+        return r;
+    }
+    int ka = 0, kb = 0;
 #pragma unroll
     for (int w = 0; w < W; w++) {
         uint64_t x = f.w[w];
         while (x) {
-            int p = 64 * w + __ffsll((long long)x) - 1;
+            const int p = 64 * w + __ffsll((long long)x) - 1;
             x &= x - 1;
-            k++;
-            r += binom[k * nbasis + p];
+            if (p & 1) kb++;
+            else ka++;
+            r += tab[ka * cols + ((p + 1) >> 1)] * tab[kb * cols + (p >> 1)];
         }
     }
     return r;
@@ -74,44 +114,62 @@ __device__ __forceinline__ uint64_t det_rank(const Det<W> &f, const uint64_t *bi
 // Sort keys of the spawned list (ranks into b.skeys, when ranks are used) and
 // the digit histograms of every pass, added into b.ghist[pass][digit].
 template <int W, int KW, bool RANK>
-__global__ void __launch_bounds__(kBlock) k_sort_hist(DevBuffers b, int nel, int nbasis) {
+__global__ void __launch_bounds__(kBlock) k_sort_hist(DevBuffers b, int rows, int cols) {
     extern __shared__ uint64_t hist_smem[];
     uint32_t *h = reinterpret_cast<uint32_t *>(hist_smem);  // [passes][kRadix]
     uint64_t *binom = hist_smem + (kMaxPasses * kRadix) / 2;
     const int passes = b.sort_passes;
     for (int k = threadIdx.x; k < passes * kRadix; k += blockDim.x) h[k] = 0;
     if (RANK)
-        for (int k = threadIdx.x; k < (nel + 1) * nbasis; k += blockDim.x) binom[k] = b.binom[k];
+        for (int k = threadIdx.x; k < rows * cols; k += blockDim.x) binom[k] = b.binom[k];
     __syncthreads();
     const int64_t n = b.state->n_spawn;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        Det<W> f = load_det<W>(b.sdets, i);
-        uint64_t key[KW];
-        if (RANK) {
-            key[0] = det_rank<W>(f, binom, nbasis);
-            b.skeys[i] = key[0];
-        } else {
+    bool bad = false;
+    // kHistUnroll entries per thread and round, their loads issued together
+    // (the loop is otherwise bound by the latency of one load per thread)
+    constexpr int kHistUnroll = 4;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += stride * kHistUnroll) {
+        Det<W> fs[kHistUnroll];
 #pragma unroll
-            for (int w = 0; w < KW; w++) key[w] = f.w[w];
+        for (int r = 0; r < kHistUnroll; r++) {
+            const int64_t i = i0 + r * stride;
+            if (i < n) fs[r] = load_det<W>(b.sdets, i);
         }
-        // Digits of the top passes take few values (ranks are far below 2^64):
-        // those are counted with one ballot per value, the others with plain
-        // shared-memory atomics (spread over 256 counters)
-        const uint32_t active = __activemask();
-        const int lane = threadIdx.x & 31;
-        for (int p = 0; p < passes; p++) {
-            uint32_t dd = os_digit<KW>(key, p * kRadixBits);
-            const int nv = p < b.sort_few_from ? kRadix : b.sort_few_values[p];
-            if (nv > 32) {
-                atomicAdd(&h[p * kRadix + dd], 1u);
+#pragma unroll
+        for (int r = 0; r < kHistUnroll; r++) {
+            const int64_t i = i0 + r * stride;
+            if (i >= n) break;
+            const Det<W> &f = fs[r];
+            uint64_t key[KW];
+            if (RANK) {
+                key[0] = det_rank<W>(f, binom, cols, b.use_rank, b.sort_na, b.sort_nb, bad);
+                if (b.key32) reinterpret_cast<uint32_t *>(b.skeys)[i] = (uint32_t)key[0];
+                else b.skeys[i] = key[0];
             } else {
-                for (int v = 0; v < nv; v++) {
-                    uint32_t c = __popc(__ballot_sync(active, dd == (uint32_t)v));
-                    if (lane == __ffs(active) - 1 && c) atomicAdd(&h[p * kRadix + v], c);
+#pragma unroll
+                for (int w = 0; w < KW; w++) key[w] = f.w[w];
+            }
+            // Digits of the top passes take few values (ranks are far below 2^64):
+            // those are counted with one ballot per value, the others with plain
+            // shared-memory atomics (spread over 256 counters)
+            const uint32_t active = __activemask();
+            const int lane = threadIdx.x & 31;
+            for (int p = 0; p < passes; p++) {
+                uint32_t dd = os_digit<KW>(key, p * kRadixBits);
+                const int nv = p < b.sort_few_from ? kRadix : b.sort_few_values[p];
+                if (nv > 32) {
+                    atomicAdd(&h[p * kRadix + dd], 1u);
+                } else {
+                    for (int v = 0; v < nv; v++) {
+                        uint32_t c = __popc(__ballot_sync(active, dd == (uint32_t)v));
+                        if (lane == __ffs(active) - 1 && c) atomicAdd(&h[p * kRadix + v], c);
+                    }
                 }
             }
         }
     }
+    if (bad) atomicOr(&b.state->error_flags, HGPU_FLAG_BAD_DET);
     __syncthreads();
     for (int k = threadIdx.x; k < passes * kRadix; k += blockDim.x)
         if (h[k]) atomicAdd(&b.ghist[k], h[k]);
@@ -132,18 +190,17 @@ __global__ void __launch_bounds__(kRadix) k_sort_offsets(DevBuffers b) {
     if (threadIdx.x == 0) *b.os_epoch += (uint32_t)kMaxPasses;
 }
 
-// One stable pass on digit `pass`: keys (KW words) and 32-bit indices (the
-// identity when idx_in is null).
-template <int KW>
-__global__ void __launch_bounds__(kOSThreads, 4) k_onesweep(DevBuffers b, int pass, const uint64_t *keys_in,
-                                                         const uint32_t *idx_in, uint64_t *keys_out,
-                                                         uint32_t *idx_out) {
-    constexpr int ITEMS = OSConf<KW>::items;
-    constexpr int TILE = OSConf<KW>::tile;
+// One stable pass on digit `pass`: keys (KW words of type K) and 32-bit
+// indices (the identity when idx_in is null).
+template <typename K, int KW>
+__global__ void __launch_bounds__(kOSThreads, 4) k_onesweep(DevBuffers b, int pass, const K *keys_in,
+                                                         const uint32_t *idx_in, K *keys_out, uint32_t *idx_out) {
+    constexpr int ITEMS = OSConf<K, KW>::items;
+    constexpr int TILE = OSConf<K, KW>::tile;
     constexpr int NW = kOSThreads / 32;
     extern __shared__ uint64_t os_smem[];
-    uint64_t *skey = os_smem;                                          // [TILE][KW]
-    uint32_t *sidx = reinterpret_cast<uint32_t *>(os_smem + TILE * KW);  // [TILE]
+    K *skey = reinterpret_cast<K *>(os_smem);                      // [TILE][KW]
+    uint32_t *sidx = reinterpret_cast<uint32_t *>(skey + TILE * KW);  // [TILE]
     __shared__ uint32_t wcnt[NW][kRadix];
     __shared__ uint32_t lstart[kRadix], gbase[kRadix];
     __shared__ uint32_t s_tile;
@@ -163,7 +220,7 @@ __global__ void __launch_bounds__(kOSThreads, 4) k_onesweep(DevBuffers b, int pa
         const int64_t tile = s_tile;
         if (tile >= ntiles) break;
         const int64_t t0 = tile * TILE;
-        uint64_t kv[ITEMS][KW];
+        K kv[ITEMS][KW];
         uint32_t iv[ITEMS], off[ITEMS], dg[ITEMS];
         // stable ranking: element t0 + (warp*ITEMS + r)*32 + lane
 #pragma unroll
@@ -256,7 +313,7 @@ __global__ void __launch_bounds__(kOSThreads, 4) k_onesweep(DevBuffers b, int pa
         __syncthreads();
         const int tn = (int)min((int64_t)TILE, n - t0);
         for (int j = threadIdx.x; j < tn; j += kOSThreads) {
-            uint64_t k[KW];
+            K k[KW];
 #pragma unroll
             for (int w = 0; w < KW; w++) k[w] = skey[j * KW + w];
             uint32_t dd = os_digit<KW>(k, shift);

@@ -56,6 +56,8 @@ enum {
 #define HGPU_FLAG_MAIN_OVERFLOW 2
 #define HGPU_FLAG_TIMEOUT 4   /* a bounded device wait gave up (results of that cycle invalid) */
 #define HGPU_FLAG_INTERNAL 8  /* an internal consistency check failed (results of that cycle invalid) */
+#define HGPU_FLAG_BAD_DET 16  /* a spawned determinant has the wrong number of alpha or beta electrons
+                                 (results of that cycle invalid) */
 
 /* System kinds (sys%system in src/system.f90). */
 enum { HGPU_SYS_HUB_K = 1, HGPU_SYS_READ_IN = 2 };

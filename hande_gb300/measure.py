@@ -25,6 +25,9 @@ SPAWN_DRAM_BYTES_PER_ATTEMPT = (18.87e6 + 7.31e6) / 3.0548e6
 # integer (ALU) pipe, in percent of peak over the kernel's active cycles.
 SPAWN_ISSUE_ACTIVE_PCT = 52.6
 SPAWN_ALU_PIPE_PCT = 49.3
+# Issue-slot utilisation of k_annihilate on the same workload
+# (profiles/k_annihilate_mol26.md).
+ANNIHILATE_ISSUE_ACTIVE_PCT = 45.7
 
 
 def entry_bytes(W: int, R: int, initiator: bool):
@@ -55,5 +58,9 @@ def roofline_figures(phases: dict, counts: dict, W: int, R: int, initiator: bool
     ach2 = ann_bytes / t_ann / 1e9 if t_ann > 0 else 0.0
     annih = {"phases": ["sort", "splits", "annihilate"], "bound": "hbm", "achieved": ach2, "peak": peak,
              "unit": "GB/s", "frac": ach2 / peak, "algorithmic_bytes": ann_bytes, "seconds": t_ann,
-             "peak_source": peak_src}
+             "peak_source": peak_src,
+             "ncu_k_annihilate_issue_active_pct": ANNIHILATE_ISSUE_ACTIVE_PCT,
+             "note": "the annihilation kernel moves its algorithmic bytes once (DRAM traffic 1.04x of them) and "
+                     "is bound by instructions (Philox rounding and exact K_ii of new determinants, the merge "
+                     "walk) and shared-memory latency; profiles/k_annihilate_mol26.md"}
     return roof, annih

@@ -38,6 +38,7 @@ module hande_gpu_m
         integer(c_int32_t) :: nspaces, ncycles, precision, reserved0
         integer(c_int64_t) :: seed, walker_length, spawned_walker_length
         integer(c_uint64_t) :: ref_det(HGPU_MAX_WORDS)
+        real(c_double) :: pattempt_parallel
     end type hgpu_config
 
     type, bind(c) :: hgpu_report

@@ -61,7 +61,7 @@ class HgpuConfig(C.Structure):
         ("real_amplitudes", C.c_int32), ("initiator_approx", C.c_int32), ("nspaces", C.c_int32),
         ("ncycles", C.c_int32), ("precision", C.c_int32), ("reserved0", C.c_int32),
         ("seed", C.c_int64), ("walker_length", C.c_int64), ("spawned_walker_length", C.c_int64),
-        ("ref_det", C.c_uint64 * MAX_WORDS),
+        ("ref_det", C.c_uint64 * MAX_WORDS), ("pattempt_parallel", C.c_double),
     ]
 
 
@@ -157,7 +157,7 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
                 vary_shift_from_proje: bool = False, real_amplitudes: bool = False,
                 spawn_cutoff: float = 0.01, excit_gen: str = "renorm",
                 pattempt_single: float = -1.0, pattempt_double: float = -1.0,
-                initiator: bool = False, initiator_threshold: float = 3.0, nspaces: int = 1,
+                pattempt_parallel: float = -1.0, initiator: bool = False, initiator_threshold: float = 3.0, nspaces: int = 1,
                 precision: int = PREC_FP64, state_size: int = 100000,
                 spawned_state_size: int = 100000, reference=None) -> HgpuConfig:
     """Configuration with HANDE's qmc{} key names (src/lua_hande_calc.f90:1318-1331)."""
@@ -171,6 +171,7 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
     cfg.spawn_cutoff = spawn_cutoff
     cfg.pattempt_single = pattempt_single
     cfg.pattempt_double = pattempt_double
+    cfg.pattempt_parallel = pattempt_parallel
     cfg.D0_population = init_pop
     cfg.vary_shift_from_proje = int(bool(vary_shift_from_proje))
     cfg.excit_gen = EXCIT_GEN[excit_gen] if isinstance(excit_gen, str) else int(excit_gen)

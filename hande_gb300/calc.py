@@ -21,7 +21,7 @@ from .systems import System
 QMC_KEYS = {
     "tau", "init_pop", "mc_cycles", "nreports", "state_size", "spawned_state_size", "rng_seed",
     "target_population", "real_amplitudes", "spawn_cutoff", "excit_gen", "pattempt_single",
-    "pattempt_double", "initiator", "initiator_threshold", "shift_damping", "vary_shift_from",
+    "pattempt_double", "pattempt_parallel", "initiator", "initiator_threshold", "shift_damping", "vary_shift_from",
     "initial_shift", "precision",
 }
 FCIQMC_KEYS = {"replica_tricks"}
@@ -52,7 +52,8 @@ def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] =
         vary_shift_from=0.0 if vsf == "proje" else float(vsf), vary_shift_from_proje=(vsf == "proje"),
         real_amplitudes=bool(qmc.get("real_amplitudes", False)), spawn_cutoff=float(qmc.get("spawn_cutoff", 0.01)),
         excit_gen=qmc.get("excit_gen", "renorm"), pattempt_single=float(qmc.get("pattempt_single", -1.0)),
-        pattempt_double=float(qmc.get("pattempt_double", -1.0)), initiator=bool(qmc.get("initiator", False)),
+        pattempt_double=float(qmc.get("pattempt_double", -1.0)),
+        pattempt_parallel=float(qmc.get("pattempt_parallel", -1.0)), initiator=bool(qmc.get("initiator", False)),
         initiator_threshold=float(qmc.get("initiator_threshold", 3.0)),
         nspaces=2 if fo.get("replica_tricks") else 1,
         precision=PREC_MIXED if prec in ("mixed", "fp32", PREC_MIXED) else PREC_FP64,

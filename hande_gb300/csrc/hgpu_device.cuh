@@ -63,8 +63,15 @@ struct alignas(16) DevSys {
     double tau;
     double pattempt_single, pattempt_double;
     uint64_t t_single;  // u < pattempt_single  <=>  k < t_single for u = k 2^-53: ceil(pattempt_single 2^53)
-    const double *pg2;  // [n_aij][xa][xb] double-excitation p_gen (pgen_double), pg2_x = max orbitals per (irrep, spin) + 1
+    const double *pg2;  // [class][n_aij][xa][xb] double-excitation p_gen (pgen_double), pg2_x = max orbitals
+                        // per (irrep, spin) + 1; class 0 (and 1, 2: alpha-alpha, beta-beta pairs of the
+                        // spin-resolved generators, whose class 0 is the opposite-spin pair)
     int pg2_x, pg2_n;
+    // renorm_spin / no_renorm_spin: u < pattempt_parallel and u < nalpha/(nalpha+nbeta)
+    // as k < t_parallel, k < t_alpha
+    int spin_ij;
+    int pad_spin;
+    uint64_t t_parallel, t_alpha;
     double initiator_pop;
     double H00;
     uint64_t seed;
@@ -773,8 +780,51 @@ __device__ __forceinline__ int pick_a(const DevSys &s, int spin, uint64_t ku) {
 // p_gen of a double excitation, pattempt_double * 2/(nel(nel-1)) * (1/n_aij) *
 // (1/xb + 1/xa) in the reference's rounding order, read from a table the host
 // fills with exactly that expression (DevSys::pg2; symmetric in xa, xb).
-__device__ __forceinline__ double pgen_double(const DevSys &s, int n_aij, int xa, int xb) {
-    return __ldg(&s.pg2[((size_t)n_aij * s.pg2_x + xa) * s.pg2_x + xb]);
+__device__ __forceinline__ double pgen_double(const DevSys &s, int cls, int n_aij, int xa, int xb) {
+    return __ldg(&s.pg2[(((size_t)cls * s.pg2_n + n_aij) * s.pg2_x + xa) * s.pg2_x + xb]);
+}
+
+// choose_ij_spin_mol (src/excit_gen_mol.f90:684-783): parallel spins with
+// probability pattempt_parallel (alpha-alpha with probability nalpha/nel), else
+// one alpha and one beta electron; false when the class has too few electrons.
+// cls: 0 opposite spins, 1 alpha-alpha, 2 beta-beta (the p_gen table class).
+template <int W>
+__device__ __forceinline__ bool choose_ij_spin(const DevSys &s, RStream &rs, const Det<W> &f, int &i, int &j,
+                                               int &cls) {
+    Det<W> ma, mb;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        ma.w[w] = f.w[w] & kAlpha;
+        mb.w[w] = f.w[w] & kBeta;
+    }
+    if (rs.next_k() < s.t_parallel) {
+        const bool alpha = rs.next_k() < s.t_alpha;
+        const int n = alpha ? s.nalpha : s.nbeta;
+        if (n < 2) return false;
+        // int(rand * real(n(n-1)) / 2): the product rounded once, halved exactly
+        const int ind = floor_un(rs.next_k(), n * (n - 1)) / 2 + 1;
+        int j_ind = (int)(1.5f + sqrtf((float)(2 * ind) - 1.75f));
+        while (j_ind * (j_ind - 1) / 2 < ind) j_ind++;
+        while ((j_ind - 1) * (j_ind - 2) / 2 >= ind) j_ind--;
+        const int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
+        const Det<W> &m = alpha ? ma : mb;
+        i = select_det<W>(m.w, i_ind - 1);
+        j = select_det<W>(m.w, j_ind - 1);
+        cls = alpha ? 1 : 2;
+    } else {
+        if (s.nbeta < 1 || s.nalpha < 1) return false;
+        const int i_ind = floor_un(rs.next_k(), s.nalpha) + 1;
+        const int j_ind = floor_un(rs.next_k(), s.nbeta) + 1;
+        i = select_det<W>(ma.w, i_ind - 1);
+        j = select_det<W>(mb.w, j_ind - 1);
+        if (j < i) {
+            const int t = i;
+            i = j;
+            j = t;
+        }
+        cls = 0;
+    }
+    return true;
 }
 
 // attempt_to_spawn (src/spawning.F90:711-768).
@@ -869,19 +919,29 @@ __device__ __forceinline__ void gen_double_mol(const DevSys &s, RStream &rs, con
                                                Attempt &out, double &pgen, Real &hm) {
     const Det<W> &f = d.f;
     out.nexcit = 2;
-    // choose_ij_mol (src/excit_gen_mol.f90:620-660)
-    int ind = floor_uab_half(rs.next_k(), s.nel, s.nel - 1) + 1;  // int(rand * nel * (nel-1) / 2) + 1
-    // int(1.5 + sqrt(2 ind - 1.75)) is exactly the j with
-    // (j-1)(j-2)/2 < ind <= j(j-1)/2; found here in integer arithmetic
-    int j_ind = (int)(1.5f + sqrtf((float)(2 * ind) - 1.75f));
-    while (j_ind * (j_ind - 1) / 2 < ind) j_ind++;
-    while ((j_ind - 1) * (j_ind - 2) / 2 >= ind) j_ind--;
-    int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
-    int i = select_det<W>(f.w, i_ind - 1);
-    int j = select_det<W>(f.w, j_ind - 1);
+    int i, j, cls = 0;
+    if (s.spin_ij) {
+        if (!choose_ij_spin<W>(s, rs, f, i, j, cls)) {
+            out.from[0] = out.from[1] = -1;
+            out.allowed = false;
+            hm = (Real)0;
+            pgen = 1.0;
+            return;
+        }
+    } else {
+        // choose_ij_mol (src/excit_gen_mol.f90:620-660)
+        int ind = floor_uab_half(rs.next_k(), s.nel, s.nel - 1) + 1;  // int(rand * nel * (nel-1) / 2) + 1
+        // int(1.5 + sqrt(2 ind - 1.75)) is exactly the j with
+        // (j-1)(j-2)/2 < ind <= j(j-1)/2; found here in integer arithmetic
+        int j_ind = (int)(1.5f + sqrtf((float)(2 * ind) - 1.75f));
+        while (j_ind * (j_ind - 1) / 2 < ind) j_ind++;
+        while ((j_ind - 1) * (j_ind - 2) / 2 >= ind) j_ind--;
+        int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
+        i = select_det<W>(f.w, i_ind - 1);
+        j = select_det<W>(f.w, j_ind - 1);
+    }
     int ij_sym = xsym(s, sym_of<W>(s, i), sym_of<W>(s, j));
     int ij_spin = ms_of(i) + ms_of(j);
-    double pgen_ij = s.pgen_ij;
     out.from[0] = i;
     out.from[1] = j;
     int a = -1, b = -1;
@@ -989,12 +1049,12 @@ __device__ __forceinline__ void gen_double_mol(const DevSys &s, RStream &rs, con
                 xb = SU(d, imsb, symb) - same;
             }
             // p_aijb = 1/xa, p_bija = 1/xb
-            pgen = pgen_double(s, n_aij, xa, xb);
+            pgen = pgen_double(s, cls, n_aij, xa, xb);
         } else {
             // calc_pgen_double_mol_no_renorm (src/excit_gen_mol.f90:1368-1445)
             int n_aij = ij_spin == -2 ? s.nvirt_beta : (ij_spin == 0 ? s.nvirt : s.nvirt_alpha);
             int same = (syma == symb && imsa == imsb) ? 1 : 0;
-            pgen = pgen_double(s, n_aij, s.nbss[syma * 2 + imsa] - same, s.nbss[symb * 2 + imsb] - same);
+            pgen = pgen_double(s, cls, n_aij, s.nbss[syma * 2 + imsa] - same, s.nbss[symb * 2 + imsb] - same);
         }
         hm = sc2_mol<Real>(s, i, j, a, b, perm2<W>(f, i, j, a, b));
     } else {
@@ -1006,7 +1066,7 @@ __device__ __forceinline__ void gen_double_mol(const DevSys &s, RStream &rs, con
 template <int W, typename Real>
 __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, int64_t parent, Attempt &out) {
     out.from[0] = out.from[1] = out.to[0] = out.to[1] = -1;
-    bool renorm = s.excit_gen == HGPU_EXCIT_GEN_RENORM;
+    bool renorm = s.excit_gen == HGPU_EXCIT_GEN_RENORM || s.excit_gen == HGPU_EXCIT_GEN_RENORM_SPIN;
     double pgen;
     Real hm;
     if (rs.next_k() < s.t_single) gen_single_mol<W, Real>(s, rs, d, renorm, out, pgen, hm);  // rand < pattempt_single

@@ -376,21 +376,39 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
         }
         for (int k = 0; k < 2 * kMaxSym; k++) s.d_nbss[k] = (double)s.nbss[k];
         h->b.nk = 0;
+        // renorm_spin / no_renorm_spin: pattempt_parallel (src/qmc.F90:974-988)
+        // and the pgen_ij of each spin class in choose_ij_spin_mol's rounding
+        // order (src/excit_gen_mol.f90:684-783)
+        double pgen_ij_cls[3] = {s.pgen_ij, 0.0, 0.0};
+        int ncls = 1;
+        s.spin_ij = c.excit_gen == HGPU_EXCIT_GEN_RENORM_SPIN || c.excit_gen == HGPU_EXCIT_GEN_NO_RENORM_SPIN;
+        if (s.spin_ij) {
+            const double pp = c.pattempt_parallel < 0.0 ? HeatBathBuilder(sys).parallel_spin_prob() : c.pattempt_parallel;
+            const double na = (double)s.nalpha, nb = (double)s.nbeta;
+            pgen_ij_cls[0] = (1.0 - pp) * (1.0 / (double)(s.nalpha * s.nbeta));
+            pgen_ij_cls[1] = s.nalpha >= 2 ? pp * (na / (na + nb)) * 2.0 * (1.0 / na) * (1.0 / (na - 1.0)) : 0.0;
+            pgen_ij_cls[2] = s.nbeta >= 2 ? pp * (nb / (na + nb)) * 2.0 * (1.0 / nb) * (1.0 / (nb - 1.0)) : 0.0;
+            s.t_parallel = (uint64_t)std::ceil(std::ldexp(pp, 53));
+            s.t_alpha = (uint64_t)std::ceil(std::ldexp(na / (na + nb), 53));
+            ncls = 3;
+        }
         {
             // double-excitation p_gen table: pattempt_double * pgen_ij * (inv[n] * (inv[xb] + inv[xa])),
-            // each product and sum rounded as the generator writes it
+            // each product and sum rounded as the generator writes it, for each pgen_ij class
             int X = 1;
             for (int k = 0; k < 2 * kMaxSym; k++) X = std::max(X, s.nbss[k] + 1);
             int Nn = s.nvirt + 1;
-            std::vector<double> tab((size_t)Nn * X * X);
-            double c0 = s.pattempt_double * s.pgen_ij;
-            for (int n = 0; n < Nn; n++)
-                for (int xa = 0; xa < X; xa++)
-                    for (int xb = 0; xb < X; xb++) {
-                        double pb = 1.0 / (double)xb, pa = 1.0 / (double)xa;
-                        double pg = (1.0 / (double)n) * (pb + pa);
-                        tab[((size_t)n * X + xa) * X + xb] = c0 * pg;
-                    }
+            std::vector<double> tab((size_t)ncls * Nn * X * X);
+            for (int cls = 0; cls < ncls; cls++) {
+                double c0 = s.pattempt_double * pgen_ij_cls[cls];
+                for (int n = 0; n < Nn; n++)
+                    for (int xa = 0; xa < X; xa++)
+                        for (int xb = 0; xb < X; xb++) {
+                            double pb = 1.0 / (double)xb, pa = 1.0 / (double)xa;
+                            double pg = (1.0 / (double)n) * (pb + pa);
+                            tab[(((size_t)cls * Nn + n) * X + xa) * X + xb] = c0 * pg;
+                        }
+            }
             if ((rc = upload(h, tab.data(), tab.size(), &s.pg2))) return rc;
             s.pg2_x = X;
             s.pg2_n = Nn;
@@ -590,11 +608,19 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     } else if (sys->kind == HGPU_SYS_READ_IN) {
         bool hb = cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM ||
                   cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE;
-        if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM && !hb)
+        if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM &&
+            cfg->excit_gen != HGPU_EXCIT_GEN_RENORM_SPIN && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM_SPIN && !hb)
             return HGPU_ERR_UNSUPPORTED;
         if (hb && sys->nel > kHBMaxEl) return HGPU_ERR_UNSUPPORTED;
     } else {
         return HGPU_ERR_INVALID;
+    }
+    // pattempt_parallel only with the spin-resolved generators, at most 1
+    // (src/check_input.F90:212-218)
+    {
+        const bool spin_gen = sys->kind == HGPU_SYS_READ_IN && (cfg->excit_gen == HGPU_EXCIT_GEN_RENORM_SPIN ||
+                                                                 cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM_SPIN);
+        if (cfg->pattempt_parallel > 0.0 && (!spin_gen || cfg->pattempt_parallel > 1.0)) return HGPU_ERR_INVALID;
     }
     int ndev = hgpu_device_count();
     if (ndev <= 0) return HGPU_ERR_NO_DEVICE;
@@ -610,7 +636,8 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
         else if (cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM ||
                  cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE)
             h->gkind = kKindHeatBathUniform;  // the singles differ at run time
-        else if (cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM) h->gkind = kKindReadInNoRenorm;
+        else if (cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM || cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM_SPIN)
+            h->gkind = kKindReadInNoRenorm;
     }
     h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;
     cudaGetDevice(&h->device);

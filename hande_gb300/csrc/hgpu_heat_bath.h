@@ -164,6 +164,44 @@ class HeatBathBuilder {
         return true;
     }
 
+    // find_parallel_spin_prob_mol (src/qmc_common.F90:265-378): the share of
+    // sum |<ij||ab>| over allowed (i, j, a, b) carried by parallel-spin pairs.
+    // The sums run over j, a, b for each i (one thread per i) and the per-i
+    // sums are added in i order, as the CPU restatement does.
+    double parallel_spin_prob() const {
+        const int nb = nb_;
+        std::vector<double> par(nb, 0.0), orth(nb, 0.0);
+        unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+        std::vector<std::thread> pool;
+        for (unsigned w = 0; w < nt; w++) {
+            pool.emplace_back([&, w]() {
+                for (int i = (int)w; i < nb; i += (int)nt) {
+                    double pi = 0.0, oi = 0.0;
+                    for (int j = 0; j < nb; j++) {
+                        if (i == j) continue;
+                        const bool parallel = sys_->orb_ms[i] == sys_->orb_ms[j];
+                        for (int a = 0; a < nb; a++)
+                            for (int b = 0; b < nb; b++) {
+                                double h = weight(i, j, a, b);
+                                if (h == 0.0) continue;
+                                if (parallel) pi = pi + h;
+                                else oi = oi + h;
+                            }
+                    }
+                    par[i] = pi;
+                    orth[i] = oi;
+                }
+            });
+        }
+        for (auto &t : pool) t.join();
+        double p = 0.0, o = 0.0;
+        for (int i = 0; i < nb; i++) {
+            p = p + par[i];
+            o = o + orth[i];
+        }
+        return p / (p + o);
+    }
+
   private:
     static int xsym(int a, int b) { return a ^ b; }
 

@@ -132,6 +132,12 @@ typedef struct hgpu_config {
     int64_t walker_length;         /* main-list capacity; < 0 means MB (state_size) */
     int64_t spawned_walker_length; /* spawned-list capacity; < 0 means MB */
     uint64_t ref_det[HGPU_MAX_WORDS]; /* reference determinant f0 */
+    double pattempt_parallel;      /* renorm_spin / no_renorm_spin: probability that a double
+                                      excitation moves two electrons of parallel spin
+                                      (choose_ij_spin_mol, src/excit_gen_mol.f90:684-783); < 0: the
+                                      |H| ratio of find_parallel_spin_prob_mol
+                                      (src/qmc_common.F90:265-378); > 0 with other generators is
+                                      refused, as check_input does (src/check_input.F90:212-218) */
 } hgpu_config;
 
 /* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */

@@ -120,6 +120,10 @@ struct oracle_ctx {
     uint64_t mask[MAXB][MAXW]; /* excit_mask (src/excitations.F90:25-70) */
     int64_t real_factor, cutoff;
     double pattempt_single, pattempt_double;
+    /* renorm_spin / no_renorm_spin: pattempt_parallel and pgen_ij of the three
+     * spin classes (alpha-alpha, beta-beta, opposite), choose_ij_spin_mol */
+    int spin_ij;
+    double pattempt_parallel, pgen_ij_aa, pgen_ij_bb, pgen_ij_ab;
     int R;
     uint64_t f0[MAXW];
     double H00;
@@ -465,6 +469,77 @@ static void choose_ij_mol(const oracle_ctx *c, rstream *rs, const det_info *d, i
     *ij_sym = cross(c, c->orb_sym[*i], c->orb_sym[*j]);
     *ij_spin = c->orb_ms[*i] + c->orb_ms[*j];
     *pgen_ij = 2.0 / (double)(c->nel * (c->nel - 1));
+}
+
+/* choose_ij_spin_mol (src/excit_gen_mol.f90:684-783): first parallel or
+ * opposite spins, then the pair; returns 0 when the spin class has too few
+ * electrons (allowed_excitation = .false.). */
+static int choose_ij_spin_mol(const oracle_ctx *c, rstream *rs, const det_info *d, int *i, int *j, int *ij_sym,
+                              int *ij_spin, double *pgen_ij) {
+    int occa[128], occb[128], na = 0, nb = 0;
+    for (int k = 0; k < d->nocc; k++) {
+        if (c->orb_ms[d->occ[k]] > 0) occa[na++] = d->occ[k];
+        else occb[nb++] = d->occ[k];
+    }
+    if (rs_next(rs) < c->pattempt_parallel) {
+        int alpha = rs_next(rs) < ((double)c->nalpha / (double)(c->nalpha + c->nbeta));
+        int n = alpha ? c->nalpha : c->nbeta;
+        const int *occ = alpha ? occa : occb;
+        if (n < 2) return 0;
+        int ind = (int)(rs_next(rs) * (double)(n * (n - 1)) / 2.0) + 1;
+        int j_ind = (int)(1.50 + sqrt((double)(2 * ind) - 1.750));
+        int i_ind = ind - ((j_ind - 1) * (j_ind - 2)) / 2;
+        *i = occ[i_ind - 1];
+        *j = occ[j_ind - 1];
+        *pgen_ij = alpha ? c->pgen_ij_aa : c->pgen_ij_bb;
+    } else {
+        if (c->nbeta < 1 || c->nalpha < 1) return 0;
+        int i_ind = (int)(rs_next(rs) * (double)c->nalpha) + 1;
+        int j_ind = (int)(rs_next(rs) * (double)c->nbeta) + 1;
+        *i = occa[i_ind - 1];
+        *j = occb[j_ind - 1];
+        if (*j < *i) {
+            int t = *i;
+            *i = *j;
+            *j = t;
+        }
+        *pgen_ij = c->pgen_ij_ab;
+    }
+    *ij_sym = cross(c, c->orb_sym[*i], c->orb_sym[*j]);
+    *ij_spin = c->orb_ms[*i] + c->orb_ms[*j];
+    return 1;
+}
+
+/* find_parallel_spin_prob_mol (src/qmc_common.F90:265-378): the share of
+ * sum |<ij||ab>| over allowed (i, j, a, b) carried by parallel-spin i, j.  The
+ * sums run over j, a, b for each i and the per-i sums are added in i order
+ * (the reference's order within one process' range of i). */
+static double find_parallel_spin_prob_mol(const oracle_ctx *c) {
+    double par = 0.0, orth = 0.0;
+    for (int i = 0; i < c->nbasis; i++) {
+        double pi = 0.0, oi = 0.0;
+        for (int j = 0; j < c->nbasis; j++) {
+            if (i == j) continue;
+            int it = j < i ? j : i, jt = j < i ? i : j;
+            int ij_sym = cross(c, c->orb_sym[it], c->orb_sym[jt]);
+            for (int a = 0; a < c->nbasis; a++) {
+                if (a == i || a == j) continue;
+                int isymb = cross(c, ij_sym, c->orb_sym[a]);
+                for (int b = 0; b < c->nbasis; b++) {
+                    int spin_ok = (c->orb_ms[it] == c->orb_ms[a] && c->orb_ms[jt] == c->orb_ms[b]) ||
+                                  (c->orb_ms[it] == c->orb_ms[b] && c->orb_ms[jt] == c->orb_ms[a]);
+                    if (!spin_ok || c->orb_sym[b] != isymb || b == a || b == i || b == j) continue;
+                    int at = b < a ? b : a, bt = b < a ? a : b;
+                    double h = fabs(sc2_mol_excit(c, it, jt, at, bt, 0));
+                    if (c->orb_ms[it] == c->orb_ms[jt]) pi = pi + h;
+                    else oi = oi + h;
+                }
+            }
+        }
+        par = par + pi;
+        orth = orth + oi;
+    }
+    return par / (par + orth);
 }
 
 /* spin-dependent (fac, shift, na) of choose_ab_mol / find_ab_mol, 0-based:
@@ -1104,7 +1179,8 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
     int gen = c->cfg.excit_gen;
     /* gen_excit_mol_heat_bath_uniform takes its singles from gen_single_excit_mol
      * (heat_bath_uniform) or gen_single_excit_heat_bath_exact (heat_bath_single) */
-    int renorm = gen == HGPU_EXCIT_GEN_RENORM || gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM;
+    int renorm = gen == HGPU_EXCIT_GEN_RENORM || gen == HGPU_EXCIT_GEN_RENORM_SPIN ||
+                 gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM;
     double pgen, hmatel;
     if (gen == HGPU_EXCIT_GEN_HEAT_BATH) {
         gen_heat_bath(c, rs, f, d, out, &pgen, &hmatel);
@@ -1135,9 +1211,14 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
         int i, j, ij_sym, ij_spin, a = -1, b = -1, ok;
         double pgen_ij;
         out->e.nexcit = 2;
-        choose_ij_mol(c, rs, d, &i, &j, &ij_sym, &ij_spin, &pgen_ij);
-        if (renorm) ok = choose_ab_mol(c, rs, f, ij_sym, ij_spin, d, &a, &b);
-        else ok = find_ab_mol(c, rs, f, ij_sym, ij_spin, &a, &b);
+        i = j = -1;
+        if (c->spin_ij) ok = choose_ij_spin_mol(c, rs, d, &i, &j, &ij_sym, &ij_spin, &pgen_ij);
+        else {
+            choose_ij_mol(c, rs, d, &i, &j, &ij_sym, &ij_spin, &pgen_ij);
+            ok = 1;
+        }
+        if (ok && renorm) ok = choose_ab_mol(c, rs, f, ij_sym, ij_spin, d, &a, &b);
+        else if (ok) ok = find_ab_mol(c, rs, f, ij_sym, ij_spin, &a, &b);
         out->allowed = ok;
         out->e.from[0] = i;
         out->e.from[1] = j;
@@ -1728,6 +1809,18 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
         c->pattempt_double = 1.0 - cfg->pattempt_single;
     }
     for (int w = 0; w < MAXW; w++) c->f0[w] = w < c->nw ? cfg->ref_det[w] : 0;
+    /* pattempt_parallel (src/qmc.F90:974-988) and the pgen_ij of each spin
+     * class, in choose_ij_spin_mol's rounding order */
+    c->spin_ij = c->kind == HGPU_SYS_READ_IN &&
+                 (cfg->excit_gen == HGPU_EXCIT_GEN_RENORM_SPIN || cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM_SPIN);
+    if (c->spin_ij) {
+        double pp = cfg->pattempt_parallel < 0.0 ? find_parallel_spin_prob_mol(c) : cfg->pattempt_parallel;
+        double na = (double)c->nalpha, nb = (double)c->nbeta;
+        c->pattempt_parallel = pp;
+        c->pgen_ij_aa = c->nalpha >= 2 ? pp * (na / (na + nb)) * 2.0 * (1.0 / na) * (1.0 / (na - 1.0)) : 0.0;
+        c->pgen_ij_bb = c->nbeta >= 2 ? pp * (nb / (na + nb)) * 2.0 * (1.0 / nb) * (1.0 / (nb - 1.0)) : 0.0;
+        c->pgen_ij_ab = (1.0 - pp) * (1.0 / (double)(c->nalpha * c->nbeta));
+    }
     if (c->kind == HGPU_SYS_HUB_K) {
         double c0 = (double)(c->nalpha * c->nbeta) * c->coulomb_k;
         int64_t B = ceil_abs(c0);
@@ -1953,6 +2046,8 @@ double oracle_hmatel(oracle_ctx *c, const int64_t *f1, const int64_t *f2) {
 
 double oracle_sc0(oracle_ctx *c, const int64_t *f) { return sc0(c, (const uint64_t *)f); }
 
+double oracle_pattempt_parallel(oracle_ctx *c) { return c->spin_ij ? c->pattempt_parallel : -1.0; }
+
 double oracle_pgen(oracle_ctx *c, const int64_t *fi, const int32_t *orbs) {
     const uint64_t *f = (const uint64_t *)fi;
     det_info d;
@@ -1963,7 +2058,7 @@ double oracle_pgen(oracle_ctx *c, const int64_t *fi, const int32_t *orbs) {
             return 1.0 / (double)(c->nalpha * c->nbeta * c->nvirt_alpha);
         return calc_pgen_hub_k(c, ij_sym, f, &d);
     }
-    int renorm = c->cfg.excit_gen == HGPU_EXCIT_GEN_RENORM;
+    int renorm = c->cfg.excit_gen == HGPU_EXCIT_GEN_RENORM || c->cfg.excit_gen == HGPU_EXCIT_GEN_RENORM_SPIN;
     if (orbs[1] < 0) {
         return c->pattempt_single *
                (renorm ? calc_pgen_single_mol(c, &d, orbs[2]) : calc_pgen_single_mol_no_renorm(c, orbs[2]));
@@ -1971,6 +2066,7 @@ double oracle_pgen(oracle_ctx *c, const int64_t *fi, const int32_t *orbs) {
     int ij_sym = cross(c, c->orb_sym[orbs[0]], c->orb_sym[orbs[1]]);
     int spin = c->orb_ms[orbs[0]] + c->orb_ms[orbs[1]];
     double pij = 2.0 / (double)(c->nel * (c->nel - 1));
+    if (c->spin_ij) pij = spin == 2 ? c->pgen_ij_aa : (spin == -2 ? c->pgen_ij_bb : c->pgen_ij_ab);
     if (renorm) return c->pattempt_double * pij * calc_pgen_double_mol(c, ij_sym, orbs[2], orbs[3], spin, &d);
     return c->pattempt_double * pij * calc_pgen_double_mol_no_renorm(c, orbs[2], orbs[3], spin);
 }

@@ -47,6 +47,8 @@ double oracle_hmatel(oracle_ctx *c, const int64_t *f1, const int64_t *f2);
 double oracle_sc0(oracle_ctx *c, const int64_t *f);
 /* pgen of an explicit excitation (calc_pgen_* of the configured generator) */
 double oracle_pgen(oracle_ctx *c, const int64_t *f, const int32_t *orbs);
+/* pattempt_parallel of the spin-resolved generators (negative for the others). */
+double oracle_pattempt_parallel(oracle_ctx *c);
 /* Counters of the last cycles (spawn attempts etc.). */
 int64_t oracle_total_attempts(oracle_ctx *c);
 /* Philox4x32-10 uniform, for cross-checking the device generator. */

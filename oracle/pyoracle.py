@@ -53,6 +53,8 @@ def lib():
         L.oracle_hmatel.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
         L.oracle_sc0.restype = C.c_double
         L.oracle_sc0.argtypes = [C.c_void_p, P(C.c_int64)]
+        L.oracle_pattempt_parallel.restype = C.c_double
+        L.oracle_pattempt_parallel.argtypes = [C.c_void_p]
         L.oracle_pgen.restype = C.c_double
         L.oracle_pgen.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int32)]
         L.oracle_total_attempts.restype = C.c_int64
@@ -164,6 +166,9 @@ class Oracle:
 
     def sc0(self, f) -> float:
         return self.L.oracle_sc0(self.h, _i64(f))
+
+    def pattempt_parallel(self) -> float:
+        return self.L.oracle_pattempt_parallel(self.h)
 
     def pgen(self, f, orbs) -> float:
         o = np.ascontiguousarray(orbs, dtype=np.int32)

@@ -39,6 +39,7 @@ module hande_gpu_m
         integer(c_int64_t) :: seed, walker_length, spawned_walker_length
         integer(c_uint64_t) :: ref_det(HGPU_MAX_WORDS)
         real(c_double) :: pattempt_parallel
+        integer(c_int32_t) :: density_matrices, density_matrix_report
     end type hgpu_config
 
     type, bind(c) :: hgpu_report
@@ -51,6 +52,7 @@ module hande_gpu_m
         integer(c_int64_t) :: nattempts, nspawned
         integer(c_int32_t) :: error_flags, reserved0
         real(c_double) :: device_ms
+        real(c_double) :: rdm_energy, rdm_trace
     end type hgpu_report
 
     interface
@@ -78,6 +80,14 @@ module hande_gpu_m
             real(c_double), intent(in) :: dat(*)
             integer(c_int64_t), value :: n
         end function hgpu_upload_walkers
+
+        integer(c_int32_t) function hgpu_rdm_download(h, rdm, capacity, n_out) bind(c, name='hgpu_rdm_download')
+            import :: c_ptr, c_int32_t, c_int64_t, c_double
+            type(c_ptr), value :: h
+            real(c_double), intent(out) :: rdm(*)
+            integer(c_int64_t), value :: capacity
+            integer(c_int64_t), intent(out) :: n_out
+        end function hgpu_rdm_download
 
         integer(c_int32_t) function hgpu_download_walkers(h, states, pops, dat, capacity, n_out) &
                 bind(c, name='hgpu_download_walkers')

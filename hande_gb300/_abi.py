@@ -62,6 +62,7 @@ class HgpuConfig(C.Structure):
         ("ncycles", C.c_int32), ("precision", C.c_int32), ("reserved0", C.c_int32),
         ("seed", C.c_int64), ("walker_length", C.c_int64), ("spawned_walker_length", C.c_int64),
         ("ref_det", C.c_uint64 * MAX_WORDS), ("pattempt_parallel", C.c_double),
+        ("density_matrices", C.c_int32), ("density_matrix_report", C.c_int32),
     ]
 
 
@@ -73,6 +74,7 @@ class HgpuReport(C.Structure):
         ("nstates", C.c_int64), ("nspawn_events", C.c_int64), ("rspawn", C.c_double),
         ("nattempts", C.c_int64), ("nspawned", C.c_int64), ("error_flags", C.c_int32),
         ("reserved0", C.c_int32), ("device_ms", C.c_double),
+        ("rdm_energy", C.c_double), ("rdm_trace", C.c_double),
     ]
 
     def as_dict(self, nspaces: int = 1) -> dict:
@@ -91,6 +93,9 @@ class HgpuReport(C.Structure):
             "error_flags": int(self.error_flags),
             "device_ms": float(self.device_ms),
         }
+        if self.rdm_trace != 0.0:
+            r["RDM energy num."] = float(self.rdm_energy)
+            r["RDM trace"] = float(self.rdm_trace)
         return r
 
 
@@ -157,7 +162,8 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
                 vary_shift_from_proje: bool = False, real_amplitudes: bool = False,
                 spawn_cutoff: float = 0.01, excit_gen: str = "renorm",
                 pattempt_single: float = -1.0, pattempt_double: float = -1.0,
-                pattempt_parallel: float = -1.0, initiator: bool = False, initiator_threshold: float = 3.0, nspaces: int = 1,
+                pattempt_parallel: float = -1.0, density_matrices: bool = False,
+                density_matrix_report: int = 0, initiator: bool = False, initiator_threshold: float = 3.0, nspaces: int = 1,
                 precision: int = PREC_FP64, state_size: int = 100000,
                 spawned_state_size: int = 100000, reference=None) -> HgpuConfig:
     """Configuration with HANDE's qmc{} key names (src/lua_hande_calc.f90:1318-1331)."""
@@ -172,6 +178,8 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
     cfg.pattempt_single = pattempt_single
     cfg.pattempt_double = pattempt_double
     cfg.pattempt_parallel = pattempt_parallel
+    cfg.density_matrices = int(bool(density_matrices))
+    cfg.density_matrix_report = int(density_matrix_report)
     cfg.D0_population = init_pop
     cfg.vary_shift_from_proje = int(bool(vary_shift_from_proje))
     cfg.excit_gen = EXCIT_GEN[excit_gen] if isinstance(excit_gen, str) else int(excit_gen)

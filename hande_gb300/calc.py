@@ -24,7 +24,7 @@ QMC_KEYS = {
     "pattempt_double", "pattempt_parallel", "initiator", "initiator_threshold", "shift_damping", "vary_shift_from",
     "initial_shift", "precision",
 }
-FCIQMC_KEYS = {"replica_tricks"}
+FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file"}
 
 
 def _opts(qmc: dict, fciqmc_opts: Optional[dict]):
@@ -55,7 +55,10 @@ def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] =
         pattempt_double=float(qmc.get("pattempt_double", -1.0)),
         pattempt_parallel=float(qmc.get("pattempt_parallel", -1.0)), initiator=bool(qmc.get("initiator", False)),
         initiator_threshold=float(qmc.get("initiator_threshold", 3.0)),
-        nspaces=2 if fo.get("replica_tricks") else 1,
+        # density_matrices turns replica_tricks on (src/lua_hande_calc.f90:1569-1573)
+        nspaces=2 if (fo.get("replica_tricks") or fo.get("density_matrices")) else 1,
+        density_matrices=bool(fo.get("density_matrices", False)),
+        density_matrix_report=int(fo.get("density_matrix_report", 0)),
         precision=PREC_MIXED if prec in ("mixed", "fp32", PREC_MIXED) else PREC_FP64,
         state_size=int(qmc.get("state_size", -1000)), spawned_state_size=int(qmc.get("spawned_state_size", -500)),
         reference=reference)
@@ -100,7 +103,41 @@ def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None
             if verbose:
                 stream.write("# Soft exit requested through %s.\n" % comm_file)
             break
+    fo = fciqmc or {}
+    if fo.get("density_matrices"):
+        rdm = eng.rdm()
+        if rdm is not None and reports and "RDM trace" in reports[-1]:
+            write_final_rdm(rdm, sys.nel, sys.nbasis, fo.get("density_matrix_file", "RDM"), stream if verbose else None)
+            if verbose:
+                stream.write(" # Final energy from RDM  %17.10e\n" %
+                             (reports[-1]["RDM energy num."] / reports[-1]["RDM trace"]))
     return {"reports": reports, "engine": eng}
+
+
+def write_final_rdm(rdm, nel: int, nbasis: int, filename: str, comment=None):
+    """write_final_rdm (src/replica_rdm.F90:266-328): normalise the trace to
+    nel (nel - 1) / 2 (normalise_rdm), make the RDM Hermitian
+    (check_hermiticity, reporting the deviation) and write the elements above
+    depsilon as `i j k l value` with 1-based spin orbitals i < j, k < l."""
+    import numpy as np
+    r = np.array(rdm, dtype=float)
+    r = r * nel * (nel - 1) * 0.5 / np.trace(r)
+    iu = np.triu_indices(r.shape[0], 1)
+    err = np.abs(r[iu] - r.T[iu])
+    if comment is not None:
+        comment.write(" # Maximum deviation from Hermiticity is: %17.10e\n" % (err.max() if err.size else 0.0))
+        comment.write(" # Average deviation from Hermiticity is: %17.10e\n" % (err.mean() if err.size else 0.0))
+    r = 0.5 * (r + r.T)
+    with open(filename, "w") as fh:
+        for i in range(nbasis):
+            for j in range(i + 1, nbasis):
+                row = j * (j - 1) // 2 + i
+                for k in range(nbasis):
+                    for l in range(k + 1, nbasis):
+                        v = r[row, l * (l - 1) // 2 + k]
+                        if abs(v) > 1e-12:
+                            fh.write("%4d%4d%4d%4d  %24.12E\n" % (i + 1, j + 1, k + 1, l + 1, v))
+    return r
 
 
 def _softexit(path: str) -> bool:

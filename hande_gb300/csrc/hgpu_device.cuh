@@ -607,6 +607,7 @@ struct Attempt {
     double pgen, hmatel;
     bool allowed;
     int64_t nspawn;
+    int64_t nspawn_rdm;  // spawn_rdm's unweighted attempt (replica 2-RDM), 0 otherwise
 };
 
 // stochastic_round_spawned_particle (src/stoch_utils.f90:87-136).
@@ -837,6 +838,19 @@ __device__ __forceinline__ void attempt_to_spawn(const DevSys &s, RStream &rs, i
     int64_t nspawn = round_spawned(s.cutoff, s.d_cutoff, pspawn, rs);
     if (nspawn > 0) nspawn = child_sign(h, parent, nspawn);
     out.nspawn = nspawn;
+}
+
+// spawn_rdm's second attempt (src/spawning.F90:664-671): attempt_to_spawn with
+// tau = 1 and hmatel = -1, drawn after the spawn itself, for the replica
+// sampling of the 2-RDM.
+__device__ __forceinline__ void attempt_to_spawn_rdm(const DevSys &s, RStream &rs, int64_t parent, Attempt &out) {
+    out.nspawn_rdm = 0;
+    if (!out.allowed) return;
+    double p = 1.0 * fabs(-1.0) / out.pgen;
+    p = p * s.d_real_factor;
+    int64_t n = round_spawned(s.cutoff, s.d_cutoff, p, rs);
+    if (n > 0) n = child_sign(-1.0, parent, n);
+    out.nspawn_rdm = n;
 }
 
 // gen_single_excit_mol / gen_single_excit_mol_no_renorm (src/excit_gen_mol.f90:384-519):

@@ -32,6 +32,10 @@ struct hgpu_handle {
     DevBuffers b;
     DevSys hsys;  // host copy of the device system struct
     int cur;      // buffer holding the current main list
+    // replica 2-RDM: accumulating (spawn_rdm on), reports ended, a report in progress
+    int rdm_on = 0;
+    int reports_done = 0;
+    bool report_open = false;
     cudaGraphExec_t graph[2];
     bool graph_ok[2];
     bool use_graphs;
@@ -551,6 +555,18 @@ static int alloc_lists(hgpu_handle *h) {
         if ((rc = dalloc(h, &b.seg_epoch, 1))) return rc;
         CK(cudaMemset(b.seg_epoch, 0, sizeof(uint32_t)));
     }
+    // replica 2-RDM (density_matrices): the RDM, the cycle's RDM spawns, row sums
+    b.rdm = nullptr;
+    b.npairs = 0;
+    if (h->cfg.density_matrices) {
+        b.npairs = (int64_t)h->hsys.nbasis * (h->hsys.nbasis - 1) / 2;
+        if ((rc = dalloc(h, &b.rdm, (size_t)(b.npairs * b.npairs)))) return rc;
+        CK(cudaMemset(b.rdm, 0, sizeof(double) * (size_t)(b.npairs * b.npairs)));
+        if ((rc = dalloc(h, &b.rdm_sdets, (size_t)b.scap * 2 * W))) return rc;
+        if ((rc = dalloc(h, &b.rdm_spops, (size_t)b.scap))) return rc;
+        if ((rc = dalloc(h, &b.rdm_sspace, (size_t)b.scap))) return rc;
+        if ((rc = dalloc(h, &b.rdm_rows, (size_t)(2 * b.npairs)))) return rc;
+    }
     if ((rc = dalloc(h, &b.scan_part, (size_t)kMaxBlocks * 2))) return rc;
     if ((rc = dalloc(h, &b.part_d, (size_t)kMaxBlocks * 4))) return rc;
     if ((rc = dalloc(h, &b.part_i, (size_t)kMaxBlocks * 4))) return rc;
@@ -615,6 +631,8 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     } else {
         return HGPU_ERR_INVALID;
     }
+    // density_matrices: replica sampling of molecular systems (two spaces)
+    if (cfg->density_matrices && (sys->kind != HGPU_SYS_READ_IN || cfg->nspaces != 2)) return HGPU_ERR_INVALID;
     // pattempt_parallel only with the spin-resolved generators, at most 1
     // (src/check_input.F90:212-218)
     {
@@ -733,6 +751,16 @@ int32_t hgpu_upload_walkers(hgpu_handle *h, const int64_t *states, const int64_t
     return set_list(h, states, pops, dat, n, dat == nullptr);
 }
 
+int32_t hgpu_rdm_download(hgpu_handle *h, double *rdm, int64_t capacity, int64_t *n_out) {
+    if (!h || !n_out) return HGPU_ERR_INVALID;
+    *n_out = h->b.rdm ? h->b.npairs * h->b.npairs : 0;
+    if (!h->b.rdm || !rdm) return HGPU_OK;  // a query of the size
+    if (capacity < *n_out) return HGPU_ERR_INVALID;
+    CK(cudaMemcpyAsync(rdm, h->b.rdm, sizeof(double) * (size_t)*n_out, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return HGPU_OK;
+}
+
 int32_t hgpu_download_walkers(hgpu_handle *h, int64_t *states, int64_t *pops, double *dat, int64_t capacity,
                               int64_t *n_out) {
     if (!h || !n_out) return HGPU_ERR_INVALID;
@@ -779,8 +807,31 @@ static int launch_one_cycle(hgpu_handle *h) {
     return HGPU_OK;
 }
 
+// The start of a report with density_matrices (src/fciqmc.f90:283-291): the RDM
+// is cleared once accumulating, and accumulating starts in the first report
+// after density_matrix_report in which every shift varies.
+static int begin_report(hgpu_handle *h) {
+    if (h->report_open) return HGPU_OK;
+    h->report_open = true;
+    if (!h->b.rdm) return HGPU_OK;
+    if (h->rdm_on)
+        CK(cudaMemsetAsync(h->b.rdm, 0, sizeof(double) * (size_t)(h->b.npairs * h->b.npairs), h->stream));
+    bool all_vary = true;
+    for (int s = 0; s < h->R; s++) all_vary = all_vary && h->vary_shift[s];
+    if (!h->rdm_on && all_vary && h->reports_done + 1 > h->cfg.density_matrix_report) {
+        h->rdm_on = 1;
+        CK(cudaMemcpyAsync(&h->b.state->rdm_on, &h->rdm_on, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    return HGPU_OK;
+}
+
 int32_t hgpu_run_cycles(hgpu_handle *h, int32_t ncycles) {
     if (!h || ncycles < 0) return HGPU_ERR_INVALID;
+    {
+        int rc = begin_report(h);
+        if (rc) return rc;
+    }
     CK(cudaEventRecord(h->ev0, h->stream));
     for (int k = 0; k < ncycles; k++) {
         int rc = launch_one_cycle(h);
@@ -885,6 +936,8 @@ int32_t hgpu_batch_run_cycles(hgpu_batch *b, int32_t ncycles) {
     if (!b || ncycles < 0) return HGPU_ERR_INVALID;
     std::vector<int> par(b->hs.size()), flip(b->hs.size());
     for (size_t i = 0; i < b->hs.size(); i++) {
+        int rc = begin_report(b->hs[i]);
+        if (rc) return rc;
         par[i] = b->hs[i]->cur;
         flip[i] = 1 - par[i];
         CK(cudaStreamSynchronize(b->hs[i]->stream));  // earlier per-handle work
@@ -938,10 +991,18 @@ int32_t hgpu_batch_destroy(hgpu_batch *b) {
 
 int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
     if (!h || !out) return HGPU_ERR_INVALID;
+    // calc_rdm_energy of the report's RDM (src/fciqmc.f90:409-411)
+    if (h->rdm_on) launch_rdm_energy(h->b, h->W, h->stream);
     DevState st;
     int rc = read_state(h, &st);
     if (rc) return rc;
     memset(out, 0, sizeof(*out));
+    if (h->rdm_on) {
+        out->rdm_energy = st.rdm_energy;
+        out->rdm_trace = st.rdm_trace;
+    }
+    h->reports_done++;
+    h->report_open = false;
     int R = h->R;
     int nc = st.rep_cycles > 0 ? st.rep_cycles : 1;
     double ntot[HGPU_MAX_SPACES] = {0, 0};

@@ -87,6 +87,7 @@ __global__ void k_set_count(int64_t *dst, const int64_t *a, int64_t mul, const i
 __global__ void k_cycle_begin(DevState *st, const DevSys *sys) {
     st->iter += 1;
     st->n_spawn = 0;
+    st->n_rdm = 0;
     st->spawn_next = 0;
     double np = (double)st->abs_pop[0] / (double)sys->real_factor;
     st->nattempts_cycle = llround(2.0 * np);
@@ -221,7 +222,8 @@ struct SpawnQueue {
 template <int W, int KIND, typename Real, bool SINGLE>
 __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
                                                const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
-                                               bool drew, uint64_t bufk, Det<W> &child, int &sp, uint32_t &info) {
+                                               bool drew, uint64_t bufk, bool rdm, Det<W> &child, int &sp,
+                                               uint32_t &info, Det<W> &parent_det, int64_t &nspawn_rdm) {
     constexpr bool single = SINGLE;
     int64_t i = slot / R;
     sp = (int)(slot - i * R);
@@ -251,8 +253,12 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
         else if (KIND == kKindHeatBathUniform) gen_heat_bath_uniform_double<W, Real>(s, rs, f, at, pgen, hm);
         else gen_double_mol<W, Real>(s, rs, d, KIND == HGPU_SYS_READ_IN, at, pgen, hm);
         attempt_to_spawn(s, rs, parent, pgen, (double)hm, at);
+        at.nspawn_rdm = 0;
+        if (rdm) attempt_to_spawn_rdm(s, rs, parent, at);
     }
-    if (at.nspawn != 0) child = excited<W>(f, at);
+    nspawn_rdm = KIND == HGPU_SYS_HUB_K ? 0 : at.nspawn_rdm;
+    parent_det = f;
+    if (at.nspawn != 0 || nspawn_rdm != 0) child = excited<W>(f, at);
     return at.nspawn;
 }
 
@@ -261,8 +267,10 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
 template <int W, int KIND, typename Real>
 __device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
                                                    const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
-                                                   uint64_t bufk, Det<W> &child, int &sp, uint32_t &info) {
-    return spawn_entry<W, KIND, Real, true>(s, t, b, R, dets, iter, slot, att, true, bufk, child, sp, info);
+                                                   uint64_t bufk, bool rdm, Det<W> &child, int &sp, uint32_t &info,
+                                                   Det<W> &parent_det, int64_t &nspawn_rdm) {
+    return spawn_entry<W, KIND, Real, true>(s, t, b, R, dets, iter, slot, att, true, bufk, rdm, child, sp, info,
+                                            parent_det, nspawn_rdm);
 }
 
 template <int W, int KIND, typename Real>
@@ -280,6 +288,8 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
     const uint64_t *dets = b.dets[cur];
     const int lane = threadIdx.x & 31;
     SpawnQueue &q = queue[threadIdx.x >> 5];
+    // replica 2-RDM sampling (spawn_rdm) once the engine turned it on
+    const bool rdm = b.rdm != nullptr && st->rdm_on != 0;
     // generators whose first draw is the single/double choice: the chunk is
     // split by that draw so that each excitation type runs with the warp
     // converged (a tenth of the attempts are singles, with their own code)
@@ -344,8 +354,8 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
             const uint8_t *list = pass == 0 ? q.dlist : q.slist;
             for (int j0 = 0; j0 < n; j0 += 32) {
                 bool want = false;
-                Det<W> child;
-                int64_t nspawn = 0;
+                Det<W> child, parent_det;
+                int64_t nspawn = 0, nrdm = 0;
                 int sp = 0;
                 uint64_t flagword = 0;
                 if (j0 + lane < n) {
@@ -353,10 +363,12 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
                     uint32_t info;
                     if (pass == 0)
                         nspawn = spawn_entry<W, KIND, Real, false>(s, t, b, R, dets, iter, q.slot[off], q.att[off],
-                                                                   drew, q.bufk[off], child, sp, info);
+                                                                   drew, q.bufk[off], rdm, child, sp, info,
+                                                                   parent_det, nrdm);
                     else
                         nspawn = spawn_entry_single<W, KIND, Real>(s, t, b, R, dets, iter, q.slot[off], q.att[off],
-                                                                   q.bufk[off], child, sp, info);
+                                                                   q.bufk[off], rdm, child, sp, info, parent_det,
+                                                                   nrdm);
                     if (nspawn != 0) {
                         want = true;
                         flagword = (uint64_t)((info >> 2) & 3u) | ((uint64_t)(cbase + off) << 2);
@@ -377,6 +389,28 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
                             if (b.sflag) b.sflag[pos] = flagword;
                         } else {
                             atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+                        }
+                    }
+                }
+                if (rdm) {
+                    // create_spawned_particle_replica_rdm: (parent, child) and the amount
+                    const uint32_t rball = __ballot_sync(FULL_MASK, nrdm != 0);
+                    if (rball) {
+                        const int leader = __ffs(rball) - 1;
+                        unsigned long long rbase = 0;
+                        if (lane == leader)
+                            rbase = atomicAdd((unsigned long long *)&st->n_rdm, (unsigned long long)__popc(rball));
+                        rbase = __shfl_sync(FULL_MASK, rbase, leader);
+                        if (nrdm != 0) {
+                            const int64_t pos = (int64_t)rbase + __popc(rball & lanemask_lt());
+                            if (pos < b.scap) {
+                                store_det<W>(b.rdm_sdets, 2 * pos, parent_det);
+                                store_det<W>(b.rdm_sdets, 2 * pos + 1, child);
+                                b.rdm_spops[pos] = nrdm;
+                                b.rdm_sspace[pos] = (uint8_t)sp;
+                            } else {
+                                atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+                            }
                         }
                     }
                 }
@@ -575,6 +609,8 @@ static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur
     if (pm) cudaEventRecord(pm->ev[3], st);
     launch_sort_annihilate(b, W, R, cur, st, pm);
     k_cycle_end<<<1, 1024, 0, st>>>(b, R, b.grid, 1);
+    // update_rdm_from_spawns on the new main list (src/fciqmc.f90:402-405)
+    if (b.rdm) launch_rdm_cycle(b, W, R, 1 - cur, st);
     if (pm) cudaEventRecord(pm->ev[7], st);
 }
 
@@ -592,6 +628,7 @@ int set_kernel_attributes(const DevBuffers &b) {
         cudaFuncSetAttribute(k_spawn<2, HGPU_SYS_HUB_K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              hub_max) != cudaSuccess)
         return 1;
+    if (set_rdm_attributes()) return 1;
     return set_annihilate_attributes(b);
 }
 

@@ -58,7 +58,12 @@ struct DevState {
     int32_t pad2;
     uint64_t spawn_next;  // next unclaimed attempt chunk of the spawning kernel
     uint32_t os_ticket[16];  // next tile of each radix pass (hgpu_sort.cuh)
-    uint32_t ann_ticket[2];  // next tile of each annihilation pass (hgpu_annihilate.cuh)
+    uint32_t ann_ticket[2];  // next tile of each annihilation pass (hgpu_annihilate.cu)
+    // replica 2-RDM (hgpu_rdm.cu)
+    int32_t rdm_on;          // spawn_rdm active (set by the host at a report's start)
+    int32_t pad4;
+    int64_t n_rdm;           // RDM spawns of the cycle
+    double rdm_energy, rdm_trace;  // calc_rdm_energy of the report
 };
 
 // Device buffers of one engine (all allocated once, at create).
@@ -101,6 +106,13 @@ struct DevBuffers {
     uint64_t *seg_status;  // per annihilation tile: look-back status word
     uint32_t *seg_epoch;   // look-back epoch of the annihilation (kept out of DevState)
     int splits_grid;       // blocks of k_ann_splits
+    // replica 2-RDM (hgpu_rdm.cu; null unless density_matrices)
+    double *rdm;            // [npairs][npairs], pairs p < q in tri_ind_distinct order
+    int64_t npairs;
+    uint64_t *rdm_sdets;    // per RDM spawn: parent words, child words (size scap)
+    int64_t *rdm_spops;     // per RDM spawn: amount
+    uint8_t *rdm_sspace;    // per RDM spawn: space of the parent
+    double *rdm_rows;       // [2][npairs]: per-row energy and diagonal of calc_rdm_energy
     // scan scratch and per-block partials
     int64_t *scan_part;     // kMaxBlocks * 2
     double *part_d;         // kMaxBlocks * 4 (proj, d0 per space)
@@ -140,5 +152,10 @@ void launch_eval_excitations(const DevBuffers &b, int W, int kind, int precision
 void launch_eval_diagonal(const DevBuffers &b, int W, const uint64_t *dets, int64_t n, double *kii, cudaStream_t st);
 void launch_load_fixed_spawns(const DevBuffers &b, int W, int R, const int64_t *sdata, int64_t n, cudaStream_t st);
 void launch_abs_pop(const DevBuffers &b, int R, int cur, cudaStream_t st);
+// Replica 2-RDM (hgpu_rdm.cu): the cycle's RDM spawns and diagonal into b.rdm
+// (main list in buffer cur), calc_rdm_energy into DevState, kernel attributes.
+void launch_rdm_cycle(const DevBuffers &b, int W, int R, int cur, cudaStream_t st);
+void launch_rdm_energy(const DevBuffers &b, int W, cudaStream_t st);
+int set_rdm_attributes();
 
 }  // namespace hgpu

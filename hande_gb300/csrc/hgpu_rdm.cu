@@ -1,0 +1,232 @@
+// hgpu_rdm.cu -- replica sampling of the two-body reduced density matrix
+// (src/replica_rdm.F90) on the device.
+//
+// With density_matrices, every allowed spawning attempt of replica s also
+// draws spawn_rdm's unweighted amount (src/spawning.F90:664-671) and records
+// (parent, child, amount) (create_spawned_particle_replica_rdm).  After the
+// annihilation of each cycle, update_rdm_from_spawns (src/replica_rdm.F90:84-159)
+// adds, for every recorded pair whose child is occupied, N_child^(other
+// replica) x amount / 2 to the RDM elements of the excitation child -> parent,
+// and every occupied determinant adds N^(1) N^(2) to its diagonal pairs.  The
+// reference first sums equal (parent, child) entries; the sum is linear, so
+// here every entry is added on its own (atomic FP64 additions: the RDM agrees
+// with the reference's to rounding).  At a report's end calc_rdm_energy
+// (src/replica_rdm.F90:215-264) contracts the RDM with the integrals: one block
+// per row, rows summed in a fixed order.
+#include "hgpu_common.cuh"
+
+namespace hgpu {
+
+// tri_ind_distinct_reorder (lib/local/utils.F90:579-611), 0-based orbitals and index.
+__device__ __forceinline__ int64_t tri_pair(int p, int q) {
+    const int64_t hi = p > q ? p : q, lo = p > q ? q : p;
+    return hi * (hi - 1) / 2 + lo;
+}
+
+// orbs_from_index (lib/local/utils.F90:613-628), 0-based: pair ind -> p < q.
+__device__ __forceinline__ void orbs_of_pair(int64_t ind, int &p, int &q) {
+    const int64_t i1 = ind + 1;
+    int qq = (int)(1.50 + sqrt((double)(2 * i1) - 1.750));
+    while ((int64_t)qq * (qq - 1) / 2 < i1) qq++;
+    while ((int64_t)(qq - 1) * (qq - 2) / 2 >= i1) qq--;
+    p = (int)(i1 - (int64_t)(qq - 1) * (qq - 2) / 2) - 1;
+    q = qq - 1;
+}
+
+// update_rdm (src/replica_rdm.F90:12-82) for a child f1 and its parent f2
+// (a single or double excitation apart).
+template <int W>
+__device__ __forceinline__ void rdm_add_pair(double *rdm, int64_t np, const Det<W> &f1, const Det<W> &f2, int nel,
+                                             double matel) {
+    const Excit e = get_excitation<W>(f1, f2, nel);
+    if (e.perm) matel = -matel;
+    if (e.nexcit == 2) {
+        atomicAdd(&rdm[tri_pair(e.to[0], e.to[1]) * np + tri_pair(e.from[0], e.from[1])], matel);
+    } else if (e.nexcit == 1) {
+        const int p = e.to[0], q = e.from[0];
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            for (uint64_t x = f1.w[w]; x; x &= x - 1) {
+                const int orb = 64 * w + __ffsll((long long)x) - 1;
+                if (orb == q) continue;
+                if (orb < p && orb < q) atomicAdd(&rdm[tri_pair(orb, p) * np + tri_pair(orb, q)], matel);
+                else if (orb > p && orb > q) atomicAdd(&rdm[tri_pair(orb, p) * np + tri_pair(q, orb)], matel);
+                else atomicAdd(&rdm[tri_pair(p, orb) * np + tri_pair(orb, q)], -matel);
+            }
+        }
+    }
+}
+
+// The cycle's RDM spawns against the new main list (buffer cur).
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_rdm_spawns(DevBuffers b, int R, int cur) {
+    const DevState *st = b.state;
+    if (!st->rdm_on) return;
+    const int64_t N = st->n_main;
+    const int64_t n = st->n_rdm < b.scap ? st->n_rdm : b.scap;
+    const uint64_t *dets = b.dets[cur];
+    const int64_t *pops = b.pops[cur];
+    const int nel = b.sys->nel;
+    const double inv_rf = 1.0 / (double)b.sys->real_factor;  // exact: a power of two
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const Det<W> fp = load_det<W>(b.rdm_sdets, 2 * k), fc = load_det<W>(b.rdm_sdets, 2 * k + 1);
+        const int64_t pos = lower_bound_det<W>(dets, N, fc);
+        if (pos >= N || !det_eq<W>(load_det<W>(dets, pos), fc)) continue;
+        const int s = b.rdm_sspace[k];
+        // pops(other replica, child) / real_factor x amount / real_factor / 2
+        const double pop1 = (double)pops[pos * R + (1 - s)] * inv_rf;
+        const double pop2 = (double)b.rdm_spops[k] * inv_rf;
+        rdm_add_pair<W>(b.rdm, b.npairs, fc, fp, nel, pop1 * pop2 / 2.0);
+    }
+}
+
+// The diagonal: N^(1) N^(2) of every occupied determinant on each of its
+// occupied pairs, summed per block in shared memory.
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_rdm_diag(DevBuffers b, int R, int cur) {
+    extern __shared__ double dsm[];  // [npairs]
+    const DevState *st = b.state;
+    if (!st->rdm_on) return;
+    const int64_t np = b.npairs;
+    for (int64_t k = threadIdx.x; k < np; k += blockDim.x) dsm[k] = 0.0;
+    __syncthreads();
+    const int64_t N = st->n_main;
+    const uint64_t *dets = b.dets[cur];
+    const int64_t *pops = b.pops[cur];
+    const double inv_rf = 1.0 / (double)b.sys->real_factor;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p0 = pops[i * R], p1 = pops[i * R + 1];
+        if (p0 == 0 || p1 == 0) continue;
+        const double matel = (double)p0 * inv_rf * ((double)p1 * inv_rf) / 1.0;
+        const Det<W> f = load_det<W>(dets, i);
+#pragma unroll
+        for (int wx = 0; wx < W; wx++) {
+            for (uint64_t x = f.w[wx]; x; x &= x - 1) {
+                const int px = 64 * wx + __ffsll((long long)x) - 1;
+                for (uint64_t y = x & (x - 1); y; y &= y - 1)
+                    atomicAdd(&dsm[tri_pair(64 * wx + __ffsll((long long)y) - 1, px)], matel);
+#pragma unroll
+                for (int wy = wx + 1; wy < W; wy++)
+                    for (uint64_t y = f.w[wy]; y; y &= y - 1)
+                        atomicAdd(&dsm[tri_pair(64 * wy + __ffsll((long long)y) - 1, px)], matel);
+            }
+        }
+    }
+    __syncthreads();
+    for (int64_t k = threadIdx.x; k < np; k += blockDim.x)
+        if (dsm[k] != 0.0) atomicAdd(&b.rdm[k * np + k], dsm[k]);
+}
+
+// get_two_e_int_mol (src/hamiltonian_molecular.f90:579-597): <ij||ab> with the
+// spin and symmetry checks of get_two_body_int_mol.
+__device__ __forceinline__ double rdm_two_e(const DevSys &s, int i, int j, int a, int b) {
+    const bool sym_ok = ((s.orbsym[i] ^ s.orbsym[j] ^ s.orbsym[a] ^ s.orbsym[b]) & (s.nsym - 1)) == 0;
+    double x = 0.0, y = 0.0;
+    if (sym_ok && ((i ^ a) & 1) == 0 && ((j ^ b) & 1) == 0) x = Ints<double>::v2(s, i, j, a, b);
+    if (sym_ok && ((i ^ b) & 1) == 0 && ((j ^ a) & 1) == 0) y = Ints<double>::v2(s, i, j, b, a);
+    return x - y;
+}
+
+// get_one_e_int_mol (src/hamiltonian_molecular.f90:599-617).
+__device__ __forceinline__ double rdm_one_e(const DevSys &s, int i, int j) {
+    if (s.orbsym[i] != s.orbsym[j] || ((i ^ j) & 1) != 0) return 0.0;
+    return s.h1[(i >> 1) * s.norb + (j >> 1)];
+}
+
+// calc_rdm_energy, one row per block iteration: the row's contribution and
+// its diagonal element into rdm_rows.
+__global__ void __launch_bounds__(kBlock) k_rdm_rows(DevBuffers b) {
+    __shared__ DevSys s;
+    __shared__ double red[kBlock];
+    stage_sys(s, b.sys);
+    __syncthreads();
+    if (!b.state->rdm_on) return;
+    const int64_t np = b.npairs;
+    const double nm1 = (double)(s.nel - 1);
+    for (int64_t row = blockIdx.x; row < np; row += gridDim.x) {
+        int a, bb;
+        orbs_of_pair(row, a, bb);
+        double e = 0.0;
+        for (int64_t j = threadIdx.x; j < np; j += blockDim.x) {
+            const double r = b.rdm[row * np + j];
+            if (fabs(r) < 1.0e-12) continue;  // depsilon (lib/local/const.F90)
+            int c, d;
+            orbs_of_pair(j, c, d);
+            e = e + r * rdm_two_e(s, a, bb, c, d);
+            if (a == c) e = e + r * rdm_one_e(s, bb, d) / nm1;
+            if (bb == d) e = e + r * rdm_one_e(s, a, c) / nm1;
+            if (a == d) e = e - r * rdm_one_e(s, bb, c) / nm1;
+            if (bb == c) e = e - r * rdm_one_e(s, a, d) / nm1;
+        }
+        red[threadIdx.x] = e;
+        __syncthreads();
+        for (int w = kBlock / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) red[threadIdx.x] = red[threadIdx.x] + red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            b.rdm_rows[row] = red[0];
+            b.rdm_rows[np + row] = b.rdm[row * np + row];
+        }
+        __syncthreads();
+    }
+}
+
+// The rows' sums in a fixed order: energy and trace (src/replica_rdm.F90:250-262).
+__global__ void __launch_bounds__(1024) k_rdm_final(DevBuffers b) {
+    __shared__ double re[1024], rt[1024];
+    DevState *st = b.state;
+    if (!st->rdm_on) return;
+    const int64_t np = b.npairs;
+    double e = 0.0, t = 0.0;
+    for (int64_t k = threadIdx.x; k < np; k += blockDim.x) {
+        e = e + b.rdm_rows[k];
+        t = t + b.rdm_rows[np + k];
+    }
+    re[threadIdx.x] = e;
+    rt[threadIdx.x] = t;
+    __syncthreads();
+    for (int w = 512; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            re[threadIdx.x] = re[threadIdx.x] + re[threadIdx.x + w];
+            rt[threadIdx.x] = rt[threadIdx.x] + rt[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const DevSys *s = b.sys;
+        double energy = re[0] * (double)s->nel * (double)(s->nel - 1) * 0.5;
+        energy = energy + (s->ecore - s->H00) * rt[0];
+        st->rdm_energy = energy;
+        st->rdm_trace = rt[0];
+    }
+}
+
+void launch_rdm_cycle(const DevBuffers &b, int W, int R, int cur, cudaStream_t st) {
+    const size_t dsm = sizeof(double) * (size_t)b.npairs;
+    if (W == 1) {
+        k_rdm_spawns<1><<<b.grid, kBlock, 0, st>>>(b, R, cur);
+        k_rdm_diag<1><<<b.grid, kBlock, dsm, st>>>(b, R, cur);
+    } else {
+        k_rdm_spawns<2><<<b.grid, kBlock, 0, st>>>(b, R, cur);
+        k_rdm_diag<2><<<b.grid, kBlock, dsm, st>>>(b, R, cur);
+    }
+}
+
+void launch_rdm_energy(const DevBuffers &b, int W, cudaStream_t st) {
+    (void)W;
+    const int rows = (int)(b.npairs < 4 * kMaxBlocks ? b.npairs : 4 * kMaxBlocks);
+    k_rdm_rows<<<rows > 0 ? rows : 1, kBlock, 0, st>>>(b);
+    k_rdm_final<<<1, 1024, 0, st>>>(b);
+}
+
+int set_rdm_attributes() {
+    // 128 spin orbitals: 8128 pairs
+    const int max_bytes = (int)sizeof(double) * (128 * 127 / 2);
+    if (cudaFuncSetAttribute(k_rdm_diag<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_bytes) != cudaSuccess ||
+        cudaFuncSetAttribute(k_rdm_diag<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_bytes) != cudaSuccess)
+        return 1;
+    return 0;
+}
+
+}  // namespace hgpu

@@ -23,7 +23,7 @@ EXPORTS = [
     "hgpu_end_report", "hgpu_run_report", "hgpu_get_state", "hgpu_set_state", "hgpu_checkpoint",
     "hgpu_restore", "hgpu_eval_excitations", "hgpu_annihilate_fixed", "hgpu_eval_diagonal",
     "hgpu_profile_cycle", "hgpu_snapshot", "hgpu_self_annihilate_noalloc",
-    "hgpu_batch_create", "hgpu_batch_run_cycles", "hgpu_batch_destroy",
+    "hgpu_batch_create", "hgpu_batch_run_cycles", "hgpu_batch_destroy", "hgpu_rdm_download",
 ]
 
 
@@ -55,6 +55,7 @@ def load_library(path: str = LIB_PATH):
     L.hgpu_initial_distribution.argtypes = [vp]
     L.hgpu_upload_walkers.argtypes = [vp, P(C.c_int64), P(C.c_int64), P(C.c_double), C.c_int64]
     L.hgpu_download_walkers.argtypes = [vp, P(C.c_int64), P(C.c_int64), P(C.c_double), C.c_int64, P(C.c_int64)]
+    L.hgpu_rdm_download.argtypes = [vp, P(C.c_double), C.c_int64, P(C.c_int64)]
     L.hgpu_run_cycles.argtypes = [vp, C.c_int32]
     L.hgpu_end_report.argtypes = [vp, P(HgpuReport)]
     L.hgpu_run_report.argtypes = [vp, P(HgpuReport)]
@@ -119,6 +120,18 @@ class Engine:
         self._check(self.L.hgpu_upload_walkers(self.h, _p(st, C.c_int64), _p(po, C.c_int64),
                                                None if da is None else _p(da, C.c_double), po.shape[0]),
                     "hgpu_upload_walkers")
+
+    def rdm(self):
+        """The replica 2-RDM of the current report, [pair][pair] (None without density_matrices)."""
+        n = C.c_int64()
+        self._check(self.L.hgpu_rdm_download(self.h, None, 0, C.byref(n)), "hgpu_rdm_download")
+        if n.value == 0:
+            return None
+        out = np.zeros(n.value)
+        m = C.c_int64()
+        self._check(self.L.hgpu_rdm_download(self.h, _p(out, C.c_double), n.value, C.byref(m)), "hgpu_rdm_download")
+        k = int(round(np.sqrt(n.value)))
+        return out.reshape(k, k)
 
     def walkers(self):
         n = C.c_int64()

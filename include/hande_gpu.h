@@ -138,6 +138,10 @@ typedef struct hgpu_config {
                                       |H| ratio of find_parallel_spin_prob_mol
                                       (src/qmc_common.F90:265-378); > 0 with other generators is
                                       refused, as check_input does (src/check_input.F90:212-218) */
+    int32_t density_matrices;      /* fciqmc_in%density_matrices: replica sampling of the 2-RDM
+                                      (src/replica_rdm.F90); needs nspaces = 2, molecular systems */
+    int32_t density_matrix_report; /* fciqmc_in%density_matrix_report: accumulate from the first
+                                      report after this one in which every shift varies */
 } hgpu_config;
 
 /* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */
@@ -156,6 +160,8 @@ typedef struct hgpu_report {
     int32_t error_flags;                     /* HGPU_FLAG_* */
     int32_t reserved0;
     double device_ms;                        /* device time of the report's cycles */
+    double rdm_energy;                       /* RDM energy numerator of the report (calc_rdm_energy) */
+    double rdm_trace;                        /* trace of the report's 2-RDM */
 } hgpu_report;
 
 typedef struct hgpu_handle hgpu_handle;
@@ -191,6 +197,15 @@ int32_t hgpu_upload_walkers(hgpu_handle *h, const int64_t *states, const int64_t
  * nothing is written when capacity < *n_out (status HGPU_ERR_INVALID). */
 int32_t hgpu_download_walkers(hgpu_handle *h, int64_t *states, int64_t *pops, double *dat,
                               int64_t capacity, int64_t *n_out);
+
+/* The replica 2-RDM of the current report (density_matrices; the RDM array of
+ * src/fciqmc.f90:134, rdm(p,q,r,s) in physical notation): rdm[row * npairs +
+ * col] with npairs = nbasis (nbasis - 1) / 2, rows and columns the pairs
+ * p < q of 0-based spin orbitals in tri_ind_distinct order (index q (q-1)/2 + p),
+ * not normalised.  *n_out receives npairs^2 (0 without an RDM); rdm = NULL only
+ * queries that size, and nothing is written when capacity is smaller
+ * (HGPU_ERR_INVALID). */
+int32_t hgpu_rdm_download(hgpu_handle *h, double *rdm, int64_t capacity, int64_t *n_out);
 
 /* Run ncycles Monte Carlo cycles (src/fciqmc.f90:293-413) on the device;
  * estimators accumulate until hgpu_end_report. */

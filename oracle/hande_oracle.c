@@ -155,6 +155,15 @@ struct oracle_ctx {
      * ija_w[(i*nb + j)*nb + a] = hb_ija%weights(a,j,i), ija_tot[i*nb + j] =
      * hb_ija%weights_tot(j,i), ijab_*[((i*nb + j)*nb + a)*nb + b] and
      * ijab_tot[(i*nb + j)*nb + a] likewise. */
+    /* replica 2-RDM (src/replica_rdm.F90): rdm[row * npairs + col], rows and
+     * columns the distinct spin-orbital pairs p < q in tri_ind_distinct order;
+     * the RDM spawns of a cycle hold (parent, child) words and R amplitudes */
+    int rdm_enabled, rdm_on, reports_done;
+    int64_t npairs, rsn;
+    double *rdm;
+    uint64_t *rsdets;
+    int64_t *rspops;
+    double rdm_energy, rdm_trace;
     int hb_on;
     double *hb_i_w, *hb_ij_w, *hb_ija_w, *hb_ija_tot, *hb_ija_U, *hb_ijab_w, *hb_ijab_tot, *hb_ijab_U;
     int32_t *hb_ija_K, *hb_ijab_K;
@@ -735,6 +744,7 @@ typedef struct {
     double pgen, hmatel;
     int allowed;
     int64_t nspawn;
+    int64_t nspawn_rdm; /* spawn_rdm's unweighted attempt (src/spawning.F90:588-676) */
 } attempt_t;
 
 /* stochastic_round_spawned_particle (src/stoch_utils.f90:87-136). */
@@ -1244,6 +1254,16 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
     int64_t nspawn = round_spawned(c->cutoff, pspawn, rs);
     if (nspawn > 0) nspawn = child_sign(hmatel, parent, nspawn);
     out->nspawn = nspawn;
+    /* spawn_rdm: attempt_to_spawn with tau = 1 and hmatel = -1 for the replica
+     * sampling of the 2-RDM, after the spawn itself (src/spawning.F90:664-671) */
+    out->nspawn_rdm = 0;
+    if (c->rdm_on && out->allowed) {
+        double prdm = 1.0 * fabs(-1.0) / pgen;
+        prdm = prdm * (double)c->real_factor;
+        int64_t nr = round_spawned(c->cutoff, prdm, rs);
+        if (nr > 0) nr = child_sign(-1.0, parent, nr);
+        out->nspawn_rdm = nr;
+    }
 }
 
 static void decode_any(const oracle_ctx *c, const uint64_t *f, det_info *d) {
@@ -1699,6 +1719,180 @@ static double nparticles(const oracle_ctx *c, int s) {
     return (double)abs_pop_sum(c, s) / (double)c->real_factor;
 }
 
+/* ------------------------------------------------------------------------- */
+/* Replica 2-RDM (src/replica_rdm.F90)                                        */
+/* ------------------------------------------------------------------------- */
+
+/* tri_ind_distinct_reorder (lib/local/utils.F90:579-611), 0-based orbitals and index. */
+static inline int64_t tri_pair(int p, int q) {
+    int64_t hi = p > q ? p : q, lo = p > q ? q : p;
+    return hi * (hi - 1) / 2 + lo;
+}
+
+/* create_spawned_particle_replica_rdm (src/spawning.F90:2019-2061). */
+static void add_rdm_spawn(oracle_ctx *c, const uint64_t *parent, const uint64_t *child, int s, int64_t n) {
+    if (c->rsn >= c->scap) {
+        c->error_flags |= HGPU_FLAG_SPAWN_OVERFLOW;
+        return;
+    }
+    int64_t k = c->rsn++;
+    memcpy(&c->rsdets[k * 2 * c->nw], parent, sizeof(uint64_t) * c->nw);
+    memcpy(&c->rsdets[k * 2 * c->nw + c->nw], child, sizeof(uint64_t) * c->nw);
+    for (int t = 0; t < c->R; t++) c->rspops[k * c->R + t] = 0;
+    c->rspops[k * c->R + s] = n;
+}
+
+/* update_rdm (src/replica_rdm.F90:12-82): one pair of determinants. */
+static void update_rdm(oracle_ctx *c, const uint64_t *f1, const uint64_t *f2, const int *occ1, double pop1,
+                       double pop2, double prob) {
+    excit_t e = get_excitation(c, f1, f2);
+    double matel = pop1 * pop2 / prob;
+    if (e.perm) matel = -matel;
+    const int64_t np = c->npairs;
+    if (e.nexcit == 0) {
+        for (int i = 0; i < c->nel; i++)
+            for (int j = i + 1; j < c->nel; j++) {
+                int64_t ind = tri_pair(occ1[i], occ1[j]);
+                c->rdm[ind * np + ind] = c->rdm[ind * np + ind] + matel;
+            }
+    } else if (e.nexcit == 1) {
+        int p = e.to[0], q = e.from[0];
+        for (int i = 0; i < c->nel; i++) {
+            int orb = occ1[i];
+            if (orb == q) continue;
+            if (orb < p && orb < q) {
+                int64_t k = tri_pair(orb, p) * np + tri_pair(orb, q);
+                c->rdm[k] = c->rdm[k] + matel;
+            } else if (orb > p && orb > q) {
+                int64_t k = tri_pair(orb, p) * np + tri_pair(q, orb);
+                c->rdm[k] = c->rdm[k] + matel;
+            } else {
+                int64_t k = tri_pair(p, orb) * np + tri_pair(orb, q);
+                c->rdm[k] = c->rdm[k] - matel;
+            }
+        }
+    } else if (e.nexcit == 2) {
+        int64_t k = tri_pair(e.to[0], e.to[1]) * np + tri_pair(e.from[0], e.from[1]);
+        c->rdm[k] = c->rdm[k] + matel;
+    }
+}
+
+static const oracle_ctx *g_rdm_ctx;
+
+static int cmp_rdm_spawn(const void *x, const void *y) {
+    const oracle_ctx *c = g_rdm_ctx;
+    int64_t i = *(const int64_t *)x, j = *(const int64_t *)y;
+    int r = det_cmp(&c->rsdets[i * 2 * c->nw], &c->rsdets[j * 2 * c->nw], 2 * c->nw);
+    if (r != 0) return r == 1 ? -1 : 1;
+    return i < j ? -1 : (i > j ? 1 : 0);
+}
+
+/* update_rdm_from_spawns (src/replica_rdm.F90:84-159): the RDM spawns sorted
+ * by (parent, child) words and annihilated (annihilate_wrapper_spawn_t), each
+ * found in the main list through its child, then the diagonal of every
+ * occupied determinant. */
+static void update_rdm_from_spawns(oracle_ctx *c) {
+    const int nw = c->nw, R = c->R;
+    int64_t n = c->rsn;
+    if (n > 0) {
+        int64_t *perm = (int64_t *)malloc(sizeof(int64_t) * n);
+        uint64_t *d2 = (uint64_t *)malloc(sizeof(uint64_t) * 2 * nw * n);
+        int64_t *p2 = (int64_t *)malloc(sizeof(int64_t) * R * n);
+        for (int64_t i = 0; i < n; i++) perm[i] = i;
+        g_rdm_ctx = c;
+        qsort(perm, (size_t)n, sizeof(int64_t), cmp_rdm_spawn);
+        /* sort, then sum equal keys and drop the ones that sum to zero */
+        int64_t m = -1;
+        for (int64_t k = 0; k < n; k++) {
+            const uint64_t *key = &c->rsdets[perm[k] * 2 * nw];
+            if (m >= 0 && det_cmp(&d2[m * 2 * nw], key, 2 * nw) == 0) {
+                for (int t = 0; t < R; t++) p2[m * R + t] += c->rspops[perm[k] * R + t];
+                continue;
+            }
+            if (m >= 0 && all_zero(&p2[m * R], R)) m--;
+            m++;
+            memcpy(&d2[m * 2 * nw], key, sizeof(uint64_t) * 2 * nw);
+            for (int t = 0; t < R; t++) p2[m * R + t] = c->rspops[perm[k] * R + t];
+        }
+        if (m >= 0 && all_zero(&p2[m * R], R)) m--;
+        int64_t istart = 0, iend = c->n - 1;
+        int occ[MAXEL];
+        for (int64_t k = 0; k <= m; k++) {
+            const uint64_t *fp = &d2[k * 2 * nw], *fc = &d2[k * 2 * nw + nw];
+            int hit;
+            int64_t pos = bsearch_main(c, fc, istart, iend, &hit);
+            if (hit) {
+                decode(c, fc, occ);
+                for (int sp = 0; sp < 2; sp++)
+                    update_rdm(c, fc, fp, occ, (double)c->pops[pos * R + sp] / (double)c->real_factor,
+                               (double)p2[k * R + (1 - sp)] / (double)c->real_factor, 2.0);
+            }
+            istart = pos;
+        }
+        free(perm); free(d2); free(p2);
+    }
+    int occ[MAXEL];
+    for (int64_t i = 0; i < c->n; i++) {
+        const uint64_t *f = &c->dets[i * nw];
+        decode(c, f, occ);
+        update_rdm(c, f, f, occ, (double)c->pops[i * R + 0] / (double)c->real_factor,
+                   (double)c->pops[i * R + 1] / (double)c->real_factor, 1.0);
+    }
+    c->rsn = 0;
+}
+
+/* get_two_e_int_mol (src/hamiltonian_molecular.f90:579-597): <ij||ab> with the
+ * spin and symmetry checks of get_two_body_int_mol. */
+static double two_e_int(const oracle_ctx *c, int i, int j, int a, int b) {
+    int sym_ok = ((c->orb_sym[i] ^ c->orb_sym[j] ^ c->orb_sym[a] ^ c->orb_sym[b]) & (c->nsym - 1)) == 0;
+    double x = 0.0, y = 0.0;
+    if (sym_ok && c->orb_ms[i] == c->orb_ms[a] && c->orb_ms[j] == c->orb_ms[b]) x = v2_get(c, i, j, a, b);
+    if (sym_ok && c->orb_ms[i] == c->orb_ms[b] && c->orb_ms[j] == c->orb_ms[a]) y = v2_get(c, i, j, b, a);
+    return x - y;
+}
+
+/* get_one_e_int_mol (src/hamiltonian_molecular.f90:599-617). */
+static double one_e_int(const oracle_ctx *c, int i, int j) {
+    if (c->orb_sym[i] != c->orb_sym[j] || c->orb_ms[i] != c->orb_ms[j]) return 0.0;
+    return h1_get(c, i, j);
+}
+
+/* orbs_from_index (lib/local/utils.F90:613-628), 0-based index and orbitals. */
+static void orbs_of_pair(int64_t ind, int *p, int *q) {
+    int64_t i1 = ind + 1;
+    int qq = (int)(1.50 + sqrt((double)(2 * i1) - 1.750));
+    int pp = (int)(i1 - ((int64_t)(qq - 1) * (qq - 2)) / 2);
+    *p = pp - 1;
+    *q = qq - 1;
+}
+
+/* calc_rdm_energy (src/replica_rdm.F90:215-264). */
+static void calc_rdm_energy(oracle_ctx *c, double *energy, double *trace) {
+    const int64_t np = c->npairs;
+    double tr = 0.0, e = 0.0;
+    for (int64_t i = 0; i < np; i++) tr = tr + c->rdm[i * np + i];
+    const double nm1 = (double)(c->nel - 1);
+    for (int64_t i = 0; i < np; i++) {
+        int a, b;
+        orbs_of_pair(i, &a, &b);
+        for (int64_t j = 0; j < np; j++) {
+            double r = c->rdm[i * np + j];
+            if (fabs(r) < DEPSILON) continue;
+            int cc, d;
+            orbs_of_pair(j, &cc, &d);
+            e = e + r * two_e_int(c, a, b, cc, d);
+            if (a == cc) e = e + r * one_e_int(c, b, d) / nm1;
+            if (b == d) e = e + r * one_e_int(c, a, cc) / nm1;
+            if (a == d) e = e - r * one_e_int(c, b, cc) / nm1;
+            if (b == cc) e = e - r * one_e_int(c, a, d) / nm1;
+        }
+    }
+    e = e * (double)c->nel * (double)(c->nel - 1) * 0.5;
+    e = e + (c->ecore - c->H00) * tr;
+    *energy = e;
+    *trace = tr;
+}
+
 static void mc_cycle(oracle_ctx *c) {
     c->iter++;
     /* init_mc_cycle (src/qmc_common.F90:950-1017) */
@@ -1725,10 +1919,15 @@ static void mc_cycle(oracle_ctx *c) {
             for (int64_t a = 0; a < nat; a++) {
                 attempt_t at;
                 rs_init(&rs, (uint64_t)c->cfg.seed, P_SPAWN, s, (uint64_t)idet, (uint64_t)a, (uint64_t)c->iter);
+                at.nspawn_rdm = 0;
                 attempt(c, &rs, f, &d, parent, &at, 0);
                 if (at.nspawn != 0) {
                     excited_det(c, f, &at.e, child);
                     add_spawn(c, child, s, at.nspawn, c->cfg.initiator_approx ? flag : 0, c->sn);
+                }
+                if (at.nspawn_rdm != 0) {
+                    excited_det(c, f, &at.e, child);
+                    add_rdm_spawn(c, f, child, s, at.nspawn_rdm);
                 }
             }
             rs_init(&rs, (uint64_t)c->cfg.seed, P_DEATH, s, (uint64_t)idet, 0, (uint64_t)c->iter);
@@ -1738,6 +1937,7 @@ static void mc_cycle(oracle_ctx *c) {
     int64_t nspawn_events = c->sn; /* calc_events_spawn_t */
     c->rep_spawned += c->sn;
     direct_annihilation(c);
+    if (c->rdm_on) update_rdm_from_spawns(c);
     c->last_nspawn_events = nspawn_events;
     /* end_mc_cycle / spawning_rate (src/qmc_common.F90:1240-1304) */
     if (nattempts_acc > 0)
@@ -1875,6 +2075,17 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
     c->sord = (int64_t *)calloc((size_t)c->scap, sizeof(int64_t));
     c->suid = (int64_t *)calloc((size_t)c->scap, sizeof(int64_t));
     for (int s = 0; s < 2; s++) c->shift[s] = cfg->initial_shift;
+    if (cfg->density_matrices) {
+        if (c->kind != HGPU_SYS_READ_IN || c->R != 2) {
+            oracle_destroy(c);
+            return NULL;
+        }
+        c->rdm_enabled = 1;
+        c->npairs = (int64_t)c->nbasis * (c->nbasis - 1) / 2;
+        c->rdm = (double *)calloc((size_t)(c->npairs * c->npairs), sizeof(double));
+        c->rsdets = (uint64_t *)calloc((size_t)(c->scap * 2 * c->nw), sizeof(uint64_t));
+        c->rspops = (int64_t *)calloc((size_t)(c->scap * c->R), sizeof(int64_t));
+    }
     return c;
 }
 
@@ -1885,6 +2096,7 @@ void oracle_destroy(oracle_ctx *c) {
     free(c->fx_h1); free(c->fx_J); free(c->fx_JK); free(c->fx_eps);
     free(c->dets); free(c->pops); free(c->kii);
     free(c->sdets); free(c->spops); free(c->sflag); free(c->sord); free(c->suid);
+    free(c->rdm); free(c->rsdets); free(c->rspops);
     free(c->hb_i_w); free(c->hb_ij_w); free(c->hb_ija_w); free(c->hb_ija_tot); free(c->hb_ija_U);
     free(c->hb_ija_K); free(c->hb_ijab_w); free(c->hb_ijab_tot); free(c->hb_ijab_U); free(c->hb_ijab_K);
     free(c);
@@ -1924,6 +2136,15 @@ int64_t oracle_get_walkers(oracle_ctx *c, int64_t *states, int64_t *pops, double
 }
 
 int oracle_run_cycles(oracle_ctx *c, int32_t ncycles) {
+    if (c->rep_cycles == 0 && c->rdm_enabled) {
+        /* start of a report (src/fciqmc.f90:283-291): clear the RDM once
+         * accumulating; start accumulating after density_matrix_report reports
+         * once every shift varies */
+        if (c->rdm_on) memset(c->rdm, 0, sizeof(double) * (size_t)(c->npairs * c->npairs));
+        int all_vary = 1;
+        for (int s = 0; s < c->R; s++) all_vary = all_vary && c->vary_shift[s];
+        if (all_vary && c->reports_done + 1 > c->cfg.density_matrix_report) c->rdm_on = 1;
+    }
     for (int k = 0; k < ncycles; k++) mc_cycle(c);
     return c->error_flags ? (c->error_flags & HGPU_FLAG_SPAWN_OVERFLOW ? HGPU_ERR_SPAWN_OVERFLOW
                                                                        : HGPU_ERR_MAIN_OVERFLOW)
@@ -1935,6 +2156,12 @@ int oracle_run_cycles(oracle_ctx *c, int32_t ncycles) {
 int oracle_end_report(oracle_ctx *c, hgpu_report *out) {
     int nc = c->rep_cycles > 0 ? c->rep_cycles : 1;
     memset(out, 0, sizeof(*out));
+    if (c->rdm_on) {
+        calc_rdm_energy(c, &c->rdm_energy, &c->rdm_trace);
+        out->rdm_energy = c->rdm_energy;
+        out->rdm_trace = c->rdm_trace;
+    }
+    c->reports_done++;
     double ntot[2];
     for (int s = 0; s < c->R; s++) {
         out->proj_energy[s] = c->acc_proj[s] / (double)nc;
@@ -2047,6 +2274,24 @@ double oracle_hmatel(oracle_ctx *c, const int64_t *f1, const int64_t *f2) {
 double oracle_sc0(oracle_ctx *c, const int64_t *f) { return sc0(c, (const uint64_t *)f); }
 
 double oracle_pattempt_parallel(oracle_ctx *c) { return c->spin_ij ? c->pattempt_parallel : -1.0; }
+
+int64_t oracle_rdm(oracle_ctx *c, double *out, int64_t n) {
+    if (!c->rdm_enabled) return 0;
+    int64_t m = c->npairs * c->npairs;
+    if (out && n >= m) memcpy(out, c->rdm, sizeof(double) * (size_t)m);
+    return m;
+}
+
+void oracle_rdm_energy(oracle_ctx *c, double *energy, double *trace) {
+    *energy = *trace = 0.0;
+    if (c->rdm_enabled) calc_rdm_energy(c, energy, trace);
+}
+
+void oracle_rdm_from_list(oracle_ctx *c) {
+    if (!c->rdm_enabled) return;
+    c->rsn = 0;
+    update_rdm_from_spawns(c);
+}
 
 double oracle_pgen(oracle_ctx *c, const int64_t *fi, const int32_t *orbs) {
     const uint64_t *f = (const uint64_t *)fi;

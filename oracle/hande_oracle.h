@@ -49,6 +49,14 @@ double oracle_sc0(oracle_ctx *c, const int64_t *f);
 double oracle_pgen(oracle_ctx *c, const int64_t *f, const int32_t *orbs);
 /* pattempt_parallel of the spin-resolved generators (negative for the others). */
 double oracle_pattempt_parallel(oracle_ctx *c);
+/* Replica 2-RDM (density_matrices): copies the current report's RDM
+ * ([pair][pair], pairs p < q in tri_ind_distinct order) into out when n is
+ * large enough and returns its element count (0 when not enabled); its
+ * calc_rdm_energy; and, for tests, the diagonal contribution of the current
+ * main list (update_rdm_from_spawns without spawns). */
+int64_t oracle_rdm(oracle_ctx *c, double *out, int64_t n);
+void oracle_rdm_energy(oracle_ctx *c, double *energy, double *trace);
+void oracle_rdm_from_list(oracle_ctx *c);
 /* Counters of the last cycles (spawn attempts etc.). */
 int64_t oracle_total_attempts(oracle_ctx *c);
 /* Philox4x32-10 uniform, for cross-checking the device generator. */

@@ -53,6 +53,10 @@ def lib():
         L.oracle_hmatel.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
         L.oracle_sc0.restype = C.c_double
         L.oracle_sc0.argtypes = [C.c_void_p, P(C.c_int64)]
+        L.oracle_rdm.restype = C.c_int64
+        L.oracle_rdm.argtypes = [C.c_void_p, P(C.c_double), C.c_int64]
+        L.oracle_rdm_energy.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+        L.oracle_rdm_from_list.argtypes = [C.c_void_p]
         L.oracle_pattempt_parallel.restype = C.c_double
         L.oracle_pattempt_parallel.argtypes = [C.c_void_p]
         L.oracle_pgen.restype = C.c_double
@@ -166,6 +170,21 @@ class Oracle:
 
     def sc0(self, f) -> float:
         return self.L.oracle_sc0(self.h, _i64(f))
+
+    def rdm(self):
+        m = self.L.oracle_rdm(self.h, None, 0)
+        out = np.zeros(m)
+        self.L.oracle_rdm(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), m)
+        n = int(round(np.sqrt(m)))
+        return out.reshape(n, n)
+
+    def rdm_energy(self):
+        e, t = C.c_double(), C.c_double()
+        self.L.oracle_rdm_energy(self.h, C.byref(e), C.byref(t))
+        return e.value, t.value
+
+    def rdm_from_list(self):
+        self.L.oracle_rdm_from_list(self.h)
 
     def pattempt_parallel(self) -> float:
         return self.L.oracle_pattempt_parallel(self.h)

@@ -155,6 +155,10 @@ void launch_abs_pop(const DevBuffers &b, int R, int cur, cudaStream_t st);
 // Replica 2-RDM (hgpu_rdm.cu): the cycle's RDM spawns and diagonal into b.rdm
 // (main list in buffer cur), calc_rdm_energy into DevState, kernel attributes.
 void launch_rdm_cycle(const DevBuffers &b, int W, int R, int cur, cudaStream_t st);
+// The spawning kernel of molecular systems that also records the RDM spawns
+// (hgpu_spawn_rdm.cu); sm = its dynamic shared memory.
+void launch_spawn_rdm(const DevBuffers &b, int W, int R, int kind, int precision, int cur, size_t sm,
+                      cudaStream_t st);
 void launch_rdm_energy(const DevBuffers &b, int W, cudaStream_t st);
 int set_rdm_attributes();
 

@@ -1,0 +1,242 @@
+// hgpu_spawn.cuh -- the spawning kernel of one cycle: excitation generation,
+// attempt_to_spawn and the append to the spawned list (src/spawning.F90:34-123,
+// 215-315, 588-768), templated on the system / generator kind, the arithmetic
+// of the generators and whether replica 2-RDM spawns are recorded.  Included by
+// the translation units that instantiate it (hgpu_kernels.cu without the RDM,
+// hgpu_spawn_rdm.cu with it).
+#pragma once
+
+#include "hgpu_common.cuh"
+
+namespace hgpu {
+
+// first k in [0, n) with off[k] > a (off is the inclusive scan of attempts)
+__device__ __forceinline__ int64_t upper_bound_off(const int64_t *off, int64_t n, int64_t a) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (off[mid] > a) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// Attempts per chunk a warp claims from the spawning kernel's work counter.
+constexpr int kSpawnChunk = 8 * 32;
+
+// A warp's chunk of attempts: (parent, space) slot, attempt number in the slot
+// and, for generators whose first draw chooses a single or a double excitation,
+// the stream position after that draw; dlist/slist hold the chunk offsets of
+// the doubles (or of every attempt) and of the singles.
+struct SpawnQueue {
+    uint32_t slot[kSpawnChunk];
+    uint32_t att[kSpawnChunk];
+    uint64_t bufk[kSpawnChunk];
+    uint8_t dlist[kSpawnChunk];
+    uint8_t slist[kSpawnChunk];
+};
+
+// One spawning attempt of a queued chunk entry; returns the spawned amount.
+template <int W, int KIND, typename Real, bool SINGLE>
+__device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
+                                               const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
+                                               bool drew, uint64_t bufk, bool rdm, Det<W> &child, int &sp,
+                                               uint32_t &info, Det<W> &parent_det, int64_t &nspawn_rdm) {
+    constexpr bool single = SINGLE;
+    int64_t i = slot / R;
+    sp = (int)(slot - i * R);
+    Det<W> f = load_det<W>(dets, i);
+    info = b.pinfo[i];
+    int64_t parent = (info >> sp) & 1u ? -1 : 1;
+    RStream rs;
+    rs.init(s.seed, P_SPAWN, sp, i, att, iter);
+    if (drew) {  // resume after the single/double draw
+        rs.block = 1;
+        rs.have = true;
+        rs.bufk = bufk;
+    }
+    Attempt at;
+    at.from[0] = at.from[1] = at.to[0] = at.to[1] = -1;
+    if (KIND == HGPU_SYS_HUB_K) {
+        attempt_hub_k<W>(s, t, rs, f, parent, false, at);
+    } else {
+        MolDet<W> d;
+        mol_decode<W>(s, f, d);
+        double pgen;
+        Real hm;
+        if (KIND == kKindHeatBath) gen_heat_bath<W, Real>(s, rs, f, at, pgen, hm);
+        else if (single && KIND == kKindHeatBathUniform && s.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE)
+            gen_single_hb_exact<W, Real>(s, rs, d, at, pgen, hm);
+        else if (single) gen_single_mol<W, Real>(s, rs, d, KIND != kKindReadInNoRenorm, at, pgen, hm);
+        else if (KIND == kKindHeatBathUniform) gen_heat_bath_uniform_double<W, Real>(s, rs, f, at, pgen, hm);
+        else gen_double_mol<W, Real>(s, rs, d, KIND == HGPU_SYS_READ_IN, at, pgen, hm);
+        attempt_to_spawn(s, rs, parent, pgen, (double)hm, at);
+        at.nspawn_rdm = 0;
+        if (rdm) attempt_to_spawn_rdm(s, rs, parent, at);
+    }
+    nspawn_rdm = KIND == HGPU_SYS_HUB_K ? 0 : at.nspawn_rdm;
+    parent_det = f;
+    if (at.nspawn != 0 || nspawn_rdm != 0) child = excited<W>(f, at);
+    return at.nspawn;
+}
+
+// The singles (a tenth of the attempts) in a function of their own, so that the
+// doubles' loop in k_spawn stays small in the instruction cache.
+template <int W, int KIND, typename Real>
+__device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
+                                                   const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
+                                                   uint64_t bufk, bool rdm, Det<W> &child, int &sp, uint32_t &info,
+                                                   Det<W> &parent_det, int64_t &nspawn_rdm) {
+    return spawn_entry<W, KIND, Real, true>(s, t, b, R, dets, iter, slot, att, true, bufk, rdm, child, sp, info,
+                                            parent_det, nspawn_rdm);
+}
+
+template <int W, int KIND, typename Real, bool RDM>
+__global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) {
+    __shared__ DevSys s;
+    __shared__ SpawnQueue queue[kBlock / 32];
+    extern __shared__ uint8_t smem[];
+    stage_sys(s, b.sys);
+    HubTables t = stage_hub(b.sys, smem);
+    __syncthreads();
+    DevState *st = b.state;
+    const int64_t A = st->n_attempts;
+    const int64_t NR = st->n_main * R;
+    const uint64_t iter = (uint64_t)st->iter;
+    const uint64_t *dets = b.dets[cur];
+    const int lane = threadIdx.x & 31;
+    SpawnQueue &q = queue[threadIdx.x >> 5];
+    // replica 2-RDM sampling (spawn_rdm) once the engine turned it on; the
+    // kernels without it (RDM false) carry none of its code
+    const bool rdm = RDM && b.rdm != nullptr && st->rdm_on != 0;
+    // generators whose first draw is the single/double choice: the chunk is
+    // split by that draw so that each excitation type runs with the warp
+    // converged (a tenth of the attempts are singles, with their own code)
+    constexpr bool drew = KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm || KIND == kKindHeatBathUniform;
+    // Each warp claims chunks of kSpawnChunk consecutive attempts.  The (parent,
+    // space) slot of attempt a is the first k with aoff[k] > a; one binary search
+    // per chunk finds the slot of its first attempt, and every later step of 32
+    // attempts searches a window of 32 slots starting at the slot of the previous
+    // step's last attempt (a lower bound), with the binary search as fallback when
+    // a window holds no slot for an attempt (runs of zero-attempt slots).
+    for (;;) {
+        unsigned long long cbase = 0;
+        if (lane == 0) cbase = atomicAdd((unsigned long long *)&st->spawn_next, (unsigned long long)kSpawnChunk);
+        cbase = __shfl_sync(FULL_MASK, cbase, 0);
+        if ((int64_t)cbase >= A) break;
+        const int64_t cend = min((int64_t)cbase + kSpawnChunk, A);
+        int64_t k0 = 0;
+        if (lane == 0) k0 = upper_bound_off(b.aoff, NR, (int64_t)cbase);
+        k0 = __shfl_sync(FULL_MASK, k0, 0);
+        int nd = 0, ns = 0;
+        for (int64_t base = (int64_t)cbase; base < cend; base += 32) {
+            int64_t a = base + lane;
+            int64_t wv = k0 + lane < NR ? b.aoff[k0 + lane] : INT64_MAX;
+            uint32_t le_mask = 0;
+#pragma unroll 1
+            for (int m = 0; m < 32; m++) {
+                int64_t v = __shfl_sync(FULL_MASK, wv, m);
+                if (v <= a) le_mask |= 1u << m;
+            }
+            int64_t k = NR;
+            bool valid = a < cend, single = false;
+            if (valid) {
+                int cnt = __popc(le_mask);
+                k = (cnt < 32 && k0 + cnt < NR) ? k0 + cnt : upper_bound_off(b.aoff, NR, a);
+                int64_t att = a - (k > 0 ? b.aoff[k - 1] : 0);
+                int off = (int)(a - (int64_t)cbase);
+                q.slot[off] = (uint32_t)k;
+                q.att[off] = (uint32_t)att;
+                if (drew) {
+                    int64_t i = k / R;
+                    RStream rs;
+                    rs.init(s.seed, P_SPAWN, (uint32_t)(k - i * R), i, att, iter);
+                    single = rs.next_k() < s.t_single;  // rs.next() < pattempt_single
+                    q.bufk[off] = rs.bufk;
+                }
+            }
+            uint32_t dball = __ballot_sync(FULL_MASK, valid && !single);
+            uint32_t sball = __ballot_sync(FULL_MASK, valid && single);
+            int off = (int)(a - (int64_t)cbase);
+            if (valid && !single) q.dlist[nd + __popc(dball & lanemask_lt())] = (uint8_t)off;
+            if (valid && single) q.slist[ns + __popc(sball & lanemask_lt())] = (uint8_t)off;
+            nd += __popc(dball);
+            ns += __popc(sball);
+            // slot of the last valid attempt of this step: lower bound for the next step
+            int last = (int)min((int64_t)31, cend - 1 - base);
+            k0 = __shfl_sync(FULL_MASK, k, last);
+        }
+        __syncwarp();
+        // doubles (or every attempt), then singles, 32 at a time
+        for (int pass = 0; pass < 2; pass++) {
+            const int n = pass == 0 ? nd : ns;
+            const uint8_t *list = pass == 0 ? q.dlist : q.slist;
+            for (int j0 = 0; j0 < n; j0 += 32) {
+                bool want = false;
+                Det<W> child, parent_det;
+                int64_t nspawn = 0, nrdm = 0;
+                int sp = 0;
+                uint64_t flagword = 0;
+                if (j0 + lane < n) {
+                    int off = list[j0 + lane];
+                    uint32_t info;
+                    if (pass == 0)
+                        nspawn = spawn_entry<W, KIND, Real, false>(s, t, b, R, dets, iter, q.slot[off], q.att[off],
+                                                                   drew, q.bufk[off], rdm, child, sp, info,
+                                                                   parent_det, nrdm);
+                    else
+                        nspawn = spawn_entry_single<W, KIND, Real>(s, t, b, R, dets, iter, q.slot[off], q.att[off],
+                                                                   q.bufk[off], rdm, child, sp, info, parent_det,
+                                                                   nrdm);
+                    if (nspawn != 0) {
+                        want = true;
+                        flagword = (uint64_t)((info >> 2) & 3u) | ((uint64_t)(cbase + off) << 2);
+                    }
+                }
+                uint32_t ball = __ballot_sync(FULL_MASK, want);
+                if (ball) {
+                    int leader = __ffs(ball) - 1;
+                    unsigned long long basepos = 0;
+                    if (lane == leader)
+                        basepos = atomicAdd((unsigned long long *)&st->n_spawn, (unsigned long long)__popc(ball));
+                    basepos = __shfl_sync(FULL_MASK, basepos, leader);
+                    if (want) {
+                        int64_t pos = (int64_t)basepos + __popc(ball & lanemask_lt());
+                        if (pos < b.scap) {
+                            store_det<W>(b.sdets, pos, child);
+                            for (int qq = 0; qq < R; qq++) b.spops[pos * R + qq] = qq == sp ? nspawn : 0;
+                            if (b.sflag) b.sflag[pos] = flagword;
+                        } else {
+                            atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+                        }
+                    }
+                }
+                if (rdm) {
+                    // create_spawned_particle_replica_rdm: (parent, child) and the amount
+                    const uint32_t rball = __ballot_sync(FULL_MASK, nrdm != 0);
+                    if (rball) {
+                        const int leader = __ffs(rball) - 1;
+                        unsigned long long rbase = 0;
+                        if (lane == leader)
+                            rbase = atomicAdd((unsigned long long *)&st->n_rdm, (unsigned long long)__popc(rball));
+                        rbase = __shfl_sync(FULL_MASK, rbase, leader);
+                        if (nrdm != 0) {
+                            const int64_t pos = (int64_t)rbase + __popc(rball & lanemask_lt());
+                            if (pos < b.scap) {
+                                store_det<W>(b.rdm_sdets, 2 * pos, parent_det);
+                                store_det<W>(b.rdm_sdets, 2 * pos + 1, child);
+                                b.rdm_spops[pos] = nrdm;
+                                b.rdm_sspace[pos] = (uint8_t)sp;
+                            } else {
+                                atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace hgpu

@@ -375,6 +375,99 @@ def precision_study(target=2e5, tau=5e-5, equil=100, reports=600, nsample=1 << 2
     return out
 
 
+LARGE_WORKLOAD = ("config5: synthetic molecule M=64 nel=20 ms=0 C1 (two-word determinants, 128-bit rank keys), "
+                  "initiator FCIQMC (threshold 3) with 2 replicas and the replica 2-RDM (variational energy), real "
+                  "amplitudes, spawn cutoff 0.01, uniform renorm generator (p_double 0.9), FP32 matrix elements and "
+                  "p_gen, FP64 estimators, grown on the device to ~5e8 walkers in total, shift from E_proj")
+
+
+def large_replica_run(target_total=5e8, tau=2e-4, cycles=5, seed=2024, max_grow=60):
+    """config 5: one large replica calculation, measured like the headline
+    step -- grown on the device (shift held at 0) until the two replicas hold
+    about target_total walkers together; then the shifts are set varying (the
+    condition for accumulating the replica 2-RDM), the walker list is saved on
+    the device, and each of `cycles` reports of one cycle starts from it
+    (restored device to device, untimed) with the RDM accumulating:
+    attempts/s, time per cycle, memory held, E_proj and the RDM (variational)
+    energy of each cycle."""
+    from hande_gb300 import systems
+    from hande_gb300._abi import PREC_MIXED, make_config
+    from hande_gb300.engine import Engine
+    s = systems.synthetic_molecule(64, 20, seed=seed)
+    main_cap, spawn_cap = int(0.6 * target_total), int(1.6 * target_total)
+    cfg = make_config(s, tau=tau, init_pop=1e6, target_population=1e300, ncycles=1, seed=5,
+                      real_amplitudes=True, spawn_cutoff=0.01, excit_gen="renorm",
+                      pattempt_single=0.1, pattempt_double=0.9, initiator=True, initiator_threshold=3.0,
+                      nspaces=2, precision=PREC_MIXED, density_matrices=True, density_matrix_report=0,
+                      state_size=main_cap, spawned_state_size=spawn_cap)
+    free0 = device_free_bytes()
+    t0 = time.perf_counter()
+    e = Engine(s, cfg)
+    e.initial_distribution()
+    setup_s = time.perf_counter() - t0
+    flags = 0
+    grown = 0
+    last = None
+    for r in range(max_grow):
+        rep = e.run_report()
+        flags |= rep.error_flags
+        grown = r + 1
+        tot = rep.nparticles[0] + rep.nparticles[1]
+        sys.stderr.write("config5 grow %d Nw=%.4g+%.4g states=%d flags=%d\n" % (
+            r, rep.nparticles[0], rep.nparticles[1], rep.nstates, rep.error_flags))
+        # stop at the target, or before a cycle that would overshoot it by 20 %
+        g = tot / last if last else 1.0
+        if flags or tot >= 0.9 * target_total or tot * g > 1.2 * target_total:
+            break
+        last = tot
+    st = e.get_state()
+    st.vary_shift[0] = st.vary_shift[1] = 1
+    e.set_state(st)
+    e.snapshot()
+    held = None if free0 is None or device_free_bytes() is None else free0 - device_free_bytes()
+    att = 0
+    dev_ms = 0.0
+    rdm = []
+    walkers = None
+    for c in range(cycles):
+        e.snapshot(restore=True)
+        rep = e.run_report()
+        flags |= rep.error_flags
+        att += rep.nattempts
+        dev_ms += rep.device_ms
+        if rep.rdm_trace:
+            rdm.append(rep.rdm_energy / rep.rdm_trace)
+        sys.stderr.write("config5 cycle %d attempts=%d ms=%.1f flags=%d\n" % (
+            c, rep.nattempts, rep.device_ms, rep.error_flags))
+    # one more cycle from the same list with per-phase device times and list sizes
+    e.snapshot(restore=True)
+    phases, counts = e.profile_cycle()
+    out = {"workload": LARGE_WORKLOAD, "tau": tau, "main_capacity": main_cap, "spawn_capacity": spawn_cap,
+           "device_bytes_held": held, "setup_s": setup_s, "growth_cycles": grown, "cycles": cycles,
+           "error_flags": flags, "input_walkers_total": tot, "input_states": int(counts["N"]),
+           "phase_ms": phases, "cycle_counts": counts,
+           "attempts_per_cycle": att / cycles,
+           "value": att / (dev_ms * 1e-3) if dev_ms > 0 else None, "unit": "attempts/s",
+           "ms_per_cycle": dev_ms / cycles,
+           "E_proj": [rep.proj_energy[q] / rep.D0_population[q] for q in range(2)],
+           "rdm_energy_per_cycle": rdm,
+           "note": "each timed cycle starts from the same device-grown ~%.2g-walker list (saved and restored on "
+                   "the device, untimed) as one report whose RDM gives one replica (variational) energy; "
+                   "energies relative to the reference determinant's H_00" % tot}
+    e.close()
+    return out
+
+
+def device_free_bytes():
+    rt = cudart()
+    if rt is None:
+        return None
+    free, total = C.c_size_t(), C.c_size_t()
+    if rt.cudaMemGetInfo(C.byref(free), C.byref(total)) != 0:
+        return None
+    return int(free.value)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -387,7 +480,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (config 4) measurement")
     ap.add_argument("--config", type=int, default=2,
-                    help="2: the headline line (default); 3: the mixed-precision study of config 3, one JSON line")
+                    help="2: the headline line (default); 3: the mixed-precision study of config 3; 5: the large "
+                         "replica run of config 5 (one JSON line each)")
+    ap.add_argument("--large-total", type=float, default=5e8, help="config 5: total walkers of both replicas")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -399,6 +494,10 @@ def main():
     if args.config == 3:
         if rank == 0:
             print(json.dumps(precision_study()))
+        return
+    if args.config == 5:
+        if rank == 0:
+            print(json.dumps(large_replica_run(target_total=args.large_total, cycles=args.steps)))
         return
 
     cpu = None

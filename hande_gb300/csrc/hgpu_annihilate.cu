@@ -568,7 +568,8 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
     const int rows = b.binom_rows, cols = b.binom_cols;
     const size_t hist_smem = sizeof(uint32_t) * kMaxPasses * kRadix +
                              (b.use_rank ? sizeof(uint64_t) * (size_t)rows * cols : 0);
-    if (b.use_rank) k_sort_hist<W, 1, true><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    if (b.use_rank && b.key_words == 2) k_sort_hist<W, 2, true><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    else if (b.use_rank) k_sort_hist<W, 1, true><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
     else k_sort_hist<W, W, false><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
     k_sort_offsets<<<1, kRadix, 0, st>>>(b);
     const uint64_t *kin = b.use_rank ? b.skeys : b.sdets;

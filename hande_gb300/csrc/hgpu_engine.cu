@@ -435,9 +435,10 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
 // electrons among M spatial orbitals (hgpu_sort.cuh, det_rank):
 // T[(ka (nb + 1) + kb) * 2M + p] = C((p + 1) / 2, ka) C(p / 2, kb) when that
 // table fits the shared memory of k_sort_hist (one load per electron), else
-// C(n, k) for k <= max(na, nb), n <= M (two loads and a product per electron).
-// Returns the bits of the largest rank, or 0 when C(M, na) C(M, nb) does not
-// fit 64 bits (then the sort keys are the determinant words).
+// C(n, k) for k <= max(na, nb), n <= M (two loads and a product per electron;
+// mode 3 when the rank needs more than 64 bits: 128-bit products, two key
+// words).  Returns the bits of the largest rank, or 0 when it needs more than
+// 128 bits (then the sort keys are the determinant words).
 static int rank_bits(int M, int na, int nb, std::vector<uint64_t> &table, int &rows, int &cols, int &mode) {
     typedef unsigned __int128 u128;
     const u128 cap = ~(uint64_t)0;
@@ -453,11 +454,25 @@ static int rank_bits(int M, int na, int nb, std::vector<uint64_t> &table, int &r
         }
     }
     const u128 ca = C(M, na), cb = C(M, nb);
-    if (ca >= cap || cb >= cap || (cb > 0 && ca > cap / cb)) return 0;
+    if (ca >= cap || cb >= cap || ca == 0 || cb == 0) return 0;
+    const u128 all = ~(u128)0;
+    if (ca > all / cb) return 0;
     const u128 total = ca * cb;
-    if (total >= cap || total == 0) return 0;
     const size_t limit = 32768 / sizeof(uint64_t);  // shared-memory table of k_sort_hist
     const int nbasis = 2 * M;
+    if (total >= cap) {
+        // 128-bit ranks: binomials up to C(M, max(na, nb)) < 2^64
+        if ((size_t)(kmax + 1) * (M + 1) > limit) return 0;
+        mode = 3;
+        rows = kmax + 1;
+        cols = M + 1;
+        table.assign((size_t)rows * cols, 0);
+        for (size_t k = 0; k < table.size(); k++) table[k] = (uint64_t)c[k];
+        const u128 maxrank = total - 1;
+        int bits = 64;
+        while (bits < 128 && (maxrank >> bits) != 0) bits++;
+        return bits;
+    }
     if ((size_t)(na + 1) * (nb + 1) * nbasis <= limit) {
         mode = 1;
         rows = (na + 1) * (nb + 1);
@@ -514,11 +529,12 @@ static int alloc_lists(hgpu_handle *h) {
         int bits = rank_bits(h->hsys.nbasis / 2, h->hsys.nalpha, h->hsys.nbeta, binom, rows, cols, mode);
         b.use_rank = bits > 0 ? mode : 0;
         b.key32 = b.use_rank && bits <= 32 ? 1 : 0;
+        if (b.use_rank == 3 && W < 2) return HGPU_ERR_UNSUPPORTED;  // two key words need two-word buffers
         b.binom_rows = rows;
         b.binom_cols = cols;
         b.sort_na = h->hsys.nalpha;
         b.sort_nb = h->hsys.nbeta;
-        b.key_words = b.use_rank ? 1 : W;
+        b.key_words = b.use_rank ? (b.use_rank == 3 ? 2 : 1) : W;
         int key_bits = b.use_rank ? bits : h->hsys.nbasis;
         b.sort_passes = (key_bits + kRadixBits - 1) / kRadixBits;
         if (b.sort_passes < 1) b.sort_passes = 1;
@@ -533,7 +549,7 @@ static int alloc_lists(hgpu_handle *h) {
         b.binom = nullptr;
         if (b.use_rank) {
             if ((rc = upload(h, binom.data(), binom.size(), &b.binom))) return rc;
-            if ((rc = dalloc(h, &b.skeys, (size_t)b.scap))) return rc;
+            if ((rc = dalloc(h, &b.skeys, (size_t)b.scap * b.key_words))) return rc;
         }
     }
     if ((rc = dalloc(h, &b.ghist, (size_t)kMaxPasses * kRadix))) return rc;
@@ -559,6 +575,7 @@ static int alloc_lists(hgpu_handle *h) {
     b.rdm = nullptr;
     b.npairs = 0;
     if (h->cfg.density_matrices) {
+        if (b.cap >= (int64_t)0xFFFFFFFF) return HGPU_ERR_UNSUPPORTED;  // 32-bit hash-table entries
         b.npairs = (int64_t)h->hsys.nbasis * (h->hsys.nbasis - 1) / 2;
         if ((rc = dalloc(h, &b.rdm, (size_t)(b.npairs * b.npairs)))) return rc;
         CK(cudaMemset(b.rdm, 0, sizeof(double) * (size_t)(b.npairs * b.npairs)));
@@ -566,6 +583,10 @@ static int alloc_lists(hgpu_handle *h) {
         if ((rc = dalloc(h, &b.rdm_spops, (size_t)b.scap))) return rc;
         if ((rc = dalloc(h, &b.rdm_sspace, (size_t)b.scap))) return rc;
         if ((rc = dalloc(h, &b.rdm_rows, (size_t)(2 * b.npairs)))) return rc;
+        int64_t hs = 16;
+        while (hs < b.cap + b.cap / 2) hs <<= 1;
+        b.rdm_hash_mask = hs - 1;
+        if ((rc = dalloc(h, &b.rdm_hash, (size_t)hs))) return rc;
     }
     if ((rc = dalloc(h, &b.scan_part, (size_t)kMaxBlocks * 2))) return rc;
     if ((rc = dalloc(h, &b.part_d, (size_t)kMaxBlocks * 4))) return rc;

@@ -92,8 +92,9 @@ struct DevBuffers {
     uint32_t *os_epoch;  // look-back epoch of the current sort (kept out of DevState,
                          // which the host rewrites, so that an epoch is never reused)
     const uint64_t *binom;  // rank table [binom_rows][binom_cols] (hgpu_sort.cuh, det_rank)
-    int use_rank;       // keys are ranks (one word; 1: one table load per electron, 2: two loads
-                        // and a product); 0: the keys are the determinant words
+    int use_rank;       // keys are ranks (1: one table load per electron, 2: two loads and a
+                        // product, 3: the same with 128-bit products, two key words); 0: the
+                        // keys are the determinant words
     int key32;          // the ranks fit 32 bits: 32-bit keys
     int key_words;
     int binom_rows, binom_cols;  // shape of the rank table
@@ -113,6 +114,8 @@ struct DevBuffers {
     int64_t *rdm_spops;     // per RDM spawn: amount
     uint8_t *rdm_sspace;    // per RDM spawn: space of the parent
     double *rdm_rows;       // [2][npairs]: per-row energy and diagonal of calc_rdm_energy
+    uint32_t *rdm_hash;     // open-addressing table of the new main list (index per slot)
+    int64_t rdm_hash_mask;  // table size - 1 (a power of two, at least 1.5 x cap)
     // scan scratch and per-block partials
     int64_t *scan_part;     // kMaxBlocks * 2
     double *part_d;         // kMaxBlocks * 4 (proj, d0 per space)

@@ -57,21 +57,81 @@ __device__ __forceinline__ void rdm_add_pair(double *rdm, int64_t np, const Det<
     }
 }
 
+// Open-addressing hash table of the new main list (index per slot, linear
+// probing), so that each RDM spawn finds its child with about two memory
+// accesses instead of a binary search of the whole list.  Probe sequences are
+// bounded by the table size; a full sweep (impossible below a load of one)
+// raises HGPU_FLAG_INTERNAL.
+constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
+
+template <int W>
+__device__ __forceinline__ uint64_t det_hash(const Det<W> &f) {
+    uint64_t x = 0x9E3779B97F4A7C15ull;
+#pragma unroll
+    for (int w = 0; w < W; w++) x = (x ^ f.w[w]) * 0xBF58476D1CE4E5B9ull;
+    // murmur3 finaliser
+    x ^= x >> 33;
+    x *= 0xFF51AFD7ED558CCDull;
+    x ^= x >> 33;
+    x *= 0xC4CEB9FE1A85EC53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+__global__ void __launch_bounds__(kBlock) k_rdm_hash_clear(DevBuffers b) {
+    if (!b.state->rdm_on) return;
+    uint4 *t = reinterpret_cast<uint4 *>(b.rdm_hash);
+    const int64_t n = (b.rdm_hash_mask + 1) / 4;
+    const uint4 e = make_uint4(kHashEmpty, kHashEmpty, kHashEmpty, kHashEmpty);
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        t[k] = e;
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_rdm_hash_insert(DevBuffers b, int cur) {
+    DevState *st = b.state;
+    if (!st->rdm_on) return;
+    const int64_t N = st->n_main;
+    const uint64_t *dets = b.dets[cur];
+    const uint64_t mask = (uint64_t)b.rdm_hash_mask;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t h = det_hash<W>(load_det<W>(dets, i)) & mask;
+        uint64_t probes = 0;
+        while (atomicCAS(&b.rdm_hash[h], kHashEmpty, (uint32_t)i) != kHashEmpty) {
+            h = (h + 1) & mask;
+            if (++probes > mask) {
+                atomicOr(&st->error_flags, HGPU_FLAG_INTERNAL);
+                break;
+            }
+        }
+    }
+}
+
 // The cycle's RDM spawns against the new main list (buffer cur).
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_rdm_spawns(DevBuffers b, int R, int cur) {
-    const DevState *st = b.state;
+    DevState *st = b.state;
     if (!st->rdm_on) return;
-    const int64_t N = st->n_main;
     const int64_t n = st->n_rdm < b.scap ? st->n_rdm : b.scap;
     const uint64_t *dets = b.dets[cur];
     const int64_t *pops = b.pops[cur];
     const int nel = b.sys->nel;
     const double inv_rf = 1.0 / (double)b.sys->real_factor;  // exact: a power of two
+    const uint64_t mask = (uint64_t)b.rdm_hash_mask;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         const Det<W> fp = load_det<W>(b.rdm_sdets, 2 * k), fc = load_det<W>(b.rdm_sdets, 2 * k + 1);
-        const int64_t pos = lower_bound_det<W>(dets, N, fc);
-        if (pos >= N || !det_eq<W>(load_det<W>(dets, pos), fc)) continue;
+        uint64_t h = det_hash<W>(fc) & mask;
+        int64_t pos = -1;
+        for (uint64_t probes = 0; probes <= mask; probes++) {
+            const uint32_t v = b.rdm_hash[h];
+            if (v == kHashEmpty) break;
+            if (det_eq<W>(load_det<W>(dets, v), fc)) {
+                pos = v;
+                break;
+            }
+            h = (h + 1) & mask;
+        }
+        if (pos < 0) continue;
         const int s = b.rdm_sspace[k];
         // pops(other replica, child) / real_factor x amount / real_factor / 2
         const double pop1 = (double)pops[pos * R + (1 - s)] * inv_rf;
@@ -204,10 +264,13 @@ __global__ void __launch_bounds__(1024) k_rdm_final(DevBuffers b) {
 
 void launch_rdm_cycle(const DevBuffers &b, int W, int R, int cur, cudaStream_t st) {
     const size_t dsm = sizeof(double) * (size_t)b.npairs;
+    k_rdm_hash_clear<<<b.grid, kBlock, 0, st>>>(b);
     if (W == 1) {
+        k_rdm_hash_insert<1><<<b.grid, kBlock, 0, st>>>(b, cur);
         k_rdm_spawns<1><<<b.grid, kBlock, 0, st>>>(b, R, cur);
         k_rdm_diag<1><<<b.grid, kBlock, dsm, st>>>(b, R, cur);
     } else {
+        k_rdm_hash_insert<2><<<b.grid, kBlock, 0, st>>>(b, cur);
         k_rdm_spawns<2><<<b.grid, kBlock, 0, st>>>(b, R, cur);
         k_rdm_diag<2><<<b.grid, kBlock, dsm, st>>>(b, R, cur);
     }

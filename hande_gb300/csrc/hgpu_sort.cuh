@@ -65,7 +65,8 @@ __device__ __forceinline__ uint32_t warp_peers8(uint32_t mask, uint32_t d) {
 // C(alpha orbitals below p, ka) C(beta orbitals below p, kb) ways, summed over
 // p.  mode 1: tab[(ka (nb + 1) + kb) * cols + p] holds that product; mode 2:
 // tab[k * cols + n] = C(n, k).  A determinant with other electron counts sets
-// bad (its key is then 0).
+// bad (its key is then 0).  det_rank128: mode 2 with 128-bit products and sum,
+// for ranks above 64 bits (two key words, low word first).
 template <int W>
 __device__ __forceinline__ uint64_t det_rank(const Det<W> &f, const uint64_t *tab, int cols, int mode, int na,
                                              int nb, bool &bad) {
@@ -111,6 +112,35 @@ __device__ __forceinline__ uint64_t det_rank(const Det<W> &f, const uint64_t *ta
     return r;
 }
 
+template <int W>
+__device__ __forceinline__ unsigned __int128 det_rank128(const Det<W> &f, const uint64_t *tab, int cols, int na,
+                                                         int nb, bool &bad) {
+    int ca = 0, cb = 0;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        ca += __popcll(f.w[w] & 0x5555555555555555ull);
+        cb += __popcll(f.w[w] & 0xAAAAAAAAAAAAAAAAull);
+    }
+    if (ca != na || cb != nb) {
+        bad = true;
+        return 0;
+    }
+    unsigned __int128 r = 0;
+    int ka = 0, kb = 0;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        uint64_t x = f.w[w];
+        while (x) {
+            const int p = 64 * w + __ffsll((long long)x) - 1;
+            x &= x - 1;
+            if (p & 1) kb++;
+            else ka++;
+            r += (unsigned __int128)tab[ka * cols + ((p + 1) >> 1)] * tab[kb * cols + (p >> 1)];
+        }
+    }
+    return r;
+}
+
 // Sort keys of the spawned list (ranks into b.skeys, when ranks are used) and
 // the digit histograms of every pass, added into b.ghist[pass][digit].
 template <int W, int KW, bool RANK>
@@ -142,7 +172,13 @@ __global__ void __launch_bounds__(kBlock) k_sort_hist(DevBuffers b, int rows, in
             if (i >= n) break;
             const Det<W> &f = fs[r];
             uint64_t key[KW];
-            if (RANK) {
+            if (RANK && KW == 2) {
+                const unsigned __int128 r = det_rank128<W>(f, binom, cols, b.sort_na, b.sort_nb, bad);
+                key[0] = (uint64_t)r;
+                key[KW - 1] = (uint64_t)(r >> 64);
+                b.skeys[2 * i] = key[0];
+                b.skeys[2 * i + 1] = key[KW - 1];
+            } else if (RANK) {
                 key[0] = det_rank<W>(f, binom, cols, b.use_rank, b.sort_na, b.sort_nb, bad);
                 if (b.key32) reinterpret_cast<uint32_t *>(b.skeys)[i] = (uint32_t)key[0];
                 else b.skeys[i] = key[0];

@@ -164,6 +164,11 @@ class Engine:
         self._check(self.L.hgpu_get_state(self.h, C.byref(s)), "hgpu_get_state")
         return s
 
+    def get_state(self) -> HgpuState:
+        s = HgpuState()
+        self._check(self.L.hgpu_get_state(self.h, C.byref(s)), "hgpu_get_state")
+        return s
+
     def set_state(self, s: HgpuState):
         self._check(self.L.hgpu_set_state(self.h, C.byref(s)), "hgpu_set_state")
 

@@ -33,6 +33,8 @@ def _systems():
         "h2o_sto2g": systems.read_in(os.path.join(GOLDEN, "H2O-RHF-sto-2g.fcidump")),
         "mol26": systems.synthetic_molecule(26, 10, seed=5),
         "mol40_w2": systems.synthetic_molecule(40, 12, seed=6),
+        # C(48,10)^2 > 2^64: two-word (128-bit) rank keys
+        "mol48_w2_r128": systems.synthetic_molecule(48, 20, seed=12),
     }
 
 
@@ -139,6 +141,8 @@ RUNS = [
     ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True, initiator=True), 5),
     ("mol40_w2", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
                       excit_gen="no_renorm"), 2),
+    ("mol48_w2_r128", dict(tau=5e-5, init_pop=2000, target_population=20000, real_amplitudes=True,
+                           initiator=True, nspaces=2), 2),
 ]
 
 

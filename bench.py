@@ -375,6 +375,52 @@ def precision_study(target=2e5, tau=5e-5, equil=100, reports=600, nsample=1 << 2
     return out
 
 
+HUBBARD_WORKLOAD = ("config1: Hubbard model in momentum space, 2D 4x4 periodic, t=1, U=4, 10 electrons (ms=0), "
+                    "integer walkers, 10 on the reference at the start, target 5e4, tau=0.005, shift damping 0.05, "
+                    "mc_cycles 10 x 2000 reports (20000 iterations), FP64")
+
+
+def hubbard_run(excit_gen="renorm", nreports=2000, seed=7):
+    """config 1 as specified: the whole 20000-iteration run on the device,
+    one report per host call; attempts/s and time per iteration over the
+    reports after the shift starts varying (device time of the cycles), and
+    the reblocked shift and E_proj of that part."""
+    from hande_gb300 import analysis, systems
+    from hande_gb300._abi import make_config
+    from hande_gb300.engine import Engine
+    s = systems.hubbard_k([[4, 0], [0, 4]], 10, U=4.0, t=1.0)
+    cfg = make_config(s, tau=0.005, init_pop=10, target_population=5e4, ncycles=10, seed=seed, shift_damping=0.05,
+                      excit_gen=excit_gen, state_size=2000000, spawned_state_size=2000000)
+    e = Engine(s, cfg)
+    e.initial_distribution()
+    t0 = time.perf_counter()
+    att = 0
+    dev_ms = 0.0
+    cycles = 0
+    shift, num, d0 = [], [], []
+    flags = 0
+    for r in range(nreports):
+        rep = e.run_report()
+        flags |= rep.error_flags
+        if rep.vary_shift[0]:
+            att += rep.nattempts
+            dev_ms += rep.device_ms
+            cycles += 10
+            shift.append(rep.shift[0])
+            num.append(rep.proj_energy[0])
+            d0.append(rep.D0_population[0])
+    wall = time.perf_counter() - t0
+    E, err, _ = analysis.projected_energy(num, d0) if len(num) > 32 else (None, None, None)
+    S, serr, _ = analysis.mean_error(shift) if len(shift) > 32 else (None, None, None)
+    e.close()
+    return {"excit_gen": excit_gen, "iterations": 10 * nreports, "wall_s": wall, "error_flags": flags,
+            "cycles_measured": cycles, "attempts_per_s": att / (dev_ms * 1e-3) if dev_ms > 0 else None,
+            "ms_per_iteration": dev_ms / cycles if cycles else None,
+            "wall_ms_per_iteration_whole_run": 1e3 * wall / (10 * nreports),
+            "walkers": rep.nparticles[0], "states": int(rep.nstates),
+            "E_proj": E, "E_proj_error": err, "shift": S, "shift_error": serr}
+
+
 LARGE_WORKLOAD = ("config5: synthetic molecule M=64 nel=20 ms=0 C1 (two-word determinants, 128-bit rank keys), "
                   "initiator FCIQMC (threshold 3) with 2 replicas and the replica 2-RDM (variational energy), real "
                   "amplitudes, spawn cutoff 0.01, uniform renorm generator (p_double 0.9), FP32 matrix elements and "
@@ -480,8 +526,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (config 4) measurement")
     ap.add_argument("--config", type=int, default=2,
-                    help="2: the headline line (default); 3: the mixed-precision study of config 3; 5: the large "
-                         "replica run of config 5 (one JSON line each)")
+                    help="2: the headline line (default); 1: the Hubbard 4x4 run of config 1; 3: the "
+                         "mixed-precision study of config 3; 5: the large replica run of config 5 (one JSON line each)")
     ap.add_argument("--large-total", type=float, default=5e8, help="config 5: total walkers of both replicas")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -494,6 +540,11 @@ def main():
     if args.config == 3:
         if rank == 0:
             print(json.dumps(precision_study()))
+        return
+    if args.config == 1:
+        if rank == 0:
+            print(json.dumps({"workload": HUBBARD_WORKLOAD, "renorm": hubbard_run("renorm"),
+                              "no_renorm": hubbard_run("no_renorm")}))
         return
     if args.config == 5:
         if rank == 0:

@@ -243,6 +243,42 @@ static int build_heat_bath(hgpu_handle *h, const hgpu_system *sys, DevSys &s) {
     return upload_heat_bath<double>(h, t, s);
 }
 
+// find_single_double_prob, read_in branch (src/qmc_common.F90:152-260): the
+// numbers of symmetry- and spin-allowed single and double excitations of the
+// reference determinant, each divided by their sum.
+static void single_double_prob(const hgpu_system *sys, const uint64_t *ref, double &psingle, double &pdouble) {
+    const int nsym = sys->nsym_pg;
+    std::vector<int64_t> virt((size_t)2 * nsym);
+    std::vector<int> occ;
+    for (int p = 0; p < sys->nbasis; p++)
+        if ((ref[p >> 6] >> (p & 63)) & 1u) occ.push_back(p);
+    for (int k = 0; k < 2 * nsym; k++) virt[k] = sys->nbasis_sym_spin[k];
+    auto slot = [&](int p) { return (size_t)((sys->orb_ms[p] + 1) / 2) * nsym + sys->orb_sym[p]; };
+    for (int p : occ) virt[slot(p)]--;
+    int64_t nsingles = 0, ndoubles = 0;
+    for (int p : occ) nsingles += virt[slot(p)];
+    const size_t n = occ.size();
+    for (size_t i = 0; i < n; i++) {
+        const int m1 = (sys->orb_ms[occ[i]] + 1) / 2;
+        for (size_t j = i + 1; j < n; j++) {
+            const int m2 = (sys->orb_ms[occ[j]] + 1) / 2;
+            const int ij = sys->orb_sym[occ[i]] ^ sys->orb_sym[occ[j]];
+            for (int sa = 0; sa < nsym; sa++) {
+                const int sb = (sa ^ ij) & (nsym - 1);
+                const int64_t va = virt[(size_t)m1 * nsym + sa], vb = virt[(size_t)m2 * nsym + sb];
+                if (sa == sb) {
+                    ndoubles += m1 == m2 ? (va * (vb - 1)) / 2 : va * vb;
+                } else if (sa < sb) {
+                    ndoubles += va * vb;
+                    if (m1 != m2) ndoubles += virt[(size_t)m2 * nsym + sa] * virt[(size_t)m1 * nsym + sb];
+                }
+            }
+        }
+    }
+    psingle = (double)nsingles / (double)(nsingles + ndoubles);
+    pdouble = (double)ndoubles / (double)(nsingles + ndoubles);
+}
+
 static int build_system(hgpu_handle *h, const hgpu_system *sys) {
     DevSys &s = h->hsys;
     memset(&s, 0, sizeof(s));
@@ -266,8 +302,12 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
     s.tau = c.tau;
     // init_excit_gen (src/qmc.F90:951-972)
     if (c.pattempt_single < 0 || c.pattempt_double < 0) {
-        s.pattempt_single = sys->kind == HGPU_SYS_HUB_K ? 0.0 : 0.1;
-        s.pattempt_double = sys->kind == HGPU_SYS_HUB_K ? 1.0 : 0.9;
+        if (sys->kind == HGPU_SYS_HUB_K) {
+            s.pattempt_single = 0.0;
+            s.pattempt_double = 1.0;
+        } else {
+            single_double_prob(sys, c.ref_det, s.pattempt_single, s.pattempt_double);
+        }
     } else {
         s.pattempt_single = c.pattempt_single / (c.pattempt_single + c.pattempt_double);
         s.pattempt_double = 1.0 - c.pattempt_single;

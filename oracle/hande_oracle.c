@@ -466,6 +466,42 @@ static void decode_mol(const oracle_ctx *c, const uint64_t *f, det_info *d) {
 /* cross_product_pg_sym / pg_sym_conj (src/pg_symmetry.f90) without Lz. */
 static inline int cross(const oracle_ctx *c, int a, int b) { return (a ^ b) & (c->nsym - 1); }
 
+/* find_single_double_prob, read_in branch (src/qmc_common.F90:152-260): the
+ * shares of the symmetry- and spin-allowed single and double excitations of
+ * the reference determinant, each divided by their sum. */
+static void single_double_prob(const oracle_ctx *c, double *psingle, double *pdouble) {
+    const int nsym = c->nsym;
+    int *virt = (int *)calloc((size_t)2 * nsym, sizeof(int));
+    int occ[MAXEL], n = 0;
+    for (int p = 0; p < c->nbasis; p++)
+        if (tbit(c->f0, p)) occ[n++] = p;
+    for (int ims = 0; ims < 2; ims++)
+        for (int s = 0; s < nsym; s++) virt[ims * nsym + s] = NBSS(ims, s);
+    for (int i = 0; i < n; i++) virt[ims_of(c, occ[i]) * nsym + c->orb_sym[occ[i]]]--;
+    int64_t nsingles = 0, ndoubles = 0;
+    for (int i = 0; i < n; i++) nsingles += virt[ims_of(c, occ[i]) * nsym + c->orb_sym[occ[i]]];
+    for (int i = 0; i < n; i++) {
+        const int m1 = ims_of(c, occ[i]);
+        for (int j = i + 1; j < n; j++) {
+            const int m2 = ims_of(c, occ[j]);
+            for (int sa = 0; sa < nsym; sa++) {
+                const int sb = cross(c, sa, cross(c, c->orb_sym[occ[i]], c->orb_sym[occ[j]]));
+                const int64_t va1 = virt[m1 * nsym + sa], vb2 = virt[m2 * nsym + sb];
+                if (sa == sb) {
+                    if (m1 == m2) ndoubles += (va1 * (vb2 - 1)) / 2;
+                    else ndoubles += va1 * vb2;
+                } else if (sa < sb) {
+                    ndoubles += va1 * vb2;
+                    if (m1 != m2) ndoubles += (int64_t)virt[m2 * nsym + sa] * virt[m1 * nsym + sb];
+                }
+            }
+        }
+    }
+    free(virt);
+    *psingle = (double)nsingles / (double)(nsingles + ndoubles);
+    *pdouble = (double)ndoubles / (double)(nsingles + ndoubles);
+}
+
 /* choose_ij_mol (src/excit_gen_mol.f90:620-660). */
 static void choose_ij_mol(const oracle_ctx *c, rstream *rs, const det_info *d, int *i, int *j, int *ij_sym,
                           int *ij_spin, double *pgen_ij) {
@@ -2000,15 +2036,15 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
     /* alloc_spawn_t: cutoff = ceiling(cutoff*real_factor); 0 for integer walkers
      * (src/spawn_data.F90:215, src/qmc.F90:1484-1485) */
     c->cutoff = cfg->real_amplitudes ? (int64_t)ceil(cfg->spawn_cutoff * (double)c->real_factor) : 0;
+    for (int w = 0; w < MAXW; w++) c->f0[w] = w < c->nw ? cfg->ref_det[w] : 0;
     /* init_excit_gen (src/qmc.F90:951-972) */
     if (cfg->pattempt_single < 0 || cfg->pattempt_double < 0) {
         if (c->kind == HGPU_SYS_HUB_K) { c->pattempt_single = 0.0; c->pattempt_double = 1.0; }
-        else { c->pattempt_single = 0.1; c->pattempt_double = 0.9; }
+        else single_double_prob(c, &c->pattempt_single, &c->pattempt_double);
     } else {
         c->pattempt_single = cfg->pattempt_single / (cfg->pattempt_single + cfg->pattempt_double);
         c->pattempt_double = 1.0 - cfg->pattempt_single;
     }
-    for (int w = 0; w < MAXW; w++) c->f0[w] = w < c->nw ? cfg->ref_det[w] : 0;
     /* pattempt_parallel (src/qmc.F90:974-988) and the pgen_ij of each spin
      * class, in choose_ij_spin_mol's rounding order */
     c->spin_ij = c->kind == HGPU_SYS_READ_IN &&
@@ -2274,6 +2310,11 @@ double oracle_hmatel(oracle_ctx *c, const int64_t *f1, const int64_t *f2) {
 double oracle_sc0(oracle_ctx *c, const int64_t *f) { return sc0(c, (const uint64_t *)f); }
 
 double oracle_pattempt_parallel(oracle_ctx *c) { return c->spin_ij ? c->pattempt_parallel : -1.0; }
+
+void oracle_pattempt(oracle_ctx *c, double *out) {
+    out[0] = c->pattempt_single;
+    out[1] = c->pattempt_double;
+}
 
 int64_t oracle_rdm(oracle_ctx *c, double *out, int64_t n) {
     if (!c->rdm_enabled) return 0;

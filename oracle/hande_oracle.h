@@ -49,6 +49,8 @@ double oracle_sc0(oracle_ctx *c, const int64_t *f);
 double oracle_pgen(oracle_ctx *c, const int64_t *f, const int32_t *orbs);
 /* pattempt_parallel of the spin-resolved generators (negative for the others). */
 double oracle_pattempt_parallel(oracle_ctx *c);
+/* pattempt_single and pattempt_double after init_excit_gen (src/qmc.F90:951-972). */
+void oracle_pattempt(oracle_ctx *c, double *out);
 /* Replica 2-RDM (density_matrices): copies the current report's RDM
  * ([pair][pair], pairs p < q in tri_ind_distinct order) into out when n is
  * large enough and returns its element count (0 when not enabled); its

@@ -59,6 +59,8 @@ def lib():
         L.oracle_rdm_from_list.argtypes = [C.c_void_p]
         L.oracle_pattempt_parallel.restype = C.c_double
         L.oracle_pattempt_parallel.argtypes = [C.c_void_p]
+        L.oracle_pattempt.restype = None
+        L.oracle_pattempt.argtypes = [C.c_void_p, P(C.c_double)]
         L.oracle_pgen.restype = C.c_double
         L.oracle_pgen.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int32)]
         L.oracle_total_attempts.restype = C.c_int64
@@ -188,6 +190,11 @@ class Oracle:
 
     def pattempt_parallel(self) -> float:
         return self.L.oracle_pattempt_parallel(self.h)
+
+    def pattempt(self):
+        out = (C.c_double * 2)()
+        self.L.oracle_pattempt(self.h, out)
+        return out[0], out[1]
 
     def pgen(self, f, orbs) -> float:
         o = np.ascontiguousarray(orbs, dtype=np.int32)

@@ -461,6 +461,24 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
             c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE) {
             if ((rc = build_heat_bath(h, sys, s))) return rc;
         }
+        if (c.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC || c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC) {
+            // the weights of gen_excit_mol_power_pitzer_occ: sqrt|<pq|qp>| for equal
+            // spins, else 0 (get_two_body_int_ex_mol_real), or sqrt|<pq|pq>|
+            // (get_two_body_int_cou_mol_real), src/hamiltonian_molecular.f90:392-434
+            const int nb = sys->nbasis;
+            const bool cs = c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC;
+            auto tri0 = [](int64_t x, int64_t y) { return x >= y ? x * (x + 1) / 2 + y : y * (y + 1) / 2 + x; };
+            std::vector<double> w((size_t)nb * nb);
+            for (int p = 0; p < nb; p++)
+                for (int q = 0; q < nb; q++) {
+                    const int64_t sp = p >> 1, sq = q >> 1;
+                    double v = 0.0;
+                    if (cs) v = sys->v2[tri0(tri0(sp, sp), tri0(sq, sq))];                   // (pp|qq)
+                    else if (sys->orb_ms[p] == sys->orb_ms[q]) v = sys->v2[tri0(tri0(sp, sq), tri0(sq, sp))];  // (pq|qp)
+                    w[(size_t)p * nb + q] = std::sqrt(std::fabs(v));
+                }
+            if ((rc = upload(h, w.data(), w.size(), &s.pp_w))) return rc;
+        }
     } else {
         return HGPU_ERR_INVALID;
     }
@@ -685,10 +703,14 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     } else if (sys->kind == HGPU_SYS_READ_IN) {
         bool hb = cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM ||
                   cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE;
+        const bool pp = cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
+                        cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC;
         if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM &&
-            cfg->excit_gen != HGPU_EXCIT_GEN_RENORM_SPIN && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM_SPIN && !hb)
+            cfg->excit_gen != HGPU_EXCIT_GEN_RENORM_SPIN && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM_SPIN && !hb &&
+            !pp)
             return HGPU_ERR_UNSUPPORTED;
         if (hb && sys->nel > kHBMaxEl) return HGPU_ERR_UNSUPPORTED;
+        if (pp && cfg->precision != HGPU_PREC_FP64) return HGPU_ERR_UNSUPPORTED;  // FP64 generator only
     } else {
         return HGPU_ERR_INVALID;
     }
@@ -717,6 +739,9 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
             h->gkind = kKindHeatBathUniform;  // the singles differ at run time
         else if (cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM || cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM_SPIN)
             h->gkind = kKindReadInNoRenorm;
+        else if (cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
+                 cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC)
+            h->gkind = kKindPowerPitzerOcc;
     }
     h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;
     cudaGetDevice(&h->device);

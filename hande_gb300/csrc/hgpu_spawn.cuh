@@ -69,7 +69,11 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
             gen_single_hb_exact<W, Real>(s, rs, d, at, pgen, hm);
         else if (single) gen_single_mol<W, Real>(s, rs, d, KIND != kKindReadInNoRenorm, at, pgen, hm);
         else if (KIND == kKindHeatBathUniform) gen_heat_bath_uniform_double<W, Real>(s, rs, f, at, pgen, hm);
-        else gen_double_mol<W, Real>(s, rs, d, KIND == HGPU_SYS_READ_IN, at, pgen, hm);
+        else if (KIND == kKindPowerPitzerOcc) {
+            double h;
+            gen_pp_occ_double<W>(s, rs, d, at, pgen, h);
+            hm = (Real)h;
+        } else gen_double_mol<W, Real>(s, rs, d, KIND == HGPU_SYS_READ_IN, at, pgen, hm);
         attempt_to_spawn(s, rs, parent, pgen, (double)hm, at);
         at.nspawn_rdm = 0;
         if (rdm) attempt_to_spawn_rdm(s, rs, parent, at);
@@ -112,7 +116,8 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
     // generators whose first draw is the single/double choice: the chunk is
     // split by that draw so that each excitation type runs with the warp
     // converged (a tenth of the attempts are singles, with their own code)
-    constexpr bool drew = KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm || KIND == kKindHeatBathUniform;
+    constexpr bool drew = KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm || KIND == kKindHeatBathUniform ||
+                          KIND == kKindPowerPitzerOcc;
     // Each warp claims chunks of kSpawnChunk consecutive attempts.  The (parent,
     // space) slot of attempt a is the first k with aoff[k] > a; one binary search
     // per chunk finds the slot of its first attempt, and every later step of 32

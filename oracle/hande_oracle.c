@@ -1218,6 +1218,118 @@ static void gen_heat_bath_uniform_double(const oracle_ctx *c, rstream *rs, const
 
 /* gen_excit_mol / gen_excit_mol_no_renorm (src/excit_gen_mol.f90:16-284) with
  * spawn_standard + attempt_to_spawn (src/spawning.F90:34-123, :711-768). */
+/* ------------------------------------------------------------------------- */
+/* uniform_power_pitzer / uniform_cauchy_schwarz                              */
+/* (gen_excit_mol_power_pitzer_occ, src/excit_gen_power_pitzer_mol.F90)      */
+/* ------------------------------------------------------------------------- */
+
+/* The weight of q for an electron in p: sqrt|<pq|qp>| for power_pitzer
+ * (get_two_body_int_ex_mol_real, src/hamiltonian_molecular.f90:392-411) or
+ * sqrt|<pq|pq>| for cauchy_schwarz (get_two_body_int_cou_mol_real, :413-434),
+ * both through get_two_body_int_mol_real's spin check
+ * (src/molecular_integrals.F90:1147-1177). */
+static double pp_weight(const oracle_ctx *c, int p, int q) {
+    double v = 0.0;
+    if (c->cfg.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC) v = v2_get(c, p, q, p, q);
+    else if (c->orb_ms[p] == c->orb_ms[q]) v = v2_get(c, p, q, q, p);
+    return sqrt(fabs(v));
+}
+
+/* create_weighted_excitation_list_mol (src/hamiltonian_molecular.f90:348-390):
+ * the weights of p over a list, 0 for the entry equal to skip, and their sum in
+ * list order. */
+static double pp_weight_list(const oracle_ctx *c, int p, int skip, const int *list, int n, double *w) {
+    double tot = 0.0;
+    for (int k = 0; k < n; k++) {
+        if (list[k] != skip) {
+            w[k] = pp_weight(c, p, list[k]);
+            tot = tot + w[k];
+        } else {
+            w[k] = 0.0;
+        }
+    }
+    return tot;
+}
+
+/* binary_search over an ascending integer list (src/search.f90): the position
+ * of x, or where it would be inserted. */
+static int int_lower_bound(const int *list, int n, int x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) / 2;
+        if (list[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+/* The double excitations of gen_excit_mol_power_pitzer_occ with i, j chosen
+ * uniformly (src/excit_gen_power_pitzer_mol.F90:1260-1547): a from the
+ * determinant's unoccupied orbitals of i's spin, b from the orbitals of the
+ * spin and irrep that conserve both (b /= a), each by an alias table built for
+ * the attempt; for parallel spins p_gen adds the reverse order (b from i, a
+ * from j). */
+static void gen_pp_occ_double(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d,
+                              attempt_t *out, double *pgen, double *hmatel) {
+    int i, j, ij_sym, ij_spin;
+    double pgen_ij;
+    out->e.nexcit = 2;
+    choose_ij_mol(c, rs, d, &i, &j, &ij_sym, &ij_spin, &pgen_ij);
+    out->e.from[0] = i;
+    out->e.from[1] = j;
+    int unocc[MAXB], nv = 0;
+    for (int p = 0; p < c->nbasis; p++)
+        if (!tbit(f, p) && c->orb_ms[p] == c->orb_ms[i]) unocc[nv++] = p;
+    double ia_w[MAXB], jb_w[MAXB], ja_w[MAXB];
+    int allowed = 0, a = -1, b = -1;
+    if (nv > 0) {
+        double ia_tot = pp_weight_list(c, i, -1, unocc, nv, ia_w);
+        if (ia_tot > 0.0) {
+            int a_ind = alias_select(rs, nv, ia_w, ia_tot);
+            a = unocc[a_ind];
+            int isymb = cross(c, ij_sym, c->orb_sym[a]);
+            int imsb = (ij_spin - c->orb_ms[a] + 1) / 2; /* 0 beta, 1 alpha */
+            int nb = NBSS(imsb, isymb);
+            int list[MAXB];
+            for (int q = 0; q < nb; q++) list[q] = SSBF(q, imsb, isymb);
+            double jb_tot = nb > 0 ? pp_weight_list(c, j, a, list, nb, jb_w) : 0.0;
+            if (jb_tot > 0.0) {
+                int b_ind = alias_select(rs, nb, jb_w, jb_tot);
+                b = list[b_ind];
+                if (!tbit(f, b)) {
+                    double pg;
+                    if (ij_spin == 0) {
+                        pg = ia_w[a_ind] / ia_tot * jb_w[b_ind] / jb_tot;
+                    } else {
+                        int b_rev = int_lower_bound(unocc, nv, b);
+                        int isyma = cross(c, ij_sym, isymb);
+                        int na = NBSS(imsb, isyma);
+                        int alist[MAXB];
+                        for (int q = 0; q < na; q++) alist[q] = SSBF(q, imsb, isyma);
+                        double ja_tot = pp_weight_list(c, j, b, alist, na, ja_w);
+                        int a_rev = int_lower_bound(alist, na, a);
+                        pg = (ia_w[a_ind] * jb_w[b_ind]) / (ia_tot * jb_tot) +
+                             (ia_w[b_rev] * ja_w[a_rev]) / (ia_tot * ja_tot);
+                    }
+                    *pgen = c->pattempt_double * pg * pgen_ij;
+                    allowed = 1;
+                }
+            }
+        }
+    }
+    out->allowed = allowed;
+    if (allowed) {
+        out->e.to[0] = a < b ? a : b;
+        out->e.to[1] = a < b ? b : a;
+        out->e.perm = perm2(c, f, out->e.from[0], out->e.from[1], out->e.to[0], out->e.to[1]);
+        *hmatel = sc2_mol_excit(c, out->e.from[0], out->e.from[1], out->e.to[0], out->e.to[1], out->e.perm);
+    } else {
+        out->e.to[0] = out->e.to[1] = -1;
+        *hmatel = 0.0;
+        *pgen = 1.0;
+    }
+}
+
 static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int64_t parent,
                         attempt_t *out) {
     memset(out, 0, sizeof(*out));
@@ -1226,7 +1338,8 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
     /* gen_excit_mol_heat_bath_uniform takes its singles from gen_single_excit_mol
      * (heat_bath_uniform) or gen_single_excit_heat_bath_exact (heat_bath_single) */
     int renorm = gen == HGPU_EXCIT_GEN_RENORM || gen == HGPU_EXCIT_GEN_RENORM_SPIN ||
-                 gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM;
+                 gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM || gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
+                 gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC;
     double pgen, hmatel;
     if (gen == HGPU_EXCIT_GEN_HEAT_BATH) {
         gen_heat_bath(c, rs, f, d, out, &pgen, &hmatel);
@@ -1253,6 +1366,8 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
         }
     } else if (gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM) {
         gen_heat_bath_uniform_double(c, rs, f, d, out, &pgen, &hmatel);
+    } else if (gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC || gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC) {
+        gen_pp_occ_double(c, rs, f, d, out, &pgen, &hmatel);
     } else {
         int i, j, ij_sym, ij_spin, a = -1, b = -1, ok;
         double pgen_ij;

@@ -29,6 +29,8 @@ SYS_READ_IN = 2
 EXCIT_GEN = {
     "renorm": 0, "renorm_spin": 1, "no_renorm": 2, "no_renorm_spin": 3,
     "uniform_power_pitzer": 5, "power_pitzer_orderM": 5, "uniform_cauchy_schwarz": 8, "cauchy_schwarz_orderM": 8,
+    "heat_bath_power_pitzer": 6, "power_pitzer_orderM_ij": 6, "heat_bath_cauchy_schwarz": 9,
+    "cauchy_schwarz_orderM_ij": 9,
     "heat_bath": 10, "heat_bath_uniform": 11, "heat_bath_single": 12,
 }
 

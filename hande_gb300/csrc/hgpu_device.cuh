@@ -1093,7 +1093,9 @@ __device__ void gen_pp_occ_double(const DevSys &s, RStream &rs, const MolDet<W> 
 template <int W, typename Real>
 __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, int64_t parent, Attempt &out) {
     out.from[0] = out.from[1] = out.to[0] = out.to[1] = -1;
-    const bool pp = s.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC || s.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC;
+    const bool pp = s.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC || s.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC ||
+                    s.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
+                    s.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ;
     bool renorm = s.excit_gen == HGPU_EXCIT_GEN_RENORM || s.excit_gen == HGPU_EXCIT_GEN_RENORM_SPIN || pp;
     double pgen;
     Real hm;
@@ -1192,97 +1194,6 @@ __device__ __forceinline__ int hb_alias_draw(RStream &rs, int n, const Real *U, 
     return x < (double)__ldg(&U[k]) ? k : (int)__ldg(&K[k]);
 }
 
-// ---------------------------------------------------------------------------
-// uniform_power_pitzer / uniform_cauchy_schwarz: the double excitations of
-// gen_excit_mol_power_pitzer_occ with uniform i, j
-// (src/excit_gen_power_pitzer_mol.F90:1260-1547)
-// ---------------------------------------------------------------------------
-
-// create_weighted_excitation_list_mol (src/hamiltonian_molecular.f90:348-390):
-// the weights w(p, q) of the set bits q of mask in ascending order (0 for
-// q == skip) into w (when not null) and their sum in that order.
-template <int W, int CAP>
-__device__ __forceinline__ double pp_weights(const DevSys &s, int p, int skip, const uint64_t *mask, double *w) {
-    const double *row = s.pp_w + (size_t)p * s.nbasis;
-    double tot = 0.0;
-    int n = 0;
-#pragma unroll
-    for (int k = 0; k < W; k++)
-        for (uint64_t x = mask[k]; x; x &= x - 1) {
-            const int q = 64 * k + __ffsll((long long)x) - 1;
-            double v = 0.0;
-            if (q != skip) {
-                v = __ldg(&row[q]);
-                tot = tot + v;
-            }
-            if (w != nullptr && n < CAP) w[n] = v;
-            n++;
-        }
-    return tot;
-}
-
-// a from the determinant's unoccupied orbitals of i's spin, b from the orbitals
-// of the spin and irrep that conserve both (a excluded), each through an alias
-// table built for the attempt (select_weighted_value); for parallel spins p_gen
-// adds the reverse order, b from i and a from j.  The weights of the reverse
-// order are read from the table directly: ia_weights(b_ind_rev) = w(i, b) and
-// ja_weights(a_ind_rev) = w(j, a), or 0 when a == b.
-template <int W>
-__device__ void gen_pp_occ_double(const DevSys &s, RStream &rs, const MolDet<W> &d, Attempt &out, double &pgen,
-                                  double &hm) {
-    constexpr int CAP = 32 * W;  // orbitals of one spin
-    const Det<W> &f = d.f;
-    out.nexcit = 2;
-    int i, j;
-    choose_ij_uniform<W>(s, rs, f, i, j);
-    out.from[0] = i;
-    out.from[1] = j;
-    out.to[0] = out.to[1] = -1;
-    out.allowed = false;
-    hm = 0.0;
-    pgen = 1.0;
-    const int ij_sym = xsym(s, s.orbsym[i], s.orbsym[j]);
-    const int ij_spin = ms_of(i) + ms_of(j);
-    const uint64_t spin_mask = ms_of(i) > 0 ? kAlpha : kBeta;
-    uint64_t um[W];
-#pragma unroll
-    for (int k = 0; k < W; k++) um[k] = ~f.w[k] & d.valid[k] & spin_mask;
-    int nv = 0;
-#pragma unroll
-    for (int k = 0; k < W; k++) nv += __popcll(um[k]);
-    if (nv == 0) return;
-    double ia_w[CAP];
-    const double ia_tot = pp_weights<W, CAP>(s, i, -1, um, ia_w);
-    if (!(ia_tot > 0.0)) return;
-    const int a_ind = hb_alias_select<double, CAP>(rs, nv, ia_w, ia_tot);
-    const int a = select_det<W>(um, a_ind);
-    const int isymb = xsym(s, ij_sym, s.orbsym[a]);
-    const int imsb = (ij_spin - ms_of(a) + 1) / 2;  // 0 beta, 1 alpha
-    const int nb = s.nbss[isymb * 2 + imsb];
-    if (nb == 0) return;
-    double jb_w[CAP];
-    const double jb_tot = pp_weights<W, CAP>(s, j, a, &s.symmask[(isymb * 2 + imsb) * W], jb_w);
-    if (!(jb_tot > 0.0)) return;
-    const int b_ind = hb_alias_select<double, CAP>(rs, nb, jb_w, jb_tot);
-    const int b = ssbf<W>(s, imsb, isymb, b_ind);
-    if (tbit<W>(f, b)) return;
-    double pg;
-    if (ij_spin == 0) {
-        pg = ia_w[a_ind] / ia_tot * jb_w[b_ind] / jb_tot;
-    } else {
-        const int isyma = xsym(s, ij_sym, isymb);
-        const double ja_tot = pp_weights<W, CAP>(s, j, b, &s.symmask[(isyma * 2 + imsb) * W], nullptr);
-        const double w_ib = __ldg(&s.pp_w[(size_t)i * s.nbasis + b]);
-        const double w_ja = a == b ? 0.0 : __ldg(&s.pp_w[(size_t)j * s.nbasis + a]);
-        pg = (ia_w[a_ind] * jb_w[b_ind]) / (ia_tot * jb_tot) + (w_ib * w_ja) / (ia_tot * ja_tot);
-    }
-    pgen = s.pattempt_double * pg * s.pgen_ij;
-    out.allowed = true;
-    out.to[0] = a < b ? a : b;
-    out.to[1] = a < b ? b : a;
-    hm = sc2_mol<double>(s, i, j, out.to[0], out.to[1], perm2<W>(f, i, j, out.to[0], out.to[1]));
-}
-
 // psingle of a single i -> a inside the heat-bath double branch
 // (src/excit_gen_heat_bath_mol.F90:396-454): 0 if the single breaks spin or
 // symmetry, |h_ia|/(W + |h_ia|) below W = hb_ijab%weights_tot, else 0.5.
@@ -1338,6 +1249,118 @@ __device__ __forceinline__ bool hb_select_ij(const DevSys &s, const HBView<Real>
         q.ji_tot = q.ji_tot + q.jiw[p];
     }
     return true;
+}
+
+// ---------------------------------------------------------------------------
+// uniform_ and heat_bath_power_pitzer / _cauchy_schwarz: the double
+// excitations of gen_excit_mol_power_pitzer_occ
+// (src/excit_gen_power_pitzer_mol.F90:1260-1547)
+// ---------------------------------------------------------------------------
+
+// create_weighted_excitation_list_mol (src/hamiltonian_molecular.f90:348-390):
+// the weights w(p, q) of the set bits q of mask in ascending order (0 for
+// q == skip) into w (when not null) and their sum in that order.
+template <int W, int CAP>
+__device__ __forceinline__ double pp_weights(const DevSys &s, int p, int skip, const uint64_t *mask, double *w) {
+    const double *row = s.pp_w + (size_t)p * s.nbasis;
+    double tot = 0.0;
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++)
+        for (uint64_t x = mask[k]; x; x &= x - 1) {
+            const int q = 64 * k + __ffsll((long long)x) - 1;
+            double v = 0.0;
+            if (q != skip) {
+                v = __ldg(&row[q]);
+                tot = tot + v;
+            }
+            if (w != nullptr && n < CAP) w[n] = v;
+            n++;
+        }
+    return tot;
+}
+
+// a from the determinant's unoccupied orbitals of i's spin, b from the orbitals
+// of the spin and irrep that conserve both (a excluded), each through an alias
+// table built for the attempt (select_weighted_value); for parallel spins p_gen
+// adds the reverse order, b from i and a from j.  The weights of the reverse
+// order are read from the table directly: ia_weights(b_ind_rev) = w(i, b) and
+// ja_weights(a_ind_rev) = w(j, a), or 0 when a == b.
+template <int W>
+__device__ void gen_pp_occ_double(const DevSys &s, RStream &rs, const MolDet<W> &d, Attempt &out, double &pgen,
+                                  double &hm) {
+    constexpr int CAP = 32 * W;  // orbitals of one spin
+    const Det<W> &f = d.f;
+    out.nexcit = 2;
+    out.to[0] = out.to[1] = -1;
+    out.allowed = false;
+    hm = 0.0;
+    pgen = 1.0;
+    int i, j;
+    double pgen_ij = s.pgen_ij;
+    if (s.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ || s.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ) {
+        // select_ij_heat_bath over ppm_i_d_weights / ppm_ij_d_weights
+        HBView<double> hb(s);
+        HBSel<double> q;
+        const bool ok = hb_select_ij<W, double>(s, hb, rs, f, q);
+        i = q.i;
+        j = q.j;
+        if (ok)
+            pgen_ij = ((q.wi[q.i_ind] / q.wi_tot) * (q.ijw[q.j_ind] / q.ij_tot)) +
+                      ((q.wi[q.j_ind] / q.wi_tot) * (q.jiw[q.i_ind] / q.ji_tot));
+        if (j >= 0 && j < i) {
+            const int t = j;
+            j = i;
+            i = t;
+        }
+        out.from[0] = i;
+        out.from[1] = j;
+        if (!ok) return;
+    } else {
+        choose_ij_uniform<W>(s, rs, f, i, j);
+        out.from[0] = i;
+        out.from[1] = j;
+    }
+    const int ij_sym = xsym(s, s.orbsym[i], s.orbsym[j]);
+    const int ij_spin = ms_of(i) + ms_of(j);
+    const uint64_t spin_mask = ms_of(i) > 0 ? kAlpha : kBeta;
+    uint64_t um[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) um[k] = ~f.w[k] & d.valid[k] & spin_mask;
+    int nv = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) nv += __popcll(um[k]);
+    if (nv == 0) return;
+    double ia_w[CAP];
+    const double ia_tot = pp_weights<W, CAP>(s, i, -1, um, ia_w);
+    if (!(ia_tot > 0.0)) return;
+    const int a_ind = hb_alias_select<double, CAP>(rs, nv, ia_w, ia_tot);
+    const int a = select_det<W>(um, a_ind);
+    const int isymb = xsym(s, ij_sym, s.orbsym[a]);
+    const int imsb = (ij_spin - ms_of(a) + 1) / 2;  // 0 beta, 1 alpha
+    const int nb = s.nbss[isymb * 2 + imsb];
+    if (nb == 0) return;
+    double jb_w[CAP];
+    const double jb_tot = pp_weights<W, CAP>(s, j, a, &s.symmask[(isymb * 2 + imsb) * W], jb_w);
+    if (!(jb_tot > 0.0)) return;
+    const int b_ind = hb_alias_select<double, CAP>(rs, nb, jb_w, jb_tot);
+    const int b = ssbf<W>(s, imsb, isymb, b_ind);
+    if (tbit<W>(f, b)) return;
+    double pg;
+    if (ij_spin == 0) {
+        pg = ia_w[a_ind] / ia_tot * jb_w[b_ind] / jb_tot;
+    } else {
+        const int isyma = xsym(s, ij_sym, isymb);
+        const double ja_tot = pp_weights<W, CAP>(s, j, b, &s.symmask[(isyma * 2 + imsb) * W], nullptr);
+        const double w_ib = __ldg(&s.pp_w[(size_t)i * s.nbasis + b]);
+        const double w_ja = a == b ? 0.0 : __ldg(&s.pp_w[(size_t)j * s.nbasis + a]);
+        pg = (ia_w[a_ind] * jb_w[b_ind]) / (ia_tot * jb_tot) + (w_ib * w_ja) / (ia_tot * ja_tot);
+    }
+    pgen = s.pattempt_double * pg * pgen_ij;
+    out.allowed = true;
+    out.to[0] = a < b ? a : b;
+    out.to[1] = a < b ? b : a;
+    hm = sc2_mol<double>(s, i, j, out.to[0], out.to[1], perm2<W>(f, i, j, out.to[0], out.to[1]));
 }
 
 // gen_excit_mol_heat_bath (src/excit_gen_heat_bath_mol.F90:258-547).

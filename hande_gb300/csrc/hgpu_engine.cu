@@ -461,12 +461,26 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
             c.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE) {
             if ((rc = build_heat_bath(h, sys, s))) return rc;
         }
-        if (c.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC || c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC) {
+        const bool pp_ij = c.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
+                           c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ;
+        if (pp_ij) {
+            // ppm_i_d_weights, ppm_ij_d_weights: read by the heat-bath choice of i, j
+            std::vector<double> iw, ijw;
+            HeatBathBuilder(sys).pair_weights(iw, ijw);
+            const double *p;
+            if ((rc = upload(h, iw.data(), iw.size(), &p))) return rc;
+            s.hb_i_w = p;
+            if ((rc = upload(h, ijw.data(), ijw.size(), &p))) return rc;
+            s.hb_ij_w = p;
+        }
+        if (pp_ij || c.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
+            c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC) {
             // the weights of gen_excit_mol_power_pitzer_occ: sqrt|<pq|qp>| for equal
             // spins, else 0 (get_two_body_int_ex_mol_real), or sqrt|<pq|pq>|
             // (get_two_body_int_cou_mol_real), src/hamiltonian_molecular.f90:392-434
             const int nb = sys->nbasis;
-            const bool cs = c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC;
+            const bool cs = c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC ||
+                            c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ;
             auto tri0 = [](int64_t x, int64_t y) { return x >= y ? x * (x + 1) / 2 + y : y * (y + 1) / 2 + x; };
             std::vector<double> w((size_t)nb * nb);
             for (int p = 0; p < nb; p++)
@@ -703,13 +717,15 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     } else if (sys->kind == HGPU_SYS_READ_IN) {
         bool hb = cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH || cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM ||
                   cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE;
-        const bool pp = cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
+        const bool pp_ij = cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
+                           cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ;
+        const bool pp = pp_ij || cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
                         cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC;
         if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM &&
             cfg->excit_gen != HGPU_EXCIT_GEN_RENORM_SPIN && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM_SPIN && !hb &&
             !pp)
             return HGPU_ERR_UNSUPPORTED;
-        if (hb && sys->nel > kHBMaxEl) return HGPU_ERR_UNSUPPORTED;
+        if ((hb || pp_ij) && sys->nel > kHBMaxEl) return HGPU_ERR_UNSUPPORTED;
         if (pp && cfg->precision != HGPU_PREC_FP64) return HGPU_ERR_UNSUPPORTED;  // FP64 generator only
     } else {
         return HGPU_ERR_INVALID;
@@ -740,7 +756,9 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
         else if (cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM || cfg->excit_gen == HGPU_EXCIT_GEN_NO_RENORM_SPIN)
             h->gkind = kKindReadInNoRenorm;
         else if (cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
-                 cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC)
+                 cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC ||
+                 cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
+                 cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ)
             h->gkind = kKindPowerPitzerOcc;
     }
     h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;

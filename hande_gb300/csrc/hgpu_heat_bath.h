@@ -164,6 +164,35 @@ class HeatBathBuilder {
         return true;
     }
 
+    // init_excit_mol_power_pitzer_orderM_ij (src/excit_gen_power_pitzer_mol.F90:574-648)
+    // with init_double_weights_ab (src/excit_gen_utils.f90:68-138): ij_w[i*nb + j]
+    // is the sum of |<ij||ab>| over the allowed ordered (a, b), a-major, and
+    // i_w[i] the sum of row i in j order; one thread per i.
+    void pair_weights(std::vector<double> &i_w, std::vector<double> &ij_w) const {
+        const int nb = nb_;
+        i_w.assign(nb, 0.0);
+        ij_w.assign((size_t)nb * nb, 0.0);
+        unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+        std::vector<std::thread> pool;
+        for (unsigned w = 0; w < nt; w++) {
+            pool.emplace_back([&, w]() {
+                for (int i = (int)w; i < nb; i += (int)nt) {
+                    double iw = 0.0;
+                    for (int j = 0; j < nb; j++) {
+                        double s = 0.0;
+                        if (i != j)
+                            for (int a = 0; a < nb; a++)
+                                for (int b = 0; b < nb; b++) s = s + weight(i, j, a, b);
+                        ij_w[(size_t)i * nb + j] = s;
+                        iw = iw + s;
+                    }
+                    i_w[i] = iw;
+                }
+            });
+        }
+        for (auto &th : pool) th.join();
+    }
+
     // find_parallel_spin_prob_mol (src/qmc_common.F90:265-378): the share of
     // sum |<ij||ab>| over allowed (i, j, a, b) carried by parallel-spin pairs.
     // The sums run over j, a, b for each i (one thread per i) and the per-i

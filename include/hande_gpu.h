@@ -63,15 +63,18 @@ enum {
 enum { HGPU_SYS_HUB_K = 1, HGPU_SYS_READ_IN = 2 };
 
 /* Excitation generators: same numbering as the excit_gen enum of
- * src/qmc_data.f90:31-68 (4 power_pitzer, 6, 7 and 9 are not provided;
- * HANDE itself refuses 4 for read_in systems, src/check_input.F90:222-226). */
+ * src/qmc_data.f90:31-68 (4 power_pitzer and 7 heat_bath_power_pitzer_ref are
+ * not provided; HANDE itself refuses 4 for read_in systems,
+ * src/check_input.F90:222-226). */
 enum {
     HGPU_EXCIT_GEN_RENORM = 0,
     HGPU_EXCIT_GEN_RENORM_SPIN = 1,
     HGPU_EXCIT_GEN_NO_RENORM = 2,
     HGPU_EXCIT_GEN_NO_RENORM_SPIN = 3,
-    HGPU_EXCIT_GEN_POWER_PITZER_OCC = 5,    /* 'uniform_power_pitzer' */
-    HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC = 8,  /* 'uniform_cauchy_schwarz' */
+    HGPU_EXCIT_GEN_POWER_PITZER_OCC = 5,       /* 'uniform_power_pitzer' */
+    HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ = 6,    /* 'heat_bath_power_pitzer' */
+    HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC = 8,     /* 'uniform_cauchy_schwarz' */
+    HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ = 9,  /* 'heat_bath_cauchy_schwarz' */
     HGPU_EXCIT_GEN_HEAT_BATH = 10,
     HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM = 11,
     HGPU_EXCIT_GEN_HEAT_BATH_SINGLE = 12

@@ -1230,7 +1230,8 @@ static void gen_heat_bath_uniform_double(const oracle_ctx *c, rstream *rs, const
  * (src/molecular_integrals.F90:1147-1177). */
 static double pp_weight(const oracle_ctx *c, int p, int q) {
     double v = 0.0;
-    if (c->cfg.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC) v = v2_get(c, p, q, p, q);
+    if (c->cfg.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC || c->cfg.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ)
+        v = v2_get(c, p, q, p, q);
     else if (c->orb_ms[p] == c->orb_ms[q]) v = v2_get(c, p, q, q, p);
     return sqrt(fabs(v));
 }
@@ -1263,20 +1264,91 @@ static int int_lower_bound(const int *list, int n, int x) {
     return lo;
 }
 
-/* The double excitations of gen_excit_mol_power_pitzer_occ with i, j chosen
- * uniformly (src/excit_gen_power_pitzer_mol.F90:1260-1547): a from the
- * determinant's unoccupied orbitals of i's spin, b from the orbitals of the
- * spin and irrep that conserve both (b /= a), each by an alias table built for
- * the attempt; for parallel spins p_gen adds the reverse order (b from i, a
- * from j). */
+/* init_double_weights_ab (src/excit_gen_utils.f90:68-138): the sum of
+ * |<ij||ab>| over every ordered pair a /= b that conserves spin and symmetry
+ * (occupied orbitals included, i and j excluded), in the reference's loop
+ * order. */
+static double double_weights_ab(const oracle_ctx *c, int i, int j) {
+    const int it = i < j ? i : j, jt = i < j ? j : i;
+    const int ij_sym = cross(c, c->orb_sym[it], c->orb_sym[jt]);
+    double w = 0.0;
+    for (int a = 0; a < c->nbasis; a++) {
+        if (a == it || a == jt) continue;
+        const int isymb = cross(c, ij_sym, c->orb_sym[a]);
+        for (int b = 0; b < c->nbasis; b++) {
+            const int spin = (c->orb_ms[it] == c->orb_ms[a] && c->orb_ms[jt] == c->orb_ms[b]) ||
+                             (c->orb_ms[it] == c->orb_ms[b] && c->orb_ms[jt] == c->orb_ms[a]);
+            if (spin && c->orb_sym[b] == isymb && a != b && b != it && b != jt) {
+                const int at = b < a ? b : a, bt = b < a ? a : b;
+                w = w + fabs(sc2_mol_excit(c, it, jt, at, bt, 0));
+            }
+        }
+    }
+    return w;
+}
+
+/* init_excit_mol_power_pitzer_orderM_ij (src/excit_gen_power_pitzer_mol.F90:574-648):
+ * ppm_ij_d_weights and ppm_i_d_weights (the sum over j in order), kept in
+ * the arrays select_ij_heat_bath reads. */
+static void init_pp_ij(oracle_ctx *c) {
+    const int nb = c->nbasis;
+    c->hb_i_w = (double *)calloc((size_t)nb, sizeof(double));
+    c->hb_ij_w = (double *)calloc((size_t)nb * nb, sizeof(double));
+    for (int i = 0; i < nb; i++) {
+        double i_weight_extra = 0.0;
+        for (int j = 0; j < nb; j++) {
+            double w = 0.0;
+            if (i != j) w = double_weights_ab(c, i, j);
+            c->hb_ij_w[(size_t)i * nb + j] = w;
+            i_weight_extra = i_weight_extra + w;
+        }
+        c->hb_i_w[i] = i_weight_extra;
+    }
+}
+
+/* The double excitations of gen_excit_mol_power_pitzer_occ
+ * (src/excit_gen_power_pitzer_mol.F90:1260-1547): i, j uniform, or by
+ * select_ij_heat_bath over ppm_ij_d_weights for the heat_bath_ variants; a
+ * from the determinant's unoccupied orbitals of i's spin, b from the orbitals
+ * of the spin and irrep that conserve both (b /= a), each by an alias table
+ * built for the attempt; for parallel spins p_gen adds the reverse order (b
+ * from i, a from j). */
 static void gen_pp_occ_double(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d,
                               attempt_t *out, double *pgen, double *hmatel) {
     int i, j, ij_sym, ij_spin;
     double pgen_ij;
     out->e.nexcit = 2;
-    choose_ij_mol(c, rs, d, &i, &j, &ij_sym, &ij_spin, &pgen_ij);
-    out->e.from[0] = i;
-    out->e.from[1] = j;
+    if (c->cfg.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
+        c->cfg.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ) {
+        hb_ij_t q;
+        const int ok = select_ij_heat_bath(c, rs, d, &q);
+        i = q.i;
+        j = q.j;
+        pgen_ij = 0.0;
+        if (ok)
+            pgen_ij = ((q.wi[q.i_ind] / q.wi_tot) * (q.ijw[q.j_ind] / q.ij_tot)) +
+                      ((q.wi[q.j_ind] / q.wi_tot) * (q.jiw[q.i_ind] / q.ji_tot));
+        if (j >= 0 && j < i) {
+            const int t = j;
+            j = i;
+            i = t;
+        }
+        out->e.from[0] = i;
+        out->e.from[1] = j;
+        if (!ok) {
+            out->allowed = 0;
+            out->e.to[0] = out->e.to[1] = -1;
+            *hmatel = 0.0;
+            *pgen = 1.0;
+            return;
+        }
+        ij_sym = cross(c, c->orb_sym[i], c->orb_sym[j]);
+        ij_spin = c->orb_ms[i] + c->orb_ms[j];
+    } else {
+        choose_ij_mol(c, rs, d, &i, &j, &ij_sym, &ij_spin, &pgen_ij);
+        out->e.from[0] = i;
+        out->e.from[1] = j;
+    }
     int unocc[MAXB], nv = 0;
     for (int p = 0; p < c->nbasis; p++)
         if (!tbit(f, p) && c->orb_ms[p] == c->orb_ms[i]) unocc[nv++] = p;
@@ -1337,9 +1409,10 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
     int gen = c->cfg.excit_gen;
     /* gen_excit_mol_heat_bath_uniform takes its singles from gen_single_excit_mol
      * (heat_bath_uniform) or gen_single_excit_heat_bath_exact (heat_bath_single) */
+    const int pp = gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC || gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC ||
+                   gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ || gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ;
     int renorm = gen == HGPU_EXCIT_GEN_RENORM || gen == HGPU_EXCIT_GEN_RENORM_SPIN ||
-                 gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM || gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
-                 gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC;
+                 gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM || pp;
     double pgen, hmatel;
     if (gen == HGPU_EXCIT_GEN_HEAT_BATH) {
         gen_heat_bath(c, rs, f, d, out, &pgen, &hmatel);
@@ -1366,7 +1439,7 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
         }
     } else if (gen == HGPU_EXCIT_GEN_HEAT_BATH_UNIFORM) {
         gen_heat_bath_uniform_double(c, rs, f, d, out, &pgen, &hmatel);
-    } else if (gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC || gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC) {
+    } else if (pp) {
         gen_pp_occ_double(c, rs, f, d, out, &pgen, &hmatel);
     } else {
         int i, j, ij_sym, ij_spin, a = -1, b = -1, ok;
@@ -2213,6 +2286,9 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
             return NULL;
         }
     }
+    if (c->kind == HGPU_SYS_READ_IN && (cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
+                                        cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ))
+        init_pp_ij(c);
     c->fx_E0 = fx_energy(c, c->f0);
     c->H00 = fx_val(c, c->fx_E0);
     c->cap = cfg->walker_length > 0 ? cfg->walker_length : 1000000;

@@ -1,5 +1,6 @@
-"""uniform_power_pitzer and uniform_cauchy_schwarz (gen_excit_mol_power_pitzer_occ
-with uniform i, j, src/excit_gen_power_pitzer_mol.F90:1260-1547) on the GPU
+"""uniform_power_pitzer, uniform_cauchy_schwarz, heat_bath_power_pitzer and
+heat_bath_cauchy_schwarz (gen_excit_mol_power_pitzer_occ,
+src/excit_gen_power_pitzer_mol.F90:1260-1547) on the GPU
 against the oracle: excitations, allowed flags and spawned amounts bit-exact,
 p_gen and H_ij to 1e-12 relative, whole runs bit-exact after every report."""
 
@@ -13,7 +14,7 @@ from tests.test_gpu_parity import SYS, assert_close, engine
 
 pytestmark = pytest.mark.gpu
 
-GENS = ["uniform_power_pitzer", "uniform_cauchy_schwarz"]
+GENS = ["uniform_power_pitzer", "uniform_cauchy_schwarz", "heat_bath_power_pitzer", "heat_bath_cauchy_schwarz"]
 
 
 @pytest.mark.parametrize("name", ["h2o_sto2g", "mol26", "mol40_w2"])
@@ -49,6 +50,10 @@ RUNS = [
                       excit_gen="uniform_cauchy_schwarz", initiator=True), 2),
     ("h2o_sto2g", dict(tau=0.01, init_pop=100, target_population=200, real_amplitudes=True, initial_shift=3.0,
                        excit_gen="uniform_power_pitzer"), 6),
+    ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
+                   excit_gen="heat_bath_power_pitzer", initiator=True), 3),
+    ("mol40_w2", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
+                      excit_gen="heat_bath_cauchy_schwarz"), 2),
 ]
 
 

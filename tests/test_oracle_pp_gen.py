@@ -1,9 +1,12 @@
-"""The oracle's uniform_power_pitzer and uniform_cauchy_schwarz generators
-(gen_excit_mol_power_pitzer_occ with uniform i, j,
-src/excit_gen_power_pitzer_mol.F90:1260-1547) on the CPU.
+"""The oracle's uniform_power_pitzer, uniform_cauchy_schwarz,
+heat_bath_power_pitzer and heat_bath_cauchy_schwarz generators
+(gen_excit_mol_power_pitzer_occ, src/excit_gen_power_pitzer_mol.F90:1260-1547)
+on the CPU.
 
-i, j are uniform over the occupied pairs; a is drawn for i among the
-determinant's unoccupied orbitals of i's spin with weights sqrt|<ia|ai>|
+i, j are uniform over the occupied pairs, or (heat_bath_ variants) i with
+weight sum_j w_ij and j with weight w_ij, w_ij = sum over ordered a /= b of
+|<ij||ab>| (init_double_weights_ab, src/excit_gen_utils.f90:68-138); a is
+drawn for i among the determinant's unoccupied orbitals of i's spin with weights sqrt|<ia|ai>|
 (power_pitzer) or sqrt|<ia|ia>| (cauchy_schwarz), b for j among the orbitals
 of the spin and irrep that conserve both, a excluded.  The probability of an
 excitation is restated here from that definition (both orders for parallel
@@ -11,7 +14,9 @@ spins) and checked against the p_gen the generator returns, and the
 frequencies of many draws from one determinant against both."""
 
 import collections
+import functools
 import math
+import os
 
 import numpy as np
 import pytest
@@ -19,6 +24,8 @@ import pytest
 from hande_gb300 import systems
 from hande_gb300._abi import make_config
 from oracle.pyoracle import Oracle
+from tests.conftest import GOLDEN
+from tests.test_oracle_spin_gen import _sc2_abs
 
 
 def _weight(s, p, q, cs):
@@ -29,9 +36,39 @@ def _weight(s, p, q, cs):
     return math.sqrt(abs(s.v2[systems.v2_index(p >> 1, q >> 1, q >> 1, p >> 1)]))  # <pq|qp> = (pq|qp)
 
 
-def _pgen_double(s, occ, i, j, a, b, cs, pdouble):
+def _ij_weights(s):
+    ms, sym = s.orb_ms, s.orb_sym
+
+    @functools.lru_cache(maxsize=None)
+    def w(i, j):
+        if i == j:
+            return 0.0
+        it, jt = min(i, j), max(i, j)
+        tot = 0.0
+        for a in range(s.nbasis):
+            if a in (it, jt):
+                continue
+            for b in range(s.nbasis):
+                if b in (a, it, jt) or sym[b] != sym[it] ^ sym[jt] ^ sym[a]:
+                    continue
+                if (ms[it] == ms[a] and ms[jt] == ms[b]) or (ms[it] == ms[b] and ms[jt] == ms[a]):
+                    tot += _sc2_abs(s, it, jt, min(a, b), max(a, b))
+        return tot
+    return w
+
+
+def _pij(s, occ, i, j, wij):
+    """select_ij_heat_bath: p(i) p(j|i) + p(j) p(i|j)."""
+    wi = {p: sum(wij(p, q) for q in range(s.nbasis)) for p in occ}
+    ti = sum(wi.values())
+
+    def cond(p, q):
+        return wij(p, q) / sum(wij(p, r) for r in occ)
+    return wi[i] / ti * cond(i, j) + wi[j] / ti * cond(j, i)
+
+
+def _pgen_double(s, occ, i, j, a, b, cs, pdouble, pij):
     """pattempt_double * p(ij) * sum over the orders (x from i, y from j)."""
-    nel = len(occ)
     occs = set(occ)
     ms, sym = s.orb_ms, s.orb_sym
     unocc_i = [p for p in range(s.nbasis) if p not in occs and ms[p] == ms[i]]
@@ -44,19 +81,19 @@ def _pgen_double(s, occ, i, j, a, b, cs, pdouble):
         lst = [p for p in range(s.nbasis) if ms[p] == ms[y] and sym[p] == sym[y]]
         wj = {p: (_weight(s, j, p, cs) if p != x else 0.0) for p in lst}
         tot += wi[x] / ti * wj[y] / sum(wj.values())
-    return pdouble * (2.0 / (nel * (nel - 1))) * tot
+    return pdouble * pij * tot
 
 
-@pytest.mark.parametrize("gen", ["uniform_power_pitzer", "uniform_cauchy_schwarz"])
+@pytest.mark.parametrize("gen", ["uniform_power_pitzer", "uniform_cauchy_schwarz", "heat_bath_power_pitzer",
+                                 "heat_bath_cauchy_schwarz"])
 @pytest.mark.parametrize("sysname", ["synthetic", "h2o"])
 def test_pp_occ_pgen_matches_sampling(gen, sysname):
-    from tests.conftest import GOLDEN
-    import os
     if sysname == "h2o":
         s = systems.read_in(os.path.join(GOLDEN, "H2O-RHF-sto-2g.fcidump"))
     else:
         s = systems.synthetic_molecule(6, 4, seed=3)
-    cs = gen == "uniform_cauchy_schwarz"
+    cs = "cauchy_schwarz" in gen
+    wij = _ij_weights(s) if gen.startswith("heat_bath") else None
     rng = np.random.default_rng(5)
     occs = [s.aufbau_occ()]
     for _ in range(2):
@@ -81,7 +118,9 @@ def test_pp_occ_pgen_matches_sampling(gen, sysname):
         for key, p in pgen.items():
             if key[1] >= 0:
                 ndouble += 1
-                ref = _pgen_double(s, occ, key[0], key[1], key[2], key[3], cs, pdouble)
+                i, j = key[0], key[1]
+                pij = _pij(s, occ, i, j, wij) if wij else 2.0 / (s.nel * (s.nel - 1))
+                ref = _pgen_double(s, occ, i, j, key[2], key[3], cs, pdouble, pij)
                 assert abs(p - ref) <= 1e-12 * ref, (key, p, ref)
         assert ndouble > 10
         total = sum(pgen.values())

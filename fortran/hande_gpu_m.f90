@@ -40,6 +40,7 @@ module hande_gpu_m
         integer(c_uint64_t) :: ref_det(HGPU_MAX_WORDS)
         real(c_double) :: pattempt_parallel
         integer(c_int32_t) :: density_matrices, density_matrix_report
+        real(c_double) :: power_pitzer_min_weight
     end type hgpu_config
 
     type, bind(c) :: hgpu_report

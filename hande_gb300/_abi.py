@@ -30,6 +30,7 @@ EXCIT_GEN = {
     "renorm": 0, "renorm_spin": 1, "no_renorm": 2, "no_renorm_spin": 3,
     "uniform_power_pitzer": 5, "power_pitzer_orderM": 5, "uniform_cauchy_schwarz": 8, "cauchy_schwarz_orderM": 8,
     "heat_bath_power_pitzer": 6, "power_pitzer_orderM_ij": 6, "heat_bath_cauchy_schwarz": 9,
+    "heat_bath_power_pitzer_ref": 7, "power_pitzer_orderN": 7,
     "cauchy_schwarz_orderM_ij": 9,
     "heat_bath": 10, "heat_bath_uniform": 11, "heat_bath_single": 12,
 }
@@ -66,6 +67,7 @@ class HgpuConfig(C.Structure):
         ("seed", C.c_int64), ("walker_length", C.c_int64), ("spawned_walker_length", C.c_int64),
         ("ref_det", C.c_uint64 * MAX_WORDS), ("pattempt_parallel", C.c_double),
         ("density_matrices", C.c_int32), ("density_matrix_report", C.c_int32),
+        ("power_pitzer_min_weight", C.c_double),
     ]
 
 
@@ -166,7 +168,8 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
                 spawn_cutoff: float = 0.01, excit_gen: str = "renorm",
                 pattempt_single: float = -1.0, pattempt_double: float = -1.0,
                 pattempt_parallel: float = -1.0, density_matrices: bool = False,
-                density_matrix_report: int = 0, initiator: bool = False, initiator_threshold: float = 3.0, nspaces: int = 1,
+                density_matrix_report: int = 0, power_pitzer_min_weight: float = 0.01, initiator: bool = False,
+                initiator_threshold: float = 3.0, nspaces: int = 1,
                 precision: int = PREC_FP64, state_size: int = 100000,
                 spawned_state_size: int = 100000, reference=None) -> HgpuConfig:
     """Configuration with HANDE's qmc{} key names (src/lua_hande_calc.f90:1318-1331)."""
@@ -183,6 +186,7 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
     cfg.pattempt_parallel = pattempt_parallel
     cfg.density_matrices = int(bool(density_matrices))
     cfg.density_matrix_report = int(density_matrix_report)
+    cfg.power_pitzer_min_weight = power_pitzer_min_weight
     cfg.D0_population = init_pop
     cfg.vary_shift_from_proje = int(bool(vary_shift_from_proje))
     cfg.excit_gen = EXCIT_GEN[excit_gen] if isinstance(excit_gen, str) else int(excit_gen)

@@ -21,8 +21,8 @@ from .systems import System
 QMC_KEYS = {
     "tau", "init_pop", "mc_cycles", "nreports", "state_size", "spawned_state_size", "rng_seed",
     "target_population", "real_amplitudes", "spawn_cutoff", "excit_gen", "pattempt_single",
-    "pattempt_double", "pattempt_parallel", "initiator", "initiator_threshold", "shift_damping", "vary_shift_from",
-    "initial_shift", "precision",
+    "pattempt_double", "pattempt_parallel", "power_pitzer_min_weight", "initiator", "initiator_threshold",
+    "shift_damping", "vary_shift_from", "initial_shift", "precision",
 }
 FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file"}
 
@@ -53,7 +53,9 @@ def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] =
         real_amplitudes=bool(qmc.get("real_amplitudes", False)), spawn_cutoff=float(qmc.get("spawn_cutoff", 0.01)),
         excit_gen=qmc.get("excit_gen", "renorm"), pattempt_single=float(qmc.get("pattempt_single", -1.0)),
         pattempt_double=float(qmc.get("pattempt_double", -1.0)),
-        pattempt_parallel=float(qmc.get("pattempt_parallel", -1.0)), initiator=bool(qmc.get("initiator", False)),
+        pattempt_parallel=float(qmc.get("pattempt_parallel", -1.0)),
+        power_pitzer_min_weight=float(qmc.get("power_pitzer_min_weight", 0.01)),
+        initiator=bool(qmc.get("initiator", False)),
         initiator_threshold=float(qmc.get("initiator_threshold", 3.0)),
         # density_matrices turns replica_tricks on (src/lua_hande_calc.f90:1569-1573)
         nspaces=2 if (fo.get("replica_tricks") or fo.get("density_matrices")) else 1,

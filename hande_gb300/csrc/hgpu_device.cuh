@@ -100,6 +100,11 @@ struct alignas(16) DevSys {
     // uniform_power_pitzer / uniform_cauchy_schwarz: w(p, q) = sqrt|<pq|qp>| or
     // sqrt|<pq|pq>|, [nbasis][nbasis]
     const double *pp_w;
+    // heat_bath_power_pitzer_ref: six weight / alias tables (hgpu_power_pitzer.h,
+    // index PPN_*), row r entry k at r * ppn_stride[t] + k
+    const double *ppn_w[6], *ppn_U[6], *ppn_tot[6];
+    const uint8_t *ppn_K[6];
+    int ppn_stride[6];
 };
 
 // ---------------------------------------------------------------------------
@@ -1089,6 +1094,12 @@ __device__ __forceinline__ void gen_double_mol(const DevSys &s, RStream &rs, con
 template <int W>
 __device__ void gen_pp_occ_double(const DevSys &s, RStream &rs, const MolDet<W> &d, Attempt &out, double &pgen,
                                   double &hm);
+template <int W>
+__device__ void gen_ppn_single(const DevSys &s, RStream &rs, const MolDet<W> &d, Attempt &out, double &pgen,
+                               double &hm);
+template <int W>
+__device__ void gen_ppn_double(const DevSys &s, RStream &rs, const MolDet<W> &d, Attempt &out, double &pgen,
+                               double &hm);
 
 template <int W, typename Real>
 __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, int64_t parent, Attempt &out) {
@@ -1099,7 +1110,12 @@ __device__ void attempt_mol(const DevSys &s, RStream &rs, const MolDet<W> &d, in
     bool renorm = s.excit_gen == HGPU_EXCIT_GEN_RENORM || s.excit_gen == HGPU_EXCIT_GEN_RENORM_SPIN || pp;
     double pgen;
     Real hm;
-    if (rs.next_k() < s.t_single) {
+    if (s.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_ORDERN) {
+        double h;
+        if (rs.next_k() < s.t_single) gen_ppn_single<W>(s, rs, d, out, pgen, h);
+        else gen_ppn_double<W>(s, rs, d, out, pgen, h);
+        hm = (Real)h;
+    } else if (rs.next_k() < s.t_single) {
         gen_single_mol<W, Real>(s, rs, d, renorm, out, pgen, hm);  // rand < pattempt_single
     } else if (pp) {
         double h;
@@ -1357,6 +1373,169 @@ __device__ void gen_pp_occ_double(const DevSys &s, RStream &rs, const MolDet<W> 
         pg = (ia_w[a_ind] * jb_w[b_ind]) / (ia_tot * jb_tot) + (w_ib * w_ja) / (ia_tot * ja_tot);
     }
     pgen = s.pattempt_double * pg * pgen_ij;
+    out.allowed = true;
+    out.to[0] = a < b ? a : b;
+    out.to[1] = a < b ? b : a;
+    hm = sc2_mol<double>(s, i, j, out.to[0], out.to[1], perm2<W>(f, i, j, out.to[0], out.to[1]));
+}
+
+// ---------------------------------------------------------------------------
+// heat_bath_power_pitzer_ref (gen_excit_mol_power_pitzer_orderN,
+// src/excit_gen_power_pitzer_mol.F90:941-1258)
+// ---------------------------------------------------------------------------
+constexpr int kPPN_IS = 0, kPPN_ID = 1, kPPN_IJD = 2, kPPN_IAS = 3, kPPN_IAD = 4, kPPN_JBD = 5;
+
+// find_diff_ref_cdet (src/excit_gen_utils.f90:220-269): the reference's
+// orbitals missing from the determinant (ascending) and the determinant's
+// extra orbitals (ascending, then swapped forward so that each matches the
+// spin of its hole, as the reference does).
+struct RefMap {
+    uint8_t hole[kHBMaxEl], part[kHBMaxEl];
+    int nex;
+};
+
+template <int W>
+__device__ __forceinline__ void ref_map_build(const DevSys &s, const Det<W> &f, RefMap &m) {
+    int nh = 0, np = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        for (uint64_t x = s.f0[k] & ~f.w[k]; x && nh < kHBMaxEl; x &= x - 1)
+            m.hole[nh++] = (uint8_t)(64 * k + __ffsll((long long)x) - 1);
+        for (uint64_t x = f.w[k] & ~s.f0[k]; x && np < kHBMaxEl; x &= x - 1)
+            m.part[np++] = (uint8_t)(64 * k + __ffsll((long long)x) - 1);
+    }
+    m.nex = nh < np ? nh : np;
+    for (int ii = 0; ii < m.nex; ii++) {
+        const int ms_ref = ms_of(m.hole[ii]);
+        if (ms_ref != ms_of(m.part[ii])) {
+            int jj = ii + 1;
+            while (jj < m.nex && ms_ref != ms_of(m.part[jj])) jj++;
+            if (jj < m.nex) {
+                const uint8_t t = m.part[ii];
+                m.part[ii] = m.part[jj];
+                m.part[jj] = t;
+            }
+        }
+    }
+}
+
+// ref_cdet_occ_list(pos): the determinant's orbital for position pos of the
+// reference's occupied list.
+template <int W>
+__device__ __forceinline__ int ref_map(const DevSys &s, const RefMap &m, int pos) {
+    const int orb = select_det<W>(s.f0, pos);
+    for (int k = 0; k < m.nex; k++)
+        if (m.hole[k] == orb) return m.part[k];
+    return orb;
+}
+
+// Number of set bits of mask below bit p (the position of p in the ascending
+// list the mask stands for).
+template <int W>
+__device__ __forceinline__ int rank_in_mask(const uint64_t *mask, int p) {
+    int r = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        if (64 * k + 64 <= p) r += __popcll(mask[k]);
+        else if (64 * k < p) r += __popcll(mask[k] & ((1ull << (p - 64 * k)) - 1));
+    }
+    return r;
+}
+
+__device__ __forceinline__ double ppn_w(const DevSys &s, int t, int r, int k) {
+    return __ldg(&s.ppn_w[t][(size_t)r * s.ppn_stride[t] + k]);
+}
+
+__device__ __forceinline__ int ppn_draw(const DevSys &s, RStream &rs, int t, int r, int n) {
+    const size_t off = (size_t)r * s.ppn_stride[t];
+    return hb_alias_draw<double>(rs, n, s.ppn_U[t] + off, s.ppn_K[t] + off);
+}
+
+// Single excitation: i from the reference's list, a from i's (spin, irrep) table.
+template <int W>
+__device__ void gen_ppn_single(const DevSys &s, RStream &rs, const MolDet<W> &d, Attempt &out, double &pgen,
+                               double &hm) {
+    const Det<W> &f = d.f;
+    RefMap m;
+    ref_map_build<W>(s, f, m);
+    out.nexcit = 1;
+    out.allowed = false;
+    out.to[0] = -1;
+    pgen = 1.0;
+    hm = 0.0;
+    const int i_ind = ppn_draw(s, rs, kPPN_IS, 0, s.nel);
+    const int i = ref_map<W>(s, m, i_ind);
+    out.from[0] = i;
+    const int ims = (ms_of(i) + 1) / 2, sym = s.orbsym[i];
+    const int na = s.nbss[sym * 2 + ims];
+    if (na <= 0) return;
+    const int a_ind = ppn_draw(s, rs, kPPN_IAS, i, na);
+    const int a = ssbf<W>(s, ims, sym, a_ind);
+    if (tbit<W>(f, a)) return;
+    out.allowed = true;
+    out.to[0] = a;
+    pgen = (ppn_w(s, kPPN_IS, 0, i_ind) / __ldg(&s.ppn_tot[kPPN_IS][0])) *
+           (ppn_w(s, kPPN_IAS, i, a_ind) / __ldg(&s.ppn_tot[kPPN_IAS][i]));
+    pgen = s.pattempt_single * pgen;
+    hm = sc1_mol<W, double>(s, f, i, a, perm1<W>(f, i, a));
+}
+
+// Double excitation: i, j positions of the reference's list mapped onto the
+// determinant, a over all orbitals of i's spin, b over the (spin, irrep) that
+// conserves both; p_gen adds the reverse order of a, b for parallel spins.
+template <int W>
+__device__ void gen_ppn_double(const DevSys &s, RStream &rs, const MolDet<W> &d, Attempt &out, double &pgen,
+                               double &hm) {
+    const Det<W> &f = d.f;
+    RefMap m;
+    ref_map_build<W>(s, f, m);
+    out.nexcit = 2;
+    out.allowed = false;
+    out.to[0] = out.to[1] = -1;
+    pgen = 1.0;
+    hm = 0.0;
+    const int i_ind = ppn_draw(s, rs, kPPN_ID, 0, s.nel);
+    int i = ref_map<W>(s, m, i_ind);
+    const int j_ind = ppn_draw(s, rs, kPPN_IJD, i, s.nel);
+    int j = ref_map<W>(s, m, j_ind);
+    out.from[0] = i;
+    out.from[1] = j;
+    if (j == i) return;
+    const double tot_id = __ldg(&s.ppn_tot[kPPN_ID][0]);
+    double pg = (ppn_w(s, kPPN_ID, 0, i_ind) / tot_id) * (ppn_w(s, kPPN_IJD, i, j_ind) / __ldg(&s.ppn_tot[kPPN_IJD][i]));
+    const int ij_spin = ms_of(i) + ms_of(j);
+    pg = pg + ((ppn_w(s, kPPN_ID, 0, j_ind) / tot_id) * (ppn_w(s, kPPN_IJD, j, i_ind) / __ldg(&s.ppn_tot[kPPN_IJD][j])));
+    if (j < i) {
+        const int t = j;
+        j = i;
+        i = t;
+    }
+    out.from[0] = i;
+    out.from[1] = j;
+    const int a_ind = ppn_draw(s, rs, kPPN_IAD, i, s.nbasis / 2);
+    const int a = 2 * a_ind + (ms_of(i) > 0 ? 0 : 1);
+    if (tbit<W>(f, a)) return;
+    const int ij_sym = xsym(s, s.orbsym[i], s.orbsym[j]);
+    const int isymb = xsym(s, ij_sym, s.orbsym[a]);
+    const int imsb = (ms_of(j) + 1) / 2;
+    const int nbb = s.nbss[isymb * 2 + imsb];
+    if (nbb == 0) return;
+    const int rb = j * s.nsym + isymb;
+    const int b_ind = ppn_draw(s, rs, kPPN_JBD, rb, nbb);
+    const int b = ssbf<W>(s, imsb, isymb, b_ind);
+    if (a == b || tbit<W>(f, b)) return;
+    const double tot_a = __ldg(&s.ppn_tot[kPPN_IAD][i]), tot_b = __ldg(&s.ppn_tot[kPPN_JBD][rb]);
+    if (ij_spin == 0) {
+        pg = pg * (ppn_w(s, kPPN_IAD, i, a_ind) / tot_a * ppn_w(s, kPPN_JBD, rb, b_ind) / tot_b);
+    } else {
+        const int isyma = xsym(s, ij_sym, isymb);
+        const int ra = j * s.nsym + isyma;
+        const int a_rev = rank_in_mask<W>(&s.symmask[(isyma * 2 + imsb) * W], a);
+        pg = pg * (ppn_w(s, kPPN_IAD, i, a_ind) / tot_a * ppn_w(s, kPPN_JBD, rb, b_ind) / tot_b +
+                   ppn_w(s, kPPN_IAD, i, b >> 1) / tot_a * ppn_w(s, kPPN_JBD, ra, a_rev) /
+                       __ldg(&s.ppn_tot[kPPN_JBD][ra]));
+    }
+    pgen = s.pattempt_double * pg;
     out.allowed = true;
     out.to[0] = a < b ? a : b;
     out.to[1] = a < b ? b : a;

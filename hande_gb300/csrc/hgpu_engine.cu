@@ -18,6 +18,7 @@
 
 #include "../../include/hande_gpu.h"
 #include "hgpu_heat_bath.h"
+#include "hgpu_power_pitzer.h"
 #include "hgpu_kernels.cuh"
 
 using namespace hgpu;
@@ -473,6 +474,23 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
             if ((rc = upload(h, ijw.data(), ijw.size(), &p))) return rc;
             s.hb_ij_w = p;
         }
+        if (c.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_ORDERN) {
+            PPNTables t;
+            PowerPitzerRefBuilder(sys, c.ref_det, c.power_pitzer_min_weight).build(t);
+            for (int k = 0; k < PPN_NTAB; k++) {
+                const double *p;
+                const uint8_t *q;
+                if ((rc = upload(h, t.w[k].data(), t.w[k].size(), &p))) return rc;
+                s.ppn_w[k] = p;
+                if ((rc = upload(h, t.U[k].data(), t.U[k].size(), &p))) return rc;
+                s.ppn_U[k] = p;
+                if ((rc = upload(h, t.tot[k].data(), t.tot[k].size(), &p))) return rc;
+                s.ppn_tot[k] = p;
+                if ((rc = upload(h, t.K[k].data(), t.K[k].size(), &q))) return rc;
+                s.ppn_K[k] = q;
+                s.ppn_stride[k] = t.stride[k];
+            }
+        }
         if (pp_ij || c.excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
             c.excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC) {
             // the weights of gen_excit_mol_power_pitzer_occ: sqrt|<pq|qp>| for equal
@@ -719,17 +737,20 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
                   cfg->excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE;
         const bool pp_ij = cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
                            cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ;
-        const bool pp = pp_ij || cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
+        const bool ppn = cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_ORDERN;
+        const bool pp = pp_ij || ppn || cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC ||
                         cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC;
         if (cfg->excit_gen != HGPU_EXCIT_GEN_RENORM && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM &&
             cfg->excit_gen != HGPU_EXCIT_GEN_RENORM_SPIN && cfg->excit_gen != HGPU_EXCIT_GEN_NO_RENORM_SPIN && !hb &&
             !pp)
             return HGPU_ERR_UNSUPPORTED;
-        if ((hb || pp_ij) && sys->nel > kHBMaxEl) return HGPU_ERR_UNSUPPORTED;
+        if ((hb || pp_ij || ppn) && sys->nel > kHBMaxEl) return HGPU_ERR_UNSUPPORTED;
         if (pp && cfg->precision != HGPU_PREC_FP64) return HGPU_ERR_UNSUPPORTED;  // FP64 generator only
     } else {
         return HGPU_ERR_INVALID;
     }
+    // src/check_input.F90:182-184
+    if (!(cfg->power_pitzer_min_weight >= 0.0 && cfg->power_pitzer_min_weight <= 1.0)) return HGPU_ERR_INVALID;
     // density_matrices: replica sampling of molecular systems (two spaces)
     if (cfg->density_matrices && (sys->kind != HGPU_SYS_READ_IN || cfg->nspaces != 2)) return HGPU_ERR_INVALID;
     // pattempt_parallel only with the spin-resolved generators, at most 1
@@ -760,6 +781,8 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
                  cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
                  cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ)
             h->gkind = kKindPowerPitzerOcc;
+        else if (cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_ORDERN)
+            h->gkind = kKindPowerPitzerRef;
     }
     h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;
     cudaGetDevice(&h->device);

@@ -385,6 +385,8 @@ static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur
     else if (kind == kKindReadInNoRenorm) HGPU_SPAWN(kKindReadInNoRenorm);
     else if (kind == kKindPowerPitzerOcc)
         k_spawn<W, kKindPowerPitzerOcc, double, false><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+    else if (kind == kKindPowerPitzerRef)
+        k_spawn<W, kKindPowerPitzerRef, double, false><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
     else HGPU_SPAWN(HGPU_SYS_READ_IN);
 #undef HGPU_SPAWN
     if (pm) cudaEventRecord(pm->ev[3], st);

@@ -16,7 +16,8 @@ constexpr int kBlock = 256;      // threads per block of the streaming kernels
 constexpr int kKindHeatBath = 3;         // molecular, heat_bath
 constexpr int kKindReadInNoRenorm = 4;   // molecular, uniform no_renorm generator
 constexpr int kKindHeatBathUniform = 5;  // molecular, heat_bath_uniform
-constexpr int kKindPowerPitzerOcc = 6;   // molecular, uniform_power_pitzer / uniform_cauchy_schwarz (FP64)
+constexpr int kKindPowerPitzerOcc = 6;   // molecular, uniform_ / heat_bath_ power_pitzer, cauchy_schwarz (FP64)
+constexpr int kKindPowerPitzerRef = 7;   // molecular, heat_bath_power_pitzer_ref (FP64)
 // Radix sort of the spawned list (hgpu_sort.cuh): 8-bit digits, at most
 // kMaxPasses passes, tiles of kOSThreads x items keys of KW words each.
 constexpr int kOSThreads = 256;  // one thread per digit value in the look-back

@@ -67,11 +67,19 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
         if (KIND == kKindHeatBath) gen_heat_bath<W, Real>(s, rs, f, at, pgen, hm);
         else if (single && KIND == kKindHeatBathUniform && s.excit_gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE)
             gen_single_hb_exact<W, Real>(s, rs, d, at, pgen, hm);
-        else if (single) gen_single_mol<W, Real>(s, rs, d, KIND != kKindReadInNoRenorm, at, pgen, hm);
+        else if (single && KIND == kKindPowerPitzerRef) {
+            double h;
+            gen_ppn_single<W>(s, rs, d, at, pgen, h);
+            hm = (Real)h;
+        } else if (single) gen_single_mol<W, Real>(s, rs, d, KIND != kKindReadInNoRenorm, at, pgen, hm);
         else if (KIND == kKindHeatBathUniform) gen_heat_bath_uniform_double<W, Real>(s, rs, f, at, pgen, hm);
         else if (KIND == kKindPowerPitzerOcc) {
             double h;
             gen_pp_occ_double<W>(s, rs, d, at, pgen, h);
+            hm = (Real)h;
+        } else if (KIND == kKindPowerPitzerRef) {
+            double h;
+            gen_ppn_double<W>(s, rs, d, at, pgen, h);
             hm = (Real)h;
         } else gen_double_mol<W, Real>(s, rs, d, KIND == HGPU_SYS_READ_IN, at, pgen, hm);
         attempt_to_spawn(s, rs, parent, pgen, (double)hm, at);
@@ -117,7 +125,7 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
     // split by that draw so that each excitation type runs with the warp
     // converged (a tenth of the attempts are singles, with their own code)
     constexpr bool drew = KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm || KIND == kKindHeatBathUniform ||
-                          KIND == kKindPowerPitzerOcc;
+                          KIND == kKindPowerPitzerOcc || KIND == kKindPowerPitzerRef;
     // Each warp claims chunks of kSpawnChunk consecutive attempts.  The (parent,
     // space) slot of attempt a is the first k with aoff[k] > a; one binary search
     // per chunk finds the slot of its first attempt, and every later step of 32

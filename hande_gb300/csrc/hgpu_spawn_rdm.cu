@@ -20,6 +20,8 @@ static void spawn_rdm_w(const DevBuffers &b, int R, int kind, int precision, int
     else if (kind == kKindReadInNoRenorm) HGPU_SPAWN_RDM(kKindReadInNoRenorm);
     else if (kind == kKindPowerPitzerOcc)
         k_spawn<W, kKindPowerPitzerOcc, double, true><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+    else if (kind == kKindPowerPitzerRef)
+        k_spawn<W, kKindPowerPitzerRef, double, true><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
     else HGPU_SPAWN_RDM(HGPU_SYS_READ_IN);
 #undef HGPU_SPAWN_RDM
 }

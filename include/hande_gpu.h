@@ -63,9 +63,8 @@ enum {
 enum { HGPU_SYS_HUB_K = 1, HGPU_SYS_READ_IN = 2 };
 
 /* Excitation generators: same numbering as the excit_gen enum of
- * src/qmc_data.f90:31-68 (4 power_pitzer and 7 heat_bath_power_pitzer_ref are
- * not provided; HANDE itself refuses 4 for read_in systems,
- * src/check_input.F90:222-226). */
+ * src/qmc_data.f90:31-68 (4 power_pitzer is not provided: HANDE itself refuses
+ * it for read_in systems, src/check_input.F90:222-226). */
 enum {
     HGPU_EXCIT_GEN_RENORM = 0,
     HGPU_EXCIT_GEN_RENORM_SPIN = 1,
@@ -73,6 +72,7 @@ enum {
     HGPU_EXCIT_GEN_NO_RENORM_SPIN = 3,
     HGPU_EXCIT_GEN_POWER_PITZER_OCC = 5,       /* 'uniform_power_pitzer' */
     HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ = 6,    /* 'heat_bath_power_pitzer' */
+    HGPU_EXCIT_GEN_POWER_PITZER_ORDERN = 7,    /* 'heat_bath_power_pitzer_ref' */
     HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC = 8,     /* 'uniform_cauchy_schwarz' */
     HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ = 9,  /* 'heat_bath_cauchy_schwarz' */
     HGPU_EXCIT_GEN_HEAT_BATH = 10,
@@ -148,6 +148,10 @@ typedef struct hgpu_config {
                                       (src/replica_rdm.F90); needs nspaces = 2, molecular systems */
     int32_t density_matrix_report; /* fciqmc_in%density_matrix_report: accumulate from the first
                                       report after this one in which every shift varies */
+    double power_pitzer_min_weight;  /* qmc_in%power_pitzer_min_weight (HANDE's default 0.01):
+                                        floor, as a share of the mean, of the weights of
+                                        heat_bath_power_pitzer_ref's i, j and single tables
+                                        (check_min_weight_ratio); must lie in [0, 1] */
 } hgpu_config;
 
 /* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */

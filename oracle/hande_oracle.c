@@ -164,6 +164,17 @@ struct oracle_ctx {
     uint64_t *rsdets;
     int64_t *rspops;
     double rdm_energy, rdm_trace;
+    /* heat_bath_power_pitzer_ref (excit_gen_power_pitzer_t of
+     * init_excit_mol_power_pitzer_orderN): the reference's occupied list and
+     * six weight/alias tables, PPN_IS (i for singles, [nel]), PPN_ID (i for
+     * doubles, [nel]), PPN_IJD (j given the orbital i, [nbasis][nel]), PPN_IAS
+     * (a of a single, [nbasis][maxss]), PPN_IAD (a of a double over all
+     * orbitals of i's spin, [nbasis][nbasis/2]), PPN_JBD (b per irrep,
+     * [nbasis*nsym][maxss]) */
+    int ppn_occ[MAXEL];
+    double *ppn_w[6], *ppn_U[6], *ppn_tot[6];
+    int32_t *ppn_K[6];
+    int ppn_stride[6];
     int hb_on;
     double *hb_i_w, *hb_ij_w, *hb_ija_w, *hb_ija_tot, *hb_ija_U, *hb_ijab_w, *hb_ijab_tot, *hb_ijab_U;
     int32_t *hb_ija_K, *hb_ijab_K;
@@ -1267,11 +1278,10 @@ static int int_lower_bound(const int *list, int n, int x) {
 /* init_double_weights_ab (src/excit_gen_utils.f90:68-138): the sum of
  * |<ij||ab>| over every ordered pair a /= b that conserves spin and symmetry
  * (occupied orbitals included, i and j excluded), in the reference's loop
- * order. */
-static double double_weights_ab(const oracle_ctx *c, int i, int j) {
+ * order, added to w (the argument is intent(inout) there). */
+static double double_weights_ab(const oracle_ctx *c, int i, int j, double w) {
     const int it = i < j ? i : j, jt = i < j ? j : i;
     const int ij_sym = cross(c, c->orb_sym[it], c->orb_sym[jt]);
-    double w = 0.0;
     for (int a = 0; a < c->nbasis; a++) {
         if (a == it || a == jt) continue;
         const int isymb = cross(c, ij_sym, c->orb_sym[a]);
@@ -1298,7 +1308,7 @@ static void init_pp_ij(oracle_ctx *c) {
         double i_weight_extra = 0.0;
         for (int j = 0; j < nb; j++) {
             double w = 0.0;
-            if (i != j) w = double_weights_ab(c, i, j);
+            if (i != j) w = double_weights_ab(c, i, j, 0.0);
             c->hb_ij_w[(size_t)i * nb + j] = w;
             i_weight_extra = i_weight_extra + w;
         }
@@ -1402,6 +1412,303 @@ static void gen_pp_occ_double(const oracle_ctx *c, rstream *rs, const uint64_t *
     }
 }
 
+/* ------------------------------------------------------------------------- */
+/* heat_bath_power_pitzer_ref (src/excit_gen_power_pitzer_mol.F90:215-572,    */
+/* 941-1258)                                                                  */
+/* ------------------------------------------------------------------------- */
+
+enum { PPN_IS = 0, PPN_ID = 1, PPN_IJD = 2, PPN_IAS = 3, PPN_IAD = 4, PPN_JBD = 5 };
+#define PPN_W(c, t, r, k) ((c)->ppn_w[t][(size_t)(r) * (c)->ppn_stride[t] + (k)])
+
+/* check_min_weight_ratio (src/excit_gen_power_pitzer_mol.F90:140-213): raises
+ * the non-zero weights below min_weight, chosen so that they carry min_ratio
+ * of their mean share, and recomputes the total. */
+static void min_weight_ratio(double *w, double *tot, int n, double min_ratio) {
+    double min_weight_tmp = 0.0, min_weight;
+    int nz = 0;
+    if (!(*tot > 0.0 && min_ratio > 0.0)) return;
+    for (int i = 0; i < n; i++)
+        if (w[i] > 0.0) nz++;
+    min_weight = (min_ratio / (double)nz) * *tot;
+    for (int it = 0; it < 100000 && fabs(min_weight_tmp - min_weight) > DEPSILON; it++) {
+        min_weight_tmp = min_weight;
+        double keep = 0.0;
+        int cnt = 0;
+        for (int k = 0; k < n; k++) {
+            if (w[k] > 0.0 && w[k] < min_weight) cnt++;
+            else keep = keep + w[k];
+        }
+        if (cnt == nz) break;
+        min_weight = (min_ratio / (double)nz) * (keep / (1.0 - (min_ratio * (double)cnt / (double)nz)));
+    }
+    double t = 0.0;
+    for (int j = 0; j < n; j++) {
+        if (w[j] > 0.0 && w[j] < min_weight) w[j] = min_weight;
+        t = t + w[j];
+    }
+    *tot = t;
+}
+
+/* single_excitation_weight_mol (src/hamiltonian_molecular.f90:444-523): the
+ * mean over the reference's occupied j and virtual b of
+ * |<ij|ja> - <ij|aj> + <ib|ab> - <ib|ba>|, each integral zero unless its spins
+ * match (get_two_body_int_mol_real); a has i's irrep in every call. */
+static double single_excitation_weight(const oracle_ctx *c, int i, int a) {
+    const int *ms = c->orb_ms;
+    int n_jb = 0;
+    double weight = 0.0;
+    for (int jj = 0; jj < c->nel; jj++) {
+        const int j = c->ppn_occ[jj];
+        for (int b = 0; b < c->nbasis; b++) {
+            if (tbit(c->f0, b)) continue;
+            n_jb++;
+            const double t1 = (ms[i] == ms[j] && ms[j] == ms[a]) ? v2_get(c, i, j, j, a) : 0.0;
+            const double t2 = ms[i] == ms[a] ? v2_get(c, i, j, a, j) : 0.0;
+            const double t3 = ms[i] == ms[a] ? v2_get(c, i, b, a, b) : 0.0;
+            const double t4 = (ms[i] == ms[b] && ms[b] == ms[a]) ? v2_get(c, i, b, b, a) : 0.0;
+            weight = weight + fabs(t1 - t2 + t3 - t4);
+        }
+    }
+    return weight / (double)n_jb;
+}
+
+static void ppn_alloc(oracle_ctx *c, int t, int rows, int stride) {
+    c->ppn_stride[t] = stride;
+    c->ppn_w[t] = (double *)calloc((size_t)rows * stride, sizeof(double));
+    c->ppn_U[t] = (double *)calloc((size_t)rows * stride, sizeof(double));
+    c->ppn_K[t] = (int32_t *)calloc((size_t)rows * stride, sizeof(int32_t));
+    c->ppn_tot[t] = (double *)calloc((size_t)rows, sizeof(double));
+}
+
+/* Row r of table t: optional min-weight floor, then its alias table. */
+static void ppn_finish_row(oracle_ctx *c, int t, int r, int n, int floor) {
+    double *w = &PPN_W(c, t, r, 0);
+    if (floor) min_weight_ratio(w, &c->ppn_tot[t][r], n, c->cfg.power_pitzer_min_weight);
+    alias_build(n, w, c->ppn_tot[t][r], &c->ppn_U[t][(size_t)r * c->ppn_stride[t]],
+                &c->ppn_K[t][(size_t)r * c->ppn_stride[t]]);
+}
+
+/* init_excit_mol_power_pitzer_orderN (src/excit_gen_power_pitzer_mol.F90:215-572). */
+static void init_ppn(oracle_ctx *c) {
+    const int nel = c->nel, nb = c->nbasis, half = nb / 2;
+    int n = 0;
+    for (int p = 0; p < nb; p++)
+        if (tbit(c->f0, p)) c->ppn_occ[n++] = p;
+    ppn_alloc(c, PPN_IS, 1, nel);
+    ppn_alloc(c, PPN_ID, 1, nel);
+    ppn_alloc(c, PPN_IJD, nb, nel);
+    ppn_alloc(c, PPN_IAS, nb, c->maxss);
+    ppn_alloc(c, PPN_IAD, nb, half);
+    ppn_alloc(c, PPN_JBD, nb * c->nsym, c->maxss);
+    /* i of a single: summed single weights over a of i's spin and irrep */
+    for (int i = 0; i < nel; i++) {
+        const int oi = c->ppn_occ[i];
+        double w = 0.0;
+        for (int a = 0; a < nb; a++)
+            if (a != oi && c->orb_sym[a] == c->orb_sym[oi] && c->orb_ms[a] == c->orb_ms[oi])
+                w = w + single_excitation_weight(c, oi, a);
+        if (w < DEPSILON) w = 10.0 * DEPSILON;
+        PPN_W(c, PPN_IS, 0, i) = w;
+    }
+    for (int i = 0; i < nel; i++) c->ppn_tot[PPN_IS][0] = c->ppn_tot[PPN_IS][0] + PPN_W(c, PPN_IS, 0, i);
+    ppn_finish_row(c, PPN_IS, 0, nel, 1);
+    /* a of a single from any orbital i */
+    for (int i = 0; i < nb; i++) {
+        const int ims = ims_of(c, i), sym = c->orb_sym[i], na = NBSS(ims, sym);
+        double tot = 0.0;
+        for (int a = 0; a < na; a++) {
+            double w = 0.0;
+            const int q = SSBF(a, ims, sym);
+            if (q != i) {
+                w = single_excitation_weight(c, i, q);
+                if (w < DEPSILON) w = 10.0 * DEPSILON;
+            }
+            PPN_W(c, PPN_IAS, i, a) = w;
+            tot = tot + w;
+        }
+        c->ppn_tot[PPN_IAS][i] = tot;
+        ppn_finish_row(c, PPN_IAS, i, na, 1);
+    }
+    /* i of a double: one accumulator over j and then a, b */
+    for (int i = 0; i < nel; i++) {
+        double w = 0.0;
+        for (int j = 0; j < nel; j++)
+            if (i != j) w = double_weights_ab(c, c->ppn_occ[i], c->ppn_occ[j], w);
+        if (w < DEPSILON) w = 10.0 * DEPSILON;
+        PPN_W(c, PPN_ID, 0, i) = w;
+    }
+    for (int i = 0; i < nel; i++) c->ppn_tot[PPN_ID][0] = c->ppn_tot[PPN_ID][0] + PPN_W(c, PPN_ID, 0, i);
+    ppn_finish_row(c, PPN_ID, 0, nel, 1);
+    /* j (a position in the reference's list) given any orbital i */
+    for (int i = 0; i < nb; i++) {
+        double tot = 0.0;
+        for (int j = 0; j < nel; j++) {
+            double w = 0.0;
+            if (c->ppn_occ[j] != i) w = double_weights_ab(c, i, c->ppn_occ[j], 0.0);
+            if (w < DEPSILON) w = 10.0 * DEPSILON;
+            PPN_W(c, PPN_IJD, i, j) = w;
+            tot = tot + w;
+        }
+        c->ppn_tot[PPN_IJD][i] = tot;
+        ppn_finish_row(c, PPN_IJD, i, nel, 1);
+    }
+    /* a of a double over all orbitals of i's spin, b per irrep (i itself weighted 0) */
+    for (int i = 0; i < nb; i++) {
+        const int ims = ims_of(c, i);
+        int list[MAXB];
+        for (int k = 0; k < half; k++) list[k] = 2 * k + (ims == 0);
+        c->ppn_tot[PPN_IAD][i] = pp_weight_list(c, i, i, list, half, &PPN_W(c, PPN_IAD, i, 0));
+        ppn_finish_row(c, PPN_IAD, i, half, 0);
+        for (int bsym = 0; bsym < c->nsym; bsym++) {
+            const int nbs = NBSS(ims, bsym), r = i * c->nsym + bsym;
+            if (nbs <= 0) continue;
+            for (int q = 0; q < nbs; q++) list[q] = SSBF(q, ims, bsym);
+            c->ppn_tot[PPN_JBD][r] = pp_weight_list(c, i, i, list, nbs, &PPN_W(c, PPN_JBD, r, 0));
+            ppn_finish_row(c, PPN_JBD, r, nbs, 0);
+        }
+    }
+}
+
+/* find_diff_ref_cdet (src/excit_gen_utils.f90:220-269) with
+ * get_excitation_locations (src/excitations.F90:467-543): for each position of
+ * the reference's occupied list, the determinant's orbital standing in for it
+ * (itself when occupied in both; otherwise the determinant's extra orbitals in
+ * order, swapped forward to match spins). */
+static void ref_cdet_occ_list(const oracle_ctx *c, const uint64_t *f, const det_info *d, int *map) {
+    int ref_store[MAXEL], det_store[MAXEL], nex = 0, np = 0;
+    for (int k = 0; k < c->nel; k++) {
+        map[k] = c->ppn_occ[k];
+        if (!tbit(f, c->ppn_occ[k])) ref_store[nex++] = k;
+    }
+    for (int k = 0; k < c->nel; k++)
+        if (!tbit(c->f0, d->occ[k])) det_store[np++] = k;
+    for (int ii = 0; ii < nex; ii++) {
+        const int ms_ref = c->orb_ms[c->ppn_occ[ref_store[ii]]];
+        if (ms_ref != c->orb_ms[d->occ[det_store[ii]]]) {
+            int jj = ii + 1;
+            while (jj < nex && ms_ref != c->orb_ms[d->occ[det_store[jj]]]) jj++;
+            if (jj < nex) {
+                const int t = det_store[ii];
+                det_store[ii] = det_store[jj];
+                det_store[jj] = t;
+            }
+        }
+        map[ref_store[ii]] = d->occ[det_store[ii]];
+    }
+}
+
+/* gen_excit_mol_power_pitzer_orderN (src/excit_gen_power_pitzer_mol.F90:941-1258):
+ * i (and j) drawn as positions of the reference's occupied list and mapped
+ * onto the determinant; a, b from the precomputed tables of the mapped
+ * orbitals. */
+static void gen_ppn(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, attempt_t *out,
+                    double *pgen_out, double *hmatel_out) {
+    int map[MAXEL];
+    ref_cdet_occ_list(c, f, d, map);
+    const int nel = c->nel;
+    int allowed = 0;
+    double pgen = 1.0, hmatel = 0.0;
+    if (rs_next(rs) < c->pattempt_single) {
+        out->e.nexcit = 1;
+        const int i_ind = alias_draw(rs, nel, c->ppn_U[PPN_IS], c->ppn_K[PPN_IS]);
+        const int i = map[i_ind];
+        const int ims = ims_of(c, i), sym = c->orb_sym[i], na = NBSS(ims, sym);
+        int a = -1, a_ind = -1;
+        if (na > 0) {
+            const size_t off = (size_t)i * c->ppn_stride[PPN_IAS];
+            a_ind = alias_draw(rs, na, c->ppn_U[PPN_IAS] + off, c->ppn_K[PPN_IAS] + off);
+            a = SSBF(a_ind, ims, sym);
+            allowed = !tbit(f, a);
+        }
+        out->e.from[0] = i;
+        out->e.to[0] = allowed ? a : -1;
+        if (allowed) {
+            pgen = (PPN_W(c, PPN_IS, 0, i_ind) / c->ppn_tot[PPN_IS][0]) *
+                   (PPN_W(c, PPN_IAS, i, a_ind) / c->ppn_tot[PPN_IAS][i]);
+            pgen = c->pattempt_single * pgen;
+            out->e.perm = perm1(c, f, i, a);
+            hmatel = sc1_mol_excit(c, d->occ, i, a, out->e.perm);
+        }
+    } else {
+        out->e.nexcit = 2;
+        const int i_ind = alias_draw(rs, nel, c->ppn_U[PPN_ID], c->ppn_K[PPN_ID]);
+        int i = map[i_ind];
+        const size_t offj = (size_t)i * c->ppn_stride[PPN_IJD];
+        const int j_ind = alias_draw(rs, nel, c->ppn_U[PPN_IJD] + offj, c->ppn_K[PPN_IJD] + offj);
+        int j = map[j_ind];
+        int ij_spin = 0, a = -1, b = -1;
+        if (j != i) {
+            allowed = 1;
+            pgen = (PPN_W(c, PPN_ID, 0, i_ind) / c->ppn_tot[PPN_ID][0]) *
+                   (PPN_W(c, PPN_IJD, i, j_ind) / c->ppn_tot[PPN_IJD][i]);
+            ij_spin = c->orb_ms[i] + c->orb_ms[j];
+            pgen = pgen + ((PPN_W(c, PPN_ID, 0, j_ind) / c->ppn_tot[PPN_ID][0]) *
+                           (PPN_W(c, PPN_IJD, j, i_ind) / c->ppn_tot[PPN_IJD][j]));
+            if (j < i) {
+                const int t = j;
+                j = i;
+                i = t;
+            }
+        }
+        out->e.from[0] = i;
+        out->e.from[1] = j;
+        int a_ind = -1, isymb = 0, imsb = 0, ij_sym = 0;
+        if (allowed) {
+            const int half = c->nbasis / 2, imsa = ims_of(c, i);
+            const size_t off = (size_t)i * c->ppn_stride[PPN_IAD];
+            a_ind = alias_draw(rs, half, c->ppn_U[PPN_IAD] + off, c->ppn_K[PPN_IAD] + off);
+            a = 2 * a_ind + (imsa == 0);
+            if (tbit(f, a)) allowed = 0;
+        }
+        if (allowed) {
+            ij_sym = cross(c, c->orb_sym[i], c->orb_sym[j]);
+            isymb = cross(c, ij_sym, c->orb_sym[a]);
+            imsb = ims_of(c, j);
+            if (NBSS(imsb, isymb) == 0) allowed = 0;
+        }
+        if (allowed) {
+            const int rb = j * c->nsym + isymb;
+            const size_t off = (size_t)rb * c->ppn_stride[PPN_JBD];
+            const int b_ind = alias_draw(rs, NBSS(imsb, isymb), c->ppn_U[PPN_JBD] + off, c->ppn_K[PPN_JBD] + off);
+            b = SSBF(b_ind, imsb, isymb);
+            if (a != b && !tbit(f, b)) {
+                const double tot_a = c->ppn_tot[PPN_IAD][i], tot_b = c->ppn_tot[PPN_JBD][rb];
+                if (ij_spin == 0) {
+                    pgen = pgen * (PPN_W(c, PPN_IAD, i, a_ind) / tot_a * PPN_W(c, PPN_JBD, rb, b_ind) / tot_b);
+                } else {
+                    const int b_rev = b >> 1;
+                    const int isyma = cross(c, ij_sym, isymb), ra = j * c->nsym + isyma;
+                    int list[MAXB];
+                    const int nl = NBSS(imsb, isyma);
+                    for (int q = 0; q < nl; q++) list[q] = SSBF(q, imsb, isyma);
+                    const int a_rev = int_lower_bound(list, nl, a);
+                    pgen = pgen * (PPN_W(c, PPN_IAD, i, a_ind) / tot_a * PPN_W(c, PPN_JBD, rb, b_ind) / tot_b +
+                                   PPN_W(c, PPN_IAD, i, b_rev) / tot_a * PPN_W(c, PPN_JBD, ra, a_rev) /
+                                       c->ppn_tot[PPN_JBD][ra]);
+                }
+                pgen = c->pattempt_double * pgen;
+            } else {
+                allowed = 0;
+            }
+        }
+        if (allowed) {
+            out->e.to[0] = a < b ? a : b;
+            out->e.to[1] = a < b ? b : a;
+            out->e.perm = perm2(c, f, i, j, out->e.to[0], out->e.to[1]);
+            hmatel = sc2_mol_excit(c, i, j, out->e.to[0], out->e.to[1], out->e.perm);
+        } else {
+            out->e.to[0] = out->e.to[1] = -1;
+        }
+    }
+    out->allowed = allowed;
+    if (!allowed) {
+        pgen = 1.0;
+        hmatel = 0.0;
+    }
+    *pgen_out = pgen;
+    *hmatel_out = hmatel;
+}
+
 static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, const det_info *d, int64_t parent,
                         attempt_t *out) {
     memset(out, 0, sizeof(*out));
@@ -1416,6 +1723,8 @@ static void attempt_mol(const oracle_ctx *c, rstream *rs, const uint64_t *f, con
     double pgen, hmatel;
     if (gen == HGPU_EXCIT_GEN_HEAT_BATH) {
         gen_heat_bath(c, rs, f, d, out, &pgen, &hmatel);
+    } else if (gen == HGPU_EXCIT_GEN_POWER_PITZER_ORDERN) {
+        gen_ppn(c, rs, f, d, out, &pgen, &hmatel);
     } else if (gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE && rs_next(rs) < c->pattempt_single) {
         gen_single_heat_bath_exact(c, rs, f, d, out, &pgen, &hmatel);
     } else if (gen == HGPU_EXCIT_GEN_HEAT_BATH_SINGLE) {
@@ -2289,6 +2598,7 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
     if (c->kind == HGPU_SYS_READ_IN && (cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_OCC_IJ ||
                                         cfg->excit_gen == HGPU_EXCIT_GEN_CAUCHY_SCHWARZ_OCC_IJ))
         init_pp_ij(c);
+    if (c->kind == HGPU_SYS_READ_IN && cfg->excit_gen == HGPU_EXCIT_GEN_POWER_PITZER_ORDERN) init_ppn(c);
     c->fx_E0 = fx_energy(c, c->f0);
     c->H00 = fx_val(c, c->fx_E0);
     c->cap = cfg->walker_length > 0 ? cfg->walker_length : 1000000;
@@ -2324,6 +2634,9 @@ void oracle_destroy(oracle_ctx *c) {
     free(c->dets); free(c->pops); free(c->kii);
     free(c->sdets); free(c->spops); free(c->sflag); free(c->sord); free(c->suid);
     free(c->rdm); free(c->rsdets); free(c->rspops);
+    for (int t = 0; t < 6; t++) {
+        free(c->ppn_w[t]); free(c->ppn_U[t]); free(c->ppn_K[t]); free(c->ppn_tot[t]);
+    }
     free(c->hb_i_w); free(c->hb_ij_w); free(c->hb_ija_w); free(c->hb_ija_tot); free(c->hb_ija_U);
     free(c->hb_ija_K); free(c->hb_ijab_w); free(c->hb_ijab_tot); free(c->hb_ijab_U); free(c->hb_ijab_K);
     free(c);

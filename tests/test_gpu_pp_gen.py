@@ -1,6 +1,7 @@
-"""uniform_power_pitzer, uniform_cauchy_schwarz, heat_bath_power_pitzer and
+"""uniform_power_pitzer, uniform_cauchy_schwarz, heat_bath_power_pitzer,
 heat_bath_cauchy_schwarz (gen_excit_mol_power_pitzer_occ,
-src/excit_gen_power_pitzer_mol.F90:1260-1547) on the GPU
+src/excit_gen_power_pitzer_mol.F90:1260-1547) and heat_bath_power_pitzer_ref
+(gen_excit_mol_power_pitzer_orderN, :941-1258) on the GPU
 against the oracle: excitations, allowed flags and spawned amounts bit-exact,
 p_gen and H_ij to 1e-12 relative, whole runs bit-exact after every report."""
 
@@ -14,7 +15,8 @@ from tests.test_gpu_parity import SYS, assert_close, engine
 
 pytestmark = pytest.mark.gpu
 
-GENS = ["uniform_power_pitzer", "uniform_cauchy_schwarz", "heat_bath_power_pitzer", "heat_bath_cauchy_schwarz"]
+GENS = ["uniform_power_pitzer", "uniform_cauchy_schwarz", "heat_bath_power_pitzer", "heat_bath_cauchy_schwarz",
+        "heat_bath_power_pitzer_ref"]
 
 
 @pytest.mark.parametrize("name", ["h2o_sto2g", "mol26", "mol40_w2"])
@@ -54,6 +56,12 @@ RUNS = [
                    excit_gen="heat_bath_power_pitzer", initiator=True), 3),
     ("mol40_w2", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
                       excit_gen="heat_bath_cauchy_schwarz"), 2),
+    ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
+                   excit_gen="heat_bath_power_pitzer_ref"), 3),
+    ("mol40_w2", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
+                      excit_gen="heat_bath_power_pitzer_ref", power_pitzer_min_weight=0.0, initiator=True), 2),
+    ("h2o_sto2g", dict(tau=0.01, init_pop=100, target_population=200, real_amplitudes=True, initial_shift=3.0,
+                       excit_gen="heat_bath_power_pitzer_ref"), 6),
 ]
 
 
@@ -80,9 +88,14 @@ def test_whole_run_pp_bit_exact(name, opts, nrep):
     assert so.shape[0] > 10
 
 
-def test_pp_fp64_only():
+def test_pp_fp64_only_and_min_weight_range():
     from hande_gb300.engine import HgpuError
     s = SYS["mol26"]
+    for gen in ("uniform_power_pitzer", "heat_bath_power_pitzer_ref"):
+        with pytest.raises(HgpuError):
+            engine(s, make_config(s, tau=0.01, excit_gen=gen, precision=PREC_MIXED, state_size=100,
+                                  spawned_state_size=100))
+    # src/check_input.F90:182-184
     with pytest.raises(HgpuError):
-        engine(s, make_config(s, tau=0.01, excit_gen="uniform_power_pitzer", precision=PREC_MIXED, state_size=100,
-                              spawned_state_size=100))
+        engine(s, make_config(s, tau=0.01, excit_gen="heat_bath_power_pitzer_ref", power_pitzer_min_weight=1.5,
+                              state_size=100, spawned_state_size=100))

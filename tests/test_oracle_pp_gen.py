@@ -129,3 +129,45 @@ def test_pp_occ_pgen_matches_sampling(gen, sysname):
         z = [(c / n - pgen[k]) / np.sqrt(pgen[k] * (1 - pgen[k]) / n) for k, c in counts.items()]
         assert max(abs(x) for x in z) < 5.0
     o.close()
+
+
+@pytest.mark.parametrize("sysname", ["synthetic", "h2o"])
+@pytest.mark.parametrize("min_weight", [0.01, 0.0])
+def test_pp_ref_pgen_matches_sampling(sysname, min_weight):
+    """heat_bath_power_pitzer_ref (gen_excit_mol_power_pitzer_orderN,
+    src/excit_gen_power_pitzer_mol.F90:941-1258): i, j positions of the
+    reference's occupied list mapped onto the determinant, a and b from tables
+    built once.  Each excitation's frequency over many draws matches its p_gen,
+    including determinants far from the reference."""
+    if sysname == "h2o":
+        s = systems.read_in(os.path.join(GOLDEN, "H2O-RHF-sto-2g.fcidump"))
+    else:
+        s = systems.synthetic_molecule(6, 4, seed=3)
+    rng = np.random.default_rng(8)
+    occs = [s.aufbau_occ()]
+    while len(occs) < 3:
+        occ = sorted(int(x) for x in rng.choice(s.nbasis, s.nel, replace=False))
+        if sum(s.orb_ms[p] for p in occ) == sum(s.orb_ms[p] for p in s.aufbau_occ()):
+            occs.append(occ)
+    n = 200000
+    cfg = make_config(s, tau=0.01, excit_gen="heat_bath_power_pitzer_ref", seed=13, state_size=1000,
+                      spawned_state_size=1000, power_pitzer_min_weight=min_weight)
+    o = Oracle(s, cfg)
+    for occ in occs:
+        parent = s.encode(occ).view(np.int64)
+        orbs, pg, hm, al, ns = o.eval_excitations(np.tile(parent, (n, 1)), np.ones(n, np.int64), 3)
+        counts = collections.Counter()
+        pgen = {}
+        for k in np.nonzero(al)[0]:
+            key = tuple(orbs[k])
+            counts[key] += 1
+            if key in pgen:
+                assert abs(pgen[key] - pg[k]) <= 1e-14 * pg[k]
+            pgen[key] = pg[k]
+        assert sum(1 for key in pgen if key[1] >= 0) > 10
+        total = sum(pgen.values())
+        frac = al.mean()
+        assert abs(frac - total) < 5 * np.sqrt(frac * (1 - frac) / n) + 1e-3
+        z = [(c / n - pgen[k]) / np.sqrt(pgen[k] * (1 - pgen[k]) / n) for k, c in counts.items()]
+        assert max(abs(x) for x in z) < 5.0
+    o.close()

@@ -41,6 +41,8 @@ module hande_gpu_m
         real(c_double) :: pattempt_parallel
         integer(c_int32_t) :: density_matrices, density_matrix_report
         real(c_double) :: power_pitzer_min_weight
+        integer(c_int32_t) :: semi_stoch_space, semi_stoch_size
+        integer(c_int64_t) :: semi_stoch_start_iter, semi_stoch_shift_iter
     end type hgpu_config
 
     type, bind(c) :: hgpu_report

@@ -68,6 +68,8 @@ class HgpuConfig(C.Structure):
         ("ref_det", C.c_uint64 * MAX_WORDS), ("pattempt_parallel", C.c_double),
         ("density_matrices", C.c_int32), ("density_matrix_report", C.c_int32),
         ("power_pitzer_min_weight", C.c_double),
+        ("semi_stoch_space", C.c_int32), ("semi_stoch_size", C.c_int32),
+        ("semi_stoch_start_iter", C.c_int64), ("semi_stoch_shift_iter", C.c_int64),
     ]
 
 
@@ -169,7 +171,8 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
                 pattempt_single: float = -1.0, pattempt_double: float = -1.0,
                 pattempt_parallel: float = -1.0, density_matrices: bool = False,
                 density_matrix_report: int = 0, power_pitzer_min_weight: float = 0.01, initiator: bool = False,
-                initiator_threshold: float = 3.0, nspaces: int = 1,
+                initiator_threshold: float = 3.0, nspaces: int = 1, semi_stoch_space: int = 0,
+                semi_stoch_size: int = 0, semi_stoch_start_iter: int = 1, semi_stoch_shift_iter: int = -1,
                 precision: int = PREC_FP64, state_size: int = 100000,
                 spawned_state_size: int = 100000, reference=None) -> HgpuConfig:
     """Configuration with HANDE's qmc{} key names (src/lua_hande_calc.f90:1318-1331)."""
@@ -187,6 +190,10 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
     cfg.density_matrices = int(bool(density_matrices))
     cfg.density_matrix_report = int(density_matrix_report)
     cfg.power_pitzer_min_weight = power_pitzer_min_weight
+    cfg.semi_stoch_space = int(semi_stoch_space)
+    cfg.semi_stoch_size = int(semi_stoch_size)
+    cfg.semi_stoch_start_iter = int(semi_stoch_start_iter)
+    cfg.semi_stoch_shift_iter = int(semi_stoch_shift_iter)
     cfg.D0_population = init_pop
     cfg.vary_shift_from_proje = int(bool(vary_shift_from_proje))
     cfg.excit_gen = EXCIT_GEN[excit_gen] if isinstance(excit_gen, str) else int(excit_gen)

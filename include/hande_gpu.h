@@ -152,6 +152,14 @@ typedef struct hgpu_config {
                                         floor, as a share of the mean, of the weights of
                                         heat_bath_power_pitzer_ref's i, j and single tables
                                         (check_min_weight_ratio); must lie in [0, 1] */
+    /* semi_stoch_in_t (src/qmc_data.f90:305-338), separate annihilation */
+    int32_t semi_stoch_space;       /* space_type: 0 none, 1 'high' (the most populated
+                                       determinants when the space is built) */
+    int32_t semi_stoch_size;        /* target_size of a 'high' space */
+    int64_t semi_stoch_start_iter;  /* start_iteration: the space is built at the start of
+                                       this iteration (HANDE's default 1) */
+    int64_t semi_stoch_shift_iter;  /* shift_start_iteration: built this many iterations after
+                                       every shift varies (-1: not used) */
 } hgpu_config;
 
 /* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */

@@ -27,7 +27,7 @@
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the stream layout.   */
 /* ------------------------------------------------------------------------- */
 
-enum { P_NATTEMPT = 1, P_SPAWN = 2, P_DEATH = 3, P_ROUND_MAIN = 4, P_ROUND_SPAWN = 5 };
+enum { P_NATTEMPT = 1, P_SPAWN = 2, P_DEATH = 3, P_ROUND_MAIN = 4, P_ROUND_SPAWN = 5, P_DETERM = 6 };
 
 static void philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
     uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
@@ -171,6 +171,17 @@ struct oracle_ctx {
      * (a of a single, [nbasis][maxss]), PPN_IAD (a of a double over all
      * orbitals of i's spin, [nbasis][nbasis/2]), PPN_JBD (b per irrep,
      * [nbasis*nsym][maxss]) */
+    /* semi-stochastic projection (semi_stoch_t, src/semi_stoch.F90): the
+     * iteration at whose start the space is built, the deterministic
+     * determinants in main-list order, the Hamiltonian by column j (rows i
+     * ascending, H(D_i, D_j), diagonal K_jj), the populations copied at the
+     * start of the cycle, the projected amplitudes and the main-list
+     * positions of the deterministic states this cycle */
+    int64_t ss_iter, nd;
+    int ss_on;
+    uint64_t *ddets;
+    int64_t *dcol_ptr, *dcol_i, *dind;
+    double *dcol_h, *dvec, *dy;
     int ppn_occ[MAXEL];
     double *ppn_w[6], *ppn_U[6], *ppn_tot[6];
     int32_t *ppn_K[6];
@@ -2135,12 +2146,27 @@ static void stochastic_round_pops(const oracle_ctx *c, int64_t *pop, int purpose
     }
 }
 
+/* check_if_determ (src/semi_stoch.F90:795-824): the index of f in the
+ * deterministic space, or -1. */
+static int64_t ss_find(const oracle_ctx *c, const uint64_t *f) {
+    int64_t lo = 0, hi = c->nd;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) / 2;
+        int cmp = det_cmp(&c->ddets[mid * c->nw], f, c->nw);
+        if (cmp == 0) return mid;
+        if (cmp == 1) lo = mid + 1;
+        else hi = mid;
+    }
+    return -1;
+}
+
 /* remove_unoccupied_dets (src/annihilation.f90:537-598). */
 static void remove_unoccupied_dets(oracle_ctx *c) {
     int64_t nzero = 0;
     for (int64_t i = 0; i < c->n; i++) {
-        if (c->cfg.real_amplitudes) stochastic_round_pops(c, &c->pops[i * c->R], P_ROUND_MAIN, i);
-        if (all_zero(&c->pops[i * c->R], c->R)) {
+        const int determ = c->ss_on && ss_find(c, &c->dets[i * c->nw]) >= 0;
+        if (c->cfg.real_amplitudes && !determ) stochastic_round_pops(c, &c->pops[i * c->R], P_ROUND_MAIN, i);
+        if (all_zero(&c->pops[i * c->R], c->R) && !determ) {
             nzero++;
         } else if (nzero > 0) {
             int64_t k = i - nzero;
@@ -2426,8 +2452,151 @@ static void calc_rdm_energy(oracle_ctx *c, double *energy, double *trace) {
     *trace = tr;
 }
 
+/* ------------------------------------------------------------------------- */
+/* Semi-stochastic projection (src/semi_stoch.F90): 'high' space, separate    */
+/* annihilation                                                               */
+/* ------------------------------------------------------------------------- */
+
+static void ss_free(oracle_ctx *c) {
+    free(c->ddets); free(c->dcol_ptr); free(c->dcol_i); free(c->dcol_h);
+    free(c->dvec); free(c->dy); free(c->dind);
+    c->ddets = NULL; c->dcol_ptr = c->dcol_i = c->dind = NULL; c->dcol_h = c->dvec = c->dy = NULL;
+    c->nd = 0;
+    c->ss_on = 0;
+}
+
+/* init_semi_stoch_t (src/semi_stoch.F90:134-377) for a 'high' space:
+ * find_most_populated_dets (:1318-1385, the target_size entries of largest
+ * sum over spaces of |population|, scanning the main list in order and
+ * replacing the first smallest), sorted; add_determ_dets_to_psip_list
+ * (:728-793, absent ones enter with zero population); create_determ_hamil
+ * (:533-685, |H| > depsilon kept; diagonal K_jj, the main list's exact
+ * difference). */
+static void ss_init(oracle_ctx *c) {
+    ss_free(c);
+    int64_t K = c->cfg.semi_stoch_size < c->n ? c->cfg.semi_stoch_size : c->n;
+    if (K < 1) return;
+    const int nw = c->nw, R = c->R;
+    uint64_t *sel = (uint64_t *)malloc(sizeof(uint64_t) * nw * K);
+    int64_t *pop = (int64_t *)malloc(sizeof(int64_t) * K);
+    for (int64_t i = 0; i < K; i++) {
+        memcpy(&sel[i * nw], &c->dets[i * nw], sizeof(uint64_t) * nw);
+        int64_t p = 0;
+        for (int s = 0; s < R; s++) p += llabs(c->pops[i * R + s]);
+        pop[i] = p;
+    }
+    int64_t min_pop = pop[0], min_ind = 0;
+    for (int64_t i = 1; i < K; i++)
+        if (pop[i] < min_pop) { min_pop = pop[i]; min_ind = i; }
+    for (int64_t i = K; i < c->n; i++) {
+        int64_t p = 0;
+        for (int s = 0; s < R; s++) p += llabs(c->pops[i * R + s]);
+        if (p > min_pop) {
+            memcpy(&sel[min_ind * nw], &c->dets[i * nw], sizeof(uint64_t) * nw);
+            pop[min_ind] = p;
+            min_pop = pop[0];
+            min_ind = 0;
+            for (int64_t j = 1; j < K; j++)
+                if (pop[j] < min_pop) { min_pop = pop[j]; min_ind = j; }
+        }
+    }
+    free(pop);
+    /* qsort into the main list's order (insertion sort: small spaces) */
+    for (int64_t i = 1; i < K; i++) {
+        uint64_t t[MAXW];
+        memcpy(t, &sel[i * nw], sizeof(uint64_t) * nw);
+        int64_t j = i - 1;
+        while (j >= 0 && det_cmp(t, &sel[j * nw], nw) == 1) {
+            memcpy(&sel[(j + 1) * nw], &sel[j * nw], sizeof(uint64_t) * nw);
+            j--;
+        }
+        memcpy(&sel[(j + 1) * nw], t, sizeof(uint64_t) * nw);
+    }
+    c->nd = K;
+    c->ddets = sel;
+    /* absent determinants join the main list with zero population */
+    int64_t istart = 0;
+    for (int64_t k = 0; k < K; k++) {
+        int hit;
+        int64_t pos = bsearch_main(c, &sel[k * nw], istart, c->n - 1, &hit);
+        if (!hit) {
+            if (c->n + 1 > c->cap) {
+                c->error_flags |= HGPU_FLAG_MAIN_OVERFLOW;
+                break;
+            }
+            memmove(&c->dets[(pos + 1) * nw], &c->dets[pos * nw], sizeof(uint64_t) * nw * (size_t)(c->n - pos));
+            memmove(&c->pops[(pos + 1) * R], &c->pops[pos * R], sizeof(int64_t) * R * (size_t)(c->n - pos));
+            memmove(&c->kii[pos + 1], &c->kii[pos], sizeof(double) * (size_t)(c->n - pos));
+            memcpy(&c->dets[pos * nw], &sel[k * nw], sizeof(uint64_t) * nw);
+            for (int s = 0; s < R; s++) c->pops[pos * R + s] = 0;
+            c->kii[pos] = kii_of(c, &sel[k * nw]);
+            c->n++;
+        }
+        istart = pos + 1;
+    }
+    /* the Hamiltonian by column */
+    c->dcol_ptr = (int64_t *)calloc((size_t)K + 1, sizeof(int64_t));
+    int64_t cap = 16, nnz = 0;
+    c->dcol_i = (int64_t *)malloc(sizeof(int64_t) * cap);
+    c->dcol_h = (double *)malloc(sizeof(double) * cap);
+    for (int64_t j = 0; j < K; j++) {
+        c->dcol_ptr[j] = nnz;
+        for (int64_t i = 0; i < K; i++) {
+            double h = i == j ? kii_of(c, &sel[j * nw]) : hmatel_any(c, &sel[i * nw], &sel[j * nw]);
+            if (!(fabs(h) > DEPSILON)) continue;
+            if (nnz == cap) {
+                cap *= 2;
+                c->dcol_i = (int64_t *)realloc(c->dcol_i, sizeof(int64_t) * cap);
+                c->dcol_h = (double *)realloc(c->dcol_h, sizeof(double) * cap);
+            }
+            c->dcol_i[nnz] = i;
+            c->dcol_h[nnz] = h;
+            nnz++;
+        }
+    }
+    c->dcol_ptr[K] = nnz;
+    c->dvec = (double *)calloc((size_t)(K * R), sizeof(double));
+    c->dy = (double *)calloc((size_t)(K * R), sizeof(double));
+    c->dind = (int64_t *)calloc((size_t)K, sizeof(int64_t));
+    c->ss_on = 1;
+}
+
+/* determ_proj_separate_annihil (src/semi_stoch.F90:1009-1094) without
+ * quasi-Newton (rho_minus_qn_weight = 0, quasi_newton_pop_control = 1), then
+ * deterministic_annihilation (src/annihilation.f90:488-535): the projected
+ * amplitudes, stochastically rounded to the walker unit, added to the main list. */
+static void ss_project(oracle_ctx *c) {
+    const int R = c->R;
+    const double a = -1.0 * c->cfg.tau;
+    for (int s = 0; s < R; s++) {
+        const double scale = -c->cfg.tau * (0.0 - c->shift[s] * 1.0);
+        for (int64_t k = 0; k < c->nd; k++) c->dy[k * R + s] = scale * c->dvec[k * R + s];
+        for (int64_t j = 0; j < c->nd; j++) {
+            double y = c->dy[j * R + s];
+            for (int64_t z = c->dcol_ptr[j]; z < c->dcol_ptr[j + 1]; z++)
+                y = y + a * c->dcol_h[z] * c->dvec[c->dcol_i[z] * R + s];
+            c->dy[j * R + s] = y;
+        }
+    }
+    for (int64_t k = 0; k < c->nd; k++) {
+        const int64_t ind = c->dind[k];
+        for (int s = 0; s < R; s++) {
+            double amp = c->dy[k * R + s] * (double)c->real_factor;
+            const int64_t sign = amp < 0.0 ? -1 : 1;
+            amp = fabs(amp);
+            int64_t n = (int64_t)amp;
+            amp = amp - (double)n;
+            rstream rs;
+            rs_init(&rs, (uint64_t)c->cfg.seed, P_DETERM, s, (uint64_t)k, 0, (uint64_t)c->iter);
+            if (amp > rs_next(&rs)) n = n + 1;
+            c->pops[ind * R + s] += sign * n;
+        }
+    }
+}
+
 static void mc_cycle(oracle_ctx *c) {
     c->iter++;
+    if (c->cfg.semi_stoch_space != 0 && c->iter == c->ss_iter) ss_init(c);
     /* init_mc_cycle (src/qmc_common.F90:950-1017) */
     int64_t nattempts_acc = llround(2.0 * nparticles(c, 0));
     int64_t ndeath = 0;
@@ -2440,6 +2609,14 @@ static void mc_cycle(oracle_ctx *c) {
         double real_pop[2];
         for (int s = 0; s < c->R; s++) real_pop[s] = (double)c->pops[idet * c->R + s] / (double)c->real_factor;
         int64_t flag = parent_flag(c, real_pop);
+        /* set_determ_info (src/semi_stoch.F90:826-857); deterministic states
+         * are initiators (set_parent_flag, src/ifciqmc.f90:14-58) */
+        const int64_t dk = c->ss_on ? ss_find(c, f) : -1;
+        if (dk >= 0) {
+            for (int s = 0; s < c->R; s++) c->dvec[dk * c->R + s] = real_pop[s];
+            c->dind[dk] = idet;
+            flag = 0;
+        }
         excit_t ex = get_excitation(c, f, c->f0);
         for (int s = 0; s < c->R; s++) {
             update_proj_energy(c, f, &d, &ex, real_pop[s], s);
@@ -2456,19 +2633,24 @@ static void mc_cycle(oracle_ctx *c) {
                 attempt(c, &rs, f, &d, parent, &at, 0);
                 if (at.nspawn != 0) {
                     excited_det(c, f, &at.e, child);
-                    add_spawn(c, child, s, at.nspawn, c->cfg.initiator_approx ? flag : 0, c->sn);
+                    /* no spawning between deterministic states (src/fciqmc.f90:777-790) */
+                    if (dk < 0 || ss_find(c, child) < 0)
+                        add_spawn(c, child, s, at.nspawn, c->cfg.initiator_approx ? flag : 0, c->sn);
                 }
                 if (at.nspawn_rdm != 0) {
                     excited_det(c, f, &at.e, child);
                     add_rdm_spawn(c, f, child, s, at.nspawn_rdm);
                 }
             }
-            rs_init(&rs, (uint64_t)c->cfg.seed, P_DEATH, s, (uint64_t)idet, 0, (uint64_t)c->iter);
-            ndeath += stochastic_death(c, &rs, c->kii[idet], c->shift[s], &c->pops[idet * c->R + s]);
+            if (dk < 0) {
+                rs_init(&rs, (uint64_t)c->cfg.seed, P_DEATH, s, (uint64_t)idet, 0, (uint64_t)c->iter);
+                ndeath += stochastic_death(c, &rs, c->kii[idet], c->shift[s], &c->pops[idet * c->R + s]);
+            }
         }
     }
     int64_t nspawn_events = c->sn; /* calc_events_spawn_t */
     c->rep_spawned += c->sn;
+    if (c->ss_on) ss_project(c);
     direct_annihilation(c);
     if (c->rdm_on) update_rdm_from_spawns(c);
     c->last_nspawn_events = nspawn_events;
@@ -2612,6 +2794,14 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
     c->sord = (int64_t *)calloc((size_t)c->scap, sizeof(int64_t));
     c->suid = (int64_t *)calloc((size_t)c->scap, sizeof(int64_t));
     for (int s = 0; s < 2; s++) c->shift[s] = cfg->initial_shift;
+    /* semi_stoch_iter = max(start_iter, mc_cycles_done + 1) (src/fciqmc.f90:229) */
+    c->ss_iter = INT64_MAX;
+    if (cfg->semi_stoch_space != 0) c->ss_iter = cfg->semi_stoch_start_iter > 1 ? cfg->semi_stoch_start_iter : 1;
+    if ((cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1) ||
+        (cfg->semi_stoch_space != 0 && cfg->density_matrices)) {
+        oracle_destroy(c);
+        return NULL;
+    }
     if (cfg->density_matrices) {
         if (c->kind != HGPU_SYS_READ_IN || c->R != 2) {
             oracle_destroy(c);
@@ -2628,6 +2818,7 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
 
 void oracle_destroy(oracle_ctx *c) {
     if (!c) return;
+    ss_free(c);
     free(c->orb_sym); free(c->orb_ms); free(c->sp_eigv);
     free(c->sym_table); free(c->inv_sym); free(c->h1); free(c->v2); free(c->nbss); free(c->ssbf);
     free(c->fx_h1); free(c->fx_J); free(c->fx_JK); free(c->fx_eps);
@@ -2715,6 +2906,8 @@ int oracle_end_report(oracle_ctx *c, hgpu_report *out) {
         }
     }
     for (int s = 0; s < c->R; s++) c->nparticles_old[s] = ntot[s];
+    int all_vary_before = 1, all_vary = 1;
+    for (int s = 0; s < c->R; s++) all_vary_before = all_vary_before && c->vary_shift[s];
     for (int s = 0; s < c->R; s++) {
         if (!c->vary_shift[s] && ntot[s] > c->cfg.target_particles) {
             c->vary_shift[s] = 1;
@@ -2722,6 +2915,10 @@ int oracle_end_report(oracle_ctx *c, hgpu_report *out) {
             else c->shift[s] = c->cfg.vary_shift_from;
         }
     }
+    /* the space follows the shift (src/qmc_common.F90:1203-1204) */
+    for (int s = 0; s < c->R; s++) all_vary = all_vary && c->vary_shift[s];
+    if (!all_vary_before && all_vary && c->cfg.semi_stoch_space != 0 && c->cfg.semi_stoch_shift_iter != -1)
+        c->ss_iter = c->cfg.semi_stoch_shift_iter + c->iter + 1;
     for (int s = 0; s < c->R; s++) {
         out->shift[s] = c->shift[s];
         out->nparticles[s] = ntot[s];
@@ -2814,6 +3011,11 @@ double oracle_hmatel(oracle_ctx *c, const int64_t *f1, const int64_t *f2) {
 double oracle_sc0(oracle_ctx *c, const int64_t *f) { return sc0(c, (const uint64_t *)f); }
 
 double oracle_pattempt_parallel(oracle_ctx *c) { return c->spin_ij ? c->pattempt_parallel : -1.0; }
+
+int64_t oracle_determ_space(oracle_ctx *c, int64_t *dets, int64_t n) {
+    if (dets && n >= c->nd) memcpy(dets, c->ddets, sizeof(uint64_t) * (size_t)(c->nd * c->nw));
+    return c->nd;
+}
 
 void oracle_pattempt(oracle_ctx *c, double *out) {
     out[0] = c->pattempt_single;

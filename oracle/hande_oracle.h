@@ -51,6 +51,9 @@ double oracle_pgen(oracle_ctx *c, const int64_t *f, const int32_t *orbs);
 double oracle_pattempt_parallel(oracle_ctx *c);
 /* pattempt_single and pattempt_double after init_excit_gen (src/qmc.F90:951-972). */
 void oracle_pattempt(oracle_ctx *c, double *out);
+/* The deterministic space of a semi-stochastic calculation (main-list order):
+ * copied into dets when n is large enough; returns its size (0 before it is built). */
+int64_t oracle_determ_space(oracle_ctx *c, int64_t *dets, int64_t n);
 /* Replica 2-RDM (density_matrices): copies the current report's RDM
  * ([pair][pair], pairs p < q in tri_ind_distinct order) into out when n is
  * large enough and returns its element count (0 when not enabled); its

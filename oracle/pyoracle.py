@@ -60,6 +60,8 @@ def lib():
         L.oracle_pattempt_parallel.restype = C.c_double
         L.oracle_pattempt_parallel.argtypes = [C.c_void_p]
         L.oracle_pattempt.restype = None
+        L.oracle_determ_space.restype = C.c_int64
+        L.oracle_determ_space.argtypes = [C.c_void_p, P(C.c_int64), C.c_int64]
         L.oracle_pattempt.argtypes = [C.c_void_p, P(C.c_double)]
         L.oracle_pgen.restype = C.c_double
         L.oracle_pgen.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int32)]
@@ -190,6 +192,12 @@ class Oracle:
 
     def pattempt_parallel(self) -> float:
         return self.L.oracle_pattempt_parallel(self.h)
+
+    def determ_space(self):
+        n = self.L.oracle_determ_space(self.h, None, 0)
+        d = np.zeros((n, self.system.nwords), dtype=np.int64)
+        self.L.oracle_determ_space(self.h, d.ctypes.data_as(C.POINTER(C.c_int64)), n)
+        return d
 
     def pattempt(self):
         out = (C.c_double * 2)()

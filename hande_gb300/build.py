@@ -17,8 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libhande_gpu.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["hgpu_kernels.cu", "hgpu_spawn_rdm.cu", "hgpu_annihilate.cu", "hgpu_rdm.cu", "hgpu_engine.cu",
-           "hgpu_noalloc.cu"]
+SOURCES = ["hgpu_kernels.cu", "hgpu_spawn_rdm.cu", "hgpu_annihilate.cu", "hgpu_rdm.cu", "hgpu_semi_stoch.cu",
+           "hgpu_engine.cu", "hgpu_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr"]

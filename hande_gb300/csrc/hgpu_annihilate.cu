@@ -414,6 +414,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
             uint32_t purpose = P_ROUND_MAIN;
             int64_t key = 0;
             const bool is_main = slot < nm;
+            bool determ = false;
             if (head) {
                 SegAcc acc;
                 acc.init();
@@ -441,6 +442,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
                 const uint64_t fl = nonzero ? acc.flag(R, initiator) : 0;
                 if (is_main) {
                     // annihilate_main_list[_initiator], then remove_unoccupied_dets
+                    // (a deterministic state is neither rounded nor removed)
+                    determ = b.nd > 0 && (b.pinfo[ia + slot] & kDetermBit) != 0;
                     p[0] = tpop[slot * R];
                     p[1] = R > 1 ? tpop[slot * R + 1] : 0;
                     if (nonzero) {
@@ -473,10 +476,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
                 }
             }
             // one rounding call for both kinds, so that the lanes that round run together
-            if (cand && real) round_pops(s, p, R, purpose, key, iter);
+            if (cand && real && !determ) round_pops(s, p, R, purpose, key, iter);
             if (cand) {
                 const bool nz = p[0] != 0 || (R > 1 && p[1] != 0);
-                if (nz || (!is_main && !real)) {
+                if (nz || determ || (!is_main && !real)) {
 #pragma unroll
                     for (int r = 0; r < 2; r++)
                         if (r < R) tpop[slot * R + r] = p[r];

@@ -24,7 +24,7 @@ constexpr int kMaxRedraw = 1 << 16;
 constexpr int kMaxSym = 8;  // D2h subgroups: at most 8 irreps
 
 // RNG stream purposes (counter word 3, bits 28..31).
-enum Purpose : uint32_t { P_NATTEMPT = 1, P_SPAWN = 2, P_DEATH = 3, P_ROUND_MAIN = 4, P_ROUND_SPAWN = 5 };
+enum Purpose : uint32_t { P_NATTEMPT = 1, P_SPAWN = 2, P_DEATH = 3, P_ROUND_MAIN = 4, P_ROUND_SPAWN = 5, P_DETERM = 6 };
 
 // Everything the kernels need to know about the system and the calculation.
 // Lives in device global memory; small tables are staged to shared memory by

@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <queue>
 #include <vector>
 
 #include "../../include/hande_gpu.h"
@@ -45,6 +46,7 @@ struct hgpu_handle {
     int vary_shift[HGPU_MAX_SPACES];
     double nparticles_old[HGPU_MAX_SPACES];
     int64_t iter;
+    int64_t ss_iter;  // iteration at whose start the deterministic space is built
     cudaEvent_t ev0, ev1;
     double report_ms;
     std::vector<void *> allocs;
@@ -751,6 +753,11 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     }
     // src/check_input.F90:182-184
     if (!(cfg->power_pitzer_min_weight >= 0.0 && cfg->power_pitzer_min_weight <= 1.0)) return HGPU_ERR_INVALID;
+    // semi-stochastic: a 'high' space (read_in: read_determ_space needs HDF5), not
+    // combined with the replica RDM
+    if (cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1) return HGPU_ERR_UNSUPPORTED;
+    if (cfg->semi_stoch_space == 1 && (cfg->semi_stoch_size < 1 || cfg->density_matrices))
+        return cfg->density_matrices ? HGPU_ERR_UNSUPPORTED : HGPU_ERR_INVALID;
     // density_matrices: replica sampling of molecular systems (two spaces)
     if (cfg->density_matrices && (sys->kind != HGPU_SYS_READ_IN || cfg->nspaces != 2)) return HGPU_ERR_INVALID;
     // pattempt_parallel only with the spin-resolved generators, at most 1
@@ -785,6 +792,9 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
             h->gkind = kKindPowerPitzerRef;
     }
     h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;
+    // semi_stoch_iter = max(start_iter, mc_cycles_done + 1) (src/fciqmc.f90:229)
+    h->ss_iter = INT64_MAX;
+    if (cfg->semi_stoch_space == 1) h->ss_iter = cfg->semi_stoch_start_iter > 1 ? cfg->semi_stoch_start_iter : 1;
     cudaGetDevice(&h->device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
@@ -909,6 +919,133 @@ int32_t hgpu_download_walkers(hgpu_handle *h, int64_t *states, int64_t *pops, do
     return HGPU_OK;
 }
 
+// init_semi_stoch_t (src/semi_stoch.F90:134-377) for a 'high' space, at the
+// start of the cycle that builds it: find_most_populated_dets (:1318-1385;
+// the first smallest entry is replaced, so a min-heap of (population, slot)
+// gives the same set), the space sorted into the main list's order, its
+// absent determinants added with zero population (add_determ_dets_to_psip_list,
+// :728-793), then the Hamiltonian by column on the device.
+static int ss_init(hgpu_handle *h) {
+    DevState st;
+    int rc = read_state(h, &st);
+    if (rc) return rc;
+    const int W = h->W, R = h->R;
+    const int64_t n = st.n_main;
+    std::vector<uint64_t> dets((size_t)n * W);
+    std::vector<int64_t> pops((size_t)n * R);
+    if (n > 0) {
+        CK(cudaMemcpyAsync(dets.data(), h->b.dets[h->cur], sizeof(uint64_t) * W * n, cudaMemcpyDeviceToHost,
+                           h->stream));
+        CK(cudaMemcpyAsync(pops.data(), h->b.pops[h->cur], sizeof(int64_t) * R * n, cudaMemcpyDeviceToHost,
+                           h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    const int64_t K = std::min<int64_t>(h->cfg.semi_stoch_size, n);
+    h->b.nd = 0;
+    if (K < 1) return HGPU_OK;
+    auto tot = [&](int64_t i) {
+        int64_t p = 0;
+        for (int s = 0; s < R; s++) p += std::llabs(pops[(size_t)i * R + s]);
+        return p;
+    };
+    std::vector<int64_t> slot_of(K);
+    std::priority_queue<std::pair<int64_t, int64_t>, std::vector<std::pair<int64_t, int64_t>>,
+                        std::greater<std::pair<int64_t, int64_t>>>
+        heap;
+    for (int64_t i = 0; i < K; i++) {
+        slot_of[i] = i;
+        heap.push({tot(i), i});
+    }
+    for (int64_t i = K; i < n; i++) {
+        const int64_t p = tot(i);
+        if (p > heap.top().first) {
+            const int64_t sl = heap.top().second;
+            heap.pop();
+            slot_of[sl] = i;
+            heap.push({p, sl});
+        }
+    }
+    // the main list is sorted, so the selected entries in index order are the
+    // space in main-list order
+    std::sort(slot_of.begin(), slot_of.end());
+    std::vector<uint64_t> dd((size_t)K * W);
+    for (int64_t k = 0; k < K; k++)
+        for (int w = 0; w < W; w++) dd[(size_t)k * W + w] = dets[(size_t)slot_of[k] * W + w];
+    uint64_t *ddets;
+    if ((rc = dalloc(h, &ddets, (size_t)K * W))) return rc;
+    CK(cudaMemcpy(ddets, dd.data(), sizeof(uint64_t) * K * W, cudaMemcpyHostToDevice));
+    h->b.ddets = ddets;
+    h->b.nd = K;
+    // the Hamiltonian by column: count, offsets, fill
+    int64_t *counts;
+    if ((rc = dalloc(h, &counts, (size_t)K))) return rc;
+    launch_determ_columns(h->b, W, h->kind, false, counts, nullptr, nullptr, h->stream);
+    std::vector<int64_t> cnt(K), ptr(K + 1);
+    CK(cudaMemcpyAsync(cnt.data(), counts, sizeof(int64_t) * K, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    ptr[0] = 0;
+    for (int64_t k = 0; k < K; k++) ptr[k + 1] = ptr[k] + cnt[k];
+    int64_t *dptr;
+    int32_t *ci;
+    double *ch, *dvec;
+    int64_t *dind;
+    if ((rc = dalloc(h, &dptr, (size_t)K + 1)) || (rc = dalloc(h, &ci, (size_t)ptr[K])) ||
+        (rc = dalloc(h, &ch, (size_t)ptr[K])) || (rc = dalloc(h, &dvec, (size_t)K * R)) ||
+        (rc = dalloc(h, &dind, (size_t)K)))
+        return rc;
+    CK(cudaMemcpy(dptr, ptr.data(), sizeof(int64_t) * (K + 1), cudaMemcpyHostToDevice));
+    h->b.dcol_ptr = dptr;
+    launch_determ_columns(h->b, W, h->kind, true, nullptr, ci, ch, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    h->b.dcol_i = ci;
+    h->b.dcol_h = ch;
+    h->b.dvec = dvec;
+    h->b.dind = dind;
+    // absent determinants join the main list with zero population
+    std::vector<uint64_t> nd_;
+    std::vector<int64_t> np_;
+    nd_.reserve((size_t)(n + K) * W);
+    np_.reserve((size_t)(n + K) * R);
+    int64_t added = 0;
+    {
+        int64_t i = 0, k = 0;
+        auto less = [&](const uint64_t *a, const uint64_t *b) {
+            for (int w = W - 1; w >= 0; w--)
+                if (a[w] != b[w]) return a[w] < b[w];
+            return false;
+        };
+        while (i < n || k < K) {
+            const uint64_t *dm = i < n ? &dets[(size_t)i * W] : nullptr;
+            const uint64_t *dk = k < K ? &dd[(size_t)k * W] : nullptr;
+            if (dk && (!dm || less(dk, dm))) {
+                nd_.insert(nd_.end(), dk, dk + W);
+                for (int s = 0; s < R; s++) np_.push_back(0);
+                added++;
+                k++;
+            } else {
+                nd_.insert(nd_.end(), dm, dm + W);
+                for (int s = 0; s < R; s++) np_.push_back(pops[(size_t)i * R + s]);
+                if (dk && !less(dm, dk)) k++;  // present in both
+                i++;
+            }
+        }
+    }
+    if (added > 0) {
+        const int64_t m = n + added;
+        if (m > h->b.cap) return HGPU_ERR_MAIN_OVERFLOW;
+        CK(cudaMemcpyAsync(h->b.dets[h->cur], nd_.data(), sizeof(uint64_t) * W * m, cudaMemcpyHostToDevice,
+                           h->stream));
+        CK(cudaMemcpyAsync(h->b.pops[h->cur], np_.data(), sizeof(int64_t) * R * m, cudaMemcpyHostToDevice,
+                           h->stream));
+        launch_eval_diagonal(h->b, W, h->b.dets[h->cur], m, h->b.kii[h->cur], h->stream);
+        st.n_main = m;
+        if ((rc = write_state(h, &st))) return rc;
+    }
+    invalidate_graphs(h);
+    return HGPU_OK;
+}
+
 static int launch_one_cycle(hgpu_handle *h) {
     int cur = h->cur;
     if (h->use_graphs) {
@@ -961,7 +1098,9 @@ int32_t hgpu_run_cycles(hgpu_handle *h, int32_t ncycles) {
     }
     CK(cudaEventRecord(h->ev0, h->stream));
     for (int k = 0; k < ncycles; k++) {
-        int rc = launch_one_cycle(h);
+        int rc;
+        if (h->ss_iter == h->iter + k + 1 && (rc = ss_init(h))) return rc;
+        rc = launch_one_cycle(h);
         if (rc) return rc;
     }
     CK(cudaEventRecord(h->ev1, h->stream));
@@ -1043,6 +1182,7 @@ int32_t hgpu_batch_create(hgpu_handle *const *handles, int32_t n, hgpu_batch **o
     std::vector<hgpu_handle *> hs(handles, handles + n);
     for (int i = 0; i < n; i++) {
         if (!hs[i] || hs[i]->device != dev) return HGPU_ERR_INVALID;
+        if (hs[i]->cfg.semi_stoch_space != 0) return HGPU_ERR_UNSUPPORTED;  // its space is built between cycles
         for (int j = 0; j < i; j++)
             if (hs[j] == hs[i]) return HGPU_ERR_INVALID;
     }
@@ -1144,6 +1284,8 @@ int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
             h->shift[s] = h->shift[s] - std::log(ntot[s] / h->nparticles_old[s]) * h->cfg.shift_damping /
                                             (1.0 * h->cfg.tau * (double)nc);
     for (int s = 0; s < R; s++) h->nparticles_old[s] = ntot[s];
+    bool all_vary_before = true, all_vary = true;
+    for (int s = 0; s < R; s++) all_vary_before = all_vary_before && h->vary_shift[s];
     for (int s = 0; s < R; s++) {
         if (!h->vary_shift[s] && ntot[s] > h->cfg.target_particles) {
             h->vary_shift[s] = 1;
@@ -1151,6 +1293,10 @@ int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
                                                        : h->cfg.vary_shift_from;
         }
     }
+    // the deterministic space follows the shift (src/qmc_common.F90:1203-1204)
+    for (int s = 0; s < R; s++) all_vary = all_vary && h->vary_shift[s];
+    if (!all_vary_before && all_vary && h->cfg.semi_stoch_space == 1 && h->cfg.semi_stoch_shift_iter != -1)
+        h->ss_iter = h->cfg.semi_stoch_shift_iter + st.iter + 1;
     for (int s = 0; s < R; s++) {
         out->shift[s] = h->shift[s];
         out->nparticles[s] = ntot[s];

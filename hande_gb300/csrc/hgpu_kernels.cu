@@ -160,6 +160,13 @@ __global__ void __launch_bounds__(kBlock) k_prep_parents(DevBuffers b, int R, in
         double h = (e.nexcit == 1 || e.nexcit == 2) ? proj_hmatel<W>(s, t, f, e) : 0.0;
         double k = kii[i];
         uint32_t info = 0;
+        // set_determ_info (src/semi_stoch.F90:826-857): a deterministic state
+        // records its population and position, is an initiator and does not die
+        int64_t dk = -1;
+        if (b.nd > 0) {
+            const int64_t q = lower_bound_det<W>(b.ddets, b.nd, f);
+            if (q < b.nd && det_eq<W>(load_det<W>(b.ddets, q), f)) dk = q;
+        }
         for (int sp = 0; sp < R; sp++) {
             int64_t p = pops[i * R + sp];
             double rp = (double)p * inv_rf;
@@ -167,14 +174,22 @@ __global__ void __launch_bounds__(kBlock) k_prep_parents(DevBuffers b, int R, in
             if (e.nexcit == 0) d0[sp] += rp;
             else proj[sp] += h * rp;
             // set_parent_flag: bit set if not an initiator
-            if (!(fabs(rp) > s.initiator_pop)) info |= 4u << sp;
+            if (!(fabs(rp) > s.initiator_pop) && dk < 0) info |= 4u << sp;
             if (p < 0) info |= 1u << sp;
             RStream rs;
             rs.init(s.seed, P_NATTEMPT, sp, i, 0, iter);
             b.natt[i * R + sp] = decide_nattempts_fx(rs, p, s.real_amplitudes ? 31 : 0, rp);
-            rs.init(s.seed, P_DEATH, sp, i, 0, iter);
-            ndeath += stochastic_death(s.tau, rs, k, shift[sp], p);
-            pops[i * R + sp] = p;
+            if (dk < 0) {
+                rs.init(s.seed, P_DEATH, sp, i, 0, iter);
+                ndeath += stochastic_death(s.tau, rs, k, shift[sp], p);
+                pops[i * R + sp] = p;
+            } else {
+                b.dvec[dk * R + sp] = rp;
+            }
+        }
+        if (dk >= 0) {
+            info |= kDetermBit;
+            b.dind[dk] = i;
         }
         b.pinfo[i] = (uint8_t)info;
     }
@@ -389,6 +404,9 @@ static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur
         k_spawn<W, kKindPowerPitzerRef, double, false><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
     else HGPU_SPAWN(HGPU_SYS_READ_IN);
 #undef HGPU_SPAWN
+    // determ_projection and deterministic_annihilation (src/fciqmc.f90:394,
+    // src/annihilation.f90:63-66) before the main list is merged
+    if (b.nd > 0) launch_determ_project(b, R, cur, st);
     if (pm) cudaEventRecord(pm->ev[3], st);
     launch_sort_annihilate(b, W, R, cur, st, pm);
     k_cycle_end<<<1, 1024, 0, st>>>(b, R, b.grid, 1);

@@ -18,6 +18,9 @@ constexpr int kKindReadInNoRenorm = 4;   // molecular, uniform no_renorm generat
 constexpr int kKindHeatBathUniform = 5;  // molecular, heat_bath_uniform
 constexpr int kKindPowerPitzerOcc = 6;   // molecular, uniform_ / heat_bath_ power_pitzer, cauchy_schwarz (FP64)
 constexpr int kKindPowerPitzerRef = 7;   // molecular, heat_bath_power_pitzer_ref (FP64)
+// pinfo bit of a main-list entry in the deterministic space (bits 0-1: sign of
+// each space, 2-3: not an initiator in each space)
+constexpr uint8_t kDetermBit = 0x80;
 // Radix sort of the spawned list (hgpu_sort.cuh): 8-bit digits, at most
 // kMaxPasses passes, tiles of kOSThreads x items keys of KW words each.
 constexpr int kOSThreads = 256;  // one thread per digit value in the look-back
@@ -118,6 +121,18 @@ struct DevBuffers {
     double *rdm_rows;       // [2][npairs]: per-row energy and diagonal of calc_rdm_energy
     uint32_t *rdm_hash;     // open-addressing table of the new main list (index per slot)
     int64_t rdm_hash_mask;  // table size - 1 (a power of two, at least 1.5 x cap)
+    // semi-stochastic projection (hgpu_semi_stoch.cu): the deterministic
+    // determinants in main-list order, the Hamiltonian by column j (rows i
+    // ascending: H(D_i, D_j), diagonal K_jj), the populations of the
+    // deterministic states at the start of the cycle ([nd][R], walker units)
+    // and their main-list positions; nd = 0 until the space is built
+    const uint64_t *ddets;
+    const int64_t *dcol_ptr;
+    const int32_t *dcol_i;
+    const double *dcol_h;
+    double *dvec;
+    int64_t *dind;
+    int64_t nd;
     // scan scratch and per-block partials
     int64_t *scan_part;     // kMaxBlocks * 2
     double *part_d;         // kMaxBlocks * 4 (proj, d0 per space)
@@ -151,6 +166,12 @@ void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, c
 // attributes they need; 0 on success.
 void launch_sort_annihilate(const DevBuffers &b, int W, int R, int cur, cudaStream_t st, const PhaseMarks *pm);
 int set_annihilate_attributes(const DevBuffers &b);
+// hgpu_semi_stoch.cu: the deterministic Hamiltonian by column (count, then fill
+// at the offsets dcol_ptr), and each cycle's deterministic projection added to
+// the main list
+void launch_determ_columns(const DevBuffers &b, int W, int kind, bool fill, int64_t *counts, int32_t *col_i,
+                           double *col_h, cudaStream_t st);
+void launch_determ_project(const DevBuffers &b, int R, int cur, cudaStream_t st);
 void launch_eval_excitations(const DevBuffers &b, int W, int kind, int precision, const uint64_t *parents,
                              const int64_t *parent_pops, int64_t n, int64_t iteration, int32_t *orbs, double *pgen,
                              double *hmatel, int32_t *allowed, int64_t *nspawn, cudaStream_t st);

@@ -89,6 +89,11 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
     nspawn_rdm = KIND == HGPU_SYS_HUB_K ? 0 : at.nspawn_rdm;
     parent_det = f;
     if (at.nspawn != 0 || nspawn_rdm != 0) child = excited<W>(f, at);
+    // no spawning from a deterministic state onto another (src/fciqmc.f90:777-790)
+    if (at.nspawn != 0 && b.nd > 0 && (info & kDetermBit)) {
+        const int64_t q = lower_bound_det<W>(b.ddets, b.nd, child);
+        if (q < b.nd && det_eq<W>(load_det<W>(b.ddets, q), child)) at.nspawn = 0;
+    }
     return at.nspawn;
 }
 

@@ -1,0 +1,91 @@
+"""Semi-stochastic projection (src/semi_stoch.F90, 'high' space, separate
+annihilation) on the GPU against the oracle: the walker lists, deterministic
+states included, bit-exact after every report, through the building of the
+space (at a given iteration or after the shift starts varying), the exact
+projection and its stochastic rounding; integer and real walkers, Hubbard and
+molecular systems, one- and two-word determinants, initiator on and off."""
+
+import numpy as np
+import pytest
+
+from hande_gb300._abi import make_config
+from oracle import fci
+from oracle.pyoracle import Oracle
+from tests.helpers import sort_dets
+from tests.test_gpu_parity import SYS, assert_close, engine
+
+pytestmark = pytest.mark.gpu
+
+RUNS = [
+    ("h2o_sto2g", dict(tau=0.01, init_pop=20, target_population=40, real_amplitudes=True, initial_shift=1.0,
+                       semi_stoch_space=1, semi_stoch_size=12, semi_stoch_start_iter=2 ** 62,
+                       semi_stoch_shift_iter=30), 14),
+    ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True, initiator=True,
+                   semi_stoch_space=1, semi_stoch_size=300, semi_stoch_start_iter=15), 3),
+    ("mol40_w2", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
+                      semi_stoch_space=1, semi_stoch_size=150, semi_stoch_start_iter=6), 3),
+    ("hub_k_4x4", dict(tau=0.01, init_pop=50, target_population=5000, semi_stoch_space=1, semi_stoch_size=40,
+                       semi_stoch_start_iter=8), 4),
+]
+
+
+@pytest.mark.parametrize("name,opts,nrep", RUNS, ids=[r[0] for r in RUNS])
+def test_whole_run_semi_stoch_bit_exact(name, opts, nrep):
+    s = SYS[name]
+    cfg = make_config(s, ncycles=10, seed=29, state_size=1500000, spawned_state_size=1500000, **opts)
+    o = Oracle(s, cfg)
+    g = engine(s, cfg)
+    o.initial_distribution()
+    g.initial_distribution()
+    for r in range(nrep):
+        ro = o.run_report()
+        rg = g.run_report()
+        assert ro.error_flags == 0 and rg.error_flags == 0
+        so, po, ko = o.walkers()
+        sg, pg, kg = g.walkers()
+        np.testing.assert_array_equal(sg, so, err_msg="report %d states" % r)
+        np.testing.assert_array_equal(pg, po, err_msg="report %d pops" % r)
+        assert_close(kg, ko)
+        assert rg.nattempts == ro.nattempts
+        assert list(rg.shift) == list(ro.shift)
+        assert_close(rg.proj_energy[0], ro.proj_energy[0], 1e-10)
+    assert o.determ_space().shape[0] == opts["semi_stoch_size"]
+    o.close()
+
+
+def test_full_space_power_iteration_bit_exact():
+    s = SYS["h2o_sto2g"]
+    sym = fci.det_symmetry(s, s.aufbau_occ())
+    dets = np.array(fci.enumerate_dets(s, sym))
+    dets = dets[sort_dets(dets)]
+    n = len(dets)
+    cfg = make_config(s, tau=0.01, ncycles=20, real_amplitudes=True, initial_shift=-0.3, target_population=1e12,
+                      semi_stoch_space=1, semi_stoch_size=n, semi_stoch_start_iter=1, state_size=10000,
+                      spawned_state_size=10000, seed=3)
+    pops = np.zeros((n, 1), dtype=np.int64)
+    pops[0, 0] = 100 << 31
+    pops[n // 2, 0] = -(7 << 31)
+    o = Oracle(s, cfg)
+    g = engine(s, cfg)
+    o.set_walkers(dets, pops)
+    g.set_walkers(dets, pops)
+    for r in range(2):
+        o.run_report()
+        g.run_report()
+        so, po, _ = o.walkers()
+        sg, pg, _ = g.walkers()
+        np.testing.assert_array_equal(sg, so)
+        np.testing.assert_array_equal(pg, po)
+    assert sg.shape[0] == n
+    o.close()
+
+
+def test_semi_stoch_refusals():
+    from hande_gb300.engine import HgpuError
+    s = SYS["mol26"]
+    with pytest.raises(HgpuError):  # the replica RDM with a deterministic space
+        engine(s, make_config(s, tau=0.01, nspaces=2, density_matrices=True, real_amplitudes=True,
+                              semi_stoch_space=1, semi_stoch_size=10, state_size=100, spawned_state_size=100))
+    with pytest.raises(HgpuError):  # read_determ_space (an HDF5 file)
+        engine(s, make_config(s, tau=0.01, semi_stoch_space=2, semi_stoch_size=10, state_size=100,
+                              spawned_state_size=100))

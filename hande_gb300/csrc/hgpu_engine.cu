@@ -855,6 +855,8 @@ static int set_list(hgpu_handle *h, const int64_t *states, const int64_t *pops, 
     if (rc) return rc;
     st.n_main = n;
     st.abs_pop[0] = st.abs_pop[1] = 0;
+    // the cycles read the shift from the device state: publish the current one
+    for (int s = 0; s < HGPU_MAX_SPACES; s++) st.shift[s] = h->shift[s];
     if ((rc = write_state(h, &st))) return rc;
     launch_abs_pop(h->b, R, 0, h->stream);
     if ((rc = read_state(h, &st))) return rc;

@@ -25,6 +25,34 @@ QMC_KEYS = {
     "shift_damping", "vary_shift_from", "initial_shift", "precision",
 }
 FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file"}
+SEMI_STOCH_KEYS = {"space", "size", "start_iteration", "shift_start_iteration", "separate_annihilation"}
+
+
+def semi_stoch_options(ss: Optional[dict]) -> dict:
+    """The semi_stoch table of read_semi_stoch_in (src/lua_hande_calc.f90:1640-1721):
+    space = 'high' with its size; start_iteration (default 1); with
+    shift_start_iteration the start waits for the shift (start_iteration =
+    huge).  'read' needs a HANDE HDF5 file and 'ci' is not provided;
+    separate_annihilation = false (combined annihilation) is not provided."""
+    if not ss:
+        return {}
+    unknown = set(ss) - SEMI_STOCH_KEYS
+    if unknown:
+        raise ValueError("unknown semi_stoch option(s): %s" % ", ".join(sorted(unknown)))
+    if "space" not in ss:
+        raise ValueError("Deterministic space not specified.")
+    if ss["space"] != "high":
+        raise ValueError("semi_stoch space %r is not provided (only 'high')" % ss["space"])
+    if "size" not in ss:
+        raise ValueError("Target space size not given.")
+    if not ss.get("separate_annihilation", True):
+        raise ValueError("semi_stoch separate_annihilation = false is not provided")
+    out = dict(semi_stoch_space=1, semi_stoch_size=int(ss["size"]),
+               semi_stoch_start_iter=int(ss.get("start_iteration", 1)), semi_stoch_shift_iter=-1)
+    if "shift_start_iteration" in ss:
+        out["semi_stoch_start_iter"] = 2 ** 62
+        out["semi_stoch_shift_iter"] = int(ss["shift_start_iteration"])
+    return out
 
 
 def _opts(qmc: dict, fciqmc_opts: Optional[dict]):
@@ -41,7 +69,8 @@ def _opts(qmc: dict, fciqmc_opts: Optional[dict]):
     return fo
 
 
-def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] = None, reference=None):
+def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] = None, reference=None,
+                        semi_stoch: Optional[dict] = None):
     fo = _opts(qmc, fciqmc_opts)
     vsf = qmc.get("vary_shift_from", 0.0)
     prec = qmc.get("precision", "fp64")
@@ -63,7 +92,7 @@ def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] =
         density_matrix_report=int(fo.get("density_matrix_report", 0)),
         precision=PREC_MIXED if prec in ("mixed", "fp32", PREC_MIXED) else PREC_FP64,
         state_size=int(qmc.get("state_size", -1000)), spawned_state_size=int(qmc.get("spawned_state_size", -500)),
-        reference=reference)
+        reference=reference, **semi_stoch_options(semi_stoch))
 
 
 HEADER = (" iterations      Shift        \\sum H_0j N_j       N_0          # H psips    # states  "
@@ -71,13 +100,13 @@ HEADER = (" iterations      Shift        \\sum H_0j N_j       N_0          # H p
 
 
 def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None, out=None,
-           comm_file: str = "HANDE.COMM", verbose: bool = True) -> dict:
+           comm_file: str = "HANDE.COMM", verbose: bool = True, semi_stoch: Optional[dict] = None) -> dict:
     """Run FCIQMC on the GPU.  Returns {'reports': [...], 'engine': Engine}.
 
     A file named ``comm_file`` containing ``softexit = true`` in the working
     directory ends the calculation after the current report (calc_interact,
     src/interact.F90:11-188)."""
-    cfg = config_from_options(sys, qmc, fciqmc, reference)
+    cfg = config_from_options(sys, qmc, fciqmc, reference, semi_stoch)
     eng = Engine(sys, cfg)
     eng.initial_distribution()
     stream = out if out is not None else sys_stdout()

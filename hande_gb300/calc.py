@@ -25,15 +25,17 @@ QMC_KEYS = {
     "shift_damping", "vary_shift_from", "initial_shift", "precision",
 }
 FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file"}
-SEMI_STOCH_KEYS = {"space", "size", "start_iteration", "shift_start_iteration", "separate_annihilation"}
+SEMI_STOCH_KEYS = {"space", "size", "start_iteration", "shift_start_iteration", "separate_annihilation", "ci_space"}
 
 
 def semi_stoch_options(ss: Optional[dict]) -> dict:
     """The semi_stoch table of read_semi_stoch_in (src/lua_hande_calc.f90:1640-1721):
-    space = 'high' with its size; start_iteration (default 1); with
+    space = 'high' with its size, or 'ci' with ci_space = {ex_level = n} (the
+    calculation's reference); start_iteration (default 1); with
     shift_start_iteration the start waits for the shift (start_iteration =
-    huge).  'read' needs a HANDE HDF5 file and 'ci' is not provided;
-    separate_annihilation = false (combined annihilation) is not provided."""
+    huge).  'read' needs a HANDE HDF5 file; separate_annihilation = false
+    (combined annihilation) and a ci_space with its own determinant are not
+    provided."""
     if not ss:
         return {}
     unknown = set(ss) - SEMI_STOCH_KEYS
@@ -41,14 +43,20 @@ def semi_stoch_options(ss: Optional[dict]) -> dict:
         raise ValueError("unknown semi_stoch option(s): %s" % ", ".join(sorted(unknown)))
     if "space" not in ss:
         raise ValueError("Deterministic space not specified.")
-    if ss["space"] != "high":
-        raise ValueError("semi_stoch space %r is not provided (only 'high')" % ss["space"])
-    if "size" not in ss:
-        raise ValueError("Target space size not given.")
+    if ss["space"] not in ("high", "ci"):
+        raise ValueError("semi_stoch space %r is not provided ('high', 'ci')" % ss["space"])
     if not ss.get("separate_annihilation", True):
         raise ValueError("semi_stoch separate_annihilation = false is not provided")
-    out = dict(semi_stoch_space=1, semi_stoch_size=int(ss["size"]),
-               semi_stoch_start_iter=int(ss.get("start_iteration", 1)), semi_stoch_shift_iter=-1)
+    out = dict(semi_stoch_start_iter=int(ss.get("start_iteration", 1)), semi_stoch_shift_iter=-1)
+    if ss["space"] == "high":
+        if "size" not in ss:
+            raise ValueError("Target space size not given.")
+        out.update(semi_stoch_space=1, semi_stoch_size=int(ss["size"]))
+    else:
+        ci = ss.get("ci_space") or {}
+        if set(ci) - {"ex_level"} or int(ci.get("ex_level", -1)) < 0:
+            raise ValueError("ci_space needs ex_level >= 0 (and no other key)")
+        out.update(semi_stoch_space=4, semi_stoch_ci_level=int(ci["ex_level"]))
     if "shift_start_iteration" in ss:
         out["semi_stoch_start_iter"] = 2 ** 62
         out["semi_stoch_shift_iter"] = int(ss["shift_start_iteration"])

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <queue>
 #include <vector>
@@ -755,9 +756,13 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     if (!(cfg->power_pitzer_min_weight >= 0.0 && cfg->power_pitzer_min_weight <= 1.0)) return HGPU_ERR_INVALID;
     // semi-stochastic: a 'high' space (read_in: read_determ_space needs HDF5), not
     // combined with the replica RDM
-    if (cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1) return HGPU_ERR_UNSUPPORTED;
-    if (cfg->semi_stoch_space == 1 && (cfg->semi_stoch_size < 1 || cfg->density_matrices))
-        return cfg->density_matrices ? HGPU_ERR_UNSUPPORTED : HGPU_ERR_INVALID;
+    if (cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1 && cfg->semi_stoch_space != 4)
+        return HGPU_ERR_UNSUPPORTED;
+    if (cfg->semi_stoch_space == 4 && sys->kind != HGPU_SYS_READ_IN) return HGPU_ERR_UNSUPPORTED;
+    if (cfg->semi_stoch_space != 0 && cfg->density_matrices) return HGPU_ERR_UNSUPPORTED;
+    if ((cfg->semi_stoch_space == 1 && cfg->semi_stoch_size < 1) ||
+        (cfg->semi_stoch_space == 4 && cfg->semi_stoch_ci_level < 0))
+        return HGPU_ERR_INVALID;
     // density_matrices: replica sampling of molecular systems (two spaces)
     if (cfg->density_matrices && (sys->kind != HGPU_SYS_READ_IN || cfg->nspaces != 2)) return HGPU_ERR_INVALID;
     // pattempt_parallel only with the spin-resolved generators, at most 1
@@ -794,7 +799,7 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     h->use_graphs = getenv("HGPU_NO_GRAPH") == nullptr;
     // semi_stoch_iter = max(start_iter, mc_cycles_done + 1) (src/fciqmc.f90:229)
     h->ss_iter = INT64_MAX;
-    if (cfg->semi_stoch_space == 1) h->ss_iter = cfg->semi_stoch_start_iter > 1 ? cfg->semi_stoch_start_iter : 1;
+    if (cfg->semi_stoch_space != 0) h->ss_iter = cfg->semi_stoch_start_iter > 1 ? cfg->semi_stoch_start_iter : 1;
     cudaGetDevice(&h->device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
@@ -942,37 +947,96 @@ static int ss_init(hgpu_handle *h) {
                            h->stream));
         CK(cudaStreamSynchronize(h->stream));
     }
-    const int64_t K = std::min<int64_t>(h->cfg.semi_stoch_size, n);
-    h->b.nd = 0;
-    if (K < 1) return HGPU_OK;
-    auto tot = [&](int64_t i) {
-        int64_t p = 0;
-        for (int s = 0; s < R; s++) p += std::llabs(pops[(size_t)i * R + s]);
-        return p;
+    auto less = [&](const uint64_t *a, const uint64_t *b) {
+        for (int w = W - 1; w >= 0; w--)
+            if (a[w] != b[w]) return a[w] < b[w];
+        return false;
     };
-    std::vector<int64_t> slot_of(K);
-    std::priority_queue<std::pair<int64_t, int64_t>, std::vector<std::pair<int64_t, int64_t>>,
-                        std::greater<std::pair<int64_t, int64_t>>>
-        heap;
-    for (int64_t i = 0; i < K; i++) {
-        slot_of[i] = i;
-        heap.push({tot(i), i});
-    }
-    for (int64_t i = K; i < n; i++) {
-        const int64_t p = tot(i);
-        if (p > heap.top().first) {
-            const int64_t sl = heap.top().second;
-            heap.pop();
-            slot_of[sl] = i;
-            heap.push({p, sl});
+    std::vector<uint64_t> dd;
+    int64_t K = 0;
+    h->b.nd = 0;
+    if (h->cfg.semi_stoch_space == 4) {
+        // create_ci_determ_space (src/semi_stoch.F90:1763-1805): every
+        // determinant of the reference's spin and symmetry within ci_level
+        // excitations of it
+        const uint64_t *f0 = h->hsys.f0;
+        std::vector<int> occ, virt;
+        for (int p = 0; p < h->hsys.nbasis; p++) {
+            if ((f0[p >> 6] >> (p & 63)) & 1u) occ.push_back(p);
+            else virt.push_back(p);
         }
+        // spin orbitals alternate alpha (even) and beta (odd); irreps as staged for the kernels
+        auto alpha = [](int p) { return (p & 1) == 0 ? 1 : 0; };
+        const uint8_t *sym = h->hsys.orbsym;
+        std::vector<uint64_t> f(f0, f0 + W);
+        std::function<void(size_t, int, int, int)> parts = [&](size_t v, int k, int na, int sy) {
+            if (k == 0) {
+                if (na == 0 && sy == 0) dd.insert(dd.end(), f.begin(), f.end());
+                return;
+            }
+            for (size_t q = v; q + k <= virt.size(); q++) {
+                const int p = virt[q], a = alpha(p);
+                if (na - a < 0) continue;
+                f[p >> 6] |= 1ull << (p & 63);
+                parts(q + 1, k - 1, na - a, sy ^ sym[p]);
+                f[p >> 6] &= ~(1ull << (p & 63));
+            }
+        };
+        std::function<void(size_t, int, int, int, int)> holes = [&](size_t o, int k, int kk, int na, int sy) {
+            if (k == 0) {
+                parts(0, kk, na, sy);
+                return;
+            }
+            for (size_t q = o; q + k <= occ.size(); q++) {
+                const int p = occ[q];
+                f[p >> 6] &= ~(1ull << (p & 63));
+                holes(q + 1, k - 1, kk, na + alpha(p), sy ^ sym[p]);
+                f[p >> 6] |= 1ull << (p & 63);
+            }
+        };
+        for (int k = 0; k <= h->cfg.semi_stoch_ci_level && k <= (int)occ.size() && k <= (int)virt.size(); k++)
+            holes(0, k, k, 0, 0);
+        K = (int64_t)(dd.size() / W);
+        std::vector<int64_t> order(K);
+        for (int64_t k = 0; k < K; k++) order[k] = k;
+        std::sort(order.begin(), order.end(),
+                  [&](int64_t x, int64_t y) { return less(&dd[(size_t)x * W], &dd[(size_t)y * W]); });
+        std::vector<uint64_t> sorted((size_t)K * W);
+        for (int64_t k = 0; k < K; k++)
+            for (int w = 0; w < W; w++) sorted[(size_t)k * W + w] = dd[(size_t)order[k] * W + w];
+        dd.swap(sorted);
+    } else {
+        K = std::min<int64_t>(h->cfg.semi_stoch_size, n);
+        auto tot = [&](int64_t i) {
+            int64_t p = 0;
+            for (int s = 0; s < R; s++) p += std::llabs(pops[(size_t)i * R + s]);
+            return p;
+        };
+        std::vector<int64_t> slot_of(K > 0 ? K : 0);
+        std::priority_queue<std::pair<int64_t, int64_t>, std::vector<std::pair<int64_t, int64_t>>,
+                            std::greater<std::pair<int64_t, int64_t>>>
+            heap;
+        for (int64_t i = 0; i < K; i++) {
+            slot_of[i] = i;
+            heap.push({tot(i), i});
+        }
+        for (int64_t i = K; i < n && K > 0; i++) {
+            const int64_t p = tot(i);
+            if (p > heap.top().first) {
+                const int64_t sl = heap.top().second;
+                heap.pop();
+                slot_of[sl] = i;
+                heap.push({p, sl});
+            }
+        }
+        // the main list is sorted, so the selected entries in index order are
+        // the space in main-list order
+        std::sort(slot_of.begin(), slot_of.end());
+        dd.resize((size_t)(K > 0 ? K : 0) * W);
+        for (int64_t k = 0; k < K; k++)
+            for (int w = 0; w < W; w++) dd[(size_t)k * W + w] = dets[(size_t)slot_of[k] * W + w];
     }
-    // the main list is sorted, so the selected entries in index order are the
-    // space in main-list order
-    std::sort(slot_of.begin(), slot_of.end());
-    std::vector<uint64_t> dd((size_t)K * W);
-    for (int64_t k = 0; k < K; k++)
-        for (int w = 0; w < W; w++) dd[(size_t)k * W + w] = dets[(size_t)slot_of[k] * W + w];
+    if (K < 1) return HGPU_OK;
     uint64_t *ddets;
     if ((rc = dalloc(h, &ddets, (size_t)K * W))) return rc;
     CK(cudaMemcpy(ddets, dd.data(), sizeof(uint64_t) * K * W, cudaMemcpyHostToDevice));
@@ -1012,11 +1076,6 @@ static int ss_init(hgpu_handle *h) {
     int64_t added = 0;
     {
         int64_t i = 0, k = 0;
-        auto less = [&](const uint64_t *a, const uint64_t *b) {
-            for (int w = W - 1; w >= 0; w--)
-                if (a[w] != b[w]) return a[w] < b[w];
-            return false;
-        };
         while (i < n || k < K) {
             const uint64_t *dm = i < n ? &dets[(size_t)i * W] : nullptr;
             const uint64_t *dk = k < K ? &dd[(size_t)k * W] : nullptr;
@@ -1297,7 +1356,7 @@ int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
     }
     // the deterministic space follows the shift (src/qmc_common.F90:1203-1204)
     for (int s = 0; s < R; s++) all_vary = all_vary && h->vary_shift[s];
-    if (!all_vary_before && all_vary && h->cfg.semi_stoch_space == 1 && h->cfg.semi_stoch_shift_iter != -1)
+    if (!all_vary_before && all_vary && h->cfg.semi_stoch_space != 0 && h->cfg.semi_stoch_shift_iter != -1)
         h->ss_iter = h->cfg.semi_stoch_shift_iter + st.iter + 1;
     for (int s = 0; s < R; s++) {
         out->shift[s] = h->shift[s];

@@ -154,12 +154,16 @@ typedef struct hgpu_config {
                                         (check_min_weight_ratio); must lie in [0, 1] */
     /* semi_stoch_in_t (src/qmc_data.f90:305-338), separate annihilation */
     int32_t semi_stoch_space;       /* space_type: 0 none, 1 'high' (the most populated
-                                       determinants when the space is built) */
+                                       determinants when the space is built), 4 'ci' (every
+                                       determinant of the reference's spin and symmetry within
+                                       semi_stoch_ci_level excitations of it; molecular systems) */
     int32_t semi_stoch_size;        /* target_size of a 'high' space */
     int64_t semi_stoch_start_iter;  /* start_iteration: the space is built at the start of
                                        this iteration (HANDE's default 1) */
     int64_t semi_stoch_shift_iter;  /* shift_start_iteration: built this many iterations after
                                        every shift varies (-1: not used) */
+    int32_t semi_stoch_ci_level;    /* ci_space%ex_level of a 'ci' space */
+    int32_t semi_stoch_reserved;    /* 0 */
 } hgpu_config;
 
 /* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */

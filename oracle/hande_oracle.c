@@ -2465,42 +2465,110 @@ static void ss_free(oracle_ctx *c) {
     c->ss_on = 0;
 }
 
-/* init_semi_stoch_t (src/semi_stoch.F90:134-377) for a 'high' space:
+/* init_semi_stoch_t (src/semi_stoch.F90:134-377) for a 'ci' space (ci_space)
+ * or a 'high' space:
  * find_most_populated_dets (:1318-1385, the target_size entries of largest
  * sum over spaces of |population|, scanning the main list in order and
  * replacing the first smallest), sorted; add_determ_dets_to_psip_list
  * (:728-793, absent ones enter with zero population); create_determ_hamil
  * (:533-685, |H| > depsilon kept; diagonal K_jj, the main list's exact
  * difference). */
+typedef struct {
+    uint64_t *d;
+    int64_t n, cap;
+} detlist_t;
+
+/* Particles of a 'ci' determinant: k more virtual orbitals from position v on,
+ * whose alpha count and irrep product must come to na and sym. */
+static void ci_particles(const oracle_ctx *c, const int *virt, int nv, int v, int k, int na, int sym,
+                         uint64_t *f, detlist_t *out) {
+    if (k == 0) {
+        if (na != 0 || sym != 0) return;
+        if (out->n == out->cap) {
+            out->cap = out->cap ? 2 * out->cap : 64;
+            out->d = (uint64_t *)realloc(out->d, sizeof(uint64_t) * c->nw * out->cap);
+        }
+        memcpy(&out->d[out->n * c->nw], f, sizeof(uint64_t) * c->nw);
+        out->n++;
+        return;
+    }
+    for (int q = v; q <= nv - k; q++) {
+        const int p = virt[q], a = c->orb_ms[p] > 0;
+        if (na - a < 0) continue;
+        f[p >> 6] |= (uint64_t)1 << (p & 63);
+        ci_particles(c, virt, nv, q + 1, k - 1, na - a, sym ^ c->orb_sym[p], f, out);
+        f[p >> 6] &= ~((uint64_t)1 << (p & 63));
+    }
+}
+
+/* Holes of a 'ci' determinant: k more occupied orbitals from position o on. */
+static void ci_holes(const oracle_ctx *c, const int *occ, int no, const int *virt, int nv, int o, int k, int kk,
+                     int na, int sym, uint64_t *f, detlist_t *out) {
+    if (k == 0) {
+        ci_particles(c, virt, nv, 0, kk, na, sym, f, out);
+        return;
+    }
+    for (int q = o; q <= no - k; q++) {
+        const int p = occ[q];
+        f[p >> 6] &= ~((uint64_t)1 << (p & 63));
+        ci_holes(c, occ, no, virt, nv, q + 1, k - 1, kk, na + (c->orb_ms[p] > 0), sym ^ c->orb_sym[p], f, out);
+        f[p >> 6] |= (uint64_t)1 << (p & 63);
+    }
+}
+
+/* create_ci_determ_space (src/semi_stoch.F90:1763-1805) with the calculation's
+ * reference: every determinant of its spin and symmetry within ci_level
+ * excitations of it (enumerate_determinants restricted to ex_level). */
+static detlist_t ci_space(const oracle_ctx *c) {
+    detlist_t out = {NULL, 0, 0};
+    int occ[MAXEL], virt[MAXB], no = 0, nv = 0;
+    for (int p = 0; p < c->nbasis; p++) {
+        if (tbit(c->f0, p)) occ[no++] = p;
+        else virt[nv++] = p;
+    }
+    uint64_t f[MAXW];
+    memcpy(f, c->f0, sizeof(f));
+    for (int k = 0; k <= c->cfg.semi_stoch_ci_level && k <= no && k <= nv; k++)
+        ci_holes(c, occ, no, virt, nv, 0, k, k, 0, 0, f, &out);
+    return out;
+}
+
 static void ss_init(oracle_ctx *c) {
     ss_free(c);
-    int64_t K = c->cfg.semi_stoch_size < c->n ? c->cfg.semi_stoch_size : c->n;
-    if (K < 1) return;
     const int nw = c->nw, R = c->R;
-    uint64_t *sel = (uint64_t *)malloc(sizeof(uint64_t) * nw * K);
-    int64_t *pop = (int64_t *)malloc(sizeof(int64_t) * K);
-    for (int64_t i = 0; i < K; i++) {
-        memcpy(&sel[i * nw], &c->dets[i * nw], sizeof(uint64_t) * nw);
-        int64_t p = 0;
-        for (int s = 0; s < R; s++) p += llabs(c->pops[i * R + s]);
-        pop[i] = p;
+    if (c->cfg.semi_stoch_space == 4) {
+        detlist_t L = ci_space(c);
+        c->nd = L.n;
+        c->ddets = L.d;
     }
-    int64_t min_pop = pop[0], min_ind = 0;
-    for (int64_t i = 1; i < K; i++)
-        if (pop[i] < min_pop) { min_pop = pop[i]; min_ind = i; }
-    for (int64_t i = K; i < c->n; i++) {
-        int64_t p = 0;
-        for (int s = 0; s < R; s++) p += llabs(c->pops[i * R + s]);
-        if (p > min_pop) {
-            memcpy(&sel[min_ind * nw], &c->dets[i * nw], sizeof(uint64_t) * nw);
-            pop[min_ind] = p;
-            min_pop = pop[0];
-            min_ind = 0;
-            for (int64_t j = 1; j < K; j++)
-                if (pop[j] < min_pop) { min_pop = pop[j]; min_ind = j; }
+    int64_t K = c->cfg.semi_stoch_space == 4 ? c->nd : (c->cfg.semi_stoch_size < c->n ? c->cfg.semi_stoch_size : c->n);
+    if (K < 1) return;
+    uint64_t *sel = c->cfg.semi_stoch_space == 4 ? c->ddets : (uint64_t *)malloc(sizeof(uint64_t) * nw * K);
+    if (c->cfg.semi_stoch_space == 1) {
+        int64_t *pop = (int64_t *)malloc(sizeof(int64_t) * K);
+        for (int64_t i = 0; i < K; i++) {
+            memcpy(&sel[i * nw], &c->dets[i * nw], sizeof(uint64_t) * nw);
+            int64_t p = 0;
+            for (int s = 0; s < R; s++) p += llabs(c->pops[i * R + s]);
+            pop[i] = p;
         }
+        int64_t min_pop = pop[0], min_ind = 0;
+        for (int64_t i = 1; i < K; i++)
+            if (pop[i] < min_pop) { min_pop = pop[i]; min_ind = i; }
+        for (int64_t i = K; i < c->n; i++) {
+            int64_t p = 0;
+            for (int s = 0; s < R; s++) p += llabs(c->pops[i * R + s]);
+            if (p > min_pop) {
+                memcpy(&sel[min_ind * nw], &c->dets[i * nw], sizeof(uint64_t) * nw);
+                pop[min_ind] = p;
+                min_pop = pop[0];
+                min_ind = 0;
+                for (int64_t j = 1; j < K; j++)
+                    if (pop[j] < min_pop) { min_pop = pop[j]; min_ind = j; }
+            }
+        }
+        free(pop);
     }
-    free(pop);
     /* qsort into the main list's order (insertion sort: small spaces) */
     for (int64_t i = 1; i < K; i++) {
         uint64_t t[MAXW];
@@ -2797,7 +2865,8 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
     /* semi_stoch_iter = max(start_iter, mc_cycles_done + 1) (src/fciqmc.f90:229) */
     c->ss_iter = INT64_MAX;
     if (cfg->semi_stoch_space != 0) c->ss_iter = cfg->semi_stoch_start_iter > 1 ? cfg->semi_stoch_start_iter : 1;
-    if ((cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1) ||
+    if ((cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1 && cfg->semi_stoch_space != 4) ||
+        (cfg->semi_stoch_space == 4 && c->kind != HGPU_SYS_READ_IN) ||
         (cfg->semi_stoch_space != 0 && cfg->density_matrices)) {
         oracle_destroy(c);
         return NULL;

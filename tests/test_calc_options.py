@@ -24,6 +24,8 @@ def test_semi_stoch_table():
     # shift_start_iteration: start_iteration = huge(0), fixed up when the shift varies
     cfg = calc.config_from_options(s, QMC, semi_stoch=dict(space="high", size=50, shift_start_iteration=7))
     assert cfg.semi_stoch_shift_iter == 7 and cfg.semi_stoch_start_iter > 2 ** 40
+    cfg = calc.config_from_options(s, QMC, semi_stoch=dict(space="ci", ci_space=dict(ex_level=2)))
+    assert (cfg.semi_stoch_space, cfg.semi_stoch_ci_level) == (4, 2)
     cfg = calc.config_from_options(s, QMC)
     assert cfg.semi_stoch_space == 0
     for bad in (dict(size=5), dict(space="high"), dict(space="read"), dict(space="high", size=5, bogus=1),

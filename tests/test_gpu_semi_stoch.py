@@ -26,10 +26,15 @@ RUNS = [
                       semi_stoch_space=1, semi_stoch_size=150, semi_stoch_start_iter=6), 3),
     ("hub_k_4x4", dict(tau=0.01, init_pop=50, target_population=5000, semi_stoch_space=1, semi_stoch_size=40,
                        semi_stoch_start_iter=8), 4),
+    # 'ci' spaces: CISD of H2O/STO-2G, CIS of the M=26 molecule
+    ("h2o_sto2g", dict(tau=0.01, init_pop=20, target_population=400, real_amplitudes=True, initial_shift=1.0,
+                       semi_stoch_space=4, semi_stoch_ci_level=2, semi_stoch_start_iter=5), 6),
+    ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
+                   semi_stoch_space=4, semi_stoch_ci_level=1, semi_stoch_start_iter=12), 3),
 ]
 
 
-@pytest.mark.parametrize("name,opts,nrep", RUNS, ids=[r[0] for r in RUNS])
+@pytest.mark.parametrize("name,opts,nrep", RUNS, ids=["%s-%d" % (r[0], i) for i, r in enumerate(RUNS)])
 def test_whole_run_semi_stoch_bit_exact(name, opts, nrep):
     s = SYS[name]
     cfg = make_config(s, ncycles=10, seed=29, state_size=1500000, spawned_state_size=1500000, **opts)
@@ -49,7 +54,10 @@ def test_whole_run_semi_stoch_bit_exact(name, opts, nrep):
         assert rg.nattempts == ro.nattempts
         assert list(rg.shift) == list(ro.shift)
         assert_close(rg.proj_energy[0], ro.proj_energy[0], 1e-10)
-    assert o.determ_space().shape[0] == opts["semi_stoch_size"]
+    if opts["semi_stoch_space"] == 1:
+        assert o.determ_space().shape[0] == opts["semi_stoch_size"]
+    else:
+        assert o.determ_space().shape[0] > 1
     o.close()
 
 

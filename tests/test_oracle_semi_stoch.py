@@ -115,3 +115,26 @@ def test_semi_stoch_energy_h2o_matches_fci():
     assert len(num) > 150
     e, err, _ = analysis.projected_energy(num, den)
     assert abs(e + h00 - e_fci) < max(4.0 * err, 2e-3), (e + h00, e_fci, err)
+
+
+def test_ci_space_contents():
+    """create_ci_determ_space: every determinant of the reference's spin and
+    symmetry within ex_level excitations of it."""
+    s = _h2o()
+    sym = fci.det_symmetry(s, s.aufbau_occ())
+    f0 = s.encode(s.aufbau_occ()).view(np.int64)
+    for level in (1, 2):
+        cfg = make_config(s, tau=0.01, real_amplitudes=True, semi_stoch_space=4, semi_stoch_ci_level=level,
+                          semi_stoch_start_iter=1, state_size=10000, spawned_state_size=10000)
+        o = Oracle(s, cfg)
+        o.initial_distribution()
+        o.run_report()
+        got = o.determ_space()
+        st, po, _ = o.walkers()
+        o.close()
+        dets = np.array(fci.enumerate_dets(s, sym))
+        xl = [bin(int(np.bitwise_xor(d, f0).view(np.uint64)[0])).count("1") // 2 for d in dets]
+        want = dets[np.array(xl) <= level]
+        want = want[sort_dets(want)]
+        np.testing.assert_array_equal(got, want)
+        assert st.shape[0] >= want.shape[0]  # all in the main list, with zero population if need be

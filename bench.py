@@ -427,6 +427,56 @@ LARGE_WORKLOAD = ("config5: synthetic molecule M=64 nel=20 ms=0 C1 (two-word det
                   "p_gen, FP64 estimators, grown on the device to ~5e8 walkers in total, shift from E_proj")
 
 
+def semi_stoch_run(size, steps=10, warmup=3, target=1e7):
+    """The config-2 cycle with a semi-stochastic 'high' space of `size`
+    determinants (src/semi_stoch.F90): the walker list is grown as for the
+    headline line, moved into a second calculation whose space is built at its
+    first cycle from that list, then whole cycles are timed from a snapshot
+    taken after the build.  Returns the per-cycle device time, the phase split
+    and the one-time cost of building the space."""
+    from hande_gb300.engine import Engine
+    s, cfg = system_and_config(target=target)
+    a = Engine(s, cfg)
+    a.initial_distribution()
+    grow(a, target)
+    st, po, da = a.walkers()
+    a.close()
+    cfg2 = type(cfg).from_buffer_copy(cfg)
+    cfg2.semi_stoch_space = 1
+    cfg2.semi_stoch_size = int(size)
+    cfg2.semi_stoch_start_iter = 1
+    b = Engine(s, cfg2)
+    b.set_walkers(st, po, da)
+    t0 = time.time()
+    b.run_cycles(1)  # builds the space at the start of iteration 1, then one cycle
+    r0 = b.end_report()
+    build_s = time.time() - t0
+    b.snapshot()
+    for _ in range(max(warmup, 3)):
+        b.snapshot(restore=True)
+        b.run_cycles(1)
+        b.end_report()
+    dev_ms, attempts, flags = 0.0, 0, r0.error_flags
+    for _ in range(steps):
+        b.snapshot(restore=True)
+        b.run_cycles(1)
+        r = b.end_report()
+        dev_ms += r.device_ms
+        attempts += r.nattempts
+        flags |= r.error_flags
+    b.snapshot(restore=True)
+    phases, counts = b.profile_cycle()
+    b.close()
+    if flags:
+        raise RuntimeError("semi-stochastic run flagged errors (%d)" % flags)
+    return {"workload": "config2 cycle with a semi-stochastic 'high' space of %d determinants, built from the "
+                        "grown %d-state list" % (size, st.shape[0]),
+            "space_size": int(size), "steps": steps, "ms_per_step": dev_ms / steps,
+            "attempts_per_s": attempts / (dev_ms / 1e3),
+            "first_cycle_with_build_s": build_s, "phase_ms": phases, "cycle_counts": counts,
+            "note": "the projection kernel runs inside the spawn phase (after k_spawn)"}
+
+
 def large_replica_run(target_total=5e8, tau=2e-4, cycles=5, seed=2024, max_grow=60):
     """config 5: one large replica calculation, measured like the headline
     step -- grown on the device (shift held at 0) until the two replicas hold
@@ -529,6 +579,8 @@ def main():
                     help="2: the headline line (default); 1: the Hubbard 4x4 run of config 1; 3: the "
                          "mixed-precision study of config 3; 5: the large replica run of config 5 (one JSON line each)")
     ap.add_argument("--large-total", type=float, default=5e8, help="config 5: total walkers of both replicas")
+    ap.add_argument("--semi-stoch", type=int, default=0,
+                    help="time the config-2 cycle with a semi-stochastic 'high' space of this size (one JSON line)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -549,6 +601,11 @@ def main():
     if args.config == 5:
         if rank == 0:
             print(json.dumps(large_replica_run(target_total=args.large_total, cycles=args.steps)))
+        return
+    if args.semi_stoch > 0:
+        if rank == 0:
+            print(json.dumps(semi_stoch_run(args.semi_stoch, steps=args.steps, warmup=args.warmup,
+                                            target=args.target)))
         return
 
     cpu = None

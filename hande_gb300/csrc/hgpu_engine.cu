@@ -1424,6 +1424,18 @@ int32_t hgpu_set_state(hgpu_handle *h, const hgpu_state *in) {
         st.shift[s] = in->shift[s];
     }
     h->iter = in->iteration;
+    // a restarted calculation builds its deterministic space again:
+    // semi_stoch_iter = max(start_iter, mc_cycles_done + 1), or mc_cycles_done + 1
+    // when every shift already varies and shift_start_iteration is set
+    // (src/fciqmc.f90:229-235)
+    if (h->cfg.semi_stoch_space != 0) {
+        bool all_vary = true;
+        for (int s = 0; s < h->R; s++) all_vary = all_vary && h->vary_shift[s];
+        h->ss_iter = std::max<int64_t>(h->cfg.semi_stoch_start_iter, h->iter + 1);
+        if (all_vary && h->cfg.semi_stoch_shift_iter != -1) h->ss_iter = h->iter + 1;
+        h->b.nd = 0;
+        invalidate_graphs(h);
+    }
     return write_state(h, &st);
 }
 

@@ -97,3 +97,23 @@ def test_semi_stoch_refusals():
     with pytest.raises(HgpuError):  # read_determ_space (an HDF5 file)
         engine(s, make_config(s, tau=0.01, semi_stoch_space=2, semi_stoch_size=10, state_size=100,
                               spawned_state_size=100))
+
+
+def test_restart_rebuilds_space(tmp_path):
+    """A restored calculation builds its deterministic space again at its first
+    iteration (src/fciqmc.f90:229-235) and carries on without errors."""
+    s = SYS["mol26"]
+    cfg = make_config(s, ncycles=10, seed=31, tau=1e-4, init_pop=2000, target_population=20000,
+                      real_amplitudes=True, semi_stoch_space=1, semi_stoch_size=200, semi_stoch_start_iter=5,
+                      state_size=1500000, spawned_state_size=1500000)
+    g = engine(s, cfg)
+    g.initial_distribution()
+    g.run_report()
+    path = str(tmp_path / "ss.ckpt")
+    g.checkpoint(path)
+    h = engine(s, cfg)
+    h.restore(path)
+    r = h.run_report()
+    assert r.error_flags == 0
+    sg, pg, _ = h.walkers()
+    assert sg.shape[0] >= 200

@@ -35,7 +35,7 @@ module hande_gpu_m
         real(c_double) :: tau, shift_damping, initial_shift, vary_shift_from, target_particles
         real(c_double) :: initiator_pop, spawn_cutoff, pattempt_single, pattempt_double, D0_population
         integer(c_int32_t) :: vary_shift_from_proje, excit_gen, real_amplitudes, initiator_approx
-        integer(c_int32_t) :: nspaces, ncycles, precision, reserved0
+        integer(c_int32_t) :: nspaces, ncycles, precision, quadrature_initiator
         integer(c_int64_t) :: seed, walker_length, spawned_walker_length
         integer(c_uint64_t) :: ref_det(HGPU_MAX_WORDS)
         real(c_double) :: pattempt_parallel
@@ -57,9 +57,33 @@ module hande_gpu_m
         integer(c_int32_t) :: error_flags, reserved0
         real(c_double) :: device_ms
         real(c_double) :: rdm_energy, rdm_trace
+        integer(c_int64_t) :: nblooms
+        real(c_double) :: tot_bloom, max_bloom
     end type hgpu_report
 
+    type, bind(c) :: hgpu_state
+        integer(c_int64_t) :: iteration
+        real(c_double) :: shift(HGPU_MAX_SPACES)
+        integer(c_int32_t) :: vary_shift(HGPU_MAX_SPACES)
+        real(c_double) :: nparticles_old(HGPU_MAX_SPACES)
+        real(c_double) :: tau
+        integer(c_int64_t) :: seed
+    end type hgpu_state
+
     interface
+        integer(c_int32_t) function hgpu_version() bind(c, name='hgpu_version')
+            import :: c_int32_t
+        end function hgpu_version
+
+        type(c_ptr) function hgpu_error_string(status) bind(c, name='hgpu_error_string')
+            import :: c_ptr, c_int32_t
+            integer(c_int32_t), value :: status
+        end function hgpu_error_string
+
+        integer(c_int32_t) function hgpu_device_count() bind(c, name='hgpu_device_count')
+            import :: c_int32_t
+        end function hgpu_device_count
+
         integer(c_int32_t) function hgpu_create(cfg, sys, h) bind(c, name='hgpu_create')
             import :: hgpu_config, hgpu_system, c_ptr, c_int32_t
             type(hgpu_config), intent(in) :: cfg
@@ -132,6 +156,76 @@ module hande_gpu_m
             type(c_ptr), value :: h
             character(kind=c_char), intent(in) :: path(*)
         end function hgpu_restore
+
+        ! Scalars of qmc_state_t for a restart-aware do_fciqmc (iteration, shift,
+        ! vary_shift, N_w of the last report, tau, seed).
+        integer(c_int32_t) function hgpu_get_state(h, st) bind(c, name='hgpu_get_state')
+            import :: c_ptr, c_int32_t, hgpu_state
+            type(c_ptr), value :: h
+            type(hgpu_state), intent(out) :: st
+        end function hgpu_get_state
+
+        integer(c_int32_t) function hgpu_set_state(h, st) bind(c, name='hgpu_set_state')
+            import :: c_ptr, c_int32_t, hgpu_state
+            type(c_ptr), value :: h
+            type(hgpu_state), intent(in) :: st
+        end function hgpu_set_state
+
+        integer(c_int32_t) function hgpu_snapshot(h, restore) bind(c, name='hgpu_snapshot')
+            import :: c_ptr, c_int32_t
+            type(c_ptr), value :: h
+            integer(c_int32_t), value :: restore
+        end function hgpu_snapshot
+
+        integer(c_int32_t) function hgpu_profile_cycle(h, phase_ms, nphase, counts) bind(c, name='hgpu_profile_cycle')
+            import :: c_ptr, c_int32_t, c_int64_t, c_double
+            type(c_ptr), value :: h
+            real(c_double), intent(out) :: phase_ms(*)
+            integer(c_int32_t), value :: nphase
+            integer(c_int64_t), intent(out) :: counts(*)
+        end function hgpu_profile_cycle
+
+        ! Parity entry points (fixed inputs, results on the host).
+        integer(c_int32_t) function hgpu_eval_excitations(h, parents, parent_pops, n, iteration, orbs, pgen, &
+                hmatel, allowed, nspawn) bind(c, name='hgpu_eval_excitations')
+            import :: c_ptr, c_int32_t, c_int64_t, c_double
+            type(c_ptr), value :: h
+            integer(c_int64_t), intent(in) :: parents(*), parent_pops(*)
+            integer(c_int64_t), value :: n, iteration
+            integer(c_int32_t), intent(out) :: orbs(*)
+            real(c_double), intent(out) :: pgen(*), hmatel(*)
+            integer(c_int32_t), intent(out) :: allowed(*)
+            integer(c_int64_t), intent(out) :: nspawn(*)
+        end function hgpu_eval_excitations
+
+        integer(c_int32_t) function hgpu_annihilate_fixed(h, sdata, n, iteration) bind(c, name='hgpu_annihilate_fixed')
+            import :: c_ptr, c_int32_t, c_int64_t
+            type(c_ptr), value :: h
+            integer(c_int64_t), intent(in) :: sdata(*)
+            integer(c_int64_t), value :: n, iteration
+        end function hgpu_annihilate_fixed
+
+        integer(c_int32_t) function hgpu_eval_diagonal(h, dets, n, kii) bind(c, name='hgpu_eval_diagonal')
+            import :: c_ptr, c_int32_t, c_int64_t, c_double
+            type(c_ptr), value :: h
+            integer(c_int64_t), intent(in) :: dets(*)
+            integer(c_int64_t), value :: n
+            real(c_double), intent(out) :: kii(*)
+        end function hgpu_eval_diagonal
+
+        ! Self-annihilation of a device-resident spawned list without device
+        ! allocation by the library (d_sdata, d_out and stream are device
+        ! pointers / a cudaStream_t passed as c_ptr).
+        integer(c_int32_t) function hgpu_self_annihilate_noalloc(d_sdata, n, nwords, nspaces, d_out, n_out, &
+                stream) bind(c, name='hgpu_self_annihilate_noalloc')
+            import :: c_ptr, c_int32_t, c_int64_t
+            type(c_ptr), value :: d_sdata
+            integer(c_int64_t), value :: n
+            integer(c_int32_t), value :: nwords, nspaces
+            type(c_ptr), value :: d_out
+            integer(c_int64_t), intent(out) :: n_out
+            type(c_ptr), value :: stream
+        end function hgpu_self_annihilate_noalloc
 
         ! Batches: many handles advanced together, one graph launch per cycle.
         integer(c_int32_t) function hgpu_batch_create(handles, n, batch) bind(c, name='hgpu_batch_create')

@@ -63,7 +63,7 @@ class HgpuConfig(C.Structure):
         ("D0_population", C.c_double),
         ("vary_shift_from_proje", C.c_int32), ("excit_gen", C.c_int32),
         ("real_amplitudes", C.c_int32), ("initiator_approx", C.c_int32), ("nspaces", C.c_int32),
-        ("ncycles", C.c_int32), ("precision", C.c_int32), ("reserved0", C.c_int32),
+        ("ncycles", C.c_int32), ("precision", C.c_int32), ("quadrature_initiator", C.c_int32),
         ("seed", C.c_int64), ("walker_length", C.c_int64), ("spawned_walker_length", C.c_int64),
         ("ref_det", C.c_uint64 * MAX_WORDS), ("pattempt_parallel", C.c_double),
         ("density_matrices", C.c_int32), ("density_matrix_report", C.c_int32),
@@ -83,6 +83,7 @@ class HgpuReport(C.Structure):
         ("nattempts", C.c_int64), ("nspawned", C.c_int64), ("error_flags", C.c_int32),
         ("reserved0", C.c_int32), ("device_ms", C.c_double),
         ("rdm_energy", C.c_double), ("rdm_trace", C.c_double),
+        ("nblooms", C.c_int64), ("tot_bloom", C.c_double), ("max_bloom", C.c_double),
     ]
 
     def as_dict(self, nspaces: int = 1) -> dict:
@@ -100,6 +101,9 @@ class HgpuReport(C.Structure):
             "spawned": int(self.nspawned),
             "error_flags": int(self.error_flags),
             "device_ms": float(self.device_ms),
+            "blooms": int(self.nblooms),
+            "bloom particles": float(self.tot_bloom),
+            "max bloom": float(self.max_bloom),
         }
         if self.rdm_trace != 0.0:
             r["RDM energy num."] = float(self.rdm_energy)
@@ -172,7 +176,8 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
                 pattempt_single: float = -1.0, pattempt_double: float = -1.0,
                 pattempt_parallel: float = -1.0, density_matrices: bool = False,
                 density_matrix_report: int = 0, power_pitzer_min_weight: float = 0.01, initiator: bool = False,
-                initiator_threshold: float = 3.0, nspaces: int = 1, semi_stoch_space: int = 0,
+                initiator_threshold: float = 3.0, quadrature_initiator: bool = True, nspaces: int = 1,
+                semi_stoch_space: int = 0,
                 semi_stoch_size: int = 0, semi_stoch_start_iter: int = 1, semi_stoch_shift_iter: int = -1,
                 semi_stoch_ci_level: int = 0,
                 precision: int = PREC_FP64, state_size: int = 100000,
@@ -202,6 +207,7 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
     cfg.excit_gen = EXCIT_GEN[excit_gen] if isinstance(excit_gen, str) else int(excit_gen)
     cfg.real_amplitudes = int(bool(real_amplitudes))
     cfg.initiator_approx = int(bool(initiator))
+    cfg.quadrature_initiator = int(bool(quadrature_initiator))
     cfg.nspaces = nspaces
     cfg.ncycles = ncycles
     cfg.precision = precision

@@ -85,10 +85,13 @@ def projected_energy(numerator: Sequence[float], d0: Sequence[float], min_blocks
     return e, max(errs) if errs else float("nan"), -1
 
 
-def mean_error(series: Sequence[float]):
-    """Reblocked mean and standard error of one series (e.g. the shift)."""
+def mean_error(series: Sequence[float], min_blocks: int = 16):
+    """Reblocked mean and standard error of one series (e.g. the shift).
+    Without an optimal block the error is the largest over the iterations that
+    keep at least min_blocks blocks (conservative; the block is then -1)."""
     blocks = reblock(np.asarray(series, float))
     opt = optimal_block(blocks)
     if opt < 0:
-        return float(blocks[0].mean[0]), float("nan"), opt
+        errs = [float(b.std_err[0]) for b in blocks if b.ndata >= min_blocks]
+        return float(blocks[0].mean[0]), max(errs) if errs else float("nan"), opt
     return float(blocks[0].mean[0]), float(blocks[opt].std_err[0]), opt

@@ -24,7 +24,8 @@ QMC_KEYS = {
     "pattempt_double", "pattempt_parallel", "power_pitzer_min_weight", "initiator", "initiator_threshold",
     "shift_damping", "vary_shift_from", "initial_shift", "precision",
 }
-FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file"}
+FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file",
+               "quadrature_initiator"}
 SEMI_STOCH_KEYS = {"space", "size", "start_iteration", "shift_start_iteration", "separate_annihilation", "ci_space"}
 
 
@@ -97,6 +98,7 @@ def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] =
         # density_matrices turns replica_tricks on (src/lua_hande_calc.f90:1569-1573)
         nspaces=2 if (fo.get("replica_tricks") or fo.get("density_matrices")) else 1,
         density_matrices=bool(fo.get("density_matrices", False)),
+        quadrature_initiator=bool(fo.get("quadrature_initiator", True)),
         density_matrix_report=int(fo.get("density_matrix_report", 0)),
         precision=PREC_MIXED if prec in ("mixed", "fp32", PREC_MIXED) else PREC_FP64,
         state_size=int(qmc.get("state_size", -1000)), spawned_state_size=int(qmc.get("spawned_state_size", -500)),

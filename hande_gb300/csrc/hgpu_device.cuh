@@ -73,6 +73,8 @@ struct alignas(16) DevSys {
     int pad_spin;
     uint64_t t_parallel, t_alpha;
     double initiator_pop;
+    int quadrature_initiator;  // two spaces share one initiator test (set_parent_flag)
+    int pad_qi;
     double H00;
     uint64_t seed;
     uint64_t f0[kMaxWords];

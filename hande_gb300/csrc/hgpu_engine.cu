@@ -48,6 +48,7 @@ struct hgpu_handle {
     double nparticles_old[HGPU_MAX_SPACES];
     int64_t iter;
     int64_t ss_iter;  // iteration at whose start the deterministic space is built
+    int64_t ss_gen = 0;  // number of deterministic spaces built or dropped so far
     cudaEvent_t ev0, ev1;
     double report_ms;
     std::vector<void *> allocs;
@@ -60,6 +61,7 @@ struct hgpu_handle {
     double *snap_kii;
     int64_t snap_n;
     int64_t snap_abs[HGPU_MAX_SPACES];
+    int64_t snap_ss_gen = -1;  // ss_gen when the snapshot was taken
 };
 
 #define CK(x)                                                \
@@ -318,6 +320,7 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
     }
     s.t_single = (uint64_t)std::ceil(std::ldexp(s.pattempt_single, 53));
     s.initiator_pop = c.initiator_pop;
+    s.quadrature_initiator = c.quadrature_initiator != 0 && h->R == 2;
     s.seed = (uint64_t)c.seed;
     for (int w = 0; w < kMaxWords; w++) s.f0[w] = w < s.nw ? c.ref_det[w] : 0;
     FxTables fx;
@@ -709,6 +712,54 @@ static void invalidate_graphs(hgpu_handle *h) {
     }
 }
 
+// Free one allocation made by dalloc (and forget it).
+static void dfree(hgpu_handle *h, const void *p) {
+    if (!p) return;
+    auto it = std::find(h->allocs.begin(), h->allocs.end(), const_cast<void *>(p));
+    if (it == h->allocs.end()) return;
+    h->allocs.erase(it);
+    cudaFree(const_cast<void *>(p));
+}
+
+// Drop the deterministic space: its determinants, Hamiltonian columns and
+// per-cycle vectors are freed and no state is deterministic any more.
+static void ss_drop(hgpu_handle *h) {
+    DevBuffers &b = h->b;
+    dfree(h, b.ddets);
+    dfree(h, b.dcol_ptr);
+    dfree(h, b.dcol_i);
+    dfree(h, b.dcol_h);
+    dfree(h, b.dvec);
+    dfree(h, b.dind);
+    b.ddets = nullptr;
+    b.dcol_ptr = nullptr;
+    b.dcol_i = nullptr;
+    b.dcol_h = nullptr;
+    b.dvec = nullptr;
+    b.dind = nullptr;
+    b.nd = 0;
+    h->ss_gen++;
+}
+
+// A main list that did not come from this calculation's own cycles (an upload,
+// a restore, a restart) need not hold the deterministic states, which HANDE
+// keeps in psip_list at all times: the space is dropped and built again at the
+// next iteration from the new list, as a restarted calculation does --
+// semi_stoch_iter = max(start_iter, mc_cycles_done + 1), or mc_cycles_done + 1
+// when every shift already varies and shift_start_iteration is set
+// (src/fciqmc.f90:229-235).
+static void ss_reschedule(hgpu_handle *h) {
+    if (h->cfg.semi_stoch_space == 0) return;
+    bool all_vary = true;
+    for (int s = 0; s < h->R; s++) all_vary = all_vary && h->vary_shift[s];
+    h->ss_iter = std::max<int64_t>(h->cfg.semi_stoch_start_iter, h->iter + 1);
+    if (all_vary && h->cfg.semi_stoch_shift_iter != -1) h->ss_iter = h->iter + 1;
+    if (h->b.nd > 0 || h->b.ddets) {
+        ss_drop(h);
+        invalidate_graphs(h);
+    }
+}
+
 static int read_state(hgpu_handle *h, DevState *st) {
     CK(cudaMemcpyAsync(st, h->b.state, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -846,6 +897,7 @@ static int set_list(hgpu_handle *h, const int64_t *states, const int64_t *pops, 
                     bool compute_kii) {
     if (n < 0 || n > h->b.cap) return HGPU_ERR_INVALID;
     int W = h->W, R = h->R;
+    ss_reschedule(h);
     h->cur = 0;
     if (n > 0) {
         CK(cudaMemcpyAsync(h->b.dets[0], states, sizeof(uint64_t) * W * n, cudaMemcpyHostToDevice, h->stream));
@@ -954,7 +1006,9 @@ static int ss_init(hgpu_handle *h) {
     };
     std::vector<uint64_t> dd;
     int64_t K = 0;
-    h->b.nd = 0;
+    // a space built before (a rebuild after a restart) is freed first
+    ss_drop(h);
+    invalidate_graphs(h);
     if (h->cfg.semi_stoch_space == 4) {
         // create_ci_determ_space (src/semi_stoch.F90:1763-1805): every
         // determinant of the reference's spin and symmetry within ci_level
@@ -1049,6 +1103,7 @@ static int ss_init(hgpu_handle *h) {
     std::vector<int64_t> cnt(K), ptr(K + 1);
     CK(cudaMemcpyAsync(cnt.data(), counts, sizeof(int64_t) * K, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    dfree(h, counts);
     ptr[0] = 0;
     for (int64_t k = 0; k < K; k++) ptr[k + 1] = ptr[k] + cnt[k];
     int64_t *dptr;
@@ -1068,6 +1123,7 @@ static int ss_init(hgpu_handle *h) {
     h->b.dcol_h = ch;
     h->b.dvec = dvec;
     h->b.dind = dind;
+    h->ss_gen++;
     // absent determinants join the main list with zero population
     std::vector<uint64_t> nd_;
     std::vector<int64_t> np_;
@@ -1372,6 +1428,9 @@ int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
     out->error_flags = st.error_flags;
     out->device_ms = h->report_ms;
     h->report_ms = 0.0;
+    out->nblooms = st.bloom_n;
+    out->tot_bloom = (double)st.bloom_tot / (double)h->hsys.real_factor;
+    out->max_bloom = (double)st.bloom_max / (double)h->hsys.real_factor;
     // reset the report accumulators, publish the new shift
     for (int s = 0; s < HGPU_MAX_SPACES; s++) {
         st.shift[s] = h->shift[s];
@@ -1380,6 +1439,7 @@ int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
     st.acc_rspawn = 0.0;
     st.acc_attempts = st.acc_spawned = 0;
     st.rep_cycles = 0;
+    st.bloom_n = st.bloom_tot = 0;  // bloom_stats_init_report_loop
     if ((rc = write_state(h, &st))) return rc;
     if (out->error_flags & HGPU_FLAG_SPAWN_OVERFLOW) return HGPU_ERR_SPAWN_OVERFLOW;
     if (out->error_flags & HGPU_FLAG_MAIN_OVERFLOW) return HGPU_ERR_MAIN_OVERFLOW;
@@ -1428,14 +1488,7 @@ int32_t hgpu_set_state(hgpu_handle *h, const hgpu_state *in) {
     // semi_stoch_iter = max(start_iter, mc_cycles_done + 1), or mc_cycles_done + 1
     // when every shift already varies and shift_start_iteration is set
     // (src/fciqmc.f90:229-235)
-    if (h->cfg.semi_stoch_space != 0) {
-        bool all_vary = true;
-        for (int s = 0; s < h->R; s++) all_vary = all_vary && h->vary_shift[s];
-        h->ss_iter = std::max<int64_t>(h->cfg.semi_stoch_start_iter, h->iter + 1);
-        if (all_vary && h->cfg.semi_stoch_shift_iter != -1) h->ss_iter = h->iter + 1;
-        h->b.nd = 0;
-        invalidate_graphs(h);
-    }
+    ss_reschedule(h);
     return write_state(h, &st);
 }
 
@@ -1580,9 +1633,13 @@ int32_t hgpu_snapshot(hgpu_handle *h, int32_t restore) {
         CK(cudaStreamSynchronize(h->stream));
         h->snap_n = n;
         for (int s = 0; s < HGPU_MAX_SPACES; s++) h->snap_abs[s] = st.abs_pop[s];
+        h->snap_ss_gen = h->ss_gen;
         return HGPU_OK;
     }
     if (!h->snap_dets) return HGPU_ERR_INVALID;
+    // a list saved under another deterministic space (or none) does not hold
+    // the current space's states: the space is built again from it
+    if (h->snap_ss_gen != h->ss_gen) ss_reschedule(h);
     int64_t n = h->snap_n;
     CK(cudaMemcpyAsync(h->b.dets[h->cur], h->snap_dets, sizeof(uint64_t) * W * n, cudaMemcpyDeviceToDevice,
                        h->stream));

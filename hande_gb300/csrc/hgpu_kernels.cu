@@ -167,14 +167,16 @@ __global__ void __launch_bounds__(kBlock) k_prep_parents(DevBuffers b, int R, in
             const int64_t q = lower_bound_det<W>(b.ddets, b.nd, f);
             if (q < b.nd && det_eq<W>(load_det<W>(b.ddets, q), f)) dk = q;
         }
+        double rpv[2] = {0.0, 0.0};
         for (int sp = 0; sp < R; sp++) {
             int64_t p = pops[i * R + sp];
             double rp = (double)p * inv_rf;
+            rpv[sp] = rp;
             // update_proj_energy
             if (e.nexcit == 0) d0[sp] += rp;
             else proj[sp] += h * rp;
             // set_parent_flag: bit set if not an initiator
-            if (!(fabs(rp) > s.initiator_pop) && dk < 0) info |= 4u << sp;
+            if (!s.quadrature_initiator && !(fabs(rp) > s.initiator_pop) && dk < 0) info |= 4u << sp;
             if (p < 0) info |= 1u << sp;
             RStream rs;
             rs.init(s.seed, P_NATTEMPT, sp, i, 0, iter);
@@ -187,6 +189,11 @@ __global__ void __launch_bounds__(kBlock) k_prep_parents(DevBuffers b, int R, in
                 b.dvec[dk * R + sp] = rp;
             }
         }
+        // set_parent_flag with quadrature_initiator and two spaces
+        // (src/ifciqmc.f90:36-45): one test of N_1^2 + N_2^2 for both
+        if (s.quadrature_initiator && !(rpv[0] * rpv[0] + rpv[1] * rpv[1] > s.initiator_pop * s.initiator_pop) &&
+            dk < 0)
+            info |= 12u;
         if (dk >= 0) {
             info |= kDetermBit;
             b.dind[dk] = i;

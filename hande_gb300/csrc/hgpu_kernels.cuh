@@ -37,6 +37,9 @@ constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortItems = 8;    // keys per thread per radix tile
 constexpr int kMaxBlocks = 1024; // upper bound of the fixed grid (partials arrays)
 constexpr int kAnnTile = 2048;   // merged elements per annihilation tile (hgpu_annihilate.cuh)
+// Bloom threshold of FCIQMC in particles: init_bloom_stats_t's default with
+// bloom_mode_fixedn (src/fciqmc.f90:214, src/bloom_handler.F90:37).
+constexpr int64_t kBloomThreshold = 3;
 
 // Per-cycle counters and per-report accumulators, resident in device memory so
 // that a whole cycle runs without host synchronisation (and can be replayed
@@ -69,6 +72,11 @@ struct DevState {
     int32_t pad4;
     int64_t n_rdm;           // RDM spawns of the cycle
     double rdm_energy, rdm_trace;  // calc_rdm_energy of the report
+    // bloom_stats_t (src/bloom_handler.F90:26-71): spawning events of at least
+    // kBloomThreshold particles -- their number and summed |amount| (encoded)
+    // in the report, the largest |amount| of the calculation
+    int64_t bloom_n, bloom_tot;
+    uint64_t bloom_max;
 };
 
 // Device buffers of one engine (all allocated once, at create).

@@ -14,10 +14,12 @@
 // holds it until the process exits, whether or not this entry point is called.
 // Host code must not use the array's name as an address (on the host it names
 // a host-side placeholder); the device address is obtained once per device with
-// cudaGetSymbolAddress, on the first call made with that device current.  All
-// calls share the one array: two calls whose work overlaps on the GPU (for
-// example on two streams) race and corrupt each other's results, so callers
-// must order them.
+// cudaGetSymbolAddress, on the first call made with that device current, and
+// kept for the life of the process: after a cudaDeviceReset (which destroys the
+// primary context and with it the module's memory) the kept address is stale,
+// so a reset between calls is not supported.  All calls share the one array:
+// two calls whose work overlaps on the GPU (for example on two streams) race
+// and corrupt each other's results, so callers must order them.
 //
 // The operation is HANDE's annihilate_spawn_t (src/spawn_data.F90:859-935)
 // after the qsort of annihilate_wrapper_spawn_t_single (:406): sort the entries

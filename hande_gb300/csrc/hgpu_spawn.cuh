@@ -228,6 +228,24 @@ __global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) 
                             atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
                         }
                     }
+                    // accumulate_bloom_stats (src/bloom_handler.F90:104-145): an event of
+                    // at least kBloomThreshold particles is a bloom; counted per warp
+                    const int64_t amag = nspawn < 0 ? -nspawn : nspawn;
+                    const bool bloom = want && amag >= kBloomThreshold * s.real_factor;
+                    const uint32_t bball = __ballot_sync(FULL_MASK, bloom);
+                    if (bball) {
+                        long long bsum = bloom ? amag : 0, bmax = bsum;
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) {
+                            bsum += __shfl_xor_sync(FULL_MASK, bsum, o);
+                            bmax = max(bmax, __shfl_xor_sync(FULL_MASK, bmax, o));
+                        }
+                        if (lane == __ffs(bball) - 1) {
+                            atomicAdd((unsigned long long *)&st->bloom_n, (unsigned long long)__popc(bball));
+                            atomicAdd((unsigned long long *)&st->bloom_tot, (unsigned long long)bsum);
+                            atomicMax((unsigned long long *)&st->bloom_max, (unsigned long long)bmax);
+                        }
+                    }
                 }
                 if (rdm) {
                     // create_spawned_particle_replica_rdm: (parent, child) and the amount

@@ -133,7 +133,10 @@ typedef struct hgpu_config {
     int32_t nspaces;               /* 1, or 2 for replica_tricks */
     int32_t ncycles;               /* mc_cycles per report */
     int32_t precision;             /* HGPU_PREC_* */
-    int32_t reserved0;
+    int32_t quadrature_initiator;  /* fciqmc_in%quadrature_initiator (HANDE's default: 1): with two
+                                      spaces the pair (N_1, N_2) of a determinant is an initiator in
+                                      both iff N_1^2 + N_2^2 > initiator_pop^2 (set_parent_flag,
+                                      src/ifciqmc.f90:14-57); 0: each space on its own */
     int64_t seed;                  /* rng_seed */
     int64_t walker_length;         /* main-list capacity; < 0 means MB (state_size) */
     int64_t spawned_walker_length; /* spawned-list capacity; < 0 means MB */
@@ -184,6 +187,12 @@ typedef struct hgpu_report {
     double device_ms;                        /* device time of the report's cycles */
     double rdm_energy;                       /* RDM energy numerator of the report (calc_rdm_energy) */
     double rdm_trace;                        /* trace of the report's 2-RDM */
+    /* bloom_stats_t (src/bloom_handler.F90:26-71, accumulate_bloom_stats :104):
+     * spawning events that created at least 3 particles (the fixed-n threshold of
+     * FCIQMC, src/fciqmc.f90:214) */
+    int64_t nblooms;                         /* nblooms_curr: blooms in the report */
+    double tot_bloom;                        /* tot_bloom_curr: particles created by them */
+    double max_bloom;                        /* max_bloom: largest bloom of the calculation so far */
 } hgpu_report;
 
 typedef struct hgpu_handle hgpu_handle;
@@ -296,8 +305,10 @@ int32_t hgpu_snapshot(hgpu_handle *h, int32_t restore);
  * library.  For callers that cannot let a library allocate device memory: a
  * host program whose pool allocator owns all device memory, or a caller that
  * must not allocate on its critical path (cudaMalloc/cudaFree can synchronise
- * the device).  No counterpart in the reference: it is an allocation-free form
- * of annihilate_spawn_t after its qsort (src/spawn_data.F90:406, :859-935).
+ * the device).  No counterpart in the reference.  The operation: sort the
+ * entries by determinant (unsigned, last word most significant), add the
+ * populations of equal determinants, drop the determinants whose populations
+ * all cancel.
  *
  * d_sdata: device array (nwords + nspaces + 1, n) column-major, as for
  * hgpu_annihilate_fixed (the flag word is ignored); d_out: device array with
@@ -311,9 +322,11 @@ int32_t hgpu_snapshot(hgpu_handle *h, int32_t restore);
  * HGPU_ERR_INVALID and *n_out = -HGPU_NOALLOC_MAX_ENTRIES.  The working space
  * is one fixed array (about 5 MB) inside the library, held on every GPU that
  * loads the library until the process exits.  The first call on a device looks
- * up that array's device address, so make it with that device current.  Every
- * call uses the same array: calls that overlap on the GPU (e.g. on two streams
- * or from two host threads) race; order them. */
+ * up that array's device address, so make it with that device current; the
+ * address is kept for the life of the process, so a cudaDeviceReset between
+ * calls (which destroys the context the address belongs to) is not supported.
+ * Every call uses the same array: calls that overlap on the GPU (e.g. on two
+ * streams or from two host threads) race; order them. */
 #define HGPU_NOALLOC_MAX_ENTRIES 65536
 int32_t hgpu_self_annihilate_noalloc(const int64_t *d_sdata, int64_t n, int32_t nwords, int32_t nspaces,
                                      int64_t *d_out, int64_t *n_out, void *stream);

@@ -146,6 +146,9 @@ struct oracle_ctx {
     int64_t last_nspawn_events, rep_attempts, rep_spawned, total_attempts;
     int rep_cycles;
     int error_flags;
+    /* bloom_stats_t (src/bloom_handler.F90:26-71): blooms of the report, their
+     * summed |amount| (encoded), the largest |amount| of the calculation */
+    int64_t bloom_n, bloom_tot, bloom_max;
     /* spawned list: W det words, R pops, flag, generation order */
     int64_t sn, scap;
     uint64_t *sdets;
@@ -1888,9 +1891,18 @@ static int64_t stochastic_death(const oracle_ctx *c, rstream *rs, double Kii, do
     return kill < 0 ? -kill : kill;
 }
 
-/* set_parent_flag (src/ifciqmc.f90:14-57): bit s set if NOT an initiator in space s. */
+/* set_parent_flag (src/ifciqmc.f90:14-57): bit s set if NOT an initiator in
+ * space s.  With quadrature_initiator (HANDE's default) and an even number of
+ * spaces, each pair of spaces is tested together on N_1^2 + N_2^2. */
 static int64_t parent_flag(const oracle_ctx *c, const double *real_pop) {
     int64_t flag = 0;
+    if (c->cfg.quadrature_initiator && c->R % 2 == 0) {
+        for (int s = 0; s < c->R; s += 2) {
+            const double magnitude = real_pop[s] * real_pop[s] + real_pop[s + 1] * real_pop[s + 1];
+            if (!(magnitude > c->cfg.initiator_pop * c->cfg.initiator_pop)) flag |= (int64_t)3 << s;
+        }
+        return flag;
+    }
     for (int s = 0; s < c->R; s++)
         if (!(fabs(real_pop[s]) > c->cfg.initiator_pop)) flag |= (int64_t)1 << s;
     return flag;
@@ -2662,6 +2674,18 @@ static void ss_project(oracle_ctx *c) {
     }
 }
 
+/* accumulate_bloom_stats (src/bloom_handler.F90:104-145) with FCIQMC's fixed-n
+ * threshold of 3 particles (init_bloom_stats_t, src/fciqmc.f90:214): the
+ * report's count and particle sum, the calculation's largest bloom.  The sum is
+ * kept exactly in encoded units (HANDE adds each real(nspawn)/factor in FP64). */
+static void accumulate_bloom_stats(oracle_ctx *c, int64_t nspawn) {
+    const int64_t a = nspawn < 0 ? -nspawn : nspawn;
+    if (a < 3 * c->real_factor) return;
+    c->bloom_n++;
+    c->bloom_tot += a;
+    if (a > c->bloom_max) c->bloom_max = a;
+}
+
 static void mc_cycle(oracle_ctx *c) {
     c->iter++;
     if (c->cfg.semi_stoch_space != 0 && c->iter == c->ss_iter) ss_init(c);
@@ -2702,8 +2726,10 @@ static void mc_cycle(oracle_ctx *c) {
                 if (at.nspawn != 0) {
                     excited_det(c, f, &at.e, child);
                     /* no spawning between deterministic states (src/fciqmc.f90:777-790) */
-                    if (dk < 0 || ss_find(c, child) < 0)
+                    if (dk < 0 || ss_find(c, child) < 0) {
                         add_spawn(c, child, s, at.nspawn, c->cfg.initiator_approx ? flag : 0, c->sn);
+                        accumulate_bloom_stats(c, at.nspawn);
+                    }
                 }
                 if (at.nspawn_rdm != 0) {
                     excited_det(c, f, &at.e, child);
@@ -2916,8 +2942,21 @@ int oracle_initial_distribution(oracle_ctx *c) {
     return 0;
 }
 
+/* A list that did not come from the calculation's own cycles need not hold the
+ * deterministic states: the space is dropped and built again at the next
+ * iteration, as a restarted calculation does (src/fciqmc.f90:229-235). */
+static void ss_reschedule(oracle_ctx *c) {
+    if (c->cfg.semi_stoch_space == 0) return;
+    int all_vary = 1;
+    for (int s = 0; s < c->R; s++) all_vary = all_vary && c->vary_shift[s];
+    c->ss_iter = c->cfg.semi_stoch_start_iter > c->iter + 1 ? c->cfg.semi_stoch_start_iter : c->iter + 1;
+    if (all_vary && c->cfg.semi_stoch_shift_iter != -1) c->ss_iter = c->iter + 1;
+    ss_free(c);
+}
+
 int oracle_set_walkers(oracle_ctx *c, const int64_t *states, const int64_t *pops, const double *dat, int64_t n) {
     if (n > c->cap) return HGPU_ERR_INVALID;
+    ss_reschedule(c);
     c->n = n;
     memcpy(c->dets, states, sizeof(uint64_t) * c->nw * n);
     memcpy(c->pops, pops, sizeof(int64_t) * c->R * n);
@@ -3000,6 +3039,10 @@ int oracle_end_report(oracle_ctx *c, hgpu_report *out) {
     out->nattempts = c->rep_attempts;
     out->nspawned = c->rep_spawned;
     out->error_flags = c->error_flags;
+    out->nblooms = c->bloom_n;
+    out->tot_bloom = (double)c->bloom_tot / (double)c->real_factor;
+    out->max_bloom = (double)c->bloom_max / (double)c->real_factor;
+    c->bloom_n = c->bloom_tot = 0; /* bloom_stats_init_report_loop */
     for (int s = 0; s < 2; s++) { c->acc_proj[s] = 0.0; c->acc_d0[s] = 0.0; }
     c->acc_rspawn = 0.0;
     c->rep_attempts = 0;
@@ -3028,6 +3071,7 @@ int oracle_set_state(oracle_ctx *c, const hgpu_state *in) {
         c->vary_shift[s] = in->vary_shift[s];
         c->nparticles_old[s] = in->nparticles_old[s];
     }
+    ss_reschedule(c);
     return 0;
 }
 

@@ -120,3 +120,53 @@ def test_restart_rebuilds_space(tmp_path):
     assert r.error_flags == 0
     sg, pg, _ = h.walkers()
     assert sg.shape[0] >= 200
+
+
+@pytest.mark.parametrize("via", ["upload", "snapshot"])
+def test_new_list_after_build_rebuilds_space(via):
+    """A list that lacks some deterministic states, put in place after the space
+    was built (an upload, or the restore of a snapshot taken before the build),
+    does not inherit the old space: the space is dropped and built again from
+    the new list at the next iteration, bit-exactly as the oracle does."""
+    s = SYS["mol26"]
+    cfg = make_config(s, ncycles=10, seed=37, tau=1e-4, init_pop=2000, target_population=20000,
+                      real_amplitudes=True, semi_stoch_space=1, semi_stoch_size=200, semi_stoch_start_iter=5,
+                      state_size=1500000, spawned_state_size=1500000)
+    o = Oracle(s, cfg)
+    g = engine(s, cfg)
+    o.initial_distribution()
+    g.initial_distribution()
+    if via == "snapshot":
+        o.run_cycles(2)
+        g.run_cycles(2)
+        g.snapshot()
+        saved = o.walkers()
+    o.run_report()
+    g.run_report()  # the space was built at iteration 5
+    space = o.determ_space()
+    assert space.shape[0] == 200
+    if via == "upload":
+        st, po, da = o.walkers()
+        # drop every other deterministic state from the list
+        drop = {tuple(x) for x in space[::2].tolist()}
+        keep = np.array([tuple(x) not in drop for x in st.tolist()])
+        st, po, da = st[keep], po[keep], da[keep]
+        o.set_walkers(st, po, da)
+        g.set_walkers(st, po, da)
+    else:
+        g.snapshot(restore=True)
+        o.set_walkers(*saved)
+        o.set_state(g.state())  # the snapshot keeps the report's N_w of the shift update
+    for r in range(2):
+        ro = o.run_report()
+        rg = g.run_report()
+        assert ro.error_flags == 0 and rg.error_flags == 0
+        so, po_, ko = o.walkers()
+        sg, pg, kg = g.walkers()
+        np.testing.assert_array_equal(sg, so, err_msg="report %d states" % r)
+        np.testing.assert_array_equal(pg, po_, err_msg="report %d pops" % r)
+        assert_close(kg, ko)
+        assert list(rg.shift) == list(ro.shift)
+    rebuilt = o.determ_space()
+    assert rebuilt.shape[0] == 200 and not np.array_equal(rebuilt, space)
+    o.close()

@@ -1,24 +1,37 @@
 """Benchmark: FCIQMC spawn attempts/s and iteration time on one GB300.
 
-Workload (one "step" = one FCIQMC Monte Carlo cycle): the synthetic molecular
-Hamiltonian with 26 spatial orbitals and 10 electrons (C1, ms=0), real
-amplitudes (2^-31 fixed point), spawn cutoff 0.01, uniform excitation
-generator with p_double = 0.9, tau = 1e-3, FP64, target population 1e7.  The
-population is grown from the reference determinant until the shift varies
-(untimed), then W warm-up and K timed cycles run on the device.
+Headline workload (one "step" = one FCIQMC Monte Carlo cycle): the large
+configuration -- the synthetic molecular Hamiltonian with 64 spatial orbitals
+(two-word determinants) and 20 electrons (C1, ms=0), initiator FCIQMC
+(threshold 3) with two replicas (quadrature initiator test) and the replica
+2-RDM accumulating, real amplitudes (2^-31 fixed point), spawn cutoff 0.01,
+uniform renorm generator with p_double 0.9, tau 2e-4, grown on the device to
+about 5e8 walkers over both replicas (~157 GB of HBM held).  Each timed step
+is one cycle (a report of one cycle) on that same walker list, restored device
+to device (untimed) before it; every replay draws fresh random numbers.
 
-  value      spawn attempts/s over the K timed cycles, device-timed with CUDA
-             events on the engine's stream (the main and spawned lists,
-             >= 200 MB each, exceed the 129 MB L2 between cycles)
-  e2e        the same metric through the C ABI with host-resident walker
-             lists: upload (pinned host -> device), one cycle, download
+  value      spawn attempts/s of the FP64 engine (the reference's precision)
+             over the K timed cycles, CUDA events on the engine's stream
+  e2e        the same through the C ABI with host-resident walker lists in
+             pinned memory: upload, one cycle, download per step
   roofline   HBM roofline of the dominant kernel (spawning) and of the
              annihilation phases (sort + self-annihilation + merge)
-  cpu_baseline  the CPU oracle (C restatement of HANDE's cycle) on a bounded
-             sample of the same workload
+  mixed_precision  the FP32 engine (FP32 H_ij, p_gen; FP64 K_ii, shift,
+             estimators) on the same workload and its E_proj against FP64
+  parity     one cycle of the GPU engine against the oracle from the same
+             list, state and iteration: a slice of the benchmark's own list at
+             the headline parameters, and the full config-2 list
+  cpu_baseline  the oracle (C restatement of HANDE's cycle), one core, on a
+             bounded slice of the same walker list
+  config2    the 26-orbital molecule of the previous headline (FP64, ~1e7
+             walkers): attempts/s, phases and rooflines
+  batched    128 Hubbard calculations advanced together
 
---impl reference times the CPU restatement of the reference algorithm on all
-host cores (the reference itself, Fortran + MPI + Lua, cannot be built here).
+--impl reference times the CPU restatement of the reference algorithm as HANDE
+runs it on many cores: one calculation hash-partitioned over all host cores
+(threads) with an all-to-all of the spawned walkers every cycle, on the same
+system and parameters at a bounded population (the reference itself, Fortran +
+MPI + Lua, cannot be built here).
 """
 
 from __future__ import annotations
@@ -143,32 +156,8 @@ def grow(eng, target, max_cycles=400, verbose=False):
     return rep
 
 
-def cpu_sample(seconds=15.0, target=2e5, seed=7):
-    """The oracle on a bounded sample of the same workload: grow to `target`
-    walkers, then time whole cycles for about `seconds` s."""
-    from oracle.pyoracle import Oracle
-    s, cfg = system_and_config(target=target, seed_rng=seed, cap_main=int(20 * target), cap_spawn=int(40 * target))
-    o = Oracle(s, cfg)
-    o.initial_distribution()
-    for _ in range(300):  # grow cycle by cycle up to the sample size
-        o.run_cycles(1)
-        if o.end_report().nparticles[0] >= target:
-            break
-    a0 = o.total_attempts()
-    t0 = time.perf_counter()
-    ncyc = 0
-    while time.perf_counter() - t0 < seconds:
-        o.run_cycles(1)
-        ncyc += 1
-    dt = time.perf_counter() - t0
-    att = o.total_attempts() - a0
-    rep = o.end_report()
-    return {"attempts": att, "seconds": dt, "cycles": ncyc, "walkers": rep.nparticles[0],
-            "states": rep.nstates}
-
-
 def cpu_sample_on_state(states, pops, dat, seconds=10.0, seed=7):
-    """The oracle timed on whole cycles of the engine's own walker list."""
+    """The oracle timed on whole cycles of the engine's own config-2 walker list."""
     from oracle.pyoracle import Oracle
     n = states.shape[0]
     s, cfg = system_and_config(target=1e7, seed_rng=seed, cap_main=int(3 * n) + 1000, cap_spawn=int(4 * n) + 1000)
@@ -185,36 +174,276 @@ def cpu_sample_on_state(states, pops, dat, seconds=10.0, seed=7):
             "states": n}
 
 
-def _cpu_worker(args):
-    seconds, target, seed = args
-    return cpu_sample(seconds, target, seed)
+def parity_cycle(s, cfg, st, po, da, state, sample):
+    """One cycle of the GPU engine and of the oracle from the same walker list,
+    state (iteration, shift, vary_shift) and hence the same random streams:
+    the resulting lists must be equal bit for bit."""
+    from hande_gb300.engine import Engine
+    from oracle.pyoracle import Oracle
+    g = Engine(s, cfg)
+    o = Oracle(s, cfg)
+    for x in (g, o):
+        x.set_walkers(st, po, da)
+        x.set_state(state)
+    t0 = time.perf_counter()
+    ro = o.run_report()
+    t_oracle = time.perf_counter() - t0
+    rg = g.run_report()
+    sg, pg, kg = g.walkers()
+    so, pq, ko = o.walkers()
+    g.close()
+    o.close()
+    same_shape = sg.shape == so.shape
+    out = {"sample": sample, "states_in": int(st.shape[0]), "states_out": int(so.shape[0]),
+           "states_equal": bool(same_shape and np.array_equal(sg, so)),
+           "pops_equal": bool(same_shape and np.array_equal(pg, pq)),
+           "kii_max_rel_err": float(np.max(np.abs(kg - ko) / np.maximum(np.abs(ko), 1e-300))) if same_shape and
+           ko.size else None,
+           "attempts_equal": rg.nattempts == ro.nattempts, "spawned_equal": rg.nspawned == ro.nspawned,
+           "blooms_equal": (rg.nblooms, rg.tot_bloom) == (ro.nblooms, ro.tot_bloom),
+           "attempts": int(ro.nattempts), "oracle_seconds": t_oracle}
+    if ro.rdm_trace:
+        out["rdm_energy_rel_err"] = abs(rg.rdm_energy - ro.rdm_energy) / abs(ro.rdm_energy)
+    return out
+
+
+LARGE_WORKLOAD = ("config5: synthetic molecule M=64 nel=20 ms=0 C1 (two-word determinants, 75-bit rank keys), "
+                  "initiator FCIQMC (threshold 3) with 2 replicas (quadrature initiator) and the replica 2-RDM, real "
+                  "amplitudes, spawn cutoff 0.01, uniform renorm generator (p_double 0.9), tau 2e-4, grown on the "
+                  "device to ~5e8 walkers over both replicas; each step = one cycle on that same walker list")
+
+
+def large_system():
+    from hande_gb300 import systems
+    return systems.synthetic_molecule(64, 20, seed=2024)
+
+
+def large_config(s, precision, main_cap, spawn_cap, init_pop=1e6, seed=5):
+    """The large configuration; the shift is held (target 1e300) while the
+    population grows."""
+    from hande_gb300._abi import make_config
+    return make_config(s, tau=2e-4, init_pop=init_pop, target_population=1e300, ncycles=1, seed=seed,
+                       real_amplitudes=True, spawn_cutoff=0.01, excit_gen="renorm", pattempt_single=0.1,
+                       pattempt_double=0.9, initiator=True, initiator_threshold=3.0, nspaces=2,
+                       precision=precision, density_matrices=True, density_matrix_report=0,
+                       state_size=main_cap, spawned_state_size=spawn_cap)
+
+
+def grow_replicas(e, target_total, max_grow=60, label="grow"):
+    """Report by report (one cycle each) until both replicas together hold
+    about target_total walkers: stop at 0.9 of it, or before a cycle that would
+    overshoot it by 20 %."""
+    last = None
+    for r in range(max_grow):
+        rep = e.run_report()
+        tot = rep.nparticles[0] + rep.nparticles[1]
+        if os.environ.get("HGPU_BENCH_VERBOSE"):
+            sys.stderr.write("%s %d Nw=%.4g+%.4g states=%d flags=%d\n" % (
+                label, r, rep.nparticles[0], rep.nparticles[1], rep.nstates, rep.error_flags))
+        if rep.error_flags:
+            raise RuntimeError("walker list overflow while growing (flags %d)" % rep.error_flags)
+        g = tot / last if last else 1.0
+        if tot >= 0.9 * target_total or tot * g > 1.2 * target_total:
+            return rep, r + 1
+        last = tot
+    return rep, max_grow
+
+
+def hold_and_save(e):
+    """Every shift varying (so the replica RDM accumulates, as after
+    equilibration), the walker list saved on the device as the step input."""
+    st = e.get_state()
+    st.vary_shift[0] = st.vary_shift[1] = 1
+    e.set_state(st)
+    e.snapshot()
+
+
+def replay_steps(e, steps, warmup, clocks=None, barrier=None):
+    """W untimed and K timed steps, each one report of one cycle started from
+    the saved list (restored device to device, untimed)."""
+    R = e.cfg.nspaces
+    for _ in range(warmup):
+        e.snapshot(restore=True)
+        e.run_report()
+    if barrier:
+        barrier()
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    dev_ms, att, flags = 0.0, 0, 0
+    eproj, rdm = [], []
+    for _ in range(steps):
+        e.snapshot(restore=True)
+        r = e.run_report()  # CUDA events on the engine stream around the cycle; synchronises
+        dev_ms += r.device_ms
+        att += r.nattempts
+        flags |= r.error_flags
+        eproj.append([r.proj_energy[q] / r.D0_population[q] if r.D0_population[q] else float("nan")
+                      for q in range(R)])
+        if r.rdm_trace:
+            rdm.append(r.rdm_energy / r.rdm_trace)
+    clk = clocks.stop() if clocks else None
+    if flags:
+        raise RuntimeError("walker list overflow during the timed cycles (flags %d)" % flags)
+    return {"dev_ms": dev_ms, "attempts": att, "eproj": np.array(eproj), "rdm": rdm, "clocks": clk}
+
+
+def e2e_measure(e, W, R, steps, main_cap):
+    """The metric through the C ABI with host-resident walker lists: per step,
+    hgpu_upload_walkers from pinned host memory, one cycle, hgpu_end_report and
+    hgpu_download_walkers into pinned host memory."""
+    from hande_gb300.engine import _p
+    rt = cudart()
+    e.snapshot(restore=True)
+    st, po, da = e.walkers()
+    n0 = st.shape[0]
+    bufs = []
+    hst, p1 = pinned_array(rt, (n0, W), np.int64)
+    hpo, p2 = pinned_array(rt, (n0, R), np.int64)
+    hda, p3 = pinned_array(rt, (n0,), np.float64)
+    ost, p4 = pinned_array(rt, (main_cap, W), np.int64)
+    opo, p5 = pinned_array(rt, (main_cap, R), np.int64)
+    oda, p6 = pinned_array(rt, (main_cap,), np.float64)
+    bufs = [p1, p2, p3, p4, p5, p6]
+    hst[:] = st
+    hpo[:] = po
+    hda[:] = da
+    del st, po, da
+    L = e.L
+    h2d = d2h = att = 0
+    t_up = t_cyc = t_down = 0.0
+    rep_ms = 0.0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ta = time.perf_counter()
+        e._check(L.hgpu_upload_walkers(e.h, _p(hst, C.c_int64), _p(hpo, C.c_int64), _p(hda, C.c_double), n0),
+                 "upload")
+        h2d += n0 * (8 * W + 8 * R + 8)
+        tb = time.perf_counter()
+        r = e.run_report()
+        att += r.nattempts
+        rep_ms += r.device_ms
+        tc = time.perf_counter()
+        m = C.c_int64()
+        e._check(L.hgpu_download_walkers(e.h, _p(ost, C.c_int64), _p(opo, C.c_int64), _p(oda, C.c_double),
+                                         main_cap, C.byref(m)), "download")
+        d2h += m.value * (8 * W + 8 * R + 8)
+        t_up += tb - ta
+        t_cyc += tc - tb
+        t_down += time.perf_counter() - tc
+    e2e_s = time.perf_counter() - t0
+    del hst, hpo, hda, ost, opo, oda
+    for p in bufs:
+        if p is not None and rt is not None:
+            rt.cudaFreeHost(p)
+    return {"value": att / e2e_s, "unit": "attempts/s", "h2d_bytes_per_step": h2d // steps,
+            "d2h_bytes_per_step": d2h // steps,
+            "note": "per step: hgpu_upload_walkers from pinned host memory, one cycle (hgpu_run_report), "
+                    "hgpu_download_walkers into pinned host memory; host wall clock",
+            "host_ms_per_step": {"upload": 1e3 * t_up / steps, "cycle": 1e3 * t_cyc / steps,
+                                 "download": 1e3 * t_down / steps},
+            "steps": steps}
+
+
+def cpu_slice(s, cfg, st, po, da, state, n, seconds):
+    """The oracle (one core) on whole cycles of a slice of the benchmark's own
+    walker list, with the benchmark's state (every shift varying, the RDM
+    accumulating)."""
+    from oracle.pyoracle import Oracle
+    i0 = max(0, (st.shape[0] - n) // 2)
+    sl = slice(i0, i0 + n)
+    c = type(cfg).from_buffer_copy(cfg)
+    c.walker_length = int(4 * n) + 1000
+    c.spawned_walker_length = int(20 * n) + 1000
+    o = Oracle(s, c)
+    att = 0
+    dt = 0.0
+    ncyc = 0
+    while ncyc == 0 or dt < seconds:
+        o.set_walkers(st[sl], po[sl], da[sl])
+        o.set_state(state)
+        a0 = o.total_attempts()
+        t0 = time.perf_counter()
+        o.run_cycles(1)
+        dt += time.perf_counter() - t0
+        o.end_report()
+        att += o.total_attempts() - a0
+        ncyc += 1
+    o.close()
+    return {"value": att / dt, "unit": "attempts/s", "cores": 1, "kind": "port",
+            "sample": "CPU oracle, 1 core, %d whole cycle(s) of a %d-state slice of the benchmark's own list "
+                      "(%.3g attempts per cycle) in %.1f s" % (ncyc, n, att / ncyc, dt)}
+
+
+REF_TARGET = 4e6  # total walkers of the reference arm's calculation (both replicas)
 
 
 def reference_arm(args):
-    """CPU restatement of HANDE's FCIQMC cycle on every host core: one
-    independent calculation per core (HANDE runs one MPI rank per core)."""
-    import multiprocessing as mp
+    """The reference algorithm as HANDE runs it on many cores: the CPU
+    restatement of the cycle, one calculation hash-partitioned over every host
+    core (threads as ranks: owner = modulo(MurmurHash2(det), ranks), the
+    spawned walkers and RDM spawns exchanged every cycle, estimators summed per
+    report), on the headline system and parameters.  The population is bounded
+    (REF_TARGET walkers over both replicas, grown from the reference
+    determinant) so that the run ends in a few minutes; then, like the GPU
+    arm, every shift varies (the RDM accumulates), the list is saved, and each
+    of W warm-up and K timed steps is one cycle from that list (restored,
+    untimed)."""
+    from hande_gb300._abi import PREC_FP64
+    from oracle.pyoracle import OraclePar
     ncores = os.cpu_count() or 1
-    seconds = float(os.environ.get("HGPU_REF_SECONDS", "20"))
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(ncores) as pool:
-        res = pool.map(_cpu_worker, [(seconds, 2e5, 7 + k) for k in range(ncores)])
-    wall = time.perf_counter() - t0
-    att = sum(r["attempts"] for r in res)
-    rate = att / max(r["seconds"] for r in res)
-    ms_per_cycle = 1e3 * np.mean([r["seconds"] / max(r["cycles"], 1) for r in res])
+    target = float(os.environ.get("HGPU_REF_TARGET", REF_TARGET))
+    s = large_system()
+    cfg = large_config(s, PREC_FP64, main_cap=int(2 * target / ncores) + 100000,
+                       spawn_cap=int(3 * target / ncores) + 100000, init_pop=target / 500.0)
+    t_start = time.perf_counter()
+    o = OraclePar(s, cfg, ncores)
+    o.initial_distribution()
+    last = None
+    grown = 0
+    for r in range(80):
+        rep = o.run_report()
+        grown = r + 1
+        if rep.error_flags:
+            raise RuntimeError("reference arm: list overflow while growing (flags %d)" % rep.error_flags)
+        tot = rep.nparticles[0] + rep.nparticles[1]
+        g = tot / last if last else 1.0
+        if tot >= 0.9 * target or tot * g > 1.2 * target:
+            break
+        last = tot
+    st = o.state()
+    st.vary_shift[0] = st.vary_shift[1] = 1
+    o.set_state(st)
+    o.snapshot()
+    for _ in range(args.warmup):
+        o.snapshot(restore=True)
+        o.run_report()
+    secs, att = [], 0
+    for _ in range(args.steps):
+        o.snapshot(restore=True)
+        o.begin_report()
+        a0 = o.total_attempts()
+        t0 = time.perf_counter()
+        o.run_cycles(1)
+        secs.append(time.perf_counter() - t0)
+        att += o.total_attempts() - a0
+        o.end_report()
+    o.close()
+    rate = att / sum(secs)
+    sample = ("one calculation over %d host cores (threads as hash-partitioned ranks), grown to %.3g walkers "
+              "(%d states) in %d cycles; each step one cycle from that list" % (
+                  ncores, rep.nparticles[0] + rep.nparticles[1], rep.nstates, grown))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "attempts/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_cycle, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": "per core: grow to 2e5 walkers, time whole cycles %.0f s" % seconds,
-                   "parallelism": "one independent calculation per host core"},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": LARGE_WORKLOAD, "sample": sample,
+                   "parallelism": "one calculation hash-partitioned over all host cores"},
         "cpu_baseline": {"value": rate, "unit": "attempts/s", "cores": ncores, "kind": "port",
-                         "sample": "%d cores x %.0f s of cycles at ~2e5 walkers (CPU restatement of HANDE's cycle)"
-                                   % (ncores, seconds)},
+                         "sample": sample + " (CPU restatement of HANDE's cycle and MPI decomposition)"},
         "e2e": {"value": rate, "unit": "attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "wall_s": wall,
+        "attempts_per_step": att / args.steps,
+        "wall_s": time.perf_counter() - t_start,
     }
     print(json.dumps(line))
 
@@ -421,16 +650,10 @@ def hubbard_run(excit_gen="renorm", nreports=2000, seed=7):
             "E_proj": E, "E_proj_error": err, "shift": S, "shift_error": serr}
 
 
-LARGE_WORKLOAD = ("config5: synthetic molecule M=64 nel=20 ms=0 C1 (two-word determinants, 128-bit rank keys), "
-                  "initiator FCIQMC (threshold 3) with 2 replicas and the replica 2-RDM (variational energy), real "
-                  "amplitudes, spawn cutoff 0.01, uniform renorm generator (p_double 0.9), FP32 matrix elements and "
-                  "p_gen, FP64 estimators, grown on the device to ~5e8 walkers in total, shift from E_proj")
-
-
 def semi_stoch_run(size, steps=10, warmup=3, target=1e7):
     """The config-2 cycle with a semi-stochastic 'high' space of `size`
     determinants (src/semi_stoch.F90): the walker list is grown as for the
-    headline line, moved into a second calculation whose space is built at its
+    config-2 line, moved into a second calculation whose space is built at its
     first cycle from that list, then whole cycles are timed from a snapshot
     taken after the build.  Returns the per-cycle device time, the phase split
     and the one-time cost of building the space."""
@@ -477,83 +700,6 @@ def semi_stoch_run(size, steps=10, warmup=3, target=1e7):
             "note": "the projection kernel runs inside the spawn phase (after k_spawn)"}
 
 
-def large_replica_run(target_total=5e8, tau=2e-4, cycles=5, seed=2024, max_grow=60):
-    """config 5: one large replica calculation, measured like the headline
-    step -- grown on the device (shift held at 0) until the two replicas hold
-    about target_total walkers together; then the shifts are set varying (the
-    condition for accumulating the replica 2-RDM), the walker list is saved on
-    the device, and each of `cycles` reports of one cycle starts from it
-    (restored device to device, untimed) with the RDM accumulating:
-    attempts/s, time per cycle, memory held, E_proj and the RDM (variational)
-    energy of each cycle."""
-    from hande_gb300 import systems
-    from hande_gb300._abi import PREC_MIXED, make_config
-    from hande_gb300.engine import Engine
-    s = systems.synthetic_molecule(64, 20, seed=seed)
-    main_cap, spawn_cap = int(0.6 * target_total), int(1.6 * target_total)
-    cfg = make_config(s, tau=tau, init_pop=1e6, target_population=1e300, ncycles=1, seed=5,
-                      real_amplitudes=True, spawn_cutoff=0.01, excit_gen="renorm",
-                      pattempt_single=0.1, pattempt_double=0.9, initiator=True, initiator_threshold=3.0,
-                      nspaces=2, precision=PREC_MIXED, density_matrices=True, density_matrix_report=0,
-                      state_size=main_cap, spawned_state_size=spawn_cap)
-    free0 = device_free_bytes()
-    t0 = time.perf_counter()
-    e = Engine(s, cfg)
-    e.initial_distribution()
-    setup_s = time.perf_counter() - t0
-    flags = 0
-    grown = 0
-    last = None
-    for r in range(max_grow):
-        rep = e.run_report()
-        flags |= rep.error_flags
-        grown = r + 1
-        tot = rep.nparticles[0] + rep.nparticles[1]
-        sys.stderr.write("config5 grow %d Nw=%.4g+%.4g states=%d flags=%d\n" % (
-            r, rep.nparticles[0], rep.nparticles[1], rep.nstates, rep.error_flags))
-        # stop at the target, or before a cycle that would overshoot it by 20 %
-        g = tot / last if last else 1.0
-        if flags or tot >= 0.9 * target_total or tot * g > 1.2 * target_total:
-            break
-        last = tot
-    st = e.get_state()
-    st.vary_shift[0] = st.vary_shift[1] = 1
-    e.set_state(st)
-    e.snapshot()
-    held = None if free0 is None or device_free_bytes() is None else free0 - device_free_bytes()
-    att = 0
-    dev_ms = 0.0
-    rdm = []
-    walkers = None
-    for c in range(cycles):
-        e.snapshot(restore=True)
-        rep = e.run_report()
-        flags |= rep.error_flags
-        att += rep.nattempts
-        dev_ms += rep.device_ms
-        if rep.rdm_trace:
-            rdm.append(rep.rdm_energy / rep.rdm_trace)
-        sys.stderr.write("config5 cycle %d attempts=%d ms=%.1f flags=%d\n" % (
-            c, rep.nattempts, rep.device_ms, rep.error_flags))
-    # one more cycle from the same list with per-phase device times and list sizes
-    e.snapshot(restore=True)
-    phases, counts = e.profile_cycle()
-    out = {"workload": LARGE_WORKLOAD, "tau": tau, "main_capacity": main_cap, "spawn_capacity": spawn_cap,
-           "device_bytes_held": held, "setup_s": setup_s, "growth_cycles": grown, "cycles": cycles,
-           "error_flags": flags, "input_walkers_total": tot, "input_states": int(counts["N"]),
-           "phase_ms": phases, "cycle_counts": counts,
-           "attempts_per_cycle": att / cycles,
-           "value": att / (dev_ms * 1e-3) if dev_ms > 0 else None, "unit": "attempts/s",
-           "ms_per_cycle": dev_ms / cycles,
-           "E_proj": [rep.proj_energy[q] / rep.D0_population[q] for q in range(2)],
-           "rdm_energy_per_cycle": rdm,
-           "note": "each timed cycle starts from the same device-grown ~%.2g-walker list (saved and restored on "
-                   "the device, untimed) as one report whose RDM gives one replica (variational) energy; "
-                   "energies relative to the reference determinant's H_00" % tot}
-    e.close()
-    return out
-
-
 def device_free_bytes():
     rt = cudart()
     if rt is None:
@@ -564,31 +710,77 @@ def device_free_bytes():
     return int(free.value)
 
 
+def config2_measure(steps, warmup, rank=0, cpu_seconds=10.0, parity=True):
+    """The 26-orbital molecule (M = 26, 10 electrons, tau 1e-3, real amplitudes,
+    FP64, ~1e7 walkers): attempts/s and iteration time over K replayed cycles,
+    per-phase times, the rooflines, one cycle of the oracle on the same list
+    (bit-exact comparison) and the one-core oracle's rate on it."""
+    from hande_gb300.engine import Engine
+    from hande_gb300.measure import roofline_figures
+    s, cfg = system_and_config(target=1e7, seed_rng=7 + rank)
+    eng = Engine(s, cfg)
+    eng.initial_distribution()
+    grown = grow(eng, 1e7)
+    eng.snapshot()
+    r = replay_steps(eng, steps, warmup)
+    eng.snapshot(restore=True)
+    phases, counts = eng.profile_cycle()
+    roof, annih = roofline_figures(phases, counts, W=s.nwords, R=1, initiator=False, peaks=load_peaks())
+    out = {"workload": WORKLOAD, "value": r["attempts"] / (r["dev_ms"] * 1e-3), "unit": "attempts/s",
+           "ms_per_step": r["dev_ms"] / steps, "walkers": grown.nparticles[0], "states": int(grown.nstates),
+           "attempts_per_step": r["attempts"] / steps, "phase_ms": phases, "cycle_counts": counts,
+           "roofline": roof, "annihilation_roofline": annih}
+    if parity:
+        eng.snapshot(restore=True)
+        st, po, da = eng.walkers()
+        state = eng.get_state()
+        out["parity"] = parity_cycle(s, cfg, st, po, da, state,
+                                     "one cycle of the whole %d-state config-2 list" % st.shape[0])
+        c = cpu_sample_on_state(st, po, da, cpu_seconds)
+        out["cpu_baseline"] = {"value": c["attempts"] / c["seconds"], "unit": "attempts/s", "cores": 1,
+                               "kind": "port", "sample": "CPU oracle, 1 core, %d whole cycle(s) of the %.3g-walker "
+                                                         "list in %.1f s" % (c["cycles"], c["walkers"], c["seconds"])}
+    eng.close()
+    return out
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path)) if os.path.exists(path) else {}
+
+
+def eproj_stats(e):
+    """Mean and standard error over the replayed cycles of each replica's
+    one-cycle E_proj (the replays are independent draws from one list)."""
+    return [(float(np.mean(e[:, q])), float(np.std(e[:, q], ddof=1) / np.sqrt(e.shape[0])))
+            for q in range(e.shape[1])]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--target", type=float, default=1e7)
-    ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--large-total", type=float, default=5e8, help="walkers of both replicas in the headline list")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the oracle legs (parity and cpu_baseline)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (config 4) measurement")
-    ap.add_argument("--config", type=int, default=2,
-                    help="2: the headline line (default); 1: the Hubbard 4x4 run of config 1; 3: the "
-                         "mixed-precision study of config 3; 5: the large replica run of config 5 (one JSON line each)")
-    ap.add_argument("--large-total", type=float, default=5e8, help="config 5: total walkers of both replicas")
+    ap.add_argument("--no-extra", action="store_true", help="skip the FP32 run and the config-2 line")
+    ap.add_argument("--config", type=int, default=5,
+                    help="5: the headline line (default); 2: the config-2 measurement alone; 1: the Hubbard 4x4 "
+                         "run of config 1; 3: the mixed-precision study of config 3 (one JSON line each)")
     ap.add_argument("--semi-stoch", type=int, default=0,
                     help="time the config-2 cycle with a semi-stochastic 'high' space of this size (one JSON line)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         if rank == 0:
             reference_arm(args)
         return
-    args.warmup = max(args.warmup, 3)
     if args.config == 3:
         if rank == 0:
             print(json.dumps(precision_study()))
@@ -598,17 +790,16 @@ def main():
             print(json.dumps({"workload": HUBBARD_WORKLOAD, "renorm": hubbard_run("renorm"),
                               "no_renorm": hubbard_run("no_renorm")}))
         return
-    if args.config == 5:
+    if args.config == 2:
         if rank == 0:
-            print(json.dumps(large_replica_run(target_total=args.large_total, cycles=args.steps)))
+            print(json.dumps(config2_measure(args.steps, args.warmup, cpu_seconds=args.cpu_seconds,
+                                             parity=not args.no_cpu)))
         return
     if args.semi_stoch > 0:
         if rank == 0:
-            print(json.dumps(semi_stoch_run(args.semi_stoch, steps=args.steps, warmup=args.warmup,
-                                            target=args.target)))
+            print(json.dumps(semi_stoch_run(args.semi_stoch, steps=args.steps, warmup=args.warmup)))
         return
 
-    cpu = None
     dist = None
     if world > 1:
         import torch
@@ -617,126 +808,96 @@ def main():
         td.init_process_group("nccl")
         dist = td
 
+    from hande_gb300._abi import PREC_FP64, PREC_MIXED
     from hande_gb300.engine import Engine
-    s, cfg = system_and_config(target=args.target, seed_rng=7 + rank)
+    from hande_gb300.measure import roofline_figures
+    s = large_system()
+    main_cap, spawn_cap = int(0.6 * args.large_total), int(1.6 * args.large_total)
+    cfg = large_config(s, PREC_FP64, main_cap, spawn_cap, init_pop=args.large_total / 500.0, seed=5 + rank)
+    free0 = device_free_bytes()
+    t0 = time.perf_counter()
     eng = Engine(s, cfg)
     eng.initial_distribution()
-    grown = grow(eng, args.target, verbose=bool(os.environ.get("HGPU_BENCH_VERBOSE")))
-    # the step input: this walker list, restored (device to device, untimed)
-    # before every cycle
-    eng.snapshot()
-    for _ in range(args.warmup):
-        eng.snapshot(restore=True)
-        eng.run_cycles(1)
-    eng.end_report()
-
+    grown, ngrow = grow_replicas(eng, args.large_total, label="fp64")
+    grow_s = time.perf_counter() - t0
+    hold_and_save(eng)
+    held = None if free0 is None or device_free_bytes() is None else free0 - device_free_bytes()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    if dist:
-        dist.barrier()
-    clocks.start()
-    time.sleep(0.3)
-    dev_ms = 0.0
-    attempts = 0
-    flags = 0
-    for _ in range(args.steps):
-        eng.snapshot(restore=True)
-        eng.run_cycles(1)  # device-timed with events on the engine stream; synchronises
-        r1 = eng.end_report()
-        dev_ms += r1.device_ms
-        attempts += r1.nattempts
-        flags |= r1.error_flags
-    clk = clocks.stop()
-    rep = grown
-    if flags:
-        raise RuntimeError("walker list overflow during the timed cycles (flags %d)" % flags)
+    r64 = replay_steps(eng, args.steps, args.warmup, clocks=clocks, barrier=dist.barrier if dist else None)
+    dev_ms, attempts = r64["dev_ms"], float(r64["attempts"])
     if dist:
         import torch
-        t = torch.tensor([dev_ms, float(attempts)], dtype=torch.float64, device="cuda")
+        t = torch.tensor([dev_ms, attempts], dtype=torch.float64, device="cuda")
         mx = t.clone()
         dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
         dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
         dev_ms, attempts = float(mx[0]), float(t[1])
     value = attempts / (dev_ms * 1e-3)
-    ms_per_step = dev_ms / args.steps
 
-    # per-phase times of one cycle and the HBM roofline figures
+    # per-phase times of one cycle from the same list and the rooflines
     eng.snapshot(restore=True)
     phases, counts = eng.profile_cycle()
-    from hande_gb300.measure import roofline_figures
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    roof, annih = roofline_figures(phases, counts, W=s.nwords, R=1, initiator=False, peaks=peaks)
+    roof, annih = roofline_figures(phases, counts, W=s.nwords, R=2, initiator=True, peaks=load_peaks())
+    # end to end through the C ABI with host walker lists
+    e2e = e2e_measure(eng, s.nwords, 2, args.e2e_steps, main_cap)
+    parity = cpu = None
+    if rank == 0 and not args.no_cpu:
+        eng.snapshot(restore=True)
+        st, po, da = eng.walkers()
+        state = eng.get_state()
+        n = 50000
+        i0 = max(0, (st.shape[0] - n) // 2)
+        sl = slice(i0, i0 + n)
+        pc = type(cfg).from_buffer_copy(cfg)
+        pc.walker_length, pc.spawned_walker_length = 40 * n, 80 * n
+        parity = parity_cycle(s, pc, st[sl], po[sl], da[sl], state,
+                              "one cycle of a %d-state slice (from state %d) of the benchmark's own %d-state list, "
+                              "the benchmark's iteration, shift and parameters (FP64)" % (n, i0, st.shape[0]))
+        cpu = cpu_slice(s, cfg, st, po, da, state, 100000, args.cpu_seconds)
+        del st, po, da
+    eng.close()
 
-    # end to end through the C ABI with host-resident walker lists
-    rt = cudart()
-    eng.snapshot(restore=True)
-    st, po, da = eng.walkers()
-    n0 = st.shape[0]
-    cap = int(n0 * 4) + 1000
-    hst, _ = pinned_array(rt, (cap, s.nwords), np.int64)
-    hpo, _ = pinned_array(rt, (cap, 1), np.int64)
-    hda, _ = pinned_array(rt, (cap,), np.float64)
-    ost, _ = pinned_array(rt, (cap, s.nwords), np.int64)
-    opo, _ = pinned_array(rt, (cap, 1), np.int64)
-    oda, _ = pinned_array(rt, (cap,), np.float64)
-    hst[:n0] = st
-    hpo[:n0] = po
-    hda[:n0] = da
-    n = n0
-    from hande_gb300.engine import _p
-    L = eng.L
-    h2d = d2h = 0
-    e_att = 0
-    eng.end_report()
-    t_up = t_cyc = t_down = 0.0
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        n = n0  # every step starts from the same host walker list
-        ta = time.perf_counter()
-        eng._check(L.hgpu_upload_walkers(eng.h, _p(hst, C.c_int64), _p(hpo, C.c_int64), _p(hda, C.c_double), n),
-                   "upload")
-        h2d += n * (8 * s.nwords + 8 + 8)
-        tb = time.perf_counter()
-        eng.run_cycles(1)
-        tc = time.perf_counter()
-        m = C.c_int64()
-        eng._check(L.hgpu_download_walkers(eng.h, _p(ost, C.c_int64), _p(opo, C.c_int64), _p(oda, C.c_double),
-                                           cap, C.byref(m)), "download")
-        d2h += m.value * (8 * s.nwords + 8 + 8)
-        t_up += tb - ta
-        t_cyc += tc - tb
-        t_down += time.perf_counter() - tc
-    e2e_s = time.perf_counter() - t0
-    e_rep = eng.end_report()
-    e_att = e_rep.nattempts
-    e2e = {"value": e_att / e2e_s, "unit": "attempts/s", "h2d_bytes_per_step": h2d // args.e2e_steps,
-           "d2h_bytes_per_step": d2h // args.e2e_steps,
-           "note": "per step: hgpu_upload_walkers from pinned host memory, one cycle, hgpu_download_walkers",
-           "host_ms_per_step": {"upload": 1e3 * t_up / args.e2e_steps, "cycle": 1e3 * t_cyc / args.e2e_steps,
-                                "download": 1e3 * t_down / args.e2e_steps}}
-
+    extra = {}
+    if rank == 0 and not args.no_extra:
+        # the FP32 engine on the same workload and its E_proj against FP64
+        cfg32 = large_config(s, PREC_MIXED, main_cap, spawn_cap, init_pop=args.large_total / 500.0, seed=5)
+        e32 = Engine(s, cfg32)
+        e32.initial_distribution()
+        grown32, _ = grow_replicas(e32, args.large_total, label="fp32")
+        hold_and_save(e32)
+        r32 = replay_steps(e32, args.steps, args.warmup)
+        e32.close()
+        s64, s32 = eproj_stats(r64["eproj"]), eproj_stats(r32["eproj"])
+        extra["mixed_precision"] = {
+            "value": r32["attempts"] / (r32["dev_ms"] * 1e-3), "unit": "attempts/s",
+            "ms_per_step": r32["dev_ms"] / args.steps, "speedup_over_fp64": (r32["attempts"] / r32["dev_ms"]) / (
+                r64["attempts"] / r64["dev_ms"]),
+            "walkers": grown32.nparticles[0] + grown32.nparticles[1],
+            "E_proj_one_cycle": {"fp64": s64, "fp32": s32},
+            "dE_proj_over_sigma": [(s32[q][0] - s64[q][0]) / float(np.hypot(s32[q][1], s64[q][1])) for q in range(2)],
+            "rdm_energy_one_cycle": {"fp64": float(np.mean(r64["rdm"])) if r64["rdm"] else None,
+                                     "fp32": float(np.mean(r32["rdm"])) if r32["rdm"] else None},
+            "note": "FP32 H_ij and p_gen, FP64 K_ii, shift and estimators; each engine grown from the same seed to "
+                    "about the same population, then K one-cycle reports replayed from its own list: mean and "
+                    "standard error of the one-cycle E_proj of each replica (relative to H_00)"}
+        extra["config2"] = config2_measure(args.steps, args.warmup, cpu_seconds=args.cpu_seconds,
+                                           parity=not args.no_cpu)
     batched = None
     if rank == 0 and not args.no_batched:
-        eng.close()
         try:
             batched = batched_measure(args.steps)
-        except Exception as exc:  # reported in the line; the config-2 numbers stand
+        except Exception as exc:  # reported in the line; the headline numbers stand
             batched = {"workload": BATCH_WORKLOAD, "error": "%s: %s" % (type(exc).__name__, exc)}
-
-    if rank == 0 and not args.no_cpu:
-        # the oracle on whole cycles of the same (device-grown) walker list, 1 core
-        r = cpu_sample_on_state(st, po, da, args.cpu_seconds)
-        cpu = {"value": r["attempts"] / r["seconds"], "unit": "attempts/s", "cores": 1, "kind": "port",
-               "sample": "CPU oracle, 1 core, %d whole cycle(s) in %.1f s on the benchmark's own %.3g-walker list"
-                         % (r["cycles"], r["seconds"], r["walkers"])}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "attempts/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "walkers": rep.nparticles[0], "states": int(rep.nstates),
-                       "attempts_per_step": attempts / args.steps / world, "l2": "inputs larger than L2",
+            "config": {"workload": LARGE_WORKLOAD, "walkers": grown.nparticles[0] + grown.nparticles[1],
+                       "states": int(grown.nstates), "attempts_per_step": attempts / args.steps / world,
+                       "growth_cycles": ngrow, "growth_s": grow_s, "device_bytes_held": held,
+                       "main_capacity": main_cap, "spawn_capacity": spawn_cap, "l2": "inputs larger than L2",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": e2e,
             "gpu_launches": int(counts["launches_per_cycle"]) * args.steps,
@@ -744,10 +905,13 @@ def main():
             "annihilation_roofline": annih,
             "phase_ms": phases,
             "cycle_counts": counts,
-            "clocks": clk,
+            "clocks": r64["clocks"],
+            "E_proj_one_cycle": eproj_stats(r64["eproj"]),
+            "parity": parity,
             "cpu_baseline": cpu,
             "batched": batched,
         }
+        line.update(extra)
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

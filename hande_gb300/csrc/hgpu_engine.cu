@@ -1680,6 +1680,8 @@ int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int
         counts[4] = st.n_main;
         counts[5] = launches_per_cycle(h->b);
         counts[6] = h->b.sort_passes;
+        // bytes one radix pass reads (and writes) per spawned entry: key and index
+        counts[7] = (h->b.key32 ? 4 : 8 * h->b.key_words) + 4;
     }
     return HGPU_OK;
 }

@@ -205,10 +205,11 @@ class Engine:
     def profile_cycle(self):
         """One cycle with per-phase device times (ms) and list sizes."""
         ms = np.zeros(7)
-        cnt = np.zeros(7, dtype=np.int64)
+        cnt = np.zeros(8, dtype=np.int64)
         self._check(self.L.hgpu_profile_cycle(self.h, _p(ms, C.c_double), 7, _p(cnt, C.c_int64)),
                     "hgpu_profile_cycle")
-        keys = ["N", "attempts", "spawned", "unique", "N_after", "launches_per_cycle", "sort_passes"]
+        keys = ["N", "attempts", "spawned", "unique", "N_after", "launches_per_cycle", "sort_passes",
+                "sort_bytes_per_entry_pass"]
         return dict(zip(self.PHASES, ms.tolist())), dict(zip(keys, cnt.tolist()))
 
     def eval_diagonal(self, dets):

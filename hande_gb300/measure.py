@@ -8,26 +8,29 @@ src/spawn_data.F90:63-71, 8-byte words):
   annihilation   sort 2 S E_s, self-annihilation S E_s + S_u E_s,
                  merge N E_m + S_u E_s + N' E_m
 with N / N' the main-list sizes before / after, S spawned and S_u unique
-spawned entries."""
+spawned entries.
+
+Everything under "achieved", "frac", "algorithmic_bytes", "seconds" and
+"sort_bytes_moved" is computed from the run's own device times and list sizes.
+Figures that only a profiler measures (issue-slot and pipe utilisation, DRAM
+bytes of a launch) come from the Nsight Compute captures recorded in
+profiles/ncu_figures.json and are reported under "from_profile" with the
+capture's workload and build."""
 
 from __future__ import annotations
 
+import json
 import os
 
-# DRAM bytes (read + write) per spawning attempt of one k_spawn launch, measured
-# by Nsight Compute on the 26-orbital synthetic molecule at 3.05e6 attempts
-# (profiles/k_spawn_mol26.md: 18.87 MB read + 7.31 MB written); the traffic of a
-# launch grows in proportion to its attempts (parents read once, spawned entries
-# written once), so the bench scales it by the attempts of its own cycle.
-SPAWN_DRAM_BYTES_PER_ATTEMPT = (18.87e6 + 7.31e6) / 3.0548e6
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PROFILE_FIGURES = os.path.join(ROOT, "profiles", "ncu_figures.json")
 
-# What bounds k_spawn instead of HBM, from the same capture: issue slots and the
-# integer (ALU) pipe, in percent of peak over the kernel's active cycles.
-SPAWN_ISSUE_ACTIVE_PCT = 52.6
-SPAWN_ALU_PIPE_PCT = 49.3
-# Issue-slot utilisation of k_annihilate on the same workload
-# (profiles/k_annihilate_mol26.md).
-ANNIHILATE_ISSUE_ACTIVE_PCT = 45.7
+
+def profile_figures() -> dict:
+    try:
+        return json.load(open(PROFILE_FIGURES))
+    except (OSError, ValueError):
+        return {}
 
 
 def entry_bytes(W: int, R: int, initiator: bool):
@@ -41,26 +44,38 @@ def roofline_figures(phases: dict, counts: dict, W: int, R: int, initiator: bool
     peak_src = "measured" if peak else "fallback"
     if not peak:
         peak = 6800.0
+    prof = profile_figures()
     t_spawn = phases["spawn"] * 1e-3
     spawn_bytes = N * Em + S * Es
     ach = spawn_bytes / t_spawn / 1e9 if t_spawn > 0 else 0.0
-    traffic = None
-    if SPAWN_DRAM_BYTES_PER_ATTEMPT:
-        traffic = SPAWN_DRAM_BYTES_PER_ATTEMPT * A
     roof = {"kernel": "k_spawn", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-            "frac": ach / peak, "traffic": traffic, "peak_source": peak_src,
-            "algorithmic_bytes": spawn_bytes,
-            "ncu_issue_active_pct": SPAWN_ISSUE_ACTIVE_PCT, "ncu_alu_pipe_pct": SPAWN_ALU_PIPE_PCT,
-            "note": "spawning is bound by integer issue (Philox, bit manipulation, generator logic), not by HBM; "
-                    "the ncu_* figures (profiles/k_spawn_mol26.md) give the issue and ALU-pipe utilisation"}
+            "frac": ach / peak, "peak_source": peak_src, "algorithmic_bytes": spawn_bytes,
+            "seconds": t_spawn, "traffic": None,
+            "note": "spawning is bound by instruction issue (Philox, bit manipulation, generator logic), not by "
+                    "HBM; from_profile gives the issue and pipe utilisation of a captured launch"}
+    ps = prof.get("k_spawn")
+    if ps:
+        per_att = (ps["dram_bytes_read"] + ps["dram_bytes_write"]) / ps["attempts"]
+        roof["traffic"] = per_att * A
+        roof["traffic_source"] = ("DRAM bytes per attempt of the captured launch (%s) x this cycle's %d attempts"
+                                  % (ps["workload"], A))
+        roof["from_profile"] = dict(ps, source=os.path.relpath(PROFILE_FIGURES, ROOT))
+    t_sort = phases["sort"] * 1e-3
     t_ann = (phases["sort"] + phases["splits"] + phases["annihilate"]) * 1e-3
     ann_bytes = 3 * S * Es + 2 * U * Es + N * Em + N2 * Em
     ach2 = ann_bytes / t_ann / 1e9 if t_ann > 0 else 0.0
+    passes = counts.get("sort_passes", 0)
+    kb = counts.get("sort_bytes_per_entry_pass", 0)
+    sort_moved = 2 * passes * kb * S  # every pass reads and writes key and index of every entry
     annih = {"phases": ["sort", "splits", "annihilate"], "bound": "hbm", "achieved": ach2, "peak": peak,
              "unit": "GB/s", "frac": ach2 / peak, "algorithmic_bytes": ann_bytes, "seconds": t_ann,
              "peak_source": peak_src,
-             "ncu_k_annihilate_issue_active_pct": ANNIHILATE_ISSUE_ACTIVE_PCT,
-             "note": "the annihilation kernel moves its algorithmic bytes once (DRAM traffic 1.04x of them) and "
-                     "is bound by instructions (Philox rounding and exact K_ii of new determinants, the merge "
-                     "walk) and shared-memory latency; profiles/k_annihilate_mol26.md"}
+             "sort_seconds": t_sort, "sort_passes": passes, "sort_bytes_moved": sort_moved,
+             "sort_algorithmic_bytes": 2 * S * Es,
+             "sort_achieved_gbs": sort_moved / t_sort / 1e9 if t_sort > 0 else 0.0,
+             "note": "the one-pass annihilation kernel moves its algorithmic bytes once; sort_bytes_moved is what "
+                     "the radix passes read and write (passes x 2 x key-and-index bytes x S)"}
+    pa = prof.get("k_annihilate")
+    if pa:
+        annih["from_profile"] = dict(pa, source=os.path.relpath(PROFILE_FIGURES, ROOT))
     return roof, annih

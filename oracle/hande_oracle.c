@@ -11,9 +11,11 @@
  * Orbitals are 0-based (HANDE orbital k is p = k-1); the parity of every
  * difference and the outcome of every comparison is unchanged by the shift.
  */
+#define _POSIX_C_SOURCE 200809L /* pthread barriers of the hash-partitioned driver */
 #include "hande_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1946,7 +1948,7 @@ static void update_proj_energy(oracle_ctx *c, const uint64_t *f, const det_info 
 /* Annihilation                                                               */
 /* ------------------------------------------------------------------------- */
 
-static const oracle_ctx *g_sort_ctx;
+static _Thread_local const oracle_ctx *g_sort_ctx; /* per thread: the partitioned driver sorts on many */
 
 static int cmp_spawn(const void *x, const void *y) {
     const oracle_ctx *c = g_sort_ctx;
@@ -2348,7 +2350,7 @@ static void update_rdm(oracle_ctx *c, const uint64_t *f1, const uint64_t *f2, co
     }
 }
 
-static const oracle_ctx *g_rdm_ctx;
+static _Thread_local const oracle_ctx *g_rdm_ctx;
 
 static int cmp_rdm_spawn(const void *x, const void *y) {
     const oracle_ctx *c = g_rdm_ctx;
@@ -2686,7 +2688,11 @@ static void accumulate_bloom_stats(oracle_ctx *c, int64_t nspawn) {
     if (a > c->bloom_max) c->bloom_max = a;
 }
 
-static void mc_cycle(oracle_ctx *c) {
+/* The first half of a Monte Carlo cycle: the loop over the occupied
+ * determinants (src/fciqmc.f90:307-392) -- estimators, attempts, spawning into
+ * the spawned list, death.  Returns the number of deaths; *nattempts_acc is
+ * init_mc_cycle's nattempts (2 N_w at the start of the cycle). */
+static int64_t mc_cycle_spawn(oracle_ctx *c, int64_t *nattempts_acc_out) {
     c->iter++;
     if (c->cfg.semi_stoch_space != 0 && c->iter == c->ss_iter) ss_init(c);
     /* init_mc_cycle (src/qmc_common.F90:950-1017) */
@@ -2742,6 +2748,13 @@ static void mc_cycle(oracle_ctx *c) {
             }
         }
     }
+    *nattempts_acc_out = nattempts_acc;
+    return ndeath;
+}
+
+/* The second half: projection of the deterministic space, direct_annihilation,
+ * the RDM update and end_mc_cycle (src/fciqmc.f90:393-405). */
+static void mc_cycle_finish(oracle_ctx *c, int64_t ndeath, int64_t nattempts_acc) {
     int64_t nspawn_events = c->sn; /* calc_events_spawn_t */
     c->rep_spawned += c->sn;
     if (c->ss_on) ss_project(c);
@@ -2752,6 +2765,12 @@ static void mc_cycle(oracle_ctx *c) {
     if (nattempts_acc > 0)
         c->acc_rspawn += ((double)nspawn_events + (double)ndeath / (double)c->real_factor) / (double)nattempts_acc;
     c->rep_cycles++;
+}
+
+static void mc_cycle(oracle_ctx *c) {
+    int64_t nattempts_acc;
+    const int64_t ndeath = mc_cycle_spawn(c, &nattempts_acc);
+    mc_cycle_finish(c, ndeath, nattempts_acc);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -2974,16 +2993,20 @@ int64_t oracle_get_walkers(oracle_ctx *c, int64_t *states, int64_t *pops, double
     return c->n;
 }
 
-int oracle_run_cycles(oracle_ctx *c, int32_t ncycles) {
+/* The start of a report (src/fciqmc.f90:283-291): clear the RDM once
+ * accumulating; start accumulating after density_matrix_report reports once
+ * every shift varies. */
+static void report_start(oracle_ctx *c) {
     if (c->rep_cycles == 0 && c->rdm_enabled) {
-        /* start of a report (src/fciqmc.f90:283-291): clear the RDM once
-         * accumulating; start accumulating after density_matrix_report reports
-         * once every shift varies */
         if (c->rdm_on) memset(c->rdm, 0, sizeof(double) * (size_t)(c->npairs * c->npairs));
         int all_vary = 1;
         for (int s = 0; s < c->R; s++) all_vary = all_vary && c->vary_shift[s];
         if (all_vary && c->reports_done + 1 > c->cfg.density_matrix_report) c->rdm_on = 1;
     }
+}
+
+int oracle_run_cycles(oracle_ctx *c, int32_t ncycles) {
+    report_start(c);
     for (int k = 0; k < ncycles; k++) mc_cycle(c);
     return c->error_flags ? (c->error_flags & HGPU_FLAG_SPAWN_OVERFLOW ? HGPU_ERR_SPAWN_OVERFLOW
                                                                        : HGPU_ERR_MAIN_OVERFLOW)
@@ -3177,3 +3200,424 @@ double oracle_pgen(oracle_ctx *c, const int64_t *fi, const int32_t *orbs) {
 }
 
 int64_t oracle_total_attempts(oracle_ctx *c) { return c->total_attempts; }
+
+/* ------------------------------------------------------------------------- */
+/* Hash-partitioned calculation on many host cores                            */
+/* ------------------------------------------------------------------------- */
+
+/* HANDE runs one calculation over MPI ranks: every determinant belongs to the
+ * rank given by a hash of its bit string (assign_particle_processor,
+ * src/spawning.F90:770-838: modulo(MurmurHash2(f), nprocs) without load
+ * balancing); each rank spawns from its own determinants into per-destination
+ * blocks of its spawned list, the blocks are exchanged with one all-to-all per
+ * cycle (src/spawn_data.F90:693,721), and each rank annihilates what it
+ * received into its own part of the main list; the estimators are summed over
+ * the ranks once per report (src/energy_evaluation.F90:191).  The replica RDM
+ * spawns go to the owner of the child and every rank keeps an RDM of its own,
+ * summed at the report end.  Here the ranks are threads, one oracle context
+ * each, and the exchange is a copy through shared memory.  The random streams
+ * of rank r are keyed by seed + 1000003 r, so ranks draw independent numbers. */
+
+/* MurmurHash2, 32-bit (Austin Appleby's published algorithm, which the
+ * reference vendors in lib/external/MurmurHash2.c), over the bytes of the
+ * determinant's words. */
+static uint32_t murmur2(const void *key, int len, uint32_t seed) {
+    const uint32_t m = 0x5bd1e995u;
+    uint32_t h = seed ^ (uint32_t)len;
+    const unsigned char *data = (const unsigned char *)key;
+    while (len >= 4) {
+        uint32_t k = (uint32_t)data[0] | ((uint32_t)data[1] << 8) | ((uint32_t)data[2] << 16) |
+                     ((uint32_t)data[3] << 24);
+        k *= m;
+        k ^= k >> 24;
+        k *= m;
+        h *= m;
+        h ^= k;
+        data += 4;
+        len -= 4;
+    }
+    switch (len) {
+        case 3: h ^= (uint32_t)data[2] << 16; /* fall through */
+        case 2: h ^= (uint32_t)data[1] << 8;  /* fall through */
+        case 1: h ^= (uint32_t)data[0]; h *= m;
+    }
+    h ^= h >> 13;
+    h *= m;
+    h ^= h >> 15;
+    return h;
+}
+
+struct oracle_par {
+    int P, nw, R;
+    oracle_ctx **ctx;
+    pthread_barrier_t bar;
+    /* per rank: spawned entries ordered by destination rank, and the
+     * destination offsets [P+1]; the same for the RDM spawns */
+    uint64_t **sd;
+    int64_t **sp, **sf, **off;
+    uint64_t **rd;
+    int64_t **rp, **roff;
+    /* snapshot of every rank's list */
+    int64_t *snap_n;
+    uint64_t **snap_d;
+    int64_t **snap_p;
+    double **snap_k;
+    int ncycles;
+    int report_open; /* oracle_par_begin_report ran for the current report */
+};
+
+static int par_owner(const oracle_par *p, const uint64_t *f) {
+    unsigned char b[8 * MAXW];
+    for (int w = 0; w < p->nw; w++)
+        for (int k = 0; k < 8; k++) b[8 * w + k] = (unsigned char)(f[w] >> (8 * k));
+    const int32_t h = (int32_t)murmur2(b, 8 * p->nw, 7u);
+    return (int)(((h % p->P) + p->P) % p->P); /* Fortran modulo */
+}
+
+/* rank r: its spawned (and RDM) entries into per-destination blocks */
+static void par_bucket(oracle_par *p, int r) {
+    oracle_ctx *c = p->ctx[r];
+    const int nw = p->nw, R = p->R, P = p->P;
+    int64_t *cnt = (int64_t *)calloc((size_t)(unsigned)P, sizeof(int64_t));
+    int *dst = (int *)malloc(sizeof(int) * (size_t)(c->sn > 0 ? c->sn : 1));
+    for (int64_t k = 0; k < c->sn; k++) cnt[dst[k] = par_owner(p, &c->sdets[k * nw])]++;
+    p->off[r][0] = 0;
+    for (int d = 0; d < P; d++) p->off[r][d + 1] = p->off[r][d] + cnt[d];
+    for (int d = 0; d < P; d++) cnt[d] = p->off[r][d];
+    for (int64_t k = 0; k < c->sn; k++) {
+        const int64_t o = cnt[dst[k]]++;
+        memcpy(&p->sd[r][o * nw], &c->sdets[k * nw], sizeof(uint64_t) * nw);
+        memcpy(&p->sp[r][o * R], &c->spops[k * R], sizeof(int64_t) * R);
+        p->sf[r][o] = c->sflag[k];
+    }
+    free(dst);
+    if (c->rdm_enabled) {
+        int *rdst = (int *)malloc(sizeof(int) * (size_t)(c->rsn > 0 ? c->rsn : 1));
+        for (int d = 0; d < P; d++) cnt[d] = 0;
+        for (int64_t k = 0; k < c->rsn; k++) cnt[rdst[k] = par_owner(p, &c->rsdets[k * 2 * nw + nw])]++;
+        p->roff[r][0] = 0;
+        for (int d = 0; d < P; d++) p->roff[r][d + 1] = p->roff[r][d] + cnt[d];
+        for (int d = 0; d < P; d++) cnt[d] = p->roff[r][d];
+        for (int64_t k = 0; k < c->rsn; k++) {
+            const int64_t o = cnt[rdst[k]]++;
+            memcpy(&p->rd[r][o * 2 * nw], &c->rsdets[k * 2 * nw], sizeof(uint64_t) * 2 * nw);
+            memcpy(&p->rp[r][o * R], &c->rspops[k * R], sizeof(int64_t) * R);
+        }
+        free(rdst);
+    }
+    free(cnt);
+}
+
+/* rank d: the blocks every rank addressed to it, in rank order, become its
+ * spawned list (the receive side of the all-to-all) */
+static void par_gather(oracle_par *p, int d) {
+    oracle_ctx *c = p->ctx[d];
+    const int nw = p->nw, R = p->R;
+    int64_t n = 0;
+    for (int r = 0; r < p->P; r++) {
+        const int64_t a = p->off[r][d], b = p->off[r][d + 1];
+        if (n + (b - a) > c->scap) {
+            c->error_flags |= HGPU_FLAG_SPAWN_OVERFLOW;
+            break;
+        }
+        memcpy(&c->sdets[n * nw], &p->sd[r][a * nw], sizeof(uint64_t) * nw * (size_t)(b - a));
+        memcpy(&c->spops[n * R], &p->sp[r][a * R], sizeof(int64_t) * R * (size_t)(b - a));
+        for (int64_t k = a; k < b; k++, n++) {
+            c->sflag[n] = p->sf[r][k];
+            c->sord[n] = n;
+        }
+    }
+    c->sn = n;
+    if (c->rdm_enabled) {
+        int64_t m = 0;
+        for (int r = 0; r < p->P; r++) {
+            const int64_t a = p->roff[r][d], b = p->roff[r][d + 1];
+            if (m + (b - a) > c->scap) {
+                c->error_flags |= HGPU_FLAG_SPAWN_OVERFLOW;
+                break;
+            }
+            memcpy(&c->rsdets[m * 2 * nw], &p->rd[r][a * 2 * nw], sizeof(uint64_t) * 2 * nw * (size_t)(b - a));
+            memcpy(&c->rspops[m * R], &p->rp[r][a * R], sizeof(int64_t) * R * (size_t)(b - a));
+            m += b - a;
+        }
+        c->rsn = m;
+    }
+}
+
+typedef struct {
+    oracle_par *p;
+    int r;
+    void *(*body)(oracle_par *, int);
+} par_arg;
+
+static void *par_thread(void *arg) {
+    par_arg *a = (par_arg *)arg;
+    return a->body(a->p, a->r);
+}
+
+/* Run body(p, r) for every rank r on its own thread. */
+static void par_each_rank(oracle_par *p, void *(*body)(oracle_par *, int)) {
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)(unsigned)p->P);
+    par_arg *args = (par_arg *)malloc(sizeof(par_arg) * (size_t)(unsigned)p->P);
+    for (int r = 0; r < p->P; r++) {
+        args[r].p = p;
+        args[r].r = r;
+        args[r].body = body;
+        pthread_create(&th[r], NULL, par_thread, &args[r]);
+    }
+    for (int r = 0; r < p->P; r++) pthread_join(th[r], NULL);
+    free(th);
+    free(args);
+}
+
+static void *par_report_start(oracle_par *p, int r) {
+    report_start(p->ctx[r]);
+    return NULL;
+}
+
+static void *par_rdm_energy(oracle_par *p, int r) {
+    oracle_ctx *c = p->ctx[r];
+    if (c->rdm_on) calc_rdm_energy(c, &c->rdm_energy, &c->rdm_trace);
+    return NULL;
+}
+
+static void *par_cycles(oracle_par *p, int r) {
+    oracle_ctx *c = p->ctx[r];
+    for (int k = 0; k < p->ncycles; k++) {
+        int64_t nacc;
+        const int64_t ndeath = mc_cycle_spawn(c, &nacc);
+        par_bucket(p, r);
+        pthread_barrier_wait(&p->bar); /* every rank's blocks are ready */
+        par_gather(p, r);
+        mc_cycle_finish(c, ndeath, nacc);
+        pthread_barrier_wait(&p->bar); /* every rank has read its blocks */
+    }
+    return NULL;
+}
+
+oracle_par *oracle_par_create(const hgpu_config *cfg, const hgpu_system *sys, int nthreads) {
+    if (nthreads < 1) return NULL;
+    oracle_par *p = (oracle_par *)calloc(1, sizeof(oracle_par));
+    p->P = nthreads;
+    p->nw = sys->nwords;
+    p->R = cfg->nspaces > 0 ? cfg->nspaces : 1;
+    p->ctx = (oracle_ctx **)calloc((size_t)nthreads, sizeof(oracle_ctx *));
+#define PAR_ARRAYS(X) X(sd, uint64_t) X(sp, int64_t) X(sf, int64_t) X(off, int64_t) X(rd, uint64_t) \
+    X(rp, int64_t) X(roff, int64_t) X(snap_d, uint64_t) X(snap_p, int64_t) X(snap_k, double)
+#define PAR_ALLOC(name, T) p->name = (T **)calloc((size_t)nthreads, sizeof(T *));
+    PAR_ARRAYS(PAR_ALLOC)
+    p->snap_n = (int64_t *)calloc((size_t)nthreads, sizeof(int64_t));
+    for (int r = 0; r < nthreads; r++) {
+        hgpu_config c = *cfg;
+        c.seed = cfg->seed + 1000003LL * r;
+        p->ctx[r] = oracle_create(&c, sys);
+        if (!p->ctx[r]) {
+            oracle_par_destroy(p);
+            return NULL;
+        }
+        const int64_t sc = p->ctx[r]->scap;
+        p->sd[r] = (uint64_t *)malloc(sizeof(uint64_t) * p->nw * (size_t)sc);
+        p->sp[r] = (int64_t *)malloc(sizeof(int64_t) * p->R * (size_t)sc);
+        p->sf[r] = (int64_t *)malloc(sizeof(int64_t) * (size_t)sc);
+        p->off[r] = (int64_t *)calloc((size_t)nthreads + 1, sizeof(int64_t));
+        p->roff[r] = (int64_t *)calloc((size_t)nthreads + 1, sizeof(int64_t));
+        if (cfg->density_matrices) {
+            p->rd[r] = (uint64_t *)malloc(sizeof(uint64_t) * 2 * p->nw * (size_t)sc);
+            p->rp[r] = (int64_t *)malloc(sizeof(int64_t) * p->R * (size_t)sc);
+        }
+    }
+    pthread_barrier_init(&p->bar, NULL, (unsigned)nthreads);
+    return p;
+}
+
+void oracle_par_destroy(oracle_par *p) {
+    if (!p) return;
+    for (int r = 0; r < p->P; r++) {
+        if (p->ctx[r]) oracle_destroy(p->ctx[r]);
+#define PAR_FREE(name, T) if (p->name) free(p->name[r]);
+        PAR_ARRAYS(PAR_FREE)
+    }
+#define PAR_FREE2(name, T) free(p->name);
+    PAR_ARRAYS(PAR_FREE2)
+    free(p->snap_n);
+    if (p->ctx[0]) pthread_barrier_destroy(&p->bar);
+    free(p->ctx);
+    free(p);
+}
+
+/* initial_distribution: the walkers on the reference, on its owner rank */
+int oracle_par_initial_distribution(oracle_par *p) {
+    const int owner = par_owner(p, p->ctx[0]->f0);
+    for (int r = 0; r < p->P; r++) {
+        oracle_ctx *c = p->ctx[r];
+        oracle_initial_distribution(c);
+        if (r != owner) c->n = 0;
+    }
+    /* N_w of the whole calculation */
+    double tot[2] = {0.0, 0.0};
+    for (int r = 0; r < p->P; r++)
+        for (int s = 0; s < p->R; s++) tot[s] += nparticles(p->ctx[r], s);
+    for (int r = 0; r < p->P; r++)
+        for (int s = 0; s < p->R; s++) p->ctx[r]->nparticles_old[s] = tot[s];
+    return 0;
+}
+
+/* The start of a report on every rank (each clears its own RDM once
+ * accumulating); oracle_par_run_cycles does it when the caller has not. */
+int oracle_par_begin_report(oracle_par *p) {
+    if (!p->report_open) par_each_rank(p, par_report_start);
+    p->report_open = 1;
+    return 0;
+}
+
+int oracle_par_run_cycles(oracle_par *p, int32_t ncycles) {
+    oracle_par_begin_report(p);
+    p->ncycles = ncycles;
+    par_each_rank(p, par_cycles);
+    int flags = 0;
+    for (int r = 0; r < p->P; r++) flags |= p->ctx[r]->error_flags;
+    return flags ? (flags & HGPU_FLAG_SPAWN_OVERFLOW ? HGPU_ERR_SPAWN_OVERFLOW : HGPU_ERR_MAIN_OVERFLOW) : 0;
+}
+
+/* The report over all ranks: sums of the estimators, N_w and counters (the
+ * estimator buffer's MPI_Allreduce), then update_shift once with the totals
+ * and the same shift on every rank. */
+int oracle_par_end_report(oracle_par *p, hgpu_report *out) {
+    oracle_ctx *c0 = p->ctx[0];
+    const int R = p->R;
+    const int nc = c0->rep_cycles > 0 ? c0->rep_cycles : 1;
+    memset(out, 0, sizeof(*out));
+    double proj[2] = {0, 0}, d0[2] = {0, 0}, ntot[2] = {0, 0}, rspawn = 0.0;
+    int64_t states = 0, events = 0;
+    p->report_open = 0;
+    if (c0->rdm_on) par_each_rank(p, par_rdm_energy);
+    for (int r = 0; r < p->P; r++) {
+        oracle_ctx *c = p->ctx[r];
+        if (c->rdm_on) {
+            out->rdm_energy += c->rdm_energy;
+            out->rdm_trace += c->rdm_trace;
+        }
+        c->reports_done++;
+        for (int s = 0; s < R; s++) {
+            proj[s] += c->acc_proj[s];
+            d0[s] += c->acc_d0[s];
+            ntot[s] += nparticles(c, s);
+        }
+        rspawn += c->acc_rspawn;
+        states += c->n;
+        events += c->last_nspawn_events;
+        out->nattempts += c->rep_attempts;
+        out->nspawned += c->rep_spawned;
+        out->error_flags |= c->error_flags;
+        out->nblooms += c->bloom_n;
+        out->tot_bloom += (double)c->bloom_tot / (double)c->real_factor;
+        if ((double)c->bloom_max / (double)c->real_factor > out->max_bloom)
+            out->max_bloom = (double)c->bloom_max / (double)c->real_factor;
+    }
+    for (int s = 0; s < R; s++) {
+        out->proj_energy[s] = proj[s] / (double)nc;
+        out->D0_population[s] = d0[s] / (double)nc;
+    }
+    double shift[2], old[2];
+    int vary[2];
+    for (int s = 0; s < 2; s++) {
+        shift[s] = c0->shift[s];
+        vary[s] = c0->vary_shift[s];
+        old[s] = c0->nparticles_old[s];
+    }
+    for (int s = 0; s < R; s++)
+        if (vary[s]) shift[s] = shift[s] - log(ntot[s] / old[s]) * c0->cfg.shift_damping / (1.0 * c0->cfg.tau * (double)nc);
+    for (int s = 0; s < R; s++) {
+        if (!vary[s] && ntot[s] > c0->cfg.target_particles) {
+            vary[s] = 1;
+            shift[s] = c0->cfg.vary_shift_from_proje ? out->proj_energy[s] / out->D0_population[s]
+                                                     : c0->cfg.vary_shift_from;
+        }
+        out->shift[s] = shift[s];
+        out->nparticles[s] = ntot[s];
+        out->vary_shift[s] = vary[s];
+    }
+    out->iteration = c0->iter;
+    out->nstates = states;
+    out->nspawn_events = events;
+    out->rspawn = rspawn / (double)nc / (double)p->P;
+    for (int r = 0; r < p->P; r++) {
+        oracle_ctx *c = p->ctx[r];
+        for (int s = 0; s < R; s++) {
+            c->shift[s] = shift[s];
+            c->vary_shift[s] = vary[s];
+            c->nparticles_old[s] = ntot[s];
+            c->acc_proj[s] = c->acc_d0[s] = 0.0;
+        }
+        c->acc_rspawn = 0.0;
+        c->rep_attempts = c->rep_spawned = 0;
+        c->rep_cycles = 0;
+        c->bloom_n = c->bloom_tot = 0;
+    }
+    return out->error_flags ? HGPU_ERR_SPAWN_OVERFLOW : 0;
+}
+
+/* Save (restore = 0) or restore (1) every rank's walker list. */
+int oracle_par_snapshot(oracle_par *p, int restore) {
+    for (int r = 0; r < p->P; r++) {
+        oracle_ctx *c = p->ctx[r];
+        if (!restore) {
+            free(p->snap_d[r]); free(p->snap_p[r]); free(p->snap_k[r]);
+            const int64_t n = c->n > 0 ? c->n : 1;
+            p->snap_d[r] = (uint64_t *)malloc(sizeof(uint64_t) * p->nw * (size_t)n);
+            p->snap_p[r] = (int64_t *)malloc(sizeof(int64_t) * p->R * (size_t)n);
+            p->snap_k[r] = (double *)malloc(sizeof(double) * (size_t)n);
+            memcpy(p->snap_d[r], c->dets, sizeof(uint64_t) * p->nw * (size_t)c->n);
+            memcpy(p->snap_p[r], c->pops, sizeof(int64_t) * p->R * (size_t)c->n);
+            memcpy(p->snap_k[r], c->kii, sizeof(double) * (size_t)c->n);
+            p->snap_n[r] = c->n;
+        } else {
+            if (!p->snap_d[r]) return HGPU_ERR_INVALID;
+            c->n = p->snap_n[r];
+            memcpy(c->dets, p->snap_d[r], sizeof(uint64_t) * p->nw * (size_t)c->n);
+            memcpy(c->pops, p->snap_p[r], sizeof(int64_t) * p->R * (size_t)c->n);
+            memcpy(c->kii, p->snap_k[r], sizeof(double) * (size_t)c->n);
+        }
+    }
+    return 0;
+}
+
+/* The qmc_state scalars of every rank (iteration, shift, vary_shift, N_w of
+ * the last report); the state of rank 0 is the calculation's. */
+int oracle_par_set_state(oracle_par *p, const hgpu_state *in) {
+    for (int r = 0; r < p->P; r++) oracle_set_state(p->ctx[r], in);
+    return 0;
+}
+
+int oracle_par_get_state(oracle_par *p, hgpu_state *out) { return oracle_get_state(p->ctx[0], out); }
+
+int64_t oracle_par_total_attempts(oracle_par *p) {
+    int64_t t = 0;
+    for (int r = 0; r < p->P; r++) t += p->ctx[r]->total_attempts;
+    return t;
+}
+
+/* The whole calculation's walker list, merged over the ranks in HANDE's order
+ * (the rank lists are each sorted); returns the number of states. */
+int64_t oracle_par_get_walkers(oracle_par *p, int64_t *states, int64_t *pops, double *dat, int64_t cap) {
+    int64_t n = 0;
+    for (int r = 0; r < p->P; r++) n += p->ctx[r]->n;
+    if (cap < n || !states) return n;
+    int64_t *pos = (int64_t *)calloc((size_t)(unsigned)p->P, sizeof(int64_t));
+    for (int64_t k = 0; k < n; k++) {
+        int best = -1;
+        for (int r = 0; r < p->P; r++) {
+            oracle_ctx *c = p->ctx[r];
+            if (pos[r] >= c->n) continue;
+            if (best < 0 || det_cmp(&c->dets[pos[r] * p->nw], &p->ctx[best]->dets[pos[best] * p->nw], p->nw) > 0)
+                best = r;
+        }
+        oracle_ctx *c = p->ctx[best];
+        memcpy(&states[k * p->nw], &c->dets[pos[best] * p->nw], sizeof(uint64_t) * p->nw);
+        if (pops) memcpy(&pops[k * p->R], &c->pops[pos[best] * p->R], sizeof(int64_t) * p->R);
+        if (dat) dat[k] = c->kii[pos[best]];
+        pos[best]++;
+    }
+    free(pos);
+    return n;
+}

@@ -64,6 +64,22 @@ void oracle_rdm_energy(oracle_ctx *c, double *energy, double *trace);
 void oracle_rdm_from_list(oracle_ctx *c);
 /* Counters of the last cycles (spawn attempts etc.). */
 int64_t oracle_total_attempts(oracle_ctx *c);
+/* One calculation hash-partitioned over nthreads ranks (threads), as HANDE
+ * runs it over MPI ranks: determinants owned by modulo(MurmurHash2, ranks),
+ * spawned entries exchanged once per cycle, estimators summed per report.
+ * Used to time the reference algorithm on all host cores. */
+typedef struct oracle_par oracle_par;
+oracle_par *oracle_par_create(const hgpu_config *cfg, const hgpu_system *sys, int nthreads);
+void oracle_par_destroy(oracle_par *p);
+int oracle_par_initial_distribution(oracle_par *p);
+int oracle_par_begin_report(oracle_par *p);
+int oracle_par_run_cycles(oracle_par *p, int32_t ncycles);
+int oracle_par_end_report(oracle_par *p, hgpu_report *out);
+int oracle_par_snapshot(oracle_par *p, int restore);
+int oracle_par_set_state(oracle_par *p, const hgpu_state *in);
+int oracle_par_get_state(oracle_par *p, hgpu_state *out);
+int64_t oracle_par_total_attempts(oracle_par *p);
+int64_t oracle_par_get_walkers(oracle_par *p, int64_t *states, int64_t *pops, double *dat, int64_t cap);
 /* Philox4x32-10 uniform, for cross-checking the device generator. */
 double oracle_uniform(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, int which);
 

@@ -67,6 +67,20 @@ def lib():
         L.oracle_pgen.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int32)]
         L.oracle_total_attempts.restype = C.c_int64
         L.oracle_total_attempts.argtypes = [C.c_void_p]
+        L.oracle_par_create.restype = C.c_void_p
+        L.oracle_par_create.argtypes = [P(HgpuConfig), P(HgpuSystem), C.c_int]
+        L.oracle_par_destroy.argtypes = [C.c_void_p]
+        L.oracle_par_initial_distribution.argtypes = [C.c_void_p]
+        L.oracle_par_run_cycles.argtypes = [C.c_void_p, C.c_int32]
+        L.oracle_par_begin_report.argtypes = [C.c_void_p]
+        L.oracle_par_end_report.argtypes = [C.c_void_p, P(HgpuReport)]
+        L.oracle_par_snapshot.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_par_set_state.argtypes = [C.c_void_p, P(HgpuState)]
+        L.oracle_par_get_state.argtypes = [C.c_void_p, P(HgpuState)]
+        L.oracle_par_total_attempts.restype = C.c_int64
+        L.oracle_par_total_attempts.argtypes = [C.c_void_p]
+        L.oracle_par_get_walkers.restype = C.c_int64
+        L.oracle_par_get_walkers.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_double), C.c_int64]
         L.oracle_uniform.restype = C.c_double
         L.oracle_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]
         _lib = L
@@ -210,6 +224,77 @@ class Oracle:
 
     def total_attempts(self) -> int:
         return self.L.oracle_total_attempts(self.h)
+
+
+class OraclePar:
+    """One calculation hash-partitioned over `nthreads` ranks (threads), as the
+    reference runs over MPI ranks (oracle_par_* in hande_oracle.c)."""
+
+    def __init__(self, system, cfg: HgpuConfig, nthreads: int):
+        self.L = lib()
+        self.sys = system
+        self.packed = PackedSystem(system)
+        self.cfg = cfg
+        self.nw = system.nwords
+        self.R = cfg.nspaces
+        self.h = self.L.oracle_par_create(C.byref(cfg), C.byref(self.packed.struct), int(nthreads))
+        if not self.h:
+            raise RuntimeError("oracle_par_create failed")
+
+    def close(self):
+        if self.h:
+            self.L.oracle_par_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initial_distribution(self):
+        self.L.oracle_par_initial_distribution(self.h)
+
+    def begin_report(self):
+        """The start of a report (each rank clears its RDM once accumulating);
+        run_cycles does it itself when it was not called."""
+        self.L.oracle_par_begin_report(self.h)
+
+    def run_cycles(self, n):
+        return self.L.oracle_par_run_cycles(self.h, int(n))
+
+    def end_report(self) -> HgpuReport:
+        r = HgpuReport()
+        self.L.oracle_par_end_report(self.h, C.byref(r))
+        return r
+
+    def run_report(self) -> HgpuReport:
+        self.run_cycles(self.cfg.ncycles)
+        return self.end_report()
+
+    def snapshot(self, restore: bool = False):
+        rc = self.L.oracle_par_snapshot(self.h, int(bool(restore)))
+        if rc:
+            raise RuntimeError("oracle_par_snapshot: no snapshot")
+
+    def total_attempts(self) -> int:
+        return int(self.L.oracle_par_total_attempts(self.h))
+
+    def state(self) -> HgpuState:
+        s = HgpuState()
+        self.L.oracle_par_get_state(self.h, C.byref(s))
+        return s
+
+    def set_state(self, s: HgpuState):
+        self.L.oracle_par_set_state(self.h, C.byref(s))
+
+    def walkers(self):
+        n = self.L.oracle_par_get_walkers(self.h, None, None, None, 0)
+        st = np.zeros((max(n, 1), self.nw), dtype=np.int64)
+        po = np.zeros((max(n, 1), self.R), dtype=np.int64)
+        da = np.zeros(max(n, 1), dtype=np.float64)
+        self.L.oracle_par_get_walkers(self.h, _i64(st), _i64(po), da.ctypes.data_as(C.POINTER(C.c_double)), n)
+        return st[:n], po[:n], da[:n]
 
 
 def uniform(seed, c0, c1, c2, c3, which=0):

@@ -55,13 +55,13 @@ WORKLOAD = ("config2: synthetic molecule M=26 nel=10 C1, real amplitudes, cutoff
             "tau=1e-3, ~1e7 walkers, FP64; each step = one full cycle on the same device-grown walker list")
 
 
-def system_and_config(target=1e7, seed_ham=2024, seed_rng=7, cap_main=None, cap_spawn=None):
+def system_and_config(target=1e7, seed_ham=2024, seed_rng=7, cap_main=None, cap_spawn=None, ncycles=10):
     from hande_gb300 import systems
     from hande_gb300._abi import make_config
     s = systems.synthetic_molecule(26, 10, seed=seed_ham)
     cm = cap_main or int(4 * target) + 200000
     cs = cap_spawn or int(4 * target) + 200000
-    cfg = make_config(s, tau=1e-3, init_pop=10, target_population=target, ncycles=10, seed=seed_rng,
+    cfg = make_config(s, tau=1e-3, init_pop=10, target_population=target, ncycles=ncycles, seed=seed_rng,
                       real_amplitudes=True, spawn_cutoff=0.01, excit_gen="renorm", pattempt_single=0.1,
                       pattempt_double=0.9, state_size=cm, spawned_state_size=cs)
     return s, cfg
@@ -717,7 +717,7 @@ def config2_measure(steps, warmup, rank=0, cpu_seconds=10.0, parity=True):
     (bit-exact comparison) and the one-core oracle's rate on it."""
     from hande_gb300.engine import Engine
     from hande_gb300.measure import roofline_figures
-    s, cfg = system_and_config(target=1e7, seed_rng=7 + rank)
+    s, cfg = system_and_config(target=1e7, seed_rng=7 + rank, ncycles=1)  # a step is one cycle
     eng = Engine(s, cfg)
     eng.initial_distribution()
     grown = grow(eng, 1e7)
@@ -841,10 +841,18 @@ def main():
     # end to end through the C ABI with host walker lists
     e2e = e2e_measure(eng, s.nwords, 2, args.e2e_steps, main_cap)
     parity = cpu = None
+    # the step input on the host: the FP32 engine replays the same list
+    eng.snapshot(restore=True)
+    st, po, da = eng.walkers()
+    state = eng.get_state()
+    xs = x64 = None
+    if rank == 0 and not args.no_extra:
+        # FP64 excitations of 2^20 parents drawn from the list, for the FP32 comparison
+        rng = np.random.default_rng(5)
+        pick = rng.integers(0, st.shape[0], 1 << 20)
+        xs = (st[pick], np.ones(1 << 20, np.int64), int(state.iteration) + 1000)
+        x64 = eng.eval_excitations(*xs)
     if rank == 0 and not args.no_cpu:
-        eng.snapshot(restore=True)
-        st, po, da = eng.walkers()
-        state = eng.get_state()
         n = 50000
         i0 = max(0, (st.shape[0] - n) // 2)
         sl = slice(i0, i0 + n)
@@ -854,32 +862,51 @@ def main():
                               "one cycle of a %d-state slice (from state %d) of the benchmark's own %d-state list, "
                               "the benchmark's iteration, shift and parameters (FP64)" % (n, i0, st.shape[0]))
         cpu = cpu_slice(s, cfg, st, po, da, state, 100000, args.cpu_seconds)
-        del st, po, da
     eng.close()
 
     extra = {}
     if rank == 0 and not args.no_extra:
-        # the FP32 engine on the same workload and its E_proj against FP64
-        cfg32 = large_config(s, PREC_MIXED, main_cap, spawn_cap, init_pop=args.large_total / 500.0, seed=5)
+        # the FP32 engine on the same list: attempts/s, the replica (RDM)
+        # energy of each replayed cycle against FP64's, and the FP32 matrix
+        # elements and p_gen of the same 2^20 generated excitations
+        cfg32 = large_config(s, PREC_MIXED, main_cap, spawn_cap, seed=5 + rank)
         e32 = Engine(s, cfg32)
-        e32.initial_distribution()
-        grown32, _ = grow_replicas(e32, args.large_total, label="fp32")
-        hold_and_save(e32)
+        e32.set_walkers(st, po, da)
+        e32.set_state(state)
+        e32.snapshot()
         r32 = replay_steps(e32, args.steps, args.warmup)
+        x32 = e32.eval_excitations(*xs)
         e32.close()
-        s64, s32 = eproj_stats(r64["eproj"]), eproj_stats(r32["eproj"])
+        same = np.all(x32[0] == x64[0], axis=1) & (x32[3] == x64[3]) & (x64[3] == 1)
+        rel_h = np.abs(x32[2][same] - x64[2][same]) / np.abs(x64[2][same])
+        rel_p = np.abs(x32[1][same] - x64[1][same]) / np.abs(x64[1][same])
+        e64 = np.array(r64["rdm"])
+        e32r = np.array(r32["rdm"])
+        ok = len(e64) > 1 and len(e32r) == len(e64)
+
+        def mse(x):
+            return [float(np.mean(x)), float(np.std(x, ddof=1) / np.sqrt(len(x)))]
+
         extra["mixed_precision"] = {
             "value": r32["attempts"] / (r32["dev_ms"] * 1e-3), "unit": "attempts/s",
             "ms_per_step": r32["dev_ms"] / args.steps, "speedup_over_fp64": (r32["attempts"] / r32["dev_ms"]) / (
                 r64["attempts"] / r64["dev_ms"]),
-            "walkers": grown32.nparticles[0] + grown32.nparticles[1],
-            "E_proj_one_cycle": {"fp64": s64, "fp32": s32},
-            "dE_proj_over_sigma": [(s32[q][0] - s64[q][0]) / float(np.hypot(s32[q][1], s64[q][1])) for q in range(2)],
-            "rdm_energy_one_cycle": {"fp64": float(np.mean(r64["rdm"])) if r64["rdm"] else None,
-                                     "fp32": float(np.mean(r32["rdm"])) if r32["rdm"] else None},
-            "note": "FP32 H_ij and p_gen, FP64 K_ii, shift and estimators; each engine grown from the same seed to "
-                    "about the same population, then K one-cycle reports replayed from its own list: mean and "
-                    "standard error of the one-cycle E_proj of each replica (relative to H_00)"}
+            "rdm_energy_one_cycle": {"fp64": mse(e64) if ok else None, "fp32": mse(e32r) if ok else None},
+            # both engines replay the same iterations, hence the same random
+            # streams: the paired difference isolates the FP32 arithmetic
+            "dE_rdm_paired": mse(e32r - e64) if ok else None,
+            "dE_rdm_over_sigma": (float(np.mean(e32r) - np.mean(e64)) /
+                                  float(np.hypot(mse(e64)[1], mse(e32r)[1]))) if ok else None,
+            "excitations": {"sampled": len(xs[0]), "same_excitation": float(same.mean()),
+                            "max_rel_err_hij": float(rel_h.max()) if rel_h.size else None,
+                            "max_rel_err_pgen": float(rel_p.max()) if rel_p.size else None},
+            "note": "FP32 H_ij and p_gen, FP64 K_ii, shift and estimators; both engines replay one-cycle reports "
+                    "from the same walker list: the replica (variational, RDM) energy of each replayed cycle, "
+                    "relative to H_00, mean and standard error over the K replays (dE_rdm_over_sigma treats the "
+                    "two sets as independent, which overstates sigma); the FP32 H_ij and p_gen of 2^20 "
+                    "excitations generated from list parents with the same random streams as FP64's"}
+    del st, po, da
+    if rank == 0 and not args.no_extra:
         extra["config2"] = config2_measure(args.steps, args.warmup, cpu_seconds=args.cpu_seconds,
                                            parity=not args.no_cpu)
     batched = None
@@ -906,7 +933,10 @@ def main():
             "phase_ms": phases,
             "cycle_counts": counts,
             "clocks": r64["clocks"],
-            "E_proj_one_cycle": eproj_stats(r64["eproj"]),
+            "E_proj": [x[0] for x in eproj_stats(r64["eproj"])],
+            "rdm_energy_one_cycle": [float(np.mean(r64["rdm"])), float(np.std(r64["rdm"], ddof=1) /
+                                                                      np.sqrt(len(r64["rdm"])))]
+            if len(r64["rdm"]) > 1 else None,
             "parity": parity,
             "cpu_baseline": cpu,
             "batched": batched,

@@ -12,7 +12,7 @@
 // the sorted spawned list (duplicates adjacent), main entry first among equal
 // determinants, so that every determinant forms one contiguous group
 // [main entry][spawned entries].  The merged sequence is cut into tiles of
-// kAnnTile elements at group boundaries (k_ann_splits); a tile (k_annihilate)
+// ann_tile<W>() elements at group boundaries (k_ann_splits); a tile (k_annihilate)
 // stages its slices in shared memory, sums every group at its head, rounds,
 // counts its survivors, takes its output offset from a decoupled look-back over
 // the preceding tiles, and writes the survivors, in order, to the other main
@@ -38,8 +38,6 @@ __global__ void k_clamp_spawns(DevState *st, int64_t scap) {
 
 namespace hgpu {
 
-
-constexpr int kAnnPer = kAnnTile / kBlock;  // consecutive merged positions per thread
 
 // Sums of one group's spawned entries; for the initiator approximation also
 // the particles from initiators, the coherent events of the others and the
@@ -177,7 +175,7 @@ struct SortedSpawns {
 };
 
 // Merge-path cuts (Odeh et al., "Merge Path", 2012) of the main list and the
-// sorted spawned list at every diagonal t * kAnnTile, and the same cuts moved
+// sorted spawned list at every diagonal t * ann_tile<W>(), and the same cuts moved
 // past the spawned entries equal to the last element before them, so that no
 // group of equal determinants straddles two tiles.  msplit[3t..3t+2] = (main
 // index, spawned index, spawned index at the group boundary).  One warp per
@@ -188,9 +186,10 @@ struct SortedSpawns {
 template <int W, bool RANK>
 __global__ void __launch_bounds__(kBlock) k_ann_splits(DevBuffers b, int cur, const uint64_t *keys,
                                                        const uint32_t *idx) {
+    constexpr int TILE = ann_tile<W>();
     DevState *st = b.state;
     const int64_t N = st->n_main, S = st->n_spawn, L = N + S;
-    const int64_t ntiles = (L + kAnnTile - 1) / kAnnTile;
+    const int64_t ntiles = (L + TILE - 1) / TILE;
     const uint64_t *mdets = b.dets[cur];
     const SortedSpawns<W, RANK> sp{keys, idx, b.sdets};
     const int lane = threadIdx.x & 31;
@@ -202,7 +201,7 @@ __global__ void __launch_bounds__(kBlock) k_ann_splits(DevBuffers b, int cur, co
     }
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t t = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t <= ntiles; t += warps) {
-        const int64_t d = t * kAnnTile < L ? t * kAnnTile : L;
+        const int64_t d = t * TILE < L ? t * TILE : L;
         // first i in [lo, hi] with spawned[d-1-i] < main[i] (hi if none): main[i]
         // precedes spawned[d-1-i] exactly when main[i] <= spawned[d-1-i]
         int64_t lo = d - S > 0 ? d - S : 0, hi = d < N ? d : N;
@@ -259,11 +258,12 @@ __global__ void __launch_bounds__(kBlock) k_ann_splits(DevBuffers b, int cur, co
 // survivors than the main list holds, and then keeps the main-list survivors
 // alone (insert_new_walkers refuses the new determinants, and the overflow is
 // flagged).  Dynamic shared memory: the exact-diagonal tables
-// (fx_table_words), the tile's populations (kAnnTile x R) and, with the
-// initiator approximation, its spawned flag words (kAnnTile).
+// (fx_table_words, unless they are read from global memory), the tile's
+// populations (TILE x R) and, with the initiator approximation, its spawned
+// flag words (TILE).
 //
 // A tile runs in phases that keep the warps converged: the merge walk (each
-// thread a run of kAnnPer merged positions, from one merge-path search) gives
+// thread a run of PER merged positions, from one merge-path search) gives
 // the slot of every merged position; the groups are then summed, combined and
 // rounded with consecutive threads on consecutive positions, so that the
 // Philox rounding of neighbouring entries runs together; the survivors are
@@ -272,27 +272,32 @@ __global__ void __launch_bounds__(kBlock) k_ann_splits(DevBuffers b, int cur, co
 template <int W, bool RANK>
 __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, int cur, const uint64_t *keys,
                                                           const uint32_t *idx, int mode) {
+    constexpr int TILE = ann_tile<W>();
+    constexpr int PER = TILE / kBlock;  // consecutive merged positions per thread
+    static_assert(PER == 4 || PER == 8, "a thread's codes are read as one 8- or 16-byte word");
     constexpr uint16_t kKept = 0x8000, kNew = 0x4000, kSlot = 0x0FFF;
     __shared__ DevSys s;
-    __shared__ uint64_t tdet[kAnnTile * W];          // main slice at [0, nm), spawned slice at [nm, nm + ns)
-    __shared__ __align__(16) uint16_t msrc[kAnnTile];  // per merged position: its slot
-    __shared__ __align__(16) uint16_t pcode[kAnnTile]; // per merged position: kKept | kNew | slot
+    __shared__ uint64_t tdet[TILE * W];          // main slice at [0, nm), spawned slice at [nm, nm + ns)
+    __shared__ __align__(16) uint16_t msrc[TILE];  // per merged position: its slot
+    __shared__ __align__(16) uint16_t pcode[TILE]; // per merged position: kKept | kNew | slot
     uint16_t *const osrc = msrc;                     // per output of the tile: kNew | slot (after the groups)
     __shared__ SegAcc s_tail;
-    __shared__ uint32_t s_tile, s_base;
+    __shared__ uint32_t s_tile, s_base, s_nnew;
     extern __shared__ int64_t dyn[];
     DevState *st = b.state;
     const uint2 prior = *reinterpret_cast<const uint2 *>(&st->n_merged_keep);
     if (mode == 1 && (int64_t)prior.y <= b.cap) return;
     stage_sys(s, b.sys);
     __syncthreads();
-    const FxTabs tb = stage_fx(s, dyn);
-    int64_t *tpop = dyn + fx_table_words(s.kind, s.nbasis, s.norb);
-    uint64_t *tflag = reinterpret_cast<uint64_t *>(tpop + (size_t)kAnnTile * R);
+    // the exact-diagonal tables: staged in shared memory, or read through L1
+    const bool fx_staged = b.fx_smem_bytes != 0;
+    const FxTabs tb = fx_staged ? stage_fx(s, dyn) : fx_tabs(s);
+    int64_t *tpop = dyn + (fx_staged ? fx_table_words(s.kind, s.nbasis, s.norb) : 0);
+    uint64_t *tflag = reinterpret_cast<uint64_t *>(tpop + (size_t)TILE * R);
     const bool initiator = b.sflag != nullptr;
     const bool real = s.real_amplitudes != 0;
     const int64_t N = st->n_main, S = st->n_spawn, L = N + S;
-    const int64_t ntiles = (L + kAnnTile - 1) / kAnnTile;
+    const int64_t ntiles = (L + TILE - 1) / TILE;
     const uint64_t iter = (uint64_t)st->iter;
     const uint32_t epoch = os_epoch(*b.seg_epoch, mode);
     const SortedSpawns<W, RANK> sp{keys, idx, b.sdets};
@@ -318,7 +323,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
         const int64_t ia = b.msplit[3 * t + 0], ja = b.msplit[3 * t + 2];
         const int64_t ib = b.msplit[3 * t + 3], jb = b.msplit[3 * t + 4], jc = b.msplit[3 * t + 5];
         int nm = 0, ns = 0;
-        if (ja <= jb && ia <= ib && (ib - ia) + (jb - ja) <= kAnnTile) {
+        if (ja <= jb && ia <= ib && (ib - ia) + (jb - ja) <= TILE) {
             nm = (int)(ib - ia);
             ns = (int)(jb - ja);
         } else if (ja <= jb) {
@@ -329,14 +334,14 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
         const int64_t ntail = n > 0 ? jc - jb : 0;
         // stage the slices: determinants, populations, flag words
         {
-            uint32_t e[kAnnPer];
+            uint32_t e[PER];
 #pragma unroll
-            for (int r = 0; r < kAnnPer; r++) {
+            for (int r = 0; r < PER; r++) {
                 const int k = threadIdx.x + r * kBlock;
                 e[r] = (k >= nm && k < n) ? sp.at(ja + (k - nm)) : 0u;
             }
 #pragma unroll
-            for (int r = 0; r < kAnnPer; r++) {
+            for (int r = 0; r < PER; r++) {
                 const int k = threadIdx.x + r * kBlock;
                 if (k >= n) continue;
                 Det<W> d;
@@ -381,7 +386,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
         __syncthreads();
         // merge walk: the slot of every merged position
         {
-            const int p0 = threadIdx.x * kAnnPer;
+            const int p0 = threadIdx.x * PER;
             if (p0 < n) {
                 int lo = p0 - ns > 0 ? p0 - ns : 0, hi = p0 < nm ? p0 : nm;
                 while (lo < hi) {
@@ -390,7 +395,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
                     else hi = mid;
                 }
                 int a = lo, bb = p0 - lo;
-                const int plen = n - p0 < kAnnPer ? n - p0 : kAnnPer;
+                const int plen = n - p0 < PER ? n - p0 : PER;
                 for (int q = 0; q < plen; q++) {
                     const bool take_main = a < nm && (bb >= ns || !det_less<W>(tile_det(nm + bb), tile_det(a)));
                     msrc[p0 + q] = take_main ? (uint16_t)a : (uint16_t)(nm + bb);
@@ -489,20 +494,24 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
             pcode[k] = code;
         }
         __syncthreads();
-        // compaction: each thread counts its kAnnPer consecutive positions
-        uint32_t codes[kAnnPer / 2];
-        {
+        // compaction: each thread counts its PER consecutive positions
+        uint32_t codes[PER / 2];
+        if constexpr (PER == 8) {
             const uint4 v = reinterpret_cast<const uint4 *>(pcode)[threadIdx.x];
             codes[0] = v.x;
             codes[1] = v.y;
             codes[2] = v.z;
             codes[3] = v.w;
+        } else {
+            const uint2 v = reinterpret_cast<const uint2 *>(pcode)[threadIdx.x];
+            codes[0] = v.x;
+            codes[1] = v.y;
         }
         uint32_t kept = 0, kept_main = 0;
 #pragma unroll
-        for (int q = 0; q < kAnnPer; q++) {
+        for (int q = 0; q < PER; q++) {
             const uint32_t c = (codes[q >> 1] >> (16 * (q & 1))) & 0xFFFFu;
-            const bool in = threadIdx.x * kAnnPer + q < n;
+            const bool in = threadIdx.x * PER + q < n;
             kept += (in && (c & kKept)) ? 1u : 0u;
             kept_main += (in && (c & kKept) && !(c & kNew)) ? 1u : 0u;
         }
@@ -523,30 +532,51 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
         {
             int o = (int)(pex & 0x1FFFFF);
 #pragma unroll
-            for (int q = 0; q < kAnnPer; q++) {
+            for (int q = 0; q < PER; q++) {
                 const uint32_t c = (codes[q >> 1] >> (16 * (q & 1))) & 0xFFFFu;
-                if (threadIdx.x * kAnnPer + q < n && (c & kKept)) osrc[o++] = (uint16_t)(c & (kNew | kSlot));
+                if (threadIdx.x * PER + q < n && (c & kKept)) osrc[o++] = (uint16_t)(c & (kNew | kSlot));
             }
         }
         __syncthreads();
-        // the survivors in merged order, coalesced; K_ii of the new determinants
-        // (insert_new_walker, src/annihilation.f90:855)
+        // the survivors in merged order, coalesced, K_ii copied for the kept
+        // main entries; the new determinants' outputs listed (in pcode, free
+        // after the compaction) for their K_ii below
         const int64_t base = s_base;
+        if (threadIdx.x == 0) s_nnew = 0;
+        __syncthreads();
+        uint16_t *newo = pcode;
         for (int o = threadIdx.x; o < (int)tkept; o += kBlock) {
             const uint16_t v = osrc[o];
             const int slot = v & kSlot;
             const Det<W> d = tile_det(slot);
             const int64_t p0v = tpop[slot * R], p1v = R > 1 ? tpop[slot * R + 1] : 0;
-            const double kii = (v & kNew) ? kii_of<W>(s, d, tb) : mkii[ia + slot];
             const int64_t dst = base + o;
+            const bool fresh = (v & kNew) != 0 && dst < b.cap;
+            const uint32_t nb = __ballot_sync(__activemask(), fresh);
+            if (fresh) {
+                const int leader = __ffs(nb) - 1;
+                uint32_t at = 0;
+                if ((threadIdx.x & 31) == leader) at = atomicAdd(&s_nnew, (uint32_t)__popc(nb));
+                at = __shfl_sync(nb, at, leader);
+                newo[at + __popc(nb & lanemask_lt())] = (uint16_t)o;
+            }
             if (dst < b.cap) {
                 store_det<W>(odets, dst, d);
                 opops[dst * R] = p0v;
                 if (R > 1) opops[dst * R + 1] = p1v;
-                okii[dst] = kii;
+                if (!(v & kNew)) okii[dst] = mkii[ia + slot];
                 ap0 += p0v < 0 ? -p0v : p0v;
                 ap1 += p1v < 0 ? -p1v : p1v;
             }
+        }
+        __syncthreads();
+        // K_ii of the new determinants (insert_new_walker, src/annihilation.f90:855),
+        // consecutive threads on consecutive new determinants, so that every lane
+        // of a warp runs the same pair sums
+        const int nnew = (int)s_nnew;
+        for (int k = threadIdx.x; k < nnew; k += kBlock) {
+            const int o = newo[k];
+            okii[base + o] = kii_of<W>(s, tile_det(osrc[o] & kSlot), tb);
         }
         __syncthreads();
     }
@@ -559,8 +589,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
 }
 
 // Dynamic shared memory of k_annihilate.
-__host__ __forceinline__ size_t ann_smem_bytes(size_t fx_bytes, int R, bool initiator) {
-    return fx_bytes + sizeof(int64_t) * (size_t)kAnnTile * (R + (initiator ? 1 : 0));
+__host__ __forceinline__ size_t ann_smem_bytes(size_t fx_bytes, int R, bool initiator, int tile) {
+    return fx_bytes + sizeof(int64_t) * (size_t)tile * (R + (initiator ? 1 : 0));
 }
 
 template <int W>
@@ -571,14 +601,47 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
     const int rows = b.binom_rows, cols = b.binom_cols;
     const size_t hist_smem = sizeof(uint32_t) * kMaxPasses * kRadix +
                              (b.use_rank ? sizeof(uint64_t) * (size_t)rows * cols : 0);
-    if (b.use_rank && b.key_words == 2) k_sort_hist<W, 2, true><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
-    else if (b.use_rank) k_sort_hist<W, 1, true><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
-    else k_sort_hist<W, W, false><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    const int kw = b.key_words == 2 ? 2 : 1;
+    if (b.sort_packed == 1 && kw == 1) k_sort_hist<W, 1, true, 1><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    else if (b.sort_packed == 2 && kw == 1) k_sort_hist<W, 1, true, 2><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    else if (b.sort_packed == 2) k_sort_hist<W, 2, true, 2><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    else if (b.use_rank && kw == 2) k_sort_hist<W, 2, true, 0><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    else if (b.use_rank) k_sort_hist<W, 1, true, 0><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
+    else k_sort_hist<W, W, false, 0><<<b.grid, kBlock, hist_smem, st>>>(b, rows, cols);
     k_sort_offsets<<<1, kRadix, 0, st>>>(b);
     const uint64_t *kin = b.use_rank ? b.skeys : b.sdets;
     const uint32_t *iin = nullptr;
     int o = 0;
-    for (int p = 0; p < b.sort_passes; p++) {
+    if (b.sort_packed) {
+        // packed records: the pass reads records of 16 bytes while the remaining
+        // key and the index need two words, then of 8; the last pass writes the
+        // index alone
+        const int ib = b.sort_ibits;
+        const void *in = b.skeys;
+        for (int p = 0; p < b.sort_passes; p++) {
+            const bool in128 = b.sort_key_bits - kRadixBits * p + ib > 64;
+            const bool last = p == b.sort_passes - 1;
+            const bool out128 = !last && b.sort_key_bits - kRadixBits * (p + 1) + ib > 64;
+            void *out = last ? (void *)b.idx[o] : (void *)b.keys[o];
+            if (in128) {
+                const P128 *ip = static_cast<const P128 *>(in);
+                const size_t sm = PKConf<P128>::smem;
+                if (last) k_onesweep_pk<P128, uint32_t><<<b.sort_grid, kOSThreads, sm, st>>>(b, p, ip, (uint32_t *)out, ib);
+                else if (out128) k_onesweep_pk<P128, P128><<<b.sort_grid, kOSThreads, sm, st>>>(b, p, ip, (P128 *)out, ib);
+                else k_onesweep_pk<P128, P64><<<b.sort_grid, kOSThreads, sm, st>>>(b, p, ip, (P64 *)out, ib);
+            } else {
+                const P64 *ip = static_cast<const P64 *>(in);
+                const size_t sm = PKConf<P64>::smem;
+                if (last) k_onesweep_pk<P64, uint32_t><<<b.sort_grid, kOSThreads, sm, st>>>(b, p, ip, (uint32_t *)out, ib);
+                else k_onesweep_pk<P64, P64><<<b.sort_grid, kOSThreads, sm, st>>>(b, p, ip, (P64 *)out, ib);
+            }
+            in = out;
+            if (last) iin = b.idx[o];
+            o ^= 1;
+        }
+        kin = nullptr;  // the annihilation reads the determinants through the indices
+    }
+    for (int p = 0; p < (b.sort_packed ? 0 : b.sort_passes); p++) {
         if (b.key32)
             k_onesweep<uint32_t, 1><<<b.sort_grid, kOSThreads, OSConf<uint32_t, 1>::smem, st>>>(
                 b, p, reinterpret_cast<const uint32_t *>(kin), iin, reinterpret_cast<uint32_t *>(b.keys[o]),
@@ -596,7 +659,7 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
     if (pm) cudaEventRecord(pm->ev[4], st);
     // merge-path cuts at group boundaries, then one pass over the merged
     // sequence; the second pass runs only after an overflow of the main list
-    const size_t ann_smem = ann_smem_bytes(b.fx_smem_bytes, R, b.sflag != nullptr);
+    const size_t ann_smem = ann_smem_bytes(b.fx_smem_bytes, R, b.sflag != nullptr, ann_tile<W>());
     if (b.use_rank) {
         k_ann_splits<W, true><<<b.splits_grid, kBlock, 0, st>>>(b, cur, kin, iin);
         if (pm) cudaEventRecord(pm->ev[5], st);
@@ -617,19 +680,30 @@ void launch_sort_annihilate(const DevBuffers &b, int W, int R, int cur, cudaStre
 }
 
 int set_annihilate_attributes(const DevBuffers &b) {
-    if (cudaFuncSetAttribute(k_onesweep<uint32_t, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_onesweep_pk<P128, uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PKConf<P128>::smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_onesweep_pk<P128, P128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PKConf<P128>::smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_onesweep_pk<P128, P64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PKConf<P128>::smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_onesweep_pk<P64, uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PKConf<P64>::smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_onesweep_pk<P64, P64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PKConf<P64>::smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_onesweep<uint32_t, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)OSConf<uint32_t, 1>::smem) != cudaSuccess ||
         cudaFuncSetAttribute(k_onesweep<uint64_t, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)OSConf<uint64_t, 1>::smem) != cudaSuccess ||
         cudaFuncSetAttribute(k_onesweep<uint64_t, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)OSConf<uint64_t, 2>::smem) != cudaSuccess)
         return 1;
-    // The largest table any supported system needs (64 spatial orbitals) with
-    // two spaces and initiator flags, so that handles of different systems in
-    // one process never lower the limit another handle's captured graph relies on.
-    const int fx_max = (int)sizeof(int64_t) * fx_table_words(HGPU_SYS_READ_IN, 128, 64);
+    // The largest staged table (32 KB; larger ones are read from global memory)
+    // with two spaces and initiator flags, so that handles of different systems
+    // in one process never lower the limit another handle's captured graph
+    // relies on.
+    const int fx_max = 32768;
     if (b.fx_smem_bytes > (size_t)fx_max) return 1;
-    const int max_bytes = (int)ann_smem_bytes((size_t)fx_max, 2, true);
+    const int max_bytes = (int)ann_smem_bytes((size_t)fx_max, 2, true, ann_tile<1>());
     const void *fns[4] = {(const void *)k_annihilate<1, true>, (const void *)k_annihilate<1, false>,
                           (const void *)k_annihilate<2, true>, (const void *)k_annihilate<2, false>};
     for (const void *f : fns)

@@ -642,10 +642,18 @@ static int alloc_lists(hgpu_handle *h) {
             b.sort_few_values[p] = bits >= kRadixBits ? kRadix : (bits > 0 ? 1 << bits : 1);
             if (p < b.sort_passes && bits <= 5 && b.sort_few_from == b.sort_passes) b.sort_few_from = p;
         }
+        // packed records (key bits and entry index in one or two words) when
+        // they fit the W-word key buffers
+        b.sort_key_bits = key_bits;
+        b.sort_ibits = 1;
+        while (b.sort_ibits < 32 && ((int64_t)1 << b.sort_ibits) < b.scap) b.sort_ibits++;
+        b.sort_packed = 0;
+        if (b.use_rank && key_bits + b.sort_ibits <= 64 * W) b.sort_packed = key_bits + b.sort_ibits <= 64 ? 1 : 2;
         b.binom = nullptr;
         if (b.use_rank) {
             if ((rc = upload(h, binom.data(), binom.size(), &b.binom))) return rc;
-            if ((rc = dalloc(h, &b.skeys, (size_t)b.scap * b.key_words))) return rc;
+            const int words = b.sort_packed ? b.sort_packed : b.key_words;
+            if ((rc = dalloc(h, &b.skeys, (size_t)b.scap * words))) return rc;
         }
     }
     if ((rc = dalloc(h, &b.ghist, (size_t)kMaxPasses * kRadix))) return rc;
@@ -660,7 +668,7 @@ static int alloc_lists(hgpu_handle *h) {
     }
     {
         // tiles of the annihilation over the merged main and spawned lists
-        size_t tiles = ((size_t)b.cap + (size_t)b.scap) / kAnnTile + 2;
+        size_t tiles = ((size_t)b.cap + (size_t)b.scap) / kAnnTileMin + 2;
         if ((rc = dalloc(h, &b.msplit, 3 * (tiles + 1)))) return rc;
         if ((rc = dalloc(h, &b.seg_status, tiles))) return rc;
         CK(cudaMemset(b.seg_status, 0, sizeof(uint64_t) * tiles));
@@ -696,7 +704,7 @@ static int alloc_lists(hgpu_handle *h) {
         b.grid = clampi(b.cap / 4096, 8, std::min(4 * sms, kMaxBlocks));
         b.spawn_grid = clampi(b.scap / 1024, 8, 8 * sms);
         b.sort_grid = clampi(b.scap / OSConf<uint64_t, 1>::tile + 1, 4, 4 * sms);  // 256 threads, <= 48 KB shared memory
-        b.splits_grid = clampi(((b.cap + b.scap) / kAnnTile + 3 + 7) / 8, 1, 4 * sms);  // a warp per cut
+        b.splits_grid = clampi(((b.cap + b.scap) / kAnnTileMin + 3 + 7) / 8, 1, 4 * sms);  // a warp per cut
     }
     if ((rc = dalloc(h, &b.state, 1))) return rc;
     CK(cudaMemset(b.state, 0, sizeof(DevState)));
@@ -860,7 +868,11 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) rc = HGPU_ERR_CUDA;
     if (!rc) rc = build_system(h, sys);
     if (!rc) {
-        h->b.fx_smem_bytes = sizeof(int64_t) * (size_t)fx_table_words(sys->kind, sys->nbasis, sys->norb);
+        // exact-diagonal tables above 32 KB (molecules beyond ~45 orbitals) stay in
+        // global memory, where the L1 cache holds them, so that they do not cost
+        // the annihilation kernel resident blocks
+        const size_t fx = sizeof(int64_t) * (size_t)fx_table_words(sys->kind, sys->nbasis, sys->norb);
+        h->b.fx_smem_bytes = fx <= 32768 ? fx : 0;
         if (set_kernel_attributes(h->b)) {
             last_error_text(cudaGetErrorString(cudaGetLastError()), "cudaFuncSetAttribute");
             rc = HGPU_ERR_CUDA;
@@ -1680,8 +1692,22 @@ int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int
         counts[4] = st.n_main;
         counts[5] = launches_per_cycle(h->b);
         counts[6] = h->b.sort_passes;
-        // bytes one radix pass reads (and writes) per spawned entry: key and index
-        counts[7] = (h->b.key32 ? 4 : 8 * h->b.key_words) + 4;
+        // bytes the radix passes read and write per spawned entry, all passes:
+        // packed records (16 bytes while the key and the index need two words,
+        // then 8, the last pass writing the 4-byte index) or key and index
+        const DevBuffers &b = h->b;
+        int64_t moved = 0;
+        for (int p = 0; p < b.sort_passes; p++) {
+            if (b.sort_packed) {
+                const int in = b.sort_key_bits - kRadixBits * p + b.sort_ibits > 64 ? 16 : 8;
+                const bool last = p == b.sort_passes - 1;
+                const int out = last ? 4 : (b.sort_key_bits - kRadixBits * (p + 1) + b.sort_ibits > 64 ? 16 : 8);
+                moved += in + out;
+            } else {
+                moved += 2 * ((b.key32 ? 4 : 8 * b.key_words) + 4);
+            }
+        }
+        counts[7] = moved;
     }
     return HGPU_OK;
 }

@@ -36,7 +36,14 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortItems = 8;    // keys per thread per radix tile
 constexpr int kMaxBlocks = 1024; // upper bound of the fixed grid (partials arrays)
-constexpr int kAnnTile = 2048;   // merged elements per annihilation tile (hgpu_annihilate.cuh)
+// Merged elements per annihilation tile (hgpu_annihilate.cu): 2048 for one-word
+// determinants, 1024 for two-word ones, whose tiles take twice the shared
+// memory per element; kAnnTileMin sizes the per-tile arrays.
+template <int W>
+constexpr int ann_tile() {
+    return W == 1 ? 2048 : 1024;
+}
+constexpr int kAnnTileMin = 1024;
 // Bloom threshold of FCIQMC in particles: init_bloom_stats_t's default with
 // bloom_mode_fixedn (src/fciqmc.f90:214, src/bloom_handler.F90:37).
 constexpr int64_t kBloomThreshold = 3;
@@ -115,6 +122,10 @@ struct DevBuffers {
     int sort_few_from;          // first pass whose digits take at most 32 values
     int sort_few_values[16];    // number of digit values of each such pass
     int sort_grid;      // blocks of the radix passes
+    int sort_packed;    // ranks sorted as packed records (hgpu_sort.cuh, P64 / P128): 0 no, else the
+                        // words of the first record (1 or 2)
+    int sort_key_bits;  // bits of the rank keys
+    int sort_ibits;     // bits of the entry index in a packed record
     // annihilation (hgpu_annihilate.cuh)
     int64_t *msplit;       // per tile boundary: main index, spawned index, spawned index at the group boundary
     uint64_t *seg_status;  // per annihilation tile: look-back status word
@@ -150,7 +161,9 @@ struct DevBuffers {
     int grid;               // blocks of the streaming kernels
     int spawn_grid;         // blocks of the spawning kernel
     int sort_passes;
-    size_t fx_smem_bytes;  // exact-diagonal tables staged by the annihilation tiles
+    size_t fx_smem_bytes;  // exact-diagonal tables staged by the annihilation tiles (0: read
+                           // through the L1 cache from global memory, for tables too large to
+                           // stage without costing resident blocks)
     int nk;                 // hub_k: number of k-points (shared-memory tables)
 };
 

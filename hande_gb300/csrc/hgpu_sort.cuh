@@ -45,6 +45,40 @@ __device__ __forceinline__ uint32_t os_digit(const uint32_t *k, int shift) {
     return (k[shift >> 5] >> (shift & 31)) & (kRadix - 1);
 }
 
+// Packed records of the rank sort.  A record holds the key bits that earlier
+// passes have not consumed, shifted down so that the digit of the next pass is
+// its lowest byte, and the entry's index in the top `ib` bits: one 64-bit word
+// (P64) or two (P128, low word first).  k_sort_hist writes the first records
+// (rank and index); a pass ranks the lowest byte and writes the record shifted
+// by one digit -- the consumed bits are not moved again -- or, after the last
+// pass, the index alone.  The host picks P64 once the remaining key and the
+// index fit one word, so later passes move 8 bytes per entry instead of 16.
+struct P64 {
+    uint64_t v;
+};
+struct P128 {
+    uint64_t lo, hi;
+};
+__device__ __forceinline__ uint32_t pk_digit(const P64 &r) { return (uint32_t)r.v & (kRadix - 1); }
+__device__ __forceinline__ uint32_t pk_digit(const P128 &r) { return (uint32_t)r.lo & (kRadix - 1); }
+__device__ __forceinline__ void pk_out(const P64 &r, int ib, uint32_t &o) { o = (uint32_t)(r.v >> (64 - ib)); }
+__device__ __forceinline__ void pk_out(const P128 &r, int ib, uint32_t &o) { o = (uint32_t)(r.hi >> (64 - ib)); }
+__device__ __forceinline__ void pk_out(const P64 &r, int ib, P64 &o) {
+    const uint64_t km = ~0ull >> ib;  // key bits of the word
+    o.v = ((r.v & km) >> kRadixBits) | (r.v & ~km);
+}
+__device__ __forceinline__ void pk_out(const P128 &r, int ib, P128 &o) {
+    const uint64_t km = ~0ull >> ib;
+    const uint64_t hk = r.hi & km;
+    o.lo = (r.lo >> kRadixBits) | (hk << (64 - kRadixBits));
+    o.hi = (hk >> kRadixBits) | (r.hi & ~km);
+}
+// the remaining key fits below the index (the host's choice of P64)
+__device__ __forceinline__ void pk_out(const P128 &r, int ib, P64 &o) {
+    const uint64_t km = ~0ull >> ib;
+    o.v = (r.lo >> kRadixBits) | ((r.hi & km) << (64 - kRadixBits)) | (r.hi & ~km);
+}
+
 // Lanes of `mask` whose 8-bit digit equals this lane's: one ballot per digit
 // bit (cheaper on this GPU than match.any).
 __device__ __forceinline__ uint32_t warp_peers8(uint32_t mask, uint32_t d) {
@@ -143,7 +177,8 @@ __device__ __forceinline__ unsigned __int128 det_rank128(const Det<W> &f, const 
 
 // Sort keys of the spawned list (ranks into b.skeys, when ranks are used) and
 // the digit histograms of every pass, added into b.ghist[pass][digit].
-template <int W, int KW, bool RANK>
+// PACK 1 / 2: the ranks are written as P64 / P128 records with the index i.
+template <int W, int KW, bool RANK, int PACK>
 __global__ void __launch_bounds__(kBlock) k_sort_hist(DevBuffers b, int rows, int cols) {
     extern __shared__ uint64_t hist_smem[];
     uint32_t *h = reinterpret_cast<uint32_t *>(hist_smem);  // [passes][kRadix]
@@ -172,7 +207,25 @@ __global__ void __launch_bounds__(kBlock) k_sort_hist(DevBuffers b, int rows, in
             if (i >= n) break;
             const Det<W> &f = fs[r];
             uint64_t key[KW];
-            if (RANK && KW == 2) {
+            if (PACK) {
+                uint64_t lo, hi = 0;
+                if (KW == 2) {
+                    const unsigned __int128 r = det_rank128<W>(f, binom, cols, b.sort_na, b.sort_nb, bad);
+                    lo = (uint64_t)r;
+                    hi = (uint64_t)(r >> 64);
+                } else {
+                    lo = det_rank<W>(f, binom, cols, b.use_rank, b.sort_na, b.sort_nb, bad);
+                }
+                key[0] = lo;
+                key[KW - 1] = KW == 2 ? hi : lo;
+                const uint64_t ix = (uint64_t)i << (64 - b.sort_ibits);
+                if (PACK == 1) {
+                    b.skeys[i] = lo | ix;
+                } else {
+                    b.skeys[2 * i] = lo;
+                    b.skeys[2 * i + 1] = hi | ix;
+                }
+            } else if (RANK && KW == 2) {
                 const unsigned __int128 r = det_rank128<W>(f, binom, cols, b.sort_na, b.sort_nb, bad);
                 key[0] = (uint64_t)r;
                 key[KW - 1] = (uint64_t)(r >> 64);
@@ -358,6 +411,138 @@ __global__ void __launch_bounds__(kOSThreads, 4) k_onesweep(DevBuffers b, int pa
 #pragma unroll
                 for (int w = 0; w < KW; w++) keys_out[pos * KW + w] = k[w];
                 idx_out[pos] = sidx[j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// One stable pass over packed records (see P64 / P128): the digit is the
+// record's lowest byte; OUT is the next pass's record or, after the last pass,
+// the 32-bit index.  Tiles, ranking and look-back as in k_onesweep.
+template <typename IN>
+struct PKConf {
+    static constexpr int items = sizeof(IN) == 8 ? 12 : 6;
+    static constexpr int tile = kOSThreads * items;
+    static constexpr size_t smem = (size_t)tile * sizeof(IN);
+};
+
+template <typename IN, typename OUT>
+__global__ void __launch_bounds__(kOSThreads, 4) k_onesweep_pk(DevBuffers b, int pass, const IN *recs_in,
+                                                            OUT *recs_out, int ib) {
+    constexpr int ITEMS = PKConf<IN>::items;
+    constexpr int TILE = PKConf<IN>::tile;
+    constexpr int NW = kOSThreads / 32;
+    extern __shared__ uint64_t os_smem[];
+    IN *srec = reinterpret_cast<IN *>(os_smem);  // [TILE], in digit order
+    __shared__ uint32_t wcnt[NW][kRadix];
+    __shared__ uint32_t lstart[kRadix], gbase[kRadix];
+    __shared__ uint32_t s_tile;
+    DevState *st = b.state;
+    const int64_t n = st->n_spawn;
+    const int64_t ntiles = (n + TILE - 1) / TILE;
+    const uint32_t epoch = os_epoch(*b.os_epoch, pass);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int d = threadIdx.x;  // digit owned in the look-back
+    uint64_t *status = b.lookback;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&st->os_ticket[pass], 1u);
+#pragma unroll
+        for (int w = 0; w < NW; w++) wcnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        const int64_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const int64_t t0 = tile * TILE;
+        IN rv[ITEMS];
+        uint32_t off[ITEMS], dg[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            const int64_t e = t0 + (int64_t)(warp * ITEMS + r) * 32 + lane;
+            if (e < n) rv[r] = recs_in[e];
+        }
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            const int64_t e = t0 + (int64_t)(warp * ITEMS + r) * 32 + lane;
+            const bool valid = e < n;
+            const uint32_t mask = __ballot_sync(FULL_MASK, valid);
+            dg[r] = 0xFFFFFFFFu;
+            if (valid) {
+                const uint32_t dd = pk_digit(rv[r]);
+                dg[r] = dd;
+                const uint32_t peers = warp_peers8(mask, dd);
+                const int leader = __ffs(peers) - 1;
+                uint32_t old = 0;
+                if (lane == leader) {
+                    old = wcnt[warp][dd];
+                    wcnt[warp][dd] = old + __popc(peers);
+                }
+                old = __shfl_sync(mask, old, leader);
+                off[r] = old + __popc(peers & lanemask_lt());
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            const uint32_t c = wcnt[w][d];
+            wcnt[w][d] = cnt;
+            cnt += c;
+        }
+        volatile uint64_t *my = status + tile * kRadix + d;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            *my = os_word(kOSPrefix, epoch, cnt);
+        } else {
+            *my = os_word(kOSAggregate, epoch, cnt);
+            int64_t k = tile - 1;
+            int spins = 0;
+            bool done = false;
+            while (!done) {
+                uint64_t v[kOSLook];
+#pragma unroll
+                for (int u = 0; u < kOSLook; u++)
+                    v[u] = k - u >= 0 ? *(volatile uint64_t *)(status + (k - u) * kRadix + d) : 0;
+                int u = 0;
+                for (; u < kOSLook && k - u >= 0; u++) {
+                    const uint32_t ve = (uint32_t)(v[u] >> 32) & 0x3FFFFFFFu;
+                    const uint64_t fl = v[u] >> 62;
+                    if (ve != (epoch & 0x3FFFFFFFu) || fl == 0) break;  // not published yet
+                    excl += (uint32_t)v[u];
+                    if (fl == kOSPrefix) {
+                        done = true;
+                        break;
+                    }
+                }
+                if (done) break;
+                k -= u;
+                if (u == 0) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(&st->error_flags, HGPU_FLAG_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            *my = os_word(kOSPrefix, epoch, excl + cnt);
+        }
+        gbase[d] = b.gofs[pass * kRadix + d] + excl;
+        uint32_t ltot;
+        lstart[d] = block_exclusive_scan<uint32_t>(cnt, &ltot);
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++)
+            if (dg[r] != 0xFFFFFFFFu) srec[lstart[dg[r]] + wcnt[warp][dg[r]] + off[r]] = rv[r];
+        __syncthreads();
+        const int tn = (int)min((int64_t)TILE, n - t0);
+        for (int j = threadIdx.x; j < tn; j += kOSThreads) {
+            const IN rec = srec[j];
+            const uint32_t dd = pk_digit(rec);
+            const int64_t pos = (int64_t)gbase[dd] + (j - (int64_t)lstart[dd]);
+            if (pos < n) {
+                OUT o;
+                pk_out(rec, ib, o);
+                recs_out[pos] = o;
             }
         }
         __syncthreads();

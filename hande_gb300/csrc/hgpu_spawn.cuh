@@ -108,8 +108,16 @@ __device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTab
                                             parent_det, nspawn_rdm);
 }
 
+// Resident blocks per SM the spawning kernel is compiled for: four (at most 64
+// registers, half the SM's warps) for the uniform generators, whose code fits
+// that budget without spilling; the others keep the compiler's choice.
+template <int KIND>
+constexpr int spawn_min_blocks() {
+    return (KIND == HGPU_SYS_HUB_K || KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm) ? 4 : 1;
+}
+
 template <int W, int KIND, typename Real, bool RDM>
-__global__ void __launch_bounds__(kBlock) k_spawn(DevBuffers b, int R, int cur) {
+__global__ void __launch_bounds__(kBlock, spawn_min_blocks<KIND>()) k_spawn(DevBuffers b, int R, int cur) {
     __shared__ DevSys s;
     __shared__ SpawnQueue queue[kBlock / 32];
     extern __shared__ uint8_t smem[];

@@ -209,7 +209,7 @@ class Engine:
         self._check(self.L.hgpu_profile_cycle(self.h, _p(ms, C.c_double), 7, _p(cnt, C.c_int64)),
                     "hgpu_profile_cycle")
         keys = ["N", "attempts", "spawned", "unique", "N_after", "launches_per_cycle", "sort_passes",
-                "sort_bytes_per_entry_pass"]
+                "sort_bytes_per_entry"]
         return dict(zip(self.PHASES, ms.tolist())), dict(zip(keys, cnt.tolist()))
 
     def eval_diagonal(self, dets):

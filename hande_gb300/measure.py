@@ -65,8 +65,7 @@ def roofline_figures(phases: dict, counts: dict, W: int, R: int, initiator: bool
     ann_bytes = 3 * S * Es + 2 * U * Es + N * Em + N2 * Em
     ach2 = ann_bytes / t_ann / 1e9 if t_ann > 0 else 0.0
     passes = counts.get("sort_passes", 0)
-    kb = counts.get("sort_bytes_per_entry_pass", 0)
-    sort_moved = 2 * passes * kb * S  # every pass reads and writes key and index of every entry
+    sort_moved = counts.get("sort_bytes_per_entry", 0) * S  # what the passes read and write
     annih = {"phases": ["sort", "splits", "annihilate"], "bound": "hbm", "achieved": ach2, "peak": peak,
              "unit": "GB/s", "frac": ach2 / peak, "algorithmic_bytes": ann_bytes, "seconds": t_ann,
              "peak_source": peak_src,
@@ -74,7 +73,7 @@ def roofline_figures(phases: dict, counts: dict, W: int, R: int, initiator: bool
              "sort_algorithmic_bytes": 2 * S * Es,
              "sort_achieved_gbs": sort_moved / t_sort / 1e9 if t_sort > 0 else 0.0,
              "note": "the one-pass annihilation kernel moves its algorithmic bytes once; sort_bytes_moved is what "
-                     "the radix passes read and write (passes x 2 x key-and-index bytes x S)"}
+                     "the radix passes read and write (packed key-and-index records, summed over the passes, x S)"}
     pa = prof.get("k_annihilate")
     if pa:
         annih["from_profile"] = dict(pa, source=os.path.relpath(PROFILE_FIGURES, ROOT))

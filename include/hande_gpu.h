@@ -336,8 +336,8 @@ int32_t hgpu_self_annihilate_noalloc(const int64_t *d_sdata, int64_t n, int32_t 
  * lib/local/parallel.F90:80-88).  phase_ms[0..6]: prep (E_proj, nattempts,
  * death), attempt scan, spawning, sort, self-annihilation, merge, end of
  * cycle.  counts[0..7] (may be NULL): N before, attempts, spawned, unique
- * spawned, N after, kernel launches per cycle, radix passes, bytes one radix
- * pass reads (and writes again) per spawned entry. */
+ * spawned, N after, kernel launches per cycle, radix passes, bytes the radix
+ * passes read and write per spawned entry (all passes together). */
 int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int64_t *counts);
 
 /* Batches: many independent calculations advanced together.  HANDE runs one

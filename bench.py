@@ -485,11 +485,14 @@ def batched_instances(n=128, seed=4):
     return out
 
 
-def batched_measure(steps, equil_cycles=150):
+def batched_measure(steps, equil_cycles=150, tune=True):
     """config 4: every instance starts with its target population on the
     reference determinant; `equil_cycles` untimed cycles (a report after each,
-    so that the shift acts every cycle) spread it out, then `steps` batch
-    cycles are timed (one graph launch each for all instances)."""
+    so that the shift acts every cycle) spread it out; the launch shapes are
+    tuned on those lists (hande_gb300.autotune, untimed); then `steps` batch
+    cycles are timed (one graph launch each for all instances), device time
+    from the CUDA events around the batch's graph launches."""
+    from hande_gb300.autotune import BatchTuner
     from hande_gb300.engine import Batch, Engine
     inst = batched_instances()
     engines = [Engine(s, cfg) for s, cfg, _ in inst]
@@ -504,6 +507,13 @@ def batched_measure(steps, equil_cycles=150):
     targets = sum(m["target"] for _, _, m in inst)
     walkers = sum(rp.nparticles[0] for rp in reps)
     states = sum(rp.nstates for rp in reps)
+    tuned = None
+    if tune:
+        t0 = time.perf_counter()
+        tuner = BatchTuner(batch, engines, trial_cycles=3)
+        choice, base_ms, best_ms = tuner.tune()
+        tuned = {"default_ms_per_cycle": base_ms, "tuned_ms_per_cycle": best_ms, "trials": len(tuner.table),
+                 "classes": tuner.summary(), "search_s": time.perf_counter() - t0}
     batch.run_cycles(3)  # warm-up
     for e in engines:
         e.end_report()
@@ -511,6 +521,7 @@ def batched_measure(steps, equil_cycles=150):
     batch.run_cycles(steps)  # synchronises at the end
     dt = time.perf_counter() - t0
     reps = [e.end_report() for e in engines]
+    dev_s = reps[0].device_ms * 1e-3  # every handle of the batch carries the batch's device time
     att = sum(rp.nattempts for rp in reps)
     flags = 0
     for rp in reps:
@@ -518,11 +529,13 @@ def batched_measure(steps, equil_cycles=150):
     batch.close()
     for e in engines:
         e.close()
-    return {"workload": BATCH_WORKLOAD, "instances": len(inst), "value": att / dt, "unit": "attempts/s",
-            "ms_per_step": 1e3 * dt / steps, "steps": steps, "walkers": walkers, "states": int(states),
+    return {"workload": BATCH_WORKLOAD, "instances": len(inst), "value": att / dev_s, "unit": "attempts/s",
+            "ms_per_step": 1e3 * dev_s / steps, "steps": steps, "walkers": walkers, "states": int(states),
             "target_walkers": targets, "instances_shift_varying": varying, "equilibration_cycles": equil_cycles,
-            "error_flags": flags, "dtype": "int64 walkers, f64",
-            "timing": "host wall clock around hgpu_batch_run_cycles (graph launches and the final synchronisation)"}
+            "error_flags": flags, "dtype": "int64 walkers, f64", "launch_tuning": tuned,
+            "host_wall_value": att / dt,
+            "timing": "device: CUDA events around the batch's graph launches (hgpu_batch_run_cycles); "
+                      "host_wall_value: host clock around the call"}
 
 
 PRECISION_WORKLOAD = ("config3: synthetic molecule M=48 nel=16 C1 (96 spin orbitals, 2-word determinants), heat-bath "

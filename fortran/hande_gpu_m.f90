@@ -61,6 +61,10 @@ module hande_gpu_m
         real(c_double) :: tot_bloom, max_bloom
     end type hgpu_report
 
+    type, bind(c) :: hgpu_launch
+        integer(c_int32_t) :: spawn_chunk, spawn_blocks, stream_blocks, sort_blocks
+    end type hgpu_launch
+
     type, bind(c) :: hgpu_state
         integer(c_int64_t) :: iteration
         real(c_double) :: shift(HGPU_MAX_SPACES)
@@ -226,6 +230,19 @@ module hande_gpu_m
             integer(c_int64_t), intent(out) :: n_out
             type(c_ptr), value :: stream
         end function hgpu_self_annihilate_noalloc
+
+        ! Launch shape of a handle's kernels (speed only; results do not depend on it).
+        integer(c_int32_t) function hgpu_get_launch(h, l) bind(c, name='hgpu_get_launch')
+            import :: c_ptr, c_int32_t, hgpu_launch
+            type(c_ptr), value :: h
+            type(hgpu_launch), intent(out) :: l
+        end function hgpu_get_launch
+
+        integer(c_int32_t) function hgpu_set_launch(h, l) bind(c, name='hgpu_set_launch')
+            import :: c_ptr, c_int32_t, hgpu_launch
+            type(c_ptr), value :: h
+            type(hgpu_launch), intent(in) :: l
+        end function hgpu_set_launch
 
         ! Batches: many handles advanced together, one graph launch per cycle.
         integer(c_int32_t) function hgpu_batch_create(handles, n, batch) bind(c, name='hgpu_batch_create')

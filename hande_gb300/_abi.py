@@ -111,6 +111,15 @@ class HgpuReport(C.Structure):
         return r
 
 
+class HgpuLaunch(C.Structure):
+    """Launch shape of a handle's kernels (hgpu_launch)."""
+    _fields_ = [("spawn_chunk", C.c_int32), ("spawn_blocks", C.c_int32), ("stream_blocks", C.c_int32),
+                ("sort_blocks", C.c_int32)]
+
+    def as_tuple(self):
+        return (int(self.spawn_chunk), int(self.spawn_blocks), int(self.stream_blocks), int(self.sort_blocks))
+
+
 class HgpuState(C.Structure):
     _fields_ = [
         ("iteration", C.c_int64), ("shift", C.c_double * MAX_SPACES),

@@ -49,6 +49,7 @@ struct hgpu_handle {
     int64_t iter;
     int64_t ss_iter;  // iteration at whose start the deterministic space is built
     int64_t ss_gen = 0;  // number of deterministic spaces built or dropped so far
+    int64_t launch_gen = 0;  // number of hgpu_set_launch calls (batch graphs follow it)
     cudaEvent_t ev0, ev1;
     double report_ms;
     std::vector<void *> allocs;
@@ -705,6 +706,7 @@ static int alloc_lists(hgpu_handle *h) {
         b.spawn_grid = clampi(b.scap / 1024, 8, 8 * sms);
         b.sort_grid = clampi(b.scap / OSConf<uint64_t, 1>::tile + 1, 4, 4 * sms);  // 256 threads, <= 48 KB shared memory
         b.splits_grid = clampi(((b.cap + b.scap) / kAnnTileMin + 3 + 7) / 8, 1, 4 * sms);  // a warp per cut
+        b.spawn_chunk = 256;
     }
     if ((rc = dalloc(h, &b.state, 1))) return rc;
     CK(cudaMemset(b.state, 0, sizeof(DevState)));
@@ -1256,6 +1258,7 @@ struct hgpu_batch {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     std::vector<int> parity[2];  // buffer parity of every handle each graph was built for
+    std::vector<int64_t> gens;   // launch shapes (launch_gen) the graphs were built with
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -1338,6 +1341,12 @@ int32_t hgpu_batch_run_cycles(hgpu_batch *b, int32_t ncycles) {
         flip[i] = 1 - par[i];
         CK(cudaStreamSynchronize(b->hs[i]->stream));  // earlier per-handle work
     }
+    std::vector<int64_t> gens(b->hs.size());
+    for (size_t i = 0; i < b->hs.size(); i++) gens[i] = b->hs[i]->launch_gen;
+    if (gens != b->gens) {
+        batch_free_graphs(b);
+        b->gens = gens;
+    }
     int slot;
     if (b->exec[0] && b->parity[0] == par) {
         slot = 0;
@@ -1372,6 +1381,30 @@ int32_t hgpu_batch_run_cycles(hgpu_batch *b, int32_t ncycles) {
         if (rc && !first) first = rc;
     }
     return first;
+}
+
+int32_t hgpu_get_launch(hgpu_handle *h, hgpu_launch *out) {
+    if (!h || !out) return HGPU_ERR_INVALID;
+    out->spawn_chunk = h->b.spawn_chunk;
+    out->spawn_blocks = h->b.spawn_grid;
+    out->stream_blocks = h->b.grid;
+    out->sort_blocks = h->b.sort_grid;
+    return HGPU_OK;
+}
+
+int32_t hgpu_set_launch(hgpu_handle *h, const hgpu_launch *in) {
+    if (!h || !in) return HGPU_ERR_INVALID;
+    if (in->spawn_chunk < 32 || in->spawn_chunk > kSpawnChunk || in->spawn_chunk % 32 != 0 || in->spawn_blocks < 1 ||
+        in->stream_blocks < 1 || in->stream_blocks > kMaxBlocks || in->sort_blocks < 1)
+        return HGPU_ERR_INVALID;
+    CK(cudaStreamSynchronize(h->stream));
+    h->b.spawn_chunk = in->spawn_chunk;
+    h->b.spawn_grid = in->spawn_blocks;
+    h->b.grid = in->stream_blocks;
+    h->b.sort_grid = in->sort_blocks;
+    invalidate_graphs(h);
+    h->launch_gen++;
+    return HGPU_OK;
 }
 
 int32_t hgpu_batch_destroy(hgpu_batch *b) {

@@ -10,6 +10,10 @@
 namespace hgpu {
 
 constexpr int kBlock = 256;      // threads per block of the streaming kernels
+// Largest chunk of attempts a warp claims from the spawning kernel's work
+// counter (its queue size); the chunk of a handle (DevBuffers::spawn_chunk) is
+// a multiple of 32 up to it.
+constexpr int kSpawnChunk = 8 * 32;
 // Generator kind of the spawning kernels (a template parameter, so that each
 // kernel holds the code of one generator): HGPU_SYS_HUB_K, HGPU_SYS_READ_IN
 // (molecular, uniform renorm generator) or one of the kinds below.
@@ -158,8 +162,9 @@ struct DevBuffers {
     int64_t *part_i;        // kMaxBlocks * 4 (abs pop per space, ndeath)
     DevState *state;
     DevSys *sys;
-    int grid;               // blocks of the streaming kernels
+    int grid;               // blocks of the streaming kernels (at most kMaxBlocks)
     int spawn_grid;         // blocks of the spawning kernel
+    int spawn_chunk;        // attempts a warp of the spawning kernel claims at a time (32..256, x32)
     int sort_passes;
     size_t fx_smem_bytes;  // exact-diagonal tables staged by the annihilation tiles (0: read
                            // through the L1 cache from global memory, for tables too large to

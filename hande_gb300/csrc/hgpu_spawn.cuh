@@ -21,8 +21,6 @@ __device__ __forceinline__ int64_t upper_bound_off(const int64_t *off, int64_t n
     return lo;
 }
 
-// Attempts per chunk a warp claims from the spawning kernel's work counter.
-constexpr int kSpawnChunk = 8 * 32;
 
 // A warp's chunk of attempts: (parent, space) slot, attempt number in the slot
 // and, for generators whose first draw chooses a single or a double excitation,
@@ -139,7 +137,7 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<KIND>()) k_spawn(DevB
     // converged (a tenth of the attempts are singles, with their own code)
     constexpr bool drew = KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm || KIND == kKindHeatBathUniform ||
                           KIND == kKindPowerPitzerOcc || KIND == kKindPowerPitzerRef;
-    // Each warp claims chunks of kSpawnChunk consecutive attempts.  The (parent,
+    // Each warp claims chunks of b.spawn_chunk consecutive attempts.  The (parent,
     // space) slot of attempt a is the first k with aoff[k] > a; one binary search
     // per chunk finds the slot of its first attempt, and every later step of 32
     // attempts searches a window of 32 slots starting at the slot of the previous
@@ -147,10 +145,10 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<KIND>()) k_spawn(DevB
     // a window holds no slot for an attempt (runs of zero-attempt slots).
     for (;;) {
         unsigned long long cbase = 0;
-        if (lane == 0) cbase = atomicAdd((unsigned long long *)&st->spawn_next, (unsigned long long)kSpawnChunk);
+        if (lane == 0) cbase = atomicAdd((unsigned long long *)&st->spawn_next, (unsigned long long)b.spawn_chunk);
         cbase = __shfl_sync(FULL_MASK, cbase, 0);
         if ((int64_t)cbase >= A) break;
-        const int64_t cend = min((int64_t)cbase + kSpawnChunk, A);
+        const int64_t cend = min((int64_t)cbase + b.spawn_chunk, A);
         int64_t k0 = 0;
         if (lane == 0) k0 = upper_bound_off(b.aoff, NR, (int64_t)cbase);
         k0 = __shfl_sync(FULL_MASK, k0, 0);

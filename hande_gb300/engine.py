@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from ._abi import (STATUS_TEXT, HgpuConfig, HgpuReport, HgpuState, HgpuSystem, PackedSystem,
+from ._abi import (STATUS_TEXT, HgpuConfig, HgpuLaunch, HgpuReport, HgpuState, HgpuSystem, PackedSystem,
                    make_config)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -24,6 +24,7 @@ EXPORTS = [
     "hgpu_restore", "hgpu_eval_excitations", "hgpu_annihilate_fixed", "hgpu_eval_diagonal",
     "hgpu_profile_cycle", "hgpu_snapshot", "hgpu_self_annihilate_noalloc",
     "hgpu_batch_create", "hgpu_batch_run_cycles", "hgpu_batch_destroy", "hgpu_rdm_download",
+    "hgpu_get_launch", "hgpu_set_launch",
 ]
 
 
@@ -69,6 +70,8 @@ def load_library(path: str = LIB_PATH):
     L.hgpu_eval_diagonal.argtypes = [vp, P(C.c_int64), C.c_int64, P(C.c_double)]
     L.hgpu_profile_cycle.argtypes = [vp, P(C.c_double), C.c_int32, P(C.c_int64)]
     L.hgpu_snapshot.argtypes = [vp, C.c_int32]
+    L.hgpu_get_launch.argtypes = [vp, P(HgpuLaunch)]
+    L.hgpu_set_launch.argtypes = [vp, P(HgpuLaunch)]
     L.hgpu_self_annihilate_noalloc.argtypes = [vp, C.c_int64, C.c_int32, C.c_int32, vp, P(C.c_int64), vp]
     for name in EXPORTS:
         if name != "hgpu_error_string":
@@ -199,6 +202,16 @@ class Engine:
 
     def snapshot(self, restore: bool = False):
         self._check(self.L.hgpu_snapshot(self.h, 1 if restore else 0), "hgpu_snapshot")
+
+    def launch(self) -> HgpuLaunch:
+        """The launch shape of the handle's kernels (spawn chunk and block counts)."""
+        x = HgpuLaunch()
+        self._check(self.L.hgpu_get_launch(self.h, C.byref(x)), "hgpu_get_launch")
+        return x
+
+    def set_launch(self, spawn_chunk, spawn_blocks, stream_blocks, sort_blocks):
+        x = HgpuLaunch(int(spawn_chunk), int(spawn_blocks), int(stream_blocks), int(sort_blocks))
+        self._check(self.L.hgpu_set_launch(self.h, C.byref(x)), "hgpu_set_launch")
 
     PHASES = ["prep", "attempt_scan", "spawn", "sort", "splits", "annihilate", "end"]
 

@@ -340,6 +340,29 @@ int32_t hgpu_self_annihilate_noalloc(const int64_t *d_sdata, int64_t n, int32_t 
  * passes read and write per spawned entry (all passes together). */
 int32_t hgpu_profile_cycle(hgpu_handle *h, double *phase_ms, int32_t nphase, int64_t *counts);
 
+/* Launch shape of a handle's kernels (no counterpart in the reference, which
+ * runs on CPU cores).  The results do not depend on it -- every count, sum and
+ * random stream of a cycle is independent of how the work is split -- only the
+ * speed does, so a caller (or an autotuner over a batch of handles) may change
+ * it between cycles.  hgpu_create picks it from the list capacities.
+ *   spawn_chunk    attempts a warp of the spawning kernel claims at a time:
+ *                  32 to 256, a multiple of 32 (small chunks balance small
+ *                  calculations, large ones cut the claims of large ones)
+ *   spawn_blocks   blocks of the spawning kernel, >= 1
+ *   stream_blocks  blocks of the streaming kernels (parent pass, scans,
+ *                  annihilation, RDM), 1 to 1024
+ *   sort_blocks    blocks of the radix-sort passes, >= 1
+ * hgpu_set_launch rejects values outside these ranges (HGPU_ERR_INVALID). */
+typedef struct hgpu_launch {
+    int32_t spawn_chunk;
+    int32_t spawn_blocks;
+    int32_t stream_blocks;
+    int32_t sort_blocks;
+} hgpu_launch;
+
+int32_t hgpu_get_launch(hgpu_handle *h, hgpu_launch *out);
+int32_t hgpu_set_launch(hgpu_handle *h, const hgpu_launch *in);
+
 /* Batches: many independent calculations advanced together.  HANDE runs one
  * calculation per process; a batch groups already-created handles (different
  * systems, sizes, seeds, replicas) on one device and advances all of them by

@@ -18,7 +18,7 @@ from tests.conftest import ROOT
 
 HEADER = open(os.path.join(ROOT, "include", "hande_gpu.h")).read()
 FORTRAN = open(os.path.join(ROOT, "fortran", "hande_gpu_m.f90")).read()
-STRUCTS = ["hgpu_system", "hgpu_config", "hgpu_report", "hgpu_state"]
+STRUCTS = ["hgpu_system", "hgpu_config", "hgpu_report", "hgpu_state", "hgpu_launch"]
 CONST = {"HGPU_MAX_WORDS": 2, "HGPU_MAX_SPACES": 2}
 
 C_KIND = {"int32_t": "i32", "int64_t": "i64", "uint64_t": "i64", "double": "f64", "char": "char", "void": "void"}

@@ -72,3 +72,59 @@ def test_batch_rejects_duplicates():
     g = engine(s, make_config(s, tau=0.02, state_size=1000, spawned_state_size=1000))
     with pytest.raises(HgpuError):
         Batch([g, g])
+
+
+def test_launch_shape_changes_nothing_but_speed():
+    """Handles of a batch with other launch shapes (spawn chunk, block counts),
+    changed between reports as the autotuner does, end where the solo runs with
+    the default shapes end; out-of-range shapes are refused."""
+    from hande_gb300.engine import Batch, HgpuError
+    members = _members()
+    solo = _make(members)
+    batched = _make(members)
+    batch = Batch(batched)
+    shapes = [(32, 1, 1, 1), (64, 7, 3, 5), (128, 300, 1024, 64), (96, 2, 17, 3)]
+    for rep in range(4):
+        for k, g in enumerate(batched):
+            g.set_launch(*shapes[(k + rep) % len(shapes)])
+        rb = batch.run_report()
+        for g, r in zip(solo, rb):
+            rs = g.run_report()
+            assert r.error_flags == 0 and rs.error_flags == 0
+            assert list(r.nparticles) == list(rs.nparticles)
+            assert r.nattempts == rs.nattempts
+    for a, b in zip(solo, batched):
+        sa, pa, _ = a.walkers()
+        sb, pb, _ = b.walkers()
+        np.testing.assert_array_equal(sa, sb)
+        np.testing.assert_array_equal(pa, pb)
+    assert batched[2].launch().as_tuple() == shapes[(2 + 3) % len(shapes)]
+    for bad in [(16, 1, 1, 1), (48, 1, 1, 1), (512, 1, 1, 1), (64, 0, 1, 1), (64, 1, 1025, 1), (64, 1, 1, 0)]:
+        with pytest.raises(HgpuError):
+            batched[0].set_launch(*bad)
+    batch.close()
+
+
+def test_autotuner_keeps_lists_and_results():
+    """The tuner restores every list and state it times on: a batch tuned and
+    then run ends where the untuned solo runs end."""
+    from hande_gb300.autotune import BatchTuner
+    from hande_gb300.engine import Batch
+    members = _members()
+    solo = _make(members)
+    batched = _make(members)
+    for g in solo + batched:
+        g.run_report()
+    batch = Batch(batched)
+    tuner = BatchTuner(batch, batched, trial_cycles=1)
+    choice, base, best = tuner.tune()
+    assert best <= base and len(tuner.table) >= 16
+    for rep in range(3):
+        rb = batch.run_report()
+        for g, r in zip(solo, rb):
+            rs = g.run_report()
+            assert list(r.nparticles) == list(rs.nparticles)
+    for a, b in zip(solo, batched):
+        np.testing.assert_array_equal(a.walkers()[0], b.walkers()[0])
+        np.testing.assert_array_equal(a.walkers()[1], b.walkers()[1])
+    batch.close()

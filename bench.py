@@ -912,6 +912,12 @@ def main():
                                   float(np.hypot(mse(e64)[1], mse(e32r)[1]))) if ok else None,
             "excitations": {"sampled": len(xs[0]), "same_excitation": float(same.mean()),
                             "max_rel_err_hij": float(rel_h.max()) if rel_h.size else None,
+                            # relative errors of near-cancelling |H_ij| (a difference of two
+                            # similar integrals) are large; against the largest |H_ij|:
+                            "max_abs_err_hij_over_max_hij": float(np.max(np.abs(x32[2][same] - x64[2][same])) /
+                                                                  np.max(np.abs(x64[2][same]))) if rel_h.size else None,
+                            "max_rel_err_hij_above_1e-3_of_max": float(rel_h[np.abs(x64[2][same]) > 1e-3 * np.max(
+                                np.abs(x64[2][same]))].max()) if rel_h.size else None,
                             "max_rel_err_pgen": float(rel_p.max()) if rel_p.size else None},
             "note": "FP32 H_ij and p_gen, FP64 K_ii, shift and estimators; both engines replay one-cycle reports "
                     "from the same walker list: the replica (variational, RDM) energy of each replayed cycle, "

@@ -34,6 +34,33 @@ struct SpawnQueue {
     uint8_t slist[kSpawnChunk];
 };
 
+// Whether a child of a deterministic parent is itself deterministic (then the
+// spawn is cancelled, src/fciqmc.f90:777-790); out of line, as it runs only
+// with a semi-stochastic space.
+template <int W>
+__device__ __noinline__ bool determ_child(const DevBuffers &b, const Det<W> &child) {
+    const int64_t q = lower_bound_det<W>(b.ddets, b.nd, child);
+    return q < b.nd && det_eq<W>(load_det<W>(b.ddets, q), child);
+}
+
+// accumulate_bloom_stats (src/bloom_handler.F90:104-145) for one warp's appends:
+// the lanes whose event is a bloom add their count, |amount| sum and maximum.
+// Out of line: blooms are rare, and the append loop stays small.  Called by
+// every lane of the warp.
+static __device__ __noinline__ void warp_blooms(DevState *st, uint32_t bball, bool bloom, int64_t amag) {
+    long long bsum = bloom ? amag : 0, bmax = bsum;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bsum += __shfl_xor_sync(FULL_MASK, bsum, o);
+        bmax = max(bmax, __shfl_xor_sync(FULL_MASK, bmax, o));
+    }
+    if ((int)(threadIdx.x & 31) == __ffs(bball) - 1) {
+        atomicAdd((unsigned long long *)&st->bloom_n, (unsigned long long)__popc(bball));
+        atomicAdd((unsigned long long *)&st->bloom_tot, (unsigned long long)bsum);
+        atomicMax((unsigned long long *)&st->bloom_max, (unsigned long long)bmax);
+    }
+}
+
 // One spawning attempt of a queued chunk entry; returns the spawned amount.
 template <int W, int KIND, typename Real, bool SINGLE>
 __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
@@ -88,10 +115,7 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
     parent_det = f;
     if (at.nspawn != 0 || nspawn_rdm != 0) child = excited<W>(f, at);
     // no spawning from a deterministic state onto another (src/fciqmc.f90:777-790)
-    if (at.nspawn != 0 && b.nd > 0 && (info & kDetermBit)) {
-        const int64_t q = lower_bound_det<W>(b.ddets, b.nd, child);
-        if (q < b.nd && det_eq<W>(load_det<W>(b.ddets, q), child)) at.nspawn = 0;
-    }
+    if (at.nspawn != 0 && b.nd > 0 && (info & kDetermBit) && determ_child<W>(b, child)) at.nspawn = 0;
     return at.nspawn;
 }
 
@@ -107,15 +131,17 @@ __device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTab
 }
 
 // Resident blocks per SM the spawning kernel is compiled for: four (at most 64
-// registers, half the SM's warps) for the uniform generators, whose code fits
-// that budget without spilling; the others keep the compiler's choice.
-template <int KIND>
+// registers, half the SM's warps) for the uniform generators of two-word
+// determinants, whose code fits that budget without spilling (measured: 3 %
+// faster on the 64-orbital replica list, 8 % slower on one-word lists); the
+// others keep the compiler's choice.
+template <int W, int KIND>
 constexpr int spawn_min_blocks() {
-    return (KIND == HGPU_SYS_HUB_K || KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm) ? 4 : 1;
+    return W == 2 && (KIND == HGPU_SYS_HUB_K || KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm) ? 4 : 1;
 }
 
 template <int W, int KIND, typename Real, bool RDM>
-__global__ void __launch_bounds__(kBlock, spawn_min_blocks<KIND>()) k_spawn(DevBuffers b, int R, int cur) {
+__global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(DevBuffers b, int R, int cur) {
     __shared__ DevSys s;
     __shared__ SpawnQueue queue[kBlock / 32];
     extern __shared__ uint8_t smem[];
@@ -239,19 +265,7 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<KIND>()) k_spawn(DevB
                     const int64_t amag = nspawn < 0 ? -nspawn : nspawn;
                     const bool bloom = want && amag >= kBloomThreshold * s.real_factor;
                     const uint32_t bball = __ballot_sync(FULL_MASK, bloom);
-                    if (bball) {
-                        long long bsum = bloom ? amag : 0, bmax = bsum;
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) {
-                            bsum += __shfl_xor_sync(FULL_MASK, bsum, o);
-                            bmax = max(bmax, __shfl_xor_sync(FULL_MASK, bmax, o));
-                        }
-                        if (lane == __ffs(bball) - 1) {
-                            atomicAdd((unsigned long long *)&st->bloom_n, (unsigned long long)__popc(bball));
-                            atomicAdd((unsigned long long *)&st->bloom_tot, (unsigned long long)bsum);
-                            atomicMax((unsigned long long *)&st->bloom_max, (unsigned long long)bmax);
-                        }
-                    }
+                    if (bball) warp_blooms(st, bball, bloom, amag);
                 }
                 if (rdm) {
                     // create_spawned_particle_replica_rdm: (parent, child) and the amount

@@ -314,6 +314,20 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
         return x;
     };
     int64_t ap0 = 0, ap1 = 0;
+    // accumulate_bloom_stats (src/bloom_handler.F90:104-145) over the spawned
+    // list: every entry is one spawning event (its amount in one space), an event
+    // of at least kBloomThreshold particles is a bloom; counted here, where the
+    // amounts are read anyway, rather than in the spawning kernel's hot loop
+    const int64_t bthr = kBloomThreshold * s.real_factor;
+    int64_t bn = 0, btot = 0, bmax = 0;
+    auto bloom_add = [&](const int64_t p[2]) {
+        const int64_t a = (p[0] < 0 ? -p[0] : p[0]) + (p[1] < 0 ? -p[1] : p[1]);
+        if (mode == 0 && a >= bthr) {
+            bn++;
+            btot += a;
+            bmax = a > bmax ? a : bmax;
+        }
+    };
     __syncthreads();
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(&st->ann_ticket[mode], 1u);
@@ -358,6 +372,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
                     for (int q = 0; q < 2; q++)
                         if (q < R) p[q] = b.spops[(int64_t)e[r] * R + q];
                     if (initiator) fl = b.sflag[e[r]];
+                    bloom_add(p);
                 }
 #pragma unroll
                 for (int w = 0; w < W; w++) tdet[k * W + w] = d.w[w];
@@ -378,6 +393,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
                 for (int q = 0; q < 2; q++)
                     if (q < R) p[q] = b.spops[(int64_t)e * R + q];
                 a.add(R, initiator, p, initiator ? b.sflag[e] : 0);
+                bloom_add(p);
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) a.merge(shfl_down_acc(a, off));
@@ -582,10 +598,17 @@ __global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, i
     }
     const int64_t r0 = block_reduce_sum<int64_t>(ap0);
     const int64_t r1 = block_reduce_sum<int64_t>(ap1);
+    const int64_t rbn = block_reduce_sum<int64_t>(bn);
+    const int64_t rbt = block_reduce_sum<int64_t>(btot);
     if (threadIdx.x == 0) {
         b.part_i[blockIdx.x * 4 + 0] = r0;
         b.part_i[blockIdx.x * 4 + 1] = r1;
+        if (rbn) {
+            atomicAdd((unsigned long long *)&st->bloom_n, (unsigned long long)rbn);
+            atomicAdd((unsigned long long *)&st->bloom_tot, (unsigned long long)rbt);
+        }
     }
+    if (bmax) atomicMax((unsigned long long *)&st->bloom_max, (unsigned long long)bmax);
 }
 
 // Dynamic shared memory of k_annihilate.

@@ -799,10 +799,8 @@ __device__ __forceinline__ double pgen_double(const DevSys &s, int cls, int n_ai
 // probability pattempt_parallel (alpha-alpha with probability nalpha/nel), else
 // one alpha and one beta electron; false when the class has too few electrons.
 // cls: 0 opposite spins, 1 alpha-alpha, 2 beta-beta (the p_gen table class).
-// Out of line: only the spin-resolved generators take it, and keeping it out of
-// the other generators' loop keeps their code small in the instruction cache.
 template <int W>
-__device__ __noinline__ bool choose_ij_spin(const DevSys &s, RStream &rs, const Det<W> &f, int &i, int &j,
+__device__ __forceinline__ bool choose_ij_spin(const DevSys &s, RStream &rs, const Det<W> &f, int &i, int &j,
                                                int &cls) {
     Det<W> ma, mb;
 #pragma unroll

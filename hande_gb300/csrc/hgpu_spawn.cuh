@@ -34,33 +34,6 @@ struct SpawnQueue {
     uint8_t slist[kSpawnChunk];
 };
 
-// Whether a child of a deterministic parent is itself deterministic (then the
-// spawn is cancelled, src/fciqmc.f90:777-790); out of line, as it runs only
-// with a semi-stochastic space.
-template <int W>
-__device__ __noinline__ bool determ_child(const DevBuffers &b, const Det<W> &child) {
-    const int64_t q = lower_bound_det<W>(b.ddets, b.nd, child);
-    return q < b.nd && det_eq<W>(load_det<W>(b.ddets, q), child);
-}
-
-// accumulate_bloom_stats (src/bloom_handler.F90:104-145) for one warp's appends:
-// the lanes whose event is a bloom add their count, |amount| sum and maximum.
-// Out of line: blooms are rare, and the append loop stays small.  Called by
-// every lane of the warp.
-static __device__ __noinline__ void warp_blooms(DevState *st, uint32_t bball, bool bloom, int64_t amag) {
-    long long bsum = bloom ? amag : 0, bmax = bsum;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        bsum += __shfl_xor_sync(FULL_MASK, bsum, o);
-        bmax = max(bmax, __shfl_xor_sync(FULL_MASK, bmax, o));
-    }
-    if ((int)(threadIdx.x & 31) == __ffs(bball) - 1) {
-        atomicAdd((unsigned long long *)&st->bloom_n, (unsigned long long)__popc(bball));
-        atomicAdd((unsigned long long *)&st->bloom_tot, (unsigned long long)bsum);
-        atomicMax((unsigned long long *)&st->bloom_max, (unsigned long long)bmax);
-    }
-}
-
 // One spawning attempt of a queued chunk entry; returns the spawned amount.
 template <int W, int KIND, typename Real, bool SINGLE>
 __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
@@ -115,7 +88,10 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
     parent_det = f;
     if (at.nspawn != 0 || nspawn_rdm != 0) child = excited<W>(f, at);
     // no spawning from a deterministic state onto another (src/fciqmc.f90:777-790)
-    if (at.nspawn != 0 && b.nd > 0 && (info & kDetermBit) && determ_child<W>(b, child)) at.nspawn = 0;
+    if (at.nspawn != 0 && b.nd > 0 && (info & kDetermBit)) {
+        const int64_t q = lower_bound_det<W>(b.ddets, b.nd, child);
+        if (q < b.nd && det_eq<W>(load_det<W>(b.ddets, q), child)) at.nspawn = 0;
+    }
     return at.nspawn;
 }
 
@@ -260,12 +236,6 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
                             atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
                         }
                     }
-                    // accumulate_bloom_stats (src/bloom_handler.F90:104-145): an event of
-                    // at least kBloomThreshold particles is a bloom; counted per warp
-                    const int64_t amag = nspawn < 0 ? -nspawn : nspawn;
-                    const bool bloom = want && amag >= kBloomThreshold * s.real_factor;
-                    const uint32_t bball = __ballot_sync(FULL_MASK, bloom);
-                    if (bball) warp_blooms(st, bball, bloom, amag);
                 }
                 if (rdm) {
                     // create_spawned_particle_replica_rdm: (parent, child) and the amount

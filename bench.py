@@ -305,6 +305,7 @@ def e2e_measure(e, W, R, steps, main_cap):
     opo, p5 = pinned_array(rt, (main_cap, R), np.int64)
     oda, p6 = pinned_array(rt, (main_cap,), np.float64)
     bufs = [p1, p2, p3, p4, p5, p6]
+    pinned = [p is not None for p in bufs]
     hst[:] = st
     hpo[:] = po
     hda[:] = da
@@ -342,7 +343,7 @@ def e2e_measure(e, W, R, steps, main_cap):
                     "hgpu_download_walkers into pinned host memory; host wall clock",
             "host_ms_per_step": {"upload": 1e3 * t_up / steps, "cycle": 1e3 * t_cyc / steps,
                                  "download": 1e3 * t_down / steps},
-            "steps": steps}
+            "pinned": pinned, "steps": steps}
 
 
 def cpu_slice(s, cfg, st, po, da, state, n, seconds):
@@ -543,77 +544,100 @@ PRECISION_WORKLOAD = ("config3: synthetic molecule M=48 nel=16 C1 (96 spin orbit
                       "(integrals, heat-bath weights, p_gen) against FP64 with the same seed")
 
 
-def precision_study(target=2e5, tau=5e-5, equil=100, reports=600, nsample=1 << 20, seed=2024, max_grow=600):
-    """config 3: the mixed-precision engine against the FP64 engine on the same
-    seed -- the largest relative error of FP32 H_ij and p_gen over nsample
-    generated excitations, the reblocked E_proj of both runs and their
-    difference in units of the combined standard error, and the attempts/s of
-    each."""
+def precision_study(target=1e8, tau=1e-4, ncycles=5, equil=40, reports=300, nsample=1 << 20, seed=2024,
+                    max_grow=400):
+    """config 3: the mixed-precision engine against the FP64 engine.  The FP64
+    engine grows the population from the reference determinant until the shift
+    varies (target walkers) and equilibrates for `equil` reports; its list and
+    state then seed both runs, so that the FP64 and FP32 engines start from the
+    same list at the same iteration and draw the same random numbers.  Each runs
+    `reports` reports of `ncycles` cycles.  Reported: the reblocked E_proj and
+    shift of each run, their difference in units of the combined standard error,
+    the reblocked per-report difference of the two runs' E_proj (paired: the
+    shared random numbers cancel most of the noise until the runs drift apart),
+    attempts/s of each, and the largest error of FP32 H_ij and p_gen over
+    nsample excitations generated from list parents with the same streams."""
     from hande_gb300 import analysis, systems
     from hande_gb300._abi import PREC_FP64, PREC_MIXED, make_config
     from hande_gb300.engine import Engine
     s = systems.synthetic_molecule(48, 16, seed=seed)
-    out = {"workload": PRECISION_WORKLOAD, "target": target, "tau": tau}
-    res = {}
+    out = {"workload": PRECISION_WORKLOAD, "target": target, "tau": tau, "ncycles": ncycles, "reports": reports}
+
+    def config(prec):
+        return make_config(s, tau=tau, init_pop=max(target / 1000.0, 100.0), target_population=target,
+                           ncycles=ncycles, seed=77, real_amplitudes=True, spawn_cutoff=0.01, excit_gen="heat_bath",
+                           initiator=True, initiator_threshold=3.0, precision=prec,
+                           state_size=int(3 * target) + 100000, spawned_state_size=int(3 * target) + 100000)
+
+    t0 = time.perf_counter()
+    e = Engine(s, config(PREC_FP64))
+    out["table_build_s"] = time.perf_counter() - t0
+    e.initial_distribution()
+    flags = 0
+    t0 = time.perf_counter()
+    for r in range(max_grow):  # until the shift varies
+        rep = e.run_report()
+        flags |= rep.error_flags
+        if rep.vary_shift[0]:
+            break
+    out["growth_reports"] = r + 1
+    for r in range(equil):
+        rep = e.run_report()
+        flags |= rep.error_flags
+    out["growth_and_equilibration_s"] = time.perf_counter() - t0
+    st, po, da = e.walkers()
+    state = e.get_state()
+    rng = np.random.default_rng(5)
+    pick = rng.integers(0, st.shape[0], nsample)
+    xs = (st[pick], np.ones(nsample, np.int64), int(state.iteration) + 1000)
+    series = {}
+    xres = {}
     for name, prec in (("fp64", PREC_FP64), ("fp32", PREC_MIXED)):
-        cfg = make_config(s, tau=tau, init_pop=2000, target_population=target, ncycles=10, seed=77,
-                          real_amplitudes=True, spawn_cutoff=0.01, excit_gen="heat_bath", initiator=True,
-                          initiator_threshold=3.0, precision=prec, state_size=int(20 * target) + 100000,
-                          spawned_state_size=int(20 * target) + 100000)
-        t0 = time.perf_counter()
-        e = Engine(s, cfg)
-        build_s = time.perf_counter() - t0
-        e.initial_distribution()
-        num, d0 = [], []
-        att = 0
-        dev_ms = 0.0
-        flags = 0
-        grown = 0
-        for r in range(max_grow):  # until the shift varies
-            rep = e.run_report()
-            flags |= rep.error_flags
-            grown = r + 1
-            if rep.vary_shift[0]:
-                break
-        for r in range(equil + reports):
+        if name == "fp32":
+            e = Engine(s, config(prec))
+            e.set_walkers(st, po, da)
+            e.set_state(state)
+        xres[name] = e.eval_excitations(*xs)
+        num, d0, shift = [], [], []
+        att, dev_ms = 0, 0.0
+        for r in range(reports):
             rep = e.run_report()
             flags |= rep.error_flags
             if r % 50 == 0:
                 sys.stderr.write("%s report %d Nw=%.4g states=%d shift=%.4f flags=%d\n" % (
                     name, r, rep.nparticles[0], rep.nstates, rep.shift[0], rep.error_flags))
-            if r >= equil:
-                num.append(rep.proj_energy[0])
-                d0.append(rep.D0_population[0])
-                att += rep.nattempts
-                dev_ms += rep.device_ms
+            num.append(rep.proj_energy[0])
+            d0.append(rep.D0_population[0])
+            shift.append(rep.shift[0])
+            att += rep.nattempts
+            dev_ms += rep.device_ms
         E, err, opt = analysis.projected_energy(num, d0)
-        res[name] = {"E_proj": E, "sigma": err, "opt_block": opt, "attempts_per_s": att / (dev_ms * 1e-3),
-                     "growth_reports": grown, "reports": reports,
-                     "walkers": rep.nparticles[0], "states": int(rep.nstates), "error_flags": flags,
-                     "table_build_s": build_s}
-        res[name + "_engine"] = e
-    # generated excitations of the same parents, FP32 against FP64
-    e64, e32 = res.pop("fp64_engine"), res.pop("fp32_engine")
-    st, po, _ = e64.walkers()
-    rng = np.random.default_rng(5)
-    pick = rng.integers(0, st.shape[0], nsample)
-    parents, pp = st[pick], np.ones(nsample, np.int64)
-    r64 = e64.eval_excitations(parents, pp, 3)
-    r32 = e32.eval_excitations(parents, pp, 3)
+        S, serr, sopt = analysis.mean_error(shift)
+        series[name] = np.array(num) / np.array(d0)
+        out[name] = {"E_proj": E, "sigma": err, "opt_block": opt, "shift": S, "shift_sigma": serr,
+                     "shift_opt_block": sopt, "attempts_per_s": att / (dev_ms * 1e-3),
+                     "ms_per_cycle": dev_ms / (reports * ncycles), "walkers": rep.nparticles[0],
+                     "states": int(rep.nstates)}
+        e.close()
+    r64, r32 = xres["fp64"], xres["fp32"]
     same = np.all(r32[0] == r64[0], axis=1) & (r32[3] == r64[3]) & (r64[3] == 1)
-    rel_h = np.abs(r32[2][same] - r64[2][same]) / np.abs(r64[2][same])
+    dh = np.abs(r32[2][same] - r64[2][same])
+    rel_h = dh / np.abs(r64[2][same])
     rel_p = np.abs(r32[1][same] - r64[1][same]) / np.abs(r64[1][same])
     big = np.abs(r64[2][same]) > 1e-3 * np.max(np.abs(r64[2][same]))
-    out.update(res)
     out["excitations"] = {"sampled": nsample, "same_excitation": float(same.sum()) / max(int((r64[3] == 1).sum()), 1),
                           "max_rel_err_hij": float(rel_h.max()), "max_rel_err_hij_above_1e-3_of_max":
-                          float(rel_h[big].max()), "max_rel_err_pgen": float(rel_p.max())}
-    d = res["fp32"]["E_proj"] - res["fp64"]["E_proj"]
-    sig = float(np.hypot(res["fp32"]["sigma"], res["fp64"]["sigma"]))
+                          float(rel_h[big].max()), "max_abs_err_hij_over_max_hij":
+                          float(dh.max() / np.max(np.abs(r64[2][same]))), "max_rel_err_pgen": float(rel_p.max())}
+    d = out["fp32"]["E_proj"] - out["fp64"]["E_proj"]
+    sig = float(np.hypot(out["fp32"]["sigma"], out["fp64"]["sigma"]))
     out["dE_proj"] = d
     out["dE_proj_over_sigma"] = d / sig if sig > 0 else None
-    e64.close()
-    e32.close()
+    pm, perr, popt = analysis.mean_error(series["fp32"] - series["fp64"])
+    out["dE_proj_paired"] = {"mean": pm, "sigma": perr, "opt_block": popt,
+                             "over_sigma": pm / perr if perr and perr > 0 else None}
+    out["fp32_speedup"] = out["fp32"]["attempts_per_s"] / out["fp64"]["attempts_per_s"]
+    out["error_flags"] = flags
     return out
 
 
@@ -784,6 +808,8 @@ def main():
     ap.add_argument("--config", type=int, default=5,
                     help="5: the headline line (default); 2: the config-2 measurement alone; 1: the Hubbard 4x4 "
                          "run of config 1; 3: the mixed-precision study of config 3 (one JSON line each)")
+    ap.add_argument("--c3-target", type=float, default=1e8, help="config 3: target population")
+    ap.add_argument("--c3-reports", type=int, default=300, help="config 3: measured reports of each precision")
     ap.add_argument("--semi-stoch", type=int, default=0,
                     help="time the config-2 cycle with a semi-stochastic 'high' space of this size (one JSON line)")
     args = ap.parse_args()
@@ -796,7 +822,7 @@ def main():
         return
     if args.config == 3:
         if rank == 0:
-            print(json.dumps(precision_study()))
+            print(json.dumps(precision_study(target=args.c3_target, reports=args.c3_reports)))
         return
     if args.config == 1:
         if rank == 0:

@@ -108,12 +108,13 @@ __device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTab
 
 // Resident blocks per SM the spawning kernel is compiled for: four (at most 64
 // registers, half the SM's warps) for the uniform generators of two-word
-// determinants, whose code fits that budget without spilling (measured: 3 %
-// faster on the 64-orbital replica list, 8 % slower on one-word lists); the
-// others keep the compiler's choice.
+// determinants, whose code fits that budget without spilling (3 % faster on the
+// 64-orbital replica list); 0 (no minimum) leaves the others to the compiler,
+// which gives the one-word uniform kernels 64 registers as well (an explicit
+// minimum of 1 lets it take 116 and halves their occupancy).
 template <int W, int KIND>
 constexpr int spawn_min_blocks() {
-    return W == 2 && (KIND == HGPU_SYS_HUB_K || KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm) ? 4 : 1;
+    return W == 2 && (KIND == HGPU_SYS_HUB_K || KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm) ? 4 : 0;
 }
 
 template <int W, int KIND, typename Real, bool RDM>

@@ -295,6 +295,7 @@ def e2e_measure(e, W, R, steps, main_cap):
     from hande_gb300.engine import _p
     rt = cudart()
     e.snapshot(restore=True)
+    e.end_report()  # close the report that a cycle run before (e.g. hgpu_profile_cycle) left open
     st, po, da = e.walkers()
     n0 = st.shape[0]
     bufs = []

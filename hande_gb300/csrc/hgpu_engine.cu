@@ -691,6 +691,9 @@ static int alloc_lists(hgpu_handle *h) {
         int64_t hs = 16;
         while (hs < b.cap + b.cap / 2) hs <<= 1;
         b.rdm_hash_mask = hs - 1;
+        CK(cudaStreamCreateWithFlags(&b.rdm_aux, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&b.rdm_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b.rdm_join, cudaEventDisableTiming));
         if ((rc = dalloc(h, &b.rdm_hash, (size_t)hs))) return rc;
     }
     if ((rc = dalloc(h, &b.scan_part, (size_t)kMaxBlocks * 2))) return rc;
@@ -902,6 +905,9 @@ int32_t hgpu_destroy(hgpu_handle *h) {
     if (h->scratch) cudaFree(h->scratch);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->b.rdm_fork) cudaEventDestroy(h->b.rdm_fork);
+    if (h->b.rdm_join) cudaEventDestroy(h->b.rdm_join);
+    if (h->b.rdm_aux) cudaStreamDestroy(h->b.rdm_aux);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return HGPU_OK;

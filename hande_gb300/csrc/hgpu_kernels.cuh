@@ -144,6 +144,10 @@ struct DevBuffers {
     double *rdm_rows;       // [2][npairs]: per-row energy and diagonal of calc_rdm_energy
     uint32_t *rdm_hash;     // open-addressing table of the new main list (index per slot)
     int64_t rdm_hash_mask;  // table size - 1 (a power of two, at least 1.5 x cap)
+    // the RDM diagonal runs on a second stream beside the RDM spawns (host
+    // handles: a fork and a join event around it)
+    cudaStream_t rdm_aux;
+    cudaEvent_t rdm_fork, rdm_join;
     // semi-stochastic projection (hgpu_semi_stoch.cu): the deterministic
     // determinants in main-list order, the Hamiltonian by column j (rows i
     // ascending: H(D_i, D_j), diagonal K_jj), the populations of the

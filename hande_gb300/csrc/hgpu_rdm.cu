@@ -262,18 +262,25 @@ __global__ void __launch_bounds__(1024) k_rdm_final(DevBuffers b) {
     }
 }
 
+// The diagonal (every occupied determinant) does not depend on the RDM spawns:
+// it runs on the second stream while the hash table is built and the spawns
+// are added (both only add into the RDM), joined before the cycle ends.
 void launch_rdm_cycle(const DevBuffers &b, int W, int R, int cur, cudaStream_t st) {
     const size_t dsm = sizeof(double) * (size_t)b.npairs;
+    cudaEventRecord(b.rdm_fork, st);
+    cudaStreamWaitEvent(b.rdm_aux, b.rdm_fork, 0);
+    if (W == 1) k_rdm_diag<1><<<b.grid, kBlock, dsm, b.rdm_aux>>>(b, R, cur);
+    else k_rdm_diag<2><<<b.grid, kBlock, dsm, b.rdm_aux>>>(b, R, cur);
+    cudaEventRecord(b.rdm_join, b.rdm_aux);
     k_rdm_hash_clear<<<b.grid, kBlock, 0, st>>>(b);
     if (W == 1) {
         k_rdm_hash_insert<1><<<b.grid, kBlock, 0, st>>>(b, cur);
         k_rdm_spawns<1><<<b.grid, kBlock, 0, st>>>(b, R, cur);
-        k_rdm_diag<1><<<b.grid, kBlock, dsm, st>>>(b, R, cur);
     } else {
         k_rdm_hash_insert<2><<<b.grid, kBlock, 0, st>>>(b, cur);
         k_rdm_spawns<2><<<b.grid, kBlock, 0, st>>>(b, R, cur);
-        k_rdm_diag<2><<<b.grid, kBlock, dsm, st>>>(b, R, cur);
     }
+    cudaStreamWaitEvent(st, b.rdm_join, 0);
 }
 
 void launch_rdm_energy(const DevBuffers &b, int W, cudaStream_t st) {

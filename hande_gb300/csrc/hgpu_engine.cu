@@ -50,6 +50,8 @@ struct hgpu_handle {
     int64_t ss_iter;  // iteration at whose start the deterministic space is built
     int64_t ss_gen = 0;  // number of deterministic spaces built or dropped so far
     int64_t launch_gen = 0;  // number of hgpu_set_launch calls (batch graphs follow it)
+    // hub_k momentum tables on the host (the 'ci' deterministic space)
+    std::vector<int> h_symtab, h_invsym;
     cudaEvent_t ev0, ev1;
     double report_ms;
     std::vector<void *> allocs;
@@ -393,6 +395,8 @@ static int build_system(hgpu_handle *h, const hgpu_system *sys) {
         s.inv_sym = dinv;
         s.nsym = 1;
         h->b.nk = nk;
+        h->h_symtab.assign(sys->sym_table, sys->sym_table + nk * nk);
+        h->h_invsym.assign(sys->inv_sym, sys->inv_sym + nk);
     } else if (sys->kind == HGPU_SYS_READ_IN) {
         if (sys->nsym_pg > kMaxSym || sys->nsym_pg < 1) return HGPU_ERR_UNSUPPORTED;
         s.norb = sys->norb;
@@ -822,7 +826,6 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     // combined with the replica RDM
     if (cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1 && cfg->semi_stoch_space != 4)
         return HGPU_ERR_UNSUPPORTED;
-    if (cfg->semi_stoch_space == 4 && sys->kind != HGPU_SYS_READ_IN) return HGPU_ERR_UNSUPPORTED;
     if (cfg->semi_stoch_space != 0 && cfg->density_matrices) return HGPU_ERR_UNSUPPORTED;
     if ((cfg->semi_stoch_space == 1 && cfg->semi_stoch_size < 1) ||
         (cfg->semi_stoch_space == 4 && cfg->semi_stoch_ci_level < 0))
@@ -1039,20 +1042,31 @@ static int ss_init(hgpu_handle *h) {
             if ((f0[p >> 6] >> (p & 63)) & 1u) occ.push_back(p);
             else virt.push_back(p);
         }
-        // spin orbitals alternate alpha (even) and beta (odd); irreps as staged for the kernels
+        // spin orbitals alternate alpha (even) and beta (odd).  The symmetry
+        // change of the holes and particles so far: molecular irreps combine by
+        // XOR (identity 0), Hubbard crystal momenta by sym_table (a hole adds
+        // -k, a particle +k; identity the Gamma point, k + (-k))
         auto alpha = [](int p) { return (p & 1) == 0 ? 1 : 0; };
+        const bool hubk = h->kind == HGPU_SYS_HUB_K;
         const uint8_t *sym = h->hsys.orbsym;
+        const int nk = hubk ? (int)h->h_invsym.size() : 0;
+        const int ident = hubk ? h->h_symtab[h->h_invsym[0]] : 0;  // k_0 + (-k_0) = Gamma
+        auto with = [&](int sy, int p, bool hole) {
+            if (!hubk) return sy ^ (int)sym[p];
+            const int k = p >> 1;  // the k-point of spin orbital p
+            return h->h_symtab[sy * nk + (hole ? h->h_invsym[k] : k)];
+        };
         std::vector<uint64_t> f(f0, f0 + W);
         std::function<void(size_t, int, int, int)> parts = [&](size_t v, int k, int na, int sy) {
             if (k == 0) {
-                if (na == 0 && sy == 0) dd.insert(dd.end(), f.begin(), f.end());
+                if (na == 0 && sy == ident) dd.insert(dd.end(), f.begin(), f.end());
                 return;
             }
             for (size_t q = v; q + k <= virt.size(); q++) {
                 const int p = virt[q], a = alpha(p);
                 if (na - a < 0) continue;
                 f[p >> 6] |= 1ull << (p & 63);
-                parts(q + 1, k - 1, na - a, sy ^ sym[p]);
+                parts(q + 1, k - 1, na - a, with(sy, p, false));
                 f[p >> 6] &= ~(1ull << (p & 63));
             }
         };
@@ -1064,12 +1078,12 @@ static int ss_init(hgpu_handle *h) {
             for (size_t q = o; q + k <= occ.size(); q++) {
                 const int p = occ[q];
                 f[p >> 6] &= ~(1ull << (p & 63));
-                holes(q + 1, k - 1, kk, na + alpha(p), sy ^ sym[p]);
+                holes(q + 1, k - 1, kk, na + alpha(p), with(sy, p, true));
                 f[p >> 6] |= 1ull << (p & 63);
             }
         };
         for (int k = 0; k <= h->cfg.semi_stoch_ci_level && k <= (int)occ.size() && k <= (int)virt.size(); k++)
-            holes(0, k, k, 0, 0);
+            holes(0, k, k, 0, ident);
         K = (int64_t)(dd.size() / W);
         std::vector<int64_t> order(K);
         for (int64_t k = 0; k < K; k++) order[k] = k;

@@ -2492,12 +2492,26 @@ typedef struct {
     int64_t n, cap;
 } detlist_t;
 
+/* The symmetry change of a 'ci' determinant's holes and particles so far, with
+ * spin orbital p added as a hole or a particle: molecular irreps combine by XOR
+ * (identity 0); Hubbard crystal momenta by sym_table, a hole adding -k and a
+ * particle +k (identity the Gamma point). */
+static int ci_sym(const oracle_ctx *c, int sym, int p, int hole) {
+    if (c->kind != HGPU_SYS_HUB_K) return sym ^ c->orb_sym[p];
+    const int k = c->orb_sym[p];
+    return c->sym_table[sym * c->nk + (hole ? c->inv_sym[k] : k)];
+}
+
+static int ci_sym_identity(const oracle_ctx *c) {
+    return c->kind == HGPU_SYS_HUB_K ? c->sym_table[0 * c->nk + c->inv_sym[0]] : 0;
+}
+
 /* Particles of a 'ci' determinant: k more virtual orbitals from position v on,
- * whose alpha count and irrep product must come to na and sym. */
+ * whose alpha count and symmetry change must come to na and the identity. */
 static void ci_particles(const oracle_ctx *c, const int *virt, int nv, int v, int k, int na, int sym,
                          uint64_t *f, detlist_t *out) {
     if (k == 0) {
-        if (na != 0 || sym != 0) return;
+        if (na != 0 || sym != ci_sym_identity(c)) return;
         if (out->n == out->cap) {
             out->cap = out->cap ? 2 * out->cap : 64;
             out->d = (uint64_t *)realloc(out->d, sizeof(uint64_t) * c->nw * out->cap);
@@ -2510,7 +2524,7 @@ static void ci_particles(const oracle_ctx *c, const int *virt, int nv, int v, in
         const int p = virt[q], a = c->orb_ms[p] > 0;
         if (na - a < 0) continue;
         f[p >> 6] |= (uint64_t)1 << (p & 63);
-        ci_particles(c, virt, nv, q + 1, k - 1, na - a, sym ^ c->orb_sym[p], f, out);
+        ci_particles(c, virt, nv, q + 1, k - 1, na - a, ci_sym(c, sym, p, 0), f, out);
         f[p >> 6] &= ~((uint64_t)1 << (p & 63));
     }
 }
@@ -2525,7 +2539,7 @@ static void ci_holes(const oracle_ctx *c, const int *occ, int no, const int *vir
     for (int q = o; q <= no - k; q++) {
         const int p = occ[q];
         f[p >> 6] &= ~((uint64_t)1 << (p & 63));
-        ci_holes(c, occ, no, virt, nv, q + 1, k - 1, kk, na + (c->orb_ms[p] > 0), sym ^ c->orb_sym[p], f, out);
+        ci_holes(c, occ, no, virt, nv, q + 1, k - 1, kk, na + (c->orb_ms[p] > 0), ci_sym(c, sym, p, 1), f, out);
         f[p >> 6] |= (uint64_t)1 << (p & 63);
     }
 }
@@ -2543,7 +2557,7 @@ static detlist_t ci_space(const oracle_ctx *c) {
     uint64_t f[MAXW];
     memcpy(f, c->f0, sizeof(f));
     for (int k = 0; k <= c->cfg.semi_stoch_ci_level && k <= no && k <= nv; k++)
-        ci_holes(c, occ, no, virt, nv, 0, k, k, 0, 0, f, &out);
+        ci_holes(c, occ, no, virt, nv, 0, k, k, 0, ci_sym_identity(c), f, &out);
     return out;
 }
 
@@ -2911,7 +2925,6 @@ oracle_ctx *oracle_create(const hgpu_config *cfg, const hgpu_system *sys) {
     c->ss_iter = INT64_MAX;
     if (cfg->semi_stoch_space != 0) c->ss_iter = cfg->semi_stoch_start_iter > 1 ? cfg->semi_stoch_start_iter : 1;
     if ((cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1 && cfg->semi_stoch_space != 4) ||
-        (cfg->semi_stoch_space == 4 && c->kind != HGPU_SYS_READ_IN) ||
         (cfg->semi_stoch_space != 0 && cfg->density_matrices)) {
         oracle_destroy(c);
         return NULL;

@@ -31,6 +31,9 @@ RUNS = [
                        semi_stoch_space=4, semi_stoch_ci_level=2, semi_stoch_start_iter=5), 6),
     ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
                    semi_stoch_space=4, semi_stoch_ci_level=1, semi_stoch_start_iter=12), 3),
+    # a 'ci' space of the Hubbard model: CISD of the 4x4 lattice (momentum conserved)
+    ("hub_k_4x4", dict(tau=0.01, init_pop=50, target_population=5000, semi_stoch_space=4, semi_stoch_ci_level=2,
+                       semi_stoch_start_iter=6), 4),
     # two replicas (replica_tricks) sharing one space, initiator on
     ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True, nspaces=2,
                    initiator=True, semi_stoch_space=1, semi_stoch_size=250, semi_stoch_start_iter=9), 3),

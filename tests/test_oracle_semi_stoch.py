@@ -138,3 +138,28 @@ def test_ci_space_contents():
         want = want[sort_dets(want)]
         np.testing.assert_array_equal(got, want)
         assert st.shape[0] >= want.shape[0]  # all in the main list, with zero population if need be
+
+
+def test_ci_space_contents_hubbard():
+    """A 'ci' space of the Hubbard model in momentum space: every determinant of
+    the reference's spin and crystal momentum within ex_level excitations of it
+    (enumerate_determinants restricted to ex_level, as create_ci_determ_space
+    asks for any system)."""
+    s = systems.hubbard_k([[3, 0], [0, 3]], 7, U=2.0, ms=1)
+    sym = fci.det_symmetry(s, s.aufbau_occ())
+    f0 = s.encode(s.aufbau_occ()).view(np.int64)
+    dets = np.array(fci.enumerate_dets(s, sym))
+    xl = np.array([bin(int(np.bitwise_xor(d, f0).view(np.uint64)[0])).count("1") // 2 for d in dets])
+    for level in (1, 2):
+        cfg = make_config(s, tau=0.01, semi_stoch_space=4, semi_stoch_ci_level=level, semi_stoch_start_iter=1,
+                          state_size=20000, spawned_state_size=20000)
+        o = Oracle(s, cfg)
+        o.initial_distribution()
+        o.run_report()
+        got = o.determ_space()
+        o.close()
+        want = dets[xl <= level]
+        want = want[sort_dets(want)]
+        # a single excitation changes the momentum: level 1 is the reference alone
+        assert want.shape[0] == 1 if level == 1 else want.shape[0] > 50
+        np.testing.assert_array_equal(got, want)

@@ -545,14 +545,18 @@ PRECISION_WORKLOAD = ("config3: synthetic molecule M=48 nel=16 C1 (96 spin orbit
                       "(integrals, heat-bath weights, p_gen) against FP64 with the same seed")
 
 
-def precision_study(target=1e8, tau=1e-4, ncycles=5, equil=40, reports=300, nsample=1 << 20, seed=2024,
-                    max_grow=400):
+def precision_study(target=1e8, tau=1e-4, ncycles=1, equil=100, reports=500, nsample=1 << 20, seed=2024,
+                    max_grow=2000):
     """config 3: the mixed-precision engine against the FP64 engine.  The FP64
     engine grows the population from the reference determinant until the shift
     varies (target walkers) and equilibrates for `equil` reports; its list and
     state then seed both runs, so that the FP64 and FP32 engines start from the
     same list at the same iteration and draw the same random numbers.  Each runs
-    `reports` reports of `ncycles` cycles.  Reported: the reblocked E_proj and
+    `reports` reports of `ncycles` cycles.  One cycle per report: the shift
+    is updated every cycle, so that once it varies the population overshoots
+    the target by less than a factor of two (with five cycles per report and
+    shift damping 0.05 it reached four times the target before the shift
+    caught up); the lists are sized for four times the target.  Reported: the reblocked E_proj and
     shift of each run, their difference in units of the combined standard error,
     the reblocked per-report difference of the two runs' E_proj (paired: the
     shared random numbers cancel most of the noise until the runs drift apart),
@@ -568,7 +572,7 @@ def precision_study(target=1e8, tau=1e-4, ncycles=5, equil=40, reports=300, nsam
         return make_config(s, tau=tau, init_pop=max(target / 1000.0, 100.0), target_population=target,
                            ncycles=ncycles, seed=77, real_amplitudes=True, spawn_cutoff=0.01, excit_gen="heat_bath",
                            initiator=True, initiator_threshold=3.0, precision=prec,
-                           state_size=int(3 * target) + 100000, spawned_state_size=int(3 * target) + 100000)
+                           state_size=int(4 * target) + 100000, spawned_state_size=int(4 * target) + 100000)
 
     t0 = time.perf_counter()
     e = Engine(s, config(PREC_FP64))
@@ -604,7 +608,7 @@ def precision_study(target=1e8, tau=1e-4, ncycles=5, equil=40, reports=300, nsam
         for r in range(reports):
             rep = e.run_report()
             flags |= rep.error_flags
-            if r % 50 == 0:
+            if r % 100 == 0:
                 sys.stderr.write("%s report %d Nw=%.4g states=%d shift=%.4f flags=%d\n" % (
                     name, r, rep.nparticles[0], rep.nstates, rep.shift[0], rep.error_flags))
             num.append(rep.proj_energy[0])
@@ -810,7 +814,7 @@ def main():
                     help="5: the headline line (default); 2: the config-2 measurement alone; 1: the Hubbard 4x4 "
                          "run of config 1; 3: the mixed-precision study of config 3 (one JSON line each)")
     ap.add_argument("--c3-target", type=float, default=1e8, help="config 3: target population")
-    ap.add_argument("--c3-reports", type=int, default=300, help="config 3: measured reports of each precision")
+    ap.add_argument("--c3-reports", type=int, default=500, help="config 3: measured reports of each precision")
     ap.add_argument("--semi-stoch", type=int, default=0,
                     help="time the config-2 cycle with a semi-stochastic 'high' space of this size (one JSON line)")
     args = ap.parse_args()

@@ -618,7 +618,7 @@ def precision_study(target=1e8, tau=1e-4, ncycles=1, equil=100, reports=500, nsa
             dev_ms += rep.device_ms
         E, err, opt = analysis.projected_energy(num, d0)
         S, serr, sopt = analysis.mean_error(shift)
-        series[name] = np.array(num) / np.array(d0)
+        series[name] = (np.array(num), np.array(d0))
         out[name] = {"E_proj": E, "sigma": err, "opt_block": opt, "shift": S, "shift_sigma": serr,
                      "shift_opt_block": sopt, "attempts_per_s": att / (dev_ms * 1e-3),
                      "ms_per_cycle": dev_ms / (reports * ncycles), "walkers": rep.nparticles[0],
@@ -638,9 +638,23 @@ def precision_study(target=1e8, tau=1e-4, ncycles=1, equil=100, reports=500, nsa
     sig = float(np.hypot(out["fp32"]["sigma"], out["fp64"]["sigma"]))
     out["dE_proj"] = d
     out["dE_proj_over_sigma"] = d / sig if sig > 0 else None
-    pm, perr, popt = analysis.mean_error(series["fp32"] - series["fp64"])
-    out["dE_proj_paired"] = {"mean": pm, "sigma": perr, "opt_block": popt,
-                             "over_sigma": pm / perr if perr and perr > 0 else None}
+    # Paired comparison: the runs share their start and random streams, so the
+    # difference of E_proj = sum(num) / sum(D0) over the same block of reports
+    # cancels much of the common noise.  Per-report ratios are not averaged (a
+    # report with a small D0 gives an outlier); the reports are cut into
+    # nblk consecutive blocks, each block's E_proj difference is formed from
+    # its sums, and the blocks' mean and standard error are reported.
+    nblk = 10
+    m = (reports // nblk) * nblk
+    if m >= nblk:
+        def bsum(x):
+            return x[:m].reshape(nblk, -1).sum(axis=1)
+        (n64, z64), (n32, z32) = series["fp64"], series["fp32"]
+        dd = bsum(n32) / bsum(z32) - bsum(n64) / bsum(z64)
+        pm, perr = float(dd.mean()), float(dd.std(ddof=1) / np.sqrt(nblk))
+        out["dE_proj_paired"] = {"blocks": nblk, "reports_per_block": m // nblk, "mean": pm, "sigma": perr,
+                                 "over_sigma": pm / perr if perr > 0 else None}
+    out["D0_mean"] = {k: float(np.mean(v[1])) for k, v in series.items()}
     out["fp32_speedup"] = out["fp32"]["attempts_per_s"] / out["fp64"]["attempts_per_s"]
     out["error_flags"] = flags
     return out

@@ -132,6 +132,14 @@ __device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1) 
     }
 }
 
+// One Philox block, out of line: every draw of a generator goes through this
+// single copy of the ten rounds instead of an inlined copy per call site.
+static __device__ __noinline__ uint4 philox_block(uint4 c, uint32_t k0, uint32_t k1) {
+    uint32_t w[4] = {c.x, c.y, c.z, c.w};
+    philox(w, k0, k1);
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
 // k * 2^-53 for k < 2^53, built from its bit pattern on the integer pipes
 // (the value is exact, so this is the same number the conversion gives).
 __device__ __forceinline__ double kdouble(uint64_t k) {
@@ -175,12 +183,11 @@ struct RStream {
             have = false;
             return bufk;
         }
-        uint32_t c[4] = {c0, c1, c2, c3 | block};
-        philox(c, k0, k1);
+        const uint4 c = philox_block(make_uint4(c0, c1, c2, c3 | block), k0, k1);
         block++;
-        bufk = k53(c[2], c[3]);
+        bufk = k53(c.z, c.w);
         have = true;
-        return k53(c[0], c[1]);
+        return k53(c.x, c.y);
     }
     // get_rand_close_open
     __device__ __forceinline__ double next() { return kdouble(next_k()); }

@@ -419,23 +419,33 @@ __global__ void __launch_bounds__(kOSThreads, 4) k_onesweep(DevBuffers b, int pa
 
 // One stable pass over packed records (see P64 / P128): the digit is the
 // record's lowest byte; OUT is the next pass's record or, after the last pass,
-// the 32-bit index.  Tiles, ranking and look-back as in k_onesweep.
+// the 32-bit index.  Look-back as in k_onesweep.  Tiles of 48 KB of records
+// (24 eight-byte or 12 sixteen-byte records per thread, two blocks per SM at
+// up to 128 registers): twice k_onesweep's, which halves the look-backs,
+// block scans and barriers per record and gives each digit of a tile twice
+// as long a contiguous run to write.  Ranking within a warp: each lane sets
+// its bit in a shared word per digit, and the word read back is the set of
+// lanes with its digit -- one shared-memory atomic instead of a ballot per
+// digit bit (16 % faster passes than tiles of 24 KB ranked by ballots, 21 %
+// with this ranking, on the 64-orbital replica lists).
+constexpr int kPKMinBlocks = 2;
 template <typename IN>
 struct PKConf {
-    static constexpr int items = sizeof(IN) == 8 ? 12 : 6;
+    static constexpr int items = sizeof(IN) == 8 ? 24 : 12;
     static constexpr int tile = kOSThreads * items;
     static constexpr size_t smem = (size_t)tile * sizeof(IN);
 };
 
 template <typename IN, typename OUT>
-__global__ void __launch_bounds__(kOSThreads, 4) k_onesweep_pk(DevBuffers b, int pass, const IN *recs_in,
-                                                            OUT *recs_out, int ib) {
+__global__ void __launch_bounds__(kOSThreads, kPKMinBlocks) k_onesweep_pk(DevBuffers b, int pass, const IN *recs_in,
+                                                                       OUT *recs_out, int ib) {
     constexpr int ITEMS = PKConf<IN>::items;
     constexpr int TILE = PKConf<IN>::tile;
     constexpr int NW = kOSThreads / 32;
     extern __shared__ uint64_t os_smem[];
     IN *srec = reinterpret_cast<IN *>(os_smem);  // [TILE], in digit order
     __shared__ uint32_t wcnt[NW][kRadix];
+    __shared__ uint32_t wmatch[NW][kRadix];  // lanes of a warp per digit, zero between items
     __shared__ uint32_t lstart[kRadix], gbase[kRadix];
     __shared__ uint32_t s_tile;
     DevState *st = b.state;
@@ -445,6 +455,8 @@ __global__ void __launch_bounds__(kOSThreads, 4) k_onesweep_pk(DevBuffers b, int
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int d = threadIdx.x;  // digit owned in the look-back
     uint64_t *status = b.lookback;
+#pragma unroll
+    for (int w = 0; w < NW; w++) wmatch[w][threadIdx.x] = 0;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(&st->os_ticket[pass], 1u);
 #pragma unroll
@@ -454,7 +466,7 @@ __global__ void __launch_bounds__(kOSThreads, 4) k_onesweep_pk(DevBuffers b, int
         if (tile >= ntiles) break;
         const int64_t t0 = tile * TILE;
         IN rv[ITEMS];
-        uint32_t off[ITEMS], dg[ITEMS];
+        uint32_t dgo[ITEMS];  // digit << 16 | rank of the record in its warp and digit
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             const int64_t e = t0 + (int64_t)(warp * ITEMS + r) * 32 + lane;
@@ -465,19 +477,24 @@ __global__ void __launch_bounds__(kOSThreads, 4) k_onesweep_pk(DevBuffers b, int
             const int64_t e = t0 + (int64_t)(warp * ITEMS + r) * 32 + lane;
             const bool valid = e < n;
             const uint32_t mask = __ballot_sync(FULL_MASK, valid);
-            dg[r] = 0xFFFFFFFFu;
+            dgo[r] = 0xFFFFFFFFu;
+            // peers of equal digit: every lane sets its bit in its digit's word
+            const uint32_t dd = pk_digit(rv[r]);
+            if (valid) atomicOr(&wmatch[warp][dd], 1u << lane);
+            __syncwarp();
+            uint32_t peers = 0;
+            if (valid) peers = wmatch[warp][dd];
+            __syncwarp();
             if (valid) {
-                const uint32_t dd = pk_digit(rv[r]);
-                dg[r] = dd;
-                const uint32_t peers = warp_peers8(mask, dd);
                 const int leader = __ffs(peers) - 1;
                 uint32_t old = 0;
                 if (lane == leader) {
                     old = wcnt[warp][dd];
                     wcnt[warp][dd] = old + __popc(peers);
+                    wmatch[warp][dd] = 0;
                 }
                 old = __shfl_sync(mask, old, leader);
-                off[r] = old + __popc(peers & lanemask_lt());
+                dgo[r] = (dd << 16) | (old + __popc(peers & lanemask_lt()));
             }
             __syncwarp();
         }
@@ -532,7 +549,10 @@ __global__ void __launch_bounds__(kOSThreads, 4) k_onesweep_pk(DevBuffers b, int
         __syncthreads();
 #pragma unroll
         for (int r = 0; r < ITEMS; r++)
-            if (dg[r] != 0xFFFFFFFFu) srec[lstart[dg[r]] + wcnt[warp][dg[r]] + off[r]] = rv[r];
+            if (dgo[r] != 0xFFFFFFFFu) {
+                const uint32_t dd = dgo[r] >> 16;
+                srec[lstart[dd] + wcnt[warp][dd] + (dgo[r] & 0xFFFFu)] = rv[r];
+            }
         __syncthreads();
         const int tn = (int)min((int64_t)TILE, n - t0);
         for (int j = threadIdx.x; j < tn; j += kOSThreads) {

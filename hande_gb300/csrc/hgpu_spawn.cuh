@@ -41,8 +41,9 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
                                                bool drew, uint64_t bufk, bool rdm, Det<W> &child, int &sp,
                                                uint32_t &info, Det<W> &parent_det, int64_t &nspawn_rdm) {
     constexpr bool single = SINGLE;
-    int64_t i = slot / R;
-    sp = (int)(slot - i * R);
+    // R is 1 or 2: a shift instead of an integer division
+    const int64_t i = slot >> (R - 1);
+    sp = (int)(slot & (uint32_t)(R - 1));
     Det<W> f = load_det<W>(dets, i);
     info = b.pinfo[i];
     int64_t parent = (info >> sp) & 1u ? -1 : 1;
@@ -158,26 +159,30 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
         int nd = 0, ns = 0;
         for (int64_t base = (int64_t)cbase; base < cend; base += 32) {
             int64_t a = base + lane;
-            int64_t wv = k0 + lane < NR ? b.aoff[k0 + lane] : INT64_MAX;
-            uint32_t le_mask = 0;
-#pragma unroll 1
-            for (int m = 0; m < 32; m++) {
-                int64_t v = __shfl_sync(FULL_MASK, wv, m);
-                if (v <= a) le_mask |= 1u << m;
-            }
+            const int64_t wv = k0 + lane < NR ? b.aoff[k0 + lane] : INT64_MAX;
+            // end of window slot m relative to this step, clamped to [0, 33]:
+            // aoff[k0 + m] <= a exactly when e_m <= lane, and e is
+            // non-decreasing in m, so the count of such m is found by a
+            // binary search over the lanes
+            const int64_t ed = wv - base;
+            const int e = ed < 0 ? 0 : (ed > 33 ? 33 : (int)ed);
+            int cnt = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(FULL_MASK, e, cnt + step - 1) <= lane) cnt += step;
+            if (__shfl_sync(FULL_MASK, e, cnt) <= lane) cnt++;
             int64_t k = NR;
             bool valid = a < cend, single = false;
             if (valid) {
-                int cnt = __popc(le_mask);
                 k = (cnt < 32 && k0 + cnt < NR) ? k0 + cnt : upper_bound_off(b.aoff, NR, a);
                 int64_t att = a - (k > 0 ? b.aoff[k - 1] : 0);
                 int off = (int)(a - (int64_t)cbase);
                 q.slot[off] = (uint32_t)k;
                 q.att[off] = (uint32_t)att;
                 if (drew) {
-                    int64_t i = k / R;
+                    const int64_t i = k >> (R - 1);
                     RStream rs;
-                    rs.init(s.seed, P_SPAWN, (uint32_t)(k - i * R), i, att, iter);
+                    rs.init(s.seed, P_SPAWN, (uint32_t)(k & (R - 1)), i, att, iter);
                     single = rs.next_k() < s.t_single;  // rs.next() < pattempt_single
                     q.bufk[off] = rs.bufk;
                 }

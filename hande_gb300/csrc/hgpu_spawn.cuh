@@ -24,14 +24,17 @@ __device__ __forceinline__ int64_t upper_bound_off(const int64_t *off, int64_t n
 
 // A warp's chunk of attempts: (parent, space) slot, attempt number in the slot
 // and, for generators whose first draw chooses a single or a double excitation,
-// the stream position after that draw; dlist/slist hold the chunk offsets of
-// the doubles (or of every attempt) and of the singles.
+// the stream position after that draw; list holds the chunk offsets of the
+// doubles (or of every attempt) from its start and those of the singles from
+// its end.  Entries kSpawnChunk + 32 t + j (t = 0 doubles, 1 singles; j < 32)
+// hold the entries of type t left over from the warp's earlier chunks (fewer
+// than 32): they run in the next group of 32 of that type, so that every group
+// but the warp's last runs with all lanes busy.
 struct SpawnQueue {
-    uint32_t slot[kSpawnChunk];
-    uint32_t att[kSpawnChunk];
-    uint64_t bufk[kSpawnChunk];
-    uint8_t dlist[kSpawnChunk];
-    uint8_t slist[kSpawnChunk];
+    uint32_t slot[kSpawnChunk + 64];
+    uint32_t att[kSpawnChunk + 64];
+    uint64_t bufk[kSpawnChunk + 64];
+    uint8_t list[kSpawnChunk];
 };
 
 // One spawning attempt of a queued chunk entry; returns the spawned amount.
@@ -108,14 +111,12 @@ __device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTab
 }
 
 // Resident blocks per SM the spawning kernel is compiled for: four (at most 64
-// registers, half the SM's warps) for the uniform generators of two-word
-// determinants, whose code fits that budget without spilling (3 % faster on the
-// 64-orbital replica list); 0 (no minimum) leaves the others to the compiler,
-// which gives the one-word uniform kernels 64 registers as well (an explicit
-// minimum of 1 lets it take 116 and halves their occupancy).
+// registers, half the SM's warps) for the uniform generators, whose code fits
+// that budget without spilling; 0 (no minimum) leaves the heat-bath and
+// power-Pitzer kernels to the compiler, which gives them up to 128.
 template <int W, int KIND>
 constexpr int spawn_min_blocks() {
-    return W == 2 && (KIND == HGPU_SYS_HUB_K || KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm) ? 4 : 0;
+    return (KIND == HGPU_SYS_HUB_K || KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm) ? 4 : 0;
 }
 
 template <int W, int KIND, typename Real, bool RDM>
@@ -147,14 +148,19 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
     // attempts searches a window of 32 slots starting at the slot of the previous
     // step's last attempt (a lower bound), with the binary search as fallback when
     // a window holds no slot for an attempt (runs of zero-attempt slots).
+    // Each type's attempts run in groups of 32; a chunk's last, partial group of
+    // a type is carried to the next chunk (SpawnQueue), and the carried entries
+    // run once the warp finds no more chunks.
+    int ncarry0 = 0, ncarry1 = 0;  // carried doubles, singles
     for (;;) {
         unsigned long long cbase = 0;
         if (lane == 0) cbase = atomicAdd((unsigned long long *)&st->spawn_next, (unsigned long long)b.spawn_chunk);
         cbase = __shfl_sync(FULL_MASK, cbase, 0);
-        if ((int64_t)cbase >= A) break;
-        const int64_t cend = min((int64_t)cbase + b.spawn_chunk, A);
+        const bool more = (int64_t)cbase < A;
+        if (!more && ncarry0 == 0 && ncarry1 == 0) break;
+        const int64_t cend = more ? min((int64_t)cbase + b.spawn_chunk, A) : (int64_t)cbase;
         int64_t k0 = 0;
-        if (lane == 0) k0 = upper_bound_off(b.aoff, NR, (int64_t)cbase);
+        if (lane == 0 && more) k0 = upper_bound_off(b.aoff, NR, (int64_t)cbase);
         k0 = __shfl_sync(FULL_MASK, k0, 0);
         int nd = 0, ns = 0;
         for (int64_t base = (int64_t)cbase; base < cend; base += 32) {
@@ -190,8 +196,8 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
             uint32_t dball = __ballot_sync(FULL_MASK, valid && !single);
             uint32_t sball = __ballot_sync(FULL_MASK, valid && single);
             int off = (int)(a - (int64_t)cbase);
-            if (valid && !single) q.dlist[nd + __popc(dball & lanemask_lt())] = (uint8_t)off;
-            if (valid && single) q.slist[ns + __popc(sball & lanemask_lt())] = (uint8_t)off;
+            if (valid && !single) q.list[nd + __popc(dball & lanemask_lt())] = (uint8_t)off;
+            if (valid && single) q.list[kSpawnChunk - 1 - ns - __popc(sball & lanemask_lt())] = (uint8_t)off;
             nd += __popc(dball);
             ns += __popc(sball);
             // slot of the last valid attempt of this step: lower bound for the next step
@@ -199,30 +205,38 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
             k0 = __shfl_sync(FULL_MASK, k, last);
         }
         __syncwarp();
-        // doubles (or every attempt), then singles, 32 at a time
+        // doubles (or every attempt), then singles, in groups of 32: the carried
+        // entries of the type first, then the chunk's; the last partial group
+        // is carried unless no chunk is left
         for (int pass = 0; pass < 2; pass++) {
-            const int n = pass == 0 ? nd : ns;
-            const uint8_t *list = pass == 0 ? q.dlist : q.slist;
-            for (int j0 = 0; j0 < n; j0 += 32) {
+            const int c = pass == 0 ? ncarry0 : ncarry1;
+            const int tot = c + (pass == 0 ? nd : ns);
+            const int full = more ? tot & ~31 : tot;
+            const int cbase_e = kSpawnChunk + 32 * pass;  // the type's carried entries
+            for (int j0 = 0; j0 < full; j0 += 32) {
                 bool want = false;
                 Det<W> child, parent_det;
                 int64_t nspawn = 0, nrdm = 0;
                 int sp = 0;
                 uint64_t flagword = 0;
-                if (j0 + lane < n) {
-                    int off = list[j0 + lane];
+                const int j = j0 + lane;
+                if (j < full) {
+                    const int e = j < c ? cbase_e + j : q.list[pass == 0 ? j - c : kSpawnChunk - 1 - (j - c)];
                     uint32_t info;
                     if (pass == 0)
-                        nspawn = spawn_entry<W, KIND, Real, false>(s, t, b, R, dets, iter, q.slot[off], q.att[off],
-                                                                   drew, q.bufk[off], rdm, child, sp, info,
+                        nspawn = spawn_entry<W, KIND, Real, false>(s, t, b, R, dets, iter, q.slot[e], q.att[e],
+                                                                   drew, q.bufk[e], rdm, child, sp, info,
                                                                    parent_det, nrdm);
                     else
-                        nspawn = spawn_entry_single<W, KIND, Real>(s, t, b, R, dets, iter, q.slot[off], q.att[off],
-                                                                   q.bufk[off], rdm, child, sp, info, parent_det,
+                        nspawn = spawn_entry_single<W, KIND, Real>(s, t, b, R, dets, iter, q.slot[e], q.att[e],
+                                                                   q.bufk[e], rdm, child, sp, info, parent_det,
                                                                    nrdm);
                     if (nspawn != 0) {
                         want = true;
-                        flagword = (uint64_t)((info >> 2) & 3u) | ((uint64_t)(cbase + off) << 2);
+                        // the attempt's index: a carried entry's from its slot (aoff[slot - 1] + att)
+                        const uint32_t sl = q.slot[e];
+                        const uint64_t aidx = e >= kSpawnChunk ? (sl > 0 ? b.aoff[sl - 1] : 0) + q.att[e] : cbase + e;
+                        flagword = (uint64_t)((info >> 2) & 3u) | (aidx << 2);
                     }
                 }
                 uint32_t ball = __ballot_sync(FULL_MASK, want);
@@ -266,8 +280,24 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
                     }
                 }
             }
+            __syncwarp();
+            // carry entries full..tot-1 (fewer than 32; none once no chunk is
+            // left): with full == 0 the carried ones stay where they are and
+            // the chunk's are appended; otherwise every carried one ran and the
+            // rest are the chunk's
+            const int rest = tot - full;
+            const int j = full + lane;
+            if (lane < rest && j >= c) {
+                const int off = q.list[pass == 0 ? j - c : kSpawnChunk - 1 - (j - c)];
+                q.slot[cbase_e + lane] = q.slot[off];
+                q.att[cbase_e + lane] = q.att[off];
+                q.bufk[cbase_e + lane] = q.bufk[off];
+            }
+            if (pass == 0) ncarry0 = rest;
+            else ncarry1 = rest;
+            __syncwarp();
         }
-        __syncwarp();
+        if (!more) break;
     }
 }
 

@@ -619,6 +619,17 @@ static int alloc_lists(hgpu_handle *h) {
     b.sflag = nullptr;
     if (h->cfg.initiator_approx)
         if ((rc = dalloc(h, &b.sflag, (size_t)b.scap))) return rc;
+    // the singles queue of the generators that classify their attempts (a
+    // tenth of the attempts with the default p_single; singles past its
+    // capacity run in the spawning kernel itself)
+    b.sq = nullptr;
+    b.sq_cap = 0;
+    const int gk = h->gkind;
+    if (gk == HGPU_SYS_READ_IN || gk == kKindReadInNoRenorm || gk == kKindHeatBathUniform ||
+        gk == kKindPowerPitzerOcc || gk == kKindPowerPitzerRef) {
+        b.sq_cap = b.scap / 4 > (1 << 16) ? b.scap / 4 : (1 << 16);
+        if ((rc = dalloc(h, &b.sq, (size_t)b.sq_cap))) return rc;
+    }
     for (int k = 0; k < 2; k++) {
         if ((rc = dalloc(h, &b.keys[k], (size_t)b.scap * W))) return rc;  // key_words <= W
         if ((rc = dalloc(h, &b.idx[k], (size_t)b.scap))) return rc;

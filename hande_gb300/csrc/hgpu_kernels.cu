@@ -89,6 +89,7 @@ __global__ void k_cycle_begin(DevState *st, const DevSys *sys) {
     st->n_spawn = 0;
     st->n_rdm = 0;
     st->spawn_next = 0;
+    st->n_sq = 0;
     double np = (double)st->abs_pop[0] / (double)sys->real_factor;
     st->nattempts_cycle = llround(2.0 * np);
 }
@@ -392,23 +393,23 @@ static void cycle_w(const DevBuffers &b, int R, int kind, int precision, int cur
     k_set_count<<<1, 1, 0, st>>>(&S->n_slots, &S->n_main, R, nullptr);
     device_scan<int64_t>(b, LoadNatt{b.natt}, StoreInclusive{b.aoff}, &S->n_slots, b.scan_part, &S->n_attempts, st);
     if (pm) cudaEventRecord(pm->ev[2], st);
-#define HGPU_SPAWN(KK)                                                                      \
-    do {                                                                                    \
-        if (precision == HGPU_PREC_MIXED)                                                   \
-            k_spawn<W, KK, float, false><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);      \
-        else                                                                                \
-            k_spawn<W, KK, double, false><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);     \
+#define HGPU_SPAWN(KK)                                                       \
+    do {                                                                     \
+        if (precision == HGPU_PREC_MIXED)                                    \
+            launch_spawn_kernels<W, KK, float, false>(b, R, cur, sm, st);    \
+        else                                                                 \
+            launch_spawn_kernels<W, KK, double, false>(b, R, cur, sm, st);   \
     } while (0)
     if (b.rdm) launch_spawn_rdm(b, W, R, kind, precision, cur, sm, st);  // hgpu_spawn_rdm.cu
     else if (kind == HGPU_SYS_HUB_K)
-        k_spawn<W, HGPU_SYS_HUB_K, double, false><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+        launch_spawn_kernels<W, HGPU_SYS_HUB_K, double, false>(b, R, cur, sm, st);
     else if (kind == kKindHeatBath) HGPU_SPAWN(kKindHeatBath);
     else if (kind == kKindHeatBathUniform) HGPU_SPAWN(kKindHeatBathUniform);
     else if (kind == kKindReadInNoRenorm) HGPU_SPAWN(kKindReadInNoRenorm);
     else if (kind == kKindPowerPitzerOcc)
-        k_spawn<W, kKindPowerPitzerOcc, double, false><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+        launch_spawn_kernels<W, kKindPowerPitzerOcc, double, false>(b, R, cur, sm, st);
     else if (kind == kKindPowerPitzerRef)
-        k_spawn<W, kKindPowerPitzerRef, double, false><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+        launch_spawn_kernels<W, kKindPowerPitzerRef, double, false>(b, R, cur, sm, st);
     else HGPU_SPAWN(HGPU_SYS_READ_IN);
 #undef HGPU_SPAWN
     // determ_projection and deterministic_annihilation (src/fciqmc.f90:394,
@@ -441,9 +442,9 @@ int set_kernel_attributes(const DevBuffers &b) {
 }
 
 int launches_per_cycle(const DevBuffers &b) {
-    // begin, prep, count, scan(3), spawn, clamp, sort_hist, sort_offsets,
-    // one per pass, ann_splits, annihilate (twice), end
-    return 2 + 1 + 3 + 1 + 1 + 2 + b.sort_passes + 3 + 1;
+    // begin, prep, count, scan(3), spawn (and singles), clamp, sort_hist,
+    // sort_offsets, one per pass, ann_splits, annihilate (twice), end
+    return 2 + 1 + 3 + 1 + (b.sq ? 1 : 0) + 1 + 2 + b.sort_passes + 3 + 1;
 }
 
 void launch_annihilation(const DevBuffers &b, int W, int R, int kind, int cur, cudaStream_t st) {

@@ -76,6 +76,7 @@ struct DevState {
     int32_t rep_cycles;
     int32_t pad2;
     uint64_t spawn_next;  // next unclaimed attempt chunk of the spawning kernel
+    int64_t n_sq;         // singles queued for the singles kernel (may pass sq_cap: see k_spawn)
     uint32_t os_ticket[16];  // next tile of each radix pass (hgpu_sort.cuh)
     uint32_t ann_ticket[2];  // next tile of each annihilation pass (hgpu_annihilate.cu)
     // replica 2-RDM (hgpu_rdm.cu)
@@ -106,6 +107,11 @@ struct DevBuffers {
     int64_t *spops;
     uint64_t *sflag;    // initiator bits | generation order << 2
     int64_t scap;
+    // singles of the generators that draw the single/double choice first:
+    // (slot, attempt in slot, stream position) queued by the spawning kernel
+    // for the singles kernel (null for the other generators)
+    uint4 *sq;
+    int64_t sq_cap;
     // sort (hgpu_sort.cuh)
     uint64_t *skeys;    // ranks of the spawned determinants (when use_rank; 32-bit words when key32)
     uint64_t *keys[2];  // key_words per entry (32-bit words when key32)

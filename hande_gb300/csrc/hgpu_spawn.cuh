@@ -110,6 +110,62 @@ __device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTab
                                             parent_det, nspawn_rdm);
 }
 
+// Generators whose first draw chooses a single or a double excitation: their
+// attempts are classified before they run, and the singles (a tenth of the
+// attempts, with code of their own) go to the singles kernel.
+template <int KIND>
+constexpr bool spawn_drew() {
+    return KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm || KIND == kKindHeatBathUniform ||
+           KIND == kKindPowerPitzerOcc || KIND == kKindPowerPitzerRef;
+}
+
+// The warp's spawned particles appended to the spawned list and, with the
+// replica 2-RDM, its RDM spawns to theirs (create_spawned_particle*): one
+// atomic per warp for each list.  Every lane of the warp takes part.
+template <int W>
+__device__ __forceinline__ void spawn_emit(const DevBuffers &b, DevState *st, int R, int lane, bool want,
+                                           const Det<W> &child, int sp, int64_t nspawn, uint64_t flagword,
+                                           bool rdm, int64_t nrdm, const Det<W> &parent_det) {
+    const uint32_t ball = __ballot_sync(FULL_MASK, want);
+    if (ball) {
+        const int leader = __ffs(ball) - 1;
+        unsigned long long basepos = 0;
+        if (lane == leader) basepos = atomicAdd((unsigned long long *)&st->n_spawn, (unsigned long long)__popc(ball));
+        basepos = __shfl_sync(FULL_MASK, basepos, leader);
+        if (want) {
+            const int64_t pos = (int64_t)basepos + __popc(ball & lanemask_lt());
+            if (pos < b.scap) {
+                store_det<W>(b.sdets, pos, child);
+                for (int qq = 0; qq < R; qq++) b.spops[pos * R + qq] = qq == sp ? nspawn : 0;
+                if (b.sflag) b.sflag[pos] = flagword;
+            } else {
+                atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+            }
+        }
+    }
+    if (rdm) {
+        // create_spawned_particle_replica_rdm: (parent, child) and the amount
+        const uint32_t rball = __ballot_sync(FULL_MASK, nrdm != 0);
+        if (rball) {
+            const int leader = __ffs(rball) - 1;
+            unsigned long long rbase = 0;
+            if (lane == leader) rbase = atomicAdd((unsigned long long *)&st->n_rdm, (unsigned long long)__popc(rball));
+            rbase = __shfl_sync(FULL_MASK, rbase, leader);
+            if (nrdm != 0) {
+                const int64_t pos = (int64_t)rbase + __popc(rball & lanemask_lt());
+                if (pos < b.scap) {
+                    store_det<W>(b.rdm_sdets, 2 * pos, parent_det);
+                    store_det<W>(b.rdm_sdets, 2 * pos + 1, child);
+                    b.rdm_spops[pos] = nrdm;
+                    b.rdm_sspace[pos] = (uint8_t)sp;
+                } else {
+                    atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+                }
+            }
+        }
+    }
+}
+
 // Resident blocks per SM the spawning kernel is compiled for: four (at most 64
 // registers, half the SM's warps) for the uniform generators, whose code fits
 // that budget without spilling; 0 (no minimum) leaves the heat-bath and
@@ -140,8 +196,7 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
     // generators whose first draw is the single/double choice: the chunk is
     // split by that draw so that each excitation type runs with the warp
     // converged (a tenth of the attempts are singles, with their own code)
-    constexpr bool drew = KIND == HGPU_SYS_READ_IN || KIND == kKindReadInNoRenorm || KIND == kKindHeatBathUniform ||
-                          KIND == kKindPowerPitzerOcc || KIND == kKindPowerPitzerRef;
+    constexpr bool drew = spawn_drew<KIND>();
     // Each warp claims chunks of b.spawn_chunk consecutive attempts.  The (parent,
     // space) slot of attempt a is the first k with aoff[k] > a; one binary search
     // per chunk finds the slot of its first attempt, and every later step of 32
@@ -205,12 +260,27 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
             k0 = __shfl_sync(FULL_MASK, k, last);
         }
         __syncwarp();
+        // the chunk's singles to the singles kernel's queue; those past its
+        // capacity (the counter may pass it) run here
+        int s0 = 0;
+        if (drew && b.sq && ns > 0) {
+            unsigned long long qb = 0;
+            if (lane == 0) qb = atomicAdd((unsigned long long *)&st->n_sq, (unsigned long long)ns);
+            qb = __shfl_sync(FULL_MASK, qb, 0);
+            const int64_t room = b.sq_cap - (int64_t)qb;
+            s0 = room <= 0 ? 0 : (room < ns ? (int)room : ns);
+            for (int j = lane; j < s0; j += 32) {
+                const int off = q.list[kSpawnChunk - 1 - j];
+                const uint64_t bk = q.bufk[off];
+                b.sq[qb + j] = make_uint4(q.slot[off], q.att[off], (uint32_t)bk, (uint32_t)(bk >> 32));
+            }
+        }
         // doubles (or every attempt), then singles, in groups of 32: the carried
         // entries of the type first, then the chunk's; the last partial group
         // is carried unless no chunk is left
         for (int pass = 0; pass < 2; pass++) {
             const int c = pass == 0 ? ncarry0 : ncarry1;
-            const int tot = c + (pass == 0 ? nd : ns);
+            const int tot = c + (pass == 0 ? nd : ns - s0);
             const int full = more ? tot & ~31 : tot;
             const int cbase_e = kSpawnChunk + 32 * pass;  // the type's carried entries
             for (int j0 = 0; j0 < full; j0 += 32) {
@@ -221,7 +291,7 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
                 uint64_t flagword = 0;
                 const int j = j0 + lane;
                 if (j < full) {
-                    const int e = j < c ? cbase_e + j : q.list[pass == 0 ? j - c : kSpawnChunk - 1 - (j - c)];
+                    const int e = j < c ? cbase_e + j : q.list[pass == 0 ? j - c : kSpawnChunk - 1 - s0 - (j - c)];
                     uint32_t info;
                     if (pass == 0)
                         nspawn = spawn_entry<W, KIND, Real, false>(s, t, b, R, dets, iter, q.slot[e], q.att[e],
@@ -239,46 +309,7 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
                         flagword = (uint64_t)((info >> 2) & 3u) | (aidx << 2);
                     }
                 }
-                uint32_t ball = __ballot_sync(FULL_MASK, want);
-                if (ball) {
-                    int leader = __ffs(ball) - 1;
-                    unsigned long long basepos = 0;
-                    if (lane == leader)
-                        basepos = atomicAdd((unsigned long long *)&st->n_spawn, (unsigned long long)__popc(ball));
-                    basepos = __shfl_sync(FULL_MASK, basepos, leader);
-                    if (want) {
-                        int64_t pos = (int64_t)basepos + __popc(ball & lanemask_lt());
-                        if (pos < b.scap) {
-                            store_det<W>(b.sdets, pos, child);
-                            for (int qq = 0; qq < R; qq++) b.spops[pos * R + qq] = qq == sp ? nspawn : 0;
-                            if (b.sflag) b.sflag[pos] = flagword;
-                        } else {
-                            atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
-                        }
-                    }
-                }
-                if (rdm) {
-                    // create_spawned_particle_replica_rdm: (parent, child) and the amount
-                    const uint32_t rball = __ballot_sync(FULL_MASK, nrdm != 0);
-                    if (rball) {
-                        const int leader = __ffs(rball) - 1;
-                        unsigned long long rbase = 0;
-                        if (lane == leader)
-                            rbase = atomicAdd((unsigned long long *)&st->n_rdm, (unsigned long long)__popc(rball));
-                        rbase = __shfl_sync(FULL_MASK, rbase, leader);
-                        if (nrdm != 0) {
-                            const int64_t pos = (int64_t)rbase + __popc(rball & lanemask_lt());
-                            if (pos < b.scap) {
-                                store_det<W>(b.rdm_sdets, 2 * pos, parent_det);
-                                store_det<W>(b.rdm_sdets, 2 * pos + 1, child);
-                                b.rdm_spops[pos] = nrdm;
-                                b.rdm_sspace[pos] = (uint8_t)sp;
-                            } else {
-                                atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
-                            }
-                        }
-                    }
-                }
+                spawn_emit<W>(b, st, R, lane, want, child, sp, nspawn, flagword, rdm, nrdm, parent_det);
             }
             __syncwarp();
             // carry entries full..tot-1 (fewer than 32; none once no chunk is
@@ -288,7 +319,7 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
             const int rest = tot - full;
             const int j = full + lane;
             if (lane < rest && j >= c) {
-                const int off = q.list[pass == 0 ? j - c : kSpawnChunk - 1 - (j - c)];
+                const int off = q.list[pass == 0 ? j - c : kSpawnChunk - 1 - s0 - (j - c)];
                 q.slot[cbase_e + lane] = q.slot[off];
                 q.att[cbase_e + lane] = q.att[off];
                 q.bufk[cbase_e + lane] = q.bufk[off];
@@ -298,6 +329,58 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
             __syncwarp();
         }
         if (!more) break;
+    }
+}
+
+// The queued singles (k_spawn above), 32 per warp at a time: the single
+// excitations' code runs in a kernel of its own, so that the spawning kernel's
+// loop stays small in the instruction cache.
+template <int W, int KIND, typename Real, bool RDM>
+__global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn_singles(DevBuffers b, int R, int cur) {
+    __shared__ DevSys s;
+    extern __shared__ uint8_t smem[];
+    stage_sys(s, b.sys);
+    HubTables t = stage_hub(b.sys, smem);
+    __syncthreads();
+    DevState *st = b.state;
+    const int64_t n = st->n_sq < b.sq_cap ? st->n_sq : b.sq_cap;
+    const uint64_t iter = (uint64_t)st->iter;
+    const uint64_t *dets = b.dets[cur];
+    const int lane = threadIdx.x & 31;
+    const bool rdm = RDM && b.rdm != nullptr && st->rdm_on != 0;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32) {
+        bool want = false;
+        Det<W> child, parent_det;
+        int64_t nspawn = 0, nrdm = 0;
+        int sp = 0;
+        uint64_t flagword = 0;
+        const int64_t j = base + lane;
+        if (j < n) {
+            const uint4 e = b.sq[j];
+            uint32_t info;
+            nspawn = spawn_entry_single<W, KIND, Real>(s, t, b, R, dets, iter, e.x, e.y,
+                                                       (uint64_t)e.z | ((uint64_t)e.w << 32), rdm, child, sp, info,
+                                                       parent_det, nrdm);
+            if (nspawn != 0) {
+                want = true;
+                // the attempt's index: aoff[slot - 1] + attempt in the slot
+                const uint64_t aidx = (e.x > 0 ? b.aoff[e.x - 1] : 0) + e.y;
+                flagword = (uint64_t)((info >> 2) & 3u) | (aidx << 2);
+            }
+        }
+        spawn_emit<W>(b, st, R, lane, want, child, sp, nspawn, flagword, rdm, nrdm, parent_det);
+    }
+}
+
+// The spawning kernel and, for the generators that classify their attempts,
+// the singles kernel after it.
+template <int W, int KIND, typename Real, bool RDM>
+void launch_spawn_kernels(const DevBuffers &b, int R, int cur, size_t sm, cudaStream_t st) {
+    k_spawn<W, KIND, Real, RDM><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+    if constexpr (spawn_drew<KIND>()) {
+        if (b.sq) k_spawn_singles<W, KIND, Real, RDM><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
     }
 }
 

@@ -8,20 +8,20 @@ namespace hgpu {
 
 template <int W>
 static void spawn_rdm_w(const DevBuffers &b, int R, int kind, int precision, int cur, size_t sm, cudaStream_t st) {
-#define HGPU_SPAWN_RDM(KK)                                                                  \
-    do {                                                                                    \
-        if (precision == HGPU_PREC_MIXED)                                                   \
-            k_spawn<W, KK, float, true><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);       \
-        else                                                                                \
-            k_spawn<W, KK, double, true><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);      \
+#define HGPU_SPAWN_RDM(KK)                                                  \
+    do {                                                                    \
+        if (precision == HGPU_PREC_MIXED)                                   \
+            launch_spawn_kernels<W, KK, float, true>(b, R, cur, sm, st);    \
+        else                                                                \
+            launch_spawn_kernels<W, KK, double, true>(b, R, cur, sm, st);   \
     } while (0)
     if (kind == kKindHeatBath) HGPU_SPAWN_RDM(kKindHeatBath);
     else if (kind == kKindHeatBathUniform) HGPU_SPAWN_RDM(kKindHeatBathUniform);
     else if (kind == kKindReadInNoRenorm) HGPU_SPAWN_RDM(kKindReadInNoRenorm);
     else if (kind == kKindPowerPitzerOcc)
-        k_spawn<W, kKindPowerPitzerOcc, double, true><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+        launch_spawn_kernels<W, kKindPowerPitzerOcc, double, true>(b, R, cur, sm, st);
     else if (kind == kKindPowerPitzerRef)
-        k_spawn<W, kKindPowerPitzerRef, double, true><<<b.spawn_grid, kBlock, sm, st>>>(b, R, cur);
+        launch_spawn_kernels<W, kKindPowerPitzerRef, double, true>(b, R, cur, sm, st);
     else HGPU_SPAWN_RDM(HGPU_SYS_READ_IN);
 #undef HGPU_SPAWN_RDM
 }

@@ -269,9 +269,20 @@ __global__ void __launch_bounds__(kBlock) k_ann_splits(DevBuffers b, int cur, co
 // Philox rounding of neighbouring entries runs together; the survivors are
 // compacted by one block scan and written, K_ii included, with consecutive
 // threads on consecutive outputs.
+// Resident blocks per SM: four for two-word determinants (tiles of 1024, the
+// exact-diagonal tables read through L1: shared memory allows four, and the
+// extra warps cover the gathers' latency -- 3 % faster than three at 80
+// registers, despite a few spilled words), three for one-word ones (tiles of
+// 2048 with staged tables, which shared memory limits to three).
+template <int W>
+constexpr int ann_min_blocks() {
+    return W == 2 ? 4 : 3;
+}
+
 template <int W, bool RANK>
-__global__ void __launch_bounds__(kBlock, 3) k_annihilate(DevBuffers b, int R, int cur, const uint64_t *keys,
-                                                          const uint32_t *idx, int mode) {
+__global__ void __launch_bounds__(kBlock, ann_min_blocks<W>()) k_annihilate(DevBuffers b, int R, int cur,
+                                                                            const uint64_t *keys, const uint32_t *idx,
+                                                                            int mode) {
     constexpr int TILE = ann_tile<W>();
     constexpr int PER = TILE / kBlock;  // consecutive merged positions per thread
     static_assert(PER == 4 || PER == 8, "a thread's codes are read as one 8- or 16-byte word");

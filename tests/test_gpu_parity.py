@@ -177,6 +177,31 @@ def test_whole_run_bit_exact(name, opts, nrep):
         assert_close(rg.rspawn, ro.rspawn, 1e-12)
 
 
+def test_singles_queue_overflow_bit_exact():
+    """The spawning kernel queues singles for the singles kernel in a queue of
+    a quarter of the spawned list's capacity (at least 65536 entries) and runs
+    the ones past it itself: with p_single = 0.8 and 2e5 attempts per cycle
+    about 1.6e5 singles meet a queue of 125000, so every cycle takes both
+    paths.  The walker lists stay those of the oracle."""
+    s = SYS["mol26"]
+    cfg = make_config(s, tau=5e-5, init_pop=2e5, target_population=1e12, real_amplitudes=True,
+                      pattempt_single=0.8, pattempt_double=0.2, ncycles=2, seed=11, state_size=1500000,
+                      spawned_state_size=500000)
+    o = Oracle(s, cfg)
+    g = engine(s, cfg)
+    o.initial_distribution()
+    g.initial_distribution()
+    for r in range(2):
+        ro = o.run_report()
+        rg = g.run_report()
+        assert ro.error_flags == 0 and rg.error_flags == 0
+        assert rg.nattempts > 2 * 150000  # two cycles of > 1.5e5 attempts: > 1.2e5 singles each
+        np.testing.assert_array_equal(g.walkers()[0], o.walkers()[0], err_msg="report %d states" % r)
+        np.testing.assert_array_equal(g.walkers()[1], o.walkers()[1], err_msg="report %d pops" % r)
+        assert rg.nspawned == ro.nspawned
+        assert rg.nattempts == ro.nattempts
+
+
 def test_checkpoint_restore_bit_exact(tmp_path):
     s = SYS["hub_k_4x4"]
     cfg = make_config(s, tau=0.005, init_pop=10, target_population=2000, ncycles=10, seed=3, state_size=100000,

@@ -1,9 +1,11 @@
-// hgpu_spawn.cuh -- the spawning kernel of one cycle: excitation generation,
+// hgpu_spawn.cuh -- the spawning kernels of one cycle: excitation generation,
 // attempt_to_spawn and the append to the spawned list (src/spawning.F90:34-123,
 // 215-315, 588-768), templated on the system / generator kind, the arithmetic
-// of the generators and whether replica 2-RDM spawns are recorded.  Included by
-// the translation units that instantiate it (hgpu_kernels.cu without the RDM,
-// hgpu_spawn_rdm.cu with it).
+// of the generators and whether replica 2-RDM spawns are recorded.  k_spawn
+// classifies the attempts and runs the doubles (or, for the generators that do
+// not draw the single/double choice first, every attempt); k_spawn_singles runs
+// the singles it queued.  Included by the translation units that instantiate
+// them (hgpu_kernels.cu without the RDM, hgpu_spawn_rdm.cu with it).
 #pragma once
 
 #include "hgpu_common.cuh"
@@ -29,7 +31,8 @@ __device__ __forceinline__ int64_t upper_bound_off(const int64_t *off, int64_t n
 // its end.  Entries kSpawnChunk + 32 t + j (t = 0 doubles, 1 singles; j < 32)
 // hold the entries of type t left over from the warp's earlier chunks (fewer
 // than 32): they run in the next group of 32 of that type, so that every group
-// but the warp's last runs with all lanes busy.
+// but the warp's last runs with all lanes busy.  (Singles reach type 1 only
+// when the singles kernel's queue is full.)
 struct SpawnQueue {
     uint32_t slot[kSpawnChunk + 64];
     uint32_t att[kSpawnChunk + 64];

@@ -390,25 +390,17 @@ def cpu_slice(s, cfg, st, po, da, state, n, seconds):
 REF_TARGET = 4e6  # total walkers of the reference arm's calculation (both replicas)
 
 
-def reference_arm(args):
-    """The reference algorithm as HANDE runs it on many cores: the CPU
-    restatement of the cycle, one calculation hash-partitioned over every host
-    core (threads as ranks: owner = modulo(MurmurHash2(det), ranks), the
-    spawned walkers and RDM spawns exchanged every cycle, estimators summed per
-    report), on the headline system and parameters.  The population is bounded
-    (REF_TARGET walkers over both replicas, grown from the reference
-    determinant) so that the run ends in a few minutes; then, like the GPU
-    arm, every shift varies (the RDM accumulates), the list is saved, and each
-    of W warm-up and K timed steps is one cycle from that list (restored,
-    untimed)."""
-    from hande_gb300._abi import PREC_FP64
+def cpu_reference_rate(s, cfg, ncores, target, steps, warmup, replicas):
+    """The CPU restatement run as HANDE runs: one calculation hash-partitioned
+    over `ncores` host threads (threads as ranks: owner =
+    modulo(MurmurHash2(det), ranks), spawned walkers and RDM spawns exchanged
+    every cycle, estimators summed per report), grown from the reference
+    determinant with the shift held until it holds about `target` walkers (the
+    bounded sample); then every shift varies, the list is saved, and each of
+    `warmup` and `steps` steps is one cycle from that list (restored, untimed),
+    the cycle timed on the host.  Returns (attempts/s, seconds per cycle,
+    walkers, states, growth reports, attempts per step)."""
     from oracle.pyoracle import OraclePar
-    ncores = os.cpu_count() or 1
-    target = float(os.environ.get("HGPU_REF_TARGET", REF_TARGET))
-    s = large_system()
-    cfg = large_config(s, PREC_FP64, main_cap=int(2 * target / ncores) + 100000,
-                       spawn_cap=int(3 * target / ncores) + 100000, init_pop=target / 500.0)
-    t_start = time.perf_counter()
     o = OraclePar(s, cfg, ncores)
     o.initial_distribution()
     last = None
@@ -417,21 +409,22 @@ def reference_arm(args):
         rep = o.run_report()
         grown = r + 1
         if rep.error_flags:
-            raise RuntimeError("reference arm: list overflow while growing (flags %d)" % rep.error_flags)
-        tot = rep.nparticles[0] + rep.nparticles[1]
+            raise RuntimeError("CPU restatement: list overflow while growing (flags %d)" % rep.error_flags)
+        tot = sum(rep.nparticles[q] for q in range(replicas))
         g = tot / last if last else 1.0
         if tot >= 0.9 * target or tot * g > 1.2 * target:
             break
         last = tot
     st = o.state()
-    st.vary_shift[0] = st.vary_shift[1] = 1
+    for q in range(replicas):
+        st.vary_shift[q] = 1
     o.set_state(st)
     o.snapshot()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         o.snapshot(restore=True)
         o.run_report()
     secs, att = [], 0
-    for _ in range(args.steps):
+    for _ in range(steps):
         o.snapshot(restore=True)
         o.begin_report()
         a0 = o.total_attempts()
@@ -441,20 +434,38 @@ def reference_arm(args):
         att += o.total_attempts() - a0
         o.end_report()
     o.close()
-    rate = att / sum(secs)
+    walkers = sum(rep.nparticles[q] for q in range(replicas))
+    return att / sum(secs), float(np.mean(secs)), walkers, int(rep.nstates), grown, att / steps
+
+
+def reference_arm(args):
+    """The reference algorithm as HANDE runs it on many cores
+    (cpu_reference_rate) on the headline system and parameters, with the
+    population bounded (REF_TARGET walkers over both replicas, grown from the
+    reference determinant) so that the run ends in a few minutes; like the GPU
+    arm, every shift then varies (the RDM accumulates), the list is saved, and
+    each of W warm-up and K timed steps is one cycle from that list."""
+    from hande_gb300._abi import PREC_FP64
+    ncores = os.cpu_count() or 1
+    target = float(os.environ.get("HGPU_REF_TARGET", REF_TARGET))
+    s = large_system()
+    cfg = large_config(s, PREC_FP64, main_cap=int(2 * target / ncores) + 100000,
+                       spawn_cap=int(3 * target / ncores) + 100000, init_pop=target / 500.0)
+    t_start = time.perf_counter()
+    rate, sec, walkers, states, grown, att_step = cpu_reference_rate(s, cfg, ncores, target, args.steps, args.warmup,
+                                                                     2)
     sample = ("one calculation over %d host cores (threads as hash-partitioned ranks), grown to %.3g walkers "
-              "(%d states) in %d cycles; each step one cycle from that list" % (
-                  ncores, rep.nparticles[0] + rep.nparticles[1], rep.nstates, grown))
+              "(%d states) in %d cycles; each step one cycle from that list" % (ncores, walkers, states, grown))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "attempts/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": LARGE_WORKLOAD, "sample": sample,
                    "parallelism": "one calculation hash-partitioned over all host cores"},
         "cpu_baseline": {"value": rate, "unit": "attempts/s", "cores": ncores, "kind": "port",
                          "sample": sample + " (CPU restatement of HANDE's cycle and MPI decomposition)"},
         "e2e": {"value": rate, "unit": "attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "attempts_per_step": att / args.steps,
+        "attempts_per_step": att_step,
         "wall_s": time.perf_counter() - t_start,
     }
     print(json.dumps(line))
@@ -556,7 +567,7 @@ PRECISION_WORKLOAD = ("config3: synthetic molecule M=48 nel=16 C1 (96 spin orbit
 
 
 def precision_study(target=1e8, tau=1e-4, ncycles=1, equil=100, reports=500, nsample=1 << 20, seed=2024,
-                    max_grow=2000):
+                    max_grow=2000, cpu=True):
     """config 3: the mixed-precision engine against the FP64 engine.  The FP64
     engine grows the population from the reference determinant until the shift
     varies (target walkers) and equilibrates for `equil` reports; its list and
@@ -571,7 +582,10 @@ def precision_study(target=1e8, tau=1e-4, ncycles=1, equil=100, reports=500, nsa
     the reblocked per-report difference of the two runs' E_proj (paired: the
     shared random numbers cancel most of the noise until the runs drift apart),
     attempts/s of each, and the largest error of FP32 H_ij and p_gen over
-    nsample excitations generated from list parents with the same streams."""
+    nsample excitations generated from list parents with the same streams.
+    With cpu, the CPU restatement of the same calculation (FP64) on every host
+    core, hash-partitioned as HANDE runs it (cpu_reference_rate), on a bounded
+    sample grown from the reference determinant."""
     from hande_gb300 import analysis, systems
     from hande_gb300._abi import PREC_FP64, PREC_MIXED, make_config
     from hande_gb300.engine import Engine
@@ -667,6 +681,21 @@ def precision_study(target=1e8, tau=1e-4, ncycles=1, equil=100, reports=500, nsa
     out["D0_mean"] = {k: float(np.mean(v[1])) for k, v in series.items()}
     out["fp32_speedup"] = out["fp32"]["attempts_per_s"] / out["fp64"]["attempts_per_s"]
     out["error_flags"] = flags
+    if cpu:
+        ncores = os.cpu_count() or 1
+        tgt = float(os.environ.get("HGPU_REF_TARGET", REF_TARGET))
+        ccfg = make_config(s, tau=tau, init_pop=tgt / 50.0, target_population=1e300, ncycles=5, seed=77,
+                           real_amplitudes=True, spawn_cutoff=0.01, excit_gen="heat_bath", initiator=True,
+                           initiator_threshold=3.0, precision=PREC_FP64, state_size=int(2 * tgt / ncores) + 100000,
+                           spawned_state_size=int(3 * tgt / ncores) + 100000)
+        t0 = time.perf_counter()
+        rate, sec, walkers, states, grown, att = cpu_reference_rate(s, ccfg, ncores, tgt, 3, 1, 1)
+        out["cpu_reference"] = {
+            "value": rate, "unit": "attempts/s", "cores": ncores, "kind": "port", "ms_per_cycle": 1e3 * sec,
+            "sample": "one FP64 calculation of the same system over %d host cores (threads as hash-partitioned "
+                      "ranks), grown to %.3g walkers (%d states) in %d reports of 5 cycles; 3 cycles from that "
+                      "list timed" % (ncores, walkers, states, grown),
+            "wall_s": time.perf_counter() - t0}
     return out
 
 
@@ -851,7 +880,7 @@ def main():
         return
     if args.config == 3:
         if rank == 0:
-            print(json.dumps(precision_study(target=args.c3_target, reports=args.c3_reports)))
+            print(json.dumps(precision_study(target=args.c3_target, reports=args.c3_reports, cpu=not args.no_cpu)))
         return
     if args.config == 1:
         if rank == 0:

@@ -20,11 +20,11 @@ to device (untimed) before it; every replay draws fresh random numbers.
              estimators) on the same workload and its E_proj against FP64
   parity     one cycle of the GPU engine against the oracle from the same
              list, state and iteration: a slice of the benchmark's own list at
-             the headline parameters, and the full config-2 list
+             the headline parameters, and the whole 26-orbital list
   cpu_baseline  the oracle (C restatement of HANDE's cycle), one core, on a
              bounded slice of the same walker list
-  config2    the 26-orbital molecule of the previous headline (FP64, ~1e7
-             walkers): attempts/s, phases and rooflines
+  mol26      the 26-orbital molecule (FP64, ~1e7 walkers): attempts/s,
+             phases and rooflines
   batched    128 Hubbard calculations advanced together
 
 --impl reference times the CPU restatement of the reference algorithm as HANDE
@@ -51,7 +51,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "spawn attempts/s & iter time @1 GB300: FP32-batched vs FP64 plain at equal E_proj σ"
-WORKLOAD = ("config2: synthetic molecule M=26 nel=10 C1, real amplitudes, cutoff 0.01, uniform renorm p_double=0.9, "
+WORKLOAD = ("synthetic molecule M=26 nel=10 C1, real amplitudes, cutoff 0.01, uniform renorm p_double=0.9, "
             "tau=1e-3, ~1e7 walkers, FP64; each step = one full cycle on the same device-grown walker list")
 
 
@@ -157,7 +157,7 @@ def grow(eng, target, max_cycles=400, verbose=False):
 
 
 def cpu_sample_on_state(states, pops, dat, seconds=10.0, seed=7):
-    """The oracle timed on whole cycles of the engine's own config-2 walker list."""
+    """The oracle timed on whole cycles of the engine's own 26-orbital walker list."""
     from oracle.pyoracle import Oracle
     n = states.shape[0]
     s, cfg = system_and_config(target=1e7, seed_rng=seed, cap_main=int(3 * n) + 1000, cap_spawn=int(4 * n) + 1000)
@@ -207,7 +207,7 @@ def parity_cycle(s, cfg, st, po, da, state, sample):
     return out
 
 
-LARGE_WORKLOAD = ("config5: synthetic molecule M=64 nel=20 ms=0 C1 (two-word determinants, 75-bit rank keys), "
+LARGE_WORKLOAD = ("synthetic molecule M=64 nel=20 ms=0 C1 (two-word determinants, 75-bit rank keys), "
                   "initiator FCIQMC (threshold 3) with 2 replicas (quadrature initiator) and the replica 2-RDM, real "
                   "amplitudes, spawn cutoff 0.01, uniform renorm generator (p_double 0.9), tau 2e-4, grown on the "
                   "device to ~5e8 walkers over both replicas; each step = one cycle on that same walker list")
@@ -471,7 +471,7 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
-BATCH_WORKLOAD = ("config4: 128 independent Hubbard k-space calculations (2D periodic LxL, L in 3..6, "
+BATCH_WORKLOAD = ("128 independent Hubbard k-space calculations (2D periodic LxL, L in 3..6, "
                   "U in {2,4,8}, electrons = sites - 2, ms = 0 or 1 for odd counts, integer walkers, targets "
                   "log-uniform in [1e4, 1e6], seeded draw) advanced together, one graph launch per cycle")
 
@@ -509,7 +509,7 @@ def batched_instances(n=128, seed=4):
 
 
 def batched_measure(steps, equil_cycles=150, tune=True):
-    """config 4: every instance starts with its target population on the
+    """The batch: every instance starts with its target population on the
     reference determinant; `equil_cycles` untimed cycles (a report after each,
     so that the shift acts every cycle) spread it out; the launch shapes are
     tuned on those lists (hande_gb300.autotune, untimed); then `steps` batch
@@ -561,14 +561,14 @@ def batched_measure(steps, equil_cycles=150, tune=True):
                       "host_wall_value: host clock around the call"}
 
 
-PRECISION_WORKLOAD = ("config3: synthetic molecule M=48 nel=16 C1 (96 spin orbitals, 2-word determinants), heat-bath "
+PRECISION_WORKLOAD = ("synthetic molecule M=48 nel=16 C1 (96 spin orbitals, 2-word determinants), heat-bath "
                       "excitation generator, initiator (threshold 3), real amplitudes, cutoff 0.01; FP32 spawning "
                       "(integrals, heat-bath weights, p_gen) against FP64 with the same seed")
 
 
 def precision_study(target=1e8, tau=1e-4, ncycles=1, equil=100, reports=500, nsample=1 << 20, seed=2024,
                     max_grow=2000, cpu=True):
-    """config 3: the mixed-precision engine against the FP64 engine.  The FP64
+    """The mixed-precision engine against the FP64 engine (48 orbitals, 1e8 walkers).  The FP64
     engine grows the population from the reference determinant until the shift
     varies (target walkers) and equilibrates for `equil` reports; its list and
     state then seed both runs, so that the FP64 and FP32 engines start from the
@@ -699,13 +699,13 @@ def precision_study(target=1e8, tau=1e-4, ncycles=1, equil=100, reports=500, nsa
     return out
 
 
-HUBBARD_WORKLOAD = ("config1: Hubbard model in momentum space, 2D 4x4 periodic, t=1, U=4, 10 electrons (ms=0), "
+HUBBARD_WORKLOAD = ("Hubbard model in momentum space, 2D 4x4 periodic, t=1, U=4, 10 electrons (ms=0), "
                     "integer walkers, 10 on the reference at the start, target 5e4, tau=0.005, shift damping 0.05, "
                     "mc_cycles 10 x 2000 reports (20000 iterations), FP64")
 
 
 def hubbard_run(excit_gen="renorm", nreports=2000, seed=7):
-    """config 1 as specified: the whole 20000-iteration run on the device,
+    """The Hubbard 4x4 run as specified: the whole 20000-iteration run on the device,
     one report per host call; attempts/s and time per iteration over the
     reports after the shift starts varying (device time of the cycles), and
     the reblocked shift and E_proj of that part."""
@@ -746,9 +746,9 @@ def hubbard_run(excit_gen="renorm", nreports=2000, seed=7):
 
 
 def semi_stoch_run(size, steps=10, warmup=3, target=1e7):
-    """The config-2 cycle with a semi-stochastic 'high' space of `size`
+    """The 26-orbital cycle with a semi-stochastic 'high' space of `size`
     determinants (src/semi_stoch.F90): the walker list is grown as for the
-    config-2 line, moved into a second calculation whose space is built at its
+    26-orbital line, moved into a second calculation whose space is built at its
     first cycle from that list, then whole cycles are timed from a snapshot
     taken after the build.  Returns the per-cycle device time, the phase split
     and the one-time cost of building the space."""
@@ -787,7 +787,7 @@ def semi_stoch_run(size, steps=10, warmup=3, target=1e7):
     b.close()
     if flags:
         raise RuntimeError("semi-stochastic run flagged errors (%d)" % flags)
-    return {"workload": "config2 cycle with a semi-stochastic 'high' space of %d determinants, built from the "
+    return {"workload": "26-orbital molecule cycle with a semi-stochastic 'high' space of %d determinants, built from the "
                         "grown %d-state list" % (size, st.shape[0]),
             "space_size": int(size), "steps": steps, "ms_per_step": dev_ms / steps,
             "attempts_per_s": attempts / (dev_ms / 1e3),
@@ -805,7 +805,7 @@ def device_free_bytes():
     return int(free.value)
 
 
-def config2_measure(steps, warmup, rank=0, cpu_seconds=10.0, parity=True):
+def mol26_measure(steps, warmup, rank=0, cpu_seconds=10.0, parity=True):
     """The 26-orbital molecule (M = 26, 10 electrons, tau 1e-3, real amplitudes,
     FP64, ~1e7 walkers): attempts/s and iteration time over K replayed cycles,
     per-phase times, the rooflines, one cycle of the oracle on the same list
@@ -830,7 +830,7 @@ def config2_measure(steps, warmup, rank=0, cpu_seconds=10.0, parity=True):
         st, po, da = eng.walkers()
         state = eng.get_state()
         out["parity"] = parity_cycle(s, cfg, st, po, da, state,
-                                     "one cycle of the whole %d-state config-2 list" % st.shape[0])
+                                     "one cycle of the whole %d-state 26-orbital list" % st.shape[0])
         c = cpu_sample_on_state(st, po, da, cpu_seconds)
         out["cpu_baseline"] = {"value": c["attempts"] / c["seconds"], "unit": "attempts/s", "cores": 1,
                                "kind": "port", "sample": "CPU oracle, 1 core, %d whole cycle(s) of the %.3g-walker "
@@ -861,15 +861,16 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle legs (parity and cpu_baseline)")
-    ap.add_argument("--no-batched", action="store_true", help="skip the batched (config 4) measurement")
-    ap.add_argument("--no-extra", action="store_true", help="skip the FP32 run and the config-2 line")
-    ap.add_argument("--config", type=int, default=5,
-                    help="5: the headline line (default); 2: the config-2 measurement alone; 1: the Hubbard 4x4 "
-                         "run of config 1; 3: the mixed-precision study of config 3 (one JSON line each)")
-    ap.add_argument("--c3-target", type=float, default=1e8, help="config 3: target population")
-    ap.add_argument("--c3-reports", type=int, default=500, help="config 3: measured reports of each precision")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched measurement (128 Hubbard calculations)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the FP32 run and the 26-orbital line")
+    ap.add_argument("--workload", default="large", choices=["large", "mol26", "hubbard", "precision"],
+                    help="large: the headline line (default); mol26: the 26-orbital measurement alone; hubbard: "
+                         "the Hubbard 4x4 run; precision: the mixed-precision study (one JSON line each)")
+    ap.add_argument("--precision-target", type=float, default=1e8, help="precision study: target population")
+    ap.add_argument("--precision-reports", type=int, default=500,
+                    help="precision study: measured reports of each precision")
     ap.add_argument("--semi-stoch", type=int, default=0,
-                    help="time the config-2 cycle with a semi-stochastic 'high' space of this size (one JSON line)")
+                    help="time the 26-orbital cycle with a semi-stochastic 'high' space of this size (one JSON line)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -878,19 +879,20 @@ def main():
         if rank == 0:
             reference_arm(args)
         return
-    if args.config == 3:
+    if args.workload == "precision":
         if rank == 0:
-            print(json.dumps(precision_study(target=args.c3_target, reports=args.c3_reports, cpu=not args.no_cpu)))
+            print(json.dumps(precision_study(target=args.precision_target, reports=args.precision_reports,
+                                             cpu=not args.no_cpu)))
         return
-    if args.config == 1:
+    if args.workload == "hubbard":
         if rank == 0:
             print(json.dumps({"workload": HUBBARD_WORKLOAD, "renorm": hubbard_run("renorm"),
                               "no_renorm": hubbard_run("no_renorm")}))
         return
-    if args.config == 2:
+    if args.workload == "mol26":
         if rank == 0:
-            print(json.dumps(config2_measure(args.steps, args.warmup, cpu_seconds=args.cpu_seconds,
-                                             parity=not args.no_cpu)))
+            print(json.dumps(mol26_measure(args.steps, args.warmup, cpu_seconds=args.cpu_seconds,
+                                           parity=not args.no_cpu)))
         return
     if args.semi_stoch > 0:
         if rank == 0:
@@ -1010,7 +1012,7 @@ def main():
                     "excitations generated from list parents with the same random streams as FP64's"}
     del st, po, da
     if rank == 0 and not args.no_extra:
-        extra["config2"] = config2_measure(args.steps, args.warmup, cpu_seconds=args.cpu_seconds,
+        extra["mol26"] = mol26_measure(args.steps, args.warmup, cpu_seconds=args.cpu_seconds,
                                            parity=not args.no_cpu)
     batched = None
     if rank == 0 and not args.no_batched:

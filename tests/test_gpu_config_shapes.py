@@ -2,16 +2,16 @@
 populations the oracle finishes in seconds: the GPU engine against the oracle,
 walker lists bit-exact after every report, counters and bloom statistics equal.
 
-- config 2: the synthetic molecule of the benchmark (M = 26, 10 electrons, C1,
+- the 26-orbital synthetic molecule of the benchmark (10 electrons, C1,
   Hamiltonian seed 2024), tau 1e-3, real amplitudes, spawn cutoff 0.01, uniform
   renorm generator with pattempt_single 0.1 / pattempt_double 0.9; plain and
   initiator (threshold 3).  This Hamiltonian grows about threefold per cycle at
   tau 1e-3, so the reports are one cycle long.
-- config 5: the synthetic molecule with M = 64 (two-word determinants, 75-bit
+- the headline's synthetic molecule with M = 64 (two-word determinants, 75-bit
   rank keys) and 20 electrons, initiator, two replicas with the quadrature
   initiator test, the replica 2-RDM accumulating; FP64 (the FP32 mode is
   checked against the oracle with tolerances in test_gpu_heat_bath.py).
-The config-2 runs spawn many events of 3 or more particles, so the bloom
+The 26-orbital runs spawn many events of 3 or more particles, so the bloom
 counters (accumulate_bloom_stats) are compared on non-zero values."""
 
 import numpy as np
@@ -24,8 +24,8 @@ from tests.test_gpu_parity import assert_close, engine
 
 pytestmark = pytest.mark.gpu
 
-CONFIG2 = dict(tau=1e-3, real_amplitudes=True, spawn_cutoff=0.01, excit_gen="renorm", pattempt_single=0.1,
-               pattempt_double=0.9, init_pop=10, target_population=5000, ncycles=1)
+MOL26 = dict(tau=1e-3, real_amplitudes=True, spawn_cutoff=0.01, excit_gen="renorm", pattempt_single=0.1,
+             pattempt_double=0.9, init_pop=10, target_population=5000, ncycles=1)
 
 
 def compare_reports(o, g, nrep, rdm=False):
@@ -55,10 +55,10 @@ def compare_reports(o, g, nrep, rdm=False):
 
 
 @pytest.mark.parametrize("initiator", [False, True])
-def test_config2_parameters_bit_exact(initiator):
+def test_mol26_benchmark_parameters_bit_exact(initiator):
     s = systems.synthetic_molecule(26, 10, seed=2024)
     cfg = make_config(s, seed=7, initiator=initiator, initiator_threshold=3.0, state_size=400000,
-                      spawned_state_size=600000, **CONFIG2)
+                      spawned_state_size=600000, **MOL26)
     o = Oracle(s, cfg)
     g = engine(s, cfg)
     o.initial_distribution()
@@ -70,7 +70,7 @@ def test_config2_parameters_bit_exact(initiator):
 
 
 @pytest.mark.parametrize("quadrature", [True, False])
-def test_config5_shape_bit_exact(quadrature):
+def test_mol64_replica_shape_bit_exact(quadrature):
     s = systems.synthetic_molecule(64, 20, seed=2024)
     cfg = make_config(s, tau=2e-4, init_pop=300, target_population=500, ncycles=2, seed=5, real_amplitudes=True,
                       spawn_cutoff=0.01, excit_gen="renorm", pattempt_single=0.1, pattempt_double=0.9,

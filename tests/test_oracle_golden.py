@@ -43,7 +43,7 @@ def test_fci_energies(case):
 
 
 def test_hubbard_4x4_basis():
-    """Config-1 lattice: 16 k-points, closed-shell aufbau reference (10 e)."""
+    """The 4x4 lattice of the benchmark's Hubbard run: 16 k-points, closed-shell aufbau reference (10 e)."""
     s = systems.hubbard_k([[4, 0], [0, 4]], 10, U=4.0, t=1.0)
     assert s.nbasis == 32 and s.nwords == 1
     assert abs(s.coulomb_k - 0.25) < 1e-15

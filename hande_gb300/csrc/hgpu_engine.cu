@@ -700,7 +700,8 @@ static int alloc_lists(hgpu_handle *h) {
         b.npairs = (int64_t)h->hsys.nbasis * (h->hsys.nbasis - 1) / 2;
         if ((rc = dalloc(h, &b.rdm, (size_t)(b.npairs * b.npairs)))) return rc;
         CK(cudaMemset(b.rdm, 0, sizeof(double) * (size_t)(b.npairs * b.npairs)));
-        if ((rc = dalloc(h, &b.rdm_sdets, (size_t)b.scap * 2 * W))) return rc;
+        if ((rc = dalloc(h, &b.rdm_schild, (size_t)b.scap * W))) return rc;
+        if ((rc = dalloc(h, &b.rdm_sparent, (size_t)b.scap))) return rc;
         if ((rc = dalloc(h, &b.rdm_spops, (size_t)b.scap))) return rc;
         if ((rc = dalloc(h, &b.rdm_sspace, (size_t)b.scap))) return rc;
         if ((rc = dalloc(h, &b.rdm_rows, (size_t)(2 * b.npairs)))) return rc;

@@ -144,7 +144,8 @@ struct DevBuffers {
     // replica 2-RDM (hgpu_rdm.cu; null unless density_matrices)
     double *rdm;            // [npairs][npairs], pairs p < q in tri_ind_distinct order
     int64_t npairs;
-    uint64_t *rdm_sdets;    // per RDM spawn: parent words, child words (size scap)
+    uint64_t *rdm_schild;   // per RDM spawn: the child's words (size scap)
+    uint32_t *rdm_sparent;  // per RDM spawn: the parent's index in the cycle's (old) main list
     int64_t *rdm_spops;     // per RDM spawn: amount
     uint8_t *rdm_sspace;    // per RDM spawn: space of the parent
     double *rdm_rows;       // [2][npairs]: per-row energy and diagonal of calc_rdm_energy

@@ -119,7 +119,9 @@ __global__ void __launch_bounds__(kBlock) k_rdm_spawns(DevBuffers b, int R, int 
     const double inv_rf = 1.0 / (double)b.sys->real_factor;  // exact: a power of two
     const uint64_t mask = (uint64_t)b.rdm_hash_mask;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        const Det<W> fp = load_det<W>(b.rdm_sdets, 2 * k), fc = load_det<W>(b.rdm_sdets, 2 * k + 1);
+        // the parent from the cycle's old main list (buffer 1 - cur, unchanged by
+        // the annihilation, which wrote the new list into buffer cur)
+        const Det<W> fp = load_det<W>(b.dets[1 - cur], b.rdm_sparent[k]), fc = load_det<W>(b.rdm_schild, k);
         uint64_t h = det_hash<W>(fc) & mask;
         int64_t pos = -1;
         for (uint64_t probes = 0; probes <= mask; probes++) {

@@ -45,7 +45,7 @@ template <int W, int KIND, typename Real, bool SINGLE>
 __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
                                                const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
                                                bool drew, uint64_t bufk, bool rdm, Det<W> &child, int &sp,
-                                               uint32_t &info, Det<W> &parent_det, int64_t &nspawn_rdm) {
+                                               uint32_t &info, int64_t &nspawn_rdm) {
     constexpr bool single = SINGLE;
     // R is 1 or 2: a shift instead of an integer division
     const int64_t i = slot >> (R - 1);
@@ -92,7 +92,6 @@ __device__ __forceinline__ int64_t spawn_entry(const DevSys &s, const HubTables 
         if (rdm) attempt_to_spawn_rdm(s, rs, parent, at);
     }
     nspawn_rdm = KIND == HGPU_SYS_HUB_K ? 0 : at.nspawn_rdm;
-    parent_det = f;
     if (at.nspawn != 0 || nspawn_rdm != 0) child = excited<W>(f, at);
     // no spawning from a deterministic state onto another (src/fciqmc.f90:777-790)
     if (at.nspawn != 0 && b.nd > 0 && (info & kDetermBit)) {
@@ -108,9 +107,9 @@ template <int W, int KIND, typename Real>
 __device__ __noinline__ int64_t spawn_entry_single(const DevSys &s, const HubTables &t, const DevBuffers &b, int R,
                                                    const uint64_t *dets, uint64_t iter, uint32_t slot, uint32_t att,
                                                    uint64_t bufk, bool rdm, Det<W> &child, int &sp, uint32_t &info,
-                                                   Det<W> &parent_det, int64_t &nspawn_rdm) {
+                                                   int64_t &nspawn_rdm) {
     return spawn_entry<W, KIND, Real, true>(s, t, b, R, dets, iter, slot, att, true, bufk, rdm, child, sp, info,
-                                            parent_det, nspawn_rdm);
+                                            nspawn_rdm);
 }
 
 // Generators whose first draw chooses a single or a double excitation: their
@@ -128,7 +127,7 @@ constexpr bool spawn_drew() {
 template <int W>
 __device__ __forceinline__ void spawn_emit(const DevBuffers &b, DevState *st, int R, int lane, bool want,
                                            const Det<W> &child, int sp, int64_t nspawn, uint64_t flagword,
-                                           bool rdm, int64_t nrdm, const Det<W> &parent_det) {
+                                           bool rdm, int64_t nrdm, uint32_t parent) {
     const uint32_t ball = __ballot_sync(FULL_MASK, want);
     if (ball) {
         const int leader = __ffs(ball) - 1;
@@ -147,7 +146,9 @@ __device__ __forceinline__ void spawn_emit(const DevBuffers &b, DevState *st, in
         }
     }
     if (rdm) {
-        // create_spawned_particle_replica_rdm: (parent, child) and the amount
+        // create_spawned_particle_replica_rdm: (parent, child) and the amount; the
+        // parent as its main-list index (its determinant is read back from the
+        // list when the RDM spawns are added)
         const uint32_t rball = __ballot_sync(FULL_MASK, nrdm != 0);
         if (rball) {
             const int leader = __ffs(rball) - 1;
@@ -157,8 +158,8 @@ __device__ __forceinline__ void spawn_emit(const DevBuffers &b, DevState *st, in
             if (nrdm != 0) {
                 const int64_t pos = (int64_t)rbase + __popc(rball & lanemask_lt());
                 if (pos < b.scap) {
-                    store_det<W>(b.rdm_sdets, 2 * pos, parent_det);
-                    store_det<W>(b.rdm_sdets, 2 * pos + 1, child);
+                    store_det<W>(b.rdm_schild, pos, child);
+                    b.rdm_sparent[pos] = parent;
                     b.rdm_spops[pos] = nrdm;
                     b.rdm_sspace[pos] = (uint8_t)sp;
                 } else {
@@ -288,22 +289,22 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
             const int cbase_e = kSpawnChunk + 32 * pass;  // the type's carried entries
             for (int j0 = 0; j0 < full; j0 += 32) {
                 bool want = false;
-                Det<W> child, parent_det;
+                Det<W> child;
                 int64_t nspawn = 0, nrdm = 0;
                 int sp = 0;
                 uint64_t flagword = 0;
+                uint32_t pidx = 0;
                 const int j = j0 + lane;
                 if (j < full) {
                     const int e = j < c ? cbase_e + j : q.list[pass == 0 ? j - c : kSpawnChunk - 1 - s0 - (j - c)];
+                    pidx = q.slot[e] >> (R - 1);
                     uint32_t info;
                     if (pass == 0)
                         nspawn = spawn_entry<W, KIND, Real, false>(s, t, b, R, dets, iter, q.slot[e], q.att[e],
-                                                                   drew, q.bufk[e], rdm, child, sp, info,
-                                                                   parent_det, nrdm);
+                                                                   drew, q.bufk[e], rdm, child, sp, info, nrdm);
                     else
                         nspawn = spawn_entry_single<W, KIND, Real>(s, t, b, R, dets, iter, q.slot[e], q.att[e],
-                                                                   q.bufk[e], rdm, child, sp, info, parent_det,
-                                                                   nrdm);
+                                                                   q.bufk[e], rdm, child, sp, info, nrdm);
                     if (nspawn != 0) {
                         want = true;
                         // the attempt's index: a carried entry's from its slot (aoff[slot - 1] + att)
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn(D
                         flagword = (uint64_t)((info >> 2) & 3u) | (aidx << 2);
                     }
                 }
-                spawn_emit<W>(b, st, R, lane, want, child, sp, nspawn, flagword, rdm, nrdm, parent_det);
+                spawn_emit<W>(b, st, R, lane, want, child, sp, nspawn, flagword, rdm, nrdm, pidx);
             }
             __syncwarp();
             // carry entries full..tot-1 (fewer than 32; none once no chunk is
@@ -355,17 +356,19 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn_s
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32) {
         bool want = false;
-        Det<W> child, parent_det;
+        Det<W> child;
         int64_t nspawn = 0, nrdm = 0;
         int sp = 0;
         uint64_t flagword = 0;
+        uint32_t pidx = 0;
         const int64_t j = base + lane;
         if (j < n) {
             const uint4 e = b.sq[j];
+            pidx = e.x >> (R - 1);
             uint32_t info;
             nspawn = spawn_entry_single<W, KIND, Real>(s, t, b, R, dets, iter, e.x, e.y,
                                                        (uint64_t)e.z | ((uint64_t)e.w << 32), rdm, child, sp, info,
-                                                       parent_det, nrdm);
+                                                       nrdm);
             if (nspawn != 0) {
                 want = true;
                 // the attempt's index: aoff[slot - 1] + attempt in the slot
@@ -373,7 +376,7 @@ __global__ void __launch_bounds__(kBlock, spawn_min_blocks<W, KIND>()) k_spawn_s
                 flagword = (uint64_t)((info >> 2) & 3u) | (aidx << 2);
             }
         }
-        spawn_emit<W>(b, st, R, lane, want, child, sp, nspawn, flagword, rdm, nrdm, parent_det);
+        spawn_emit<W>(b, st, R, lane, want, child, sp, nspawn, flagword, rdm, nrdm, pidx);
     }
 }
 

@@ -637,7 +637,7 @@ static void annihilation_w(const DevBuffers &b, int R, int cur, cudaStream_t st,
                              (b.use_rank ? sizeof(uint64_t) * (size_t)rows * cols : 0);
     const int kw = b.key_words == 2 ? 2 : 1;
     // twice the streaming grid: the rank computation is latency-bound at four
-    // blocks per SM (1.5 % faster passes of the 64-orbital lists with eight)
+    // blocks per SM (the 64-orbital sort phase is 1.6 % shorter with eight)
     const int hist_grid = 2 * b.grid;
     if (b.sort_packed == 1 && kw == 1) k_sort_hist<W, 1, true, 1><<<hist_grid, kBlock, hist_smem, st>>>(b, rows, cols);
     else if (b.sort_packed == 2 && kw == 1) k_sort_hist<W, 1, true, 2><<<hist_grid, kBlock, hist_smem, st>>>(b, rows, cols);

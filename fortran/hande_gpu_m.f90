@@ -43,7 +43,7 @@ module hande_gpu_m
         real(c_double) :: power_pitzer_min_weight
         integer(c_int32_t) :: semi_stoch_space, semi_stoch_size
         integer(c_int64_t) :: semi_stoch_start_iter, semi_stoch_shift_iter
-        integer(c_int32_t) :: semi_stoch_ci_level, semi_stoch_reserved
+        integer(c_int32_t) :: semi_stoch_ci_level, semi_stoch_combined
     end type hgpu_config
 
     type, bind(c) :: hgpu_report

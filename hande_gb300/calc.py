@@ -34,9 +34,9 @@ def semi_stoch_options(ss: Optional[dict]) -> dict:
     space = 'high' with its size, or 'ci' with ci_space = {ex_level = n} (the
     calculation's reference); start_iteration (default 1); with
     shift_start_iteration the start waits for the shift (start_iteration =
-    huge).  'read' needs a HANDE HDF5 file; separate_annihilation = false
-    (combined annihilation) and a ci_space with its own determinant are not
-    provided."""
+    huge); separate_annihilation = false puts the projected amplitudes into
+    the spawned list (combined annihilation).  'read' needs a HANDE HDF5 file;
+    a ci_space with its own determinant is not provided."""
     if not ss:
         return {}
     unknown = set(ss) - SEMI_STOCH_KEYS
@@ -46,9 +46,8 @@ def semi_stoch_options(ss: Optional[dict]) -> dict:
         raise ValueError("Deterministic space not specified.")
     if ss["space"] not in ("high", "ci"):
         raise ValueError("semi_stoch space %r is not provided ('high', 'ci')" % ss["space"])
-    if not ss.get("separate_annihilation", True):
-        raise ValueError("semi_stoch separate_annihilation = false is not provided")
-    out = dict(semi_stoch_start_iter=int(ss.get("start_iteration", 1)), semi_stoch_shift_iter=-1)
+    out = dict(semi_stoch_start_iter=int(ss.get("start_iteration", 1)), semi_stoch_shift_iter=-1,
+               semi_stoch_combined=0 if ss.get("separate_annihilation", True) else 1)
     if ss["space"] == "high":
         if "size" not in ss:
             raise ValueError("Target space size not given.")

@@ -331,9 +331,12 @@ __global__ void __launch_bounds__(kBlock, ann_min_blocks<W>()) k_annihilate(DevB
     // amounts are read anyway, rather than in the spawning kernel's hot loop
     const int64_t bthr = kBloomThreshold * s.real_factor;
     int64_t bn = 0, btot = 0, bmax = 0;
-    auto bloom_add = [&](const int64_t p[2]) {
+    // (the deterministic projection's entries of combined semi-stochastic
+    // annihilation, at and past n_spawn_stoch, are not spawning events)
+    const int64_t nstoch = st->n_spawn_stoch;
+    auto bloom_add = [&](const int64_t p[2], int64_t e) {
         const int64_t a = (p[0] < 0 ? -p[0] : p[0]) + (p[1] < 0 ? -p[1] : p[1]);
-        if (mode == 0 && a >= bthr) {
+        if (mode == 0 && a >= bthr && e < nstoch) {
             bn++;
             btot += a;
             bmax = a > bmax ? a : bmax;
@@ -383,7 +386,7 @@ __global__ void __launch_bounds__(kBlock, ann_min_blocks<W>()) k_annihilate(DevB
                     for (int q = 0; q < 2; q++)
                         if (q < R) p[q] = b.spops[(int64_t)e[r] * R + q];
                     if (initiator) fl = b.sflag[e[r]];
-                    bloom_add(p);
+                    bloom_add(p, e[r]);
                 }
 #pragma unroll
                 for (int w = 0; w < W; w++) tdet[k * W + w] = d.w[w];
@@ -404,7 +407,7 @@ __global__ void __launch_bounds__(kBlock, ann_min_blocks<W>()) k_annihilate(DevB
                 for (int q = 0; q < 2; q++)
                     if (q < R) p[q] = b.spops[(int64_t)e * R + q];
                 a.add(R, initiator, p, initiator ? b.sflag[e] : 0);
-                bloom_add(p);
+                bloom_add(p, e);
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) a.merge(shfl_down_acc(a, off));

@@ -728,6 +728,7 @@ static int alloc_lists(hgpu_handle *h) {
         b.splits_grid = clampi(((b.cap + b.scap) / kAnnTileMin + 3 + 7) / 8, 1, 4 * sms);  // a warp per cut
         b.spawn_chunk = 256;
     }
+    b.ss_combined = h->cfg.semi_stoch_combined;
     if ((rc = dalloc(h, &b.state, 1))) return rc;
     CK(cudaMemset(b.state, 0, sizeof(DevState)));
     CK(cudaMemset(b.part_i, 0, sizeof(int64_t) * kMaxBlocks * 4));
@@ -840,6 +841,7 @@ int32_t hgpu_create(const hgpu_config *cfg, const hgpu_system *sys, hgpu_handle 
     if (cfg->semi_stoch_space != 0 && cfg->semi_stoch_space != 1 && cfg->semi_stoch_space != 4)
         return HGPU_ERR_UNSUPPORTED;
     if (cfg->semi_stoch_space != 0 && cfg->density_matrices) return HGPU_ERR_UNSUPPORTED;
+    if (cfg->semi_stoch_combined != 0 && cfg->semi_stoch_combined != 1) return HGPU_ERR_INVALID;
     if ((cfg->semi_stoch_space == 1 && cfg->semi_stoch_size < 1) ||
         (cfg->semi_stoch_space == 4 && cfg->semi_stoch_ci_level < 0))
         return HGPU_ERR_INVALID;

@@ -90,6 +90,7 @@ __global__ void k_cycle_begin(DevState *st, const DevSys *sys) {
     st->n_rdm = 0;
     st->spawn_next = 0;
     st->n_sq = 0;
+    st->n_spawn_stoch = INT64_MAX;
     double np = (double)st->abs_pop[0] / (double)sys->real_factor;
     st->nattempts_cycle = llround(2.0 * np);
 }

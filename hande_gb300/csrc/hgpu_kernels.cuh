@@ -77,6 +77,8 @@ struct DevState {
     int32_t pad2;
     uint64_t spawn_next;  // next unclaimed attempt chunk of the spawning kernel
     int64_t n_sq;         // singles queued for the singles kernel (may pass sq_cap: see k_spawn)
+    int64_t n_spawn_stoch; // spawned entries from spawning attempts (the rest, with combined
+                           // semi-stochastic annihilation, are the deterministic projection's)
     uint32_t os_ticket[16];  // next tile of each radix pass (hgpu_sort.cuh)
     uint32_t ann_ticket[2];  // next tile of each annihilation pass (hgpu_annihilate.cu)
     // replica 2-RDM (hgpu_rdm.cu)
@@ -167,6 +169,7 @@ struct DevBuffers {
     double *dvec;
     int64_t *dind;
     int64_t nd;
+    int ss_combined;        // combined annihilation: the projection goes to the spawned list
     // scan scratch and per-block partials
     int64_t *scan_part;     // kMaxBlocks * 2
     double *part_d;         // kMaxBlocks * 4 (proj, d0 per space)

@@ -106,10 +106,63 @@ void launch_determ_columns(const DevBuffers &b, int W, int kind, bool fill, int6
     }
 }
 
+// The spawned entries of the deterministic space come after every spawning
+// attempt's: their count marks where they start in the spawned list.
+__global__ void k_mark_stoch_spawns(DevState *st) { st->n_spawn_stoch = st->n_spawn; }
+
+// determ_proj_combined_annihil (src/semi_stoch.F90:897-975) without
+// quasi-Newton (rho_minus_qn_weight = 0, quasi_newton_pop_control = 1), one
+// thread per deterministic state r: for each space, out = sum_j H(r, j) v_j
+// over row r in ascending column order (csrpgemv_single_row,
+// lib/local/csr.f90:206-235; row r of the symmetric matrix is the stored
+// column r), then out = -tau (out + (-S) v_r); create_spawned_particle_determ
+// (:1096-1146): out in walker units, rounded up with probability of its
+// fraction (the same stream as the separate projection's), appended to the
+// spawned list as a spawn from an initiator, generation order after every
+// spawning attempt (row-major over (state, space)).
+__global__ void __launch_bounds__(kBlock) k_determ_spawn(DevBuffers b, int R) {
+    const DevSys *s = b.sys;
+    DevState *st = b.state;
+    const uint64_t iter = (uint64_t)st->iter;
+    const double tau = s->tau, rf = (double)s->real_factor;
+    const int W = s->nw;
+    const uint64_t abase = (uint64_t)st->n_attempts;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < b.nd; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t z0 = b.dcol_ptr[r], z1 = b.dcol_ptr[r + 1];
+        for (int sp = 0; sp < R; sp++) {
+            double out = 0.0;
+            for (int64_t z = z0; z < z1; z++) out = out + b.dcol_h[z] * b.dvec[(int64_t)b.dcol_i[z] * R + sp];
+            const double coef = 0.0 * 0.0 - 1.0 * st->shift[sp];
+            out = -tau * (out + coef * b.dvec[r * R + sp]);
+            const double scaled = out * rf;
+            const int64_t sign = scaled < 0.0 ? -1 : 1;
+            const double amp = fabs(scaled);
+            int64_t n = (int64_t)amp;
+            RStream rs;
+            rs.init(s->seed, P_DETERM, sp, r, 0, iter);
+            if (amp - (double)n > rs.next()) n = n + 1;
+            n = n * sign;
+            const unsigned long long pos = atomicAdd((unsigned long long *)&st->n_spawn, 1ull);
+            if ((int64_t)pos >= b.scap) {
+                atomicOr(&st->error_flags, HGPU_FLAG_SPAWN_OVERFLOW);
+                continue;
+            }
+            for (int w = 0; w < W; w++) b.sdets[pos * W + w] = b.ddets[r * W + w];
+            for (int q = 0; q < R; q++) b.spops[pos * R + q] = q == sp ? n : 0;
+            if (b.sflag) b.sflag[pos] = (abase + (uint64_t)r * R + sp) << 2;
+        }
+    }
+}
+
 void launch_determ_project(const DevBuffers &b, int R, int cur, cudaStream_t st) {
     int64_t blocks = (b.nd + kBlock - 1) / kBlock;
     const int grid = (int)(blocks < 1 ? 1 : (blocks > b.grid ? b.grid : blocks));
-    k_determ_project<<<grid, kBlock, 0, st>>>(b, R, cur);
+    if (b.ss_combined) {
+        k_mark_stoch_spawns<<<1, 1, 0, st>>>(b.state);
+        k_determ_spawn<<<grid, kBlock, 0, st>>>(b, R);
+    } else {
+        k_determ_project<<<grid, kBlock, 0, st>>>(b, R, cur);
+    }
 }
 
 }  // namespace hgpu

@@ -155,7 +155,7 @@ typedef struct hgpu_config {
                                         floor, as a share of the mean, of the weights of
                                         heat_bath_power_pitzer_ref's i, j and single tables
                                         (check_min_weight_ratio); must lie in [0, 1] */
-    /* semi_stoch_in_t (src/qmc_data.f90:305-338), separate annihilation */
+    /* semi_stoch_in_t (src/qmc_data.f90:305-338) */
     int32_t semi_stoch_space;       /* space_type: 0 none, 1 'high' (the most populated
                                        determinants when the space is built), 4 'ci' (every
                                        determinant of the reference's spin and symmetry within
@@ -166,7 +166,11 @@ typedef struct hgpu_config {
     int64_t semi_stoch_shift_iter;  /* shift_start_iteration: built this many iterations after
                                        every shift varies (-1: not used) */
     int32_t semi_stoch_ci_level;    /* ci_space%ex_level of a 'ci' space */
-    int32_t semi_stoch_reserved;    /* 0 */
+    int32_t semi_stoch_combined;    /* 0: separate annihilation (HANDE's default: the projected
+                                       amplitudes added to the main list); 1: combined
+                                       (separate_annihilation = false: they join the spawned list
+                                       as spawns from initiators, determ_proj_combined_annihil,
+                                       src/semi_stoch.F90:897-975) */
 } hgpu_config;
 
 /* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */

@@ -2690,6 +2690,35 @@ static void ss_project(oracle_ctx *c) {
     }
 }
 
+/* determ_proj_combined_annihil (src/semi_stoch.F90:897-975) without
+ * quasi-Newton (rho_minus_qn_weight = 0, quasi_newton_pop_control = 1): for each
+ * deterministic state (row) and space, out = sum_j H(row, j) v_j over the row in
+ * ascending column order (csrpgemv_single_row, lib/local/csr.f90:206-235; the
+ * symmetric matrix's row is its stored column), out = -tau (out + (E 0 - 1 S) v_row),
+ * then create_spawned_particle_determ (:1096-1146): out in walker units,
+ * rounded up with probability of its fraction, appended to the spawned list as a
+ * spawn from an initiator (flag 0) after every spawning attempt's entries. */
+static void ss_project_combined(oracle_ctx *c) {
+    const int R = c->R;
+    for (int64_t r = 0; r < c->nd; r++) {
+        for (int s = 0; s < R; s++) {
+            double out = 0.0;
+            for (int64_t z = c->dcol_ptr[r]; z < c->dcol_ptr[r + 1]; z++)
+                out = out + c->dcol_h[z] * c->dvec[c->dcol_i[z] * R + s];
+            const double coef = 0.0 * 0.0 - 1.0 * c->shift[s];
+            out = -c->cfg.tau * (out + coef * c->dvec[r * R + s]);
+            const double scaled = out * (double)c->real_factor;
+            const int64_t sign = scaled < 0.0 ? -1 : 1;
+            const double amp = fabs(scaled);
+            int64_t n = (int64_t)amp;
+            rstream rs;
+            rs_init(&rs, (uint64_t)c->cfg.seed, P_DETERM, s, (uint64_t)r, 0, (uint64_t)c->iter);
+            if (amp - (double)n > rs_next(&rs)) n = n + 1;
+            add_spawn(c, &c->ddets[r * c->nw], s, n * sign, 0, c->sn);
+        }
+    }
+}
+
 /* accumulate_bloom_stats (src/bloom_handler.F90:104-145) with FCIQMC's fixed-n
  * threshold of 3 particles (init_bloom_stats_t, src/fciqmc.f90:214): the
  * report's count and particle sum, the calculation's largest bloom.  The sum is
@@ -2769,9 +2798,12 @@ static int64_t mc_cycle_spawn(oracle_ctx *c, int64_t *nattempts_acc_out) {
 /* The second half: projection of the deterministic space, direct_annihilation,
  * the RDM update and end_mc_cycle (src/fciqmc.f90:393-405). */
 static void mc_cycle_finish(oracle_ctx *c, int64_t ndeath, int64_t nattempts_acc) {
+    /* combined annihilation: the projection's spawns join the list first, and
+     * calc_events_spawn_t counts them (direct_annihilation, src/annihilation.f90:52) */
+    if (c->ss_on && c->cfg.semi_stoch_combined) ss_project_combined(c);
     int64_t nspawn_events = c->sn; /* calc_events_spawn_t */
     c->rep_spawned += c->sn;
-    if (c->ss_on) ss_project(c);
+    if (c->ss_on && !c->cfg.semi_stoch_combined) ss_project(c);
     direct_annihilation(c);
     if (c->rdm_on) update_rdm_from_spawns(c);
     c->last_nspawn_events = nspawn_events;

@@ -28,8 +28,12 @@ def test_semi_stoch_table():
     assert (cfg.semi_stoch_space, cfg.semi_stoch_ci_level) == (4, 2)
     cfg = calc.config_from_options(s, QMC)
     assert cfg.semi_stoch_space == 0
-    for bad in (dict(size=5), dict(space="high"), dict(space="read"), dict(space="high", size=5, bogus=1),
-                dict(space="high", size=5, separate_annihilation=False)):
+    # separate_annihilation = false: combined annihilation
+    cfg = calc.config_from_options(s, QMC, semi_stoch=dict(space="high", size=5, separate_annihilation=False))
+    assert (cfg.semi_stoch_space, cfg.semi_stoch_combined) == (1, 1)
+    cfg = calc.config_from_options(s, QMC, semi_stoch=dict(space="high", size=5))
+    assert cfg.semi_stoch_combined == 0
+    for bad in (dict(size=5), dict(space="high"), dict(space="read"), dict(space="high", size=5, bogus=1)):
         with pytest.raises(ValueError):
             calc.config_from_options(s, QMC, semi_stoch=bad)
 

@@ -1,9 +1,10 @@
-"""Semi-stochastic projection (src/semi_stoch.F90, 'high' space, separate
-annihilation) on the GPU against the oracle: the walker lists, deterministic
-states included, bit-exact after every report, through the building of the
-space (at a given iteration or after the shift starts varying), the exact
-projection and its stochastic rounding; integer and real walkers, Hubbard and
-molecular systems, one- and two-word determinants, initiator on and off."""
+"""Semi-stochastic projection (src/semi_stoch.F90, 'high' and 'ci' spaces,
+separate and combined annihilation) on the GPU against the oracle: the walker
+lists, deterministic states included, bit-exact after every report, through the
+building of the space (at a given iteration or after the shift starts varying),
+the exact projection and its stochastic rounding; integer and real walkers,
+Hubbard and molecular systems, one- and two-word determinants, initiator on and
+off."""
 
 import numpy as np
 import pytest
@@ -37,6 +38,17 @@ RUNS = [
     # two replicas (replica_tricks) sharing one space, initiator on
     ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True, nspaces=2,
                    initiator=True, semi_stoch_space=1, semi_stoch_size=250, semi_stoch_start_iter=9), 3),
+    # combined annihilation (separate_annihilation = false): the projection as
+    # spawns from initiators in the spawned list
+    ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True, initiator=True,
+                   semi_stoch_space=1, semi_stoch_size=300, semi_stoch_start_iter=15, semi_stoch_combined=1), 3),
+    ("hub_k_4x4", dict(tau=0.01, init_pop=50, target_population=5000, semi_stoch_space=1, semi_stoch_size=40,
+                       semi_stoch_start_iter=8, semi_stoch_combined=1), 4),
+    ("mol40_w2", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,
+                      semi_stoch_space=4, semi_stoch_ci_level=1, semi_stoch_start_iter=6, semi_stoch_combined=1), 3),
+    ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True, nspaces=2,
+                   initiator=True, semi_stoch_space=1, semi_stoch_size=250, semi_stoch_start_iter=9,
+                   semi_stoch_combined=1), 3),
 ]
 
 
@@ -58,6 +70,8 @@ def test_whole_run_semi_stoch_bit_exact(name, opts, nrep):
         np.testing.assert_array_equal(pg, po, err_msg="report %d pops" % r)
         assert_close(kg, ko)
         assert rg.nattempts == ro.nattempts
+        assert rg.nspawn_events == ro.nspawn_events
+        assert rg.nblooms == ro.nblooms
         assert list(rg.shift) == list(ro.shift)
         assert_close(rg.proj_energy[0], ro.proj_energy[0], 1e-10)
     if opts["semi_stoch_space"] == 1:

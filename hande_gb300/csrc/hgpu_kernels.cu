@@ -343,7 +343,10 @@ __global__ void __launch_bounds__(kBlock) k_load_fixed(DevBuffers b, int R, cons
         for (int q = 0; q < R; q++) b.spops[i * R + q] = e[W + q];
         if (b.sflag) b.sflag[i] = ((uint64_t)e[W + R] & 3ull) | ((uint64_t)i << 2);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) b.state->n_spawn = n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        b.state->n_spawn = n;
+        b.state->n_spawn_stoch = INT64_MAX;  // every entry a spawning event
+    }
 }
 
 __global__ void __launch_bounds__(kBlock) k_abs_pop(DevBuffers b, int R, int cur) {

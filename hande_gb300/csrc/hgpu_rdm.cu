@@ -143,34 +143,84 @@ __global__ void __launch_bounds__(kBlock) k_rdm_spawns(DevBuffers b, int R, int 
 }
 
 // The diagonal: N^(1) N^(2) of every occupied determinant on each of its
-// occupied pairs, summed per block in shared memory.
+// occupied pairs, summed per block in shared memory.  A warp loads 32
+// determinants and runs those occupied in both spaces one after the other,
+// its lanes on the determinant's pairs: lane l holds the l-th occupied orbital,
+// and pair k of the pair table (x, y), x < y, is added by lane k mod 32 from
+// the orbitals of lanes x and y -- the same work for every determinant, so
+// the lanes stay busy whatever mix of determinants a warp meets.  Up to 32
+// electrons (a table of at most 496 pairs); more take one determinant per lane.
+constexpr int kDiagMaxPairs = 32 * 31 / 2;
+
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_rdm_diag(DevBuffers b, int R, int cur) {
     extern __shared__ double dsm[];  // [npairs]
+    __shared__ uint16_t ptab[kDiagMaxPairs];  // x | y << 8
     const DevState *st = b.state;
     if (!st->rdm_on) return;
     const int64_t np = b.npairs;
+    const int nel = b.sys->nel;
+    const int nep = nel * (nel - 1) / 2;
     for (int64_t k = threadIdx.x; k < np; k += blockDim.x) dsm[k] = 0.0;
+    if (nel <= 32)
+        for (int k = threadIdx.x; k < nep; k += blockDim.x) {
+            int y = 1;
+            while ((y + 1) * y / 2 <= k) y++;
+            ptab[k] = (uint16_t)((k - y * (y - 1) / 2) | (y << 8));
+        }
     __syncthreads();
     const int64_t N = st->n_main;
     const uint64_t *dets = b.dets[cur];
     const int64_t *pops = b.pops[cur];
     const double inv_rf = 1.0 / (double)b.sys->real_factor;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t p0 = pops[i * R], p1 = pops[i * R + 1];
-        if (p0 == 0 || p1 == 0) continue;
-        const double matel = (double)p0 * inv_rf * ((double)p1 * inv_rf) / 1.0;
-        const Det<W> f = load_det<W>(dets, i);
+    const int lane = threadIdx.x & 31;
+    if (nel <= 32) {
+        const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+        for (int64_t base = warp * 32; base < N; base += nwarps * 32) {
+            const int64_t i = base + lane;
+            int64_t p0 = 0, p1 = 0;
+            Det<W> f;
 #pragma unroll
-        for (int wx = 0; wx < W; wx++) {
-            for (uint64_t x = f.w[wx]; x; x &= x - 1) {
-                const int px = 64 * wx + __ffsll((long long)x) - 1;
-                for (uint64_t y = x & (x - 1); y; y &= y - 1)
-                    atomicAdd(&dsm[tri_pair(64 * wx + __ffsll((long long)y) - 1, px)], matel);
+            for (int w = 0; w < W; w++) f.w[w] = 0;
+            if (i < N) {
+                p0 = pops[i * R];
+                p1 = pops[i * R + 1];
+                f = load_det<W>(dets, i);
+            }
+            const double matel = (double)p0 * inv_rf * ((double)p1 * inv_rf) / 1.0;
+            for (uint32_t m = __ballot_sync(FULL_MASK, p0 != 0 && p1 != 0); m; m &= m - 1) {
+                const int src = __ffs(m) - 1;
+                Det<W> g;
 #pragma unroll
-                for (int wy = wx + 1; wy < W; wy++)
-                    for (uint64_t y = f.w[wy]; y; y &= y - 1)
-                        atomicAdd(&dsm[tri_pair(64 * wy + __ffsll((long long)y) - 1, px)], matel);
+                for (int w = 0; w < W; w++) g.w[w] = __shfl_sync(FULL_MASK, f.w[w], src);
+                const double v = __shfl_sync(FULL_MASK, matel, src);
+                const int occ = lane < nel ? select_det<W>(g.w, lane) : 0;
+                for (int k0 = 0; k0 < nep; k0 += 32) {
+                    const int k = k0 + lane;
+                    const uint16_t xy = k < nep ? ptab[k] : 0;
+                    const int a = __shfl_sync(FULL_MASK, occ, xy & 0xFF), c = __shfl_sync(FULL_MASK, occ, xy >> 8);
+                    if (k < nep) atomicAdd(&dsm[tri_pair(c, a)], v);
+                }
+            }
+        }
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t p0 = pops[i * R], p1 = pops[i * R + 1];
+            if (p0 == 0 || p1 == 0) continue;
+            const double matel = (double)p0 * inv_rf * ((double)p1 * inv_rf) / 1.0;
+            const Det<W> f = load_det<W>(dets, i);
+#pragma unroll
+            for (int wx = 0; wx < W; wx++) {
+                for (uint64_t x = f.w[wx]; x; x &= x - 1) {
+                    const int px = 64 * wx + __ffsll((long long)x) - 1;
+                    for (uint64_t y = x & (x - 1); y; y &= y - 1)
+                        atomicAdd(&dsm[tri_pair(64 * wx + __ffsll((long long)y) - 1, px)], matel);
+#pragma unroll
+                    for (int wy = wx + 1; wy < W; wy++)
+                        for (uint64_t y = f.w[wy]; y; y &= y - 1)
+                            atomicAdd(&dsm[tri_pair(64 * wy + __ffsll((long long)y) - 1, px)], matel);
+                }
             }
         }
     }

@@ -708,6 +708,9 @@ static int alloc_lists(hgpu_handle *h) {
         int64_t hs = 16;
         while (hs < b.cap + b.cap / 2) hs <<= 1;
         b.rdm_hash_mask = hs - 1;
+        int ibits = 1;  // smallest with 2^ibits > cap: no entry equals the empty marker
+        while (ibits < 32 && ((int64_t)1 << ibits) <= b.cap) ibits++;
+        b.rdm_hash_tagmask = ibits >= 32 ? 0u : ~((1u << ibits) - 1u);
         CK(cudaStreamCreateWithFlags(&b.rdm_aux, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&b.rdm_fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&b.rdm_join, cudaEventDisableTiming));

@@ -153,6 +153,7 @@ struct DevBuffers {
     double *rdm_rows;       // [2][npairs]: per-row energy and diagonal of calc_rdm_energy
     uint32_t *rdm_hash;     // open-addressing table of the new main list (index per slot)
     int64_t rdm_hash_mask;  // table size - 1 (a power of two, at least 1.5 x cap)
+    uint32_t rdm_hash_tagmask;  // entry bits above the list index: a tag from the hash's high word
     // the RDM diagonal runs on a second stream beside the RDM spawns (host
     // handles: a fork and a join event around it)
     cudaStream_t rdm_aux;

@@ -33,33 +33,13 @@ __device__ __forceinline__ void orbs_of_pair(int64_t ind, int &p, int &q) {
     q = qq - 1;
 }
 
-// update_rdm (src/replica_rdm.F90:12-82) for a child f1 and its parent f2
-// (a single or double excitation apart).
-template <int W>
-__device__ __forceinline__ void rdm_add_pair(double *rdm, int64_t np, const Det<W> &f1, const Det<W> &f2, int nel,
-                                             double matel) {
-    const Excit e = get_excitation<W>(f1, f2, nel);
-    if (e.perm) matel = -matel;
-    if (e.nexcit == 2) {
-        atomicAdd(&rdm[tri_pair(e.to[0], e.to[1]) * np + tri_pair(e.from[0], e.from[1])], matel);
-    } else if (e.nexcit == 1) {
-        const int p = e.to[0], q = e.from[0];
-#pragma unroll
-        for (int w = 0; w < W; w++) {
-            for (uint64_t x = f1.w[w]; x; x &= x - 1) {
-                const int orb = 64 * w + __ffsll((long long)x) - 1;
-                if (orb == q) continue;
-                if (orb < p && orb < q) atomicAdd(&rdm[tri_pair(orb, p) * np + tri_pair(orb, q)], matel);
-                else if (orb > p && orb > q) atomicAdd(&rdm[tri_pair(orb, p) * np + tri_pair(q, orb)], matel);
-                else atomicAdd(&rdm[tri_pair(p, orb) * np + tri_pair(orb, q)], -matel);
-            }
-        }
-    }
-}
-
 // Open-addressing hash table of the new main list (index per slot, linear
 // probing), so that each RDM spawn finds its child with about two memory
-// accesses instead of a binary search of the whole list.  Probe sequences are
+// accesses instead of a binary search of the whole list.  The index needs the
+// low bits of a slot (the fewest that hold the list's capacity); the bits above
+// it hold a tag from the high word of the determinant's hash, so that a probe
+// loads a determinant only when the tags agree (three tag bits at a capacity of
+// 3e8 skip 7 in 8 of the loads that would not match).  Probe sequences are
 // bounded by the table size; a full sweep (impossible below a load of one)
 // raises HGPU_FLAG_INTERNAL.
 constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
@@ -95,9 +75,11 @@ __global__ void __launch_bounds__(kBlock) k_rdm_hash_insert(DevBuffers b, int cu
     const uint64_t *dets = b.dets[cur];
     const uint64_t mask = (uint64_t)b.rdm_hash_mask;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        uint64_t h = det_hash<W>(load_det<W>(dets, i)) & mask;
+        const uint64_t hx = det_hash<W>(load_det<W>(dets, i));
+        const uint32_t entry = ((uint32_t)(hx >> 32) & b.rdm_hash_tagmask) | (uint32_t)i;
+        uint64_t h = hx & mask;
         uint64_t probes = 0;
-        while (atomicCAS(&b.rdm_hash[h], kHashEmpty, (uint32_t)i) != kHashEmpty) {
+        while (atomicCAS(&b.rdm_hash[h], kHashEmpty, entry) != kHashEmpty) {
             h = (h + 1) & mask;
             if (++probes > mask) {
                 atomicOr(&st->error_flags, HGPU_FLAG_INTERNAL);
@@ -107,7 +89,11 @@ __global__ void __launch_bounds__(kBlock) k_rdm_hash_insert(DevBuffers b, int cu
     }
 }
 
-// The cycle's RDM spawns against the new main list (buffer cur).
+// The cycle's RDM spawns against the new main list (buffer cur).  A double
+// adds one element; a single adds one per other occupied orbital of the child,
+// done by the warp's lanes together (lane l on the child's l-th occupied
+// orbital) for each single of the warp in turn, so that the few singles among
+// a warp's spawns do not hold the others through their loops.
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_rdm_spawns(DevBuffers b, int R, int cur) {
     DevState *st = b.state;
@@ -116,29 +102,71 @@ __global__ void __launch_bounds__(kBlock) k_rdm_spawns(DevBuffers b, int R, int 
     const uint64_t *dets = b.dets[cur];
     const int64_t *pops = b.pops[cur];
     const int nel = b.sys->nel;
+    const int64_t np = b.npairs;
     const double inv_rf = 1.0 / (double)b.sys->real_factor;  // exact: a power of two
     const uint64_t mask = (uint64_t)b.rdm_hash_mask;
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        // the parent from the cycle's old main list (buffer 1 - cur, unchanged by
-        // the annihilation, which wrote the new list into buffer cur)
-        const Det<W> fp = load_det<W>(b.dets[1 - cur], b.rdm_sparent[k]), fc = load_det<W>(b.rdm_schild, k);
-        uint64_t h = det_hash<W>(fc) & mask;
-        int64_t pos = -1;
-        for (uint64_t probes = 0; probes <= mask; probes++) {
-            const uint32_t v = b.rdm_hash[h];
-            if (v == kHashEmpty) break;
-            if (det_eq<W>(load_det<W>(dets, v), fc)) {
-                pos = v;
-                break;
+    const uint32_t tagmask = b.rdm_hash_tagmask;
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int64_t k = base + lane;
+        bool single = false;
+        double matel = 0.0;
+        int p = 0, q = 0;
+        Det<W> fc;
+#pragma unroll
+        for (int w = 0; w < W; w++) fc.w[w] = 0;
+        if (k < n) {
+            // the parent from the cycle's old main list (buffer 1 - cur, unchanged by
+            // the annihilation, which wrote the new list into buffer cur)
+            const Det<W> fp = load_det<W>(b.dets[1 - cur], b.rdm_sparent[k]);
+            fc = load_det<W>(b.rdm_schild, k);
+            const uint64_t hx = det_hash<W>(fc);
+            const uint32_t tag = (uint32_t)(hx >> 32) & tagmask;
+            uint64_t h = hx & mask;
+            int64_t pos = -1;
+            for (uint64_t probes = 0; probes <= mask; probes++) {
+                const uint32_t v = b.rdm_hash[h];
+                if (v == kHashEmpty) break;
+                if ((v & tagmask) == tag && det_eq<W>(load_det<W>(dets, v & ~tagmask), fc)) {
+                    pos = v & ~tagmask;
+                    break;
+                }
+                h = (h + 1) & mask;
             }
-            h = (h + 1) & mask;
+            if (pos >= 0) {
+                const int s = b.rdm_sspace[k];
+                // pops(other replica, child) / real_factor x amount / real_factor / 2
+                const double pop1 = (double)pops[pos * R + (1 - s)] * inv_rf;
+                const double pop2 = (double)b.rdm_spops[k] * inv_rf;
+                matel = pop1 * pop2 / 2.0;
+                // update_rdm (src/replica_rdm.F90:12-82) for the child and its parent
+                const Excit e = get_excitation<W>(fc, fp, nel);
+                if (e.perm) matel = -matel;
+                if (e.nexcit == 2) {
+                    atomicAdd(&b.rdm[tri_pair(e.to[0], e.to[1]) * np + tri_pair(e.from[0], e.from[1])], matel);
+                } else if (e.nexcit == 1) {
+                    single = true;
+                    p = e.to[0];
+                    q = e.from[0];
+                }
+            }
         }
-        if (pos < 0) continue;
-        const int s = b.rdm_sspace[k];
-        // pops(other replica, child) / real_factor x amount / real_factor / 2
-        const double pop1 = (double)pops[pos * R + (1 - s)] * inv_rf;
-        const double pop2 = (double)b.rdm_spops[k] * inv_rf;
-        rdm_add_pair<W>(b.rdm, b.npairs, fc, fp, nel, pop1 * pop2 / 2.0);
+        for (uint32_t m = __ballot_sync(FULL_MASK, single); m; m &= m - 1) {
+            const int src = __ffs(m) - 1;
+            Det<W> g;
+#pragma unroll
+            for (int w = 0; w < W; w++) g.w[w] = __shfl_sync(FULL_MASK, fc.w[w], src);
+            const double v = __shfl_sync(FULL_MASK, matel, src);
+            const int pp = __shfl_sync(FULL_MASK, p, src), qq = __shfl_sync(FULL_MASK, q, src);
+            for (int l = lane; l < nel; l += 32) {
+                const int orb = select_det<W>(g.w, l);
+                if (orb == qq) continue;
+                if (orb < pp && orb < qq) atomicAdd(&b.rdm[tri_pair(orb, pp) * np + tri_pair(orb, qq)], v);
+                else if (orb > pp && orb > qq) atomicAdd(&b.rdm[tri_pair(orb, pp) * np + tri_pair(qq, orb)], v);
+                else atomicAdd(&b.rdm[tri_pair(pp, orb) * np + tri_pair(orb, qq)], -v);
+            }
+        }
     }
 }
 

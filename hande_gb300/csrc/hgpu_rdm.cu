@@ -91,9 +91,9 @@ __global__ void __launch_bounds__(kBlock) k_rdm_hash_insert(DevBuffers b, int cu
 
 // The cycle's RDM spawns against the new main list (buffer cur).  A double
 // adds one element; a single adds one per other occupied orbital of the child,
-// done by the warp's lanes together (lane l on the child's l-th occupied
-// orbital) for each single of the warp in turn, so that the few singles among
-// a warp's spawns do not hold the others through their loops.
+// done by the warp's lanes together (lane l tests orbitals l, l + 32, ...) for
+// each single of the warp in turn, so that the few singles among a warp's
+// spawns do not hold the others through their loops.
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_rdm_spawns(DevBuffers b, int R, int cur) {
     DevState *st = b.state;
@@ -159,9 +159,10 @@ __global__ void __launch_bounds__(kBlock) k_rdm_spawns(DevBuffers b, int R, int 
             for (int w = 0; w < W; w++) g.w[w] = __shfl_sync(FULL_MASK, fc.w[w], src);
             const double v = __shfl_sync(FULL_MASK, matel, src);
             const int pp = __shfl_sync(FULL_MASK, p, src), qq = __shfl_sync(FULL_MASK, q, src);
-            for (int l = lane; l < nel; l += 32) {
-                const int orb = select_det<W>(g.w, l);
-                if (orb == qq) continue;
+#pragma unroll
+            for (int c = 0; c < 2 * W; c++) {
+                const int orb = 32 * c + lane;
+                if (((g.w[c >> 1] >> (orb & 63)) & 1ull) == 0 || orb == qq) continue;
                 if (orb < pp && orb < qq) atomicAdd(&b.rdm[tri_pair(orb, pp) * np + tri_pair(orb, qq)], v);
                 else if (orb > pp && orb > qq) atomicAdd(&b.rdm[tri_pair(orb, pp) * np + tri_pair(qq, orb)], v);
                 else atomicAdd(&b.rdm[tri_pair(pp, orb) * np + tri_pair(orb, qq)], -v);

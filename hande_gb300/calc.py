@@ -14,6 +14,7 @@ import sys
 import time
 from typing import Optional
 
+from . import restart as restart_files
 from ._abi import PREC_FP64, PREC_MIXED, make_config
 from .engine import Engine
 from .systems import System
@@ -27,6 +28,15 @@ QMC_KEYS = {
 FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file",
                "quadrature_initiator"}
 SEMI_STOCH_KEYS = {"space", "size", "start_iteration", "shift_start_iteration", "separate_annihilation", "ci_space"}
+RESTART_KEYS = {"read", "write", "write_frequency"}
+
+
+def _restart_id(v) -> Optional[int]:
+    """read / write of the restart table: an id, or true for id 0 (the file
+    names HANDE.RS.<id>.p<rank>.H5 of restart_info_t)."""
+    if v is None or v is False:
+        return None
+    return 0 if v is True else int(v)
 
 
 def semi_stoch_options(ss: Optional[dict]) -> dict:
@@ -109,15 +119,33 @@ HEADER = (" iterations      Shift        \\sum H_0j N_j       N_0          # H p
 
 
 def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None, out=None,
-           comm_file: str = "HANDE.COMM", verbose: bool = True, semi_stoch: Optional[dict] = None) -> dict:
+           comm_file: str = "HANDE.COMM", verbose: bool = True, semi_stoch: Optional[dict] = None,
+           restart: Optional[dict] = None, directory: str = ".") -> dict:
     """Run FCIQMC on the GPU.  Returns {'reports': [...], 'engine': Engine}.
 
     A file named ``comm_file`` containing ``softexit = true`` in the working
     directory ends the calculation after the current report (calc_interact,
-    src/interact.F90:11-188)."""
+    src/interact.F90:11-188).
+
+    ``restart`` takes the keys of HANDE's restart table
+    (src/lua_hande_calc.f90, restart_info_t): ``read`` starts from the walker
+    list and state of HANDE restart files HANDE.RS.<read>.p*.H5 in
+    ``directory`` (written by HANDE or by this driver) instead of the initial
+    distribution; ``write`` writes HANDE.RS.<write>.p0.H5 at the end, and every
+    ``write_frequency`` iterations when that is set."""
+    rs = dict(restart or {})
+    bad = set(rs) - RESTART_KEYS
+    if bad:
+        raise ValueError("unknown restart options %s" % sorted(bad))
     cfg = config_from_options(sys, qmc, fciqmc, reference, semi_stoch)
     eng = Engine(sys, cfg)
-    eng.initial_distribution()
+    read_id, write_id = _restart_id(rs.get("read")), _restart_id(rs.get("write"))
+    write_freq = int(rs.get("write_frequency", 0) or 0)
+    write_path = None if write_id is None else os.path.join(directory, "HANDE.RS.%d.p0.H5" % write_id)
+    if read_id is not None:
+        restart_files.load_into(eng, restart_files.restart_paths(read_id, directory))
+    else:
+        eng.initial_distribution()
     stream = out if out is not None else sys_stdout()
     if verbose:
         stream.write(HEADER + "\n")
@@ -130,6 +158,8 @@ def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None
         row["time"] = t1 - t0
         t0 = t1
         reports.append(row)
+        if write_path and write_freq > 0 and row["iterations"] % write_freq == 0:
+            restart_files.save_from(eng, write_path, report=row)
         if verbose:
             stream.write(" %10d  %14.8f  %16.8f  %12.4f  %14.4f  %10d  %10d  %8.4f  %7.4f\n" % (
                 row["iterations"], row["Shift"][0], row["\\sum H_0j N_j"][0], row["N_0"][0], row["# H psips"][0],
@@ -143,6 +173,8 @@ def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None
             if verbose:
                 stream.write("# Soft exit requested through %s.\n" % comm_file)
             break
+    if write_path:
+        restart_files.save_from(eng, write_path, report=reports[-1] if reports else None)
     fo = fciqmc or {}
     if fo.get("density_matrices"):
         rdm = eng.rdm()

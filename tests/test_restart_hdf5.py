@@ -164,3 +164,43 @@ def test_restart_continues_on_oracle(tmp_path):
     np.testing.assert_array_equal(back["pops"], po2)
     assert back["iteration"] == rep.iteration
     o.close()
+
+
+REF_SUITE = "/root/reference/test_suite"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SUITE), reason="HANDE's test suite is not present")
+def test_reader_opens_every_hande_file():
+    import glob
+    import re
+    files = sorted(glob.glob(os.path.join(REF_SUITE, "**", "*.H5"), recursive=True))
+    assert len(files) >= 40
+    sets = {}
+    for p in files:
+        d = hdf5lite.read(p)
+        m = re.match(r"(.*)/HANDE\.RS\.(\d+)\.p(\d+)\.H5$", p)
+        if m:
+            n = d["/qmc/psips/determinants"].shape[0]
+            assert d["/qmc/psips/populations"].shape[0] == n and d["/qmc/psips/data"].shape[0] == n, p
+            sets.setdefault((m.group(1), m.group(2)), []).append(d)
+    assert len(sets) >= 20
+    for (directory, rid), ds in sets.items():
+        i0 = int(ds[0]["/metadata/i0_length"])
+        info = int(ds[0]["/basis/info string len"]) if "/basis/info string len" in ds[0] else 0
+        nbasis = int(ds[0]["/basis/nbasis"]) if "/basis/nbasis" in ds[0] else 0
+        nw = (nbasis + i0 - 1) // i0 if nbasis else ds[0]["/qmc/psips/determinants"].shape[1] - info
+        counts = set()
+        tot = 0.0
+        for d in ds:
+            w = np.ascontiguousarray(d["/qmc/psips/determinants"][:, :nw])
+            w = w.view(np.uint64) if i0 == 64 else w.astype(np.int64) & 0xFFFFFFFF
+            counts |= {sum(bin(int(x)).count("1") for x in row) for row in w}
+            scale = int(d["/qmc/psips/population scale factor"][0]) if "/qmc/psips/population scale factor" in d else 1
+            tot += np.abs(d["/qmc/psips/populations"][:, 0].astype(np.float64)).sum() / scale
+        # one electron count per calculation (CCMC excitors carry no fixed count)
+        if "/metadata/calc type" in ds[0] and int(ds[0]["/metadata/calc type"]) == 4:
+            assert len(counts) == 1, (directory, rid, counts)
+            want = float(np.ravel(ds[0]["/qmc/psips/total population"])[0])
+            # complex populations: the first column is the real part only
+            if ds[0]["/qmc/psips/populations"].shape[1] == 1:
+                assert abs(tot - want) <= 1e-6 * want + 1.0, (directory, rid, tot, want)

@@ -137,13 +137,16 @@ def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None
     bad = set(rs) - RESTART_KEYS
     if bad:
         raise ValueError("unknown restart options %s" % sorted(bad))
+    read_id, write_id = _restart_id(rs.get("read")), _restart_id(rs.get("write"))
+    read_paths = restart_files.restart_paths(read_id, directory) if read_id is not None else None
+    if read_paths and reference is None:
+        reference = restart_files.reference_of(read_paths, sys)
     cfg = config_from_options(sys, qmc, fciqmc, reference, semi_stoch)
     eng = Engine(sys, cfg)
-    read_id, write_id = _restart_id(rs.get("read")), _restart_id(rs.get("write"))
     write_freq = int(rs.get("write_frequency", 0) or 0)
     write_path = None if write_id is None else os.path.join(directory, "HANDE.RS.%d.p0.H5" % write_id)
-    if read_id is not None:
-        restart_files.load_into(eng, restart_files.restart_paths(read_id, directory))
+    if read_paths:
+        restart_files.load_into(eng, read_paths)
     else:
         eng.initial_distribution()
     stream = out if out is not None else sys_stdout()

@@ -195,13 +195,31 @@ def _get_state(calc):
     return calc.get_state() if hasattr(calc, "get_state") else calc.state()
 
 
+def reference_of(paths, system):
+    """The reference determinant of a restart as occupied spin orbitals: a
+    restarted HANDE calculation takes its reference from the file
+    (get_reference_hdf5, src/restart_hdf5.F90:935-1030), and the stored K_ii
+    are relative to it."""
+    if isinstance(paths, (str, os.PathLike)):
+        paths = [paths]
+    f0 = hdf5lite.read(paths[0])
+    i0 = int(f0["/metadata/i0_length"])
+    info_len = int(f0["/basis/info string len"]) if "/basis/info string len" in f0 else 0
+    ref = np.asarray(f0["/qmc/reference/reference determinant"]).reshape(1, -1)
+    return system.decode(_words64(ref, i0, system.nbasis, info_len)[0])
+
+
 def load_into(engine, paths):
     """Replace a calculation's walker list and state (the device engine's, or
     the oracle's) by those of HANDE restart files; returns what read()
-    returned."""
+    returned.  The calculation must have been created with the restart's
+    reference determinant (reference_of)."""
     s = engine.system
     rf = (1 << 31) if engine.cfg.real_amplitudes else 1
     r = read(paths, s.nbasis, engine.R, rf)
+    ours = [int(engine.cfg.ref_det[w]) & 0xFFFFFFFFFFFFFFFF for w in range(s.nwords)]
+    if ours != [int(x) & 0xFFFFFFFFFFFFFFFF for x in r["reference"]]:
+        raise ValueError("the calculation's reference determinant differs from the restart's")
     engine.set_walkers(r["states"], r["pops"], r["kii"])
     st = _get_state(engine)
     st.iteration = r["iteration"]

@@ -143,8 +143,10 @@ def test_restart_continues_on_oracle(tmp_path):
     s = _hubbard()
     cfg = make_config(s, tau=0.01, ncycles=25, seed=7, target_population=5500, state_size=40000,
                       spawned_state_size=40000)
+    paths = restart.restart_paths(0, str(tmp_path))
+    assert restart.reference_of(paths, s) == list(range(18))
     o = Oracle(s, cfg)
-    r = restart.load_into(o, restart.restart_paths(0, str(tmp_path)))
+    r = restart.load_into(o, paths)
     st = o.state()
     assert st.iteration == r["iteration"] and st.vary_shift[0] == 1
     assert st.shift[0] == r["shift"][0]
@@ -160,6 +162,12 @@ def test_restart_continues_on_oracle(tmp_path):
     restart.save_from(o, out, report=rep.as_dict(1), mtime=1_700_000_000)
     back = restart.read([out], s.nbasis, 1, 1)
     st2, po2, da2 = o.walkers()
+    # a calculation around another reference refuses the file
+    other = Oracle(s, make_config(s, tau=0.01, state_size=40000, spawned_state_size=40000,
+                                  reference=list(range(17)) + [19]))
+    with pytest.raises(ValueError):
+        restart.load_into(other, paths)
+    other.close()
     np.testing.assert_array_equal(back["states"], st2)
     np.testing.assert_array_equal(back["pops"], po2)
     assert back["iteration"] == rep.iteration

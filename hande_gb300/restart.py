@@ -23,7 +23,11 @@ version 3, one rank, 64-bit determinant words and the datasets that
 read_restart_hdf5 requires or reads when present.  The engine draws from
 counter-based Philox streams, not dSFMT, so the rng group is written empty: a
 HANDE calculation restarted from the file seeds its generator afresh, as it
-does for any restart file without an rng state.
+does for any restart file without an rng state.  The calc type is
+fciqmc_calc, which HANDE sets for every FCIQMC calculation
+(src/lua_hande_calc.f90:399); nprocs is 1, and HANDE restarts on a different
+number of processes only from files its redistribute step rewrote
+(src/restart_hdf5.F90:663-666): `redistribute {nprocs = N, read = id, write = id2}`.
 """
 
 import glob

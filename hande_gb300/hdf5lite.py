@@ -76,10 +76,13 @@ class _Reader:
     def group_members(self, btree, heap):
         """(name, object header address) of every link of a symbol-table group."""
         out = []
-        self._walk_btree(btree, heap, out)
+        self._walk_btree(btree, heap, out, set())
         return out
 
-    def _walk_btree(self, node, heap, out):
+    def _walk_btree(self, node, heap, out, seen):
+        if node in seen or len(seen) > 4096:
+            raise FormatError("group B-tree revisits node %d" % node)
+        seen.add(node)
         if self.d[node:node + 4] != b"TREE":
             raise FormatError("v1 B-tree node expected at %d" % node)
         ntype, level, used = self.d[node + 4], self.d[node + 5], self.u("H", node + 6)[0]
@@ -93,7 +96,7 @@ class _Reader:
             p += 8
         for c in children:
             if level > 0:
-                self._walk_btree(c, heap, out)
+                self._walk_btree(c, heap, out, seen)
             else:
                 self._snod(c, heap, out)
 
@@ -216,7 +219,9 @@ def read(path):
     return out
 
 
-def _read_group(r, hdr, btree, heap, prefix, out):
+def _read_group(r, hdr, btree, heap, prefix, out, depth=0):
+    if depth > 64:
+        raise FormatError("groups nested deeper than 64 levels")
     if btree is None:
         for mtype, _f, m in r.messages(hdr):
             if mtype == 0x11:
@@ -227,7 +232,7 @@ def _read_group(r, hdr, btree, heap, prefix, out):
         path = prefix + "/" + name
         if stab:
             b, h = struct.unpack_from("<QQ", stab[0], 0)
-            _read_group(r, child, b, h, path, out)
+            _read_group(r, child, b, h, path, out, depth + 1)
         else:
             out[path] = r.dataset(msgs)
 

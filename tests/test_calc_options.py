@@ -49,3 +49,14 @@ def test_generator_names_and_weights():
     assert "power_pitzer" not in EXCIT_GEN  # refused by HANDE for read_in systems
     with pytest.raises(ValueError):
         calc.config_from_options(s, dict(QMC, not_an_option=1))
+
+
+def test_restart_table(tmp_path):
+    s = _sys()
+    # keys outside HANDE's restart table, and a read without files, stop before any device work
+    with pytest.raises(ValueError):
+        calc.fciqmc(s, QMC, restart=dict(read=0, bogus=1), directory=str(tmp_path), verbose=False)
+    with pytest.raises(FileNotFoundError):
+        calc.fciqmc(s, QMC, restart=dict(read=3), directory=str(tmp_path), verbose=False)
+    assert calc._restart_id(True) == 0 and calc._restart_id(5) == 5
+    assert calc._restart_id(False) is None and calc._restart_id(None) is None

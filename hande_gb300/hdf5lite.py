@@ -21,6 +21,7 @@ a Fortran states(W, n) dataset is read as an (n, W) array, which is also the
 layout of hgpu_upload_walkers' column-major input.
 """
 
+import mmap
 import struct
 
 import numpy as np
@@ -70,8 +71,10 @@ class _Reader:
             raise FormatError("local heap expected at %d" % heap)
         seg, = self.u("Q", heap + 24)
         s = seg + off
-        e = self.d.index(b"\0", s)
-        return self.d[s:e].decode()
+        e = self.d.find(b"\0", s)
+        if e < 0:
+            raise FormatError("unterminated name in the local heap at %d" % heap)
+        return bytes(self.d[s:e]).decode()
 
     def group_members(self, btree, heap):
         """(name, object header address) of every link of a symbol-table group."""
@@ -146,13 +149,14 @@ class _Reader:
         kind, where, nbytes = layout
         count = int(np.prod(shape)) if shape else 1
         if kind == "compact":
-            raw = where
+            arr = np.frombuffer(where, dtype=dtype, count=count).copy()
+        elif where == UNDEF:
+            arr = np.zeros(count, dtype=dtype)
         else:
-            if where == UNDEF:
-                raw = b"\0" * (count * dtype.itemsize)
-            else:
-                raw = self.d[self.base + where:self.base + where + count * dtype.itemsize]
-        arr = np.frombuffer(raw, dtype=dtype, count=count).copy()
+            off = self.base + where
+            if off + count * dtype.itemsize > len(self.d):
+                raise FormatError("dataset data past the end of the file")
+            arr = np.frombuffer(self.d, dtype=dtype, count=count, offset=off).copy()
         return arr.reshape(shape) if shape else arr.reshape(())
 
 
@@ -208,15 +212,25 @@ def _layout(m):
     raise FormatError("data layout version %d" % ver)
 
 
+def _mapped(path):
+    """The file mapped read-only (datasets are copied out of it, so a list of
+    many GB is not read into memory twice)."""
+    with open(path, "rb") as f:
+        return mmap.mmap(f.fileno(), 0, access=mmap.ACCESS_READ)
+
+
 def read(path):
     """Every dataset of the file by its path ('/group/name'); strings come back
     as numpy bytes arrays (scalars as 0-d arrays)."""
-    with open(path, "rb") as f:
-        r = _Reader(f.read())
-    out = {}
-    _, hdr, btree, heap = r.entry(r.root_entry)
-    _read_group(r, hdr, btree, heap, "", out)
-    return out
+    mm = _mapped(path)
+    try:
+        r = _Reader(mm)
+        out = {}
+        _, hdr, btree, heap = r.entry(r.root_entry)
+        _read_group(r, hdr, btree, heap, "", out)
+        return out
+    finally:
+        mm.close()
 
 
 def _read_group(r, hdr, btree, heap, prefix, out, depth=0):
@@ -310,32 +324,56 @@ def _dataspace_msg(shape):
 
 
 class _Writer:
+    """Lays the file out in address order: metadata blocks are kept in memory,
+    dataset contents are written straight from their arrays at the end."""
+
     def __init__(self, mtime):
-        self.buf = bytearray(96)  # superblock and root entry, filled last
+        self.size = 0
+        self.blocks = {}  # address -> bytearray (metadata)
+        self.arrays = []  # (address, contiguous little-endian array)
         self.mtime = int(mtime) & 0xFFFFFFFF
+        self.alloc(96)    # superblock and root entry, filled last
 
     def alloc(self, n):
-        addr = len(self.buf)
-        self.buf += b"\0" * _pad8(n)
+        addr = self.size
+        self.size += _pad8(n)
+        self.blocks[addr] = bytearray(_pad8(n))
+        return addr
+
+    def alloc_array(self, arr):
+        addr = self.size
+        self.size += _pad8(arr.nbytes)
+        self.arrays.append((addr, arr))
         return addr
 
     def put(self, addr, data):
-        self.buf[addr:addr + len(data)] = data
+        blk = self.blocks[addr]
+        blk[:len(data)] = data
+
+    def flush(self, f):
+        for addr, blk in self.blocks.items():
+            f.seek(addr)
+            f.write(blk)
+        for addr, arr in self.arrays:
+            f.seek(addr)
+            arr.tofile(f)
+        f.truncate(self.size)
 
     def dataset(self, arr):
         arr = np.asarray(arr)
         if arr.dtype.kind in "iuf":
-            arr = arr.astype(arr.dtype.newbyteorder("<"))
-        raw = arr.tobytes()
+            arr = arr.astype(arr.dtype.newbyteorder("<"), copy=False)
+        if not arr.flags.c_contiguous:
+            arr = arr.copy(order="C")  # (np.ascontiguousarray would turn a scalar into a vector)
+        nbytes = arr.nbytes
         hdr = self.alloc(16 + DATASET_HEADER)
-        addr = self.alloc(len(raw)) if raw else UNDEF
-        if raw:
-            self.put(addr, raw)
+        addr = self.alloc_array(arr) if nbytes else UNDEF
+        raw_len = nbytes
         msgs = [
             _msg(0x01, 0, _dataspace_msg(arr.shape)),
             _msg(0x03, 1, _dtype_msg(arr.dtype)),
             _msg(0x05, 1, struct.pack("<BBBBI", 2, 2, 2, 1, 0)),
-            _msg(0x08, 1, struct.pack("<BBQQ", 3, 1, addr, len(raw))),
+            _msg(0x08, 1, struct.pack("<BBQQ", 3, 1, addr, raw_len)),
             _msg(0x12, 0, struct.pack("<B3xI", 1, self.mtime)),
         ]
         body = b"".join(msgs)
@@ -415,8 +453,8 @@ def write(path, datasets, groups=(), mtime=0):
     w = _Writer(mtime)
     hdr, btree, heap = w.group(_tree(conv, groups))
     sb = SIGNATURE + struct.pack("<8BHHI", 0, 0, 0, 0, 0, 8, 8, 0, LEAF_K, INTERNAL_K, 0)
-    sb += struct.pack("<4Q", 0, UNDEF, len(w.buf), UNDEF)
+    sb += struct.pack("<4Q", 0, UNDEF, w.size, UNDEF)
     sb += struct.pack("<QQI4xQQ", 0, hdr, 1, btree, heap)
     w.put(0, sb)
     with open(path, "wb") as f:
-        f.write(bytes(w.buf))
+        w.flush(f)

@@ -15,7 +15,10 @@ reduced to what the tests check:
   He2-aug-cc-pVDZ.fcidump here; int32 integer populations, scale factor 1);
 - restart_structure.json: the header-message signature (type, flags,
   version) of every object of a restart-version-2 FCIQMC file and of a
-  restart-version-3 file, which the writer's files are compared against.
+  restart-version-3 file, which the writer's files are compared against;
+- restart_continuation.json: HANDE's own continuation of the Hubbard restart
+  (the report table of the test's benchmark output), reblocked after a
+  10-report window with hande_gb300.analysis, with the run's parameters.
 The tests never need the reference tree."""
 
 from __future__ import annotations
@@ -30,6 +33,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from hande_gb300 import hdf5lite, restart  # noqa: E402
+from tests.golden.make_reference_runs import json_echo, report_table, summarise  # noqa: E402
 
 CASES = [
     # fixture, test directory, restart id, nbasis, nspaces, real factor of the calculation reading it
@@ -62,6 +66,20 @@ def main(ref_root: str):
         out[name] = {k: [list(m) for m in v] for k, v in hdf5lite.structure(os.path.join(suite, rel)).items()}
     with open(os.path.join(HERE, "restart_structure.json"), "w") as f:
         json.dump(out, f, indent=0, sort_keys=True)
+    import glob
+    d = os.path.join(suite, "fciqmc/np2/hubbard_k_2d_restart")
+    bench = glob.glob(os.path.join(d, "benchmark.out.*inp=hubbard.in"))[0]
+    text = open(bench).read()
+    q = json_echo(text)["qmc"]
+    table = report_table(text[text.index("-- End JSON block --"):])
+    cont = {"source": "test_suite/fciqmc/np2/hubbard_k_2d_restart/%s" % os.path.basename(bench),
+            "qmc": {k: q[k] for k in ("tau", "rng_seed", "ncycles", "nreport", "target_particles", "shift_damping")
+                    if k in q},
+            "first_iteration": int(table[0, 0]), "reports_in_output": int(table.shape[0] - 1),
+            "reference_stats": summarise(table[1:], 0.0)}
+    with open(os.path.join(HERE, "restart_continuation.json"), "w") as f:
+        json.dump(cont, f, indent=1)
+    print(cont)
 
 
 if __name__ == "__main__":

@@ -75,3 +75,8 @@ def test_fciqmc_driver_reads_and_writes_restarts(tmp_path):
     np.testing.assert_array_equal(back["states"], st)
     np.testing.assert_array_equal(back["pops"], po)
     res["engine"].close()
+
+
+def test_engine_continues_hande_restart_like_hande(tmp_path):
+    from tests.test_restart_hdf5 import continue_and_compare
+    continue_and_compare(engine, tmp_path, 1000)

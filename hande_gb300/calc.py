@@ -24,6 +24,7 @@ QMC_KEYS = {
     "target_population", "real_amplitudes", "spawn_cutoff", "excit_gen", "pattempt_single",
     "pattempt_double", "pattempt_parallel", "power_pitzer_min_weight", "initiator", "initiator_threshold",
     "shift_damping", "vary_shift_from", "initial_shift", "precision",
+    "shift_harmonic_forcing", "shift_harmonic_crit_damp", "shift_harmonic_forcing_two_stage",
 }
 FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file",
                "quadrature_initiator"}
@@ -87,6 +88,17 @@ def _opts(qmc: dict, fciqmc_opts: Optional[dict]):
     return fo
 
 
+def harmonic_forcing(qmc: dict) -> float:
+    """qs%shift_harmonic_forcing as init_qmc sets it (src/qmc.F90:193-208):
+    shift_damping^2 / 4 (critical damping) with shift_harmonic_crit_damp.
+    Otherwise it stays 0: init_qmc copies the input's shift_harmonic_forcing
+    only when the state's value is already non-zero, which it never is there,
+    so the option alone leaves the dynamics unchanged; the same here."""
+    if qmc.get("shift_harmonic_crit_damp", False):
+        return float(qmc.get("shift_damping", 0.05)) ** 2 / 4.0
+    return 0.0
+
+
 def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] = None, reference=None,
                         semi_stoch: Optional[dict] = None):
     fo = _opts(qmc, fciqmc_opts)
@@ -96,6 +108,7 @@ def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] =
         system, tau=qmc["tau"], ncycles=int(qmc["mc_cycles"]), seed=int(qmc.get("rng_seed", 7)),
         init_pop=float(qmc["init_pop"]), target_population=float(qmc.get("target_population", 1e300)),
         shift_damping=float(qmc.get("shift_damping", 0.05)), initial_shift=float(qmc.get("initial_shift", 0.0)),
+        shift_harmonic_forcing=harmonic_forcing(qmc),
         vary_shift_from=0.0 if vsf == "proje" else float(vsf), vary_shift_from_proje=(vsf == "proje"),
         real_amplitudes=bool(qmc.get("real_amplitudes", False)), spawn_cutoff=float(qmc.get("spawn_cutoff", 0.01)),
         excit_gen=qmc.get("excit_gen", "renorm"), pattempt_single=float(qmc.get("pattempt_single", -1.0)),
@@ -149,6 +162,13 @@ def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None
         restart_files.load_into(eng, read_paths)
     else:
         eng.initial_distribution()
+        if cfg.shift_harmonic_forcing != 0.0 and not qmc.get("shift_harmonic_forcing_two_stage", False):
+            # with harmonic forcing the shift varies from the start unless the
+            # forcing waits for the target population (src/qmc.F90:209-212)
+            st = eng.get_state()
+            for q in range(eng.R):
+                st.vary_shift[q] = 1
+            eng.set_state(st)
     stream = out if out is not None else sys_stdout()
     if verbose:
         stream.write(HEADER + "\n")

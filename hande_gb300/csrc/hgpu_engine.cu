@@ -1520,11 +1520,16 @@ int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
         out->D0_population[s] = (st.acc_d0[s] + st.acc_d0_c[s]) / (double)nc;
         ntot[s] = (double)st.abs_pop[s] / (double)h->hsys.real_factor;
     }
-    // update_shift (src/energy_evaluation.F90:659-711), shift_harmonic_forcing = 0
+    // update_shift (src/energy_evaluation.F90:659-711): the damping term, then the
+    // harmonic forcing toward target_particles
     for (int s = 0; s < R; s++)
-        if (h->vary_shift[s])
+        if (h->vary_shift[s]) {
             h->shift[s] = h->shift[s] - std::log(ntot[s] / h->nparticles_old[s]) * h->cfg.shift_damping /
                                             (1.0 * h->cfg.tau * (double)nc);
+            if (h->cfg.shift_harmonic_forcing != 0.0 && h->cfg.target_particles > 0.0)
+                h->shift[s] = h->shift[s] - std::log(ntot[s] / h->cfg.target_particles) *
+                                                h->cfg.shift_harmonic_forcing / (1.0 * h->cfg.tau * (double)nc);
+        }
     for (int s = 0; s < R; s++) h->nparticles_old[s] = ntot[s];
     bool all_vary_before = true, all_vary = true;
     for (int s = 0; s < R; s++) all_vary_before = all_vary_before && h->vary_shift[s];

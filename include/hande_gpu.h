@@ -171,6 +171,11 @@ typedef struct hgpu_config {
                                        (separate_annihilation = false: they join the spawned list
                                        as spawns from initiators, determ_proj_combined_annihil,
                                        src/semi_stoch.F90:897-975) */
+    double shift_harmonic_forcing;  /* qs%shift_harmonic_forcing, the restoring factor zeta of the
+                                       harmonic population control (update_shift,
+                                       src/energy_evaluation.F90:659-711): every shift update also
+                                       subtracts zeta ln(N_w / target_particles) / (tau A) when
+                                       target_particles > 0; 0 gives the original dynamics */
 } hgpu_config;
 
 /* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */

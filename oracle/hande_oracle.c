@@ -3059,7 +3059,8 @@ int oracle_run_cycles(oracle_ctx *c, int32_t ncycles) {
 }
 
 /* communicated_energy_estimators (src/energy_evaluation.F90:425-657) and
- * update_shift (:659-711), for one process and shift_harmonic_forcing = 0. */
+ * update_shift (:659-711), for one process: the damping term, then the
+ * harmonic forcing toward target_particles (when shift_harmonic_forcing != 0). */
 int oracle_end_report(oracle_ctx *c, hgpu_report *out) {
     int nc = c->rep_cycles > 0 ? c->rep_cycles : 1;
     memset(out, 0, sizeof(*out));
@@ -3079,6 +3080,9 @@ int oracle_end_report(oracle_ctx *c, hgpu_report *out) {
         if (c->vary_shift[s]) {
             c->shift[s] = c->shift[s] - log(ntot[s] / c->nparticles_old[s]) * c->cfg.shift_damping /
                                             (1.0 * c->cfg.tau * (double)nc);
+            if (c->cfg.shift_harmonic_forcing != 0.0 && c->cfg.target_particles > 0.0)
+                c->shift[s] = c->shift[s] - log(ntot[s] / c->cfg.target_particles) * c->cfg.shift_harmonic_forcing /
+                                                (1.0 * c->cfg.tau * (double)nc);
         }
     }
     for (int s = 0; s < c->R; s++) c->nparticles_old[s] = ntot[s];
@@ -3571,7 +3575,12 @@ int oracle_par_end_report(oracle_par *p, hgpu_report *out) {
         old[s] = c0->nparticles_old[s];
     }
     for (int s = 0; s < R; s++)
-        if (vary[s]) shift[s] = shift[s] - log(ntot[s] / old[s]) * c0->cfg.shift_damping / (1.0 * c0->cfg.tau * (double)nc);
+        if (vary[s]) {
+            shift[s] = shift[s] - log(ntot[s] / old[s]) * c0->cfg.shift_damping / (1.0 * c0->cfg.tau * (double)nc);
+            if (c0->cfg.shift_harmonic_forcing != 0.0 && c0->cfg.target_particles > 0.0)
+                shift[s] = shift[s] - log(ntot[s] / c0->cfg.target_particles) * c0->cfg.shift_harmonic_forcing /
+                                          (1.0 * c0->cfg.tau * (double)nc);
+        }
     for (int s = 0; s < R; s++) {
         if (!vary[s] && ntot[s] > c0->cfg.target_particles) {
             vary[s] = 1;

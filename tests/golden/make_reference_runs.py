@@ -44,7 +44,8 @@ CASES = [
 
 QMC_KEYS = ["tau", "rng_seed", "D0_population", "ncycles", "nreport", "target_particles", "initial_shift",
             "shift_damping", "initiator_approx", "initiator_pop", "excit_gen", "real_amplitudes",
-            "vary_shift_from", "vary_shift_from_proje", "spawn_cutoff"]
+            "vary_shift_from", "vary_shift_from_proje", "spawn_cutoff", "shift_harmonic_forcing",
+            "shift_harmonic_forcing_two_stage"]
 
 
 def json_echo(text: str) -> dict:

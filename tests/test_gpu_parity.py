@@ -134,6 +134,9 @@ def test_annihilate_empty_and_no_spawns():
 RUNS = [
     ("hub_k_4x4", dict(tau=0.005, init_pop=10, target_population=1000, excit_gen="renorm"), 6),
     ("hub_k_4x4", dict(tau=0.005, init_pop=10, target_population=1000, excit_gen="no_renorm"), 5),
+    # harmonic population control (critical damping: zeta = shift_damping^2 / 4)
+    ("hub_k_4x4", dict(tau=0.005, init_pop=10, target_population=60, shift_damping=0.04,
+                       shift_harmonic_forcing=0.0004), 8),
     ("hub_k_3x3_ms1", dict(tau=0.02, init_pop=100, target_population=500, initiator=True), 8),
     ("h2o_sto2g", dict(tau=0.01, init_pop=100, target_population=200, real_amplitudes=True, initial_shift=3.0), 10),
     ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,

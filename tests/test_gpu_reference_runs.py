@@ -44,7 +44,7 @@ def build_config(case, s, nreport=None):
         quadrature_initiator=case["quadrature_initiator"],
         nspaces=2 if (case["replica_tricks"] or case["density_matrices"]) else 1,
         density_matrices=case["density_matrices"], reference=[d - 1 for d in case["reference_det"]],
-        state_size=ncap, spawned_state_size=ncap)
+        shift_harmonic_forcing=q.get("shift_harmonic_forcing", 0.0), state_size=ncap, spawned_state_size=ncap)
 
 
 def window(shift, initial_shift):
@@ -59,6 +59,13 @@ def run_and_compare(case, make_engine, nreport=None):
     cfg = build_config(case, s)
     e = make_engine(s, cfg)
     e.initial_distribution()
+    q = case["qmc"]
+    if q.get("shift_harmonic_forcing", 0.0) and not q.get("shift_harmonic_forcing_two_stage", False):
+        # harmonic forcing from the first report (src/qmc.F90:209-212)
+        st = e.get_state() if hasattr(e, "get_state") else e.state()
+        for k in range(e.R):
+            st.vary_shift[k] = 1
+        e.set_state(st)
     shift, num, d0 = [], [], []
     for _ in range(nreport or case["qmc"]["nreport"]):
         r = e.run_report()
@@ -88,3 +95,71 @@ def run_and_compare(case, make_engine, nreport=None):
 def test_engine_matches_reference_run(name):
     from hande_gb300.engine import Engine
     run_and_compare(BY_NAME[name], Engine)
+
+
+def exact_energy(s, cfg):
+    """Lowest eigenvalue, relative to the reference's diagonal element, of the
+    Hamiltonian over every determinant with the system's alpha and beta
+    electron counts (the oracle's matrix elements; a few thousand
+    determinants)."""
+    import itertools
+    import scipy.sparse as sparse
+    import scipy.sparse.linalg as sla
+    from oracle.pyoracle import Oracle
+    o = Oracle(s, cfg)
+    norb = s.nbasis // 2
+    words = []
+    for a in itertools.combinations(range(norb), s.nalpha):
+        for b in itertools.combinations(range(norb), s.nbeta):
+            words.append(int(s.encode([2 * i for i in a] + [2 * i + 1 for i in b])[0]))
+    as_det = lambda x: np.array([x], dtype=np.uint64).astype(np.int64)
+    e0 = o.sc0(as_det(int(cfg.ref_det[0])))
+    rows, cols, vals = [], [], []
+    for i, fi in enumerate(words):
+        for j in range(i, len(words)):
+            if bin(fi ^ words[j]).count("1") > 4:
+                continue
+            v = o.sc0(as_det(fi)) - e0 if i == j else o.hmatel(as_det(fi), as_det(words[j]))
+            if v != 0.0:
+                rows += [i, j] if i != j else [i]
+                cols += [j, i] if i != j else [i]
+                vals += [v, v] if i != j else [v]
+    o.close()
+    h = sparse.csr_matrix((vals, (rows, cols)), shape=(len(words), len(words)))
+    return float(sla.eigsh(h, k=1, which="SA")[0][0])
+
+
+@pytest.mark.gpu
+def test_harmonic_population_control_n2():
+    """HANDE's N2 STO-3G test with critically damped harmonic population control
+    switched on at the target (test_suite/fciqmc/np4/N2-RHF-STO-3G-harmonic_pop_control_two_stage:
+    tau 0.001, 10 cycles a report, seed 21, 100 initial walkers, target 2e4,
+    shift_damping 0.04, shift_harmonic_crit_damp, shift_harmonic_forcing_two_stage).
+    HANDE's own run reaches its target at report 2657 of 2800, too late for its
+    statistics (133 reports, no reblocking plateau; its E_proj lies 4 standard
+    errors from the exact energy), so the run here is compared with the exact
+    energy of the 3136-determinant space: 4000 reports, E_proj within 3
+    standard errors, and the population held at the target."""
+    from hande_gb300.engine import Engine
+    s = systems.read_in(os.path.join(GOLDEN, "N2-RHF-STO-3G.fcidump"))
+    cfg = make_config(s, tau=0.001, ncycles=10, seed=21, init_pop=100, target_population=2e4, shift_damping=0.04,
+                      shift_harmonic_forcing=0.04 ** 2 / 4, state_size=200000, spawned_state_size=200000)
+    e_exact = exact_energy(s, cfg)
+    e = Engine(s, cfg)
+    e.initial_distribution()
+    shift, num, d0, nw = [], [], [], []
+    for _ in range(4000):
+        r = e.run_report()
+        assert r.error_flags == 0
+        shift.append(r.shift[0])
+        num.append(r.proj_energy[0])
+        d0.append(r.D0_population[0])
+        nw.append(r.nparticles[0])
+    e.close()
+    k0 = window(shift, 0.0)
+    assert len(shift) - k0 >= 500, "the target population was reached too late"
+    E, Eerr, _ = analysis.projected_energy(num[k0:], d0[k0:])
+    msg = "E_proj %.6f(%.6f) vs exact %.6f" % (E, Eerr, e_exact)
+    print(msg)
+    assert abs(E - e_exact) < 3.0 * Eerr, msg
+    assert abs(np.mean(nw[k0:]) - 2e4) < 0.1 * 2e4, np.mean(nw[k0:])

@@ -45,6 +45,7 @@ module hande_gpu_m
         integer(c_int64_t) :: semi_stoch_start_iter, semi_stoch_shift_iter
         integer(c_int32_t) :: semi_stoch_ci_level, semi_stoch_combined
         real(c_double) :: shift_harmonic_forcing
+        integer(c_int32_t) :: target_reference, reserved0
     end type hgpu_config
 
     type, bind(c) :: hgpu_report

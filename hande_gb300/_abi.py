@@ -71,7 +71,7 @@ class HgpuConfig(C.Structure):
         ("semi_stoch_space", C.c_int32), ("semi_stoch_size", C.c_int32),
         ("semi_stoch_start_iter", C.c_int64), ("semi_stoch_shift_iter", C.c_int64),
         ("semi_stoch_ci_level", C.c_int32), ("semi_stoch_combined", C.c_int32),
-        ("shift_harmonic_forcing", C.c_double),
+        ("shift_harmonic_forcing", C.c_double), ("target_reference", C.c_int32), ("reserved0", C.c_int32),
     ]
 
 
@@ -190,6 +190,7 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
                 semi_stoch_space: int = 0,
                 semi_stoch_size: int = 0, semi_stoch_start_iter: int = 1, semi_stoch_shift_iter: int = -1,
                 semi_stoch_ci_level: int = 0, semi_stoch_combined: int = 0, shift_harmonic_forcing: float = 0.0,
+                target_reference: bool = False,
                 precision: int = PREC_FP64, state_size: int = 100000,
                 spawned_state_size: int = 100000, reference=None) -> HgpuConfig:
     """Configuration with HANDE's qmc{} key names (src/lua_hande_calc.f90:1318-1331)."""
@@ -214,6 +215,7 @@ def make_config(s: System, tau: float, *, ncycles: int = 10, seed: int = 7, init
     cfg.semi_stoch_ci_level = int(semi_stoch_ci_level)
     cfg.semi_stoch_combined = int(semi_stoch_combined)
     cfg.shift_harmonic_forcing = float(shift_harmonic_forcing)
+    cfg.target_reference = int(bool(target_reference))
     cfg.D0_population = init_pop
     cfg.vary_shift_from_proje = int(bool(vary_shift_from_proje))
     cfg.excit_gen = EXCIT_GEN[excit_gen] if isinstance(excit_gen, str) else int(excit_gen)

@@ -25,6 +25,7 @@ QMC_KEYS = {
     "pattempt_double", "pattempt_parallel", "power_pitzer_min_weight", "initiator", "initiator_threshold",
     "shift_damping", "vary_shift_from", "initial_shift", "precision",
     "shift_harmonic_forcing", "shift_harmonic_crit_damp", "shift_harmonic_forcing_two_stage",
+    "reference_target",
 }
 FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file",
                "quadrature_initiator"}
@@ -102,11 +103,16 @@ def harmonic_forcing(qmc: dict) -> float:
 def config_from_options(system: System, qmc: dict, fciqmc_opts: Optional[dict] = None, reference=None,
                         semi_stoch: Optional[dict] = None):
     fo = _opts(qmc, fciqmc_opts)
+    # reference_target: the target is the reference population (src/lua_hande_calc.f90:1412-1417)
+    if "reference_target" in qmc and "target_population" in qmc:
+        raise ValueError("Cannot provide both target_population and reference_target")
+    target = float(qmc["reference_target"]) if "reference_target" in qmc else \
+        float(qmc.get("target_population", 1e300))
     vsf = qmc.get("vary_shift_from", 0.0)
     prec = qmc.get("precision", "fp64")
     return make_config(
         system, tau=qmc["tau"], ncycles=int(qmc["mc_cycles"]), seed=int(qmc.get("rng_seed", 7)),
-        init_pop=float(qmc["init_pop"]), target_population=float(qmc.get("target_population", 1e300)),
+        init_pop=float(qmc["init_pop"]), target_population=target, target_reference="reference_target" in qmc,
         shift_damping=float(qmc.get("shift_damping", 0.05)), initial_shift=float(qmc.get("initial_shift", 0.0)),
         shift_harmonic_forcing=harmonic_forcing(qmc),
         vary_shift_from=0.0 if vsf == "proje" else float(vsf), vary_shift_from_proje=(vsf == "proje"),

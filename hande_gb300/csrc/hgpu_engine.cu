@@ -1534,7 +1534,8 @@ int32_t hgpu_end_report(hgpu_handle *h, hgpu_report *out) {
     bool all_vary_before = true, all_vary = true;
     for (int s = 0; s < R; s++) all_vary_before = all_vary_before && h->vary_shift[s];
     for (int s = 0; s < R; s++) {
-        if (!h->vary_shift[s] && ntot[s] > h->cfg.target_particles) {
+        const double above = h->cfg.target_reference ? out->D0_population[s] : ntot[s];
+        if (!h->vary_shift[s] && above > h->cfg.target_particles) {
             h->vary_shift[s] = 1;
             h->shift[s] = h->cfg.vary_shift_from_proje ? out->proj_energy[s] / out->D0_population[s]
                                                        : h->cfg.vary_shift_from;

@@ -176,6 +176,12 @@ typedef struct hgpu_config {
                                        src/energy_evaluation.F90:659-711): every shift update also
                                        subtracts zeta ln(N_w / target_particles) / (tau A) when
                                        target_particles > 0; 0 gives the original dynamics */
+    int32_t target_reference;       /* qmc_in%target_reference (the reference_target option): a
+                                       shift starts to vary when its space's reference population
+                                       N_0, not its total population, exceeds target_particles
+                                       (communicated_energy_estimators,
+                                       src/energy_evaluation.F90:638-650) */
+    int32_t reserved0;
 } hgpu_config;
 
 /* One report line: the columns of write_qmc_report (src/qmc_io.f90:23-136). */

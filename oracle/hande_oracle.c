@@ -3089,7 +3089,8 @@ int oracle_end_report(oracle_ctx *c, hgpu_report *out) {
     int all_vary_before = 1, all_vary = 1;
     for (int s = 0; s < c->R; s++) all_vary_before = all_vary_before && c->vary_shift[s];
     for (int s = 0; s < c->R; s++) {
-        if (!c->vary_shift[s] && ntot[s] > c->cfg.target_particles) {
+        const double above = c->cfg.target_reference ? out->D0_population[s] : ntot[s];
+        if (!c->vary_shift[s] && above > c->cfg.target_particles) {
             c->vary_shift[s] = 1;
             if (c->cfg.vary_shift_from_proje) c->shift[s] = out->proj_energy[s] / out->D0_population[s];
             else c->shift[s] = c->cfg.vary_shift_from;
@@ -3582,7 +3583,8 @@ int oracle_par_end_report(oracle_par *p, hgpu_report *out) {
                                           (1.0 * c0->cfg.tau * (double)nc);
         }
     for (int s = 0; s < R; s++) {
-        if (!vary[s] && ntot[s] > c0->cfg.target_particles) {
+        const double above = c0->cfg.target_reference ? out->D0_population[s] : ntot[s];
+        if (!vary[s] && above > c0->cfg.target_particles) {
             vary[s] = 1;
             shift[s] = c0->cfg.vary_shift_from_proje ? out->proj_energy[s] / out->D0_population[s]
                                                      : c0->cfg.vary_shift_from;

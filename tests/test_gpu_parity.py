@@ -137,6 +137,8 @@ RUNS = [
     # harmonic population control (critical damping: zeta = shift_damping^2 / 4)
     ("hub_k_4x4", dict(tau=0.005, init_pop=10, target_population=60, shift_damping=0.04,
                        shift_harmonic_forcing=0.0004), 8),
+    # the shift starts to vary on the reference population (reference_target)
+    ("hub_k_4x4", dict(tau=0.005, init_pop=10, target_population=11, target_reference=True), 6),
     ("hub_k_3x3_ms1", dict(tau=0.02, init_pop=100, target_population=500, initiator=True), 8),
     ("h2o_sto2g", dict(tau=0.01, init_pop=100, target_population=200, real_amplitudes=True, initial_shift=3.0), 10),
     ("mol26", dict(tau=1e-4, init_pop=2000, target_population=20000, real_amplitudes=True,

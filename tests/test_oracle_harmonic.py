@@ -63,3 +63,30 @@ def test_forcing_options():
     s = systems.hubbard_k([[4, 0], [0, 4]], 10, U=4.0)
     cfg = calc.config_from_options(s, dict(q, shift_harmonic_crit_damp=True, shift_harmonic_forcing_two_stage=True))
     assert cfg.shift_harmonic_forcing == 0.04 ** 2 / 4
+
+
+def test_reference_target_switches_on_the_reference_population():
+    """reference_target (src/energy_evaluation.F90:638-650): the shift starts to
+    vary at the first report whose averaged reference population exceeds the
+    target, whatever the total population."""
+    s = _hubbard()
+    q = dict(tau=0.01, init_pop=1000, mc_cycles=10, nreports=1, reference_target=900.0)
+    cfg = calc.config_from_options(s, q)
+    assert cfg.target_reference == 1 and cfg.target_particles == 900.0
+    o = Oracle(s, cfg)
+    o.initial_distribution()
+    switched = None
+    for k in range(200):
+        r = o.run_report()
+        if r.vary_shift[0]:
+            switched = (k, r)
+            break
+        assert r.D0_population[0] <= 900.0
+    assert switched is not None
+    k, r = switched
+    assert r.D0_population[0] > 900.0
+    assert r.nparticles[0] > 900.0  # the total population passed the target well before
+    o.close()
+    import pytest
+    with pytest.raises(ValueError):
+        calc.config_from_options(s, dict(q, target_population=5.0))

@@ -25,7 +25,7 @@ QMC_KEYS = {
     "pattempt_double", "pattempt_parallel", "power_pitzer_min_weight", "initiator", "initiator_threshold",
     "shift_damping", "vary_shift_from", "initial_shift", "precision",
     "shift_harmonic_forcing", "shift_harmonic_crit_damp", "shift_harmonic_forcing_two_stage",
-    "reference_target",
+    "reference_target", "vary_shift",
 }
 FCIQMC_KEYS = {"replica_tricks", "density_matrices", "density_matrix_report", "density_matrix_file",
                "quadrature_initiator"}
@@ -175,6 +175,15 @@ def fciqmc(sys: System, qmc: dict, fciqmc: Optional[dict] = None, reference=None
             for q in range(eng.R):
                 st.vary_shift[q] = 1
             eng.set_state(st)
+    if "vary_shift" in qmc:
+        # the input's vary_shift overrides everything else, a restart included; a
+        # shift that does not vary starts from initial_shift (src/qmc.F90:881-893)
+        st = eng.get_state()
+        for q in range(eng.R):
+            st.vary_shift[q] = int(bool(qmc["vary_shift"]))
+            if not qmc["vary_shift"]:
+                st.shift[q] = float(qmc.get("initial_shift", 0.0))
+        eng.set_state(st)
     stream = out if out is not None else sys_stdout()
     if verbose:
         stream.write(HEADER + "\n")

@@ -261,3 +261,31 @@ def continue_and_compare(make_calc, tmp_path, nreports):
 
 def test_oracle_continues_hande_restart_like_hande(tmp_path):
     continue_and_compare(lambda s, cfg: Oracle(s, cfg), tmp_path, 400)
+
+
+def test_driver_vary_shift_option_overrides_restart(tmp_path, monkeypatch):
+    """qmc.vary_shift (init_estimators, src/qmc.F90:881-893) overrides the
+    restart's vary shift, and a shift that does not vary restarts from
+    initial_shift; the fciqmc driver's host logic, run with the oracle in the
+    engine's place."""
+    from hande_gb300 import calc
+
+    class OracleEngine(Oracle):
+        def get_state(self):
+            return self.state()
+
+    monkeypatch.setattr(calc, "Engine", OracleEngine)
+    g = _golden("restart_hubbard_k_2d")
+    _write(str(tmp_path / "HANDE.RS.0.p0.H5"), g)
+    # a target the population never reaches: the switch at a report's end stays out of play
+    qmc = dict(tau=0.01, rng_seed=7, init_pop=10, mc_cycles=25, nreports=2, target_population=1e9,
+               state_size=40000, spawned_state_size=40000, initial_shift=-0.25)
+    res = calc.fciqmc(_hubbard(), dict(qmc, vary_shift=False), restart={"read": 0}, directory=str(tmp_path),
+                      verbose=False)
+    for rep in res["reports"]:
+        assert rep["vary_shift"] == [0] and rep["Shift"] == [-0.25]
+    res["engine"].close()
+    res = calc.fciqmc(_hubbard(), qmc, restart={"read": 0}, directory=str(tmp_path), verbose=False)
+    assert res["reports"][0]["vary_shift"] == [1]
+    assert res["reports"][0]["Shift"][0] != -0.25
+    res["engine"].close()
